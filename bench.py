@@ -1,0 +1,376 @@
+"""Benchmark: closest-hit Mrays/s on the BVH stress workload.
+
+Workload (one "step" = one closest-hit launch, 1 spp): a seeded icosphere
+subdivided to 1,310,720 triangles, displaced by 3-octave value noise,
+instanced 64 times with seeded rigid transforms inside a 100^3 cube; rays =
+1920x1080 jittered pinhole primaries + one cosine-weighted diffuse bounce per
+primary hit, cast together through the C ABI (``mrg_cast_closest``).  Inputs
+(rays 32 B + hits 16 B + meta hits 8 B per ray, ~230 MB) exceed the 129 MB L2,
+so no flush is needed between steps; each step restores the rays' tMax first.
+
+``value``: rays per step / device time per step (CUDA events on the launching
+stream, K timed steps after W warm-ups, max over ranks).  ``e2e``: the same
+metric through the host-buffer entry point ``mrg_cast_closest_host`` with
+pinned host buffers (H2D + cast + D2H + sync inside the timed region).
+``--impl reference``: the CPU restatement of MRay's host-backend LBVH cast
+(oracle/) on all host cores over a bounded sample of the same rays.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s closest-hit"
+UNIT = "Mrays/s"
+WIDTH, HEIGHT = 1920, 1080
+WORKLOAD = "bvh-stress: 1,310,720-tri displaced icosphere x 64 rigid instances, 1920x1080 primary + 1 diffuse bounce"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def make_workload(seed=0):
+    from mray_gb300 import scenes
+    pos, idx, m = scenes.bvh_stress_scene(seed=seed)
+    prim = scenes.primary_rays(WIDTH, HEIGHT, seed)
+    return pos, idx, m, prim
+
+
+def gpu_arm(args):
+    import torch
+    import torch.distributed as dist
+    from mray_gb300 import Accelerator, scenes
+    from mray_gb300 import build as B
+    B.build()
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+
+    pos, idx, m, prim = make_workload(seed=rank)
+    acc = Accelerator(local)
+    mesh = acc.upload_mesh(pos, idx, prim_key_base=0x10000000)
+    for i in range(m.shape[0]):
+        acc.add_instance(mesh, m[i], light_or_mat_key=i, trans_key=(1 << 24) | i, accel_key=(2 << 20) | i)
+    t0 = time.perf_counter()
+    acc.construct()
+    build_s = time.perf_counter() - t0
+    st = acc.stats()
+
+    # primary hits -> bounce rays (one diffuse bounce per primary hit)
+    pr = torch.from_numpy(prim).to(dev)
+    ph = torch.zeros((prim.shape[0], 4), dtype=torch.int32, device=dev)
+    pm = torch.zeros((prim.shape[0], 2), dtype=torch.float32, device=dev)
+    acc.cast_rays(pr, ph, pm, stream=stream)
+    acc.sync_status(stream)
+    prh = pr.cpu().numpy()
+    phh = ph.cpu().numpy().view(np.uint32)
+    hit = prh[:, 7] < 3e38
+    inst = np.where(hit, phh[:, 2] & 0xFFFFFF, 0xFFFFFFFF).astype(np.uint32)
+    primk = (phh[:, 0] - 0x10000000).astype(np.uint32)
+    bounce, _ = scenes.bounce_rays(prim, inst, primk, prh[:, 7], pos, idx, m, seed=rank + 1)
+    rays_np = np.vstack([prim, bounce]).astype(np.float32)
+    n = rays_np.shape[0]
+
+    pristine = torch.from_numpy(rays_np).to(dev)
+    rays = pristine.clone()
+    hits = torch.zeros((n, 4), dtype=torch.int32, device=dev)
+    meta = torch.zeros((n, 2), dtype=torch.float32, device=dev)
+
+    # traversal counts over the whole ray set (algorithmic bytes per ray)
+    counts = acc.traversal_counts(pristine, stream=stream)
+
+    def step():
+        rays.copy_(pristine)
+        acc.cast_rays(rays, hits, meta, stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    acc.sync_status(stream)
+
+    # kernel-only timing (events around the cast launch alone)
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        rays.copy_(pristine)
+        kev[k][0].record(stream)
+        acc.cast_rays(rays, hits, meta, stream=stream)
+        kev[k][1].record(stream)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    acc.sync_status(stream)
+    total_ms = e0.elapsed_time(e1)
+    kernel_ms = sum(a.elapsed_time(b) for a, b in kev) / args.steps
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = (n * ws) / (ms_per_step * 1e-3) / 1e6
+
+    # e2e: host buffers through mrg_cast_closest_host (pinned)
+    h_rays = torch.from_numpy(rays_np).pin_memory()
+    h_hits = torch.zeros((n, 4), dtype=torch.int32).pin_memory()
+    h_meta = torch.zeros((n, 2), dtype=torch.float32).pin_memory()
+    hr, hh, hm = h_rays.numpy(), h_hits.numpy().view(np.uint32), h_meta.numpy()
+    acc.cast_rays_host(hr, hh, hm)           # grow staging buffers (untimed)
+    e2e_times = []
+    for _ in range(max(3, min(args.steps, 10))):
+        hr[:] = rays_np
+        t0 = time.perf_counter()
+        acc.cast_rays_host(hr, hh, hm)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_times)
+    e2e_val = n / e2e_s / 1e6
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_val = n * ws / float(t.item()) / 1e6
+
+    # any-hit (shadow rays from the bounce origins to a point light)
+    shadow = torch.from_numpy(scenes.shadow_rays(bounce, (0.0, 80.0, -60.0))).to(dev)
+    vis = torch.zeros(((shadow.shape[0] + 31) // 32,), dtype=torch.int32, device=dev)
+    for _ in range(2):
+        acc.cast_visibility_rays(vis, shadow, stream=stream)
+    a0 = torch.cuda.Event(enable_timing=True)
+    a1 = torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    for _ in range(args.steps):
+        acc.cast_visibility_rays(vis, shadow, stream=stream)
+    a1.record(stream)
+    torch.cuda.synchronize(dev)
+    any_ms = a0.elapsed_time(a1) / args.steps
+    any_val = shadow.shape[0] / (any_ms * 1e-3) / 1e6
+
+    peak, peak_kind = load_peaks()
+    per_ray = (32 + 28 + 80.0 * counts["node_visits"] / counts["rays"] +
+               48.0 * counts["tri_tests"] / counts["rays"] + 64.0 * counts["instance_entries"] / counts["rays"])
+    achieved = per_ray * n / (kernel_ms * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traverse_closest_traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene and rays)",
+        "config": {"workload": WORKLOAD, "rays_per_step": n, "primary_rays": int(prim.shape[0]),
+                   "bounce_rays": int(bounce.shape[0]), "triangles_per_instance": int(idx.shape[0]),
+                   "instances": int(m.shape[0]), "l2": "inputs larger than L2 (~%d MB per step)" % (n * 56 // 2**20),
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "e2e": {"value": round(e2e_val, 2), "unit": UNIT, "h2d_bytes_per_step": n * 56,
+                "d2h_bytes_per_step": n * 56},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 3), "traffic": traffic,
+                     "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured" else "fallback",
+                     "kernel": "k_trace<closest>", "kernel_ms": round(kernel_ms, 4),
+                     "algorithmic_bytes_per_ray": round(per_ray, 1),
+                     "node_visits_per_ray": round(counts["node_visits"] / counts["rays"], 2),
+                     "tri_tests_per_ray": round(counts["tri_tests"] / counts["rays"], 2)},
+        "clocks": clocks,
+        "extra": {"anyhit_mrays_s": round(any_val, 1), "shadow_rays": int(shadow.shape[0]),
+                  "build_ms": round(st["buildMs"], 1), "build_wall_s": round(build_s, 3),
+                  "bvh_device_mb": round(st["deviceBytes"] / 2**20, 1),
+                  "blas_nodes": st["blasNodes"]},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(pos, idx, m, rays_np, budget_s=args.cpu_seconds)
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def oracle_scene(pos, idx, m):
+    import oracle
+    S = oracle.Scene()
+    mid = S.add_mesh(pos, idx, prim_key_base=0x10000000)
+    for i in range(m.shape[0]):
+        S.add_instance(mid, m[i], lm_key=i, trans_key=(1 << 24) | i, accel_key=(2 << 20) | i)
+    S.build()
+    return S
+
+
+def sample_rays(rays, k):
+    stride = max(1, rays.shape[0] // k)
+    return np.ascontiguousarray(rays[::stride][:k])
+
+
+def cpu_baseline(pos, idx, m, rays_np, budget_s=15.0):
+    """The oracle (C restatement of MRay's host-backend LBVH cast) on every
+    host core over a stride sample of the same ray set."""
+    import oracle
+    S = oracle_scene(pos, idx, m)
+    threads = oracle.default_threads()
+    k = 65536
+    s = sample_rays(rays_np, k)
+    t0 = time.perf_counter()
+    S.cast_closest(s, threads=threads)
+    dt = time.perf_counter() - t0
+    rate = s.shape[0] / dt
+    # grow the sample to roughly the time budget
+    k2 = int(min(rays_np.shape[0], max(k, rate * budget_s)))
+    s2 = sample_rays(rays_np, k2)
+    t0 = time.perf_counter()
+    S.cast_closest(s2, threads=threads)
+    dt2 = time.perf_counter() - t0
+    return {"value": round(s2.shape[0] / dt2 / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of %d rays (stride sample of primary+bounce set), %.1f s" % (s2.shape[0], rays_np.shape[0], dt2)}
+
+
+def reference_arm(args):
+    """CPU restatement of MRay's host-backend cast (no reference CUDA path runs
+    here: the reference's GPU backend needs OptiX or its own CUDA build)."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from mray_gb300 import build as B
+    from mray_gb300 import scenes
+    import oracle
+    B.build_scenes()
+    pos, idx, m, prim = make_workload()
+    S = oracle_scene(pos, idx, m)
+    threads = oracle.default_threads()
+    # same primary+bounce mix as the GPU arm: sample primaries, bounce from their hits
+    ps = sample_rays(prim, 32768)
+    r, h, _, inst = S.cast_closest(ps, threads=threads)
+    bounce, _ = scenes.bounce_rays(ps, inst, (h[:, 0] - 0x10000000).astype(np.uint32), r[:, 7], pos, idx, m, seed=1)
+    sample = np.vstack([ps, bounce]).astype(np.float32)
+    for _ in range(args.warmup):
+        S.cast_closest(sample[:4096], threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        S.cast_closest(sample, threads=threads)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = sample.shape[0] * args.steps / tot / 1e6
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(tot / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and rays)",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "rays_per_step": int(sample.shape[0]),
+                   "sample": "32768 stride-sampled primaries + their diffuse bounces",
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d rays per step" % sample.shape[0]},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,174 @@
+/*
+ * mray_gb300.h -- C ABI of the GB300-native MRay ray-tracing hot path.
+ *
+ * The library (mray_gb300/libmray_gb300.so) replaces the CUDA backend's
+ * accelerator slot of MRay's TracerDLL: a GPU-built wide BVH (8-wide,
+ * quantised child boxes) traversed in software by hand-written sm_103a
+ * kernels.  Every entry point below names the reference interface it stands
+ * in for (paths relative to the MRay source tree).
+ *
+ * Conventions
+ *  - Plain C types only; no exceptions cross this boundary.  Every call
+ *    returns an mrg_status; mrg_last_error() gives a message for the calling
+ *    thread's last failure.
+ *  - "d_" pointers are caller-owned DEVICE buffers; "h_" pointers are host
+ *    buffers.  Outputs are written in place at the ray's index, like MRay's
+ *    Span-based interfaces (Source/Tracer/AcceleratorC.h:375-430).
+ *  - stream is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *    Calls are stream-ordered; the cast calls do not synchronise.
+ *  - One context per thread at a time (MRay drives TracerI from a single
+ *    tracer thread, Source/MRay/TracerThread.cpp:498).
+ */
+#ifndef MRAY_GB300_H
+#define MRAY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mrg_status
+{
+    MRG_OK                  = 0,
+    MRG_ERR_INVALID_ARG     = 1,   /* null pointer, bad id, size out of range */
+    MRG_ERR_CUDA            = 2,   /* a CUDA runtime call failed */
+    MRG_ERR_OUT_OF_MEMORY   = 3,
+    MRG_ERR_NOT_BUILT       = 4,   /* cast before mrg_build / after a scene change */
+    MRG_ERR_LIMIT           = 5,   /* a documented capacity was exceeded */
+    MRG_ERR_TRAVERSAL       = 6    /* a kernel reported a stack overflow / step cap */
+} mrg_status;
+
+/* RayGMem (Source/Tracer/TracerTypes.h:276-283): 32 bytes, 32-byte aligned. */
+typedef struct mrg_ray
+{
+    float pos[3];
+    float tMin;
+    float dir[3];
+    float tMax;
+} mrg_ray;
+
+/* HitKeyPack (Source/Tracer/TracerTypes.h:199-205): 16 bytes.  Key encodings
+ * follow Source/Tracer/TracerTypes.h:165-178: PrimitiveKey 4|28,
+ * LightOrMatKey 1|10|21, TransformKey 8|24, AcceleratorKey 12|20 (batch|id). */
+typedef struct mrg_hit_keys
+{
+    uint32_t primKey;
+    uint32_t lightOrMatKey;
+    uint32_t transKey;
+    uint32_t accelKey;
+} mrg_hit_keys;
+
+/* MetaHit of a triangle hit (PrimitiveDefaultTriangle.h:32): the first two
+ * barycentrics in MRay's order (w, u) with w = 1 - u - v. */
+typedef struct mrg_meta_hit
+{
+    float bary[2];
+} mrg_meta_hit;
+
+typedef struct mrg_params
+{
+    int      device;           /* CUDA device ordinal */
+    uint32_t reserved[7];
+} mrg_params;
+
+typedef struct mrg_accel_stats
+{
+    uint64_t blasNodes;        /* 8-wide nodes over all BLASes */
+    uint64_t blasTriangles;    /* triangle records */
+    uint64_t tlasNodes;
+    uint64_t instances;
+    uint64_t deviceBytes;      /* accelerator bytes resident on the device */
+    double   buildMs;          /* last mrg_build wall time */
+} mrg_accel_stats;
+
+typedef struct mrg_ctx mrg_ctx;
+
+/* Instance flags. */
+#define MRG_INSTANCE_CULL_BACKFACE 0x1u   /* cullFaceFlags, default on (SceneLoaderMRay/JsonNode.hpp:31-32) */
+/* MRay's Matrix3x4::Inverse stores +s1 for the [1][2] element whose cofactor
+ * is -s1 (Source/Core/Matrix.hpp:888), so its world->local transform is wrong
+ * for rotations with m0*m6 != m2*m4.  By default the inverse reproduces that
+ * arithmetic bit for bit (parity with MRay); this flag negates the element. */
+#define MRG_INSTANCE_CORRECTED_INVERSE 0x2u
+
+/* Context.  Replaces ConstructTracer / DestroyTracer for the accelerator
+ * slot (Source/TracerDLL/EntryPoint.h:12-18, Source/TracerDLL/EntryPoint.cpp:4-13)
+ * and the BaseAcceleratorLBVH constructor (Source/Tracer/AcceleratorLBVH.h:236-330). */
+mrg_status mrg_create(const mrg_params* params, mrg_ctx** out_ctx);
+mrg_status mrg_destroy(mrg_ctx* ctx);
+const char* mrg_last_error(void);
+const char* mrg_status_string(mrg_status s);
+
+/* Upload an indexed triangle mesh (host pointers, copied).  Replaces
+ * PrimGroupTriangle attribute pushes (TracerI::PushPrimAttribute,
+ * Source/Core/TracerI.h:209-219; TriangleData, PrimitiveDefaultTriangle.h:22-30).
+ * Primitive keys of the mesh are prim_key_base + local triangle index. */
+mrg_status mrg_upload_mesh(mrg_ctx* ctx, const float* h_pos, uint32_t vertex_count,
+                           const uint32_t* h_idx, uint32_t triangle_count,
+                           uint32_t prim_key_base, uint32_t* out_mesh_id);
+
+/* Add an instance of a mesh with a row-major 3x4 local-to-world transform.
+ * Replaces CreateSurface + TransformGroupSingle pushes (TracerI.h:270-281;
+ * Source/Tracer/TransformsDefault.h:13-17).  The inverse is computed here
+ * with MRay's Matrix3x4::Inverse arithmetic (Source/Core/Matrix.hpp:855-904);
+ * see MRG_INSTANCE_CORRECTED_INVERSE. */
+mrg_status mrg_add_instance(mrg_ctx* ctx, uint32_t mesh_id, const float m3x4[12],
+                            uint32_t flags, uint32_t light_or_mat_key,
+                            uint32_t trans_key, uint32_t accel_key,
+                            uint32_t* out_instance_id);
+
+/* Build every BLAS and the TLAS on the GPU.  Replaces
+ * BaseAccelerator::Construct (Source/Tracer/AcceleratorCommon.cu:709-805)
+ * + AllocateForTraversal (Source/Tracer/AcceleratorLBVH.cu:742-758).
+ * Synchronous. */
+mrg_status mrg_build(mrg_ctx* ctx);
+
+/* Closest hit.  Replaces BaseAcceleratorI::CastRays
+ * (Source/Tracer/AcceleratorC.h:391-398; Source/Tracer/AcceleratorLBVH.cu:760-896).
+ * For i in [0, n): r = d_ray_idx ? d_ray_idx[i] : i.  On a hit in
+ * [tMin, tMax): d_hits[r], d_meta[r] and d_rays[r].tMax are written; misses
+ * leave all three untouched.  d_rays must be 32-byte aligned. */
+mrg_status mrg_cast_closest(mrg_ctx* ctx, mrg_ray* d_rays, const uint32_t* d_ray_idx,
+                            uint32_t n, mrg_hit_keys* d_hits, mrg_meta_hit* d_meta,
+                            void* stream);
+
+/* Any hit (occlusion).  Replaces BaseAcceleratorI::CastVisibilityRays
+ * (Source/Tracer/AcceleratorC.h:400-405; Source/Tracer/AcceleratorLBVH.cu:898-1035).
+ * Bit r of d_visible_bits is set for every listed ray, then cleared if any
+ * hit lies in [tMin, tMax). */
+mrg_status mrg_cast_visibility(mrg_ctx* ctx, uint32_t* d_visible_bits,
+                               const mrg_ray* d_rays, const uint32_t* d_ray_idx,
+                               uint32_t n, void* stream);
+
+/* Closest hit on HOST buffers: copies h_rays to the device, casts, copies the
+ * hits, meta hits and updated rays back, and synchronises.  The staging
+ * buffers are owned by the context and grow to the largest n seen. */
+mrg_status mrg_cast_closest_host(mrg_ctx* ctx, mrg_ray* h_rays, uint32_t n,
+                                 mrg_hit_keys* h_hits, mrg_meta_hit* h_meta);
+
+/* World-space AABB of the scene (BaseAcceleratorI::SceneAABB,
+ * Source/Tracer/AcceleratorC.h:416): min xyz, max xyz. */
+mrg_status mrg_scene_aabb(mrg_ctx* ctx, float out_minmax[6]);
+
+mrg_status mrg_get_stats(mrg_ctx* ctx, mrg_accel_stats* out);
+
+/* Synchronises `stream` and reports (then clears) a traversal error recorded
+ * by any cast since the last check: MRG_ERR_TRAVERSAL if a ray overflowed the
+ * traversal stack or hit the step cap.  MRay's kernels trap instead
+ * (HybridTerminateOrTrap, Source/Core/Definitions.h); here the kernel records
+ * the fault, abandons the ray and returns, so the context stays usable. */
+mrg_status mrg_sync_status(mrg_ctx* ctx, void* stream);
+
+/* Traversal statistics for the algorithmic-byte count: casts the rays with
+ * counters on and returns [0] rays, [1] wide-node visits, [2] triangle tests,
+ * [3] instance entries.  Rays are not modified. */
+mrg_status mrg_cast_closest_stats(mrg_ctx* ctx, const mrg_ray* d_rays, uint32_t n,
+                                  uint64_t out_counts[4], void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MRAY_GB300_H */

@@ -1,0 +1,475 @@
+// api.cpp -- the C ABI (include/mray_gb300.h): context, scene upload, build,
+// casts.  Host C++ over the CUDA runtime; no exceptions cross the boundary.
+#include "mray_gb300.h"
+#include "mrg_build.h"
+#include "host_math.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace mrg {
+
+// Device-side record layouts, mirrored on the host for uploads.
+struct HostInstRecord
+{
+    float    inv[12];
+    uint32_t keys[4];
+};
+static_assert(sizeof(HostInstRecord) == 64, "instance record is 64 bytes");
+constexpr size_t kWideNodeBytes = 80;
+constexpr size_t kTriRecordBytes = 48;
+
+} // namespace mrg
+
+struct mrg_ctx
+{
+    int device = 0;
+    int smCount = 0;
+    cudaStream_t buildStream = nullptr;
+
+    struct Mesh
+    {
+        std::vector<float>    pos;
+        std::vector<uint32_t> idx;
+        uint32_t              primKeyBase = 0;
+        float                 box[6] = { 0, 0, 0, 0, 0, 0 };
+        uint32_t              rootNode = 0;
+    };
+    struct Inst
+    {
+        uint32_t mesh = 0;
+        float    m[12];
+        float    inv[12];
+        uint32_t flags = 0, lm = 0, trans = 0, accel = 0;
+    };
+    std::vector<Mesh> meshes;
+    std::vector<Inst> insts;
+    bool built = false;
+
+    // accelerator (device)
+    void*     dNodes = nullptr;
+    void*     dTris = nullptr;
+    void*     dInsts = nullptr;
+    uint32_t* dTlasLeaf = nullptr;
+    uint64_t  blasNodes = 0, blasTris = 0, tlasNodes = 0;
+    mrg::TraceScene scene;
+    float     sceneBox[6] = { 0, 0, 0, 0, 0, 0 };
+    double    buildMs = 0.0;
+
+    // scratch: [0] work counter, [1] error flag; stats in a separate block
+    uint32_t*           dScratch = nullptr;
+    unsigned long long* dStats = nullptr;
+
+    // staging for the host-buffer cast
+    mrg_ray*      dStageRays = nullptr;
+    mrg_hit_keys* dStageHits = nullptr;
+    mrg_meta_hit* dStageMeta = nullptr;
+    size_t        stageCap = 0;
+};
+
+namespace {
+
+thread_local std::string g_lastError;
+
+mrg_status fail(mrg_status s, const std::string& msg)
+{
+    g_lastError = msg;
+    return s;
+}
+
+mrg_status cuda_fail(cudaError_t e, const char* what)
+{
+    cudaGetLastError();
+    return fail(e == cudaErrorMemoryAllocation ? MRG_ERR_OUT_OF_MEMORY : MRG_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define MRG_TRY(call, what) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return cuda_fail(e_, what); } while(0)
+
+void free_accel(mrg_ctx* c)
+{
+    cudaFree(c->dNodes); c->dNodes = nullptr;
+    cudaFree(c->dTris); c->dTris = nullptr;
+    cudaFree(c->dInsts); c->dInsts = nullptr;
+    cudaFree(c->dTlasLeaf); c->dTlasLeaf = nullptr;
+    c->blasNodes = c->blasTris = c->tlasNodes = 0;
+    c->scene = mrg::TraceScene{};
+    c->built = false;
+}
+
+struct DeviceGuard
+{
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if(cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if(prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() { if(prev >= 0) cudaSetDevice(prev); }
+};
+
+mrg::TraceScratch scratch_of(mrg_ctx* c)
+{
+    mrg::TraceScratch s;
+    s.workCounter = c->dScratch;
+    s.errorFlag = c->dScratch + 1;
+    s.stats = c->dStats;
+    return s;
+}
+
+} // namespace
+
+extern "C" {
+
+const char* mrg_last_error(void) { return g_lastError.c_str(); }
+
+const char* mrg_status_string(mrg_status s)
+{
+    switch(s)
+    {
+        case MRG_OK: return "ok";
+        case MRG_ERR_INVALID_ARG: return "invalid argument";
+        case MRG_ERR_CUDA: return "CUDA error";
+        case MRG_ERR_OUT_OF_MEMORY: return "out of memory";
+        case MRG_ERR_NOT_BUILT: return "accelerator not built";
+        case MRG_ERR_LIMIT: return "capacity limit exceeded";
+        case MRG_ERR_TRAVERSAL: return "traversal error";
+    }
+    return "unknown status";
+}
+
+mrg_status mrg_create(const mrg_params* params, mrg_ctx** out)
+{
+    if(!out) return fail(MRG_ERR_INVALID_ARG, "mrg_create: out_ctx is null");
+    *out = nullptr;
+    int dev = params ? params->device : 0;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if(e != cudaSuccess) return cuda_fail(e, "mrg_create: cudaGetDeviceCount");
+    if(dev < 0 || dev >= count) return fail(MRG_ERR_INVALID_ARG, "mrg_create: bad device ordinal");
+    mrg_ctx* c = new(std::nothrow) mrg_ctx();
+    if(!c) return fail(MRG_ERR_OUT_OF_MEMORY, "mrg_create: host allocation");
+    c->device = dev;
+    DeviceGuard g(dev);
+    if((e = cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+       (e = cudaStreamCreateWithFlags(&c->buildStream, cudaStreamNonBlocking)) != cudaSuccess ||
+       (e = cudaMalloc(&c->dScratch, 8 * sizeof(uint32_t))) != cudaSuccess ||
+       (e = cudaMalloc(&c->dStats, 4 * sizeof(unsigned long long))) != cudaSuccess ||
+       (e = cudaMemset(c->dScratch, 0, 8 * sizeof(uint32_t))) != cudaSuccess)
+    {
+        mrg_status s = cuda_fail(e, "mrg_create");
+        mrg_destroy(c);
+        return s;
+    }
+    *out = c;
+    return MRG_OK;
+}
+
+mrg_status mrg_destroy(mrg_ctx* c)
+{
+    if(!c) return MRG_OK;
+    DeviceGuard g(c->device);
+    free_accel(c);
+    cudaFree(c->dScratch);
+    cudaFree(c->dStats);
+    cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
+    if(c->buildStream) cudaStreamDestroy(c->buildStream);
+    delete c;
+    return MRG_OK;
+}
+
+mrg_status mrg_upload_mesh(mrg_ctx* c, const float* pos, uint32_t nv, const uint32_t* idx,
+                           uint32_t nt, uint32_t primKeyBase, uint32_t* outId)
+{
+    if(!c || !pos || !idx || nv == 0 || nt == 0)
+        return fail(MRG_ERR_INVALID_ARG, "mrg_upload_mesh: null pointer or empty mesh");
+    if(nt > (1u << 28) || (uint64_t)primKeyBase + nt > 0xFFFFFFFFull)
+        return fail(MRG_ERR_LIMIT, "mrg_upload_mesh: more than 2^28 triangles or key overflow");
+    for(uint64_t i = 0; i < 3ull * nt; i++)
+        if(idx[i] >= nv) return fail(MRG_ERR_INVALID_ARG, "mrg_upload_mesh: index out of range");
+    mrg_ctx::Mesh m;
+    try
+    {
+        m.pos.assign(pos, pos + 3ull * nv);
+        m.idx.assign(idx, idx + 3ull * nt);
+    }
+    catch(...) { return fail(MRG_ERR_OUT_OF_MEMORY, "mrg_upload_mesh: host allocation"); }
+    m.primKeyBase = primKeyBase;
+    c->meshes.push_back(std::move(m));
+    c->built = false;
+    if(outId) *outId = (uint32_t)(c->meshes.size() - 1);
+    return MRG_OK;
+}
+
+mrg_status mrg_add_instance(mrg_ctx* c, uint32_t mesh, const float m[12], uint32_t flags,
+                            uint32_t lm, uint32_t trans, uint32_t accel, uint32_t* outId)
+{
+    if(!c || !m) return fail(MRG_ERR_INVALID_ARG, "mrg_add_instance: null pointer");
+    if(mesh >= c->meshes.size()) return fail(MRG_ERR_INVALID_ARG, "mrg_add_instance: bad mesh id");
+    if(c->insts.size() >= (1u << 24)) return fail(MRG_ERR_LIMIT, "mrg_add_instance: more than 2^24 instances");
+    mrg_ctx::Inst in;
+    in.mesh = mesh;
+    std::memcpy(in.m, m, sizeof(in.m));
+    mrg::mat34_inverse(in.m, in.inv, (flags & MRG_INSTANCE_CORRECTED_INVERSE) != 0);
+    in.flags = flags; in.lm = lm; in.trans = trans; in.accel = accel;
+    c->insts.push_back(in);
+    c->built = false;
+    if(outId) *outId = (uint32_t)(c->insts.size() - 1);
+    return MRG_OK;
+}
+
+mrg_status mrg_build(mrg_ctx* c)
+{
+    if(!c) return fail(MRG_ERR_INVALID_ARG, "mrg_build: null context");
+    if(c->insts.empty()) return fail(MRG_ERR_INVALID_ARG, "mrg_build: no instances");
+    DeviceGuard g(c->device);
+    auto t0 = std::chrono::steady_clock::now();
+    free_accel(c);
+    cudaStream_t st = c->buildStream;
+    std::string err;
+
+    // 1. one BLAS per mesh
+    std::vector<mrg::BuildResult> blas(c->meshes.size());
+    for(size_t mi = 0; mi < c->meshes.size(); mi++)
+    {
+        auto& m = c->meshes[mi];
+        float* dPos = nullptr; uint32_t* dIdx = nullptr;
+        MRG_TRY(cudaMalloc(&dPos, sizeof(float) * m.pos.size()), "mrg_build: mesh upload");
+        cudaError_t e = cudaMalloc(&dIdx, sizeof(uint32_t) * m.idx.size());
+        if(e == cudaSuccess) e = cudaMemcpyAsync(dPos, m.pos.data(), sizeof(float) * m.pos.size(), cudaMemcpyHostToDevice, st);
+        if(e == cudaSuccess) e = cudaMemcpyAsync(dIdx, m.idx.data(), sizeof(uint32_t) * m.idx.size(), cudaMemcpyHostToDevice, st);
+        if(e != cudaSuccess) { cudaFree(dPos); cudaFree(dIdx); return cuda_fail(e, "mrg_build: mesh upload"); }
+        mrg::BuildInput bi;
+        bi.kind = 0; bi.pos = dPos; bi.idx = dIdx;
+        bi.count = (uint32_t)(m.idx.size() / 3);
+        bi.primKeyBase = m.primKeyBase;
+        bi.maxLeaf = 3;
+        bool ok = mrg::build_wide_bvh(bi, blas[mi], st, err);
+        cudaFree(dPos); cudaFree(dIdx);
+        if(!ok)
+        {
+            for(auto& b : blas) { cudaFree(b.nodes); cudaFree(b.tris); }
+            return fail(MRG_ERR_CUDA, "mrg_build: BLAS build: " + err);
+        }
+        std::memcpy(m.box, blas[mi].box, sizeof(m.box));
+    }
+
+    // 2. instance world boxes + TLAS
+    const uint32_t ni = (uint32_t)c->insts.size();
+    std::vector<float> instBoxes(6ull * ni);
+    for(uint32_t i = 0; i < ni; i++)
+        mrg::transform_box_conservative(c->insts[i].m, c->meshes[c->insts[i].mesh].box, &instBoxes[6ull * i]);
+    for(int k = 0; k < 3; k++) { c->sceneBox[k] = 3.0e38f; c->sceneBox[3 + k] = -3.0e38f; }
+    for(uint32_t i = 0; i < ni; i++)
+        for(int k = 0; k < 3; k++)
+        {
+            c->sceneBox[k] = std::min(c->sceneBox[k], instBoxes[6ull * i + k]);
+            c->sceneBox[3 + k] = std::max(c->sceneBox[3 + k], instBoxes[6ull * i + 3 + k]);
+        }
+    float* dBoxes = nullptr;
+    mrg::BuildResult tlas;
+    {
+        cudaError_t e = cudaMalloc(&dBoxes, sizeof(float) * instBoxes.size());
+        if(e == cudaSuccess) e = cudaMemcpyAsync(dBoxes, instBoxes.data(), sizeof(float) * instBoxes.size(), cudaMemcpyHostToDevice, st);
+        if(e != cudaSuccess)
+        {
+            cudaFree(dBoxes);
+            for(auto& b : blas) { cudaFree(b.nodes); cudaFree(b.tris); }
+            return cuda_fail(e, "mrg_build: instance boxes");
+        }
+        mrg::BuildInput bi;
+        bi.kind = 1; bi.boxes = dBoxes; bi.count = ni; bi.maxLeaf = 1;
+        bool ok = mrg::build_wide_bvh(bi, tlas, st, err);
+        cudaFree(dBoxes);
+        if(!ok)
+        {
+            for(auto& b : blas) { cudaFree(b.nodes); cudaFree(b.tris); }
+            return fail(MRG_ERR_CUDA, "mrg_build: TLAS build: " + err);
+        }
+    }
+
+    // 3. place everything in shared arrays
+    uint64_t totalNodes = 0, totalTris = 0;
+    for(auto& b : blas) { totalNodes += b.nodeCount; totalTris += b.payloadCount; }
+    const uint64_t tlasOff = totalNodes;
+    totalNodes += tlas.nodeCount;
+    cudaError_t e = cudaMalloc(&c->dNodes, mrg::kWideNodeBytes * totalNodes);
+    if(e == cudaSuccess) e = cudaMalloc(&c->dTris, mrg::kTriRecordBytes * totalTris);
+    if(e == cudaSuccess) e = cudaMalloc(&c->dInsts, sizeof(mrg::HostInstRecord) * ni);
+    if(e == cudaSuccess) e = cudaMalloc(&c->dTlasLeaf, sizeof(uint32_t) * ni);
+    uint64_t nodeOff = 0, triOff = 0;
+    for(size_t mi = 0; mi < blas.size() && e == cudaSuccess; mi++)
+    {
+        auto& b = blas[mi];
+        c->meshes[mi].rootNode = (uint32_t)nodeOff;
+        if(!mrg::relocate_nodes(b.nodes, reinterpret_cast<mrg::WideNode*>(
+                                    static_cast<char*>(c->dNodes) + mrg::kWideNodeBytes * nodeOff),
+                                b.nodeCount, (uint32_t)nodeOff, (uint32_t)triOff, st))
+            e = cudaErrorLaunchFailure;
+        if(e == cudaSuccess)
+            e = cudaMemcpyAsync(static_cast<char*>(c->dTris) + mrg::kTriRecordBytes * triOff, b.tris,
+                                mrg::kTriRecordBytes * b.payloadCount, cudaMemcpyDeviceToDevice, st);
+        nodeOff += b.nodeCount; triOff += b.payloadCount;
+    }
+    if(e == cudaSuccess &&
+       !mrg::relocate_nodes(tlas.nodes, reinterpret_cast<mrg::WideNode*>(
+                                static_cast<char*>(c->dNodes) + mrg::kWideNodeBytes * tlasOff),
+                            tlas.nodeCount, (uint32_t)tlasOff, 0u, st))
+        e = cudaErrorLaunchFailure;
+    if(e == cudaSuccess)
+        e = cudaMemcpyAsync(c->dTlasLeaf, tlas.leafIds, sizeof(uint32_t) * ni, cudaMemcpyDeviceToDevice, st);
+    std::vector<mrg::HostInstRecord> recs(ni);
+    for(uint32_t i = 0; i < ni; i++)
+    {
+        const auto& in = c->insts[i];
+        std::memcpy(recs[i].inv, in.inv, sizeof(in.inv));
+        recs[i].keys[0] = in.lm;
+        recs[i].keys[1] = in.trans;
+        recs[i].keys[2] = in.accel;
+        recs[i].keys[3] = c->meshes[in.mesh].rootNode |
+                          ((in.flags & MRG_INSTANCE_CULL_BACKFACE) ? 0x80000000u : 0u);
+    }
+    if(e == cudaSuccess)
+        e = cudaMemcpyAsync(c->dInsts, recs.data(), sizeof(mrg::HostInstRecord) * ni, cudaMemcpyHostToDevice, st);
+    if(e == cudaSuccess) e = cudaStreamSynchronize(st);
+    for(auto& b : blas) { cudaFree(b.nodes); cudaFree(b.tris); }
+    cudaFree(tlas.nodes); cudaFree(tlas.leafIds);
+    if(e != cudaSuccess) { free_accel(c); return cuda_fail(e, "mrg_build: placement"); }
+
+    c->blasNodes = totalNodes - tlas.nodeCount;
+    c->blasTris = totalTris;
+    c->tlasNodes = tlas.nodeCount;
+    c->scene.nodes = static_cast<const mrg::WideNode*>(c->dNodes);
+    c->scene.tris = static_cast<const mrg::TriRecord*>(c->dTris);
+    c->scene.insts = static_cast<const mrg::InstRecord*>(c->dInsts);
+    c->scene.tlasLeaf = c->dTlasLeaf;
+    c->scene.tlasRoot = (uint32_t)tlasOff;
+    c->scene.instCount = ni;
+    c->built = true;
+    c->buildMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return MRG_OK;
+}
+
+mrg_status mrg_cast_closest(mrg_ctx* c, mrg_ray* dRays, const uint32_t* dIdx, uint32_t n,
+                            mrg_hit_keys* dHits, mrg_meta_hit* dMeta, void* stream)
+{
+    if(!c) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_closest: null context");
+    if(!c->built) return fail(MRG_ERR_NOT_BUILT, "mrg_cast_closest: call mrg_build first");
+    if(n == 0) return MRG_OK;
+    if(!dRays || !dHits || !dMeta) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_closest: null buffer");
+    if(reinterpret_cast<uintptr_t>(dRays) % 32 != 0 || reinterpret_cast<uintptr_t>(dHits) % 16 != 0 ||
+       reinterpret_cast<uintptr_t>(dMeta) % 8 != 0)
+        return fail(MRG_ERR_INVALID_ARG, "mrg_cast_closest: misaligned buffer");
+    DeviceGuard g(c->device);
+    cudaError_t e = mrg::launch_closest(c->scene, scratch_of(c), dRays, dIdx, n, dHits, dMeta,
+                                        c->smCount, static_cast<cudaStream_t>(stream));
+    if(e != cudaSuccess) return cuda_fail(e, "mrg_cast_closest");
+    return MRG_OK;
+}
+
+mrg_status mrg_cast_visibility(mrg_ctx* c, uint32_t* dVis, const mrg_ray* dRays,
+                               const uint32_t* dIdx, uint32_t n, void* stream)
+{
+    if(!c) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_visibility: null context");
+    if(!c->built) return fail(MRG_ERR_NOT_BUILT, "mrg_cast_visibility: call mrg_build first");
+    if(n == 0) return MRG_OK;
+    if(!dRays || !dVis) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_visibility: null buffer");
+    if(reinterpret_cast<uintptr_t>(dRays) % 32 != 0 || reinterpret_cast<uintptr_t>(dVis) % 4 != 0)
+        return fail(MRG_ERR_INVALID_ARG, "mrg_cast_visibility: misaligned buffer");
+    DeviceGuard g(c->device);
+    cudaError_t e = mrg::launch_visibility(c->scene, scratch_of(c), dVis, dRays, dIdx, n,
+                                           c->smCount, static_cast<cudaStream_t>(stream));
+    if(e != cudaSuccess) return cuda_fail(e, "mrg_cast_visibility");
+    return MRG_OK;
+}
+
+mrg_status mrg_cast_closest_host(mrg_ctx* c, mrg_ray* hRays, uint32_t n, mrg_hit_keys* hHits,
+                                 mrg_meta_hit* hMeta)
+{
+    if(!c) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_closest_host: null context");
+    if(!c->built) return fail(MRG_ERR_NOT_BUILT, "mrg_cast_closest_host: call mrg_build first");
+    if(n == 0) return MRG_OK;
+    if(!hRays || !hHits || !hMeta) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_closest_host: null buffer");
+    DeviceGuard g(c->device);
+    if(n > c->stageCap)
+    {
+        cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
+        c->dStageRays = nullptr; c->dStageHits = nullptr; c->dStageMeta = nullptr; c->stageCap = 0;
+        MRG_TRY(cudaMalloc(&c->dStageRays, sizeof(mrg_ray) * (size_t)n), "mrg_cast_closest_host: staging");
+        MRG_TRY(cudaMalloc(&c->dStageHits, sizeof(mrg_hit_keys) * (size_t)n), "mrg_cast_closest_host: staging");
+        MRG_TRY(cudaMalloc(&c->dStageMeta, sizeof(mrg_meta_hit) * (size_t)n), "mrg_cast_closest_host: staging");
+        c->stageCap = n;
+    }
+    cudaStream_t st = c->buildStream;
+    MRG_TRY(cudaMemcpyAsync(c->dStageRays, hRays, sizeof(mrg_ray) * (size_t)n, cudaMemcpyHostToDevice, st), "H2D rays");
+    MRG_TRY(cudaMemcpyAsync(c->dStageHits, hHits, sizeof(mrg_hit_keys) * (size_t)n, cudaMemcpyHostToDevice, st), "H2D hits");
+    MRG_TRY(cudaMemcpyAsync(c->dStageMeta, hMeta, sizeof(mrg_meta_hit) * (size_t)n, cudaMemcpyHostToDevice, st), "H2D meta");
+    MRG_TRY(mrg::launch_closest(c->scene, scratch_of(c), c->dStageRays, nullptr, n, c->dStageHits,
+                                c->dStageMeta, c->smCount, st), "cast");
+    MRG_TRY(cudaMemcpyAsync(hRays, c->dStageRays, sizeof(mrg_ray) * (size_t)n, cudaMemcpyDeviceToHost, st), "D2H rays");
+    MRG_TRY(cudaMemcpyAsync(hHits, c->dStageHits, sizeof(mrg_hit_keys) * (size_t)n, cudaMemcpyDeviceToHost, st), "D2H hits");
+    MRG_TRY(cudaMemcpyAsync(hMeta, c->dStageMeta, sizeof(mrg_meta_hit) * (size_t)n, cudaMemcpyDeviceToHost, st), "D2H meta");
+    return mrg_sync_status(c, st);
+}
+
+mrg_status mrg_scene_aabb(mrg_ctx* c, float out[6])
+{
+    if(!c || !out) return fail(MRG_ERR_INVALID_ARG, "mrg_scene_aabb: null pointer");
+    if(!c->built) return fail(MRG_ERR_NOT_BUILT, "mrg_scene_aabb: call mrg_build first");
+    std::memcpy(out, c->sceneBox, sizeof(c->sceneBox));
+    return MRG_OK;
+}
+
+mrg_status mrg_get_stats(mrg_ctx* c, mrg_accel_stats* out)
+{
+    if(!c || !out) return fail(MRG_ERR_INVALID_ARG, "mrg_get_stats: null pointer");
+    out->blasNodes = c->blasNodes;
+    out->blasTriangles = c->blasTris;
+    out->tlasNodes = c->tlasNodes;
+    out->instances = c->insts.size();
+    out->deviceBytes = mrg::kWideNodeBytes * (c->blasNodes + c->tlasNodes) +
+                       mrg::kTriRecordBytes * c->blasTris +
+                       (sizeof(mrg::HostInstRecord) + 4) * c->insts.size();
+    out->buildMs = c->buildMs;
+    return MRG_OK;
+}
+
+mrg_status mrg_sync_status(mrg_ctx* c, void* stream)
+{
+    if(!c) return fail(MRG_ERR_INVALID_ARG, "mrg_sync_status: null context");
+    DeviceGuard g(c->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    MRG_TRY(cudaStreamSynchronize(st), "mrg_sync_status: stream");
+    uint32_t flag = 0;
+    MRG_TRY(cudaMemcpy(&flag, c->dScratch + 1, sizeof(flag), cudaMemcpyDeviceToHost), "mrg_sync_status: read flag");
+    if(flag)
+    {
+        MRG_TRY(cudaMemset(c->dScratch + 1, 0, sizeof(uint32_t)), "mrg_sync_status: clear flag");
+        return fail(MRG_ERR_TRAVERSAL, (flag & mrg::kTraceStackOverflow) ? "traversal stack overflow"
+                                                                         : "traversal step cap reached");
+    }
+    return MRG_OK;
+}
+
+mrg_status mrg_cast_closest_stats(mrg_ctx* c, const mrg_ray* dRays, uint32_t n,
+                                  uint64_t out[4], void* stream)
+{
+    if(!c || !out) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_closest_stats: null pointer");
+    if(!c->built) return fail(MRG_ERR_NOT_BUILT, "mrg_cast_closest_stats: call mrg_build first");
+    DeviceGuard g(c->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    MRG_TRY(mrg::launch_closest_stats(c->scene, scratch_of(c), dRays, n, c->smCount, st), "stats cast");
+    unsigned long long h[4] = { 0, 0, 0, 0 };
+    MRG_TRY(cudaMemcpyAsync(h, c->dStats, sizeof(h), cudaMemcpyDeviceToHost, st), "stats read");
+    MRG_TRY(cudaStreamSynchronize(st), "stats sync");
+    for(int i = 0; i < 4; i++) out[i] = h[i];
+    return MRG_OK;
+}
+
+} // extern "C"

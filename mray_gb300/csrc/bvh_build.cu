@@ -1,0 +1,602 @@
+// bvh_build.cu -- GPU builder of the 8-wide compressed BVH.
+//
+// Replaces MRay's LBVH construction (Source/Tracer/AcceleratorLBVH.hpp:584-899,
+// Source/Tracer/AcceleratorLBVH.cu:96-435, .cu:537-740) with:
+//   1. leaf boxes + centroid bounds          (k_leaf_boxes_*)
+//   2. 63-bit Morton codes in fp32/int       (k_morton; the reference quantises
+//      in double, which is slow on this part and changes only the tree shape)
+//   3. radix sort of (code, leaf)            (CUB DeviceRadixSort, build only)
+//   4. Karras 2012 binary radix tree         (k_karras)
+//   5. bottom-up boxes + leaf counts         (k_bottom_up; fence + atomic)
+//   6. top-down collapse to 8-wide nodes     (k_collapse, one launch per level)
+//      with 8-bit quantised child boxes, up to `maxLeaf` primitives per leaf
+//      child, children placed in slots by direction so that traversal visits
+//      them near-to-far (Ylitie, Karras, Laine 2017).
+// Closest-hit results do not depend on the tree shape: every box is inflated
+// outward (see `inflate`) so no box can cull a hit the triangle test accepts.
+#include "mrg_build.h"
+#include "mrg_device.cuh"
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cfloat>
+#include <vector>
+#include <cstring>
+
+namespace mrg {
+
+namespace {
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr uint32_t kNoParent = 0xFFFFFFFFu;
+constexpr int kTPB = 256;
+
+struct BinNode
+{
+    uint32_t left, right, parent, leafCount;
+};
+
+struct BoxF
+{
+    float mn[3];
+    float mx[3];
+};
+
+__device__ __forceinline__ uint32_t f2ord(float f)
+{
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// Triangle leaves: box of the three vertices, centroid bounds (ordered ints).
+__global__ void k_leaf_boxes_tri(const float* __restrict__ pos, const uint32_t* __restrict__ idx,
+                                 uint32_t n, BoxF* __restrict__ boxes, float* __restrict__ cent,
+                                 uint32_t* __restrict__ cbounds)
+{
+    __shared__ uint32_t sb[6];
+    if(threadIdx.x < 6) sb[threadIdx.x] = (threadIdx.x < 3) ? 0xFFFFFFFFu : 0u;
+    __syncthreads();
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n)
+    {
+        uint32_t a = idx[3 * i], b = idx[3 * i + 1], c = idx[3 * i + 2];
+        BoxF bx;
+        for(int k = 0; k < 3; k++)
+        {
+            float va = pos[3 * a + k], vb = pos[3 * b + k], vc = pos[3 * c + k];
+            bx.mn[k] = fminf(va, fminf(vb, vc));
+            bx.mx[k] = fmaxf(va, fmaxf(vb, vc));
+            float cc = 0.5f * (bx.mn[k] + bx.mx[k]);
+            cent[3 * i + k] = cc;
+            atomicMin(&sb[k], f2ord(cc));
+            atomicMax(&sb[3 + k], f2ord(cc));
+        }
+        boxes[i] = bx;
+    }
+    __syncthreads();
+    if(threadIdx.x < 3) atomicMin(&cbounds[threadIdx.x], sb[threadIdx.x]);
+    else if(threadIdx.x < 6) atomicMax(&cbounds[threadIdx.x], sb[threadIdx.x]);
+}
+
+// Box leaves (TLAS over instance boxes).
+__global__ void k_leaf_boxes_given(const BoxF* __restrict__ in, uint32_t n,
+                                   BoxF* __restrict__ boxes, float* __restrict__ cent,
+                                   uint32_t* __restrict__ cbounds)
+{
+    __shared__ uint32_t sb[6];
+    if(threadIdx.x < 6) sb[threadIdx.x] = (threadIdx.x < 3) ? 0xFFFFFFFFu : 0u;
+    __syncthreads();
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n)
+    {
+        BoxF bx = in[i];
+        boxes[i] = bx;
+        for(int k = 0; k < 3; k++)
+        {
+            float cc = 0.5f * (bx.mn[k] + bx.mx[k]);
+            cent[3 * i + k] = cc;
+            atomicMin(&sb[k], f2ord(cc));
+            atomicMax(&sb[3 + k], f2ord(cc));
+        }
+    }
+    __syncthreads();
+    if(threadIdx.x < 3) atomicMin(&cbounds[threadIdx.x], sb[threadIdx.x]);
+    else if(threadIdx.x < 6) atomicMax(&cbounds[threadIdx.x], sb[threadIdx.x]);
+}
+
+__device__ __forceinline__ uint64_t expand21(uint32_t v)
+{
+    uint64_t x = v & 0x1FFFFFu;
+    x = (x | x << 32) & 0x001F00000000FFFFull;
+    x = (x | x << 16) & 0x001F0000FF0000FFull;
+    x = (x | x << 8)  & 0x100F00F00F00F00Full;
+    x = (x | x << 4)  & 0x10C30C30C30C30C3ull;
+    x = (x | x << 2)  & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(const float* __restrict__ cent, const uint32_t* __restrict__ cbounds,
+                         uint32_t n, uint64_t* __restrict__ codes, uint32_t* __restrict__ ids)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    uint32_t q[3];
+    for(int k = 0; k < 3; k++)
+    {
+        float lo = ord2f(cbounds[k]), hi = ord2f(cbounds[3 + k]);
+        float ext = hi - lo;
+        float s = (ext > 0.0f) ? (2097151.0f / ext) : 0.0f;
+        float v = (cent[3 * i + k] - lo) * s;
+        v = fminf(fmaxf(v, 0.0f), 2097151.0f);
+        q[k] = (uint32_t)v;
+    }
+    codes[i] = expand21(q[0]) | (expand21(q[1]) << 1) | (expand21(q[2]) << 2);
+    ids[i] = i;
+}
+
+__device__ __forceinline__ int k_delta(const uint64_t* __restrict__ c, int n, int i, int j)
+{
+    if(j < 0 || j >= n) return -1;
+    uint64_t a = c[i], b = c[j];
+    if(a == b) return 64 + __clz((uint32_t)(i ^ j));
+    return __clzll(a ^ b);
+}
+
+// Karras 2012, "Maximizing parallelism in the construction of BVHs".
+__global__ void k_karras(const uint64_t* __restrict__ codes, int n, BinNode* __restrict__ nodes,
+                         uint32_t* __restrict__ leafParent)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n - 1) return;
+    int d = (k_delta(codes, n, i, i + 1) - k_delta(codes, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = k_delta(codes, n, i, i - d);
+    int lmax = 2;
+    while(k_delta(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for(int t = lmax >> 1; t >= 1; t >>= 1)
+        if(k_delta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = k_delta(codes, n, i, j);
+    int s = 0;
+    int t = l;
+    do
+    {
+        t = (t + 1) >> 1;
+        if(k_delta(codes, n, i, i + (s + t) * d) > dnode) s += t;
+    } while(t > 1);
+    int gamma = i + s * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    BinNode& me = nodes[i];
+    if(lo == gamma) { me.left = kLeafBit | (uint32_t)gamma; leafParent[gamma] = (uint32_t)i; }
+    else            { me.left = (uint32_t)gamma; nodes[gamma].parent = (uint32_t)i; }
+    if(hi == gamma + 1) { me.right = kLeafBit | (uint32_t)(gamma + 1); leafParent[gamma + 1] = (uint32_t)i; }
+    else                { me.right = (uint32_t)(gamma + 1); nodes[gamma + 1].parent = (uint32_t)i; }
+    if(i == 0) me.parent = kNoParent;
+}
+
+// Bottom-up boxes and leaf counts.  The second thread to reach a node merges
+// its children.  Writers fence before the counter atomic; readers of another
+// thread's node box load through L2 (__ldcg) since L1 is not coherent.
+__global__ void k_bottom_up(const uint32_t* __restrict__ leafParent, const uint32_t* __restrict__ sortedIds,
+                            const BoxF* __restrict__ leafBoxes, BinNode* nodes, BoxF* nodeBoxes,
+                            uint32_t* counters, int n)
+{
+    int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if(li >= n) return;
+    uint32_t p = leafParent[li];
+    while(p != kNoParent)
+    {
+        uint32_t old = atomicAdd(&counters[p], 1u);
+        if(old == 0) return;
+        __threadfence();
+        uint32_t ch[2] = { __ldcg(&nodes[p].left), __ldcg(&nodes[p].right) };
+        BoxF b;
+        uint32_t cnt = 0;
+        for(int k = 0; k < 3; k++) { b.mn[k] = FLT_MAX; b.mx[k] = -FLT_MAX; }
+        for(int c = 0; c < 2; c++)
+        {
+            BoxF cb;
+            if(ch[c] & kLeafBit)
+            {
+                cb = leafBoxes[sortedIds[ch[c] & ~kLeafBit]];
+                cnt += 1;
+            }
+            else
+            {
+                const float* src = reinterpret_cast<const float*>(&nodeBoxes[ch[c]]);
+                for(int k = 0; k < 3; k++) { cb.mn[k] = __ldcg(src + k); cb.mx[k] = __ldcg(src + 3 + k); }
+                cnt += __ldcg(&nodes[ch[c]].leafCount);
+            }
+            for(int k = 0; k < 3; k++) { b.mn[k] = fminf(b.mn[k], cb.mn[k]); b.mx[k] = fmaxf(b.mx[k], cb.mx[k]); }
+        }
+        nodeBoxes[p] = b;
+        nodes[p].leafCount = cnt;
+        __threadfence();
+        p = __ldcg(&nodes[p].parent);
+    }
+}
+
+struct CollapseArgs
+{
+    const BinNode*  nodes;
+    const BoxF*     nodeBoxes;
+    const BoxF*     leafBoxes;
+    const uint32_t* sortedIds;
+    // triangle payload (kind 0) or leaf ids (kind 1)
+    const float*    pos;
+    const uint32_t* idx;
+    uint32_t        primKeyBase;
+    int             kind;
+    uint32_t        maxLeaf;
+    float           inflate;
+    // outputs
+    WideNode*       wnodes;
+    TriRecord*      tris;
+    uint32_t*       leafIds;
+    uint32_t*       counters;   // [0] nodes, [1] leaf payloads, [2] next-queue size
+};
+
+__device__ __forceinline__ void ref_box(const CollapseArgs& a, uint32_t ref, BoxF& b, uint32_t& cnt)
+{
+    if(ref & kLeafBit) { b = a.leafBoxes[a.sortedIds[ref & ~kLeafBit]]; cnt = 1; }
+    else { b = a.nodeBoxes[ref]; cnt = a.nodes[ref].leafCount; }
+}
+
+__device__ __forceinline__ float half_area(const BoxF& b)
+{
+    float dx = b.mx[0] - b.mn[0], dy = b.mx[1] - b.mn[1], dz = b.mx[2] - b.mn[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ __forceinline__ void emit_payload(const CollapseArgs& a, uint32_t leafPos, uint32_t dst)
+{
+    uint32_t prim = a.sortedIds[leafPos];
+    if(a.kind == 1) { a.leafIds[dst] = prim; return; }
+    uint32_t i0 = a.idx[3 * prim], i1 = a.idx[3 * prim + 1], i2 = a.idx[3 * prim + 2];
+    float v0x = a.pos[3 * i0], v0y = a.pos[3 * i0 + 1], v0z = a.pos[3 * i0 + 2];
+    float v1x = a.pos[3 * i1], v1y = a.pos[3 * i1 + 1], v1z = a.pos[3 * i1 + 2];
+    float v2x = a.pos[3 * i2], v2y = a.pos[3 * i2 + 1], v2z = a.pos[3 * i2 + 2];
+    TriRecord r;
+    r.v0 = make_float4(v0x, v0y, v0z, __uint_as_float(a.primKeyBase + prim));
+    r.e0 = make_float4(__fsub_rn(v1x, v0x), __fsub_rn(v1y, v0y), __fsub_rn(v1z, v0z), 0.0f);
+    r.e1 = make_float4(__fsub_rn(v2x, v0x), __fsub_rn(v2y, v0y), __fsub_rn(v2z, v0z), 0.0f);
+    a.tris[dst] = r;
+}
+
+// One thread per wide node of the current level.
+__global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint32_t qn,
+                           uint2* __restrict__ nextQueue)
+{
+    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if(w >= qn) return;
+    uint2 item = queue[w];
+    uint32_t root = item.x;
+    uint32_t wideIdx = item.y;
+
+    uint32_t cand[8];
+    BoxF cbox[8];
+    uint32_t ccnt[8];
+    int nc = 0;
+    BoxF nbox; uint32_t ncnt;
+    ref_box(a, root, nbox, ncnt);
+    if((root & kLeafBit) || ncnt <= a.maxLeaf)
+    {
+        cand[0] = root; cbox[0] = nbox; ccnt[0] = ncnt; nc = 1;
+    }
+    else
+    {
+        const BinNode& bn = a.nodes[root];
+        cand[0] = bn.left;  ref_box(a, bn.left, cbox[0], ccnt[0]);
+        cand[1] = bn.right; ref_box(a, bn.right, cbox[1], ccnt[1]);
+        nc = 2;
+        while(nc < 8)
+        {
+            int best = -1; float bestA = -1.0f;
+            for(int c = 0; c < nc; c++)
+            {
+                if((cand[c] & kLeafBit) || ccnt[c] <= a.maxLeaf) continue;
+                float ar = half_area(cbox[c]);
+                if(ar > bestA) { bestA = ar; best = c; }
+            }
+            if(best < 0) break;
+            const BinNode& on = a.nodes[cand[best]];
+            cand[best] = on.left;  ref_box(a, on.left, cbox[best], ccnt[best]);
+            cand[nc] = on.right;   ref_box(a, on.right, cbox[nc], ccnt[nc]);
+            nc++;
+        }
+    }
+
+    // Quantisation frame: p = inflated min, 2^e * 255 >= inflated extent.
+    float px[3];
+    uint32_t eb[3];
+    float invS[3];
+    for(int k = 0; k < 3; k++)
+    {
+        float lo = __fsub_rd(nbox.mn[k], a.inflate);
+        float hi = __fadd_ru(nbox.mx[k], a.inflate);
+        float ext = __fsub_ru(hi, lo);
+        float x = __fdiv_ru(ext, 255.0f);
+        uint32_t bits = __float_as_uint(x);
+        int ex = (int)((bits >> 23) & 0xFF);
+        int e;
+        if(ex == 0) e = -126;
+        else e = ex - 127 + (((bits & 0x7FFFFFu) != 0u) ? 1 : 0);
+        e = max(-126, min(e, 126));
+        eb[k] = (uint32_t)(e + 127);
+        px[k] = lo;
+        invS[k] = __uint_as_float((uint32_t)(127 - e) << 23);
+    }
+
+    // Slot assignment by direction: slot s holds the child whose centre lies
+    // farthest towards corner s (bit i of s set = +axis i).
+    float ncx = 0.5f * (nbox.mn[0] + nbox.mx[0]);
+    float ncy = 0.5f * (nbox.mn[1] + nbox.mx[1]);
+    float ncz = 0.5f * (nbox.mn[2] + nbox.mx[2]);
+    int slotOf[8];
+    int childInSlot[8];
+    for(int s = 0; s < 8; s++) childInSlot[s] = -1;
+    for(int c = 0; c < 8; c++) slotOf[c] = -1;
+    for(int it = 0; it < nc; it++)
+    {
+        float bestV = -FLT_MAX; int bc = -1, bs = -1;
+        for(int c = 0; c < nc; c++)
+        {
+            if(slotOf[c] >= 0) continue;
+            float vx = 0.5f * (cbox[c].mn[0] + cbox[c].mx[0]) - ncx;
+            float vy = 0.5f * (cbox[c].mn[1] + cbox[c].mx[1]) - ncy;
+            float vz = 0.5f * (cbox[c].mn[2] + cbox[c].mx[2]) - ncz;
+            for(int s = 0; s < 8; s++)
+            {
+                if(childInSlot[s] >= 0) continue;
+                float v = ((s & 1) ? vx : -vx) + ((s & 2) ? vy : -vy) + ((s & 4) ? vz : -vz);
+                if(v > bestV) { bestV = v; bc = c; bs = s; }
+            }
+        }
+        slotOf[bc] = bs;
+        childInSlot[bs] = bc;
+    }
+
+    // Allocate children and payloads.
+    uint32_t numInternal = 0, numPayload = 0;
+    for(int c = 0; c < nc; c++)
+    {
+        bool leaf = (cand[c] & kLeafBit) || ccnt[c] <= a.maxLeaf;
+        if(leaf) numPayload += ccnt[c]; else numInternal++;
+    }
+    uint32_t childBase = numInternal ? atomicAdd(&a.counters[0], numInternal) : 0u;
+    uint32_t triBase = numPayload ? atomicAdd(&a.counters[1], numPayload) : 0u;
+    uint32_t qBase = numInternal ? atomicAdd(&a.counters[2], numInternal) : 0u;
+
+    uint8_t meta[8], qlo[3][8], qhi[3][8];
+    uint32_t imask = 0;
+    uint32_t rank = 0, triOff = 0;
+    for(int s = 0; s < 8; s++)
+    {
+        int c = childInSlot[s];
+        if(c < 0)
+        {
+            meta[s] = 0;
+            for(int k = 0; k < 3; k++) { qlo[k][s] = 0; qhi[k][s] = 0; }
+            continue;
+        }
+        for(int k = 0; k < 3; k++)
+        {
+            float lo = __fsub_rd(cbox[c].mn[k], a.inflate);
+            float hi = __fadd_ru(cbox[c].mx[k], a.inflate);
+            float ql = floorf(__fmul_rd(__fsub_rd(lo, px[k]), invS[k]));
+            float qh = ceilf(__fmul_ru(__fsub_ru(hi, px[k]), invS[k]));
+            qlo[k][s] = (uint8_t)fminf(fmaxf(ql, 0.0f), 255.0f);
+            qhi[k][s] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
+        }
+        bool leaf = (cand[c] & kLeafBit) || ccnt[c] <= a.maxLeaf;
+        if(!leaf)
+        {
+            imask |= 1u << s;
+            meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
+            nextQueue[qBase + rank] = make_uint2(cand[c], childBase + rank);
+            rank++;
+        }
+        else
+        {
+            uint32_t k = ccnt[c];
+            meta[s] = (uint8_t)((((1u << k) - 1u) << 5) | triOff);
+            // gather the subtree's leaves (at most maxLeaf <= 3)
+            uint32_t stack[8]; int sp = 0; stack[sp++] = cand[c];
+            uint32_t m = 0;
+            while(sp > 0)
+            {
+                uint32_t r = stack[--sp];
+                if(r & kLeafBit) { emit_payload(a, r & ~kLeafBit, triBase + triOff + m); m++; }
+                else { stack[sp++] = a.nodes[r].right; stack[sp++] = a.nodes[r].left; }
+            }
+            triOff += k;
+        }
+    }
+
+    WideNode out;
+    out.w0 = make_float4(px[0], px[1], px[2],
+                         __uint_as_float(eb[0] | (eb[1] << 8) | (eb[2] << 16) | (imask << 24)));
+    uint32_t m0 = meta[0] | (meta[1] << 8) | (meta[2] << 16) | ((uint32_t)meta[3] << 24);
+    uint32_t m1 = meta[4] | (meta[5] << 8) | (meta[6] << 16) | ((uint32_t)meta[7] << 24);
+    out.w1 = make_uint4(childBase, triBase, m0, m1);
+    uint32_t qw[12];
+    for(int k = 0; k < 3; k++)
+    {
+        qw[2 * k + 0] = qlo[k][0] | (qlo[k][1] << 8) | (qlo[k][2] << 16) | ((uint32_t)qlo[k][3] << 24);
+        qw[2 * k + 1] = qlo[k][4] | (qlo[k][5] << 8) | (qlo[k][6] << 16) | ((uint32_t)qlo[k][7] << 24);
+        qw[6 + 2 * k + 0] = qhi[k][0] | (qhi[k][1] << 8) | (qhi[k][2] << 16) | ((uint32_t)qhi[k][3] << 24);
+        qw[6 + 2 * k + 1] = qhi[k][4] | (qhi[k][5] << 8) | (qhi[k][6] << 16) | ((uint32_t)qhi[k][7] << 24);
+    }
+    out.q[0] = make_uint4(qw[0], qw[1], qw[2], qw[3]);
+    out.q[1] = make_uint4(qw[4], qw[5], qw[6], qw[7]);
+    out.q[2] = make_uint4(qw[8], qw[9], qw[10], qw[11]);
+    a.wnodes[wideIdx] = out;
+}
+
+// Adds fixed offsets to child / payload bases when a build is placed into the
+// shared node and triangle arrays.
+__global__ void k_relocate(const WideNode* __restrict__ in, WideNode* __restrict__ out, uint32_t n,
+                           uint32_t nodeOff, uint32_t triOff)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    WideNode w = in[i];
+    uint32_t imask = __float_as_uint(w.w0.w) >> 24;
+    if(imask) w.w1.x += nodeOff;
+    w.w1.y += triOff;
+    out[i] = w;
+}
+
+inline unsigned gridFor(uint32_t n, int tpb = kTPB) { return (unsigned)((n + tpb - 1) / tpb); }
+
+#define MRG_CK(x) do { cudaError_t e_ = (x); if(e_ != cudaSuccess) { err = std::string(#x) + ": " + cudaGetErrorString(e_); goto fail; } } while(0)
+
+} // namespace
+
+bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std::string& err)
+{
+    const uint32_t n = in.count;
+    out = BuildResult{};
+    if(n == 0) { err = "empty build"; return false; }
+
+    BoxF* dLeafBoxes = nullptr; float* dCent = nullptr; uint32_t* dCB = nullptr;
+    uint64_t* dCodes[2] = { nullptr, nullptr }; uint32_t* dIds[2] = { nullptr, nullptr };
+    void* dTemp = nullptr; size_t tempBytes = 0;
+    BinNode* dNodes = nullptr; BoxF* dNodeBoxes = nullptr; uint32_t* dLeafParent = nullptr;
+    uint32_t* dCnt = nullptr; uint2* dQ[2] = { nullptr, nullptr };
+    uint32_t* dCounters = nullptr;
+    WideNode* dW = nullptr;
+    const uint32_t nInt = (n > 1) ? (n - 1) : 1;
+    const uint32_t wideCap = n;      // each wide node consumes >= 1 binary node
+    uint32_t cbInit[6] = { 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u };
+    uint32_t hostCounters[3];
+    BoxF rootBox;
+    cub::DoubleBuffer<uint64_t> kb;
+    cub::DoubleBuffer<uint32_t> vb;
+    uint32_t qn = 1;
+    int cur = 0;
+    uint2 rootItem;
+    CollapseArgs ca;
+    float ext;
+
+    MRG_CK(cudaMallocAsync(&dLeafBoxes, sizeof(BoxF) * n, st));
+    MRG_CK(cudaMallocAsync(&dCent, sizeof(float) * 3 * n, st));
+    MRG_CK(cudaMallocAsync(&dCB, sizeof(uint32_t) * 6, st));
+    MRG_CK(cudaMallocAsync(&dCodes[0], sizeof(uint64_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dCodes[1], sizeof(uint64_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dIds[0], sizeof(uint32_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dIds[1], sizeof(uint32_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dNodes, sizeof(BinNode) * nInt, st));
+    MRG_CK(cudaMallocAsync(&dNodeBoxes, sizeof(BoxF) * nInt, st));
+    MRG_CK(cudaMallocAsync(&dLeafParent, sizeof(uint32_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dCnt, sizeof(uint32_t) * nInt, st));
+    MRG_CK(cudaMallocAsync(&dQ[0], sizeof(uint2) * wideCap, st));
+    MRG_CK(cudaMallocAsync(&dQ[1], sizeof(uint2) * wideCap, st));
+    MRG_CK(cudaMallocAsync(&dCounters, sizeof(uint32_t) * 3, st));
+    MRG_CK(cudaMallocAsync(&dW, sizeof(WideNode) * wideCap, st));
+    if(in.kind == 0) MRG_CK(cudaMallocAsync(&out.tris, sizeof(TriRecord) * n, st));
+    else             MRG_CK(cudaMallocAsync(&out.leafIds, sizeof(uint32_t) * n, st));
+
+    MRG_CK(cudaMemcpyAsync(dCB, cbInit, sizeof(cbInit), cudaMemcpyHostToDevice, st));
+    if(in.kind == 0)
+        k_leaf_boxes_tri<<<gridFor(n), kTPB, 0, st>>>(in.pos, in.idx, n, dLeafBoxes, dCent, dCB);
+    else
+        k_leaf_boxes_given<<<gridFor(n), kTPB, 0, st>>>(reinterpret_cast<const BoxF*>(in.boxes), n,
+                                                        dLeafBoxes, dCent, dCB);
+    MRG_CK(cudaGetLastError());
+    k_morton<<<gridFor(n), kTPB, 0, st>>>(dCent, dCB, n, dCodes[0], dIds[0]);
+    MRG_CK(cudaGetLastError());
+
+    kb = cub::DoubleBuffer<uint64_t>(dCodes[0], dCodes[1]);
+    vb = cub::DoubleBuffer<uint32_t>(dIds[0], dIds[1]);
+    MRG_CK(cub::DeviceRadixSort::SortPairs(nullptr, tempBytes, kb, vb, (int)n, 0, 63, st));
+    MRG_CK(cudaMallocAsync(&dTemp, tempBytes, st));
+    MRG_CK(cub::DeviceRadixSort::SortPairs(dTemp, tempBytes, kb, vb, (int)n, 0, 63, st));
+
+    if(n > 1)
+    {
+        MRG_CK(cudaMemsetAsync(dNodes, 0xFF, sizeof(BinNode) * nInt, st));
+        k_karras<<<gridFor(n - 1), kTPB, 0, st>>>(kb.Current(), (int)n, dNodes, dLeafParent);
+        MRG_CK(cudaGetLastError());
+        MRG_CK(cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * nInt, st));
+        k_bottom_up<<<gridFor(n), kTPB, 0, st>>>(dLeafParent, vb.Current(), dLeafBoxes, dNodes,
+                                                 dNodeBoxes, dCnt, (int)n);
+        MRG_CK(cudaGetLastError());
+        MRG_CK(cudaMemcpyAsync(&rootBox, dNodeBoxes, sizeof(BoxF), cudaMemcpyDeviceToHost, st));
+        rootItem = make_uint2(0u, 0u);
+    }
+    else
+    {
+        MRG_CK(cudaMemcpyAsync(&rootBox, dLeafBoxes, sizeof(BoxF), cudaMemcpyDeviceToHost, st));
+        rootItem = make_uint2(kLeafBit | 0u, 0u);
+    }
+    MRG_CK(cudaStreamSynchronize(st));
+    for(int k = 0; k < 3; k++) { out.box[k] = rootBox.mn[k]; out.box[3 + k] = rootBox.mx[k]; }
+
+    ext = 0.0f;
+    for(int k = 0; k < 3; k++)
+    {
+        float e = fabsf(rootBox.mx[k]) > fabsf(rootBox.mn[k]) ? fabsf(rootBox.mx[k]) : fabsf(rootBox.mn[k]);
+        ext = (ext > e) ? ext : e;
+        float sp = rootBox.mx[k] - rootBox.mn[k];
+        ext = (ext > sp) ? ext : sp;
+    }
+
+    ca.nodes = dNodes; ca.nodeBoxes = dNodeBoxes; ca.leafBoxes = dLeafBoxes;
+    ca.sortedIds = vb.Current(); ca.pos = in.pos; ca.idx = in.idx;
+    ca.primKeyBase = in.primKeyBase; ca.kind = in.kind; ca.maxLeaf = in.maxLeaf;
+    ca.inflate = ext * 1.0e-5f + 1.0e-30f;
+    ca.wnodes = dW; ca.tris = out.tris; ca.leafIds = out.leafIds; ca.counters = dCounters;
+
+    hostCounters[0] = 1; hostCounters[1] = 0; hostCounters[2] = 0;
+    MRG_CK(cudaMemcpyAsync(dCounters, hostCounters, sizeof(hostCounters), cudaMemcpyHostToDevice, st));
+    MRG_CK(cudaMemcpyAsync(dQ[0], &rootItem, sizeof(uint2), cudaMemcpyHostToDevice, st));
+    for(int level = 0; qn > 0; level++)
+    {
+        if(level > 64) { err = "wide BVH deeper than 64 levels"; goto fail; }
+        MRG_CK(cudaMemsetAsync(dCounters + 2, 0, sizeof(uint32_t), st));
+        k_collapse<<<gridFor(qn, 128), 128, 0, st>>>(ca, dQ[cur], qn, dQ[cur ^ 1]);
+        MRG_CK(cudaGetLastError());
+        MRG_CK(cudaMemcpyAsync(hostCounters, dCounters, sizeof(hostCounters), cudaMemcpyDeviceToHost, st));
+        MRG_CK(cudaStreamSynchronize(st));
+        if(hostCounters[0] > wideCap) { err = "wide node capacity exceeded"; goto fail; }
+        qn = hostCounters[2];
+        cur ^= 1;
+    }
+    if(hostCounters[1] != n) { err = "payload count mismatch"; goto fail; }
+    out.nodeCount = hostCounters[0];
+    MRG_CK(cudaMallocAsync(&out.nodes, sizeof(WideNode) * out.nodeCount, st));
+    MRG_CK(cudaMemcpyAsync(out.nodes, dW, sizeof(WideNode) * out.nodeCount, cudaMemcpyDeviceToDevice, st));
+    out.payloadCount = n;
+
+    cudaFreeAsync(dLeafBoxes, st); cudaFreeAsync(dCent, st); cudaFreeAsync(dCB, st);
+    cudaFreeAsync(dCodes[0], st); cudaFreeAsync(dCodes[1], st);
+    cudaFreeAsync(dIds[0], st); cudaFreeAsync(dIds[1], st); cudaFreeAsync(dTemp, st);
+    cudaFreeAsync(dNodes, st); cudaFreeAsync(dNodeBoxes, st); cudaFreeAsync(dLeafParent, st);
+    cudaFreeAsync(dCnt, st); cudaFreeAsync(dQ[0], st); cudaFreeAsync(dQ[1], st);
+    cudaFreeAsync(dCounters, st); cudaFreeAsync(dW, st);
+    if(cudaStreamSynchronize(st) != cudaSuccess) { err = "stream sync failed"; return false; }
+    return true;
+
+fail:
+    cudaStreamSynchronize(st);
+    cudaFree(dLeafBoxes); cudaFree(dCent); cudaFree(dCB); cudaFree(dCodes[0]); cudaFree(dCodes[1]);
+    cudaFree(dIds[0]); cudaFree(dIds[1]); cudaFree(dTemp); cudaFree(dNodes); cudaFree(dNodeBoxes);
+    cudaFree(dLeafParent); cudaFree(dCnt); cudaFree(dQ[0]); cudaFree(dQ[1]); cudaFree(dCounters);
+    cudaFree(dW); cudaFree(out.nodes); cudaFree(out.tris); cudaFree(out.leafIds);
+    out = BuildResult{};
+    return false;
+}
+
+bool relocate_nodes(const WideNode* src, WideNode* dst, uint32_t n, uint32_t nodeOff,
+                    uint32_t triOff, cudaStream_t st)
+{
+    if(n == 0) return true;
+    k_relocate<<<gridFor(n), kTPB, 0, st>>>(src, dst, n, nodeOff, triOff);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+} // namespace mrg

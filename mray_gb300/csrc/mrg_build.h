@@ -1,0 +1,71 @@
+// mrg_build.h -- host interface of the GPU wide-BVH builder and the kernels.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <cuda_runtime.h>
+
+namespace mrg {
+
+struct WideNode;
+struct TriRecord;
+struct InstRecord;
+
+struct BuildInput
+{
+    int             kind = 0;          // 0: triangles (pos/idx), 1: boxes (TLAS)
+    const float*    pos = nullptr;     // device, 3 floats per vertex
+    const uint32_t* idx = nullptr;     // device, 3 per triangle
+    const float*    boxes = nullptr;   // device, 6 floats per leaf (min xyz, max xyz)
+    uint32_t        count = 0;         // triangles or boxes
+    uint32_t        primKeyBase = 0;
+    uint32_t        maxLeaf = 3;       // primitives per leaf child (<= 3)
+};
+
+struct BuildResult
+{
+    WideNode*   nodes = nullptr;       // device, nodeCount (child bases local to this build)
+    uint32_t    nodeCount = 0;
+    TriRecord*  tris = nullptr;        // kind 0: device, payloadCount records
+    uint32_t*   leafIds = nullptr;     // kind 1: device, payloadCount leaf ids
+    uint32_t    payloadCount = 0;
+    float       box[6] = { 0, 0, 0, 0, 0, 0 };
+};
+
+bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std::string& err);
+bool relocate_nodes(const WideNode* src, WideNode* dst, uint32_t n, uint32_t nodeOff,
+                    uint32_t triOff, cudaStream_t st);
+
+// Traversal launch parameters (device pointers).
+struct TraceScene
+{
+    const WideNode*   nodes = nullptr;     // all BLAS nodes then TLAS nodes
+    const TriRecord*  tris = nullptr;
+    const InstRecord* insts = nullptr;
+    const uint32_t*   tlasLeaf = nullptr;  // instance id per TLAS payload slot
+    uint32_t          tlasRoot = 0;
+    uint32_t          instCount = 0;
+};
+
+struct TraceScratch
+{
+    uint32_t*           workCounter = nullptr;   // 1 word, zeroed before each launch
+    uint32_t*           errorFlag = nullptr;     // 1 word, sticky error bits
+    unsigned long long* stats = nullptr;         // 4 words (stats kernel only)
+};
+
+enum TraceErrorBits : uint32_t
+{
+    kTraceStackOverflow = 1u,
+    kTraceStepCap       = 2u
+};
+
+cudaError_t launch_closest(const TraceScene& sc, const TraceScratch& scr, void* rays,
+                           const uint32_t* rayIdx, uint32_t n, void* hits, void* meta,
+                           int smCount, cudaStream_t st);
+cudaError_t launch_visibility(const TraceScene& sc, const TraceScratch& scr, uint32_t* visBits,
+                              const void* rays, const uint32_t* rayIdx, uint32_t n,
+                              int smCount, cudaStream_t st);
+cudaError_t launch_closest_stats(const TraceScene& sc, const TraceScratch& scr, const void* rays,
+                                 uint32_t n, int smCount, cudaStream_t st);
+
+} // namespace mrg

@@ -1,0 +1,126 @@
+// mrg_device.cuh -- device-side data layout and exact-arithmetic helpers.
+//
+// HBM layout of one accelerator (all arrays 16-byte aligned):
+//   WideNode  wnodes[]   80 B each: 8-wide node with 8-bit quantised child
+//                        boxes (compressed wide BVH, Ylitie/Karras/Laine 2017).
+//   TriRecord tris[]     48 B each: v0, e0 = v1 - v0, e1 = v2 - v0, primKey.
+//                        e0/e1 are the exact float differences MRay's
+//                        Moller-Trumbore forms first (Source/Core/Ray.hpp:131-132),
+//                        so storing them keeps the test bit-identical.
+//   InstRecord insts[]   64 B each: inverse 3x4 transform rows + keys.
+//   uint32    tlasLeaf[] instance index per TLAS leaf slot.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mrg {
+
+struct __align__(16) WideNode
+{
+    // w0: origin p (x,y,z) + packed (ex | ey<<8 | ez<<16 | imask<<24)
+    float4 w0;
+    // w1: childBase, triBase, meta[0..3], meta[4..7]
+    uint4  w1;
+    // q[0]: qlo_x[0..7] qlo_y[0..7]; q[1]: qlo_z qhi_x; q[2]: qhi_y qhi_z
+    uint4  q[3];
+};
+static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
+
+struct __align__(16) TriRecord
+{
+    float4 v0;   // w = primKey (bit pattern)
+    float4 e0;   // w = 0
+    float4 e1;   // w = 0
+};
+static_assert(sizeof(TriRecord) == 48, "triangle record must be 48 bytes");
+
+struct __align__(16) InstRecord
+{
+    float4 inv[3];   // rows of the world->local 3x4 matrix
+    uint4  keys;     // lightOrMatKey, transKey, accelKey, blasRoot | cull<<31
+};
+static_assert(sizeof(InstRecord) == 64, "instance record must be 64 bytes");
+
+constexpr uint32_t kCullBit = 0x80000000u;
+constexpr uint32_t kInvalidIndex = 0xFFFFFFFFu;
+
+// -------------------------------------------------------------------------
+// Exact arithmetic in MRay's operation order.  Each helper uses
+// round-to-nearest intrinsics, which nvcc never contracts or reassociates,
+// so results are bit-identical to the reference host build.
+// -------------------------------------------------------------------------
+// Math::Dot (Source/Core/Math.h:1586-1596): r = 0; r = fma(a_i, b_i, r).
+__device__ __forceinline__ float dot3_exact(float ax, float ay, float az,
+                                            float bx, float by, float bz)
+{
+    float r = __fmaf_rn(ax, bx, 0.0f);
+    r = __fmaf_rn(ay, by, r);
+    r = __fmaf_rn(az, bz, r);
+    return r;
+}
+// 4-term Dot with w = 1 (Matrix3x4 * Vector4(p, 1), Source/Core/Matrix.hpp:777-788).
+__device__ __forceinline__ float dot4w1_exact(float4 row, float px, float py, float pz)
+{
+    float r = __fmaf_rn(row.x, px, 0.0f);
+    r = __fmaf_rn(row.y, py, r);
+    r = __fmaf_rn(row.z, pz, r);
+    r = __fmaf_rn(row.w, 1.0f, r);
+    return r;
+}
+// Math::Cross (Source/Core/Math.h:1627-1633).
+__device__ __forceinline__ void cross_exact(float ax, float ay, float az,
+                                            float bx, float by, float bz,
+                                            float& ox, float& oy, float& oz)
+{
+    ox = __fmaf_rn(ay, bz, -__fmul_rn(az, by));
+    oy = __fmaf_rn(az, bx, -__fmul_rn(ax, bz));
+    oz = __fmaf_rn(ax, by, -__fmul_rn(ay, bx));
+}
+
+constexpr float kSmallEpsilon = 1.0e-7f;   // MathConstants::SmallEpsilon
+
+// Ray::IntersectsTriangle (Source/Core/Ray.hpp:121-167) on a stored record.
+// Returns true on a hit; t, b0 (= u) and b1 (= v) are MRay's values; the
+// reported MetaHit is (1 - u - v, u).
+__device__ __forceinline__ bool intersect_tri_exact(const float3& o, const float3& d,
+                                                    const float4& v0, const float4& e0,
+                                                    const float4& e1, bool cull,
+                                                    float& tOut, float& uOut, float& vOut)
+{
+    float px, py, pz;
+    cross_exact(d.x, d.y, d.z, e1.x, e1.y, e1.z, px, py, pz);
+    float det = dot3_exact(e0.x, e0.y, e0.z, px, py, pz);
+    bool backface = det < kSmallEpsilon;
+    bool parallel = fabsf(det) < kSmallEpsilon;
+    if((cull && backface) || parallel) return false;
+    float invDet = __frcp_rn(det);          // IEEE 1/det
+    float tx = __fsub_rn(o.x, v0.x);
+    float ty = __fsub_rn(o.y, v0.y);
+    float tz = __fsub_rn(o.z, v0.z);
+    float u = __fmul_rn(dot3_exact(tx, ty, tz, px, py, pz), invDet);
+    if(u < 0.0f || u > 1.0f) return false;
+    float qx, qy, qz;
+    cross_exact(tx, ty, tz, e0.x, e0.y, e0.z, qx, qy, qz);
+    float v = __fmul_rn(dot3_exact(d.x, d.y, d.z, qx, qy, qz), invDet);
+    if(v < 0.0f || __fadd_rn(v, u) > 1.0f) return false;
+    float t = __fmul_rn(dot3_exact(e1.x, e1.y, e1.z, qx, qy, qz), invDet);
+    if(t <= kSmallEpsilon) return false;
+    tOut = t; uOut = u; vOut = v;
+    return true;
+}
+
+// Matrix3x4::TransformRay (Source/Core/Matrix.hpp:906-913) with the inverse.
+__device__ __forceinline__ void transform_ray_exact(const float4 r0, const float4 r1,
+                                                    const float4 r2,
+                                                    const float3& o, const float3& d,
+                                                    float3& lo, float3& ld)
+{
+    ld.x = dot3_exact(r0.x, r0.y, r0.z, d.x, d.y, d.z);
+    ld.y = dot3_exact(r1.x, r1.y, r1.z, d.x, d.y, d.z);
+    ld.z = dot3_exact(r2.x, r2.y, r2.z, d.x, d.y, d.z);
+    lo.x = dot4w1_exact(r0, o.x, o.y, o.z);
+    lo.y = dot4w1_exact(r1, o.x, o.y, o.z);
+    lo.z = dot4w1_exact(r2, o.x, o.y, o.z);
+}
+
+} // namespace mrg

@@ -1,0 +1,219 @@
+"""CPU oracle for the mray_gb300 hot path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` (as the checker) and bench.py's CPU
+baseline / reference arm may import this package.  The product (mray_gb300)
+never does.
+
+``Scene`` wraps the C restatement of MRay's host-backend LBVH path
+(mrg_oracle.c); ``RefCore`` wraps the reference's own compiled core math
+(oracle/_ref/libmray_ref_core.so, built from the MRay source tree where it is
+present).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_ref = None
+
+vp = C.c_void_p
+u32 = C.c_uint32
+
+
+def _vp(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = C.CDLL(path)
+        L.orc_intersect_triangle.argtypes = [vp] * 5 + [C.c_int, vp, vp, vp]
+        L.orc_intersect_triangle.restype = C.c_int
+        L.orc_intersect_aabb.argtypes = [vp] * 6
+        L.orc_intersect_aabb.restype = C.c_int
+        L.orc_mat34_inverse.argtypes = [vp, vp]
+        L.orc_transform_ray.argtypes = [vp] * 5
+        L.orc_transform_aabb.argtypes = [vp] * 5
+        L.orc_morton3d_u64.argtypes = [u32, u32, u32]
+        L.orc_morton3d_u64.restype = C.c_uint64
+        L.orc_nudge.argtypes = [vp, vp, vp]
+        L.orc_scene_create.restype = vp
+        L.orc_scene_destroy.argtypes = [vp]
+        L.orc_scene_add_mesh.argtypes = [vp, vp, u32, vp, u32, u32]
+        L.orc_scene_add_mesh.restype = C.c_int
+        L.orc_scene_add_instance.argtypes = [vp, u32, vp, u32, u32, u32, u32]
+        L.orc_mat34_inverse_corrected.argtypes = [vp, vp]
+        L.orc_scene_add_instance.restype = C.c_int
+        L.orc_scene_build.argtypes = [vp]
+        L.orc_scene_build.restype = C.c_int
+        L.orc_scene_instance_inverse.argtypes = [vp, u32, vp]
+        for f in ("orc_cast_closest", "orc_cast_closest_linear"):
+            getattr(L, f).argtypes = [vp, vp, vp, u32, vp, vp, vp, C.c_int]
+        L.orc_cast_visibility.argtypes = [vp, vp, vp, u32, vp, C.c_int]
+        L.orc_scene_stats.argtypes = [vp, vp]
+        _lib = L
+    return _lib
+
+
+def default_threads():
+    return max(1, os.cpu_count() or 1)
+
+
+class Scene:
+    """Two-level LBVH scene with MRay host-backend semantics."""
+
+    def __init__(self):
+        self._L = lib()
+        self._h = self._L.orc_scene_create()
+        self._keep = []
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._L.orc_scene_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def add_mesh(self, pos, idx, prim_key_base=0):
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        idx = np.ascontiguousarray(idx, np.uint32).reshape(-1, 3)
+        r = self._L.orc_scene_add_mesh(self._h, _vp(pos), pos.shape[0], _vp(idx), idx.shape[0],
+                                       prim_key_base)
+        if r < 0:
+            raise ValueError("oracle: bad mesh")
+        return r
+
+    def add_instance(self, mesh, m34, cull=True, lm_key=0, trans_key=0, accel_key=0,
+                     corrected_inverse=False):
+        m = np.ascontiguousarray(m34, np.float32).reshape(12)
+        flags = (1 if cull else 0) | (2 if corrected_inverse else 0)
+        r = self._L.orc_scene_add_instance(self._h, mesh, _vp(m), flags, lm_key,
+                                           trans_key, accel_key)
+        if r < 0:
+            raise ValueError("oracle: bad instance")
+        return r
+
+    def build(self):
+        if self._L.orc_scene_build(self._h) != 0:
+            raise RuntimeError("oracle build failed")
+
+    def instance_inverse(self, i):
+        out = np.empty(12, np.float32)
+        self._L.orc_scene_instance_inverse(self._h, i, _vp(out))
+        return out
+
+    def cast_closest(self, rays, ray_idx=None, hits=None, meta=None, linear=False, threads=None):
+        """Returns (rays (tMax updated), hits [N,4] u32, meta [N,2] f32, inst [N] u32)."""
+        rays = np.array(rays, np.float32, copy=True, order="C")
+        n_total = rays.shape[0]
+        hits = np.zeros((n_total, 4), np.uint32) if hits is None else np.array(hits, np.uint32, copy=True)
+        meta = np.zeros((n_total, 2), np.float32) if meta is None else np.array(meta, np.float32, copy=True)
+        inst = np.full(n_total, 0xFFFFFFFF, np.uint32)
+        ridx = None if ray_idx is None else np.ascontiguousarray(ray_idx, np.uint32)
+        n = n_total if ridx is None else ridx.shape[0]
+        f = self._L.orc_cast_closest_linear if linear else self._L.orc_cast_closest
+        f(self._h, _vp(rays), _vp(ridx), n, _vp(hits), _vp(meta), _vp(inst),
+          threads or default_threads())
+        return rays, hits, meta, inst
+
+    def cast_visibility(self, rays, ray_idx=None, bits=None, threads=None):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n_total = rays.shape[0]
+        words = (n_total + 31) // 32
+        bits = np.zeros(words, np.uint32) if bits is None else np.array(bits, np.uint32, copy=True)
+        ridx = None if ray_idx is None else np.ascontiguousarray(ray_idx, np.uint32)
+        n = n_total if ridx is None else ridx.shape[0]
+        self._L.orc_cast_visibility(self._h, _vp(rays), _vp(ridx), n, _vp(bits),
+                                    threads or default_threads())
+        return bits
+
+    def stats(self):
+        out = np.zeros(4, np.uint64)
+        self._L.orc_scene_stats(self._h, _vp(out))
+        return out
+
+
+def intersect_triangle(dir, pos, v0, v1, v2, cull):
+    L = lib()
+    a = [np.ascontiguousarray(x, np.float32) for x in (dir, pos, v0, v1, v2)]
+    bary = np.zeros(3, np.float32)
+    t = np.zeros(1, np.float32)
+    bf = np.zeros(1, np.int32)
+    hit = L.orc_intersect_triangle(*[_vp(x) for x in a], 1 if cull else 0, _vp(bary), _vp(t), _vp(bf))
+    return bool(hit), bary, float(t[0]), bool(bf[0])
+
+
+class RefCore:
+    """The reference's own compiled core math (oracle/_ref), when built."""
+
+    def __init__(self):
+        global _ref
+        if _ref is None:
+            path = _build.build_ref()
+            if path is None or not os.path.exists(path):
+                raise FileNotFoundError("reference core library unavailable (MRay source tree absent)")
+            R = C.CDLL(path)
+            R.ref_intersect_triangles.argtypes = [u32, vp, vp, C.c_int, vp, vp, vp]
+            R.ref_intersect_aabbs.argtypes = [u32, vp, vp, vp, vp, vp]
+            R.ref_mat34_inverse.argtypes = [vp, vp]
+            R.ref_transform_rays.argtypes = [u32, vp, vp, vp]
+            R.ref_transform_aabb.argtypes = [vp, vp, vp]
+            R.ref_morton3d_u64.argtypes = [u32, vp, vp]
+            R.ref_nudge.argtypes = [u32, vp, vp, vp]
+            _ref = R
+        self.R = _ref
+
+    def intersect_triangles(self, rays6, tris9, cull):
+        n = rays6.shape[0]
+        rays6 = np.ascontiguousarray(rays6, np.float32)
+        tris9 = np.ascontiguousarray(tris9, np.float32)
+        hit = np.zeros(n, np.uint32)
+        bary = np.zeros((n, 3), np.float32)
+        t = np.zeros(n, np.float32)
+        self.R.ref_intersect_triangles(n, _vp(rays6), _vp(tris9), 1 if cull else 0, _vp(hit),
+                                       _vp(bary), _vp(t))
+        return hit, bary, t
+
+    def intersect_aabbs(self, rays6, boxes6, tmm2):
+        n = rays6.shape[0]
+        hit = np.zeros(n, np.uint32)
+        tout = np.zeros((n, 2), np.float32)
+        self.R.ref_intersect_aabbs(n, _vp(np.ascontiguousarray(rays6, np.float32)),
+                                   _vp(np.ascontiguousarray(boxes6, np.float32)),
+                                   _vp(np.ascontiguousarray(tmm2, np.float32)), _vp(hit), _vp(tout))
+        return hit, tout
+
+    def mat34_inverse(self, m):
+        out = np.zeros(12, np.float32)
+        self.R.ref_mat34_inverse(_vp(np.ascontiguousarray(m, np.float32)), _vp(out))
+        return out
+
+    def transform_rays(self, m, rays6):
+        out = np.zeros_like(rays6, dtype=np.float32)
+        self.R.ref_transform_rays(rays6.shape[0], _vp(np.ascontiguousarray(m, np.float32)),
+                                  _vp(np.ascontiguousarray(rays6, np.float32)), _vp(out))
+        return out
+
+    def transform_aabb(self, m, box6):
+        out = np.zeros(6, np.float32)
+        self.R.ref_transform_aabb(_vp(np.ascontiguousarray(m, np.float32)),
+                                  _vp(np.ascontiguousarray(box6, np.float32)), _vp(out))
+        return out
+
+    def morton3d(self, xyz):
+        xyz = np.ascontiguousarray(xyz, np.uint32)
+        out = np.zeros(xyz.shape[0], np.uint64)
+        self.R.ref_morton3d_u64(xyz.shape[0], _vp(xyz), _vp(out))
+        return out
+
+    def nudge(self, pos, dirs):
+        pos = np.ascontiguousarray(pos, np.float32)
+        out = np.zeros_like(pos)
+        self.R.ref_nudge(pos.shape[0], _vp(pos), _vp(np.ascontiguousarray(dirs, np.float32)), _vp(out))
+        return out

@@ -1,0 +1,164 @@
+"""GPU parity of the closest-hit / any-hit kernels against the CPU oracle,
+through the C ABI.  Bar: bit-exact hit keys, barycentrics and t for every ray
+except exact-t ties between different primitives (first-found wins in MRay,
+Source/Tracer/AcceleratorLBVH.hpp:363-367); bit-exact visibility bits."""
+import numpy as np
+import pytest
+
+import oracle
+from mray_gb300 import MRGError, scenes
+from parity_util import (MISS, build_pair, compare_closest, gpu_closest, gpu_visibility,
+                         stress_workload)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _libs(cuda_lib, built_libs):
+    return True
+
+
+def small(level=3, ninst=8, seed=0, box=6.0):
+    pos, idx = scenes.icosphere(level, 1.0, 0.05, 4.0, seed)
+    m = scenes.instance_field(ninst, seed, box=box, jitter=0.3)
+    return pos, idx, m
+
+
+@pytest.mark.parametrize("level,ninst", [(0, 1), (1, 3), (3, 8), (4, 27), (5, 64)])
+@pytest.mark.parametrize("cull", [True, False])
+def test_closest_small_scenes(level, ninst, cull):
+    pos, idx, m = small(level, ninst, seed=level)
+    acc, S = build_pair(pos, idx, m, cull=cull)
+    rays = scenes.primary_rays(97, 61, level, eye=(0, 0, -14), tan_half_fov=0.5)
+    ora = S.cast_closest(rays)
+    gpu = gpu_closest(acc, rays)
+    n, hits, ties = compare_closest(ora, gpu)
+    assert hits > 0
+
+
+def test_corrected_inverse_mode_general_rotations():
+    """General random rotations (MRay's inverse is wrong for them) in the
+    corrected mode; also the default mode on the same rotations."""
+    rng = np.random.default_rng(5)
+    pos, idx = scenes.icosphere(3, 1.0, 0.05, 4.0, 0)
+    mats = []
+    for i in range(12):
+        q = rng.normal(size=4); q /= np.linalg.norm(q)
+        w, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        mats.append(np.hstack([R, rng.uniform(-3, 3, (3, 1))]).reshape(12))
+    mats = np.array(mats, np.float32)
+    rays = scenes.primary_rays(80, 80, 9, eye=(0, 0, -12), tan_half_fov=0.5)
+    for corrected in (True, False):
+        acc, S = build_pair(pos, idx, mats, corrected=corrected)
+        compare_closest(S.cast_closest(rays), gpu_closest(acc, rays))
+
+
+def test_indirection_partial_lists_and_prefilled_hits():
+    pos, idx, m = small(4, 27)
+    acc, S = build_pair(pos, idx, m)
+    rays = scenes.primary_rays(64, 64, 3, eye=(0, 0, -12), tan_half_fov=0.6)
+    rng = np.random.default_rng(1)
+    sel = rng.permutation(rays.shape[0])[:1237].astype(np.uint32)
+    pre = np.full((rays.shape[0], 4), 0x5A5A5A5A, np.uint32)
+    ora = S.cast_closest(rays, ray_idx=sel, hits=pre)
+    gpu = gpu_closest(acc, rays, ray_idx=sel, pre_hits=pre)
+    compare_closest(ora, gpu)      # all rays: unlisted ones must be untouched too
+    assert (gpu[1][np.setdiff1d(np.arange(rays.shape[0]), sel)] == 0x5A5A5A5A).all()
+
+
+def test_visibility_small():
+    pos, idx, m = small(4, 27)
+    acc, S = build_pair(pos, idx, m)
+    rays = scenes.primary_rays(71, 53, 4, eye=(0, 0, -12), tan_half_fov=0.6)
+    closest = S.cast_closest(rays)
+    hitm = closest[3] != MISS
+    seg = rays.copy()
+    seg[hitm, 7] = closest[0][hitm, 7] * np.float32(1.0001)   # segments ending just after the hit
+    seg[::3, 7] = closest[0][::3, 7] * np.float32(0.5)
+    for rs in (rays, seg):
+        assert np.array_equal(gpu_visibility(acc, rs), S.cast_visibility(rs))
+    sel = np.arange(0, rays.shape[0], 7, dtype=np.uint32)
+    pre = np.full((rays.shape[0] + 31) // 32, 0xFFFF0000, np.uint32)
+    assert np.array_equal(gpu_visibility(acc, seg, ray_idx=sel, pre_bits=pre),
+                          S.cast_visibility(seg, ray_idx=sel, bits=pre))
+
+
+def test_edge_rays():
+    """Axis-parallel directions (zero components), rays starting inside the
+    geometry, empty [tMin, tMax), far tMin, degenerate triangles."""
+    pos, idx, m = small(3, 8)
+    pos = pos.copy()
+    idx = np.vstack([idx, [[0, 0, 1]], [[2, 2, 2]]]).astype(np.uint32)   # degenerate tris
+    acc, S = build_pair(pos, idx, m, cull=False)
+    rng = np.random.default_rng(11)
+    n = 4096
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-4, 4, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d[: n // 4, 1:] = 0.0
+    d[n // 4: n // 2, 0] = 0.0
+    d[n // 2: n // 2 + 16] = [0.0, -0.0, 1.0]
+    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 3] = 0.0
+    rays[:, 7] = 3.4e38
+    rays[100:200, 3] = 50.0          # tMin beyond everything
+    rays[200:300, 7] = 0.0           # empty interval
+    rays[300:400, 3] = 1.0
+    rays[300:400, 7] = 1.0           # [1, 1): empty for a half-open range
+    compare_closest(S.cast_closest(rays), gpu_closest(acc, rays))
+    assert np.array_equal(gpu_visibility(acc, rays), S.cast_visibility(rays))
+
+
+def test_zero_rays_and_not_built_errors():
+    import torch
+    from mray_gb300 import Accelerator
+    acc = Accelerator(0)
+    dr = torch.zeros((4, 8), device="cuda")
+    hits = torch.zeros((4, 4), dtype=torch.int32, device="cuda")
+    meta = torch.zeros((4, 2), device="cuda")
+    with pytest.raises(MRGError):
+        acc.cast_rays(dr, hits, meta)
+    pos, idx, m = small(1, 1)
+    acc.upload_mesh(pos, idx)
+    acc.add_instance(0, m[0])
+    acc.construct()
+    acc.cast_rays(dr, hits, meta, count=0)
+    acc.sync_status()
+    with pytest.raises(MRGError):
+        acc.add_instance(5, m[0])
+
+
+def test_host_buffer_entry_point_matches_device():
+    pos, idx, m = small(4, 27)
+    acc, S = build_pair(pos, idx, m)
+    rays = scenes.primary_rays(128, 96, 6, eye=(0, 0, -12), tan_half_fov=0.6)
+    hr = rays.copy()
+    hh = np.zeros((rays.shape[0], 4), np.uint32)
+    hm = np.zeros((rays.shape[0], 2), np.float32)
+    acc.cast_rays_host(hr, hh, hm)
+    ora = S.cast_closest(rays)
+    compare_closest(ora, (hr, hh, hm))
+
+
+def test_stress_scene_full_size_parity():
+    """1.31M-triangle icosphere x 64 instances, 1920x1080 primary rays plus
+    one diffuse bounce (~4M rays) and shadow rays: bit-exact against the
+    oracle at the benchmark's full size."""
+    pos, idx, m, prim = stress_workload()
+    acc, S = build_pair(pos, idx, m)
+    ora_p = S.cast_closest(prim)
+    gpu_p = gpu_closest(acc, prim)
+    n, hits, ties = compare_closest(ora_p, gpu_p)
+    assert hits > 0.8 * n
+    bounce, src = scenes.bounce_rays(prim, ora_p[3], ora_p[1][:, 0] - 0x10000000, ora_p[0][:, 7],
+                                     pos, idx, m, seed=1)
+    ora_b = S.cast_closest(bounce)
+    gpu_b = gpu_closest(acc, bounce)
+    compare_closest(ora_b, gpu_b)
+    shadow = scenes.shadow_rays(bounce, (0.0, 80.0, -60.0))
+    assert np.array_equal(gpu_visibility(acc, shadow), S.cast_visibility(shadow))
+    st = acc.stats()
+    assert st["blasTriangles"] == 1310720 and st["instances"] == 64
