@@ -351,6 +351,8 @@ mrg_status mrg_build(mrg_ctx* c)
     c->scene.tlasLeaf = c->dTlasLeaf;
     c->scene.tlasRoot = (uint32_t)tlasOff;
     c->scene.instCount = ni;
+    c->scene.nodeCount = (uint32_t)totalNodes;
+    c->scene.triCount = (uint32_t)totalTris;
     c->built = true;
     c->buildMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return MRG_OK;
@@ -452,7 +454,8 @@ mrg_status mrg_sync_status(mrg_ctx* c, void* stream)
     {
         MRG_TRY(cudaMemset(c->dScratch + 1, 0, sizeof(uint32_t)), "mrg_sync_status: clear flag");
         return fail(MRG_ERR_TRAVERSAL, (flag & mrg::kTraceStackOverflow) ? "traversal stack overflow"
-                                                                         : "traversal step cap reached");
+                                       : (flag & mrg::kTraceBadIndex) ? "traversal read an out-of-range index"
+                                                                      : "traversal step cap reached");
     }
     return MRG_OK;
 }

@@ -182,17 +182,25 @@ __global__ void k_karras(const uint64_t* __restrict__ codes, int n, BinNode* __r
 // thread's node box load through L2 (__ldcg) since L1 is not coherent.
 __global__ void k_bottom_up(const uint32_t* __restrict__ leafParent, const uint32_t* __restrict__ sortedIds,
                             const BoxF* __restrict__ leafBoxes, BinNode* nodes, BoxF* nodeBoxes,
-                            uint32_t* counters, int n)
+                            uint32_t* counters, int n, uint32_t* errorFlag)
 {
     int li = blockIdx.x * blockDim.x + threadIdx.x;
     if(li >= n) return;
+    const uint32_t nInt = (uint32_t)(n - 1);
     uint32_t p = leafParent[li];
-    while(p != kNoParent)
+    for(int guard = 0; p != kNoParent; guard++)
     {
+        if(p >= nInt || guard > n) { atomicOr(errorFlag, 1u); return; }
         uint32_t old = atomicAdd(&counters[p], 1u);
         if(old == 0) return;
         __threadfence();
         uint32_t ch[2] = { __ldcg(&nodes[p].left), __ldcg(&nodes[p].right) };
+        for(int c = 0; c < 2; c++)
+        {
+            const bool leaf = (ch[c] & kLeafBit) != 0u;
+            const uint32_t ix = ch[c] & ~kLeafBit;
+            if((leaf && ix >= (uint32_t)n) || (!leaf && ix >= nInt)) { atomicOr(errorFlag, 1u); return; }
+        }
         BoxF b;
         uint32_t cnt = 0;
         for(int k = 0; k < 3; k++) { b.mn[k] = FLT_MAX; b.mx[k] = -FLT_MAX; }
@@ -236,13 +244,32 @@ struct CollapseArgs
     WideNode*       wnodes;
     TriRecord*      tris;
     uint32_t*       leafIds;
-    uint32_t*       counters;   // [0] nodes, [1] leaf payloads, [2] next-queue size
+    uint32_t*       counters;   // [0] nodes, [1] leaf payloads, [2] next-queue size, [3] error
+    uint32_t        leafCount;  // leaves (payload capacity)
+    uint32_t        wideCap;    // wide node / queue capacity
 };
+
+// Child references are validated before every dereference: a malformed tree
+// sets counters[3] and yields an empty box instead of an out-of-range read.
+__device__ __forceinline__ bool ref_ok(const CollapseArgs& a, uint32_t ref)
+{
+    const bool ok = (ref & kLeafBit) ? ((ref & ~kLeafBit) < a.leafCount)
+                                     : (ref < (a.leafCount > 1 ? a.leafCount - 1 : 1));
+    if(!ok) atomicOr(&a.counters[3], 1u);
+    return ok;
+}
 
 __device__ __forceinline__ void ref_box(const CollapseArgs& a, uint32_t ref, BoxF& b, uint32_t& cnt)
 {
+    if(!ref_ok(a, ref))
+    {
+        for(int k = 0; k < 3; k++) { b.mn[k] = 0.0f; b.mx[k] = 0.0f; }
+        cnt = 1;
+        return;
+    }
     if(ref & kLeafBit) { b = a.leafBoxes[a.sortedIds[ref & ~kLeafBit]]; cnt = 1; }
     else { b = a.nodeBoxes[ref]; cnt = a.nodes[ref].leafCount; }
+    if(cnt == 0u || cnt > a.leafCount) { atomicOr(&a.counters[3], 1u); cnt = 1; }
 }
 
 __device__ __forceinline__ float half_area(const BoxF& b)
@@ -301,7 +328,7 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
                 float ar = half_area(cbox[c]);
                 if(ar > bestA) { bestA = ar; best = c; }
             }
-            if(best < 0) break;
+            if(best < 0 || !ref_ok(a, cand[best])) break;
             const BinNode& on = a.nodes[cand[best]];
             cand[best] = on.left;  ref_box(a, on.left, cbox[best], ccnt[best]);
             cand[nc] = on.right;   ref_box(a, on.right, cbox[nc], ccnt[nc]);
@@ -369,6 +396,12 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
     uint32_t childBase = numInternal ? atomicAdd(&a.counters[0], numInternal) : 0u;
     uint32_t triBase = numPayload ? atomicAdd(&a.counters[1], numPayload) : 0u;
     uint32_t qBase = numInternal ? atomicAdd(&a.counters[2], numInternal) : 0u;
+    if(childBase + numInternal > a.wideCap || qBase + numInternal > a.wideCap ||
+       triBase + numPayload > a.leafCount || wideIdx >= a.wideCap)
+    {
+        atomicOr(&a.counters[3], 2u);
+        return;
+    }
 
     uint8_t meta[8], qlo[3][8], qhi[3][8];
     uint32_t imask = 0;
@@ -409,8 +442,15 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
             while(sp > 0)
             {
                 uint32_t r = stack[--sp];
-                if(r & kLeafBit) { emit_payload(a, r & ~kLeafBit, triBase + triOff + m); m++; }
-                else { stack[sp++] = a.nodes[r].right; stack[sp++] = a.nodes[r].left; }
+                if(!ref_ok(a, r)) continue;
+                if(r & kLeafBit)
+                {
+                    if(m < k) emit_payload(a, r & ~kLeafBit, triBase + triOff + m);
+                    else atomicOr(&a.counters[3], 4u);
+                    m++;
+                }
+                else if(sp + 2 <= 8) { stack[sp++] = a.nodes[r].right; stack[sp++] = a.nodes[r].left; }
+                else atomicOr(&a.counters[3], 4u);
             }
             triOff += k;
         }
@@ -472,7 +512,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     const uint32_t nInt = (n > 1) ? (n - 1) : 1;
     const uint32_t wideCap = n;      // each wide node consumes >= 1 binary node
     uint32_t cbInit[6] = { 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u };
-    uint32_t hostCounters[3];
+    uint32_t hostCounters[4];
     BoxF rootBox;
     cub::DoubleBuffer<uint64_t> kb;
     cub::DoubleBuffer<uint32_t> vb;
@@ -495,7 +535,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     MRG_CK(cudaMallocAsync(&dCnt, sizeof(uint32_t) * nInt, st));
     MRG_CK(cudaMallocAsync(&dQ[0], sizeof(uint2) * wideCap, st));
     MRG_CK(cudaMallocAsync(&dQ[1], sizeof(uint2) * wideCap, st));
-    MRG_CK(cudaMallocAsync(&dCounters, sizeof(uint32_t) * 3, st));
+    MRG_CK(cudaMallocAsync(&dCounters, sizeof(uint32_t) * 4, st));
     MRG_CK(cudaMallocAsync(&dW, sizeof(WideNode) * wideCap, st));
     if(in.kind == 0) MRG_CK(cudaMallocAsync(&out.tris, sizeof(TriRecord) * n, st));
     else             MRG_CK(cudaMallocAsync(&out.leafIds, sizeof(uint32_t) * n, st));
@@ -519,11 +559,13 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     if(n > 1)
     {
         MRG_CK(cudaMemsetAsync(dNodes, 0xFF, sizeof(BinNode) * nInt, st));
+        MRG_CK(cudaMemsetAsync(dLeafParent, 0xFF, sizeof(uint32_t) * n, st));
         k_karras<<<gridFor(n - 1), kTPB, 0, st>>>(kb.Current(), (int)n, dNodes, dLeafParent);
         MRG_CK(cudaGetLastError());
         MRG_CK(cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * nInt, st));
+        MRG_CK(cudaMemsetAsync(dCounters, 0, sizeof(uint32_t) * 4, st));
         k_bottom_up<<<gridFor(n), kTPB, 0, st>>>(dLeafParent, vb.Current(), dLeafBoxes, dNodes,
-                                                 dNodeBoxes, dCnt, (int)n);
+                                                 dNodeBoxes, dCnt, (int)n, dCounters + 3);
         MRG_CK(cudaGetLastError());
         MRG_CK(cudaMemcpyAsync(&rootBox, dNodeBoxes, sizeof(BoxF), cudaMemcpyDeviceToHost, st));
         rootItem = make_uint2(0u, 0u);
@@ -533,7 +575,9 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
         MRG_CK(cudaMemcpyAsync(&rootBox, dLeafBoxes, sizeof(BoxF), cudaMemcpyDeviceToHost, st));
         rootItem = make_uint2(kLeafBit | 0u, 0u);
     }
+    MRG_CK(cudaMemcpyAsync(hostCounters, dCounters, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st));
     MRG_CK(cudaStreamSynchronize(st));
+    if(n > 1 && hostCounters[3] != 0) { err = "binary tree construction produced an invalid node"; goto fail; }
     for(int k = 0; k < 3; k++) { out.box[k] = rootBox.mn[k]; out.box[3 + k] = rootBox.mx[k]; }
 
     ext = 0.0f;
@@ -550,8 +594,9 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     ca.primKeyBase = in.primKeyBase; ca.kind = in.kind; ca.maxLeaf = in.maxLeaf;
     ca.inflate = ext * 1.0e-5f + 1.0e-30f;
     ca.wnodes = dW; ca.tris = out.tris; ca.leafIds = out.leafIds; ca.counters = dCounters;
+    ca.leafCount = n; ca.wideCap = wideCap;
 
-    hostCounters[0] = 1; hostCounters[1] = 0; hostCounters[2] = 0;
+    hostCounters[0] = 1; hostCounters[1] = 0; hostCounters[2] = 0; hostCounters[3] = 0;
     MRG_CK(cudaMemcpyAsync(dCounters, hostCounters, sizeof(hostCounters), cudaMemcpyHostToDevice, st));
     MRG_CK(cudaMemcpyAsync(dQ[0], &rootItem, sizeof(uint2), cudaMemcpyHostToDevice, st));
     for(int level = 0; qn > 0; level++)
@@ -562,6 +607,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
         MRG_CK(cudaGetLastError());
         MRG_CK(cudaMemcpyAsync(hostCounters, dCounters, sizeof(hostCounters), cudaMemcpyDeviceToHost, st));
         MRG_CK(cudaStreamSynchronize(st));
+        if(hostCounters[3] != 0) { err = "wide BVH collapse reported an invalid tree"; goto fail; }
         if(hostCounters[0] > wideCap) { err = "wide node capacity exceeded"; goto fail; }
         qn = hostCounters[2];
         cur ^= 1;

@@ -44,6 +44,8 @@ struct TraceScene
     const uint32_t*   tlasLeaf = nullptr;  // instance id per TLAS payload slot
     uint32_t          tlasRoot = 0;
     uint32_t          instCount = 0;
+    uint32_t          nodeCount = 0;       // bounds for every index read from the tree
+    uint32_t          triCount = 0;
 };
 
 struct TraceScratch
@@ -56,7 +58,8 @@ struct TraceScratch
 enum TraceErrorBits : uint32_t
 {
     kTraceStackOverflow = 1u,
-    kTraceStepCap       = 2u
+    kTraceStepCap       = 2u,
+    kTraceBadIndex      = 4u
 };
 
 cudaError_t launch_closest(const TraceScene& sc, const TraceScratch& scr, void* rays,

@@ -169,6 +169,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     ng.y &= ~(1u << bit);
                     const uint32_t rank = __popc((ng.y & 0xFFu) & ((1u << slot) - 1u));
                     const uint32_t ni = ng.x + rank;
+                    if(ni >= sc.nodeCount) { atomicOr(scr.errorFlag, kTraceBadIndex); break; }
                     if(ng.y > 0x00FFFFFFu)
                     {
                         if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); break; }
@@ -194,6 +195,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     const uint32_t pi = tg.x + b;
                     if(blasBase >= 0)
                     {
+                        if(pi >= sc.triCount) { atomicOr(scr.errorFlag, kTraceBadIndex); stop = true; break; }
                         const float4* tp = reinterpret_cast<const float4*>(sc.tris + pi);
                         const float4 v0 = __ldg(tp), e0 = __ldg(tp + 1), e1 = __ldg(tp + 2);
                         if(STATS) statTris++;
@@ -209,7 +211,9 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     }
                     else
                     {
+                        if(pi >= sc.instCount) { atomicOr(scr.errorFlag, kTraceBadIndex); stop = true; break; }
                         const uint32_t inst = __ldg(sc.tlasLeaf + pi);
+                        if(inst >= sc.instCount) { atomicOr(scr.errorFlag, kTraceBadIndex); stop = true; break; }
                         if(ng.y > 0x00FFFFFFu)
                         {
                             if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); stop = true; break; }
