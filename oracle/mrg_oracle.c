@@ -716,7 +716,7 @@ static int scene_cast(const orc_scene* s, const orc_ray_gmem* r, int anyHit, sce
                 continue;
             float ld[3], lp[3];
             orc_transform_ray(in->inv, r->dir, r->pos, ld, lp);
-            blas_hit h;
+            blas_hit h; memset(&h, 0, sizeof(h));
             if(blas_traverse(&s->meshes[in->mesh], in->cull, ld, lp, tmm, anyHit, &h))
             {
                 out->hit = 1; out->t = h.t; out->prim = h.prim; out->inst = ii;
