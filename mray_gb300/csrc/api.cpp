@@ -20,8 +20,10 @@ struct HostInstRecord
 {
     float    inv[12];
     uint32_t keys[4];
+    float    wmin[4];
+    float    wmax[4];
 };
-static_assert(sizeof(HostInstRecord) == 64, "instance record is 64 bytes");
+static_assert(sizeof(HostInstRecord) == 96, "instance record is 96 bytes");
 constexpr size_t kWideNodeBytes = 80;
 constexpr size_t kTriRecordBytes = 48;
 
@@ -334,6 +336,10 @@ mrg_status mrg_build(mrg_ctx* c)
         recs[i].keys[2] = in.accel;
         recs[i].keys[3] = c->meshes[in.mesh].rootNode |
                           ((in.flags & MRG_INSTANCE_CULL_BACKFACE) ? 0x80000000u : 0u);
+        float wb[6];
+        mrg::transform_box_exact(in.m, c->meshes[in.mesh].box, wb);
+        for(int k = 0; k < 3; k++) { recs[i].wmin[k] = wb[k]; recs[i].wmax[k] = wb[3 + k]; }
+        recs[i].wmin[3] = 0.0f; recs[i].wmax[3] = 0.0f;
     }
     if(e == cudaSuccess)
         e = cudaMemcpyAsync(c->dInsts, recs.data(), sizeof(mrg::HostInstRecord) * ni, cudaMemcpyHostToDevice, st);

@@ -70,4 +70,25 @@ void transform_box_conservative(const float m[12], const float box[6], float out
     }
 }
 
+// Matrix3x4::TransformAABB (Source/Core/Matrix.hpp:915-931): each corner
+// (w = 1) through the 4-term fma Dot per row, std::min/std::max accumulation.
+void transform_box_exact(const float m[12], const float box[6], float out[6])
+{
+    float rmin[3] = { INFINITY, INFINITY, INFINITY };
+    float rmax[3] = { -INFINITY, -INFINITY, -INFINITY };
+    for(unsigned c = 0; c < 8; c++)
+    {
+        const float v[4] = { (c & 1u) ? box[3] : box[0], (c & 2u) ? box[4] : box[1],
+                             (c & 4u) ? box[5] : box[2], 1.0f };
+        for(int r = 0; r < 3; r++)
+        {
+            float acc = 0.0f;
+            for(int k = 0; k < 4; k++) acc = std::fma(m[4 * r + k], v[k], acc);
+            rmax[r] = (rmax[r] < acc) ? acc : rmax[r];
+            rmin[r] = (acc < rmin[r]) ? acc : rmin[r];
+        }
+    }
+    for(int r = 0; r < 3; r++) { out[r] = rmin[r]; out[3 + r] = rmax[r]; }
+}
+
 } // namespace mrg

@@ -7,7 +7,7 @@
 //                        e0/e1 are the exact float differences MRay's
 //                        Moller-Trumbore forms first (Source/Core/Ray.hpp:131-132),
 //                        so storing them keeps the test bit-identical.
-//   InstRecord insts[]   64 B each: inverse 3x4 transform rows + keys.
+//   InstRecord insts[]   96 B each: inverse 3x4 transform rows, keys, exact world AABB.
 //   uint32    tlasLeaf[] instance index per TLAS leaf slot.
 #pragma once
 #include <cstdint>
@@ -38,8 +38,10 @@ struct __align__(16) InstRecord
 {
     float4 inv[3];   // rows of the world->local 3x4 matrix
     uint4  keys;     // lightOrMatKey, transKey, accelKey, blasRoot | cull<<31
+    float4 wmin;     // exact world AABB (Matrix3x4::TransformAABB of the BLAS box), w unused
+    float4 wmax;
 };
-static_assert(sizeof(InstRecord) == 64, "instance record must be 64 bytes");
+static_assert(sizeof(InstRecord) == 96, "instance record must be 96 bytes");
 
 constexpr uint32_t kCullBit = 0x80000000u;
 constexpr uint32_t kInvalidIndex = 0xFFFFFFFFu;
@@ -121,6 +123,35 @@ __device__ __forceinline__ void transform_ray_exact(const float4 r0, const float
     lo.x = dot4w1_exact(r0, o.x, o.y, o.z);
     lo.y = dot4w1_exact(r1, o.x, o.y, o.z);
     lo.z = dot4w1_exact(r2, o.x, o.y, o.z);
+}
+
+// std::max / std::min as the reference host build evaluates them
+// (Source/Core/Math.h:342-380): the first argument wins unless the compare holds.
+__device__ __forceinline__ float std_max(float x, float y) { return (x < y) ? y : x; }
+__device__ __forceinline__ float std_min(float x, float y) { return (y < x) ? y : x; }
+
+// Ray::IntersectsAABB (Source/Core/Ray.hpp:192-219), bit-exact: the decision
+// MRay takes at every TLAS leaf (AcceleratorLBVH.cu:465-473).
+__device__ __forceinline__ bool intersect_aabb_exact(float ox, float oy, float oz,
+                                                     float dx, float dy, float dz,
+                                                     const float4& bmin, const float4& bmax,
+                                                     float tmin, float tmax)
+{
+    const float id[3] = { __fdiv_rn(1.0f, dx), __fdiv_rn(1.0f, dy), __fdiv_rn(1.0f, dz) };
+    const float o[3] = { ox, oy, oz };
+    const float lo[3] = { bmin.x, bmin.y, bmin.z };
+    const float hi[3] = { bmax.x, bmax.y, bmax.z };
+    float o0 = tmin, o1 = tmax;
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+    {
+        float t0 = __fmul_rn(__fsub_rn(lo[i], o[i]), id[i]);
+        float t1 = __fmul_rn(__fsub_rn(hi[i], o[i]), id[i]);
+        if(id[i] < 0.0f) { float s = t0; t0 = t1; t1 = s; }
+        o0 = std_max(o0, std_min(t0, t1));
+        o1 = std_min(o1, std_max(t0, t1));
+    }
+    return o1 >= o0;
 }
 
 } // namespace mrg

@@ -214,6 +214,12 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                         if(pi >= sc.instCount) { atomicOr(scr.errorFlag, kTraceBadIndex); stop = true; break; }
                         const uint32_t inst = __ldg(sc.tlasLeaf + pi);
                         if(inst >= sc.instCount) { atomicOr(scr.errorFlag, kTraceBadIndex); stop = true; break; }
+                        const float4* ip = reinterpret_cast<const float4*>(sc.insts + inst);
+                        // MRay's own leaf test decides whether the instance is entered
+                        // (the wide TLAS boxes above are conservative and only cull).
+                        if(!intersect_aabb_exact(wox, woy, woz, wdx, wdy, wdz, __ldg(ip + 4), __ldg(ip + 5),
+                                                 tmin, tmax))
+                            continue;
                         if(ng.y > 0x00FFFFFFu)
                         {
                             if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); stop = true; break; }
@@ -225,7 +231,6 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                             stack[sp++] = tg;
                         }
                         blasBase = sp;
-                        const float4* ip = reinterpret_cast<const float4*>(sc.insts + inst);
                         const float4 m0 = __ldg(ip), m1 = __ldg(ip + 1), m2 = __ldg(ip + 2);
                         const uint4 keys = __ldg(reinterpret_cast<const uint4*>(ip + 3));
                         transform_ray_exact(m0, m1, m2, make_float3(wox, woy, woz),
