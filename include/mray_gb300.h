@@ -148,6 +148,26 @@ mrg_status mrg_cast_visibility(mrg_ctx* ctx, uint32_t* d_visible_bits,
 mrg_status mrg_cast_closest_host(mrg_ctx* ctx, mrg_ray* h_rays, uint32_t n,
                                  mrg_hit_keys* h_hits, mrg_meta_hit* h_meta);
 
+/* Closest hit on HOST buffers without any device allocation.  No
+ * counterpart in the reference.  For callers that cannot call cudaMalloc
+ * when they cast (an application whose own allocator owns all device memory,
+ * or a real-time / plugin thread that may not grow the device heap): the
+ * device staging for rays, hit keys and meta hits plus the kernel's work
+ * counter and error flag live in one static __device__ array of the library
+ * (about 14 MiB, held by every GPU that loads the library until exit).  It
+ * calls no cudaMalloc / cudaFree and nothing that allocates.
+ *  - n must be <= MRG_NOALLOC_MAX_RAYS, otherwise MRG_ERR_LIMIT;
+ *  - the first call on a device looks up the array's device address (once
+ *    per device, with that device current); make that first call before any
+ *    stream capture;
+ *  - every call shares the one array and leaves its contents behind, so calls
+ *    that overlap on the GPU (other threads, other contexts on the same
+ *    device) race: serialise them.
+ * Same semantics and results as mrg_cast_closest_host; synchronous. */
+#define MRG_NOALLOC_MAX_RAYS 262144u
+mrg_status mrg_cast_closest_host_noalloc(mrg_ctx* ctx, mrg_ray* h_rays, uint32_t n,
+                                         mrg_hit_keys* h_hits, mrg_meta_hit* h_meta);
+
 /* World-space AABB of the scene (BaseAcceleratorI::SceneAABB,
  * Source/Tracer/AcceleratorC.h:416): min xyz, max xyz. */
 mrg_status mrg_scene_aabb(mrg_ctx* ctx, float out_minmax[6]);

@@ -27,8 +27,11 @@ EXPORTED = [
     "mrg_create", "mrg_destroy", "mrg_last_error", "mrg_status_string",
     "mrg_upload_mesh", "mrg_add_instance", "mrg_build", "mrg_cast_closest",
     "mrg_cast_visibility", "mrg_cast_closest_host", "mrg_scene_aabb", "mrg_get_stats",
-    "mrg_sync_status", "mrg_cast_closest_stats",
+    "mrg_sync_status", "mrg_cast_closest_stats", "mrg_cast_closest_host_noalloc",
 ]
+
+#: capacity of mrg_cast_closest_host_noalloc (rays per call)
+MRG_NOALLOC_MAX_RAYS = 262144
 
 
 class MrgParams(C.Structure):
@@ -68,6 +71,7 @@ def _declare(lib):
         "mrg_cast_closest": (C.c_int, [vp, vp, vp, u32, vp, vp, vp]),
         "mrg_cast_visibility": (C.c_int, [vp, vp, vp, vp, u32, vp]),
         "mrg_cast_closest_host": (C.c_int, [vp, vp, u32, vp, vp]),
+        "mrg_cast_closest_host_noalloc": (C.c_int, [vp, vp, u32, vp, vp]),
         "mrg_scene_aabb": (C.c_int, [vp, fp]),
         "mrg_get_stats": (C.c_int, [vp, C.POINTER(MrgAccelStats)]),
         "mrg_sync_status": (C.c_int, [vp, vp]),

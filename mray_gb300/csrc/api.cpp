@@ -1,7 +1,6 @@
 // api.cpp -- the C ABI (include/mray_gb300.h): context, scene upload, build,
 // casts.  Host C++ over the CUDA runtime; no exceptions cross the boundary.
-#include "mray_gb300.h"
-#include "mrg_build.h"
+#include "mrg_ctx.h"
 #include "host_math.h"
 
 #include <cuda_runtime.h>
@@ -13,68 +12,6 @@
 #include <string>
 #include <vector>
 
-namespace mrg {
-
-// Device-side record layouts, mirrored on the host for uploads.
-struct HostInstRecord
-{
-    float    inv[12];
-    uint32_t keys[4];
-    float    wmin[4];
-    float    wmax[4];
-};
-static_assert(sizeof(HostInstRecord) == 96, "instance record is 96 bytes");
-constexpr size_t kWideNodeBytes = 80;
-constexpr size_t kTriRecordBytes = 48;
-
-} // namespace mrg
-
-struct mrg_ctx
-{
-    int device = 0;
-    int smCount = 0;
-    cudaStream_t buildStream = nullptr;
-
-    struct Mesh
-    {
-        std::vector<float>    pos;
-        std::vector<uint32_t> idx;
-        uint32_t              primKeyBase = 0;
-        float                 box[6] = { 0, 0, 0, 0, 0, 0 };
-        uint32_t              rootNode = 0;
-    };
-    struct Inst
-    {
-        uint32_t mesh = 0;
-        float    m[12];
-        float    inv[12];
-        uint32_t flags = 0, lm = 0, trans = 0, accel = 0;
-    };
-    std::vector<Mesh> meshes;
-    std::vector<Inst> insts;
-    bool built = false;
-
-    // accelerator (device)
-    void*     dNodes = nullptr;
-    void*     dTris = nullptr;
-    void*     dInsts = nullptr;
-    uint32_t* dTlasLeaf = nullptr;
-    uint64_t  blasNodes = 0, blasTris = 0, tlasNodes = 0;
-    mrg::TraceScene scene;
-    float     sceneBox[6] = { 0, 0, 0, 0, 0, 0 };
-    double    buildMs = 0.0;
-
-    // scratch: [0] work counter, [1] error flag; stats in a separate block
-    uint32_t*           dScratch = nullptr;
-    unsigned long long* dStats = nullptr;
-
-    // staging for the host-buffer cast
-    mrg_ray*      dStageRays = nullptr;
-    mrg_hit_keys* dStageHits = nullptr;
-    mrg_meta_hit* dStageMeta = nullptr;
-    size_t        stageCap = 0;
-};
-
 namespace {
 
 thread_local std::string g_lastError;
@@ -84,6 +21,15 @@ mrg_status fail(mrg_status s, const std::string& msg)
     g_lastError = msg;
     return s;
 }
+
+} // namespace
+
+mrg_status mrg::set_error(mrg_status s, const std::string& msg)
+{
+    return fail(s, msg);
+}
+
+namespace {
 
 mrg_status cuda_fail(cudaError_t e, const char* what)
 {
