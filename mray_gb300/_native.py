@@ -8,7 +8,8 @@ import ctypes as C
 import os
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_PKG, "libmray_gb300.so")
+# MRAY_GB300_LIB selects another build of the library (e.g. a tuning variant).
+LIB_PATH = os.environ.get("MRAY_GB300_LIB") or os.path.join(_PKG, "libmray_gb300.so")
 SCENES_PATH = os.path.join(_PKG, "libmrg_scenes.so")
 
 MRG_OK = 0

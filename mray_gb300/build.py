@@ -63,26 +63,33 @@ def build_scenes(force=False, verbose=False):
     return SCENES_LIB
 
 
-def build(force=False, verbose=False, ptxas_verbose=False):
+def build(force=False, verbose=False, ptxas_verbose=False, defines=None, lib_path=None,
+          obj_dir=None):
+    """Builds the library.  ``defines`` (e.g. ``{"MRG_TRACE_STEP_BUDGET": 8}``)
+    override the kernels' compile-time tuning knobs; ``lib_path`` / ``obj_dir``
+    place such a variant elsewhere (the default library is untouched)."""
     build_scenes(force=force, verbose=verbose)
+    lib_out = lib_path or LIB
+    obj = obj_dir or OBJ
+    dflags = ["-D%s=%s" % (k, v) for k, v in sorted((defines or {}).items())]
     cu, cpp, hdr = _sources()
     srcs = [os.path.join(CSRC, f) for f in cu + cpp]
     newest = max(os.path.getmtime(p) for p in srcs + hdr + [__file__])
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
-        return LIB
+    if not force and os.path.exists(lib_out) and os.path.getmtime(lib_out) >= newest:
+        return lib_out
     home = cuda_home()
     nvcc = os.path.join(home, "bin", "nvcc")
-    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(obj, exist_ok=True)
     jobs = []
     for f in cu:
-        o = os.path.join(OBJ, f + ".o")
-        cmd = [nvcc] + GENCODE + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+        o = os.path.join(obj, f + ".o")
+        cmd = [nvcc] + GENCODE + dflags + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                                   "-I", CSRC, "-I", INCLUDE, "-c", os.path.join(CSRC, f), "-o", o]
         if ptxas_verbose:
             cmd += ["-Xptxas", "-v"]
         jobs.append((cmd, o))
     for f in cpp:
-        o = os.path.join(OBJ, f + ".o")
+        o = os.path.join(obj, f + ".o")
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
                "-I", CSRC, "-I", INCLUDE, "-I", os.path.join(home, "include"),
                "-c", os.path.join(CSRC, f), "-o", o]
@@ -92,13 +99,13 @@ def build(force=False, verbose=False, ptxas_verbose=False):
         futs = [ex.submit(_compile, cmd, verbose) for cmd, _ in jobs]
         for fu in futs:
             logs.append(fu.result())
-    tmp = LIB + ".tmp%d" % os.getpid()
+    tmp = lib_out + ".tmp%d" % os.getpid()
     link = [nvcc] + GENCODE + ["-shared", "-cudart", "static", "-o", tmp] + [o for _, o in jobs]
     _compile(link, verbose)
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib_out)
     if ptxas_verbose:
         sys.stderr.write("".join(logs))
-    return LIB
+    return lib_out
 
 
 if __name__ == "__main__":

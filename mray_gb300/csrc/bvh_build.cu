@@ -336,7 +336,11 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
         }
     }
 
-    // Quantisation frame: p = inflated min, 2^e * 255 >= inflated extent.
+    // Quantisation frame.  Children are stored one quantum wider on each side
+    // than their outward-rounded box (the traversal evaluates planes with a
+    // 2^23-biased byte, whose offset term can be off by half a quantum), so
+    // the frame reserves a quantum below and above: 2^e * 252 >= extent and
+    // p = inflated min - 2^e.  Every stored child then lies in [0, 255].
     float px[3];
     uint32_t eb[3];
     float invS[3];
@@ -345,7 +349,7 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
         float lo = __fsub_rd(nbox.mn[k], a.inflate);
         float hi = __fadd_ru(nbox.mx[k], a.inflate);
         float ext = __fsub_ru(hi, lo);
-        float x = __fdiv_ru(ext, 255.0f);
+        float x = __fdiv_ru(ext, 252.0f);
         uint32_t bits = __float_as_uint(x);
         int ex = (int)((bits >> 23) & 0xFF);
         int e;
@@ -353,7 +357,7 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
         else e = ex - 127 + (((bits & 0x7FFFFFu) != 0u) ? 1 : 0);
         e = max(-126, min(e, 126));
         eb[k] = (uint32_t)(e + 127);
-        px[k] = lo;
+        px[k] = __fsub_rd(lo, __uint_as_float((uint32_t)(e + 127) << 23));
         invS[k] = __uint_as_float((uint32_t)(127 - e) << 23);
     }
 
@@ -419,8 +423,8 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
         {
             float lo = __fsub_rd(cbox[c].mn[k], a.inflate);
             float hi = __fadd_ru(cbox[c].mx[k], a.inflate);
-            float ql = floorf(__fmul_rd(__fsub_rd(lo, px[k]), invS[k]));
-            float qh = ceilf(__fmul_ru(__fsub_ru(hi, px[k]), invS[k]));
+            float ql = floorf(__fmul_rd(__fsub_rd(lo, px[k]), invS[k])) - 1.0f;
+            float qh = ceilf(__fmul_ru(__fsub_ru(hi, px[k]), invS[k])) + 1.0f;
             qlo[k][s] = (uint8_t)fminf(fmaxf(ql, 0.0f), 255.0f);
             qhi[k][s] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
         }
