@@ -131,13 +131,15 @@ __device__ __forceinline__ float std_max(float x, float y) { return (x < y) ? y 
 __device__ __forceinline__ float std_min(float x, float y) { return (y < x) ? y : x; }
 
 // Ray::IntersectsAABB (Source/Core/Ray.hpp:192-219), bit-exact: the decision
-// MRay takes at every TLAS leaf (AcceleratorLBVH.cu:465-473).
+// MRay takes at every TLAS leaf (AcceleratorLBVH.cu:465-473).  ix/iy/iz are
+// the IEEE reciprocals of the direction, 1 / dir (__frcp_rn gives exactly the
+// correctly rounded quotient), computed once per ray by the caller.
 __device__ __forceinline__ bool intersect_aabb_exact(float ox, float oy, float oz,
-                                                     float dx, float dy, float dz,
+                                                     float ix, float iy, float iz,
                                                      const float4& bmin, const float4& bmax,
                                                      float tmin, float tmax)
 {
-    const float id[3] = { __fdiv_rn(1.0f, dx), __fdiv_rn(1.0f, dy), __fdiv_rn(1.0f, dz) };
+    const float id[3] = { ix, iy, iz };
     const float o[3] = { ox, oy, oz };
     const float lo[3] = { bmin.x, bmin.y, bmin.z };
     const float hi[3] = { bmax.x, bmax.y, bmax.z };

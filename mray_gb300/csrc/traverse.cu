@@ -23,7 +23,7 @@ namespace {
 
 // Tuning knobs (compile-time; the defaults are the measured best on GB300).
 #ifndef MRG_TRACE_MIN_BLOCKS
-#define MRG_TRACE_MIN_BLOCKS 6       // resident 128-thread blocks per SM the register budget targets
+#define MRG_TRACE_MIN_BLOCKS 8       // resident 128-thread blocks per SM the register budget targets
 #endif
 #ifndef MRG_TRACE_REFILL
 #define MRG_TRACE_REFILL 8           // refill when at least this many lanes are idle
@@ -31,8 +31,11 @@ namespace {
 #ifndef MRG_TRACE_STEP_BUDGET
 #define MRG_TRACE_STEP_BUDGET 16     // traversal iterations between refill checks
 #endif
+#ifndef MRG_TRACE_PREFETCH
+#define MRG_TRACE_PREFETCH 1         // L1 prefetch of the next node
+#endif
 #ifndef MRG_TRACE_POSTPONE
-#define MRG_TRACE_POSTPONE 6         // postpone triangles when fewer lanes want them
+#define MRG_TRACE_POSTPONE 0         // postpone triangles when fewer lanes want them
 #endif
 
 constexpr int kTraceTPB = 128;
@@ -50,10 +53,14 @@ struct LevelRay
     uint32_t octRep;    // oct7 replicated into 4 bytes
 };
 
+// Inverse direction for the quantised box tests.  A fast reciprocal is
+// enough: its one-ulp error scales each axis' plane distances by 1 +- 2^-23,
+// far inside the boxes' inflation (1e-5 of the accelerator extent plus one
+// quantum).  Tiny components are clamped so the planes stay finite.
 __device__ __forceinline__ float guard_inv(float d)
 {
     float a = (fabsf(d) > 1.0e-20f) ? d : copysignf(1.0e-20f, d);
-    return 1.0f / a;
+    return __fdividef(1.0f, a);
 }
 
 __device__ __forceinline__ void setup_level(LevelRay& r, float ox, float oy, float oz,
@@ -145,12 +152,9 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
             const float tfz = fmaf(qbias(farZ, k), sz, az);
             const float tn = fmaxf(max3f(tnx, tny, tnz), tmin);
             const float tf = fminf(min3f(tfx, tfy, tfz), tmax);
-            if(tn <= tf)
-            {
-                const uint32_t cb = (bits4 >> (8u * k)) & 0xFFu;
-                const uint32_t bi = (bitIdx4 >> (8u * k)) & 0xFFu;
-                hm |= cb << bi;
-            }
+            const uint32_t cb = (bits4 >> (8u * k)) & 0xFFu;
+            const uint32_t bi = (bitIdx4 >> (8u * k)) & 0xFFu;
+            hm |= (tn <= tf) ? (cb << bi) : 0u;
         }
     }
     return hm;
@@ -170,6 +174,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
     bool live = false;
     uint32_t ri = 0;
     float wox = 0, woy = 0, woz = 0, wdx = 0, wdy = 0, wdz = 0, tmin = 0, tmax = 0;
+    float wix = 0, wiy = 0, wiz = 0;   // IEEE 1/dir of the world ray (exact leaf slab test)
     LevelRay lr;
     float3 lo = make_float3(0, 0, 0), ld = make_float3(0, 0, 0);
     uint2 ng = make_uint2(0, 0), tg = make_uint2(0, 0);
@@ -203,6 +208,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     const float4 r1 = rays[2 * (size_t)ri + 1];
                     wox = r0.x; woy = r0.y; woz = r0.z; tmin = r0.w;
                     wdx = r1.x; wdy = r1.y; wdz = r1.z; tmax = r1.w;
+                    wix = __frcp_rn(wdx); wiy = __frcp_rn(wdy); wiz = __frcp_rn(wdz);
                     setup_level(lr, wox, woy, woz, wdx, wdy, wdz);
                     ng = make_uint2(sc.tlasRoot, (1u << (24u + lr.oct7)) | 1u);
                     tg = make_uint2(0u, 0u);
@@ -240,6 +246,20 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                 if(STATS) statNodes++;
                 ng = make_uint2(cb, (hm & 0xFF000000u) ? ((hm & 0xFF000000u) | im) : 0u);
                 tg = make_uint2(tb, hm & 0x00FFFFFFu);
+                if(MRG_TRACE_PREFETCH && ng.y)
+                {
+                    // The nearest hit child is visited next: start its fetch now
+                    // so the triangle work below overlaps the L2 latency.
+                    const uint32_t nb = 31u - __clz(ng.y);
+                    const uint32_t nslot = (nb - 24u) ^ lr.oct7;
+                    const uint32_t nni = cb + __popc(im & ((1u << nslot) - 1u));
+                    if(nni < sc.nodeCount)
+                    {
+                        const char* np = reinterpret_cast<const char*>(sc.nodes + nni);
+                        asm volatile("prefetch.global.L1 [%0];" :: "l"(np));
+                        asm volatile("prefetch.global.L1 [%0];" :: "l"(np + 64));
+                    }
+                }
             }
             else
             {
@@ -293,7 +313,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     const float4* ip = reinterpret_cast<const float4*>(sc.insts + inst);
                     // MRay's own leaf test decides whether the instance is entered
                     // (the wide TLAS boxes above are conservative and only cull).
-                    if(!intersect_aabb_exact(wox, woy, woz, wdx, wdy, wdz, __ldg(ip + 4), __ldg(ip + 5),
+                    if(!intersect_aabb_exact(wox, woy, woz, wix, wiy, wiz, __ldg(ip + 4), __ldg(ip + 5),
                                              tmin, tmax))
                         continue;
                     if(ng.y > 0x00FFFFFFu)
