@@ -232,7 +232,7 @@ def gpu_arm(args):
 
     peak, peak_kind = load_peaks()
     per_ray = (32 + 28 + 80.0 * counts["node_visits"] / counts["rays"] +
-               48.0 * counts["tri_tests"] / counts["rays"] + 64.0 * counts["instance_entries"] / counts["rays"])
+               48.0 * counts["tri_tests"] / counts["rays"] + 96.0 * counts["instance_entries"] / counts["rays"])
     achieved = per_ray * n / (kernel_ms * 1e-3) / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traverse_closest_traffic.json")
@@ -260,7 +260,9 @@ def gpu_arm(args):
                      "kernel": "k_trace<closest>", "kernel_ms": round(kernel_ms, 4),
                      "algorithmic_bytes_per_ray": round(per_ray, 1),
                      "node_visits_per_ray": round(counts["node_visits"] / counts["rays"], 2),
-                     "tri_tests_per_ray": round(counts["tri_tests"] / counts["rays"], 2)},
+                     "tlas_node_visits_per_ray": round(counts["tlas_node_visits"] / counts["rays"], 2),
+                     "tri_tests_per_ray": round(counts["tri_tests"] / counts["rays"], 2),
+                     "instance_entries_per_ray": round(counts["instance_entries"] / counts["rays"], 2)},
         "clocks": clocks,
         "extra": {"anyhit_mrays_s": round(any_val, 1), "shadow_rays": int(shadow.shape[0]),
                   "build_ms": round(st["buildMs"], 1), "build_wall_s": round(build_s, 3),

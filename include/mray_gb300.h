@@ -183,9 +183,10 @@ mrg_status mrg_sync_status(mrg_ctx* ctx, void* stream);
 
 /* Traversal statistics for the algorithmic-byte count: casts the rays with
  * counters on and returns [0] rays, [1] wide-node visits, [2] triangle tests,
- * [3] instance entries.  Rays are not modified. */
+ * [3] instance entries, [4] of [1] in the TLAS, [5] of [3] that found no
+ * closer hit, [6..7] zero.  Rays are not modified. */
 mrg_status mrg_cast_closest_stats(mrg_ctx* ctx, const mrg_ray* d_rays, uint32_t n,
-                                  uint64_t out_counts[4], void* stream);
+                                  uint64_t out_counts[8], void* stream);
 
 #ifdef __cplusplus
 }

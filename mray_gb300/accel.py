@@ -121,8 +121,8 @@ class Accelerator:
         N.check(self._lib.mrg_sync_status(self._h, _stream_ptr(stream)))
 
     def traversal_counts(self, rays, stream=None):
-        out = (C.c_uint64 * 4)()
+        out = (C.c_uint64 * 8)()
         N.check(self._lib.mrg_cast_closest_stats(self._h, _ptr(rays), int(rays.shape[0]), out,
                                                  _stream_ptr(stream)))
         return {"rays": out[0], "node_visits": out[1], "tri_tests": out[2],
-                "instance_entries": out[3]}
+                "instance_entries": out[3], "tlas_node_visits": out[4], "dry_instance_entries": out[5]}

@@ -108,7 +108,7 @@ mrg_status mrg_create(const mrg_params* params, mrg_ctx** out)
     if((e = cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
        (e = cudaStreamCreateWithFlags(&c->buildStream, cudaStreamNonBlocking)) != cudaSuccess ||
        (e = cudaMalloc(&c->dScratch, 8 * sizeof(uint32_t))) != cudaSuccess ||
-       (e = cudaMalloc(&c->dStats, 4 * sizeof(unsigned long long))) != cudaSuccess ||
+       (e = cudaMalloc(&c->dStats, 8 * sizeof(unsigned long long))) != cudaSuccess ||
        (e = cudaMemset(c->dScratch, 0, 8 * sizeof(uint32_t))) != cudaSuccess)
     {
         mrg_status s = cuda_fail(e, "mrg_create");
@@ -413,17 +413,17 @@ mrg_status mrg_sync_status(mrg_ctx* c, void* stream)
 }
 
 mrg_status mrg_cast_closest_stats(mrg_ctx* c, const mrg_ray* dRays, uint32_t n,
-                                  uint64_t out[4], void* stream)
+                                  uint64_t out[8], void* stream)
 {
     if(!c || !out) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_closest_stats: null pointer");
     if(!c->built) return fail(MRG_ERR_NOT_BUILT, "mrg_cast_closest_stats: call mrg_build first");
     DeviceGuard g(c->device);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     MRG_TRY(mrg::launch_closest_stats(c->scene, scratch_of(c), dRays, n, c->smCount, st), "stats cast");
-    unsigned long long h[4] = { 0, 0, 0, 0 };
+    unsigned long long h[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
     MRG_TRY(cudaMemcpyAsync(h, c->dStats, sizeof(h), cudaMemcpyDeviceToHost, st), "stats read");
     MRG_TRY(cudaStreamSynchronize(st), "stats sync");
-    for(int i = 0; i < 4; i++) out[i] = h[i];
+    for(int i = 0; i < 8; i++) out[i] = h[i];
     return MRG_OK;
 }
 

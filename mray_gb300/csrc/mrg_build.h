@@ -52,7 +52,7 @@ struct TraceScratch
 {
     uint32_t*           workCounter = nullptr;   // 1 word, zeroed before each launch
     uint32_t*           errorFlag = nullptr;     // 1 word, sticky error bits
-    unsigned long long* stats = nullptr;         // 4 words (stats kernel only)
+    unsigned long long* stats = nullptr;         // 8 words (stats kernel only)
 };
 
 enum TraceErrorBits : uint32_t

@@ -137,7 +137,7 @@ __device__ __forceinline__ float std_min(float x, float y) { return (y < x) ? y 
 __device__ __forceinline__ bool intersect_aabb_exact(float ox, float oy, float oz,
                                                      float ix, float iy, float iz,
                                                      const float4& bmin, const float4& bmax,
-                                                     float tmin, float tmax)
+                                                     float tmin, float tmax, float& tEnter)
 {
     const float id[3] = { ix, iy, iz };
     const float o[3] = { ox, oy, oz };
@@ -153,6 +153,7 @@ __device__ __forceinline__ bool intersect_aabb_exact(float ox, float oy, float o
         o0 = std_max(o0, std_min(t0, t1));
         o1 = std_min(o1, std_max(t0, t1));
     }
+    tEnter = o0;
     return o1 >= o0;
 }
 

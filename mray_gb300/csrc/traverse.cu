@@ -23,7 +23,7 @@ namespace {
 
 // Tuning knobs (compile-time; the defaults are the measured best on GB300).
 #ifndef MRG_TRACE_MIN_BLOCKS
-#define MRG_TRACE_MIN_BLOCKS 8       // resident 128-thread blocks per SM the register budget targets
+#define MRG_TRACE_MIN_BLOCKS 7       // resident 128-thread blocks per SM the register budget targets
 #endif
 #ifndef MRG_TRACE_REFILL
 #define MRG_TRACE_REFILL 8           // refill when at least this many lanes are idle
@@ -32,7 +32,10 @@ namespace {
 #define MRG_TRACE_STEP_BUDGET 16     // traversal iterations between refill checks
 #endif
 #ifndef MRG_TRACE_PREFETCH
-#define MRG_TRACE_PREFETCH 1         // L1 prefetch of the next node
+#define MRG_TRACE_PREFETCH 0         // L1 prefetch of the next node
+#endif
+#ifndef MRG_TRACE_SORT_INST
+#define MRG_TRACE_SORT_INST 1        // enter the instances of a TLAS leaf group nearest-first
 #endif
 #ifndef MRG_TRACE_POSTPONE
 #define MRG_TRACE_POSTPONE 0         // postpone triangles when fewer lanes want them
@@ -183,7 +186,9 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
     bool cull = false;
     float hitU = 0.0f, hitV = 0.0f;
     uint32_t steps = 0;
-    uint32_t statNodes = 0, statTris = 0, statInst = 0;
+    uint32_t statNodes = 0, statTris = 0, statInst = 0, statTlasNodes = 0, statDry = 0;
+    uint32_t instHitBefore = kInvalidIndex;
+    float instTBefore = 0.0f;
     bool warpDone = false;
 
     for(;;)
@@ -215,7 +220,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     sp = 0; blasBase = -1;
                     curInst = kInvalidIndex; hitInst = kInvalidIndex;
                     steps = 0;
-                    if(STATS) { statNodes = 0; statTris = 0; statInst = 0; }
+                    if(STATS) { statNodes = 0; statTris = 0; statInst = 0; statTlasNodes = 0; statDry = 0; }
                     live = true;
                 }
             }
@@ -243,7 +248,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                 }
                 uint32_t cb, tb, im;
                 const uint32_t hm = intersect_node(sc.nodes, ni, lr, tmin, tmax, cb, tb, im);
-                if(STATS) statNodes++;
+                if(STATS) { statNodes++; if(blasBase < 0) statTlasNodes++; }
                 ng = make_uint2(cb, (hm & 0xFF000000u) ? ((hm & 0xFF000000u) | im) : 0u);
                 tg = make_uint2(tb, hm & 0x00FFFFFFu);
                 if(MRG_TRACE_PREFETCH && ng.y)
@@ -301,51 +306,68 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
             }
             else
             {
-                // instances of a TLAS leaf group
-                while(tg.y != 0u)
+                // instances of a TLAS leaf group.  MRay's exact slab test on the
+                // exact world AABB decides entry (the wide TLAS boxes above are
+                // conservative and only cull); among the candidates that pass
+                // it, the nearest entry is taken first and the rest go back on
+                // the stack, to be re-tested against the shrunken tMax.
+                if(tg.y != 0u)
                 {
-                    const uint32_t bt = __ffs(tg.y) - 1u;
-                    tg.y &= tg.y - 1u;
-                    const uint32_t pi = tg.x + bt;
-                    if(pi >= sc.instCount) { atomicOr(scr.errorFlag, kTraceBadIndex); finished = true; break; }
-                    const uint32_t inst = __ldg(sc.tlasLeaf + pi);
-                    if(inst >= sc.instCount) { atomicOr(scr.errorFlag, kTraceBadIndex); finished = true; break; }
-                    const float4* ip = reinterpret_cast<const float4*>(sc.insts + inst);
-                    // MRay's own leaf test decides whether the instance is entered
-                    // (the wide TLAS boxes above are conservative and only cull).
-                    if(!intersect_aabb_exact(wox, woy, woz, wix, wiy, wiz, __ldg(ip + 4), __ldg(ip + 5),
-                                             tmin, tmax))
-                        continue;
-                    if(ng.y > 0x00FFFFFFu)
+                    uint32_t keep = 0u, best = 32u;
+                    float bestT = 0.0f;
+                    for(uint32_t cand = tg.y; cand != 0u; cand &= cand - 1u)
                     {
-                        if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); finished = true; break; }
-                        stack[sp++] = ng;
+                        const uint32_t bt = __ffs(cand) - 1u;
+                        const uint32_t pi = tg.x + bt;
+                        if(pi >= sc.instCount) { atomicOr(scr.errorFlag, kTraceBadIndex); finished = true; break; }
+                        const uint32_t inst = __ldg(sc.tlasLeaf + pi);
+                        if(inst >= sc.instCount) { atomicOr(scr.errorFlag, kTraceBadIndex); finished = true; break; }
+                        const float4* ip = reinterpret_cast<const float4*>(sc.insts + inst);
+                        float tEnter;
+                        if(!intersect_aabb_exact(wox, woy, woz, wix, wiy, wiz, __ldg(ip + 4), __ldg(ip + 5),
+                                                 tmin, tmax, tEnter))
+                            continue;
+                        keep |= 1u << bt;
+                        if(best == 32u || (MRG_TRACE_SORT_INST && tEnter < bestT)) { best = bt; bestT = tEnter; }
+                        if(!MRG_TRACE_SORT_INST) break;
                     }
-                    if(tg.y != 0u)
-                    {
-                        if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); finished = true; break; }
-                        stack[sp++] = tg;
-                    }
-                    blasBase = sp;
-                    const float4 m0 = __ldg(ip), m1 = __ldg(ip + 1), m2 = __ldg(ip + 2);
-                    const uint4 keys = __ldg(reinterpret_cast<const uint4*>(ip + 3));
-                    transform_ray_exact(m0, m1, m2, make_float3(wox, woy, woz),
-                                        make_float3(wdx, wdy, wdz), lo, ld);
-                    setup_level(lr, lo.x, lo.y, lo.z, ld.x, ld.y, ld.z);
-                    cull = (keys.w & kCullBit) != 0u;
-                    curInst = inst;
-                    if(STATS) statInst++;
-                    ng = make_uint2(keys.w & ~kCullBit, (1u << (24u + lr.oct7)) | 1u);
+                    if(finished) break;
+                    if(!MRG_TRACE_SORT_INST && best != 32u) keep = tg.y;   // untested ones stay candidates
                     tg.y = 0u;
-                    break;
+                    if(best != 32u)
+                    {
+                        keep &= ~(1u << best);
+                        const uint32_t inst = __ldg(sc.tlasLeaf + tg.x + best);
+                        const float4* ip = reinterpret_cast<const float4*>(sc.insts + inst);
+                        if(ng.y > 0x00FFFFFFu)
+                        {
+                            if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); finished = true; break; }
+                            stack[sp++] = ng;
+                        }
+                        if(keep != 0u)
+                        {
+                            if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); finished = true; break; }
+                            stack[sp++] = make_uint2(tg.x, keep);
+                        }
+                        blasBase = sp;
+                        const float4 m0 = __ldg(ip), m1 = __ldg(ip + 1), m2 = __ldg(ip + 2);
+                        const uint4 keys = __ldg(reinterpret_cast<const uint4*>(ip + 3));
+                        transform_ray_exact(m0, m1, m2, make_float3(wox, woy, woz),
+                                            make_float3(wdx, wdy, wdz), lo, ld);
+                        setup_level(lr, lo.x, lo.y, lo.z, ld.x, ld.y, ld.z);
+                        cull = (keys.w & kCullBit) != 0u;
+                        curInst = inst;
+                        if(STATS) { statInst++; instHitBefore = hitInst; instTBefore = tmax; }
+                        ng = make_uint2(keys.w & ~kCullBit, (1u << (24u + lr.oct7)) | 1u);
+                    }
                 }
-                if(finished) break;
             }
 
             if(ng.y <= 0x00FFFFFFu)
             {
                 if(blasBase >= 0 && sp == blasBase)
                 {
+                    if(STATS && tmax == instTBefore) statDry++;
                     blasBase = -1;
                     setup_level(lr, wox, woy, woz, wdx, wdy, wdz);
                 }
@@ -364,6 +386,8 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                 atomicAdd(&scr.stats[1], (unsigned long long)statNodes);
                 atomicAdd(&scr.stats[2], (unsigned long long)statTris);
                 atomicAdd(&scr.stats[3], (unsigned long long)statInst);
+                atomicAdd(&scr.stats[4], (unsigned long long)statTlasNodes);
+                atomicAdd(&scr.stats[5], (unsigned long long)statDry);
             }
             else if(ANY)
             {
@@ -431,7 +455,7 @@ cudaError_t launch_closest_stats(const TraceScene& sc, const TraceScratch& scr, 
     if(n == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(scr.workCounter, 0, sizeof(uint32_t), st);
     if(e != cudaSuccess) return e;
-    e = cudaMemsetAsync(scr.stats, 0, 4 * sizeof(unsigned long long), st);
+    e = cudaMemsetAsync(scr.stats, 0, 8 * sizeof(unsigned long long), st);
     if(e != cudaSuccess) return e;
     k_trace<false, true><<<blocks_for<false, true>(smCount), kTraceTPB, 0, st>>>(
         sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), nullptr, n, nullptr,
