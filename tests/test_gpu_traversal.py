@@ -36,24 +36,43 @@ def test_closest_small_scenes(level, ninst, cull):
     assert hits > 0
 
 
-def test_corrected_inverse_mode_general_rotations():
-    """General random rotations (MRay's inverse is wrong for them) in the
-    corrected mode; also the default mode on the same rotations."""
-    rng = np.random.default_rng(5)
-    pos, idx = scenes.icosphere(3, 1.0, 0.05, 4.0, 0)
+def _general_rotations(n=12, seed=5):
+    rng = np.random.default_rng(seed)
     mats = []
-    for i in range(12):
+    for i in range(n):
         q = rng.normal(size=4); q /= np.linalg.norm(q)
         w, x, y, z = q
         R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
                       [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
                       [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
         mats.append(np.hstack([R, rng.uniform(-3, 3, (3, 1))]).reshape(12))
-    mats = np.array(mats, np.float32)
+    return np.array(mats, np.float32)
+
+
+def test_corrected_inverse_mode_general_rotations():
+    """General random rotations with the corrected inverse: bit-exact on every ray."""
+    pos, idx = scenes.icosphere(3, 1.0, 0.05, 4.0, 0)
+    mats = _general_rotations()
     rays = scenes.primary_rays(80, 80, 9, eye=(0, 0, -12), tan_half_fov=0.5)
-    for corrected in (True, False):
-        acc, S = build_pair(pos, idx, mats, corrected=corrected)
-        compare_closest(S.cast_closest(rays), gpu_closest(acc, rays))
+    acc, S = build_pair(pos, idx, mats, corrected=True)
+    compare_closest(S.cast_closest(rays), gpu_closest(acc, rays))
+
+
+def test_reference_inverse_mode_general_rotations():
+    """MRay's own inverse on general rotations misplaces the BLAS geometry
+    relative to its world AABB, so MRay's answer depends on its TLAS visiting
+    order (its LBVH result differs from its brute force).  Wherever it does
+    not (oracle LBVH == oracle brute force), the GPU must match bit for bit."""
+    pos, idx = scenes.icosphere(3, 1.0, 0.05, 4.0, 0)
+    mats = _general_rotations()
+    rays = scenes.primary_rays(80, 80, 9, eye=(0, 0, -12), tan_half_fov=0.5)
+    acc, S = build_pair(pos, idx, mats, corrected=False)
+    ora = S.cast_closest(rays)
+    lin = S.cast_closest(rays, linear=True)
+    stable = np.nonzero(ora[0][:, 7].view(np.uint32) == lin[0][:, 7].view(np.uint32))[0]
+    assert stable.size > 0.8 * rays.shape[0]
+    gpu = gpu_closest(acc, rays)
+    compare_closest(ora, gpu, listed=stable)
 
 
 def test_indirection_partial_lists_and_prefilled_hits():
