@@ -60,19 +60,41 @@ def test_corrected_inverse_mode_general_rotations():
 
 def test_reference_inverse_mode_general_rotations():
     """MRay's own inverse on general rotations misplaces the BLAS geometry
-    relative to its world AABB, so MRay's answer depends on its TLAS visiting
-    order (its LBVH result differs from its brute force).  Wherever it does
-    not (oracle LBVH == oracle brute force), the GPU must match bit for bit."""
+    relative to the instance's world AABB, so which hit MRay reports depends on
+    the order its TLAS visits instances (its LBVH result differs from its own
+    brute force on ~14% of these rays).  The GPU visits nearest-first; it must
+    agree bit for bit on >= 99% of rays, and every ray where it differs must
+    carry a genuine MRay hit: the reported triangle, intersected with the
+    oracle's MT in that instance's (MRay-inverted) space, gives exactly the
+    reported t and barycentrics."""
     pos, idx = scenes.icosphere(3, 1.0, 0.05, 4.0, 0)
     mats = _general_rotations()
     rays = scenes.primary_rays(80, 80, 9, eye=(0, 0, -12), tan_half_fov=0.5)
     acc, S = build_pair(pos, idx, mats, corrected=False)
     ora = S.cast_closest(rays)
-    lin = S.cast_closest(rays, linear=True)
-    stable = np.nonzero(ora[0][:, 7].view(np.uint32) == lin[0][:, 7].view(np.uint32))[0]
-    assert stable.size > 0.8 * rays.shape[0]
-    gpu = gpu_closest(acc, rays)
-    compare_closest(ora, gpu, listed=stable)
+    gr, gh, gm = gpu_closest(acc, rays)
+    diff = np.nonzero(ora[0][:, 7].view(np.uint32) != gr[:, 7].view(np.uint32))[0]
+    assert diff.size <= 0.01 * rays.shape[0]
+    for k in diff:
+        if gr[k, 7] >= 3e38:
+            continue
+        inst = int(gh[k, 2] & 0xFFFFFF)
+        prim = int(gh[k, 0] - 0x10000000)
+        inv = S.instance_inverse(inst)
+        R = inv.reshape(3, 4)
+        import ctypes as C
+        L = oracle.lib()
+        d = np.ascontiguousarray(rays[k, 4:7]); p = np.ascontiguousarray(rays[k, 0:3])
+        ld = np.zeros(3, np.float32); lp = np.zeros(3, np.float32)
+        L.orc_transform_ray(inv.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p),
+                            p.ctypes.data_as(C.c_void_p), ld.ctypes.data_as(C.c_void_p),
+                            lp.ctypes.data_as(C.c_void_p))
+        v = pos[idx[prim]]
+        hit, bary, t, _ = oracle.intersect_triangle(ld, lp, v[0], v[1], v[2], True)
+        assert hit and np.float32(t).view(np.uint32) == gr[k, 7].view(np.uint32)
+        assert np.array_equal(bary[:2].view(np.uint32), gm[k].view(np.uint32))
+    other = np.setdiff1d(np.arange(rays.shape[0]), diff)
+    compare_closest(ora, (gr, gh, gm), listed=other)
 
 
 def test_indirection_partial_lists_and_prefilled_hits():
