@@ -35,7 +35,7 @@ namespace {
 #define MRG_TRACE_PREFETCH 0         // L1 prefetch of the next node
 #endif
 #ifndef MRG_TRACE_SORT_INST
-#define MRG_TRACE_SORT_INST 1        // enter the instances of a TLAS leaf group nearest-first
+#define MRG_TRACE_SORT_INST 0        // 1: enter the instances of a TLAS leaf group nearest-first
 #endif
 #ifndef MRG_TRACE_POSTPONE
 #define MRG_TRACE_POSTPONE 0         // postpone triangles when fewer lanes want them
