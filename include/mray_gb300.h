@@ -188,6 +188,50 @@ mrg_status mrg_sync_status(mrg_ctx* ctx, void* stream);
 mrg_status mrg_cast_closest_stats(mrg_ctx* ctx, const mrg_ray* d_rays, uint32_t n,
                                   uint64_t out_counts[8], void* stream);
 
+/* ---------------------------------------------------------------------- */
+/* Path tracer (MRay's PathTracerRenderer, RGB; TracerI::CreateRenderer /   */
+/* PushRendererAttribute / DoRenderWork, Source/Core/TracerI.h:331-376;     */
+/* options Source/TracerDLL/PathTracerRendererShaders.h:36-45)              */
+/* ---------------------------------------------------------------------- */
+#define MRG_PT_PURE     0u   /* SampleMode "Pure" */
+#define MRG_PT_NEE      1u   /* "WithNextEventEstimation" */
+#define MRG_PT_NEE_MIS  2u   /* "WithNEEAndMIS" */
+
+typedef struct mrg_pt_params
+{
+    uint32_t width, height;      /* film size */
+    uint32_t spp;                /* samples per pixel rendered by this call */
+    uint32_t samplesPerPass;     /* paths in flight = width * height * samplesPerPass (0 = auto) */
+    uint32_t rrStart, maxDepth;  /* russianRouletteRange (RR from rrStart, paths end at maxDepth) */
+    uint32_t sampleMode;         /* MRG_PT_* */
+    uint32_t seed;
+    float    filterRadius;       /* Gaussian film filter radius in pixels (MRay default 1) */
+    float    camPos[3];          /* pinhole camera: position, gaze point, up */
+    float    camGaze[3];
+    float    camUp[3];
+    float    fov[2];             /* radians, x and y */
+    float    nearFar[2];
+    uint32_t sampleStart;        /* index of the first sample (continue an accumulation) */
+} mrg_pt_params;
+
+/* Surface description of an instance, the equivalent of attaching a
+ * material / light group to a surface (TracerI::CreateSurface, CreateLightSurface).
+ * Rendering requires trans_key index = instance id and dense primitive keys. */
+mrg_status mrg_pt_set_lambert(mrg_ctx* ctx, uint32_t instance_id, const float albedo[3]);
+mrg_status mrg_pt_set_area_light(mrg_ctx* ctx, uint32_t instance_id, const float radiance[3],
+                                 uint32_t two_sided);
+
+/* The pinhole frame MRay derives from the camera parameters
+ * (CameraPinhole ctor, Source/Tracer/CamerasDefault.hpp:6-30): out = position[3],
+ * bottomLeft[3], right[3], up[3], planeSize[2], near, far. */
+mrg_status mrg_pt_camera_frame(const mrg_pt_params* params, float out[16]);
+
+/* Renders params->spp samples per pixel and ADDS them to d_image, a device
+ * float4 per pixel (R, G, B, filter weight), row 0 at the bottom of the image
+ * plane; pixel value = RGB / weight.  Stream-ordered, no host synchronisation
+ * inside a pass. */
+mrg_status mrg_pt_render(mrg_ctx* ctx, const mrg_pt_params* params, float* d_image, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,7 +29,20 @@ EXPORTED = [
     "mrg_upload_mesh", "mrg_add_instance", "mrg_build", "mrg_cast_closest",
     "mrg_cast_visibility", "mrg_cast_closest_host", "mrg_scene_aabb", "mrg_get_stats",
     "mrg_sync_status", "mrg_cast_closest_stats", "mrg_cast_closest_host_noalloc",
+    "mrg_pt_set_lambert", "mrg_pt_set_area_light", "mrg_pt_camera_frame", "mrg_pt_render",
 ]
+
+MRG_PT_PURE = 0
+MRG_PT_NEE = 1
+MRG_PT_NEE_MIS = 2
+
+
+class MrgPtParams(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32),
+                ("samplesPerPass", C.c_uint32), ("rrStart", C.c_uint32), ("maxDepth", C.c_uint32),
+                ("sampleMode", C.c_uint32), ("seed", C.c_uint32), ("filterRadius", C.c_float),
+                ("camPos", C.c_float * 3), ("camGaze", C.c_float * 3), ("camUp", C.c_float * 3),
+                ("fov", C.c_float * 2), ("nearFar", C.c_float * 2), ("sampleStart", C.c_uint32)]
 
 #: capacity of mrg_cast_closest_host_noalloc (rays per call)
 MRG_NOALLOC_MAX_RAYS = 262144
@@ -77,6 +90,10 @@ def _declare(lib):
         "mrg_get_stats": (C.c_int, [vp, C.POINTER(MrgAccelStats)]),
         "mrg_sync_status": (C.c_int, [vp, vp]),
         "mrg_cast_closest_stats": (C.c_int, [vp, vp, u32, C.POINTER(C.c_uint64), vp]),
+        "mrg_pt_set_lambert": (C.c_int, [vp, u32, fp]),
+        "mrg_pt_set_area_light": (C.c_int, [vp, u32, fp, u32]),
+        "mrg_pt_camera_frame": (C.c_int, [C.POINTER(MrgPtParams), fp]),
+        "mrg_pt_render": (C.c_int, [vp, C.POINTER(MrgPtParams), vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

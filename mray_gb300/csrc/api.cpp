@@ -126,6 +126,7 @@ mrg_status mrg_destroy(mrg_ctx* c)
     free_accel(c);
     cudaFree(c->dScratch);
     cudaFree(c->dStats);
+    cudaFree(c->dPtSurfaces); cudaFree(c->dPtLights); cudaFree(c->dPtTris); cudaFree(c->ptPathMem);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);
     delete c;
@@ -179,6 +180,7 @@ mrg_status mrg_build(mrg_ctx* c)
     DeviceGuard g(c->device);
     auto t0 = std::chrono::steady_clock::now();
     free_accel(c);
+    c->ptDirty = true;
     cudaStream_t st = c->buildStream;
     std::string err;
 

@@ -62,12 +62,14 @@ enum TraceErrorBits : uint32_t
     kTraceBadIndex      = 4u
 };
 
+// nDevice (optional): device word holding the ray count, read by the kernel
+// (device-driven wavefronts); when given, n is ignored.
 cudaError_t launch_closest(const TraceScene& sc, const TraceScratch& scr, void* rays,
                            const uint32_t* rayIdx, uint32_t n, void* hits, void* meta,
-                           int smCount, cudaStream_t st);
+                           int smCount, cudaStream_t st, const uint32_t* nDevice = nullptr);
 cudaError_t launch_visibility(const TraceScene& sc, const TraceScratch& scr, uint32_t* visBits,
                               const void* rays, const uint32_t* rayIdx, uint32_t n,
-                              int smCount, cudaStream_t st);
+                              int smCount, cudaStream_t st, const uint32_t* nDevice = nullptr);
 cudaError_t launch_closest_stats(const TraceScene& sc, const TraceScratch& scr, const void* rays,
                                  uint32_t n, int smCount, cudaStream_t st);
 

@@ -3,6 +3,7 @@
 #pragma once
 #include "mray_gb300.h"
 #include "mrg_build.h"
+#include "mrg_pt.h"
 
 #include <cuda_runtime.h>
 
@@ -63,6 +64,23 @@ struct mrg_ctx
     // scratch: [0] work counter, [1] error flag; stats in a separate block
     uint32_t*           dScratch = nullptr;
     unsigned long long* dStats = nullptr;
+
+    // path tracer: per-instance surface description, device tables, path state
+    struct PtSurfaceDesc
+    {
+        int      kind = 0;            // 0 unset, 1 Lambert, 2 area light
+        float    albedo[3] = { 0, 0, 0 };
+        float    radiance[3] = { 0, 0, 0 };
+        uint32_t twoSided = 0;
+    };
+    std::vector<PtSurfaceDesc> ptDesc;       // indexed by instance
+    bool      ptDirty = true;
+    void*     dPtSurfaces = nullptr;
+    void*     dPtLights = nullptr;
+    void*     dPtTris = nullptr;
+    uint32_t  ptSurfaceCount = 0, ptLightCount = 0, ptTriCount = 0;
+    mrg::PtPaths ptPaths{};
+    void*     ptPathMem = nullptr;
 
     // staging for the host-buffer cast
     mrg_ray*      dStageRays = nullptr;

@@ -1,0 +1,82 @@
+// mrg_pt.h -- device data and host launch interface of the wavefront path tracer.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mrg_build.h"
+
+namespace mrg {
+
+// Per surface (= per instance; indexed by the transform key's index portion).
+struct __align__(16) PtSurface
+{
+    float4 m[3];        // local -> world rows
+    float4 inv[3];      // world -> local rows (normals use its transpose)
+    float4 albedo;      // Lambert albedo (xyz)
+    uint4  info;        // x: 1 if light, y: first light index, z: primitive key base, w: 0
+};
+
+// One light per emitting triangle (MRay's primitive-backed lights,
+// Source/Tracer/LightsDefault.hpp:14-160), in world space.
+struct __align__(16) PtLight
+{
+    float4 p0;          // w: area
+    float4 p1;
+    float4 p2;
+    float4 n;           // geometric normal, w: two-sided (0/1)
+    float4 radiance;
+};
+
+struct PtCamera
+{
+    float pos[3];
+    float bottomLeft[3];
+    float right[3];
+    float up[3];
+    float planeSize[2];
+    float nearT, farT;
+};
+
+struct PtLaunch
+{
+    uint32_t width, height;
+    uint32_t slots;          // paths per pass = width * height * samplesPerPass
+    uint32_t samplesPerPass;
+    uint32_t sampleBase;     // sample index of the pass's first sample
+    uint32_t rrStart, maxDepth;
+    uint32_t sampleMode;     // 0 pure, 1 NEE, 2 NEE + MIS
+    uint32_t seed;
+    uint32_t nLights;
+    float    filterSigma;
+    PtCamera cam;
+};
+
+// Path state, structure of arrays (device).
+struct PtPaths
+{
+    float4*   rays;          // 2 per slot (RayGMem)
+    uint4*    hits;          // HitKeyPack per slot
+    float2*   meta;          // MetaHit per slot
+    float4*   thr;           // throughput xyz, w = pdf of the last BxDF sample
+    float4*   rad;           // radiance xyz, w = film weight
+    uint32_t* state;         // depth | type << 8
+    float4*   shadowRays;    // 2 per slot
+    float4*   shadowRad;
+    uint32_t* visBits;       // visibility, one bit per slot
+    uint32_t* listA;         // alive lists (ping-pong)
+    uint32_t* listB;
+    uint32_t* shadowList;
+    uint32_t* counts;        // [0] list A count, [1] list B count, [2] shadow count, [3] pad
+    uint32_t  capacity;
+};
+
+cudaError_t pt_raygen(const PtLaunch& L, const PtPaths& P, uint32_t* aliveList, uint32_t* aliveCount,
+                      int smCount, cudaStream_t st);
+cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSurface* surfaces, uint32_t nSurfaces,
+                          const PtLight* lights, const float4* tris, uint32_t nTris,
+                          const uint32_t* aliveList, const uint32_t* aliveCount,
+                          uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st);
+cudaError_t pt_resolve(const PtLaunch& L, const PtPaths& P, uint32_t depth, int smCount, cudaStream_t st);
+cudaError_t pt_film(const PtLaunch& L, const PtPaths& P, float4* image, cudaStream_t st);
+
+} // namespace mrg

@@ -1,0 +1,431 @@
+// pt.cu -- wavefront path tracer kernels (RGB, NEE + MIS, Russian roulette).
+//
+// The estimator is MRay's (Source/TracerDLL/PathTracerRendererShaders.h:
+// 203-300 BxDF sample + RR, 354-445 NEE, 450-517 light hits with MIS;
+// Source/TracerDLL/PathTracerRenderer.cu:13-31 shadow accumulation).  The
+// structure is GB300-first: one pass is
+//     raygen -> [closest hit -> shade -> any hit -> resolve] x maxDepth -> film
+// where every kernel is a fixed-size persistent grid that reads its work count
+// from device memory, so the host enqueues a pass without a single
+// synchronisation (MRay waits on the host at least four times per bounce).
+// Live paths are compacted with warp ballots; NEE and the BxDF sample of a
+// surface hit run in one fused shade kernel; the film is resolved per pixel
+// without atomics, so images are bit-reproducible run to run.
+//
+// Random numbers are a counter-based hash of (seed, pixel, sample, bounce,
+// dimension): no per-path RNG state is stored or advanced.
+//
+// Arithmetic that the CPU oracle mirrors uses the _rn intrinsics (no fused
+// multiply-add), so both render the same paths up to the library's sin / cos
+// / log, which differ between CUDA and the host C library by a few ulps.
+#include "mrg_pt.h"
+#include "mrg_device.cuh"
+
+namespace mrg {
+
+namespace {
+
+constexpr int kPtTPB = 256;
+constexpr uint32_t kMissMark = 0xFFFFFFFFu;
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInvPi = 0.318309886183790671538f;
+
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t v)
+{
+    const uint32_t state = v * 747796405u + 2891336453u;
+    const uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+__device__ __forceinline__ uint32_t path_key(uint32_t seed, uint32_t pixel, uint32_t sample)
+{
+    return pcg_hash(pcg_hash(seed ^ 0x9E3779B9u) ^ pcg_hash(pixel) ^ pcg_hash(sample + 0x632BE5ABu));
+}
+__device__ __forceinline__ float rnd(uint32_t key, uint32_t bounce, uint32_t dim)
+{
+    const uint32_t h = pcg_hash(key ^ pcg_hash((bounce << 4) | dim));
+    return __fmul_rn((float)(h >> 8), 1.0f / 16777216.0f);
+}
+
+// Unfused a*b + c and friends (the oracle is compiled without contraction).
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float dot3(float3 a, float3 b)
+{
+    return add(add(mul(a.x, b.x), mul(a.y, b.y)), mul(a.z, b.z));
+}
+__device__ __forceinline__ float3 cross3(float3 a, float3 b)
+{
+    return make_float3(sub(mul(a.y, b.z), mul(a.z, b.y)),
+                       sub(mul(a.z, b.x), mul(a.x, b.z)),
+                       sub(mul(a.x, b.y), mul(a.y, b.x)));
+}
+__device__ __forceinline__ float3 normalize3(float3 v)
+{
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(v, v)));
+    return make_float3(mul(v.x, inv), mul(v.y, inv), mul(v.z, inv));
+}
+__device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
+
+// Ray::Nudge (Source/Core/Ray.hpp:258-300).
+__device__ __forceinline__ float nudge1(float p, float n)
+{
+    const int32_t ofi = (int32_t)(mul(256.0f, n));
+    int32_t pi = __float_as_int(p);
+    pi += (p < 0.0f) ? -ofi : ofi;
+    return (fabsf(p) < (1.0f / 32.0f)) ? add(p, mul(1.0f / 65536.0f, n)) : __int_as_float(pi);
+}
+__device__ __forceinline__ float3 nudge(float3 p, float3 n)
+{
+    return make_float3(nudge1(p.x, n.x), nudge1(p.y, n.y), nudge1(p.z, n.z));
+}
+
+// Duff et al. orthonormal basis about n.
+__device__ __forceinline__ void onb(float3 n, float3& t, float3& b)
+{
+    const float sign = copysignf(1.0f, n.z);
+    const float a = __fdiv_rn(-1.0f, add(sign, n.z));
+    const float bb = mul(mul(n.x, n.y), a);
+    t = make_float3(add(1.0f, mul(mul(mul(sign, n.x), n.x), a)), mul(sign, bb), -mul(sign, n.x));
+    b = make_float3(bb, add(sign, mul(mul(n.y, n.y), a)), -n.y);
+}
+
+__device__ __forceinline__ uint32_t slot_pixel(const PtLaunch& L, uint32_t i) { return i % (L.width * L.height); }
+__device__ __forceinline__ uint32_t slot_sample(const PtLaunch& L, uint32_t i)
+{
+    return L.sampleBase + i / (L.width * L.height);
+}
+
+// ---------------------------------------------------------------------------
+// Camera rays: pinhole (CamerasDefault.hpp:94-140), Gaussian film filter
+// sampled with Box-Muller (filter / pdf = 1 per sample, Filters.h:195-233).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kPtTPB)
+k_raygen(PtLaunch L, PtPaths P, uint32_t* aliveList, uint32_t* aliveCount)
+{
+    if(blockIdx.x == 0 && threadIdx.x == 0) *aliveCount = L.slots;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < L.slots; i += gridDim.x * blockDim.x)
+    {
+        const uint32_t pixel = slot_pixel(L, i);
+        const uint32_t x = pixel % L.width, y = pixel / L.width;
+        const uint32_t key = path_key(L.seed, pixel, slot_sample(L, i));
+        const float u1 = rnd(key, 0, 6), u2 = rnd(key, 0, 7);
+        const float r = mul(L.filterSigma, __fsqrt_rn(mul(-2.0f, logf(sub(1.0f, u1)))));
+        const float ang = mul(mul(2.0f, kPi), u2);
+        const float ox = mul(r, cosf(ang)), oy = mul(r, sinf(ang));
+        const float dx = __fdiv_rn(L.cam.planeSize[0], (float)L.width);
+        const float dy = __fdiv_rn(L.cam.planeSize[1], (float)L.height);
+        const float sx = mul(add((float)x, add(ox, 0.5f)), dx);
+        const float sy = mul(add((float)y, add(oy, 0.5f)), dy);
+        float3 d;
+        d.x = sub(add(add(L.cam.bottomLeft[0], mul(sx, L.cam.right[0])), mul(sy, L.cam.up[0])), L.cam.pos[0]);
+        d.y = sub(add(add(L.cam.bottomLeft[1], mul(sx, L.cam.right[1])), mul(sy, L.cam.up[1])), L.cam.pos[1]);
+        d.z = sub(add(add(L.cam.bottomLeft[2], mul(sx, L.cam.right[2])), mul(sy, L.cam.up[2])), L.cam.pos[2]);
+        d = normalize3(d);
+        P.rays[2 * (size_t)i] = make_float4(L.cam.pos[0], L.cam.pos[1], L.cam.pos[2], L.cam.nearT);
+        P.rays[2 * (size_t)i + 1] = make_float4(d.x, d.y, d.z, L.cam.farT);
+        P.hits[i].x = kMissMark;
+        P.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        P.rad[i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        P.state[i] = 0u;
+        aliveList[i] = i;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Shade: light hits (emission with MIS), surface hits (NEE + Lambert sample +
+// Russian roulette).  Live paths and shadow rays are appended to their lists
+// with one atomic per warp.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void warp_append(bool pred, uint32_t value, uint32_t* list, uint32_t* count)
+{
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, pred);
+    if(m == 0u) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if((int)lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if(pred) list[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+__global__ void __launch_bounds__(kPtTPB)
+k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t nSurfaces,
+        const PtLight* __restrict__ lights, const float4* __restrict__ tris, uint32_t nTris,
+        const uint32_t* __restrict__ aliveList, const uint32_t* __restrict__ aliveCount,
+        uint32_t* nextList, uint32_t* nextCount)
+{
+    const uint32_t n = *aliveCount;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // warp-uniform trip count so every lane reaches the ballots
+    const uint32_t first = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    for(uint32_t base = first; base < n; base += stride)
+    {
+        const uint32_t idx = base + (threadIdx.x & 31u);
+        bool alive = false, shadow = false;
+        uint32_t i = 0;
+        if(idx < n)
+        {
+            i = aliveList[idx];
+            const uint4 hk = P.hits[i];
+            uint32_t st = P.state[i];
+            uint32_t depth = st & 0xFFu;
+            uint32_t type = (st >> 8) & 3u;
+            const uint32_t key = path_key(L.seed, slot_pixel(L, i), slot_sample(L, i));
+            const uint32_t surfIdx = hk.z & 0x00FFFFFFu;
+            if(hk.x != kMissMark && surfIdx < nSurfaces)
+            {
+                const float4 r0 = P.rays[2 * (size_t)i], r1 = P.rays[2 * (size_t)i + 1];
+                const float3 org = f3(r0), dir = f3(r1);
+                const PtSurface sf = surfaces[surfIdx];
+                const uint32_t gprim = hk.x;
+                const uint32_t localPrim = gprim - sf.info.z;
+                const float2 mh = P.meta[i];
+                const float bu = mh.y;
+                const float bv = sub(sub(1.0f, mh.x), mh.y);
+                float4 v0 = make_float4(0, 0, 0, 0), e0 = v0, e1 = v0;
+                if(gprim < nTris)
+                {
+                    v0 = tris[3 * (size_t)gprim]; e0 = tris[3 * (size_t)gprim + 1]; e1 = tris[3 * (size_t)gprim + 2];
+                }
+                const float3 pl = make_float3(add(add(v0.x, mul(e0.x, bu)), mul(e1.x, bv)),
+                                              add(add(v0.y, mul(e0.y, bu)), mul(e1.y, bv)),
+                                              add(add(v0.z, mul(e0.z, bu)), mul(e1.z, bv)));
+                float3 pos;
+                pos.x = add(add(add(mul(sf.m[0].x, pl.x), mul(sf.m[0].y, pl.y)), mul(sf.m[0].z, pl.z)), sf.m[0].w);
+                pos.y = add(add(add(mul(sf.m[1].x, pl.x), mul(sf.m[1].y, pl.y)), mul(sf.m[1].z, pl.z)), sf.m[1].w);
+                pos.z = add(add(add(mul(sf.m[2].x, pl.x), mul(sf.m[2].y, pl.y)), mul(sf.m[2].z, pl.z)), sf.m[2].w);
+                const float3 nl = cross3(f3(e0), f3(e1));
+                float3 gn;
+                gn.x = add(add(mul(sf.inv[0].x, nl.x), mul(sf.inv[1].x, nl.y)), mul(sf.inv[2].x, nl.z));
+                gn.y = add(add(mul(sf.inv[0].y, nl.x), mul(sf.inv[1].y, nl.y)), mul(sf.inv[2].y, nl.z));
+                gn.z = add(add(mul(sf.inv[0].z, nl.x), mul(sf.inv[1].z, nl.y)), mul(sf.inv[2].z, nl.z));
+                gn = normalize3(gn);
+                const float invN = L.nLights ? __fdiv_rn(1.0f, (float)L.nLights) : 0.0f;
+                float4 thr = P.thr[i];
+                float4 rad = P.rad[i];
+
+                if(sf.info.x)
+                {
+                    // ---- light hit (LightWorkFunction[WithNEE]) ----
+                    const PtLight lt = lights[sf.info.y + localPrim];
+                    const bool neeOnly = (L.sampleMode == 1u && type != 0u);
+                    if(!neeOnly)
+                    {
+                        float3 tp = f3(thr);
+                        if(L.sampleMode == 2u && type == 1u)
+                        {
+                            float ndl = -dot3(f3(lt.n), dir);
+                            ndl = (lt.n.w != 0.0f) ? fabsf(ndl) : fmaxf(0.0f, ndl);
+                            const float3 dd = make_float3(sub(org.x, pos.x), sub(org.y, pos.y), sub(org.z, pos.z));
+                            float lpdf = (ndl == 0.0f) ? 0.0f : __fdiv_rn(__fdiv_rn(1.0f, lt.p0.w), ndl);
+                            lpdf = mul(lpdf, dot3(dd, dd));
+                            lpdf = mul(lpdf, invN);
+                            const float misPdf = add(thr.w, lpdf);
+                            tp = make_float3(mul(tp.x, thr.w), mul(tp.y, thr.w), mul(tp.z, thr.w));
+                            if(misPdf == 0.0f) tp = make_float3(0, 0, 0);
+                            else
+                            {
+                                const float inv = __fdiv_rn(1.0f, misPdf);
+                                tp = make_float3(mul(tp.x, inv), mul(tp.y, inv), mul(tp.z, inv));
+                            }
+                        }
+                        const float3 wo = make_float3(-dir.x, -dir.y, -dir.z);
+                        const bool emits = (lt.n.w != 0.0f) || (dot3(f3(lt.n), wo) > 0.0f);
+                        if(emits && depth + 1u <= L.maxDepth)
+                        {
+                            rad.x = add(rad.x, mul(lt.radiance.x, tp.x));
+                            rad.y = add(rad.y, mul(lt.radiance.y, tp.y));
+                            rad.z = add(rad.z, mul(lt.radiance.z, tp.z));
+                        }
+                    }
+                }
+                else
+                {
+                    const float3 albedo = f3(sf.albedo);
+                    const float3 nrm = gn;
+                    float3 tng, btg;
+                    onb(nrm, tng, btg);
+                    // ---- NEE (WorkFunctionNEE) ----
+                    if(L.sampleMode != 0u && L.nLights > 0u && depth + 2u <= L.maxDepth)
+                    {
+                        const float dXi = rnd(key, depth, 3);
+                        uint32_t li = (uint32_t)mul(dXi, (float)L.nLights);
+                        li = min(li, L.nLights - 1u);
+                        const PtLight lt = lights[li];
+                        const float r1 = __fsqrt_rn(rnd(key, depth, 4)), r2 = rnd(key, depth, 5);
+                        const float a = sub(1.0f, r1), b = mul(sub(1.0f, r2), r1), c = mul(r1, r2);
+                        const float3 lp = make_float3(add(add(mul(lt.p0.x, a), mul(lt.p1.x, b)), mul(lt.p2.x, c)),
+                                                      add(add(mul(lt.p0.y, a), mul(lt.p1.y, b)), mul(lt.p2.y, c)),
+                                                      add(add(mul(lt.p0.z, a), mul(lt.p1.z, b)), mul(lt.p2.z, c)));
+                        float3 sd = make_float3(sub(pos.x, lp.x), sub(pos.y, lp.y), sub(pos.z, lp.z));
+                        const float distSq = dot3(sd, sd);
+                        sd = normalize3(sd);
+                        float ndl = dot3(f3(lt.n), sd);
+                        ndl = (lt.n.w != 0.0f) ? fabsf(ndl) : fmaxf(0.0f, ndl);
+                        float ppdf = (ndl == 0.0f) ? 0.0f : __fdiv_rn(__fdiv_rn(1.0f, lt.p0.w), ndl);
+                        ppdf = mul(ppdf, distSq);
+                        const float lightPdf = mul(invN, ppdf);
+                        const bool emits = (lt.n.w != 0.0f) || (dot3(f3(lt.n), sd) > 0.0f);
+                        const float3 emis = emits ? f3(lt.radiance) : make_float3(0, 0, 0);
+                        float3 sdir = normalize3(make_float3(sub(lp.x, pos.x), sub(lp.y, pos.y), sub(lp.z, pos.z)));
+                        const float3 lpn = nudge(lp, make_float3(-sdir.x, -sdir.y, -sdir.z));
+                        const float3 seg = make_float3(sub(lpn.x, pos.x), sub(lpn.y, pos.y), sub(lpn.z, pos.z));
+                        const float length = __fsqrt_rn(dot3(seg, seg));
+                        const float cosL = dot3(nrm, sdir);
+                        const float refl = mul(fmaxf(cosL, 0.0f), kInvPi);
+                        float pdf;
+                        if(L.sampleMode == 2u)
+                        {
+                            float bpdf = mul(cosL, kInvPi);
+                            bpdf = (bpdf <= 1.0e-5f) ? 0.0f : bpdf;
+                            pdf = add(bpdf, lightPdf);
+                        }
+                        else pdf = lightPdf;
+                        float3 srad = make_float3(mul(mul(thr.x, mul(albedo.x, refl)), emis.x),
+                                                  mul(mul(thr.y, mul(albedo.y, refl)), emis.y),
+                                                  mul(mul(thr.z, mul(albedo.z, refl)), emis.z));
+                        if(pdf == 0.0f) srad = make_float3(0, 0, 0);
+                        else
+                        {
+                            const float inv = __fdiv_rn(1.0f, pdf);
+                            srad = make_float3(mul(srad.x, inv), mul(srad.y, inv), mul(srad.z, inv));
+                        }
+                        const float3 so = nudge(pos, nrm);
+                        P.shadowRays[2 * (size_t)i] = make_float4(so.x, so.y, so.z, 1.0e-5f);
+                        P.shadowRays[2 * (size_t)i + 1] = make_float4(sdir.x, sdir.y, sdir.z,
+                                                                      mul(length, sub(1.0f, 1.0e-4f)));
+                        P.shadowRad[i] = make_float4(srad.x, srad.y, srad.z, 0.0f);
+                        shadow = true;
+                    }
+                    // ---- BxDF sample + Russian roulette (WorkFunction) ----
+                    const float xi0 = rnd(key, depth, 0), xi1 = rnd(key, depth, 1);
+                    const float ang = mul(mul(2.0f, kPi), xi1), sr = __fsqrt_rn(xi0);
+                    const float lx = mul(sr, cosf(ang)), ly = mul(sr, sinf(ang));
+                    const float lz = __fsqrt_rn(fmaxf(0.0f, sub(1.0f, add(mul(lx, lx), mul(ly, ly)))));
+                    const float bpdf = mul(lz, kInvPi);
+                    float3 wi = make_float3(add(add(mul(tng.x, lx), mul(btg.x, ly)), mul(nrm.x, lz)),
+                                            add(add(mul(tng.y, lx), mul(btg.y, ly)), mul(nrm.y, lz)),
+                                            add(add(mul(tng.z, lx), mul(btg.z, ly)), mul(nrm.z, lz)));
+                    wi = normalize3(wi);
+                    const float cw = mul(fmaxf(lz, 0.0f), kInvPi);
+                    thr.x = mul(thr.x, mul(albedo.x, cw));
+                    thr.y = mul(thr.y, mul(albedo.y, cw));
+                    thr.z = mul(thr.z, mul(albedo.z, cw));
+                    depth += 1u;
+                    bool dead = depth >= L.maxDepth;
+                    if(!dead && depth >= L.rrStart)
+                    {
+                        float pr = mul(add(add(thr.x, thr.y), thr.z), 0.33333333f);
+                        pr = fminf(fmaxf(pr, 0.1f), 1.0f);
+                        const float xr = rnd(key, depth - 1u, 2);
+                        if(xr >= pr) dead = true;
+                        else
+                        {
+                            const float inv = __fdiv_rn(1.0f, pr);
+                            thr.x = mul(thr.x, inv); thr.y = mul(thr.y, inv); thr.z = mul(thr.z, inv);
+                        }
+                    }
+                    type = 1u;
+                    if(!dead)
+                    {
+                        if(bpdf == 0.0f) { thr.x = 0.0f; thr.y = 0.0f; thr.z = 0.0f; }
+                        else
+                        {
+                            const float inv = __fdiv_rn(1.0f, bpdf);
+                            thr.x = mul(thr.x, inv); thr.y = mul(thr.y, inv); thr.z = mul(thr.z, inv);
+                        }
+                        thr.w = bpdf;
+                        const float3 no = nudge(pos, nrm);
+                        P.rays[2 * (size_t)i] = make_float4(no.x, no.y, no.z, 1.0e-4f);
+                        P.rays[2 * (size_t)i + 1] = make_float4(wi.x, wi.y, wi.z, 3.402823466e+38f);
+                        P.hits[i].x = kMissMark;
+                        P.thr[i] = thr;
+                        P.state[i] = depth | (type << 8);
+                        alive = true;
+                    }
+                }
+                P.rad[i] = rad;
+            }
+        }
+        warp_append(alive, i, nextList, nextCount);
+        warp_append(shadow, i, P.shadowList, P.counts + 2);
+    }
+}
+
+// Adds the radiance of every shadow ray that reached its light
+// (KCAccumulateShadowRaysPT; the depth limit was applied when it was cast).
+__global__ void __launch_bounds__(kPtTPB)
+k_resolve(PtPaths P)
+{
+    const uint32_t n = P.counts[2];
+    for(uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    {
+        const uint32_t i = P.shadowList[k];
+        if((P.visBits[i >> 5] >> (i & 31u)) & 1u)
+        {
+            const float4 s = P.shadowRad[i];
+            float4 r = P.rad[i];
+            r.x = add(r.x, s.x); r.y = add(r.y, s.y); r.z = add(r.z, s.z);
+            P.rad[i] = r;
+        }
+    }
+}
+
+// Film: every pixel sums its samples of the pass (slots p, p + WH, ...).
+__global__ void __launch_bounds__(kPtTPB)
+k_film(PtLaunch L, PtPaths P, float4* __restrict__ image)
+{
+    const uint32_t wh = L.width * L.height;
+    for(uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wh; p += gridDim.x * blockDim.x)
+    {
+        float4 acc = image[p];
+        for(uint32_t k = 0; k < L.samplesPerPass; k++)
+        {
+            const float4 r = P.rad[p + (size_t)k * wh];
+            acc.x = add(acc.x, r.x); acc.y = add(acc.y, r.y); acc.z = add(acc.z, r.z);
+            acc.w = add(acc.w, r.w);
+        }
+        image[p] = acc;
+    }
+}
+
+inline unsigned grid_for(uint32_t n, int smCount)
+{
+    const uint32_t want = (n + kPtTPB - 1) / kPtTPB;
+    const uint32_t cap = (uint32_t)smCount * 8u;
+    return (unsigned)(want < cap ? (want ? want : 1u) : cap);
+}
+
+} // namespace
+
+cudaError_t pt_raygen(const PtLaunch& L, const PtPaths& P, uint32_t* aliveList, uint32_t* aliveCount,
+                      int smCount, cudaStream_t st)
+{
+    k_raygen<<<grid_for(L.slots, smCount), kPtTPB, 0, st>>>(L, P, aliveList, aliveCount);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSurface* surfaces, uint32_t nSurfaces,
+                          const PtLight* lights, const float4* tris, uint32_t nTris,
+                          const uint32_t* aliveList, const uint32_t* aliveCount,
+                          uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st)
+{
+    k_shade<<<(unsigned)smCount * 8u, kPtTPB, 0, st>>>(L, P, surfaces, nSurfaces, lights, tris, nTris,
+                                                     aliveList, aliveCount, nextList, nextCount);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_resolve(const PtLaunch&, const PtPaths& P, uint32_t, int smCount, cudaStream_t st)
+{
+    k_resolve<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_film(const PtLaunch& L, const PtPaths& P, float4* image, cudaStream_t st)
+{
+    k_film<<<grid_for(L.width * L.height, 152), kPtTPB, 0, st>>>(L, P, image);
+    return cudaGetLastError();
+}
+
+} // namespace mrg

@@ -1,0 +1,315 @@
+// pt_api.cpp -- C ABI of the wavefront path tracer (include/mray_gb300.h,
+// "Path tracer" section): surface / light description, camera frame, and the
+// host-side enqueue of device-driven render passes.
+#include "mrg_ctx.h"
+#include "host_math.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+mrg_status cuda_err(cudaError_t e, const char* what)
+{
+    cudaGetLastError();
+    return mrg::set_error(e == cudaErrorMemoryAllocation ? MRG_ERR_OUT_OF_MEMORY : MRG_ERR_CUDA,
+                          std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define PT_TRY(call, what) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return cuda_err(e_, what); } while(0)
+
+struct DevGuard
+{
+    int prev = -1;
+    explicit DevGuard(int d) { if(cudaGetDevice(&prev) != cudaSuccess) prev = -1; if(prev != d) cudaSetDevice(d); }
+    ~DevGuard() { if(prev >= 0) cudaSetDevice(prev); }
+};
+
+float dot_fma(const float a[3], const float b[3])
+{
+    return std::fma(a[2], b[2], std::fma(a[1], b[1], std::fma(a[0], b[0], 0.0f)));
+}
+void cross_fma(const float a[3], const float b[3], float o[3])
+{
+    const float x = std::fma(a[1], b[2], -a[2] * b[1]);
+    const float y = std::fma(a[2], b[0], -a[0] * b[2]);
+    const float z = std::fma(a[0], b[1], -a[1] * b[0]);
+    o[0] = x; o[1] = y; o[2] = z;
+}
+void normalize_fma(float v[3])
+{
+    const float inv = 1.0f / std::sqrt(dot_fma(v, v));
+    v[0] *= inv; v[1] *= inv; v[2] *= inv;
+}
+
+// CameraPinhole's constructor (Source/Tracer/CamerasDefault.hpp:6-30).
+void camera_frame(const mrg_pt_params& p, mrg::PtCamera& c)
+{
+    const float wh = std::tan(p.fov[0] * 0.5f) * p.nearFar[0];
+    const float hh = std::tan(p.fov[1] * 0.5f) * p.nearFar[0];
+    float g[3] = { p.camGaze[0] - p.camPos[0], p.camGaze[1] - p.camPos[1], p.camGaze[2] - p.camPos[2] };
+    float r[3], u[3];
+    cross_fma(g, p.camUp, r); normalize_fma(r);
+    cross_fma(r, g, u); normalize_fma(u);
+    cross_fma(u, r, g); normalize_fma(g);
+    for(int k = 0; k < 3; k++)
+    {
+        c.pos[k] = p.camPos[k];
+        c.right[k] = r[k];
+        c.up[k] = u[k];
+        c.bottomLeft[k] = ((p.camPos[k] - r[k] * wh) - u[k] * hh) + g[k] * p.nearFar[0];
+    }
+    c.planeSize[0] = wh * 2.0f;
+    c.planeSize[1] = hh * 2.0f;
+    c.nearT = p.nearFar[0];
+    c.farT = p.nearFar[1];
+}
+
+// Light triangle in world space: ApplyP with MRay's 4-term fma Dot
+// (TransformsDefault.hpp:19-23), Triangle::Normal / Area (ShapeFunctions.h:60-73).
+void make_light(const float m[12], const float v[9], const float radiance[3], uint32_t twoSided,
+                mrg::PtLight& out)
+{
+    float w[3][3];
+    for(int c = 0; c < 3; c++)
+        for(int r = 0; r < 3; r++)
+        {
+            float acc = 0.0f;
+            acc = std::fma(m[4 * r + 0], v[3 * c + 0], acc);
+            acc = std::fma(m[4 * r + 1], v[3 * c + 1], acc);
+            acc = std::fma(m[4 * r + 2], v[3 * c + 2], acc);
+            acc = std::fma(m[4 * r + 3], 1.0f, acc);
+            w[c][r] = acc;
+        }
+    const float e0[3] = { w[1][0] - w[0][0], w[1][1] - w[0][1], w[1][2] - w[0][2] };
+    const float e1[3] = { w[2][0] - w[0][0], w[2][1] - w[0][1], w[2][2] - w[0][2] };
+    float cr[3];
+    cross_fma(e0, e1, cr);
+    const float len = std::sqrt(std::fma(cr[2], cr[2], std::fma(cr[1], cr[1], std::fma(cr[0], cr[0], 0.0f))));
+    const float area = len * 0.5f;
+    const float inv = 1.0f / len;
+    out.p0 = make_float4(w[0][0], w[0][1], w[0][2], area);
+    out.p1 = make_float4(w[1][0], w[1][1], w[1][2], 0.0f);
+    out.p2 = make_float4(w[2][0], w[2][1], w[2][2], 0.0f);
+    out.n = make_float4(cr[0] * inv, cr[1] * inv, cr[2] * inv, twoSided ? 1.0f : 0.0f);
+    out.radiance = make_float4(radiance[0], radiance[1], radiance[2], 0.0f);
+}
+
+// Uploads surfaces, lights and the primitive-indexed triangle table.
+mrg_status pt_prepare(mrg_ctx* c)
+{
+    if(!c->ptDirty) return MRG_OK;
+    const uint32_t ni = (uint32_t)c->insts.size();
+    if(c->ptDesc.size() < ni) c->ptDesc.resize(ni);
+    std::vector<mrg::PtSurface> surf(ni);
+    std::vector<mrg::PtLight> lights;
+    uint32_t maxPrim = 0;
+    for(const auto& m : c->meshes)
+        maxPrim = std::max<uint32_t>(maxPrim, m.primKeyBase + (uint32_t)(m.idx.size() / 3));
+    if(maxPrim > (1u << 28))
+        return mrg::set_error(MRG_ERR_LIMIT, "mrg_pt: primitive keys must be dense indices below 2^28");
+    std::vector<float4> tris(3ull * maxPrim, make_float4(0, 0, 0, 0));
+    for(const auto& m : c->meshes)
+    {
+        const uint32_t nt = (uint32_t)(m.idx.size() / 3);
+        for(uint32_t t = 0; t < nt; t++)
+        {
+            const float* a = &m.pos[3ull * m.idx[3ull * t]];
+            const float* b = &m.pos[3ull * m.idx[3ull * t + 1]];
+            const float* d = &m.pos[3ull * m.idx[3ull * t + 2]];
+            const size_t g = 3ull * (m.primKeyBase + t);
+            tris[g] = make_float4(a[0], a[1], a[2], 0.0f);
+            tris[g + 1] = make_float4(b[0] - a[0], b[1] - a[1], b[2] - a[2], 0.0f);
+            tris[g + 2] = make_float4(d[0] - a[0], d[1] - a[1], d[2] - a[2], 0.0f);
+        }
+    }
+    for(uint32_t i = 0; i < ni; i++)
+    {
+        const auto& in = c->insts[i];
+        const auto& d = c->ptDesc[i];
+        const auto& mesh = c->meshes[in.mesh];
+        mrg::PtSurface& s = surf[i];
+        for(int r = 0; r < 3; r++)
+        {
+            s.m[r] = make_float4(in.m[4 * r], in.m[4 * r + 1], in.m[4 * r + 2], in.m[4 * r + 3]);
+            s.inv[r] = make_float4(in.inv[4 * r], in.inv[4 * r + 1], in.inv[4 * r + 2], in.inv[4 * r + 3]);
+        }
+        s.albedo = make_float4(d.albedo[0], d.albedo[1], d.albedo[2], 0.0f);
+        s.info = make_uint4(d.kind == 2 ? 1u : 0u, (uint32_t)lights.size(), mesh.primKeyBase, 0u);
+        if(d.kind == 2)
+        {
+            const uint32_t nt = (uint32_t)(mesh.idx.size() / 3);
+            for(uint32_t t = 0; t < nt; t++)
+            {
+                float v[9];
+                for(int k = 0; k < 3; k++)
+                    for(int q = 0; q < 3; q++) v[3 * k + q] = mesh.pos[3ull * mesh.idx[3ull * t + k] + q];
+                mrg::PtLight L;
+                make_light(in.m, v, d.radiance, d.twoSided, L);
+                lights.push_back(L);
+            }
+        }
+    }
+    cudaFree(c->dPtSurfaces); cudaFree(c->dPtLights); cudaFree(c->dPtTris);
+    c->dPtSurfaces = c->dPtLights = c->dPtTris = nullptr;
+    PT_TRY(cudaMalloc(&c->dPtSurfaces, sizeof(mrg::PtSurface) * std::max<size_t>(1, surf.size())), "mrg_pt: surfaces");
+    PT_TRY(cudaMalloc(&c->dPtLights, sizeof(mrg::PtLight) * std::max<size_t>(1, lights.size())), "mrg_pt: lights");
+    PT_TRY(cudaMalloc(&c->dPtTris, sizeof(float4) * std::max<size_t>(1, tris.size())), "mrg_pt: triangles");
+    if(!surf.empty()) PT_TRY(cudaMemcpy(c->dPtSurfaces, surf.data(), sizeof(mrg::PtSurface) * surf.size(), cudaMemcpyHostToDevice), "mrg_pt: upload");
+    if(!lights.empty()) PT_TRY(cudaMemcpy(c->dPtLights, lights.data(), sizeof(mrg::PtLight) * lights.size(), cudaMemcpyHostToDevice), "mrg_pt: upload");
+    if(!tris.empty()) PT_TRY(cudaMemcpy(c->dPtTris, tris.data(), sizeof(float4) * tris.size(), cudaMemcpyHostToDevice), "mrg_pt: upload");
+    c->ptSurfaceCount = ni;
+    c->ptLightCount = (uint32_t)lights.size();
+    c->ptTriCount = maxPrim;
+    c->ptDirty = false;
+    return MRG_OK;
+}
+
+mrg_status pt_paths(mrg_ctx* c, uint32_t slots)
+{
+    if(c->ptPaths.capacity >= slots && c->ptPathMem) return MRG_OK;
+    cudaFree(c->ptPathMem);
+    c->ptPathMem = nullptr;
+    c->ptPaths = mrg::PtPaths{};
+    const size_t n = slots;
+    const size_t words = (n + 31) / 32;
+    // one allocation, every array 256-byte aligned
+    const size_t sizes[13] = { n * 32, n * 16, n * 8, n * 16, n * 16, n * 4, n * 32, n * 16,
+                               words * 4, n * 4, n * 4, n * 4, 64 };
+    size_t need = 0;
+    for(size_t sz : sizes) need += (sz + 255) & ~size_t(255);
+    char* base = nullptr;
+    PT_TRY(cudaMalloc(&base, need), "mrg_pt: path state");
+    c->ptPathMem = base;
+    size_t off = 0;
+    int k = 0;
+    auto take = [&]() { char* q = base + off; off += (sizes[k++] + 255) & ~size_t(255); return q; };
+    mrg::PtPaths& P = c->ptPaths;
+    P.rays = reinterpret_cast<float4*>(take());
+    P.hits = reinterpret_cast<uint4*>(take());
+    P.meta = reinterpret_cast<float2*>(take());
+    P.thr = reinterpret_cast<float4*>(take());
+    P.rad = reinterpret_cast<float4*>(take());
+    P.state = reinterpret_cast<uint32_t*>(take());
+    P.shadowRays = reinterpret_cast<float4*>(take());
+    P.shadowRad = reinterpret_cast<float4*>(take());
+    P.visBits = reinterpret_cast<uint32_t*>(take());
+    P.listA = reinterpret_cast<uint32_t*>(take());
+    P.listB = reinterpret_cast<uint32_t*>(take());
+    P.shadowList = reinterpret_cast<uint32_t*>(take());
+    P.counts = reinterpret_cast<uint32_t*>(take());
+    P.capacity = slots;
+    return MRG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+mrg_status mrg_pt_set_lambert(mrg_ctx* c, uint32_t inst, const float albedo[3])
+{
+    if(!c || !albedo) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_lambert: null pointer");
+    if(inst >= c->insts.size()) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_lambert: bad instance id");
+    if(c->ptDesc.size() < c->insts.size()) c->ptDesc.resize(c->insts.size());
+    auto& d = c->ptDesc[inst];
+    d.kind = 1;
+    std::memcpy(d.albedo, albedo, sizeof(d.albedo));
+    c->ptDirty = true;
+    return MRG_OK;
+}
+
+mrg_status mrg_pt_set_area_light(mrg_ctx* c, uint32_t inst, const float radiance[3], uint32_t twoSided)
+{
+    if(!c || !radiance) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_area_light: null pointer");
+    if(inst >= c->insts.size()) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_area_light: bad instance id");
+    if(c->ptDesc.size() < c->insts.size()) c->ptDesc.resize(c->insts.size());
+    auto& d = c->ptDesc[inst];
+    d.kind = 2;
+    std::memcpy(d.radiance, radiance, sizeof(d.radiance));
+    d.twoSided = twoSided;
+    c->ptDirty = true;
+    return MRG_OK;
+}
+
+mrg_status mrg_pt_camera_frame(const mrg_pt_params* p, float out[16])
+{
+    if(!p || !out) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_camera_frame: null pointer");
+    mrg::PtCamera cam;
+    camera_frame(*p, cam);
+    std::memcpy(out, cam.pos, 12); std::memcpy(out + 3, cam.bottomLeft, 12);
+    std::memcpy(out + 6, cam.right, 12); std::memcpy(out + 9, cam.up, 12);
+    out[12] = cam.planeSize[0]; out[13] = cam.planeSize[1]; out[14] = cam.nearT; out[15] = cam.farT;
+    return MRG_OK;
+}
+
+mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void* stream)
+{
+    if(!c || !p || !dImage) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: null pointer");
+    if(!c->built) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_pt_render: call mrg_build first");
+    if(p->width == 0 || p->height == 0 || p->spp == 0)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: empty image or zero samples");
+    if(p->maxDepth == 0 || p->maxDepth > 255 || p->sampleMode > MRG_PT_NEE_MIS)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: maxDepth must be in [1, 255], sampleMode in [0, 2]");
+    const uint64_t wh = (uint64_t)p->width * p->height;
+    uint32_t spp = p->samplesPerPass ? p->samplesPerPass : std::max<uint32_t>(1, (uint32_t)std::min<uint64_t>(p->spp, (1ull << 22) / wh));
+    spp = std::min(spp, p->spp);
+    if(p->spp % spp != 0) spp = 1;
+    if(wh * spp > (1ull << 26))
+        return mrg::set_error(MRG_ERR_LIMIT, "mrg_pt_render: more than 2^26 paths per pass");
+    DevGuard g(c->device);
+    for(uint32_t i = 0; i < c->insts.size(); i++)
+        if(i >= c->ptDesc.size() || c->ptDesc[i].kind == 0)
+            return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: instance " + std::to_string(i) +
+                                  " has no material or light");
+    mrg_status s = pt_prepare(c);
+    if(s != MRG_OK) return s;
+    const uint32_t slots = (uint32_t)(wh * spp);
+    if((s = pt_paths(c, slots)) != MRG_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+    mrg::PtLaunch L{};
+    L.width = p->width; L.height = p->height;
+    L.slots = slots; L.samplesPerPass = spp;
+    L.rrStart = p->rrStart; L.maxDepth = p->maxDepth;
+    L.sampleMode = p->sampleMode; L.seed = p->seed;
+    L.nLights = c->ptLightCount;
+    L.filterSigma = p->filterRadius * 0.285714f;
+    camera_frame(*p, L.cam);
+    mrg::PtPaths& P = c->ptPaths;
+    mrg::TraceScratch scr;
+    scr.workCounter = c->dScratch;
+    scr.errorFlag = c->dScratch + 1;
+    scr.stats = c->dStats;
+    const auto* surf = static_cast<const mrg::PtSurface*>(c->dPtSurfaces);
+    const auto* lights = static_cast<const mrg::PtLight*>(c->dPtLights);
+    const auto* tris = static_cast<const float4*>(c->dPtTris);
+    for(uint32_t pass = 0; pass < p->spp / spp; pass++)
+    {
+        L.sampleBase = p->sampleStart + pass * spp;
+        PT_TRY(mrg::pt_raygen(L, P, P.listA, P.counts + 0, c->smCount, st), "raygen");
+        for(uint32_t depth = 0; depth < p->maxDepth; depth++)
+        {
+            uint32_t* alive = (depth & 1u) ? P.listB : P.listA;
+            uint32_t* next = (depth & 1u) ? P.listA : P.listB;
+            uint32_t* aliveCount = P.counts + ((depth & 1u) ? 1 : 0);
+            uint32_t* nextCount = P.counts + ((depth & 1u) ? 0 : 1);
+            PT_TRY(cudaMemsetAsync(nextCount, 0, sizeof(uint32_t), st), "reset");
+            PT_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), st), "reset");
+            PT_TRY(mrg::launch_closest(c->scene, scr, P.rays, alive, 0, P.hits, P.meta, c->smCount, st,
+                                       aliveCount), "closest hit");
+            PT_TRY(mrg::pt_shade_impl(L, P, surf, c->ptSurfaceCount, lights, tris, c->ptTriCount, alive,
+                                      aliveCount, next, nextCount, c->smCount, st), "shade");
+            PT_TRY(mrg::launch_visibility(c->scene, scr, P.visBits, P.shadowRays, P.shadowList, 0,
+                                          c->smCount, st, P.counts + 2), "shadow rays");
+            PT_TRY(mrg::pt_resolve(L, P, depth, c->smCount, st), "resolve");
+        }
+        PT_TRY(mrg::pt_film(L, P, reinterpret_cast<float4*>(dImage), st), "film");
+    }
+    return MRG_OK;
+}
+
+} // extern "C"

@@ -166,9 +166,12 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
 template<bool ANY, bool STATS>
 __global__ void __launch_bounds__(kTraceTPB, MRG_TRACE_MIN_BLOCKS)
 k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
-        const uint32_t* __restrict__ rayIdx, uint32_t n,
+        const uint32_t* __restrict__ rayIdx, uint32_t nHost, const uint32_t* __restrict__ nDevice,
         uint4* __restrict__ hits, float2* __restrict__ meta, uint32_t* __restrict__ visBits)
 {
+    // The ray count comes from the host or, for casts inside a device-driven
+    // wavefront, from device memory written by the previous kernel.
+    const uint32_t n = nDevice ? *nDevice : nHost;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t laneLt = (1u << lane) - 1u;
     uint2 stack[kStackSize];
@@ -425,26 +428,26 @@ int blocks_for(int smCount)
 
 cudaError_t launch_closest(const TraceScene& sc, const TraceScratch& scr, void* rays,
                            const uint32_t* rayIdx, uint32_t n, void* hits, void* meta,
-                           int smCount, cudaStream_t st)
+                           int smCount, cudaStream_t st, const uint32_t* nDevice)
 {
-    if(n == 0) return cudaSuccess;
+    if(n == 0 && nDevice == nullptr) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(scr.workCounter, 0, sizeof(uint32_t), st);
     if(e != cudaSuccess) return e;
     k_trace<false, false><<<blocks_for<false, false>(smCount), kTraceTPB, 0, st>>>(
-        sc, scr, static_cast<float4*>(rays), rayIdx, n, static_cast<uint4*>(hits),
+        sc, scr, static_cast<float4*>(rays), rayIdx, n, nDevice, static_cast<uint4*>(hits),
         static_cast<float2*>(meta), nullptr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_visibility(const TraceScene& sc, const TraceScratch& scr, uint32_t* visBits,
                               const void* rays, const uint32_t* rayIdx, uint32_t n,
-                              int smCount, cudaStream_t st)
+                              int smCount, cudaStream_t st, const uint32_t* nDevice)
 {
-    if(n == 0) return cudaSuccess;
+    if(n == 0 && nDevice == nullptr) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(scr.workCounter, 0, sizeof(uint32_t), st);
     if(e != cudaSuccess) return e;
     k_trace<true, false><<<blocks_for<true, false>(smCount), kTraceTPB, 0, st>>>(
-        sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), rayIdx, n, nullptr,
+        sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), rayIdx, n, nDevice, nullptr,
         nullptr, visBits);
     return cudaGetLastError();
 }
@@ -458,7 +461,7 @@ cudaError_t launch_closest_stats(const TraceScene& sc, const TraceScratch& scr, 
     e = cudaMemsetAsync(scr.stats, 0, 8 * sizeof(unsigned long long), st);
     if(e != cudaSuccess) return e;
     k_trace<false, true><<<blocks_for<false, true>(smCount), kTraceTPB, 0, st>>>(
-        sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), nullptr, n, nullptr,
+        sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), nullptr, n, nullptr, nullptr,
         nullptr, nullptr);
     return cudaGetLastError();
 }

@@ -1,0 +1,94 @@
+"""Host-side mirror of MRay's path-tracer renderer over the C ABI.
+
+``PathTracer`` wraps ``mrg_pt_*``: surfaces get a Lambert material or an
+area light (MRay's primitive-backed lights: every triangle of a light surface
+is one light), ``params`` mirrors the renderer attributes (totalSPP,
+russianRouletteRange, sampleMode, film filter radius, pinhole camera) and
+``render`` accumulates samples into a device film of (R, G, B, weight).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .accel import Accelerator, _stream_ptr
+
+
+class PathTracer:
+    def __init__(self, device=0):
+        self.acc = Accelerator(device)
+        self.device = device
+        self.n_instances = 0
+        self._prim_base = 0
+
+    def add_surface(self, pos, idx, m34, cull=True):
+        """Adds a mesh instance with dense primitive keys and trans_key =
+        instance id (what the renderer's shading looks up)."""
+        nt = int(np.asarray(idx).reshape(-1, 3).shape[0])
+        mesh = self.acc.upload_mesh(pos, idx, prim_key_base=self._prim_base)
+        inst = self.n_instances
+        self.acc.add_instance(mesh, m34, cull=cull, trans_key=inst, accel_key=inst)
+        self._prim_base += nt
+        self.n_instances += 1
+        return inst
+
+    def set_lambert(self, inst, albedo):
+        a = (C.c_float * 3)(*[float(x) for x in albedo])
+        N.check(N.lib().mrg_pt_set_lambert(self.acc._h, inst, a))
+
+    def set_area_light(self, inst, radiance, two_sided=False):
+        r = (C.c_float * 3)(*[float(x) for x in radiance])
+        N.check(N.lib().mrg_pt_set_area_light(self.acc._h, inst, r, 1 if two_sided else 0))
+
+    def build(self):
+        self.acc.construct()
+
+    @staticmethod
+    def params(width, height, spp, camera, max_depth=8, rr_start=3, sample_mode=N.MRG_PT_NEE_MIS,
+               seed=0, filter_radius=1.0, samples_per_pass=0, sample_start=0):
+        p = N.MrgPtParams()
+        p.width, p.height, p.spp = width, height, spp
+        p.samplesPerPass = samples_per_pass
+        p.rrStart, p.maxDepth = rr_start, max_depth
+        p.sampleMode, p.seed = sample_mode, seed
+        p.filterRadius = filter_radius
+        p.camPos[:] = [float(x) for x in camera["pos"]]
+        p.camGaze[:] = [float(x) for x in camera["gaze"]]
+        p.camUp[:] = [float(x) for x in camera["up"]]
+        p.fov[:] = [float(x) for x in camera["fov"]]
+        p.nearFar[:] = [float(x) for x in camera["near_far"]]
+        p.sampleStart = sample_start
+        return p
+
+    @staticmethod
+    def camera_frame(p):
+        out = (C.c_float * 16)()
+        N.check(N.lib().mrg_pt_camera_frame(C.byref(p), out))
+        return np.array(out[:], np.float32)
+
+    def render(self, p, image=None, stream=None):
+        """Adds p.spp samples per pixel to `image` (a device float32 tensor
+        [H, W, 4], created zeroed when None) and returns it."""
+        import torch
+        if image is None:
+            image = torch.zeros((p.height, p.width, 4), dtype=torch.float32, device="cuda")
+        N.check(N.lib().mrg_pt_render(self.acc._h, C.byref(p), C.c_void_p(image.data_ptr()),
+                                      _stream_ptr(stream)))
+        return image
+
+    def close(self):
+        self.acc.close()
+
+
+def load_box_scene(pt, seed=0):
+    """Adds the box scene's surfaces to a PathTracer; returns the surface list."""
+    from . import scenes
+    surf = scenes.box_scene(seed)
+    for s in surf:
+        inst = pt.add_surface(s["pos"], s["idx"], s["m34"])
+        if s["kind"] == "light":
+            pt.set_area_light(inst, s["radiance"])
+        else:
+            pt.set_lambert(inst, s["albedo"])
+    pt.build()
+    return surf

@@ -89,3 +89,77 @@ def shadow_rays(origins, light):
     out = np.empty_like(origins)
     N.scenes_lib().mrgs_shadow_rays(origins.shape[0], _vp(origins), _d3(light), _vp(out))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Box scene (the small path-tracing configuration): five inward-facing walls
+# of the unit cube, two boxes rotated about y by seeded angles, one ceiling
+# quad light with radiance 15, Lambert albedos uniform in [0.1, 0.8]^3.
+# ---------------------------------------------------------------------------
+def _hash32(x):
+    x &= 0xFFFFFFFF
+    x ^= x >> 16; x = (x * 0x7feb352d) & 0xFFFFFFFF
+    x ^= x >> 15; x = (x * 0x846ca68b) & 0xFFFFFFFF
+    x ^= x >> 16
+    return x
+
+
+def _u01(seed, i):
+    return _hash32(_hash32(seed * 0x9E3779B9 + 0x1234567) ^ (i * 0x85EBCA6B)) / 4294967296.0
+
+
+def _quad(o, u, v):
+    o, u, v = (np.asarray(a, np.float64) for a in (o, u, v))
+    pos = np.array([o, o + u, o + u + v, o + v], np.float64)
+    idx = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    return pos, idx
+
+
+def _box(w, h, d):
+    faces = [((0.5, -0.5, -0.5), (0, 1, 0), (0, 0, 1)), ((-0.5, -0.5, -0.5), (0, 0, 1), (0, 1, 0)),
+             ((-0.5, 0.5, -0.5), (0, 0, 1), (1, 0, 0)), ((-0.5, -0.5, -0.5), (1, 0, 0), (0, 0, 1)),
+             ((-0.5, -0.5, 0.5), (1, 0, 0), (0, 1, 0)), ((-0.5, -0.5, -0.5), (0, 1, 0), (1, 0, 0))]
+    P, I = [], []
+    for k, (o, u, v) in enumerate(faces):
+        p, i = _quad(o, u, v)
+        P.append(p)
+        I.append(i + 4 * k)
+    s = np.array([w, h, d], np.float64)
+    return np.vstack(P) * s, np.vstack(I)
+
+
+def box_scene(seed=0):
+    """Surfaces of the box scene: list of dicts with pos, idx, m34, kind
+    ("lambert" / "light"), albedo or radiance.  36 triangles in total."""
+    I34 = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
+    walls = [((0, 0, 0), (0, 0, 1), (1, 0, 0)),      # floor, +y
+             ((0, 1, 0), (1, 0, 0), (0, 0, 1)),      # ceiling, -y
+             ((0, 0, 1), (0, 1, 0), (1, 0, 0)),      # back, -z
+             ((0, 0, 0), (0, 1, 0), (0, 0, 1)),      # left, +x
+             ((1, 0, 0), (0, 0, 1), (0, 1, 0))]      # right, -x
+    out = []
+    k = 0
+    for o, u, v in walls:
+        p, i = _quad(o, u, v)
+        alb = [0.1 + 0.7 * _u01(seed, 3 * k + j) for j in range(3)]
+        out.append(dict(pos=p.astype(np.float32), idx=i, m34=I34.copy(), kind="lambert", albedo=alb))
+        k += 1
+    for size, at in (((0.28, 0.6, 0.28), (0.33, 0.3, 0.62)), ((0.28, 0.28, 0.28), (0.68, 0.14, 0.35))):
+        p, i = _box(*size)
+        t = 2.0 * _u01(seed, 100 + k) - 1.0
+        c, s = (1 - t * t) / (1 + t * t), 2 * t / (1 + t * t)
+        m = np.array([c, 0, s, at[0], 0, 1, 0, at[1], -s, 0, c, at[2]], np.float32)
+        alb = [0.1 + 0.7 * _u01(seed, 3 * k + j) for j in range(3)]
+        out.append(dict(pos=p.astype(np.float32), idx=i, m34=m, kind="lambert", albedo=alb))
+        k += 1
+    p, i = _quad((0.35, 0.999, 0.35), (0.3, 0, 0), (0, 0, 0.3))
+    out.append(dict(pos=p.astype(np.float32), idx=i, m34=I34.copy(), kind="light",
+                    radiance=[15.0, 15.0, 15.0]))
+    return out
+
+
+def box_camera():
+    """Pinhole camera of the box scene (position, gaze point, up, fov radians, near/far)."""
+    f = 40.0 * np.pi / 180.0
+    return dict(pos=(0.5, 0.5, -1.4), gaze=(0.5, 0.5, 0.5), up=(0.0, 1.0, 0.0), fov=(f, f),
+                near_far=(0.05, 100.0))

@@ -56,6 +56,10 @@ def lib():
             getattr(L, f).argtypes = [vp, vp, vp, u32, vp, vp, vp, C.c_int]
         L.orc_cast_visibility.argtypes = [vp, vp, vp, u32, vp, C.c_int]
         L.orc_scene_stats.argtypes = [vp, vp]
+        L.orc_pt_render.argtypes = [vp, vp, vp, vp, u32, vp, C.c_int]
+        L.orc_pt_render.restype = C.c_int
+        L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
+        L.orc_pt_make_light.argtypes = [vp, vp, vp, C.c_int, vp]
         _lib = L
     return _lib
 
@@ -217,3 +221,93 @@ class RefCore:
         out = np.zeros_like(pos)
         self.R.ref_nudge(pos.shape[0], _vp(pos), _vp(np.ascontiguousarray(dirs, np.float32)), _vp(out))
         return out
+
+
+# ---------------------------------------------------------------------------
+# path-tracer oracle
+# ---------------------------------------------------------------------------
+PT_PURE, PT_NEE, PT_NEE_MIS = 0, 1, 2
+
+
+class PtParams(C.Structure):
+    _fields_ = [("width", u32), ("height", u32), ("spp", u32), ("sampleStart", u32),
+                ("rrStart", u32), ("maxDepth", u32), ("sampleMode", u32), ("seed", u32),
+                ("filterRadius", C.c_float), ("camPos", C.c_float * 3),
+                ("camBottomLeft", C.c_float * 3), ("camRight", C.c_float * 3),
+                ("camUp", C.c_float * 3), ("planeSize", C.c_float * 2),
+                ("nearT", C.c_float), ("farT", C.c_float)]
+
+
+class PtSurface(C.Structure):
+    _fields_ = [("isLight", C.c_int), ("albedo", C.c_float * 3), ("lightBase", u32),
+                ("primKeyBase", u32), ("triangles", vp), ("m", C.c_float * 12),
+                ("inv", C.c_float * 12)]
+
+
+class PtLightTri(C.Structure):
+    _fields_ = [("p0", C.c_float * 3), ("p1", C.c_float * 3), ("p2", C.c_float * 3),
+                ("n", C.c_float * 3), ("area", C.c_float), ("radiance", C.c_float * 3),
+                ("twoSided", C.c_int)]
+
+
+class PtScene:
+    """The CPU path-tracer oracle over a list of surfaces (dicts with pos,
+    idx, m34, kind, albedo / radiance), keyed like mray_gb300.pt.PathTracer:
+    dense primitive keys, instance id = surface index."""
+
+    def __init__(self, surfaces, cull=True):
+        self.L = lib()
+        self.S = Scene()
+        self._keep = []
+        prim = 0
+        lights = []
+        surf = (PtSurface * len(surfaces))()
+        for k, s in enumerate(surfaces):
+            pos = np.ascontiguousarray(s["pos"], np.float32)
+            idx = np.ascontiguousarray(s["idx"], np.uint32)
+            mid = self.S.add_mesh(pos, idx, prim_key_base=prim)
+            lm = (0x80000000 | k) if s["kind"] == "light" else k
+            self.S.add_instance(mid, s["m34"], cull=cull, lm_key=lm, trans_key=k, accel_key=k)
+            tri = np.ascontiguousarray(pos[idx].reshape(-1, 9), np.float32)
+            self._keep.append(tri)
+            sf = surf[k]
+            sf.isLight = 1 if s["kind"] == "light" else 0
+            sf.albedo[:] = [float(x) for x in s.get("albedo", (0, 0, 0))]
+            sf.lightBase = len(lights)
+            sf.primKeyBase = prim
+            sf.triangles = tri.ctypes.data_as(vp)
+            sf.m[:] = [float(x) for x in np.asarray(s["m34"], np.float32).reshape(12)]
+            if s["kind"] == "light":
+                rad = (C.c_float * 3)(*[float(x) for x in s["radiance"]])
+                m = np.ascontiguousarray(s["m34"], np.float32).reshape(12)
+                for t in range(tri.shape[0]):
+                    lt = PtLightTri()
+                    self.L.orc_pt_make_light(_vp(m), _vp(tri[t]), rad, 0, C.byref(lt))
+                    lights.append(lt)
+            prim += idx.shape[0]
+        self.S.build()
+        for k in range(len(surfaces)):
+            surf[k].inv[:] = [float(x) for x in self.S.instance_inverse(k)]
+        self.surf = surf
+        self.lights = (PtLightTri * max(1, len(lights)))(*lights)
+        self.n_lights = len(lights)
+
+    @staticmethod
+    def params(width, height, spp, camera, max_depth=8, rr_start=3, sample_mode=PT_NEE_MIS, seed=0,
+               filter_radius=1.0, sample_start=0):
+        p = PtParams()
+        p.width, p.height, p.spp, p.sampleStart = width, height, spp, sample_start
+        p.rrStart, p.maxDepth, p.sampleMode, p.seed = rr_start, max_depth, sample_mode, seed
+        p.filterRadius = filter_radius
+        pos = (C.c_float * 3)(*camera["pos"])
+        gaze = (C.c_float * 3)(*camera["gaze"])
+        up = (C.c_float * 3)(*camera["up"])
+        lib().orc_pt_camera_frame(pos, gaze, up, float(camera["fov"][0]), float(camera["fov"][1]),
+                                  float(camera["near_far"][0]), float(camera["near_far"][1]), C.byref(p))
+        return p
+
+    def render(self, p, image=None, threads=None):
+        img = np.zeros((p.height, p.width, 4), np.float32) if image is None else image
+        self.L.orc_pt_render(self.S._h, C.byref(p), self.surf, self.lights, self.n_lights,
+                             _vp(img), threads or default_threads())
+        return img

@@ -1,0 +1,407 @@
+/*
+ * pt_oracle.c -- CPU path-tracer oracle (TEST INFRASTRUCTURE ONLY).
+ *
+ * Restates the estimator of MRay's wavefront path tracer with next-event
+ * estimation and MIS (RGB variant), one path at a time:
+ *   - camera rays, pinhole + stochastic Gaussian film filter
+ *       Source/Tracer/RayGenKernels.kt.h:157-226, CamerasDefault.hpp:94-140,
+ *       Filters.h:195-233 (sigma = 0.285714 r; weight = filter / pdf = 1)
+ *   - surface work: NEE (light sample, shadow ray, MIS balance)
+ *       Source/TracerDLL/PathTracerRendererShaders.h:354-445
+ *   - BxDF sample, Russian roulette, next ray
+ *       PathTracerRendererShaders.h:203-300; DistributionFunctions.h:943-953
+ *   - light hit with MIS       PathTracerRendererShaders.h:450-517
+ *   - shadow accumulation      Source/TracerDLL/PathTracerRenderer.cu:13-31
+ *   - Lambert                  Source/Tracer/MaterialsDefault.hpp:29-110
+ *   - triangle area light      Source/Tracer/LightsDefault.hpp:24-160,
+ *                              PrimitiveDefaultTriangle.hpp:49-75
+ *   - uniform light sampler    Source/Tracer/LightSampler.hpp:6-120
+ *   - film                     Source/Tracer/TextureFilter.cu:673-697
+ * Random numbers come from a counter-based hash of (seed, pixel, sample,
+ * bounce, dimension), the same one the GPU renderer uses, so both render the
+ * same paths (MRay's own streams depend on its ray-slot scheduling and cannot
+ * be reproduced).  Intersections go through the LBVH oracle (mrg_oracle.c).
+ */
+#include "mrg_oracle.h"
+#include "pt_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define PI_F 3.14159265358979323846f
+#define INV_PI_F 0.318309886183790671538f
+
+/* PCG hash (Jarzynski & Olano, "Hash Functions for GPU Rendering", 2020). */
+static inline uint32_t pcg_hash(uint32_t v)
+{
+    uint32_t state = v * 747796405u + 2891336453u;
+    uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+static inline uint32_t path_key(uint32_t seed, uint32_t pixel, uint32_t sample)
+{
+    return pcg_hash(pcg_hash(seed ^ 0x9E3779B9u) ^ pcg_hash(pixel) ^ pcg_hash(sample + 0x632BE5ABu));
+}
+static inline float rnd(uint32_t key, uint32_t bounce, uint32_t dim)
+{
+    uint32_t h = pcg_hash(key ^ pcg_hash((bounce << 4) | dim));
+    return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
+static inline float dot3f(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static inline void cross3f(const float a[3], const float b[3], float o[3])
+{
+    float x = a[1] * b[2] - a[2] * b[1];
+    float y = a[2] * b[0] - a[0] * b[2];
+    float z = a[0] * b[1] - a[1] * b[0];
+    o[0] = x; o[1] = y; o[2] = z;
+}
+static inline void normalize3f(float v[3])
+{
+    float inv = 1.0f / sqrtf(dot3f(v, v));
+    v[0] *= inv; v[1] *= inv; v[2] *= inv;
+}
+
+/* Orthonormal basis about n (Duff et al., "Building an Orthonormal Basis,
+ * Revisited", JCGT 2017). */
+static void onb(const float n[3], float t[3], float b[3])
+{
+    float sign = copysignf(1.0f, n[2]);
+    float a = -1.0f / (sign + n[2]);
+    float bb = n[0] * n[1] * a;
+    t[0] = 1.0f + sign * n[0] * n[0] * a; t[1] = sign * bb; t[2] = -sign * n[0];
+    b[0] = bb; b[1] = sign + n[1] * n[1] * a; b[2] = -n[1];
+}
+
+typedef struct
+{
+    const orc_scene*          scene;
+    const orc_pt_params*      p;
+    const orc_pt_surface*     surfaces;     /* per instance */
+    const orc_pt_light_tri*   lights;
+    uint32_t                  nLights;
+    float*                    image;
+    atomic_uint               nextRow;
+} pt_job;
+
+/* One ray cast through the oracle accelerator. */
+static int cast1(const orc_scene* s, const float o[3], const float d[3], float tmin, float tmax,
+                 orc_hit_keys* hk, orc_meta_hit* mh, uint32_t* inst, float* tOut)
+{
+    orc_ray_gmem r;
+    memcpy(r.pos, o, 12); memcpy(r.dir, d, 12);
+    r.tMin = tmin; r.tMax = tmax;
+    uint32_t in = 0xFFFFFFFFu;
+    orc_cast_closest(s, &r, NULL, 1, hk, mh, &in, 1);
+    *inst = in;
+    *tOut = r.tMax;
+    return in != 0xFFFFFFFFu;
+}
+static int visible1(const orc_scene* s, const float o[3], const float d[3], float tmin, float tmax)
+{
+    orc_ray_gmem r;
+    memcpy(r.pos, o, 12); memcpy(r.dir, d, 12);
+    r.tMin = tmin; r.tMax = tmax;
+    uint32_t bits = 0;
+    orc_cast_visibility(s, &r, NULL, 1, &bits, 1);
+    return (bits & 1u) != 0u;
+}
+
+/* Surface point of a hit: barycentric position in instance space, moved to
+ * world space with ApplyP; geometric normal with ApplyN (transpose of the
+ * inverse, TransformsDefault.hpp:19-36). */
+static void surface_of(const orc_pt_surface* sf, const float* tri9 /* v0 v1 v2 local */,
+                       float u, float v, float pos[3], float n[3])
+{
+    float e0[3] = { tri9[3] - tri9[0], tri9[4] - tri9[1], tri9[5] - tri9[2] };
+    float e1[3] = { tri9[6] - tri9[0], tri9[7] - tri9[1], tri9[8] - tri9[2] };
+    float pl[3];
+    for(int k = 0; k < 3; k++) pl[k] = tri9[k] + e0[k] * u + e1[k] * v;
+    for(int r = 0; r < 3; r++)
+        pos[r] = sf->m[4 * r] * pl[0] + sf->m[4 * r + 1] * pl[1] + sf->m[4 * r + 2] * pl[2] + sf->m[4 * r + 3];
+    float nl[3];
+    cross3f(e0, e1, nl);
+    /* ApplyN: inv^T * n */
+    for(int c = 0; c < 3; c++)
+        n[c] = sf->inv[c] * nl[0] + sf->inv[4 + c] * nl[1] + sf->inv[8 + c] * nl[2];
+    normalize3f(n);
+}
+
+static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, float outRad[3])
+{
+    const orc_pt_params* P = J->p;
+    const uint32_t pixel = y * P->width + x;
+    const uint32_t key = path_key(P->seed, pixel, sample);
+    outRad[0] = outRad[1] = outRad[2] = 0.0f;
+
+    /* camera ray: Gaussian offset by Box-Muller, weight filter/pdf = 1 */
+    float sigma = P->filterRadius * 0.285714f;
+    float u1 = rnd(key, 0, 6), u2 = rnd(key, 0, 7);
+    float rr = sigma * sqrtf(-2.0f * logf(1.0f - u1));
+    float ox = rr * cosf(2.0f * PI_F * u2), oy = rr * sinf(2.0f * PI_F * u2);
+    float dx = P->planeSize[0] / (float)P->width, dy = P->planeSize[1] / (float)P->height;
+    /* (sampleId + (offset + 0.5)) * delta, CamerasDefault.hpp:102-108 */
+    float sx = ((float)x + (ox + 0.5f)) * dx, sy = ((float)y + (oy + 0.5f)) * dy;
+    float sp[3], dir[3], org[3];
+    for(int k = 0; k < 3; k++)
+    {
+        sp[k] = P->camBottomLeft[k] + sx * P->camRight[k] + sy * P->camUp[k];
+        dir[k] = sp[k] - P->camPos[k];
+        org[k] = P->camPos[k];
+    }
+    normalize3f(dir);
+    float tmin = P->nearT, tmax = P->farT;
+
+    float thr[3] = { 1.0f, 1.0f, 1.0f };
+    float rad[3] = { 0.0f, 0.0f, 0.0f };
+    uint32_t depth = 0;
+    int type = 0;           /* 0 camera, 1 path (diffuse) */
+    float prevPdf = 0.0f;
+    const float invN = J->nLights ? 1.0f / (float)J->nLights : 0.0f;
+
+    for(;;)
+    {
+        orc_hit_keys hk; orc_meta_hit mh; uint32_t inst; float t;
+        if(!cast1(J->scene, org, dir, tmin, tmax, &hk, &mh, &inst, &t)) break;
+        const orc_pt_surface* sf = &J->surfaces[inst];
+        uint32_t localPrim = hk.primKey - sf->primKeyBase;
+        const float* tri9 = &sf->triangles[9 * localPrim];
+        /* MetaHit = (w, u); v = 1 - w - u */
+        float bu = mh.bary[1];
+        float bv = 1.0f - mh.bary[0] - mh.bary[1];
+        float pos[3], gn[3];
+        surface_of(sf, tri9, bu, bv, pos, gn);
+
+        if(sf->isLight)
+        {
+            if(P->sampleMode == ORC_PT_NEE && type != 0) break;
+            float tp[3] = { thr[0], thr[1], thr[2] };
+            if(P->sampleMode == ORC_PT_NEE_MIS && type == 1)
+            {
+                const orc_pt_light_tri* L = &J->lights[sf->lightBase + localPrim];
+                /* PdfSolidAngle(hit, ray.pos, ray.dir) * 1/N */
+                float ndl = -(L->n[0] * dir[0] + L->n[1] * dir[1] + L->n[2] * dir[2]);
+                ndl = L->twoSided ? fabsf(ndl) : fmaxf(0.0f, ndl);
+                float dd[3] = { org[0] - pos[0], org[1] - pos[1], org[2] - pos[2] };
+                float lpdf = (ndl == 0.0f) ? 0.0f : (1.0f / L->area) / ndl;
+                lpdf *= dot3f(dd, dd);
+                lpdf *= invN;
+                float misPdf = prevPdf + lpdf;
+                for(int k = 0; k < 3; k++) tp[k] *= prevPdf;
+                if(misPdf == 0.0f) { tp[0] = tp[1] = tp[2] = 0.0f; }
+                else { float inv = 1.0f / misPdf; for(int k = 0; k < 3; k++) tp[k] *= inv; }
+            }
+            const orc_pt_light_tri* L = &J->lights[sf->lightBase + localPrim];
+            float wo[3] = { -dir[0], -dir[1], -dir[2] };
+            float ndl = dot3f(L->n, wo);
+            int emits = L->twoSided ? 1 : (ndl > 0.0f);
+            if(emits && depth + 1u <= P->maxDepth)
+                for(int k = 0; k < 3; k++) rad[k] += L->radiance[k] * tp[k];
+            break;
+        }
+
+        const float* albedo = sf->albedo;
+        /* shading normal = geometric normal facing the incoming ray */
+        float nrm[3] = { gn[0], gn[1], gn[2] };
+        float tng[3], btg[3];
+        onb(nrm, tng, btg);
+
+        /* ---- NEE ---- */
+        if(P->sampleMode != ORC_PT_PURE && J->nLights > 0)
+        {
+            float dXi = rnd(key, depth, 3);
+            uint32_t li = (uint32_t)(dXi * (float)J->nLights);
+            if(li > J->nLights - 1u) li = J->nLights - 1u;
+            const orc_pt_light_tri* L = &J->lights[li];
+            float r1 = sqrtf(rnd(key, depth, 4)), r2 = rnd(key, depth, 5);
+            float a = 1.0f - r1, b = (1.0f - r2) * r1, c = r1 * r2;
+            float lp[3];
+            for(int k = 0; k < 3; k++) lp[k] = L->p0[k] * a + L->p1[k] * b + L->p2[k] * c;
+            float sd[3] = { pos[0] - lp[0], pos[1] - lp[1], pos[2] - lp[2] };
+            float distSq = dot3f(sd, sd);
+            normalize3f(sd);
+            float ndl = dot3f(L->n, sd);
+            ndl = L->twoSided ? fabsf(ndl) : fmaxf(0.0f, ndl);
+            float ppdf = (ndl == 0.0f) ? 0.0f : (1.0f / L->area) / ndl;
+            ppdf *= distSq;
+            float lightPdf = invN * ppdf;
+            /* EmitViaSurfacePoint with wO = normalize(surface - light point) */
+            float emis[3] = { 0, 0, 0 };
+            if(L->twoSided || dot3f(L->n, sd) > 0.0f)
+                for(int k = 0; k < 3; k++) emis[k] = L->radiance[k];
+            /* SampledRay: direction, nudged light point, segment length */
+            float sdir[3] = { lp[0] - pos[0], lp[1] - pos[1], lp[2] - pos[2] };
+            normalize3f(sdir);
+            float nd[3] = { -sdir[0], -sdir[1], -sdir[2] };
+            float lpn[3];
+            orc_nudge(lp, nd, lpn);
+            float seg[3] = { lpn[0] - pos[0], lpn[1] - pos[1], lpn[2] - pos[2] };
+            float length = sqrtf(dot3f(seg, seg));
+            float cosL = dot3f(nrm, sdir);
+            float refl = fmaxf(cosL, 0.0f) * INV_PI_F;
+            float pdf;
+            if(P->sampleMode == ORC_PT_NEE_MIS)
+            {
+                float bpdf = cosL * INV_PI_F;
+                bpdf = (bpdf <= 1.0e-5f) ? 0.0f : bpdf;
+                pdf = bpdf + lightPdf;
+            }
+            else pdf = lightPdf;
+            float srad[3];
+            for(int k = 0; k < 3; k++) srad[k] = thr[k] * (albedo[k] * refl) * emis[k];
+            if(pdf == 0.0f) srad[0] = srad[1] = srad[2] = 0.0f;
+            else { float inv = 1.0f / pdf; for(int k = 0; k < 3; k++) srad[k] *= inv; }
+            float sorg[3];
+            orc_nudge(pos, nrm, sorg);
+            if(depth + 2u <= P->maxDepth &&
+               visible1(J->scene, sorg, sdir, 1.0e-5f, length * (1.0f - 1.0e-4f)))
+                for(int k = 0; k < 3; k++) rad[k] += srad[k];
+        }
+
+        /* ---- BxDF sample (Lambert, cosine hemisphere) ---- */
+        float xi0 = rnd(key, depth, 0), xi1 = rnd(key, depth, 1);
+        float ang = 2.0f * PI_F * xi1, sr = sqrtf(xi0);
+        float lx = sr * cosf(ang), ly = sr * sinf(ang);
+        float lz = sqrtf(fmaxf(0.0f, 1.0f - (lx * lx + ly * ly)));
+        float bpdf = lz * INV_PI_F;
+        float wi[3];
+        for(int k = 0; k < 3; k++) wi[k] = tng[k] * lx + btg[k] * ly + nrm[k] * lz;
+        normalize3f(wi);
+        for(int k = 0; k < 3; k++) thr[k] *= albedo[k] * (fmaxf(lz, 0.0f) * INV_PI_F);
+        depth += 1u;
+        int dead = depth >= P->maxDepth;
+        if(!dead && depth >= P->rrStart)
+        {
+            float pr = (thr[0] + thr[1] + thr[2]) * 0.33333333f;
+            pr = fminf(fmaxf(pr, 0.1f), 1.0f);
+            float xr = rnd(key, depth - 1u, 2);
+            if(xr >= pr) dead = 1;
+            else { float inv = 1.0f / pr; for(int k = 0; k < 3; k++) thr[k] *= inv; }
+        }
+        type = 1;
+        if(dead) break;
+        if(bpdf == 0.0f) { thr[0] = thr[1] = thr[2] = 0.0f; }
+        else { float inv = 1.0f / bpdf; for(int k = 0; k < 3; k++) thr[k] *= inv; }
+        prevPdf = bpdf;
+        orc_nudge(pos, nrm, org);
+        memcpy(dir, wi, 12);
+        tmin = 1.0e-4f;
+        tmax = 3.402823466e+38f;
+    }
+    outRad[0] = rad[0]; outRad[1] = rad[1]; outRad[2] = rad[2];
+}
+
+static void* pt_worker(void* arg)
+{
+    pt_job* J = (pt_job*)arg;
+    const orc_pt_params* P = J->p;
+    for(;;)
+    {
+        uint32_t y = atomic_fetch_add(&J->nextRow, 1u);
+        if(y >= P->height) break;
+        for(uint32_t x = 0; x < P->width; x++)
+        {
+            float* px = &J->image[4ull * (y * P->width + x)];
+            for(uint32_t s = 0; s < P->spp; s++)
+            {
+                float r[3];
+                trace_sample(J, x, y, P->sampleStart + s, r);
+                px[0] += r[0]; px[1] += r[1]; px[2] += r[2]; px[3] += 1.0f;
+            }
+        }
+    }
+    return NULL;
+}
+
+int orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
+                  const orc_pt_light_tri* lights, uint32_t nLights, float* image, int nthreads)
+{
+    if(!s || !p || !surfaces || !image) return -1;
+    pt_job J;
+    memset(&J, 0, sizeof(J));
+    J.scene = s; J.p = p; J.surfaces = surfaces; J.lights = lights; J.nLights = nLights;
+    J.image = image;
+    atomic_init(&J.nextRow, 0u);
+    if(nthreads < 1) nthreads = 1;
+    if(nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    int started = 0;
+    for(int t = 1; t < nthreads; t++)
+        if(pthread_create(&th[started], NULL, pt_worker, &J) == 0) started++;
+    pt_worker(&J);
+    for(int t = 0; t < started; t++) pthread_join(th[t], NULL);
+    return 0;
+}
+
+/* CameraPinhole constructor (Source/Tracer/CamerasDefault.hpp:6-30): image
+ * plane at distance near, frame from gaze point and up. */
+static void cross_fma(const float a[3], const float b[3], float o[3])
+{
+    float x = fmaf(a[1], b[2], -a[2] * b[1]);
+    float y = fmaf(a[2], b[0], -a[0] * b[2]);
+    float z = fmaf(a[0], b[1], -a[1] * b[0]);
+    o[0] = x; o[1] = y; o[2] = z;
+}
+static void normalize_fma(float v[3])
+{
+    float l = sqrtf(fmaf(v[2], v[2], fmaf(v[1], v[1], fmaf(v[0], v[0], 0.0f))));
+    float inv = 1.0f / l;
+    v[0] *= inv; v[1] *= inv; v[2] *= inv;
+}
+void orc_pt_camera_frame(const float pos[3], const float gaze[3], const float up[3],
+                         float fovX, float fovY, float nearT, float farT, orc_pt_params* p)
+{
+    float wh = tanf(fovX * 0.5f) * nearT;
+    float hh = tanf(fovY * 0.5f) * nearT;
+    float g[3] = { gaze[0] - pos[0], gaze[1] - pos[1], gaze[2] - pos[2] };
+    float r[3], u[3];
+    cross_fma(g, up, r); normalize_fma(r);
+    cross_fma(r, g, u); normalize_fma(u);
+    cross_fma(u, r, g); normalize_fma(g);
+    for(int k = 0; k < 3; k++)
+    {
+        p->camPos[k] = pos[k];
+        p->camRight[k] = r[k];
+        p->camUp[k] = u[k];
+        p->camBottomLeft[k] = ((pos[k] - r[k] * wh) - u[k] * hh) + g[k] * nearT;
+    }
+    p->planeSize[0] = wh * 2.0f;
+    p->planeSize[1] = hh * 2.0f;
+    p->nearT = nearT;
+    p->farT = farT;
+}
+
+/* World-space light triangle from instance-space vertices (ApplyP with the
+ * 4-term fma Dot, TransformsDefault.hpp:19-23; Normal / Area,
+ * ShapeFunctions.h:60-73). */
+void orc_pt_make_light(const float m[12], const float* v9, const float radiance[3], int twoSided,
+                       orc_pt_light_tri* out)
+{
+    float w[3][3];
+    for(int c = 0; c < 3; c++)
+        for(int r = 0; r < 3; r++)
+        {
+            float acc = 0.0f;
+            acc = fmaf(m[4 * r + 0], v9[3 * c + 0], acc);
+            acc = fmaf(m[4 * r + 1], v9[3 * c + 1], acc);
+            acc = fmaf(m[4 * r + 2], v9[3 * c + 2], acc);
+            acc = fmaf(m[4 * r + 3], 1.0f, acc);
+            w[c][r] = acc;
+        }
+    memcpy(out->p0, w[0], 12); memcpy(out->p1, w[1], 12); memcpy(out->p2, w[2], 12);
+    float e0[3] = { w[1][0] - w[0][0], w[1][1] - w[0][1], w[1][2] - w[0][2] };
+    float e1[3] = { w[2][0] - w[0][0], w[2][1] - w[0][1], w[2][2] - w[0][2] };
+    float c[3];
+    c[0] = fmaf(e0[1], e1[2], -e0[2] * e1[1]);
+    c[1] = fmaf(e0[2], e1[0], -e0[0] * e1[2]);
+    c[2] = fmaf(e0[0], e1[1], -e0[1] * e1[0]);
+    float len = sqrtf(fmaf(c[2], c[2], fmaf(c[1], c[1], fmaf(c[0], c[0], 0.0f))));
+    out->area = len * 0.5f;
+    float inv = 1.0f / len;
+    out->n[0] = c[0] * inv; out->n[1] = c[1] * inv; out->n[2] = c[2] * inv;
+    memcpy(out->radiance, radiance, 12);
+    out->twoSided = twoSided;
+}
