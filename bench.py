@@ -269,6 +269,7 @@ def gpu_arm(args):
                   "bvh_device_mb": round(st["deviceBytes"] / 2**20, 1),
                   "blas_nodes": st["blasNodes"]},
     }
+    line["extra"].update(box_scene_pt(args, dev))
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, idx, m, rays_np, budget_s=args.cpu_seconds)
     if ws > 1:
@@ -276,6 +277,34 @@ def gpu_arm(args):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line))
+
+
+def box_scene_pt(args, dev):
+    """Box-scene path tracing (256x256, 16 spp, depth 8, RR from depth 3,
+    NEE + MIS): samples per second and paths per second on the device."""
+    import torch
+    from mray_gb300.pt import PathTracer, load_box_scene
+    from mray_gb300 import scenes
+    pt = PathTracer(dev.index or 0)
+    load_box_scene(pt, 0)
+    cam = scenes.box_camera()
+    p = PathTracer.params(256, 256, 16, cam, max_depth=8, rr_start=3, seed=0)
+    img = pt.render(p)
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = max(3, min(args.steps, 20))
+    e0.record()
+    for r in range(reps):
+        p.sampleStart = 16 * (r + 1)
+        pt.render(p, image=img)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    pt.close()
+    return {"box_pt_ms_per_16spp": round(ms, 3),
+            "box_pt_spp_per_s": round(16.0 / (ms * 1e-3), 1),
+            "box_pt_mpaths_per_s": round(256 * 256 * 16 / (ms * 1e-3) / 1e6, 1)}
 
 
 def oracle_scene(pos, idx, m):
