@@ -218,6 +218,23 @@ typedef struct mrg_pt_params
  * material / light group to a surface (TracerI::CreateSurface, CreateLightSurface).
  * Rendering requires trans_key index = instance id and dense primitive keys. */
 mrg_status mrg_pt_set_lambert(mrg_ctx* ctx, uint32_t instance_id, const float albedo[3]);
+
+/* Material groups (Source/Tracer/MaterialsDefault.h): Lambert, Reflect,
+ * Refract (smooth dielectric; RGB uses the first Cauchy coefficient as the
+ * index of refraction, front / back), Unreal (GGX metallic-roughness).
+ * Refracting surfaces need their instance added without back-face culling. */
+#define MRG_MAT_LAMBERT 0u
+#define MRG_MAT_REFLECT 1u
+#define MRG_MAT_REFRACT 2u
+#define MRG_MAT_UNREAL  3u
+typedef struct mrg_pt_material
+{
+    uint32_t type;               /* MRG_MAT_* */
+    float    albedo[3];
+    float    roughness, metallic, specular;
+    float    iorFront, iorBack;
+} mrg_pt_material;
+mrg_status mrg_pt_set_material(mrg_ctx* ctx, uint32_t instance_id, const mrg_pt_material* material);
 mrg_status mrg_pt_set_area_light(mrg_ctx* ctx, uint32_t instance_id, const float radiance[3],
                                  uint32_t two_sided);
 

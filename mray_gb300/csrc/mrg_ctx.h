@@ -68,8 +68,11 @@ struct mrg_ctx
     // path tracer: per-instance surface description, device tables, path state
     struct PtSurfaceDesc
     {
-        int      kind = 0;            // 0 unset, 1 Lambert, 2 area light
+        int      kind = 0;            // 0 unset, 1 material, 2 area light
+        uint32_t material = 0;        // MRG_MAT_*
         float    albedo[3] = { 0, 0, 0 };
+        float    roughness = 0, metallic = 0, specular = 0;
+        float    iorFront = 1, iorBack = 1;
         float    radiance[3] = { 0, 0, 0 };
         uint32_t twoSided = 0;
     };

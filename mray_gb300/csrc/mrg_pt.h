@@ -8,12 +8,21 @@
 namespace mrg {
 
 // Per surface (= per instance; indexed by the transform key's index portion).
+enum PtMaterial : uint32_t
+{
+    kMatLambert = 0,    // MaterialsDefault.hpp:29-110
+    kMatReflect = 1,    // perfect mirror
+    kMatRefract = 2,    // smooth dielectric, Fresnel-sampled (:230-355)
+    kMatUnreal  = 3     // GGX metallic-roughness + Burley diffuse (:465-720)
+};
+
 struct __align__(16) PtSurface
 {
     float4 m[3];        // local -> world rows
     float4 inv[3];      // world -> local rows (normals use its transpose)
-    float4 albedo;      // Lambert albedo (xyz)
-    uint4  info;        // x: 1 if light, y: first light index, z: primitive key base, w: 0
+    float4 albedo;      // xyz albedo, w: roughness
+    float4 mat;         // x: metallic, y: specular, z: front IoR, w: back IoR
+    uint4  info;        // x: 1 if light, y: first light index, z: primitive key base, w: PtMaterial
 };
 
 // One light per emitting triangle (MRay's primitive-backed lights,

@@ -90,6 +90,164 @@ __device__ __forceinline__ void onb(float3 n, float3& t, float3& b)
     b = make_float3(bb, add(sign, mul(mul(n.y, n.y), a)), -n.y);
 }
 
+
+// ---------------------------------------------------------------------------
+// Materials (MaterialsDefault.hpp, DistributionFunctions.h), unfused float
+// arithmetic mirroring the oracle.  Vectors are in the tangent frame (z = n).
+// ---------------------------------------------------------------------------
+constexpr float kSpecularThreshold = 0.95f;   // MaterialC.h:11
+
+__device__ __forceinline__ float sqrt_max(float x) { return __fsqrt_rn(fmaxf(x, 0.0f)); }
+
+__device__ __forceinline__ float d_ggx(float ndh, float alpha)
+{
+    const float a2 = mul(alpha, alpha);
+    float den = add(mul(mul(ndh, ndh), sub(a2, 1.0f)), 1.0f);
+    den = mul(den, den);
+    den = mul(den, kPi);
+    return __fdiv_rn(a2, den);
+}
+__device__ __forceinline__ float lambda_smith(float3 v, float alpha)
+{
+    const float a2 = mul(alpha, alpha);
+    const float inner = __fdiv_rn(mul(a2, add(mul(v.x, v.x), mul(v.y, v.y))), mul(v.z, v.z));
+    return mul(sub(__fsqrt_rn(add(1.0f, inner)), 1.0f), 0.5f);
+}
+__device__ __forceinline__ float g_single(float3 v, float alpha)
+{
+    return __fdiv_rn(1.0f, add(1.0f, lambda_smith(v, alpha)));
+}
+__device__ __forceinline__ float g_correlated(float3 o, float3 i, float alpha)
+{
+    return __fdiv_rn(1.0f, add(add(lambda_smith(o, alpha), lambda_smith(i, alpha)), 1.0f));
+}
+__device__ __forceinline__ float schlick1(float vdh, float f0)
+{
+    const float pw = sub(1.0f, vdh);
+    const float pw2 = mul(pw, pw);
+    const float pw5 = mul(mul(pw2, pw2), pw);
+    return add(mul(sub(1.0f, f0), pw5), f0);
+}
+__device__ __forceinline__ float vndf_pdf(float3 V, float3 H, float alpha)
+{
+    const float vdh = fmaxf(0.0f, dot3(H, V));
+    const float ndh = fmaxf(0.0f, H.z);
+    const float ndv = fmaxf(0.0f, V.z);
+    const float D = d_ggx(ndh, alpha);
+    const float G = g_single(V, alpha);
+    if(ndv == 0.0f) return 0.0f;
+    return __fdiv_rn(mul(mul(vdh, D), G), ndv);
+}
+// Heitz 2018, "Sampling the GGX Distribution of Visible Normals".
+__device__ __forceinline__ float3 vndf_sample(float3 V, float a, float xi0, float xi1)
+{
+    float3 vh = normalize3(make_float3(mul(a, V.x), mul(a, V.y), V.z));
+    const float len2 = add(mul(vh.x, vh.x), mul(vh.y, vh.y));
+    float3 T1;
+    if(len2 > 0.0f)
+    {
+        const float rs = __fdiv_rn(1.0f, __fsqrt_rn(len2));
+        T1 = make_float3(mul(-vh.y, rs), mul(vh.x, rs), 0.0f);
+    }
+    else T1 = make_float3(1.0f, 0.0f, 0.0f);
+    const float3 T2 = cross3(vh, T1);
+    const float r = __fsqrt_rn(xi0);
+    const float phi = mul(mul(2.0f, kPi), xi1);
+    const float t1 = mul(r, cosf(phi));
+    float t2 = mul(r, sinf(phi));
+    const float sS = mul(0.5f, add(1.0f, vh.z));
+    t2 = add(mul(sub(1.0f, sS), __fsqrt_rn(sub(1.0f, mul(t1, t1)))), mul(sS, t2));
+    const float val = sub(sub(1.0f, mul(t1, t1)), mul(t2, t2));
+    const float sq = sqrt_max(val);
+    const float3 nh = make_float3(add(add(mul(t1, T1.x), mul(t2, T2.x)), mul(sq, vh.x)),
+                                  add(add(mul(t1, T1.y), mul(t2, T2.y)), mul(sq, vh.y)),
+                                  add(add(mul(t1, T1.z), mul(t2, T2.z)), mul(sq, vh.z)));
+    const float3 nm = make_float3(mul(a, nh.x), mul(a, nh.y), sqrt_max(nh.z));
+    const float n2 = dot3(nm, nm);
+    if(n2 < 1.0e-5f) return make_float3(0.0f, 0.0f, 1.0f);
+    const float rs = __fdiv_rn(1.0f, __fsqrt_rn(n2));
+    return make_float3(mul(nm.x, rs), mul(nm.y, rs), mul(nm.z, rs));
+}
+__device__ __forceinline__ float burley(float ndl, float ndv, float ldh, float rough)
+{
+    const float fd90 = add(0.5f, mul(mul(mul(2.0f, rough), ldh), ldh));
+    const float p1 = sub(1.0f, ndl), p2 = sub(1.0f, ndv);
+    const float a = add(1.0f, mul(sub(fd90, 1.0f), mul(mul(mul(mul(p1, p1), p1), p1), p1)));
+    const float b = add(1.0f, mul(sub(fd90, 1.0f), mul(mul(mul(mul(p2, p2), p2), p2), p2)));
+    return mul(a, b);
+}
+__device__ __forceinline__ float unreal_ratio(const PtSurface& m, float avg)
+{
+    float integ = mul(mul(2.0f, kPi), avg);
+    integ = mul(integ, sub(1.0f, m.mat.x));
+    const float specR = add(mul(m.mat.y, sub(1.0f, m.mat.x)), mul(avg, m.mat.x));
+    const float total = add(specR, integ);
+    return (total == 0.0f) ? 0.0f : __fdiv_rn(integ, total);
+}
+__device__ __forceinline__ float avg_albedo(const PtSurface& m)
+{
+    return mul(add(add(m.albedo.x, m.albedo.y), m.albedo.z), 0.3333f);
+}
+__device__ __forceinline__ float specularity(const PtSurface& m)
+{
+    if(m.info.w == kMatReflect || m.info.w == kMatRefract) return 1.0f;
+    if(m.info.w == kMatUnreal) return sub(1.0f, unreal_ratio(m, avg_albedo(m)));
+    return 0.0f;
+}
+__device__ __forceinline__ float f0_of(const PtSurface& m, float alb)
+{
+    return add(mul(mul(m.mat.y, 0.08f), sub(1.0f, m.mat.x)), mul(alb, m.mat.x));
+}
+// UnrealMaterial::Evaluate + Pdf (V, L in the tangent frame).
+__device__ __forceinline__ float3 unreal_eval(const PtSurface& m, float3 V, float3 L, float& pdfOut)
+{
+    const float rough = m.albedo.w;
+    const float alpha = mul(rough, rough);
+    const float3 H = normalize3(make_float3(add(L.x, V.x), add(L.y, V.y), add(L.z, V.z)));
+    const float ldh = fmaxf(0.0f, dot3(L, H));
+    const float vdh = fmaxf(0.0f, dot3(V, H));
+    const float ndh = fmaxf(0.0f, H.z);
+    const float ndv = fmaxf(0.0f, V.z);
+    const float D = d_ggx(ndh, alpha);
+    const bool dBad = isnan(D) || isinf(D);
+    const float Dn = dBad ? 0.0f : D;
+    float G = g_correlated(V, L, alpha);
+    G = (ldh == 0.0f) ? 0.0f : G;
+    G = (vdh == 0.0f) ? 0.0f : G;
+    const float ndl = fmaxf(0.0f, L.z);
+    const float corr = burley(ndl, ndv, ldh, rough);
+    const float alb[3] = { m.albedo.x, m.albedo.y, m.albedo.z };
+    float out[3];
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+    {
+        const float F = schlick1(vdh, f0_of(m, alb[k]));
+        const float spec = (ndv == 0.0f) ? 0.0f : __fdiv_rn(mul(mul(mul(Dn, F), G), 0.25f), ndv);
+        const float diff = mul(mul(mul(ndl, mul(sub(1.0f, m.mat.x), alb[k])), kInvPi), corr);
+        out[k] = add(diff, spec);
+    }
+    const float ratio = unreal_ratio(m, avg_albedo(m));
+    float pd = mul(L.z, kInvPi);
+    pd = (pd <= 1.0e-5f) ? 0.0f : pd;
+    float ps = vndf_pdf(V, H, alpha);
+    ps = dBad ? 0.0f : ps;
+    ps = (vdh == 0.0f) ? 0.0f : __fdiv_rn(ps, mul(4.0f, vdh));
+    pdfOut = add(mul(pd, ratio), mul(ps, sub(1.0f, ratio)));
+    return make_float3(out[0], out[1], out[2]);
+}
+__device__ __forceinline__ float fresnel_dielectric(float cosF, float etaF, float etaB)
+{
+    const float sinF = sqrt_max(sub(1.0f, mul(cosF, cosF)));
+    const float sinB = mul(__fdiv_rn(etaF, etaB), sinF);
+    if(sinF >= 1.0f) return 1.0f;
+    const float cosB = sqrt_max(sub(1.0f, mul(sinB, sinB)));
+    float par = __fdiv_rn(sub(mul(etaB, cosF), mul(etaF, cosB)), add(mul(etaB, cosF), mul(etaF, cosB)));
+    par = mul(par, par);
+    float per = __fdiv_rn(sub(mul(etaF, cosF), mul(etaB, cosB)), add(mul(etaF, cosF), mul(etaB, cosB)));
+    per = mul(per, per);
+    return mul(add(par, per), 0.5f);
+}
+
 __device__ __forceinline__ uint32_t slot_pixel(const PtLaunch& L, uint32_t i) { return i % (L.width * L.height); }
 __device__ __forceinline__ uint32_t slot_sample(const PtLaunch& L, uint32_t i)
 {
@@ -209,7 +367,7 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                 {
                     // ---- light hit (LightWorkFunction[WithNEE]) ----
                     const PtLight lt = lights[sf.info.y + localPrim];
-                    const bool neeOnly = (L.sampleMode == 1u && type != 0u);
+                    const bool neeOnly = (L.sampleMode == 1u && type == 1u);
                     if(!neeOnly)
                     {
                         float3 tp = f3(thr);
@@ -242,12 +400,19 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                 }
                 else
                 {
-                    const float3 albedo = f3(sf.albedo);
+                    // GenerateSurface flips the normal towards the ray
+                    // (PrimitiveDefaultTriangle.hpp:480-486).
+                    const bool backSide = dot3(gn, dir) > 0.0f;
+                    if(backSide) gn = make_float3(-gn.x, -gn.y, -gn.z);
                     const float3 nrm = gn;
                     float3 tng, btg;
                     onb(nrm, tng, btg);
-                    // ---- NEE (WorkFunctionNEE) ----
-                    if(L.sampleMode != 0u && L.nLights > 0u && depth + 2u <= L.maxDepth)
+                    const float3 wo = make_float3(-dir.x, -dir.y, -dir.z);
+                    const float3 V = make_float3(dot3(wo, tng), dot3(wo, btg), dot3(wo, nrm));
+                    const bool isSpec = specularity(sf) >= kSpecularThreshold;
+                    const uint32_t mt = sf.info.w;
+                    // ---- NEE (WorkFunctionNEE); specular materials cast none ----
+                    if(L.sampleMode != 0u && L.nLights > 0u && !isSpec && depth + 2u <= L.maxDepth)
                     {
                         const float dXi = rnd(key, depth, 3);
                         uint32_t li = (uint32_t)mul(dXi, (float)L.nLights);
@@ -268,23 +433,25 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                         const float lightPdf = mul(invN, ppdf);
                         const bool emits = (lt.n.w != 0.0f) || (dot3(f3(lt.n), sd) > 0.0f);
                         const float3 emis = emits ? f3(lt.radiance) : make_float3(0, 0, 0);
-                        float3 sdir = normalize3(make_float3(sub(lp.x, pos.x), sub(lp.y, pos.y), sub(lp.z, pos.z)));
+                        const float3 sdir = normalize3(make_float3(sub(lp.x, pos.x), sub(lp.y, pos.y), sub(lp.z, pos.z)));
                         const float3 lpn = nudge(lp, make_float3(-sdir.x, -sdir.y, -sdir.z));
                         const float3 seg = make_float3(sub(lpn.x, pos.x), sub(lpn.y, pos.y), sub(lpn.z, pos.z));
                         const float length = __fsqrt_rn(dot3(seg, seg));
-                        const float cosL = dot3(nrm, sdir);
-                        const float refl = mul(fmaxf(cosL, 0.0f), kInvPi);
-                        float pdf;
-                        if(L.sampleMode == 2u)
+                        const float3 Ls = make_float3(dot3(sdir, tng), dot3(sdir, btg), dot3(sdir, nrm));
+                        float3 refl;
+                        float bpdf;
+                        if(mt == kMatUnreal) refl = unreal_eval(sf, V, Ls, bpdf);
+                        else
                         {
-                            float bpdf = mul(cosL, kInvPi);
+                            const float cw = mul(fmaxf(Ls.z, 0.0f), kInvPi);
+                            refl = make_float3(mul(sf.albedo.x, cw), mul(sf.albedo.y, cw), mul(sf.albedo.z, cw));
+                            bpdf = mul(Ls.z, kInvPi);
                             bpdf = (bpdf <= 1.0e-5f) ? 0.0f : bpdf;
-                            pdf = add(bpdf, lightPdf);
                         }
-                        else pdf = lightPdf;
-                        float3 srad = make_float3(mul(mul(thr.x, mul(albedo.x, refl)), emis.x),
-                                                  mul(mul(thr.y, mul(albedo.y, refl)), emis.y),
-                                                  mul(mul(thr.z, mul(albedo.z, refl)), emis.z));
+                        const float pdf = (L.sampleMode == 2u) ? add(bpdf, lightPdf) : lightPdf;
+                        float3 srad = make_float3(mul(mul(thr.x, refl.x), emis.x),
+                                                  mul(mul(thr.y, refl.y), emis.y),
+                                                  mul(mul(thr.z, refl.z), emis.z));
                         if(pdf == 0.0f) srad = make_float3(0, 0, 0);
                         else
                         {
@@ -299,26 +466,116 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                         shadow = true;
                     }
                     // ---- BxDF sample + Russian roulette (WorkFunction) ----
-                    const float xi0 = rnd(key, depth, 0), xi1 = rnd(key, depth, 1);
-                    const float ang = mul(mul(2.0f, kPi), xi1), sr = __fsqrt_rn(xi0);
-                    const float lx = mul(sr, cosf(ang)), ly = mul(sr, sinf(ang));
-                    const float lz = __fsqrt_rn(fmaxf(0.0f, sub(1.0f, add(mul(lx, lx), mul(ly, ly)))));
-                    const float bpdf = mul(lz, kInvPi);
-                    float3 wi = make_float3(add(add(mul(tng.x, lx), mul(btg.x, ly)), mul(nrm.x, lz)),
-                                            add(add(mul(tng.y, lx), mul(btg.y, ly)), mul(nrm.y, lz)),
-                                            add(add(mul(tng.z, lx), mul(btg.z, ly)), mul(nrm.z, lz)));
+                    float3 Ll, refl;
+                    float bpdf;
+                    bool passed = false;
+                    float3 pre = pos;
+                    if(mt == kMatReflect)
+                    {
+                        Ll = normalize3(make_float3(-V.x, -V.y, sub(mul(2.0f, V.z), V.z)));
+                        bpdf = 1.0f;
+                        refl = make_float3(1.0f, 1.0f, 1.0f);
+                    }
+                    else if(mt == kMatRefract)
+                    {
+                        float fromEta = sf.mat.z, toEta = sf.mat.w;
+                        if(backSide) { const float t = fromEta; fromEta = toEta; toEta = t; }
+                        const float f = fresnel_dielectric(fabsf(V.z), fromEta, toEta);
+                        const bool doRefl = rnd(key, depth, 0) < f;
+                        if(doRefl) Ll = make_float3(-V.x, -V.y, sub(mul(2.0f, V.z), V.z));
+                        else
+                        {
+                            const float eta = __fdiv_rn(fromEta, toEta);
+                            const float cosIn = V.z;
+                            const float sin2 = fmaxf(0.0f, sub(1.0f, mul(cosIn, cosIn)));
+                            const float sinOut2 = mul(mul(eta, eta), sin2);
+                            const float cosOut = sqrt_max(sub(1.0f, sinOut2));
+                            Ll = make_float3(mul(eta, -V.x), mul(eta, -V.y),
+                                             add(mul(eta, -V.z), sub(mul(eta, cosIn), cosOut)));
+                        }
+                        bpdf = doRefl ? f : sub(1.0f, f);
+                        refl = make_float3(bpdf, bpdf, bpdf);
+                        passed = !doRefl;
+                        pre = nudge(pos, nrm);
+                    }
+                    else if(mt == kMatUnreal)
+                    {
+                        const float rough = sf.albedo.w;
+                        const float alpha = mul(rough, rough);
+                        const float ratio = unreal_ratio(sf, avg_albedo(sf));
+                        const float sXi = rnd(key, depth, 0), x0 = rnd(key, depth, 1), x1 = rnd(key, depth, 2);
+                        float3 H;
+                        float pd, ps;
+                        if(sXi < ratio)
+                        {
+                            const float ang = mul(mul(2.0f, kPi), x1), sr = __fsqrt_rn(x0);
+                            Ll.x = mul(sr, cosf(ang)); Ll.y = mul(sr, sinf(ang));
+                            Ll.z = sqrt_max(sub(1.0f, add(mul(Ll.x, Ll.x), mul(Ll.y, Ll.y))));
+                            pd = mul(Ll.z, kInvPi);
+                            H = normalize3(make_float3(add(Ll.x, V.x), add(Ll.y, V.y), add(Ll.z, V.z)));
+                            const float vdh = fmaxf(0.0f, dot3(V, H));
+                            ps = vndf_pdf(V, H, alpha);
+                            ps = (vdh == 0.0f) ? 0.0f : __fdiv_rn(ps, mul(4.0f, vdh));
+                        }
+                        else
+                        {
+                            H = vndf_sample(V, alpha, x0, x1);
+                            const float dv = mul(2.0f, dot3(V, H));
+                            Ll = make_float3(sub(mul(dv, H.x), V.x), sub(mul(dv, H.y), V.y), sub(mul(dv, H.z), V.z));
+                            const float vdh = fmaxf(0.0f, dot3(V, H));
+                            ps = vndf_pdf(V, H, alpha);
+                            ps = (vdh == 0.0f) ? 0.0f : __fdiv_rn(ps, mul(4.0f, vdh));
+                            pd = mul(Ll.z, kInvPi);
+                            pd = (pd <= 1.0e-5f) ? 0.0f : pd;
+                        }
+                        const float vdh = fmaxf(0.0f, dot3(V, H));
+                        const float ldh = fmaxf(0.0f, dot3(Ll, H));
+                        const float ndh = fmaxf(0.0f, H.z);
+                        const float ndv = fmaxf(0.0f, V.z);
+                        const float D = d_ggx(ndh, alpha);
+                        float G = g_correlated(V, Ll, alpha);
+                        G = (ldh == 0.0f) ? 0.0f : G;
+                        G = (vdh == 0.0f) ? 0.0f : G;
+                        const bool dBad = isinf(D) || isnan(D);
+                        const float gs = dBad ? g_single(V, alpha) : 1.0f;
+                        if(dBad) ps = 1.0f;
+                        const float ndl = fmaxf(0.0f, Ll.z);
+                        const float corr = burley(ndl, ndv, ldh, rough);
+                        const float alb[3] = { sf.albedo.x, sf.albedo.y, sf.albedo.z };
+                        float rr[3];
+#pragma unroll
+                        for(int k = 0; k < 3; k++)
+                        {
+                            const float F = schlick1(vdh, f0_of(sf, alb[k]));
+                            float spec = (ndv == 0.0f) ? 0.0f : __fdiv_rn(mul(mul(mul(D, F), G), 0.25f), ndv);
+                            if(dBad) spec = __fdiv_rn(mul(G, F), gs);
+                            rr[k] = add(mul(mul(mul(ndl, mul(sub(1.0f, sf.mat.x), alb[k])), kInvPi), corr), spec);
+                        }
+                        refl = make_float3(rr[0], rr[1], rr[2]);
+                        bpdf = add(mul(pd, ratio), mul(ps, sub(1.0f, ratio)));
+                    }
+                    else
+                    {
+                        const float xi0 = rnd(key, depth, 0), xi1 = rnd(key, depth, 1);
+                        const float ang = mul(mul(2.0f, kPi), xi1), sr = __fsqrt_rn(xi0);
+                        Ll.x = mul(sr, cosf(ang)); Ll.y = mul(sr, sinf(ang));
+                        Ll.z = __fsqrt_rn(fmaxf(0.0f, sub(1.0f, add(mul(Ll.x, Ll.x), mul(Ll.y, Ll.y)))));
+                        bpdf = mul(Ll.z, kInvPi);
+                        const float cw = mul(fmaxf(Ll.z, 0.0f), kInvPi);
+                        refl = make_float3(mul(sf.albedo.x, cw), mul(sf.albedo.y, cw), mul(sf.albedo.z, cw));
+                    }
+                    float3 wi = make_float3(add(add(mul(tng.x, Ll.x), mul(btg.x, Ll.y)), mul(nrm.x, Ll.z)),
+                                            add(add(mul(tng.y, Ll.x), mul(btg.y, Ll.y)), mul(nrm.y, Ll.z)),
+                                            add(add(mul(tng.z, Ll.x), mul(btg.z, Ll.y)), mul(nrm.z, Ll.z)));
                     wi = normalize3(wi);
-                    const float cw = mul(fmaxf(lz, 0.0f), kInvPi);
-                    thr.x = mul(thr.x, mul(albedo.x, cw));
-                    thr.y = mul(thr.y, mul(albedo.y, cw));
-                    thr.z = mul(thr.z, mul(albedo.z, cw));
+                    thr.x = mul(thr.x, refl.x); thr.y = mul(thr.y, refl.y); thr.z = mul(thr.z, refl.z);
                     depth += 1u;
                     bool dead = depth >= L.maxDepth;
-                    if(!dead && depth >= L.rrStart)
+                    if(!dead && depth >= L.rrStart && !isSpec)
                     {
                         float pr = mul(add(add(thr.x, thr.y), thr.z), 0.33333333f);
                         pr = fminf(fmaxf(pr, 0.1f), 1.0f);
-                        const float xr = rnd(key, depth - 1u, 2);
+                        const float xr = rnd(key, depth - 1u, 8);
                         if(xr >= pr) dead = true;
                         else
                         {
@@ -326,7 +583,7 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                             thr.x = mul(thr.x, inv); thr.y = mul(thr.y, inv); thr.z = mul(thr.z, inv);
                         }
                     }
-                    type = 1u;
+                    type = isSpec ? 2u : 1u;
                     if(!dead)
                     {
                         if(bpdf == 0.0f) { thr.x = 0.0f; thr.y = 0.0f; thr.z = 0.0f; }
@@ -336,7 +593,8 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                             thr.x = mul(thr.x, inv); thr.y = mul(thr.y, inv); thr.z = mul(thr.z, inv);
                         }
                         thr.w = bpdf;
-                        const float3 no = nudge(pos, nrm);
+                        const float3 nn = passed ? make_float3(-nrm.x, -nrm.y, -nrm.z) : nrm;
+                        const float3 no = nudge(pre, nn);
                         P.rays[2 * (size_t)i] = make_float4(no.x, no.y, no.z, 1.0e-4f);
                         P.rays[2 * (size_t)i + 1] = make_float4(wi.x, wi.y, wi.z, 3.402823466e+38f);
                         P.hits[i].x = kMissMark;

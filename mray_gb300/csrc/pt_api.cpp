@@ -138,8 +138,9 @@ mrg_status pt_prepare(mrg_ctx* c)
             s.m[r] = make_float4(in.m[4 * r], in.m[4 * r + 1], in.m[4 * r + 2], in.m[4 * r + 3]);
             s.inv[r] = make_float4(in.inv[4 * r], in.inv[4 * r + 1], in.inv[4 * r + 2], in.inv[4 * r + 3]);
         }
-        s.albedo = make_float4(d.albedo[0], d.albedo[1], d.albedo[2], 0.0f);
-        s.info = make_uint4(d.kind == 2 ? 1u : 0u, (uint32_t)lights.size(), mesh.primKeyBase, 0u);
+        s.albedo = make_float4(d.albedo[0], d.albedo[1], d.albedo[2], d.roughness);
+        s.mat = make_float4(d.metallic, d.specular, d.iorFront, d.iorBack);
+        s.info = make_uint4(d.kind == 2 ? 1u : 0u, (uint32_t)lights.size(), mesh.primKeyBase, d.material);
         if(d.kind == 2)
         {
             const uint32_t nt = (uint32_t)(mesh.idx.size() / 3);
@@ -218,6 +219,22 @@ mrg_status mrg_pt_set_lambert(mrg_ctx* c, uint32_t inst, const float albedo[3])
     auto& d = c->ptDesc[inst];
     d.kind = 1;
     std::memcpy(d.albedo, albedo, sizeof(d.albedo));
+    c->ptDirty = true;
+    return MRG_OK;
+}
+
+mrg_status mrg_pt_set_material(mrg_ctx* c, uint32_t inst, const mrg_pt_material* m)
+{
+    if(!c || !m) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_material: null pointer");
+    if(inst >= c->insts.size()) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_material: bad instance id");
+    if(m->type > MRG_MAT_UNREAL) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_material: unknown type");
+    if(c->ptDesc.size() < c->insts.size()) c->ptDesc.resize(c->insts.size());
+    auto& d = c->ptDesc[inst];
+    d.kind = 1;
+    d.material = m->type;
+    std::memcpy(d.albedo, m->albedo, sizeof(d.albedo));
+    d.roughness = m->roughness; d.metallic = m->metallic; d.specular = m->specular;
+    d.iorFront = m->iorFront; d.iorBack = m->iorBack;
     c->ptDirty = true;
     return MRG_OK;
 }

@@ -36,6 +36,18 @@ class PathTracer:
         a = (C.c_float * 3)(*[float(x) for x in albedo])
         N.check(N.lib().mrg_pt_set_lambert(self.acc._h, inst, a))
 
+    _MAT = {"lambert": N.MRG_MAT_LAMBERT, "reflect": N.MRG_MAT_REFLECT,
+            "refract": N.MRG_MAT_REFRACT, "unreal": N.MRG_MAT_UNREAL}
+
+    def set_material(self, inst, kind, albedo=(0.0, 0.0, 0.0), roughness=0.0, metallic=0.0,
+                     specular=0.5, ior=(1.0, 1.5)):
+        m = N.MrgPtMaterial()
+        m.type = self._MAT[kind]
+        m.albedo[:] = [float(x) for x in albedo]
+        m.roughness, m.metallic, m.specular = float(roughness), float(metallic), float(specular)
+        m.iorFront, m.iorBack = float(ior[0]), float(ior[1])
+        N.check(N.lib().mrg_pt_set_material(self.acc._h, inst, C.byref(m)))
+
     def set_area_light(self, inst, radiance, two_sided=False):
         r = (C.c_float * 3)(*[float(x) for x in radiance])
         N.check(N.lib().mrg_pt_set_area_light(self.acc._h, inst, r, 1 if two_sided else 0))
@@ -81,14 +93,17 @@ class PathTracer:
 
 
 def load_box_scene(pt, seed=0):
-    """Adds the box scene's surfaces to a PathTracer; returns the surface list."""
+    """Adds the box scene's surfaces (or a given surface list) to a
+    PathTracer; returns the surface list."""
     from . import scenes
-    surf = scenes.box_scene(seed)
+    surf = scenes.box_scene(seed) if isinstance(seed, int) else seed
     for s in surf:
-        inst = pt.add_surface(s["pos"], s["idx"], s["m34"])
+        inst = pt.add_surface(s["pos"], s["idx"], s["m34"], cull=s.get("cull", True))
         if s["kind"] == "light":
             pt.set_area_light(inst, s["radiance"])
         else:
-            pt.set_lambert(inst, s["albedo"])
+            pt.set_material(inst, s.get("material", "lambert"), s["albedo"],
+                            roughness=s.get("roughness", 0.0), metallic=s.get("metallic", 0.0),
+                            specular=s.get("specular", 0.5), ior=s.get("ior", (1.0, 1.5)))
     pt.build()
     return surf

@@ -158,6 +158,19 @@ def box_scene(seed=0):
     return out
 
 
+def box_scene_mixed(seed=0):
+    """Box scene with every material group: the tall box GGX metal (Unreal,
+    metallic 1, roughness 0.3), the short box glass (Refract, IoR 1.5, no
+    back-face culling), the back wall a rough dielectric-coated Unreal
+    surface (metallic 0, roughness 0.5), the left wall a mirror."""
+    s = box_scene(seed)
+    s[2].update(material="unreal", roughness=0.5, metallic=0.0, specular=0.5)
+    s[3].update(material="reflect")
+    s[5].update(material="unreal", roughness=0.3, metallic=1.0, specular=0.5)
+    s[6].update(material="refract", ior=(1.0, 1.5), cull=False)
+    return s
+
+
 def box_camera():
     """Pinhole camera of the box scene (position, gaze point, up, fov radians, near/far)."""
     f = 40.0 * np.pi / 180.0

@@ -239,7 +239,9 @@ class PtParams(C.Structure):
 
 
 class PtSurface(C.Structure):
-    _fields_ = [("isLight", C.c_int), ("albedo", C.c_float * 3), ("lightBase", u32),
+    _fields_ = [("isLight", C.c_int), ("albedo", C.c_float * 3), ("matType", C.c_int),
+                ("roughness", C.c_float), ("metallic", C.c_float), ("specular", C.c_float),
+                ("iorFront", C.c_float), ("iorBack", C.c_float), ("lightBase", u32),
                 ("primKeyBase", u32), ("triangles", vp), ("m", C.c_float * 12),
                 ("inv", C.c_float * 12)]
 
@@ -267,12 +269,19 @@ class PtScene:
             idx = np.ascontiguousarray(s["idx"], np.uint32)
             mid = self.S.add_mesh(pos, idx, prim_key_base=prim)
             lm = (0x80000000 | k) if s["kind"] == "light" else k
-            self.S.add_instance(mid, s["m34"], cull=cull, lm_key=lm, trans_key=k, accel_key=k)
+            self.S.add_instance(mid, s["m34"], cull=s.get("cull", cull), lm_key=lm, trans_key=k,
+                                accel_key=k)
             tri = np.ascontiguousarray(pos[idx].reshape(-1, 9), np.float32)
             self._keep.append(tri)
             sf = surf[k]
             sf.isLight = 1 if s["kind"] == "light" else 0
             sf.albedo[:] = [float(x) for x in s.get("albedo", (0, 0, 0))]
+            sf.matType = {"lambert": 0, "reflect": 1, "refract": 2, "unreal": 3}[s.get("material", "lambert")]
+            sf.roughness = float(s.get("roughness", 0.0))
+            sf.metallic = float(s.get("metallic", 0.0))
+            sf.specular = float(s.get("specular", 0.5))
+            ior = s.get("ior", (1.0, 1.5))
+            sf.iorFront, sf.iorBack = float(ior[0]), float(ior[1])
             sf.lightBase = len(lights)
             sf.primKeyBase = prim
             sf.triangles = tri.ctypes.data_as(vp)

@@ -76,6 +76,164 @@ static void onb(const float n[3], float t[3], float b[3])
     b[0] = bb; b[1] = sign + n[1] * n[1] * a; b[2] = -n[1];
 }
 
+
+/* ---------------------------------------------------------------------- */
+/* Materials (Source/Tracer/MaterialsDefault.hpp; DistributionFunctions.h) */
+/* ---------------------------------------------------------------------- */
+#define SPECULAR_THRESHOLD 0.95f   /* MaterialC.h:11 */
+
+static inline float sqrt_max(float x) { return sqrtf(fmaxf(x, 0.0f)); }
+
+/* BxDF::DGGX (DistributionFunctions.h:434-443) */
+static float d_ggx(float ndh, float alpha)
+{
+    float a2 = alpha * alpha;
+    float den = ndh * ndh * (a2 - 1.0f) + 1.0f;
+    den = den * den;
+    den *= PI_F;
+    return a2 / den;
+}
+/* BxDF::LambdaSmith (:445-454) */
+static float lambda_smith(const float v[3], float alpha)
+{
+    float a2 = alpha * alpha;
+    float inner = a2 * (v[0] * v[0] + v[1] * v[1]) / (v[2] * v[2]);
+    return (sqrtf(1.0f + inner) - 1.0f) * 0.5f;
+}
+static float g_single(const float v[3], float alpha) { return 1.0f / (1.0f + lambda_smith(v, alpha)); }
+static float g_correlated(const float o[3], const float i[3], float alpha)
+{
+    return 1.0f / (lambda_smith(o, alpha) + lambda_smith(i, alpha) + 1.0f);
+}
+/* BxDF::FSchlick (:502-511) */
+static void f_schlick(float vdh, const float f0[3], float out[3])
+{
+    float pw = 1.0f - vdh;
+    float pw2 = pw * pw;
+    float pw5 = pw2 * pw2 * pw;
+    for(int k = 0; k < 3; k++) out[k] = (1.0f - f0[k]) * pw5 + f0[k];
+}
+/* BxDF::VNDFGGXSmithPDF (:515-527) */
+static float vndf_pdf(const float V[3], const float H[3], float alpha)
+{
+    float vdh = fmaxf(0.0f, dot3f(H, V));
+    float ndh = fmaxf(0.0f, H[2]);
+    float ndv = fmaxf(0.0f, V[2]);
+    float D = d_ggx(ndh, alpha);
+    float G = g_single(V, alpha);
+    if(ndv == 0.0f) return 0.0f;
+    return vdh * D * G / ndv;
+}
+/* BxDF::VNDFGGXSmithSample (:529-590), Heitz 2018 */
+static void vndf_sample(const float V[3], float a, float xi0, float xi1, float H[3])
+{
+    float vh[3] = { a * V[0], a * V[1], V[2] };
+    normalize3f(vh);
+    float len2 = vh[0] * vh[0] + vh[1] * vh[1];
+    float T1[3];
+    if(len2 > 0.0f)
+    {
+        float rs = 1.0f / sqrtf(len2);
+        T1[0] = -vh[1] * rs; T1[1] = vh[0] * rs; T1[2] = 0.0f;
+    }
+    else { T1[0] = 1.0f; T1[1] = 0.0f; T1[2] = 0.0f; }
+    float T2[3];
+    cross3f(vh, T1, T2);
+    float r = sqrtf(xi0);
+    float phi = 2.0f * PI_F * xi1;
+    float t1 = r * cosf(phi), t2 = r * sinf(phi);
+    float sS = 0.5f * (1.0f + vh[2]);
+    t2 = (1.0f - sS) * sqrtf(1.0f - t1 * t1) + sS * t2;
+    float val = 1.0f - t1 * t1 - t2 * t2;
+    float sq = sqrt_max(val);
+    float nh[3];
+    for(int k = 0; k < 3; k++) nh[k] = t1 * T1[k] + t2 * T2[k] + sq * vh[k];
+    float nm[3] = { a * nh[0], a * nh[1], sqrt_max(nh[2]) };
+    float n2 = dot3f(nm, nm);
+    if(n2 < 1.0e-5f) { H[0] = 0.0f; H[1] = 0.0f; H[2] = 1.0f; }
+    else { float rs = 1.0f / sqrtf(n2); H[0] = nm[0] * rs; H[1] = nm[1] * rs; H[2] = nm[2] * rs; }
+}
+/* BxDF::BurleyDiffuseCorrection (:592-603) */
+static float burley(float ndl, float ndv, float ldh, float rough)
+{
+    float fd90 = 0.5f + 2.0f * rough * ldh * ldh;
+    float p1 = 1.0f - ndl, p2 = 1.0f - ndv;
+    float a = 1.0f + (fd90 - 1.0f) * (p1 * p1 * p1 * p1 * p1);
+    float b = 1.0f + (fd90 - 1.0f) * (p2 * p2 * p2 * p2 * p2);
+    return a * b;
+}
+/* UnrealMaterial::MISRatio (MaterialsDefault.hpp:470-478) */
+static float unreal_mis_ratio(const orc_pt_surface* m, float avgAlbedo)
+{
+    float integ = 2.0f * PI_F * avgAlbedo;
+    integ *= (1.0f - m->metallic);
+    float specR = m->specular * (1.0f - m->metallic) + avgAlbedo * m->metallic;   /* Lerp */
+    float total = specR + integ;
+    return (total == 0.0f) ? 0.0f : integ / total;
+}
+static float specularity(const orc_pt_surface* m)
+{
+    if(m->matType == ORC_MAT_REFLECT || m->matType == ORC_MAT_REFRACT) return 1.0f;
+    if(m->matType == ORC_MAT_UNREAL)
+    {
+        float avg = (m->albedo[0] + m->albedo[1] + m->albedo[2]) * 0.3333f;
+        return 1.0f - unreal_mis_ratio(m, avg);
+    }
+    return 0.0f;
+}
+/* UnrealMaterial::Evaluate / Pdf (MaterialsDefault.hpp:628-720) in the
+ * tangent frame; V, L unit vectors. */
+static void unreal_eval(const orc_pt_surface* m, const float V[3], const float L[3],
+                        float refl[3], float* pdfOut)
+{
+    float alpha = m->roughness * m->roughness;
+    float H[3] = { L[0] + V[0], L[1] + V[1], L[2] + V[2] };
+    normalize3f(H);
+    float ldh = fmaxf(0.0f, dot3f(L, H));
+    float vdh = fmaxf(0.0f, dot3f(V, H));
+    float ndh = fmaxf(0.0f, H[2]);
+    float ndv = fmaxf(0.0f, V[2]);
+    float D = d_ggx(ndh, alpha);
+    int dBad = isnan(D) || isinf(D);
+    float Dn = dBad ? 0.0f : D;
+    float G = g_correlated(V, L, alpha);
+    G = (ldh == 0.0f) ? 0.0f : G;
+    G = (vdh == 0.0f) ? 0.0f : G;
+    float f0[3];
+    for(int k = 0; k < 3; k++) f0[k] = (m->specular * 0.08f) * (1.0f - m->metallic) + m->albedo[k] * m->metallic;
+    float F[3];
+    f_schlick(vdh, f0, F);
+    float ndl = fmaxf(0.0f, L[2]);
+    float corr = burley(ndl, ndv, ldh, m->roughness);
+    for(int k = 0; k < 3; k++)
+    {
+        float spec = (ndv == 0.0f) ? 0.0f : Dn * F[k] * G * 0.25f / ndv;
+        float diff = ndl * ((1.0f - m->metallic) * m->albedo[k]) * INV_PI_F * corr;
+        refl[k] = diff + spec;
+    }
+    float avg = (m->albedo[0] + m->albedo[1] + m->albedo[2]) * 0.3333f;
+    float ratio = unreal_mis_ratio(m, avg);
+    float pd = L[2] * INV_PI_F;
+    pd = (pd <= 1.0e-5f) ? 0.0f : pd;
+    float ps = vndf_pdf(V, H, alpha);
+    ps = dBad ? 0.0f : ps;
+    ps = (vdh == 0.0f) ? 0.0f : ps / (4.0f * vdh);
+    *pdfOut = pd * ratio + ps * (1.0f - ratio);
+}
+/* Fresnel for dielectrics (DistributionFunctions.h:382-398) */
+static float fresnel_dielectric(float cosF, float etaF, float etaB)
+{
+    float sinF = sqrt_max(1.0f - cosF * cosF);
+    float sinB = etaF / etaB * sinF;
+    if(sinF >= 1.0f) return 1.0f;
+    float cosB = sqrt_max(1.0f - sinB * sinB);
+    float par = (etaB * cosF - etaF * cosB) / (etaB * cosF + etaF * cosB);
+    par = par * par;
+    float per = (etaF * cosF - etaB * cosB) / (etaF * cosF + etaB * cosB);
+    per = per * per;
+    return (par + per) * 0.5f;
+}
+
 typedef struct
 {
     const orc_scene*          scene;
@@ -177,7 +335,8 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
 
         if(sf->isLight)
         {
-            if(P->sampleMode == ORC_PT_NEE && type != 0) break;
+            /* NEE-only mode: only camera and specular rays see emission */
+            if(P->sampleMode == ORC_PT_NEE && type == 1) break;
             float tp[3] = { thr[0], thr[1], thr[2] };
             if(P->sampleMode == ORC_PT_NEE_MIS && type == 1)
             {
@@ -203,14 +362,18 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
             break;
         }
 
-        const float* albedo = sf->albedo;
-        /* shading normal = geometric normal facing the incoming ray */
+        /* GenerateSurface flips the normal towards the ray (PrimitiveDefaultTriangle.hpp:480-486) */
+        int backSide = dot3f(gn, dir) > 0.0f;
+        if(backSide) { gn[0] = -gn[0]; gn[1] = -gn[1]; gn[2] = -gn[2]; }
         float nrm[3] = { gn[0], gn[1], gn[2] };
         float tng[3], btg[3];
         onb(nrm, tng, btg);
+        const float wo[3] = { -dir[0], -dir[1], -dir[2] };
+        const float V[3] = { dot3f(wo, tng), dot3f(wo, btg), dot3f(wo, nrm) };
+        const int isSpec = specularity(sf) >= SPECULAR_THRESHOLD;
 
-        /* ---- NEE ---- */
-        if(P->sampleMode != ORC_PT_PURE && J->nLights > 0)
+        /* ---- NEE (WorkFunctionNEE); no shadow ray for specular materials ---- */
+        if(P->sampleMode != ORC_PT_PURE && J->nLights > 0 && !isSpec)
         {
             float dXi = rnd(key, depth, 3);
             uint32_t li = (uint32_t)(dXi * (float)J->nLights);
@@ -228,11 +391,9 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
             float ppdf = (ndl == 0.0f) ? 0.0f : (1.0f / L->area) / ndl;
             ppdf *= distSq;
             float lightPdf = invN * ppdf;
-            /* EmitViaSurfacePoint with wO = normalize(surface - light point) */
             float emis[3] = { 0, 0, 0 };
             if(L->twoSided || dot3f(L->n, sd) > 0.0f)
                 for(int k = 0; k < 3; k++) emis[k] = L->radiance[k];
-            /* SampledRay: direction, nudged light point, segment length */
             float sdir[3] = { lp[0] - pos[0], lp[1] - pos[1], lp[2] - pos[2] };
             normalize3f(sdir);
             float nd[3] = { -sdir[0], -sdir[1], -sdir[2] };
@@ -240,18 +401,20 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
             orc_nudge(lp, nd, lpn);
             float seg[3] = { lpn[0] - pos[0], lpn[1] - pos[1], lpn[2] - pos[2] };
             float length = sqrtf(dot3f(seg, seg));
-            float cosL = dot3f(nrm, sdir);
-            float refl = fmaxf(cosL, 0.0f) * INV_PI_F;
-            float pdf;
-            if(P->sampleMode == ORC_PT_NEE_MIS)
+            float refl[3], bpdf;
+            const float Ls[3] = { dot3f(sdir, tng), dot3f(sdir, btg), dot3f(sdir, nrm) };
+            if(sf->matType == ORC_MAT_UNREAL)
+                unreal_eval(sf, V, Ls, refl, &bpdf);
+            else
             {
-                float bpdf = cosL * INV_PI_F;
+                float cw = fmaxf(Ls[2], 0.0f) * INV_PI_F;
+                for(int k = 0; k < 3; k++) refl[k] = sf->albedo[k] * cw;
+                bpdf = Ls[2] * INV_PI_F;
                 bpdf = (bpdf <= 1.0e-5f) ? 0.0f : bpdf;
-                pdf = bpdf + lightPdf;
             }
-            else pdf = lightPdf;
+            float pdf = (P->sampleMode == ORC_PT_NEE_MIS) ? (bpdf + lightPdf) : lightPdf;
             float srad[3];
-            for(int k = 0; k < 3; k++) srad[k] = thr[k] * (albedo[k] * refl) * emis[k];
+            for(int k = 0; k < 3; k++) srad[k] = thr[k] * refl[k] * emis[k];
             if(pdf == 0.0f) srad[0] = srad[1] = srad[2] = 0.0f;
             else { float inv = 1.0f / pdf; for(int k = 0; k < 3; k++) srad[k] *= inv; }
             float sorg[3];
@@ -261,32 +424,128 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
                 for(int k = 0; k < 3; k++) rad[k] += srad[k];
         }
 
-        /* ---- BxDF sample (Lambert, cosine hemisphere) ---- */
-        float xi0 = rnd(key, depth, 0), xi1 = rnd(key, depth, 1);
-        float ang = 2.0f * PI_F * xi1, sr = sqrtf(xi0);
-        float lx = sr * cosf(ang), ly = sr * sinf(ang);
-        float lz = sqrtf(fmaxf(0.0f, 1.0f - (lx * lx + ly * ly)));
-        float bpdf = lz * INV_PI_F;
+        /* ---- BxDF sample (WorkFunction) ---- */
+        float Ll[3], refl[3], bpdf;
+        int passed = 0;
+        float presample[3] = { pos[0], pos[1], pos[2] };    /* ray origin before the final nudge */
+        if(sf->matType == ORC_MAT_REFLECT)
+        {
+            float d2 = 2.0f * V[2];
+            Ll[0] = -V[0]; Ll[1] = -V[1]; Ll[2] = d2 - V[2];
+            normalize3f(Ll);
+            bpdf = 1.0f;
+            refl[0] = refl[1] = refl[2] = 1.0f;
+        }
+        else if(sf->matType == ORC_MAT_REFRACT)
+        {
+            float fromEta = sf->iorFront, toEta = sf->iorBack;
+            if(backSide) { float t = fromEta; fromEta = toEta; toEta = t; }
+            float cosT = fabsf(V[2]);
+            float f = fresnel_dielectric(cosT, fromEta, toEta);
+            int doRefl = rnd(key, depth, 0) < f;
+            if(doRefl) { Ll[0] = -V[0]; Ll[1] = -V[1]; Ll[2] = 2.0f * V[2] - V[2]; }
+            else
+            {
+                float eta = fromEta / toEta;
+                float cosIn = V[2];
+                float sin2 = fmaxf(0.0f, 1.0f - cosIn * cosIn);
+                float sinOut2 = eta * eta * sin2;
+                float cosOut = sqrt_max(1.0f - sinOut2);
+                for(int k = 0; k < 2; k++) Ll[k] = eta * -V[k];
+                Ll[2] = eta * -V[2] + (eta * cosIn - cosOut);
+            }
+            bpdf = doRefl ? f : (1.0f - f);
+            refl[0] = refl[1] = refl[2] = bpdf;
+            passed = !doRefl;
+            orc_nudge(pos, nrm, presample);                 /* SampleBxDF nudges along n first */
+        }
+        else if(sf->matType == ORC_MAT_UNREAL)
+        {
+            float alpha = sf->roughness * sf->roughness;
+            float avg = (sf->albedo[0] + sf->albedo[1] + sf->albedo[2]) * 0.3333f;
+            float ratio = unreal_mis_ratio(sf, avg);
+            float sXi = rnd(key, depth, 0), x0 = rnd(key, depth, 1), x1 = rnd(key, depth, 2);
+            float H[3], pd, ps;
+            if(sXi < ratio)
+            {
+                float ang = 2.0f * PI_F * x1, sr = sqrtf(x0);
+                Ll[0] = sr * cosf(ang); Ll[1] = sr * sinf(ang);
+                Ll[2] = sqrt_max(1.0f - (Ll[0] * Ll[0] + Ll[1] * Ll[1]));
+                pd = Ll[2] * INV_PI_F;
+                H[0] = Ll[0] + V[0]; H[1] = Ll[1] + V[1]; H[2] = Ll[2] + V[2];
+                normalize3f(H);
+                float vdh = fmaxf(0.0f, dot3f(V, H));
+                ps = vndf_pdf(V, H, alpha);
+                ps = (vdh == 0.0f) ? 0.0f : ps / (4.0f * vdh);
+            }
+            else
+            {
+                vndf_sample(V, alpha, x0, x1, H);
+                float dv = 2.0f * dot3f(V, H);
+                for(int k = 0; k < 3; k++) Ll[k] = dv * H[k] - V[k];
+                float vdh = fmaxf(0.0f, dot3f(V, H));
+                ps = vndf_pdf(V, H, alpha);
+                ps = (vdh == 0.0f) ? 0.0f : ps / (4.0f * vdh);
+                pd = Ll[2] * INV_PI_F;
+                pd = (pd <= 1.0e-5f) ? 0.0f : pd;
+            }
+            float vdh = fmaxf(0.0f, dot3f(V, H));
+            float ldh = fmaxf(0.0f, dot3f(Ll, H));
+            float ndh = fmaxf(0.0f, H[2]);
+            float ndv = fmaxf(0.0f, V[2]);
+            float D = d_ggx(ndh, alpha);
+            float G = g_correlated(V, Ll, alpha);
+            G = (ldh == 0.0f) ? 0.0f : G;
+            G = (vdh == 0.0f) ? 0.0f : G;
+            float f0[3], F[3];
+            for(int k = 0; k < 3; k++) f0[k] = (sf->specular * 0.08f) * (1.0f - sf->metallic) + sf->albedo[k] * sf->metallic;
+            f_schlick(vdh, f0, F);
+            float spec[3];
+            for(int k = 0; k < 3; k++) spec[k] = (ndv == 0.0f) ? 0.0f : D * F[k] * G * 0.25f / ndv;
+            if(isinf(D) || isnan(D))
+            {
+                float gs = g_single(V, alpha);
+                for(int k = 0; k < 3; k++) spec[k] = G * F[k] / gs;
+                ps = 1.0f;
+            }
+            float ndl = fmaxf(0.0f, Ll[2]);
+            float corr = burley(ndl, ndv, ldh, sf->roughness);
+            for(int k = 0; k < 3; k++)
+                refl[k] = ndl * ((1.0f - sf->metallic) * sf->albedo[k]) * INV_PI_F * corr + spec[k];
+            bpdf = pd * ratio + ps * (1.0f - ratio);
+        }
+        else
+        {
+            float xi0 = rnd(key, depth, 0), xi1 = rnd(key, depth, 1);
+            float ang = 2.0f * PI_F * xi1, sr = sqrtf(xi0);
+            Ll[0] = sr * cosf(ang); Ll[1] = sr * sinf(ang);
+            Ll[2] = sqrtf(fmaxf(0.0f, 1.0f - (Ll[0] * Ll[0] + Ll[1] * Ll[1])));
+            bpdf = Ll[2] * INV_PI_F;
+            float cw = fmaxf(Ll[2], 0.0f) * INV_PI_F;
+            for(int k = 0; k < 3; k++) refl[k] = sf->albedo[k] * cw;
+        }
         float wi[3];
-        for(int k = 0; k < 3; k++) wi[k] = tng[k] * lx + btg[k] * ly + nrm[k] * lz;
+        for(int k = 0; k < 3; k++) wi[k] = tng[k] * Ll[0] + btg[k] * Ll[1] + nrm[k] * Ll[2];
         normalize3f(wi);
-        for(int k = 0; k < 3; k++) thr[k] *= albedo[k] * (fmaxf(lz, 0.0f) * INV_PI_F);
+        for(int k = 0; k < 3; k++) thr[k] *= refl[k];
         depth += 1u;
         int dead = depth >= P->maxDepth;
-        if(!dead && depth >= P->rrStart)
+        if(!dead && depth >= P->rrStart && !isSpec)
         {
             float pr = (thr[0] + thr[1] + thr[2]) * 0.33333333f;
             pr = fminf(fmaxf(pr, 0.1f), 1.0f);
-            float xr = rnd(key, depth - 1u, 2);
+            float xr = rnd(key, depth - 1u, 8);
             if(xr >= pr) dead = 1;
             else { float inv = 1.0f / pr; for(int k = 0; k < 3; k++) thr[k] *= inv; }
         }
-        type = 1;
+        type = isSpec ? 2 : 1;
         if(dead) break;
         if(bpdf == 0.0f) { thr[0] = thr[1] = thr[2] = 0.0f; }
         else { float inv = 1.0f / bpdf; for(int k = 0; k < 3; k++) thr[k] *= inv; }
         prevPdf = bpdf;
-        orc_nudge(pos, nrm, org);
+        float nn[3] = { nrm[0], nrm[1], nrm[2] };
+        if(passed) { nn[0] = -nn[0]; nn[1] = -nn[1]; nn[2] = -nn[2]; }
+        orc_nudge(presample, nn, org);
         memcpy(dir, wi, 12);
         tmin = 1.0e-4f;
         tmax = 3.402823466e+38f;

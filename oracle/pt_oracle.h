@@ -34,10 +34,18 @@ typedef struct
 
 /* Per instance (surface): Lambert albedo or light, instance-space triangles
  * (9 floats each, indexed by local primitive), transform and inverse. */
+#define ORC_MAT_LAMBERT 0
+#define ORC_MAT_REFLECT 1
+#define ORC_MAT_REFRACT 2
+#define ORC_MAT_UNREAL  3
+
 typedef struct
 {
     int          isLight;
     float        albedo[3];
+    int          matType;       /* ORC_MAT_* */
+    float        roughness, metallic, specular;
+    float        iorFront, iorBack;
     uint32_t     lightBase;     /* first light index of this surface */
     uint32_t     primKeyBase;
     const float* triangles;

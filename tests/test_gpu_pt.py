@@ -61,3 +61,24 @@ def test_high_spp_against_oracle(box):
     g = _img(pt.render(PathTracer.params(64, 64, 512, cam, seed=11)))
     o = _img(S.render(S.params(64, 64, 512, cam, seed=12)))
     assert relmse(g, o) <= 0.01
+
+
+@pytest.fixture(scope="module")
+def mixed():
+    pt = PathTracer(0)
+    surf = load_box_scene(pt, scenes.box_scene_mixed(0))
+    return pt, oracle.PtScene(surf)
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_mixed_materials_per_pixel(mixed, mode):
+    """Lambert, mirror, glass (refraction through back faces) and GGX
+    metallic-roughness surfaces against the oracle."""
+    pt, S = mixed
+    cam = scenes.box_camera()
+    g = _img(pt.render(PathTracer.params(64, 64, 16, cam, sample_mode=mode, seed=7)))
+    o = _img(S.render(S.params(64, 64, 16, cam, sample_mode=mode, seed=7)))
+    close = np.abs(g - o) <= 1e-4 * (1.0 + np.abs(o))
+    frac = close.all(axis=-1).mean()
+    assert frac >= 0.95, frac
+    assert relmse(g, o) <= 2e-3
