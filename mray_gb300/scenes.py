@@ -144,7 +144,9 @@ def box_scene(seed=0):
         alb = [0.1 + 0.7 * _u01(seed, 3 * k + j) for j in range(3)]
         out.append(dict(pos=p.astype(np.float32), idx=i, m34=I34.copy(), kind="lambert", albedo=alb))
         k += 1
-    for size, at in (((0.28, 0.6, 0.28), (0.33, 0.3, 0.62)), ((0.28, 0.28, 0.28), (0.68, 0.14, 0.35))):
+    # boxes float 1e-3 above the floor: coplanar faces would make exact-t ties
+    # whose winner depends on traversal order
+    for size, at in (((0.28, 0.6, 0.28), (0.33, 0.301, 0.62)), ((0.28, 0.28, 0.28), (0.68, 0.141, 0.35))):
         p, i = _box(*size)
         t = 2.0 * _u01(seed, 100 + k) - 1.0
         c, s = (1 - t * t) / (1 + t * t), 2 * t / (1 + t * t)
