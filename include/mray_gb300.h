@@ -169,7 +169,9 @@ mrg_status mrg_cast_closest_host_noalloc(mrg_ctx* ctx, mrg_ray* h_rays, uint32_t
                                          mrg_hit_keys* h_hits, mrg_meta_hit* h_meta);
 
 /* World-space AABB of the scene (BaseAcceleratorI::SceneAABB,
- * Source/Tracer/AcceleratorC.h:416): min xyz, max xyz. */
+ * Source/Tracer/AcceleratorC.h:416): min xyz, max xyz; the union of every
+ * instance's TransformAABB of its mesh box, as MRay computes it (the TLAS
+ * itself uses slightly padded boxes). */
 mrg_status mrg_scene_aabb(mrg_ctx* ctx, float out_minmax[6]);
 
 mrg_status mrg_get_stats(mrg_ctx* ctx, mrg_accel_stats* out);
@@ -237,6 +239,17 @@ typedef struct mrg_pt_material
 mrg_status mrg_pt_set_material(mrg_ctx* ctx, uint32_t instance_id, const mrg_pt_material* material);
 mrg_status mrg_pt_set_area_light(mrg_ctx* ctx, uint32_t instance_id, const float radiance[3],
                                  uint32_t two_sided);
+
+/* Skysphere boundary light (LightGroupSkysphere<SphericalCoordConverter>,
+ * Source/Tracer/LightsDefault.hpp:300-420, 700-915): a lat-long radiance map
+ * of width x height RGBA f32 texels (row-major, row 0 at v = 0; 1 x 1 = a
+ * constant radiance) and an optional 3x4 transform (NULL = identity; only its
+ * rotation is used).  The map is copied; its importance-sampling distribution
+ * (luminance, piecewise-constant 2D) is built at the next render.  It joins
+ * the uniform light sampler after the area lights and is seen by rays that
+ * leave the scene.  width = 0 removes it. */
+mrg_status mrg_pt_set_env(mrg_ctx* ctx, uint32_t width, uint32_t height, const float* rgba,
+                          const float m3x4[12]);
 
 /* The pinhole frame MRay derives from the camera parameters
  * (CameraPinhole ctor, Source/Tracer/CamerasDefault.hpp:6-30): out = position[3],

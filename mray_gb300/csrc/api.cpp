@@ -127,6 +127,7 @@ mrg_status mrg_destroy(mrg_ctx* c)
     cudaFree(c->dScratch);
     cudaFree(c->dStats);
     cudaFree(c->dPtSurfaces); cudaFree(c->dPtLights); cudaFree(c->dPtTris); cudaFree(c->ptPathMem);
+    cudaFree(c->dPtEnv);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);
     delete c;
@@ -275,6 +276,7 @@ mrg_status mrg_build(mrg_ctx* c)
     if(e == cudaSuccess)
         e = cudaMemcpyAsync(c->dTlasLeaf, tlas.leafIds, sizeof(uint32_t) * ni, cudaMemcpyDeviceToDevice, st);
     std::vector<mrg::HostInstRecord> recs(ni);
+    for(int k = 0; k < 3; k++) { c->sceneBoxExact[k] = 3.0e38f; c->sceneBoxExact[3 + k] = -3.0e38f; }
     for(uint32_t i = 0; i < ni; i++)
     {
         const auto& in = c->insts[i];
@@ -286,7 +288,12 @@ mrg_status mrg_build(mrg_ctx* c)
                           ((in.flags & MRG_INSTANCE_CULL_BACKFACE) ? 0x80000000u : 0u);
         float wb[6];
         mrg::transform_box_exact(in.m, c->meshes[in.mesh].box, wb);
-        for(int k = 0; k < 3; k++) { recs[i].wmin[k] = wb[k]; recs[i].wmax[k] = wb[3 + k]; }
+        for(int k = 0; k < 3; k++)
+        {
+            recs[i].wmin[k] = wb[k]; recs[i].wmax[k] = wb[3 + k];
+            c->sceneBoxExact[k] = std::min(c->sceneBoxExact[k], wb[k]);
+            c->sceneBoxExact[3 + k] = std::max(c->sceneBoxExact[3 + k], wb[3 + k]);
+        }
         recs[i].wmin[3] = 0.0f; recs[i].wmax[3] = 0.0f;
     }
     if(e == cudaSuccess)
@@ -378,7 +385,7 @@ mrg_status mrg_scene_aabb(mrg_ctx* c, float out[6])
 {
     if(!c || !out) return fail(MRG_ERR_INVALID_ARG, "mrg_scene_aabb: null pointer");
     if(!c->built) return fail(MRG_ERR_NOT_BUILT, "mrg_scene_aabb: call mrg_build first");
-    std::memcpy(out, c->sceneBox, sizeof(c->sceneBox));
+    std::memcpy(out, c->sceneBoxExact, sizeof(c->sceneBoxExact));
     return MRG_OK;
 }
 

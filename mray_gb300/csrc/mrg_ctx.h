@@ -58,7 +58,8 @@ struct mrg_ctx
     uint32_t* dTlasLeaf = nullptr;
     uint64_t  blasNodes = 0, blasTris = 0, tlasNodes = 0;
     mrg::TraceScene scene;
-    float     sceneBox[6] = { 0, 0, 0, 0, 0, 0 };
+    float     sceneBox[6] = { 0, 0, 0, 0, 0, 0 };        // conservative (TLAS) box
+    float     sceneBoxExact[6] = { 0, 0, 0, 0, 0, 0 };   // union of the exact instance boxes
     double    buildMs = 0.0;
 
     // scratch: [0] work counter, [1] error flag; stats in a separate block
@@ -84,6 +85,14 @@ struct mrg_ctx
     uint32_t  ptSurfaceCount = 0, ptLightCount = 0, ptTriCount = 0;
     mrg::PtPaths ptPaths{};
     void*     ptPathMem = nullptr;
+    // skysphere boundary light: host copy of the radiance map and transform,
+    // device block [texels | cdfX | cdfY]
+    bool               ptEnvSet = false;
+    uint32_t           ptEnvW = 0, ptEnvH = 0;
+    std::vector<float> ptEnvTexels;          // RGBA per texel
+    float              ptEnvM[12] = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0 };
+    void*              dPtEnv = nullptr;
+    mrg::PtEnv         ptEnv{};
 
     // staging for the host-buffer cast
     mrg_ray*      dStageRays = nullptr;

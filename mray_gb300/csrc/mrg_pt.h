@@ -36,6 +36,22 @@ struct __align__(16) PtLight
     float4 radiance;
 };
 
+// Skysphere boundary light (LightSkysphere<SphericalCoordConverter>,
+// Source/Tracer/LightsDefault.hpp:175-222, 300-420): a lat-long radiance map
+// with its piecewise-constant 2D sampling distribution (Distributions.h).
+// It is the last light of the uniform light sampler.
+struct PtEnv
+{
+    const float4* texels;        // RGBA per texel, row-major, row 0 at v = 0
+    const float*  cdfX;          // width * height row CDFs
+    const float*  cdfY;          // height marginal CDF
+    float4        m[3];          // ApplyV rows
+    float4        inv[3];        // InvApplyV rows
+    uint32_t      width, height; // 1 x 1: constant radiance, uniform uv sampling
+    float         sceneDiameter; // |(span.x, span.z)| of the scene box
+    uint32_t      enabled;
+};
+
 struct PtCamera
 {
     float pos[3];
@@ -55,9 +71,10 @@ struct PtLaunch
     uint32_t rrStart, maxDepth;
     uint32_t sampleMode;     // 0 pure, 1 NEE, 2 NEE + MIS
     uint32_t seed;
-    uint32_t nLights;
+    uint32_t nLights;        // triangle lights; the skysphere, if enabled, follows them
     float    filterSigma;
     PtCamera cam;
+    PtEnv    env;
 };
 
 // Path state, structure of arrays (device).

@@ -248,6 +248,139 @@ __device__ __forceinline__ float fresnel_dielectric(float cosF, float etaF, floa
     return mul(add(par, per), 0.5f);
 }
 
+// ---------------------------------------------------------------------------
+// Skysphere (LightsDefault.hpp:175-222, 300-420) and its piecewise-constant
+// 2D distribution (Distributions.h:128-270).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int32_t wrap_index(int32_t i, int32_t n)
+{
+    i = i % n;
+    return (i < 0) ? i + n : i;
+}
+
+// Bilinear, wrap-addressed read with the host texture view's fraction rule
+// (a negative texel coordinate keeps the absolute value of its fraction).
+__device__ float3 env_read(const PtEnv& E, float u, float v)
+{
+    const float tx = sub(mul(u, (float)E.width), 0.5f), ty = sub(mul(v, (float)E.height), 0.5f);
+    float bx, by;
+    float fx = modff(tx, &bx), fy = modff(ty, &by);
+    int32_t sx = (int32_t)bx, sy = (int32_t)by;
+    if(fx < 0.0f) { sx -= 1; fx = fabsf(fx); }
+    if(fy < 0.0f) { sy -= 1; fy = fabsf(fy); }
+    const int32_t x0 = wrap_index(sx, (int32_t)E.width), x1 = wrap_index(sx + 1, (int32_t)E.width);
+    const int32_t y0 = wrap_index(sy, (int32_t)E.height), y1 = wrap_index(sy + 1, (int32_t)E.height);
+    const float4 p00 = __ldg(&E.texels[(size_t)y0 * E.width + x0]);
+    const float4 p10 = __ldg(&E.texels[(size_t)y0 * E.width + x1]);
+    const float4 p01 = __ldg(&E.texels[(size_t)y1 * E.width + x0]);
+    const float4 p11 = __ldg(&E.texels[(size_t)y1 * E.width + x1]);
+    const float gx = sub(1.0f, fx), gy = sub(1.0f, fy);
+    const float ax = add(mul(p00.x, gx), mul(p10.x, fx)), bxx = add(mul(p01.x, gx), mul(p11.x, fx));
+    const float ay = add(mul(p00.y, gx), mul(p10.y, fx)), byy = add(mul(p01.y, gx), mul(p11.y, fx));
+    const float az = add(mul(p00.z, gx), mul(p10.z, fx)), bzz = add(mul(p01.z, gx), mul(p11.z, fx));
+    return make_float3(add(mul(ax, gy), mul(bxx, fy)), add(mul(ay, gy), mul(byy, fy)),
+                       add(mul(az, gy), mul(bzz, fy)));
+}
+
+__device__ __forceinline__ float2 env_dir_to_uv(float3 d)
+{
+    // Y-up -> Z-up (z, x, y); azimuth atan2(y, x), inclination acos(z)
+    const float az = atan2f(d.x, d.z);
+    const float incl = acosf(fminf(fmaxf(d.y, -1.0f), 1.0f));
+    return make_float2(__fdiv_rn(mul(add(az, kPi), 0.5f), kPi), sub(1.0f, mul(incl, kInvPi)));
+}
+
+__device__ __forceinline__ float env_sa_pdf_sin(float pdf, float sinPhi)
+{
+    return (sinPhi <= 0.0f) ? 0.0f : __fdiv_rn(pdf, mul(mul(2.0f, mul(kPi, kPi)), sinPhi));
+}
+
+__device__ __forceinline__ float3 rows_apply(const float4 (&m)[3], float3 v)
+{
+    return make_float3(add(add(mul(m[0].x, v.x), mul(m[0].y, v.y)), mul(m[0].z, v.z)),
+                       add(add(mul(m[1].x, v.x), mul(m[1].y, v.y)), mul(m[1].z, v.z)),
+                       add(add(mul(m[2].x, v.x), mul(m[2].y, v.y)), mul(m[2].z, v.z)));
+}
+
+// DistributionPwC<1>::SampleIndex: lower bound, position in the bin, and
+// every value >= 1 moved down by one ulp.
+__device__ float pwc1_sample_index(const float* __restrict__ cdf, uint32_t n, float xi, float& pdf)
+{
+    uint32_t lo = 0, cnt = n;
+    while(cnt > 0u)
+    {
+        const uint32_t step = cnt >> 1, mid = lo + step;
+        if(__ldg(&cdf[mid]) < xi) { lo = mid + 1u; cnt -= step + 1u; }
+        else cnt = step;
+    }
+    const float prev = (lo == 0u) ? 0.0f : __ldg(&cdf[lo - 1u]);
+    const float my = __ldg(&cdf[lo]);
+    const float t = __fdiv_rn(sub(xi, prev), sub(my, prev));
+    float indexF = add((float)lo, t);
+    indexF = (indexF < 1.0f) ? indexF : nextafterf(indexF, -3.402823466e+38f);
+    pdf = mul(sub(my, prev), (float)n);
+    return indexF;
+}
+
+__device__ __forceinline__ float pwc1_pdf_index(const float* __restrict__ cdf, uint32_t n, float index)
+{
+    const uint32_t i = (uint32_t)index;
+    const float prev = (i == 0u) ? 0.0f : __ldg(&cdf[i - 1u]);
+    return mul(sub(__ldg(&cdf[i]), prev), (float)n);
+}
+
+__device__ __forceinline__ bool env_constant(const PtEnv& E) { return E.width == 1u && E.height == 1u; }
+
+// EmitViaSurfacePoint: radiance arriving along -d (d points away from the
+// receiver, into the sky).
+__device__ float3 env_emit(const PtEnv& E, float3 d)
+{
+    const float3 dy = normalize3(rows_apply(E.inv, d));
+    const float2 uv = env_constant(E) ? make_float2(0.0f, 0.0f) : env_dir_to_uv(dy);
+    return env_read(E, uv.x, uv.y);
+}
+
+// PdfSolidAngle(dir)
+__device__ float env_pdf(const PtEnv& E, float3 d)
+{
+    const float3 dy = rows_apply(E.inv, d);
+    const float2 uv = env_dir_to_uv(normalize3(dy));
+    float pdf = 1.0f;
+    if(!env_constant(E))
+    {
+        float ix = mul(uv.x, (float)E.width), iy = mul(uv.y, (float)E.height);
+        ix = (ix < sub((float)E.width, 1.0f)) ? ix : sub((float)E.width, 1.0f);
+        iy = (iy < sub((float)E.height, 1.0f)) ? iy : sub((float)E.height, 1.0f);
+        const uint32_t row = (uint32_t)iy;
+        const float marginal = pwc1_pdf_index(E.cdfY, E.height, iy);
+        const float conditional = pwc1_pdf_index(E.cdfX + (size_t)row * E.width, E.width, ix);
+        pdf = mul(conditional, marginal);
+    }
+    return env_sa_pdf_sin(pdf, sinf(acosf(fminf(fmaxf(dy.y, -1.0f), 1.0f))));
+}
+
+// SampleSolidAngle: world direction, solid-angle pdf.
+__device__ float3 env_sample(const PtEnv& E, float xi0, float xi1, float& pdf)
+{
+    float2 uv;
+    float uvPdf;
+    if(env_constant(E)) { uv = make_float2(xi0, xi1); uvPdf = 1.0f; }
+    else
+    {
+        float py, px;
+        const float iy = pwc1_sample_index(E.cdfY, E.height, xi1, py);
+        const uint32_t row = (uint32_t)iy;
+        const float ix = pwc1_sample_index(E.cdfX + (size_t)row * E.width, E.width, xi0, px);
+        uv = make_float2(mul(ix, __fdiv_rn(1.0f, (float)E.width)), mul(iy, __fdiv_rn(1.0f, (float)E.height)));
+        uvPdf = mul(py, px);
+    }
+    const float theta = sub(mul(mul(uv.x, kPi), 2.0f), kPi);
+    const float phi = mul(sub(1.0f, uv.y), kPi);
+    const float sT = sinf(theta), cT = cosf(theta), sP = sinf(phi), cP = cosf(phi);
+    pdf = env_sa_pdf_sin(uvPdf, sP);
+    return rows_apply(E.m, make_float3(mul(sT, sP), cP, mul(cT, sP)));
+}
+
 __device__ __forceinline__ uint32_t slot_pixel(const PtLaunch& L, uint32_t i) { return i % (L.width * L.height); }
 __device__ __forceinline__ uint32_t slot_sample(const PtLaunch& L, uint32_t i)
 {
@@ -359,7 +492,8 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                 gn.y = add(add(mul(sf.inv[0].y, nl.x), mul(sf.inv[1].y, nl.y)), mul(sf.inv[2].y, nl.z));
                 gn.z = add(add(mul(sf.inv[0].z, nl.x), mul(sf.inv[1].z, nl.y)), mul(sf.inv[2].z, nl.z));
                 gn = normalize3(gn);
-                const float invN = L.nLights ? __fdiv_rn(1.0f, (float)L.nLights) : 0.0f;
+                const uint32_t nAll = L.nLights + (L.env.enabled ? 1u : 0u);
+                const float invN = nAll ? __fdiv_rn(1.0f, (float)nAll) : 0.0f;
                 float4 thr = P.thr[i];
                 float4 rad = P.rad[i];
 
@@ -412,27 +546,44 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                     const bool isSpec = specularity(sf) >= kSpecularThreshold;
                     const uint32_t mt = sf.info.w;
                     // ---- NEE (WorkFunctionNEE); specular materials cast none ----
-                    if(L.sampleMode != 0u && L.nLights > 0u && !isSpec && depth + 2u <= L.maxDepth)
+                    if(L.sampleMode != 0u && nAll > 0u && !isSpec && depth + 2u <= L.maxDepth)
                     {
                         const float dXi = rnd(key, depth, 3);
-                        uint32_t li = (uint32_t)mul(dXi, (float)L.nLights);
-                        li = min(li, L.nLights - 1u);
-                        const PtLight lt = lights[li];
-                        const float r1 = __fsqrt_rn(rnd(key, depth, 4)), r2 = rnd(key, depth, 5);
-                        const float a = sub(1.0f, r1), b = mul(sub(1.0f, r2), r1), c = mul(r1, r2);
-                        const float3 lp = make_float3(add(add(mul(lt.p0.x, a), mul(lt.p1.x, b)), mul(lt.p2.x, c)),
-                                                      add(add(mul(lt.p0.y, a), mul(lt.p1.y, b)), mul(lt.p2.y, c)),
-                                                      add(add(mul(lt.p0.z, a), mul(lt.p1.z, b)), mul(lt.p2.z, c)));
-                        float3 sd = make_float3(sub(pos.x, lp.x), sub(pos.y, lp.y), sub(pos.z, lp.z));
-                        const float distSq = dot3(sd, sd);
-                        sd = normalize3(sd);
-                        float ndl = dot3(f3(lt.n), sd);
-                        ndl = (lt.n.w != 0.0f) ? fabsf(ndl) : fmaxf(0.0f, ndl);
-                        float ppdf = (ndl == 0.0f) ? 0.0f : __fdiv_rn(__fdiv_rn(1.0f, lt.p0.w), ndl);
-                        ppdf = mul(ppdf, distSq);
-                        const float lightPdf = mul(invN, ppdf);
-                        const bool emits = (lt.n.w != 0.0f) || (dot3(f3(lt.n), sd) > 0.0f);
-                        const float3 emis = emits ? f3(lt.radiance) : make_float3(0, 0, 0);
+                        uint32_t li = (uint32_t)mul(dXi, (float)nAll);
+                        li = min(li, nAll - 1u);
+                        float3 lp, emis;
+                        float lightPdf;
+                        if(li == L.nLights)
+                        {
+                            // skysphere: a point sceneDiameter away along the sampled direction
+                            float spdf;
+                            const float3 wd = env_sample(L.env, rnd(key, depth, 4), rnd(key, depth, 5), spdf);
+                            lp = make_float3(add(pos.x, mul(wd.x, L.env.sceneDiameter)),
+                                             add(pos.y, mul(wd.y, L.env.sceneDiameter)),
+                                             add(pos.z, mul(wd.z, L.env.sceneDiameter)));
+                            const float3 sd = normalize3(make_float3(sub(pos.x, lp.x), sub(pos.y, lp.y), sub(pos.z, lp.z)));
+                            emis = env_emit(L.env, make_float3(-sd.x, -sd.y, -sd.z));
+                            lightPdf = mul(invN, spdf);
+                        }
+                        else
+                        {
+                            const PtLight lt = lights[li];
+                            const float r1 = __fsqrt_rn(rnd(key, depth, 4)), r2 = rnd(key, depth, 5);
+                            const float a = sub(1.0f, r1), b = mul(sub(1.0f, r2), r1), c = mul(r1, r2);
+                            lp = make_float3(add(add(mul(lt.p0.x, a), mul(lt.p1.x, b)), mul(lt.p2.x, c)),
+                                             add(add(mul(lt.p0.y, a), mul(lt.p1.y, b)), mul(lt.p2.y, c)),
+                                             add(add(mul(lt.p0.z, a), mul(lt.p1.z, b)), mul(lt.p2.z, c)));
+                            float3 sd = make_float3(sub(pos.x, lp.x), sub(pos.y, lp.y), sub(pos.z, lp.z));
+                            const float distSq = dot3(sd, sd);
+                            sd = normalize3(sd);
+                            float ndl = dot3(f3(lt.n), sd);
+                            ndl = (lt.n.w != 0.0f) ? fabsf(ndl) : fmaxf(0.0f, ndl);
+                            float ppdf = (ndl == 0.0f) ? 0.0f : __fdiv_rn(__fdiv_rn(1.0f, lt.p0.w), ndl);
+                            ppdf = mul(ppdf, distSq);
+                            lightPdf = mul(invN, ppdf);
+                            const bool emits = (lt.n.w != 0.0f) || (dot3(f3(lt.n), sd) > 0.0f);
+                            emis = emits ? f3(lt.radiance) : make_float3(0, 0, 0);
+                        }
                         const float3 sdir = normalize3(make_float3(sub(lp.x, pos.x), sub(lp.y, pos.y), sub(lp.z, pos.z)));
                         const float3 lpn = nudge(lp, make_float3(-sdir.x, -sdir.y, -sdir.z));
                         const float3 seg = make_float3(sub(lpn.x, pos.x), sub(lpn.y, pos.y), sub(lpn.z, pos.z));
@@ -604,6 +755,36 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                     }
                 }
                 P.rad[i] = rad;
+            }
+            else if(hk.x == kMissMark && L.env.enabled)
+            {
+                // ---- miss: skysphere emission (LightWorkFunction[WithNEE]) ----
+                const bool neeOnly = (L.sampleMode == 1u && type == 1u);
+                if(!neeOnly && depth + 1u <= L.maxDepth)
+                {
+                    const float3 dir = f3(P.rays[2 * (size_t)i + 1]);
+                    const float4 thr = P.thr[i];
+                    float4 rad = P.rad[i];
+                    float3 tp = f3(thr);
+                    if(L.sampleMode == 2u && type == 1u)
+                    {
+                        const float invN = __fdiv_rn(1.0f, (float)(L.nLights + 1u));
+                        const float lpdf = mul(env_pdf(L.env, dir), invN);
+                        const float misPdf = add(thr.w, lpdf);
+                        tp = make_float3(mul(tp.x, thr.w), mul(tp.y, thr.w), mul(tp.z, thr.w));
+                        if(misPdf == 0.0f) tp = make_float3(0, 0, 0);
+                        else
+                        {
+                            const float inv = __fdiv_rn(1.0f, misPdf);
+                            tp = make_float3(mul(tp.x, inv), mul(tp.y, inv), mul(tp.z, inv));
+                        }
+                    }
+                    const float3 em = env_emit(L.env, dir);
+                    rad.x = add(rad.x, mul(em.x, tp.x));
+                    rad.y = add(rad.y, mul(em.y, tp.y));
+                    rad.z = add(rad.z, mul(em.z, tp.z));
+                    P.rad[i] = rad;
+                }
             }
         }
         warp_append(alive, i, nextList, nextCount);

@@ -99,6 +99,103 @@ void make_light(const float m[12], const float v[9], const float radiance[3], ui
     out.radiance = make_float4(radiance[0], radiance[1], radiance[2], 0.0f);
 }
 
+// ---- skysphere: luminance and the piecewise-constant 2D distribution ----
+// Bilinear, wrap-addressed texel read of the host texture view
+// (Device/CPU/TextureViewCPU.h:196-375), used for the luminance at texel centres.
+void env_read_host(const float* tex, uint32_t w, uint32_t h, float u, float v, float rgb[3])
+{
+    const float tx = u * (float)w - 0.5f, ty = v * (float)h - 0.5f;
+    float bx, by;
+    float fx = std::modf(tx, &bx), fy = std::modf(ty, &by);
+    int32_t sx = (int32_t)bx, sy = (int32_t)by;
+    if(fx < 0.0f) { sx -= 1; fx = std::fabs(fx); }
+    if(fy < 0.0f) { sy -= 1; fy = std::fabs(fy); }
+    auto wrap = [](int32_t i, int32_t n) { i %= n; return i < 0 ? i + n : i; };
+    const float* p[4];
+    for(int j = 0; j < 2; j++)
+        for(int i = 0; i < 2; i++)
+            p[2 * j + i] = &tex[4 * ((size_t)wrap(sy + j, (int32_t)h) * w + (size_t)wrap(sx + i, (int32_t)w))];
+    for(int k = 0; k < 3; k++)
+    {
+        const float a = p[0][k] * (1.0f - fx) + p[1][k] * fx;
+        const float b = p[2][k] * (1.0f - fx) + p[3][k] * fx;
+        rgb[k] = a * (1.0f - fy) + b * fy;
+    }
+}
+
+// KCExtractLuminance (Tracer/ColorConverter.cu:405-475): Y of the Rec.709
+// (D65) RGB -> XYZ transform, one texel centre at a time; then
+// DistributionGroupPwC2D::Construct (Tracer/Distributions.cu:233-330, host
+// backend): double row scans of |f|, a float scan of the row totals, and a
+// double normalisation of every row and of the marginal.
+void env_distribution(const std::vector<float>& tex, uint32_t w, uint32_t h,
+                      std::vector<float>& cdfX, std::vector<float>& cdfY)
+{
+    cdfX.assign((size_t)w * h, 0.0f);
+    cdfY.assign(h, 0.0f);
+    const float rx = 1.0f / (float)w, ry = 1.0f / (float)h;
+    for(uint32_t y = 0; y < h; y++)
+    {
+        double sum = 0.0;
+        for(uint32_t x = 0; x < w; x++)
+        {
+            float c[3];
+            env_read_host(tex.data(), w, h, ((float)x + 0.5f) * rx, ((float)y + 0.5f) * ry, c);
+            const float lum = std::fma(0.0721750f, c[2], std::fma(0.7151522f, c[1], 0.2126729f * c[0]));
+            sum += (double)std::fabs(lum);
+            cdfX[(size_t)y * w + x] = (float)sum;
+        }
+    }
+    float run = 0.0f;
+    for(uint32_t y = 0; y < h; y++) { run += cdfX[(size_t)y * w + (w - 1)]; cdfY[y] = run; }
+    for(uint32_t y = 0; y < h; y++)
+    {
+        float* row = &cdfX[(size_t)y * w];
+        const double r = 1.0 / (double)row[w - 1];
+        for(uint32_t x = 0; x < w; x++) row[x] = (float)((double)row[x] * r);
+    }
+    const double r = 1.0 / (double)cdfY[h - 1];
+    for(uint32_t y = 0; y < h; y++) cdfY[y] = (float)((double)cdfY[y] * r);
+}
+
+mrg_status env_prepare(mrg_ctx* c)
+{
+    cudaFree(c->dPtEnv);
+    c->dPtEnv = nullptr;
+    c->ptEnv = mrg::PtEnv{};
+    if(!c->ptEnvSet) return MRG_OK;
+    const uint32_t w = c->ptEnvW, h = c->ptEnvH;
+    std::vector<float> cdfX, cdfY;
+    env_distribution(c->ptEnvTexels, w, h, cdfX, cdfY);
+    const size_t texBytes = sizeof(float) * c->ptEnvTexels.size();
+    const size_t xBytes = (sizeof(float) * cdfX.size() + 255) & ~size_t(255);
+    const size_t yBytes = sizeof(float) * cdfY.size();
+    PT_TRY(cudaMalloc(&c->dPtEnv, texBytes + xBytes + yBytes), "mrg_pt: skysphere");
+    char* base = static_cast<char*>(c->dPtEnv);
+    PT_TRY(cudaMemcpy(base, c->ptEnvTexels.data(), texBytes, cudaMemcpyHostToDevice), "mrg_pt: skysphere upload");
+    PT_TRY(cudaMemcpy(base + texBytes, cdfX.data(), sizeof(float) * cdfX.size(), cudaMemcpyHostToDevice),
+           "mrg_pt: skysphere upload");
+    PT_TRY(cudaMemcpy(base + texBytes + xBytes, cdfY.data(), yBytes, cudaMemcpyHostToDevice), "mrg_pt: skysphere upload");
+    mrg::PtEnv& E = c->ptEnv;
+    E.texels = reinterpret_cast<const float4*>(base);
+    E.cdfX = reinterpret_cast<const float*>(base + texBytes);
+    E.cdfY = reinterpret_cast<const float*>(base + texBytes + xBytes);
+    float inv[12];
+    mrg::mat34_inverse(c->ptEnvM, inv, true);
+    for(int r = 0; r < 3; r++)
+    {
+        E.m[r] = make_float4(c->ptEnvM[4 * r], c->ptEnvM[4 * r + 1], c->ptEnvM[4 * r + 2], 0.0f);
+        E.inv[r] = make_float4(inv[4 * r], inv[4 * r + 1], inv[4 * r + 2], 0.0f);
+    }
+    E.width = w; E.height = h;
+    // TracerBase.cpp:1650-1664: the diagonal of the scene box over the XZ plane
+    const float sx = c->sceneBoxExact[3] - c->sceneBoxExact[0];
+    const float sz = c->sceneBoxExact[5] - c->sceneBoxExact[2];
+    E.sceneDiameter = std::sqrt(std::fma(sz, sz, sx * sx));
+    E.enabled = 1u;
+    return MRG_OK;
+}
+
 // Uploads surfaces, lights and the primitive-indexed triangle table.
 mrg_status pt_prepare(mrg_ctx* c)
 {
@@ -166,6 +263,8 @@ mrg_status pt_prepare(mrg_ctx* c)
     c->ptSurfaceCount = ni;
     c->ptLightCount = (uint32_t)lights.size();
     c->ptTriCount = maxPrim;
+    mrg_status es = env_prepare(c);
+    if(es != MRG_OK) return es;
     c->ptDirty = false;
     return MRG_OK;
 }
@@ -252,6 +351,31 @@ mrg_status mrg_pt_set_area_light(mrg_ctx* c, uint32_t inst, const float radiance
     return MRG_OK;
 }
 
+mrg_status mrg_pt_set_env(mrg_ctx* c, uint32_t width, uint32_t height, const float* rgba, const float m3x4[12])
+{
+    if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_env: null context");
+    if(width == 0)
+    {
+        c->ptEnvSet = false;
+        c->ptEnvTexels.clear();
+        c->ptDirty = true;
+        return MRG_OK;
+    }
+    if(!rgba || height == 0) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_env: null map or zero height");
+    if((uint64_t)width * height > (1ull << 26))
+        return mrg::set_error(MRG_ERR_LIMIT, "mrg_pt_set_env: more than 2^26 texels");
+    const size_t n = 4ull * width * height;
+    for(size_t i = 0; i < n; i++)
+        if(!std::isfinite(rgba[i])) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_env: non-finite texel");
+    c->ptEnvTexels.assign(rgba, rgba + n);
+    c->ptEnvW = width; c->ptEnvH = height;
+    const float ident[12] = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0 };
+    std::memcpy(c->ptEnvM, m3x4 ? m3x4 : ident, sizeof(c->ptEnvM));
+    c->ptEnvSet = true;
+    c->ptDirty = true;
+    return MRG_OK;
+}
+
 mrg_status mrg_pt_camera_frame(const mrg_pt_params* p, float out[16])
 {
     if(!p || !out) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_camera_frame: null pointer");
@@ -294,6 +418,7 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
     L.rrStart = p->rrStart; L.maxDepth = p->maxDepth;
     L.sampleMode = p->sampleMode; L.seed = p->seed;
     L.nLights = c->ptLightCount;
+    L.env = c->ptEnv;
     L.filterSigma = p->filterRadius * 0.285714f;
     camera_frame(*p, L.cam);
     mrg::PtPaths& P = c->ptPaths;

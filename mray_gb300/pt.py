@@ -52,6 +52,19 @@ class PathTracer:
         r = (C.c_float * 3)(*[float(x) for x in radiance])
         N.check(N.lib().mrg_pt_set_area_light(self.acc._h, inst, r, 1 if two_sided else 0))
 
+    def set_env(self, texels, m34=None):
+        """Skysphere radiance map, (h, w, 4) float32 RGBA (row 0 at v = 0);
+        None removes it."""
+        if texels is None:
+            N.check(N.lib().mrg_pt_set_env(self.acc._h, 0, 0, None, None))
+            return
+        t = np.ascontiguousarray(texels, np.float32)
+        if t.ndim != 3 or t.shape[2] != 4:
+            raise ValueError("skysphere texels must be (height, width, 4)")
+        m = None if m34 is None else np.ascontiguousarray(m34, np.float32).reshape(12)
+        N.check(N.lib().mrg_pt_set_env(self.acc._h, t.shape[1], t.shape[0], t.ctypes.data,
+                                       None if m is None else m.ctypes.data))
+
     def build(self):
         self.acc.construct()
 

@@ -173,6 +173,41 @@ def box_scene_mixed(seed=0):
     return s
 
 
+def sky_map(width=64, height=32, seed=0, sun=(0.3, 0.8), sun_radiance=40.0):
+    """Seeded lat-long sky radiance, (height, width, 4) float32 RGBA rounded
+    through float16 (a half-float HDR map): a blue gradient above the horizon,
+    dim ground below, a small bright sun disc at uv = sun and +-10% value
+    noise.  Every texel is positive, so no row of the sampling distribution is
+    empty.  Row 0 is v = 0 (straight down)."""
+    v = (np.arange(height, dtype=np.float64) + 0.5) / height
+    u = (np.arange(width, dtype=np.float64) + 0.5) / width
+    V, U = np.meshgrid(v, u, indexing="ij")
+    up = np.clip((V - 0.5) * 2.0, 0.0, 1.0)
+    rgb = np.empty((height, width, 3), np.float64)
+    sky = np.stack([0.35 + 0.25 * (1 - up), 0.55 + 0.2 * (1 - up), 0.95 + 0.0 * up], -1) * 1.5
+    ground = np.stack([0.25 + 0 * V, 0.2 + 0 * V, 0.15 + 0 * V], -1)
+    rgb[:] = np.where((V >= 0.5)[..., None], sky, ground)
+    du = np.minimum(np.abs(U - sun[0]), 1.0 - np.abs(U - sun[0]))
+    d2 = (du * 2.0) ** 2 + (V - sun[1]) ** 2
+    rgb += sun_radiance * np.exp(-d2 / (2 * 0.03 ** 2))[..., None] * np.array([1.0, 0.9, 0.75])
+    noise = np.array([_u01(seed, 7919 + i) for i in range(height * width)]).reshape(height, width)
+    rgb *= (0.9 + 0.2 * noise)[..., None]
+    rgb = np.maximum(rgb, 0.02)
+    out = np.ones((height, width, 4), np.float32)
+    out[..., :3] = rgb.astype(np.float16).astype(np.float32)
+    return out
+
+
+def sky_scene(seed=0):
+    """Open variant of the box scene lit by a sky: floor, left wall, the GGX
+    metal tall box, the Lambert short box and the ceiling light quad; the
+    ceiling, back and right walls are left out, so paths leave the scene and
+    camera rays see the sky."""
+    s = box_scene(seed)
+    s[5].update(material="unreal", roughness=0.3, metallic=1.0, specular=0.5)
+    return [s[0], s[3], s[5], s[6], s[7]]
+
+
 def box_camera():
     """Pinhole camera of the box scene (position, gaze point, up, fov radians, near/far)."""
     f = 40.0 * np.pi / 180.0

@@ -56,7 +56,18 @@ def lib():
             getattr(L, f).argtypes = [vp, vp, vp, u32, vp, vp, vp, C.c_int]
         L.orc_cast_visibility.argtypes = [vp, vp, vp, u32, vp, C.c_int]
         L.orc_scene_stats.argtypes = [vp, vp]
-        L.orc_pt_render.argtypes = [vp, vp, vp, vp, u32, vp, C.c_int]
+        L.orc_pt_render.argtypes = [vp, vp, vp, vp, u32, vp, vp, C.c_int]
+        L.orc_scene_aabb.argtypes = [vp, vp]
+        L.orc_scene_diameter.argtypes = [vp]
+        L.orc_scene_diameter.restype = C.c_float
+        L.orc_pwc2d_build.argtypes = [vp, u32, u32, vp, vp]
+        L.orc_pwc2d_sample_uv.argtypes = [vp, vp, u32, u32, vp, vp, vp]
+        L.orc_pwc2d_pdf_uv.argtypes = [vp, vp, u32, u32, vp]
+        L.orc_pwc2d_pdf_uv.restype = C.c_float
+        L.orc_env_luminance.argtypes = [vp, u32, u32, vp]
+        L.orc_env_read.argtypes = [vp, u32, u32, vp, vp]
+        L.orc_env_dir_to_uv.argtypes = [vp, vp]
+        L.orc_env_uv_to_dir.argtypes = [vp, vp]
         L.orc_pt_render.restype = C.c_int
         L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
         L.orc_pt_make_light.argtypes = [vp, vp, vp, C.c_int, vp]
@@ -252,12 +263,77 @@ class PtLightTri(C.Structure):
                 ("twoSided", C.c_int)]
 
 
+class PtEnv(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("texels", C.c_void_p),
+                ("cdfX", C.c_void_p), ("cdfY", C.c_void_p), ("m", C.c_float * 12),
+                ("inv", C.c_float * 12), ("sceneDiameter", C.c_float)]
+
+
+class Pwc2D:
+    """Piecewise-constant 2D distribution over a (h, w) function."""
+
+    def __init__(self, func):
+        func = np.ascontiguousarray(func, np.float32)
+        self.h, self.w = func.shape
+        self.cdf_x = np.zeros((self.h, self.w), np.float32)
+        self.cdf_y = np.zeros(self.h, np.float32)
+        lib().orc_pwc2d_build(_vp(func), self.w, self.h, _vp(self.cdf_x), _vp(self.cdf_y))
+
+    def sample_uv(self, xi):
+        xi = np.ascontiguousarray(xi, np.float32).reshape(-1, 2)
+        uv = np.zeros_like(xi)
+        pdf = np.zeros(xi.shape[0], np.float32)
+        L = lib()
+        for i in range(xi.shape[0]):
+            L.orc_pwc2d_sample_uv(_vp(self.cdf_x), _vp(self.cdf_y), self.w, self.h,
+                                  _vp(xi[i]), _vp(uv[i]), _vp(pdf[i:i + 1]))
+        return uv, pdf
+
+    def pdf_uv(self, uv):
+        uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        L = lib()
+        return np.array([L.orc_pwc2d_pdf_uv(_vp(self.cdf_x), _vp(self.cdf_y), self.w, self.h, _vp(uv[i]))
+                         for i in range(uv.shape[0])], np.float32)
+
+
+def env_luminance(texels):
+    t = np.ascontiguousarray(texels, np.float32)
+    out = np.zeros(t.shape[:2], np.float32)
+    lib().orc_env_luminance(_vp(t), t.shape[1], t.shape[0], _vp(out))
+    return out
+
+
+def env_read(texels, uv):
+    t = np.ascontiguousarray(texels, np.float32)
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    out = np.zeros((uv.shape[0], 3), np.float32)
+    for i in range(uv.shape[0]):
+        lib().orc_env_read(_vp(t), t.shape[1], t.shape[0], _vp(uv[i]), _vp(out[i]))
+    return out
+
+
+def env_dir_to_uv(d):
+    d = np.ascontiguousarray(d, np.float32).reshape(-1, 3)
+    out = np.zeros((d.shape[0], 2), np.float32)
+    for i in range(d.shape[0]):
+        lib().orc_env_dir_to_uv(_vp(d[i]), _vp(out[i]))
+    return out
+
+
+def env_uv_to_dir(uv):
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    out = np.zeros((uv.shape[0], 3), np.float32)
+    for i in range(uv.shape[0]):
+        lib().orc_env_uv_to_dir(_vp(uv[i]), _vp(out[i]))
+    return out
+
+
 class PtScene:
     """The CPU path-tracer oracle over a list of surfaces (dicts with pos,
     idx, m34, kind, albedo / radiance), keyed like mray_gb300.pt.PathTracer:
     dense primitive keys, instance id = surface index."""
 
-    def __init__(self, surfaces, cull=True):
+    def __init__(self, surfaces, cull=True, env=None):
         self.L = lib()
         self.S = Scene()
         self._keep = []
@@ -300,6 +376,30 @@ class PtScene:
         self.surf = surf
         self.lights = (PtLightTri * max(1, len(lights)))(*lights)
         self.n_lights = len(lights)
+        self.env = None
+        if env is not None:
+            # env: {"texels": (h, w, 4) f32, "m34": optional rotation}
+            tex = np.ascontiguousarray(env["texels"], np.float32)
+            h, w = tex.shape[:2]
+            self._env_tex = tex
+            self._env_dist = Pwc2D(env_luminance(tex))
+            E = PtEnv()
+            E.width, E.height = w, h
+            E.texels = tex.ctypes.data
+            E.cdfX = self._env_dist.cdf_x.ctypes.data
+            E.cdfY = self._env_dist.cdf_y.ctypes.data
+            m = np.asarray(env.get("m34", np.eye(3, 4)), np.float32).reshape(3, 4)
+            E.m[:] = [float(x) for x in m.reshape(12)]
+            inv = np.zeros(12, np.float32)
+            self.L.orc_mat34_inverse_corrected(_vp(np.ascontiguousarray(m.reshape(12))), _vp(inv))
+            E.inv[:] = [float(x) for x in inv]
+            E.sceneDiameter = self.L.orc_scene_diameter(self.S._h)
+            self.env = E
+
+    def scene_aabb(self):
+        out = np.zeros(6, np.float32)
+        self.L.orc_scene_aabb(self.S._h, _vp(out))
+        return out
 
     @staticmethod
     def params(width, height, spp, camera, max_depth=8, rr_start=3, sample_mode=PT_NEE_MIS, seed=0,
@@ -318,5 +418,6 @@ class PtScene:
     def render(self, p, image=None, threads=None):
         img = np.zeros((p.height, p.width, 4), np.float32) if image is None else image
         self.L.orc_pt_render(self.S._h, C.byref(p), self.surf, self.lights, self.n_lights,
+                             C.byref(self.env) if self.env is not None else None,
                              _vp(img), threads or default_threads())
         return img

@@ -610,6 +610,27 @@ void orc_scene_instance_inverse(const orc_scene* s, uint32_t inst, float inv[12]
     memcpy(inv, s->insts[inst].inv, sizeof(float) * 12);
 }
 
+void orc_scene_aabb(const orc_scene* s, float out[6])
+{
+    for(int k = 0; k < 3; k++) { out[k] = 3.0e38f; out[3 + k] = -3.0e38f; }
+    for(uint32_t i = 0; i < s->instCount; i++)
+        for(int k = 0; k < 3; k++)
+        {
+            const aabb3* w = &s->insts[i].world;
+            out[k] = (w->mn[k] < out[k]) ? w->mn[k] : out[k];
+            out[3 + k] = (out[3 + k] < w->mx[k]) ? w->mx[k] : out[3 + k];
+        }
+}
+
+float orc_scene_diameter(const orc_scene* s)
+{
+    float b[6];
+    orc_scene_aabb(s, b);
+    float sx = b[3] - b[0], sz = b[5] - b[2];
+    /* Math::Length of a Vector2: sqrt of the fused dot product */
+    return sqrtf(fmaf(sz, sz, sx * sx));
+}
+
 void orc_scene_stats(const orc_scene* s, uint64_t out[4])
 {
     uint64_t nodes = 0, leaves = 0;

@@ -79,6 +79,11 @@ void orc_cast_visibility(const orc_scene*, const orc_ray_gmem* rays, const uint3
                          uint32_t n, uint32_t* visible_bits, int nthreads);
 /* Node / leaf statistics of the last build. */
 void orc_scene_stats(const orc_scene*, uint64_t out[4]);
+/* Union of the instances' world AABBs (TransformAABB of each BLAS root box)
+ * and MRay's boundary-light scene diameter, |(span.x, span.z)|
+ * (TracerBase.cpp:1650-1664). */
+void  orc_scene_aabb(const orc_scene*, float out[6]);
+float orc_scene_diameter(const orc_scene*);
 
 #ifdef __cplusplus
 }

@@ -16,6 +16,11 @@
  *   - triangle area light      Source/Tracer/LightsDefault.hpp:24-160,
  *                              PrimitiveDefaultTriangle.hpp:49-75
  *   - uniform light sampler    Source/Tracer/LightSampler.hpp:6-120
+ *   - skysphere boundary light Source/Tracer/LightsDefault.hpp:175-222,
+ *                              300-420 (spherical mapping), sampled with
+ *                              the piecewise-constant 2D distribution of
+ *                              Distributions.h:14-270 / Distributions.cu
+ *                              (host-backend construction)
  *   - film                     Source/Tracer/TextureFilter.cu:673-697
  * Random numbers come from a counter-based hash of (seed, pixel, sample,
  * bounce, dimension), the same one the GPU renderer uses, so both render the
@@ -234,13 +239,229 @@ static float fresnel_dielectric(float cosF, float etaF, float etaB)
     return (par + per) * 0.5f;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Piecewise-constant 2D distribution (Source/Tracer/Distributions.h:14-270, */
+/* construction Distributions.cu:233-330, host backend)                     */
+/* ------------------------------------------------------------------------ */
+void orc_pwc2d_build(const float* func, uint32_t w, uint32_t h, float* cdfX, float* cdfY)
+{
+    /* KCSegmentedScanPrecise: per row, double running sum of |f| */
+    for(uint32_t y = 0; y < h; y++)
+    {
+        double sum = 0.0;
+        for(uint32_t x = 0; x < w; x++)
+        {
+            sum += (double)fabsf(func[(size_t)y * w + x]);
+            cdfX[(size_t)y * w + x] = (float)sum;
+        }
+    }
+    /* KCCopyScanY: float running sum of the row totals (before normalising) */
+    float s = 0.0f;
+    for(uint32_t y = 0; y < h; y++)
+    {
+        s += cdfX[(size_t)y * w + (w - 1)];
+        cdfY[y] = s;
+    }
+    /* KCNormalizeXY: every row and the marginal, in double */
+    for(uint32_t y = 0; y < h; y++)
+    {
+        float* row = cdfX + (size_t)y * w;
+        double rr = 1.0 / (double)row[w - 1];
+        for(uint32_t x = 0; x < w; x++) row[x] = (float)((double)row[x] * rr);
+    }
+    double ry = 1.0 / (double)cdfY[h - 1];
+    for(uint32_t y = 0; y < h; y++) cdfY[y] = (float)((double)cdfY[y] * ry);
+}
+
+/* DistributionPwC<1>::SampleIndex (Distributions.h:128-146): lower bound,
+ * linear position inside the bin, and the quirk that every value >= 1 is
+ * moved down by one ulp. */
+static float pwc1_sample_index(const float* cdf, uint32_t n, float xi, float* pdf)
+{
+    uint32_t lo = 0, cnt = n;
+    while(cnt > 0)
+    {
+        uint32_t step = cnt / 2, mid = lo + step;
+        if(cdf[mid] < xi) { lo = mid + 1; cnt -= step + 1; }
+        else cnt = step;
+    }
+    uint32_t index = lo;
+    float prev = (index == 0) ? 0.0f : cdf[index - 1];
+    float my = cdf[index];
+    float t = (xi - prev) / (my - prev);
+    float indexF = (float)index + t;
+    indexF = (indexF < 1.0f) ? indexF : nextafterf(indexF, -3.402823466e+38f);
+    *pdf = (my - prev) * (float)n;
+    return indexF;
+}
+
+static float pwc1_pdf_index(const float* cdf, uint32_t n, float index)
+{
+    uint32_t i = (uint32_t)index;
+    float prev = (i == 0) ? 0.0f : cdf[i - 1];
+    return (cdf[i] - prev) * (float)n;
+}
+
+void orc_pwc2d_sample_uv(const float* cdfX, const float* cdfY, uint32_t w, uint32_t h,
+                         const float xi[2], float uv[2], float* pdf)
+{
+    float py, px;
+    float iy = pwc1_sample_index(cdfY, h, xi[1], &py);
+    uint32_t row = (uint32_t)iy;
+    float ix = pwc1_sample_index(cdfX + (size_t)row * w, w, xi[0], &px);
+    uv[0] = ix * (1.0f / (float)w);
+    uv[1] = iy * (1.0f / (float)h);
+    *pdf = py * px;
+}
+
+float orc_pwc2d_pdf_uv(const float* cdfX, const float* cdfY, uint32_t w, uint32_t h, const float uv[2])
+{
+    float ix = uv[0] * (float)w, iy = uv[1] * (float)h;
+    ix = (ix < (float)w - 1.0f) ? ix : (float)w - 1.0f;
+    iy = (iy < (float)h - 1.0f) ? iy : (float)h - 1.0f;
+    uint32_t row = (uint32_t)iy;
+    float marginal = pwc1_pdf_index(cdfY, h, iy);
+    float conditional = pwc1_pdf_index(cdfX + (size_t)row * w, w, ix);
+    return conditional * marginal;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Skysphere light (Source/Tracer/LightsDefault.hpp:175-222, 300-420)        */
+/* ------------------------------------------------------------------------ */
+#define PI_SQR_F (PI_F * PI_F)
+/* Rec.709 / D65 luminance row of RGB -> XYZ (Color::XYZToYxy(ToXYZ(rgb)).x) */
+#define LUM_R 0.2126729f
+#define LUM_G 0.7151522f
+#define LUM_B 0.0721750f
+
+static inline int32_t wrap_index(int32_t i, int32_t n)
+{
+    i = i % n;
+    return (i < 0) ? i + n : i;
+}
+
+/* ReadInterpolatedPixel + FindInterpolants of the host texture view,
+ * including its treatment of negative texel coordinates (the fraction of a
+ * negative coordinate is its absolute value). */
+void orc_env_read(const float* texels, uint32_t w, uint32_t h, const float uv[2], float rgb[3])
+{
+    float tx = uv[0] * (float)w - 0.5f, ty = uv[1] * (float)h - 0.5f;
+    float bx, by;
+    float fx = modff(tx, &bx), fy = modff(ty, &by);
+    int32_t sx = (int32_t)bx, sy = (int32_t)by;
+    if(fx < 0.0f) { sx -= 1; fx = fabsf(fx); }
+    if(fy < 0.0f) { sy -= 1; fy = fabsf(fy); }
+    float pix[4][3];
+    for(int j = 0; j < 2; j++)
+        for(int i = 0; i < 2; i++)
+        {
+            int32_t x = wrap_index(sx + i, (int32_t)w), y = wrap_index(sy + j, (int32_t)h);
+            const float* t = &texels[4 * ((size_t)y * w + (size_t)x)];
+            for(int k = 0; k < 3; k++) pix[(j << 1) + i][k] = t[k];
+        }
+    for(int k = 0; k < 3; k++)
+    {
+        float a = pix[0][k] * (1.0f - fx) + pix[1][k] * fx;
+        float b = pix[2][k] * (1.0f - fx) + pix[3][k] * fx;
+        rgb[k] = a * (1.0f - fy) + b * fy;
+    }
+}
+
+void orc_env_luminance(const float* texels, uint32_t w, uint32_t h, float* out)
+{
+    const float rx = 1.0f / (float)w, ry = 1.0f / (float)h;
+    for(uint32_t y = 0; y < h; y++)
+        for(uint32_t x = 0; x < w; x++)
+        {
+            float uv[2] = { ((float)x + 0.5f) * rx, ((float)y + 0.5f) * ry };
+            float c[3];
+            orc_env_read(texels, w, h, uv, c);
+            out[(size_t)y * w + x] = fmaf(LUM_B, c[2], fmaf(LUM_G, c[1], LUM_R * c[0]));
+        }
+}
+
+/* SphericalCoordConverter::DirToUV: Y-up -> Z-up, (azimuth, inclination),
+ * u = (azimuth + pi) / 2pi, v = 1 - inclination / pi. */
+void orc_env_dir_to_uv(const float d[3], float uv[2])
+{
+    float zx = d[2], zy = d[0], zz = d[1];
+    float az = atan2f(zy, zx);
+    float cl = (zz < -1.0f) ? -1.0f : ((zz > 1.0f) ? 1.0f : zz);
+    float incl = acosf(cl);
+    uv[0] = (az + PI_F) * 0.5f / PI_F;
+    uv[1] = 1.0f - incl * INV_PI_F;
+}
+
+void orc_env_uv_to_dir(const float uv[2], float d[3])
+{
+    float theta = uv[0] * PI_F * 2.0f - PI_F;
+    float phi = (1.0f - uv[1]) * PI_F;
+    float sT = sinf(theta), cT = cosf(theta), sP = sinf(phi), cP = cosf(phi);
+    /* Z-up (cT sP, sT sP, cP) -> Y-up */
+    d[0] = sT * sP; d[1] = cP; d[2] = cT * sP;
+}
+
+static inline float env_sa_pdf_sin(float pdf, float sinPhi)
+{
+    return (sinPhi <= 0.0f) ? 0.0f : pdf / (2.0f * PI_SQR_F * sinPhi);
+}
+
+static void rows_apply(const float m[12], const float v[3], float o[3])
+{
+    for(int r = 0; r < 3; r++) o[r] = m[4 * r] * v[0] + m[4 * r + 1] * v[1] + m[4 * r + 2] * v[2];
+}
+
+static inline int env_constant(const orc_pt_env* E) { return E->width == 1u && E->height == 1u; }
+
+/* EmitViaSurfacePoint(wO): radiance seen along -wO. */
+static void env_emit(const orc_pt_env* E, const float minusWo[3], float rgb[3])
+{
+    float dy[3];
+    rows_apply(E->inv, minusWo, dy);
+    normalize3f(dy);
+    float uv[2] = { 0.0f, 0.0f };
+    if(!env_constant(E)) orc_env_dir_to_uv(dy, uv);
+    orc_env_read(E->texels, E->width, E->height, uv, rgb);
+}
+
+/* PdfSolidAngle(dir) (solid-angle density of sampling dir). */
+static float env_pdf(const orc_pt_env* E, const float dir[3])
+{
+    float dy[3];
+    rows_apply(E->inv, dir, dy);
+    float dn[3] = { dy[0], dy[1], dy[2] };
+    normalize3f(dn);
+    float uv[2];
+    orc_env_dir_to_uv(dn, uv);
+    float pdf = env_constant(E) ? 1.0f : orc_pwc2d_pdf_uv(E->cdfX, E->cdfY, E->width, E->height, uv);
+    float cl = (dy[1] < -1.0f) ? -1.0f : ((dy[1] > 1.0f) ? 1.0f : dy[1]);
+    return env_sa_pdf_sin(pdf, sinf(acosf(cl)));
+}
+
+/* SampleSolidAngle: world direction and solid-angle pdf. */
+static void env_sample(const orc_pt_env* E, float xi0, float xi1, float wdir[3], float* pdf)
+{
+    float uv[2], uvPdf;
+    if(env_constant(E)) { uv[0] = xi0; uv[1] = xi1; uvPdf = 1.0f; }
+    else
+    {
+        const float xi[2] = { xi0, xi1 };
+        orc_pwc2d_sample_uv(E->cdfX, E->cdfY, E->width, E->height, xi, uv, &uvPdf);
+    }
+    float dy[3];
+    orc_env_uv_to_dir(uv, dy);
+    *pdf = env_sa_pdf_sin(uvPdf, sinf((1.0f - uv[1]) * PI_F));
+    rows_apply(E->m, dy, wdir);
+}
+
 typedef struct
 {
     const orc_scene*          scene;
     const orc_pt_params*      p;
     const orc_pt_surface*     surfaces;     /* per instance */
     const orc_pt_light_tri*   lights;
-    uint32_t                  nLights;
+    uint32_t                  nLights;      /* triangle lights */
+    const orc_pt_env*         env;          /* boundary light (last), or NULL */
     float*                    image;
     atomic_uint               nextRow;
 } pt_job;
@@ -318,12 +539,33 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
     uint32_t depth = 0;
     int type = 0;           /* 0 camera, 1 path (diffuse) */
     float prevPdf = 0.0f;
-    const float invN = J->nLights ? 1.0f / (float)J->nLights : 0.0f;
+    const orc_pt_env* E = J->env;
+    const uint32_t nAll = J->nLights + (E ? 1u : 0u);
+    const float invN = nAll ? 1.0f / (float)nAll : 0.0f;
 
     for(;;)
     {
         orc_hit_keys hk; orc_meta_hit mh; uint32_t inst; float t;
-        if(!cast1(J->scene, org, dir, tmin, tmax, &hk, &mh, &inst, &t)) break;
+        if(!cast1(J->scene, org, dir, tmin, tmax, &hk, &mh, &inst, &t))
+        {
+            /* miss: boundary light work (LightWorkFunction[WithNEE] with the
+             * skysphere, PathTracerRendererShaders.h:308-345, 450-517) */
+            if(!E || (P->sampleMode == ORC_PT_NEE && type == 1)) break;
+            float tp[3] = { thr[0], thr[1], thr[2] };
+            if(P->sampleMode == ORC_PT_NEE_MIS && type == 1)
+            {
+                float lpdf = env_pdf(E, dir) * invN;
+                float misPdf = prevPdf + lpdf;
+                for(int k = 0; k < 3; k++) tp[k] *= prevPdf;
+                if(misPdf == 0.0f) { tp[0] = tp[1] = tp[2] = 0.0f; }
+                else { float inv = 1.0f / misPdf; for(int k = 0; k < 3; k++) tp[k] *= inv; }
+            }
+            float em[3];
+            env_emit(E, dir, em);
+            if(depth + 1u <= P->maxDepth)
+                for(int k = 0; k < 3; k++) rad[k] += em[k] * tp[k];
+            break;
+        }
         const orc_pt_surface* sf = &J->surfaces[inst];
         uint32_t localPrim = hk.primKey - sf->primKeyBase;
         const float* tri9 = &sf->triangles[9 * localPrim];
@@ -373,27 +615,42 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
         const int isSpec = specularity(sf) >= SPECULAR_THRESHOLD;
 
         /* ---- NEE (WorkFunctionNEE); no shadow ray for specular materials ---- */
-        if(P->sampleMode != ORC_PT_PURE && J->nLights > 0 && !isSpec)
+        if(P->sampleMode != ORC_PT_PURE && nAll > 0 && !isSpec)
         {
             float dXi = rnd(key, depth, 3);
-            uint32_t li = (uint32_t)(dXi * (float)J->nLights);
-            if(li > J->nLights - 1u) li = J->nLights - 1u;
-            const orc_pt_light_tri* L = &J->lights[li];
-            float r1 = sqrtf(rnd(key, depth, 4)), r2 = rnd(key, depth, 5);
-            float a = 1.0f - r1, b = (1.0f - r2) * r1, c = r1 * r2;
-            float lp[3];
-            for(int k = 0; k < 3; k++) lp[k] = L->p0[k] * a + L->p1[k] * b + L->p2[k] * c;
-            float sd[3] = { pos[0] - lp[0], pos[1] - lp[1], pos[2] - lp[2] };
-            float distSq = dot3f(sd, sd);
-            normalize3f(sd);
-            float ndl = dot3f(L->n, sd);
-            ndl = L->twoSided ? fabsf(ndl) : fmaxf(0.0f, ndl);
-            float ppdf = (ndl == 0.0f) ? 0.0f : (1.0f / L->area) / ndl;
-            ppdf *= distSq;
-            float lightPdf = invN * ppdf;
+            uint32_t li = (uint32_t)(dXi * (float)nAll);
+            if(li > nAll - 1u) li = nAll - 1u;
+            float lp[3], lightPdf;
             float emis[3] = { 0, 0, 0 };
-            if(L->twoSided || dot3f(L->n, sd) > 0.0f)
-                for(int k = 0; k < 3; k++) emis[k] = L->radiance[k];
+            if(li == J->nLights)
+            {
+                /* skysphere: a point sceneDiameter away along the sampled direction */
+                float wd[3], spdf;
+                env_sample(E, rnd(key, depth, 4), rnd(key, depth, 5), wd, &spdf);
+                for(int k = 0; k < 3; k++) lp[k] = pos[k] + wd[k] * E->sceneDiameter;
+                float sd[3] = { pos[0] - lp[0], pos[1] - lp[1], pos[2] - lp[2] };
+                normalize3f(sd);
+                float toward[3] = { -sd[0], -sd[1], -sd[2] };
+                env_emit(E, toward, emis);
+                lightPdf = invN * spdf;
+            }
+            else
+            {
+                const orc_pt_light_tri* L = &J->lights[li];
+                float r1 = sqrtf(rnd(key, depth, 4)), r2 = rnd(key, depth, 5);
+                float a = 1.0f - r1, b = (1.0f - r2) * r1, c = r1 * r2;
+                for(int k = 0; k < 3; k++) lp[k] = L->p0[k] * a + L->p1[k] * b + L->p2[k] * c;
+                float sd[3] = { pos[0] - lp[0], pos[1] - lp[1], pos[2] - lp[2] };
+                float distSq = dot3f(sd, sd);
+                normalize3f(sd);
+                float ndl = dot3f(L->n, sd);
+                ndl = L->twoSided ? fabsf(ndl) : fmaxf(0.0f, ndl);
+                float ppdf = (ndl == 0.0f) ? 0.0f : (1.0f / L->area) / ndl;
+                ppdf *= distSq;
+                lightPdf = invN * ppdf;
+                if(L->twoSided || dot3f(L->n, sd) > 0.0f)
+                    for(int k = 0; k < 3; k++) emis[k] = L->radiance[k];
+            }
             float sdir[3] = { lp[0] - pos[0], lp[1] - pos[1], lp[2] - pos[2] };
             normalize3f(sdir);
             float nd[3] = { -sdir[0], -sdir[1], -sdir[2] };
@@ -576,12 +833,14 @@ static void* pt_worker(void* arg)
 }
 
 int orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
-                  const orc_pt_light_tri* lights, uint32_t nLights, float* image, int nthreads)
+                  const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
+                  float* image, int nthreads)
 {
     if(!s || !p || !surfaces || !image) return -1;
     pt_job J;
     memset(&J, 0, sizeof(J));
     J.scene = s; J.p = p; J.surfaces = surfaces; J.lights = lights; J.nLights = nLights;
+    J.env = env;
     J.image = image;
     atomic_init(&J.nextRow, 0u);
     if(nthreads < 1) nthreads = 1;

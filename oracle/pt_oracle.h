@@ -62,10 +62,39 @@ typedef struct
     int      twoSided;
 } orc_pt_light_tri;
 
+/* Skysphere boundary light with a spherical (lat-long) radiance map
+ * (LightSkysphere<SphericalCoordConverter>).  A 1x1 map is a constant
+ * radiance, sampled uniformly over uv. */
+typedef struct
+{
+    uint32_t     width, height;
+    const float* texels;        /* RGBA f32 per texel, row-major, row 0 at v = 0 */
+    const float* cdfX;          /* width * height row CDFs (orc_pwc2d_build) */
+    const float* cdfY;          /* height: marginal CDF */
+    float        m[12];         /* ApplyV rows (translation ignored) */
+    float        inv[12];       /* InvApplyV rows */
+    float        sceneDiameter; /* orc_scene_diameter */
+} orc_pt_env;
+
 /* Accumulates spp samples per pixel into image (R, G, B, weight) per pixel,
- * row 0 at the bottom of the image plane. */
+ * row 0 at the bottom of the image plane.  env may be NULL (no boundary
+ * light); it is the last light of the uniform light sampler. */
 int  orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
-                   const orc_pt_light_tri* lights, uint32_t nLights, float* image, int nthreads);
+                   const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
+                   float* image, int nthreads);
+
+/* Piecewise-constant 2D distribution (Source/Tracer/Distributions.h/.cu). */
+void  orc_pwc2d_build(const float* func, uint32_t w, uint32_t h, float* cdfX, float* cdfY);
+void  orc_pwc2d_sample_uv(const float* cdfX, const float* cdfY, uint32_t w, uint32_t h,
+                          const float xi[2], float uv[2], float* pdf);
+float orc_pwc2d_pdf_uv(const float* cdfX, const float* cdfY, uint32_t w, uint32_t h, const float uv[2]);
+/* Luminance of every texel of an RGBA map, read at texel centres through the
+ * bilinear filter (ColorConverter.cu:405-475). */
+void  orc_env_luminance(const float* texels, uint32_t w, uint32_t h, float* out);
+/* Bilinear, wrap-addressed read (TextureViewCPU.h:196-375). */
+void  orc_env_read(const float* texels, uint32_t w, uint32_t h, const float uv[2], float rgb[3]);
+void  orc_env_dir_to_uv(const float dirYUp[3], float uv[2]);
+void  orc_env_uv_to_dir(const float uv[2], float dirYUp[3]);
 void orc_pt_camera_frame(const float pos[3], const float gaze[3], const float up[3],
                          float fovX, float fovY, float nearT, float farT, orc_pt_params* p);
 void orc_pt_make_light(const float m[12], const float* v9, const float radiance[3], int twoSided,

@@ -90,3 +90,56 @@ def test_mixed_materials_per_pixel(mixed, mode):
     assert frac >= 0.97, frac
     assert rel_kept <= 1e-5, rel_kept
     assert abs(g.mean() - o.mean()) <= 0.05 * o.mean()
+
+
+# ---- skysphere boundary light ---------------------------------------------
+
+def _sky_pair(env_kwargs):
+    pt = PathTracer(0)
+    surf = load_box_scene(pt, scenes.sky_scene(0))
+    pt.set_env(env_kwargs["texels"], env_kwargs.get("m34"))
+    return pt, oracle.PtScene(surf, env=env_kwargs)
+
+
+def _compare(pt, S, mode, spp=16, size=64, seed=11):
+    cam = scenes.box_camera()
+    g = _img(pt.render(PathTracer.params(size, size, spp, cam, sample_mode=mode, seed=seed)))
+    o = _img(S.render(S.params(size, size, spp, cam, sample_mode=mode, seed=seed)))
+    close = np.abs(g - o) <= 1e-4 * (1.0 + np.abs(o))
+    return g, o, close.all(axis=-1).mean()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_sky_scene_per_pixel(mode):
+    """Open scene under a sun-and-sky map: misses see the sky (with MIS
+    against the importance-sampled sky in NEE+MIS mode), NEE picks the sky
+    or the area light.  Library atan2 / acos / sin differ by ulps between
+    CUDA and the host, so a few paths may part."""
+    pt, S = _sky_pair(dict(texels=scenes.sky_map(64, 32, seed=0)))
+    g, o, frac = _compare(pt, S, mode)
+    print("sky mode %d: close %.4f relMSE %.3g" % (mode, frac, relmse(g, o)))
+    assert frac >= 0.97, frac
+    assert relmse(g, o) <= 1e-3
+    pt.close()
+
+
+def test_sky_constant_and_rotated():
+    """A 1 x 1 map (constant radiance, uniform sampling) and a map rotated
+    about +y by a rational rotation."""
+    pt, S = _sky_pair(dict(texels=np.full((1, 1, 4), 0.8, np.float32)))
+    g, o, frac = _compare(pt, S, 2)
+    assert frac >= 0.97 and relmse(g, o) <= 1e-3, (frac, relmse(g, o))
+    pt.close()
+    c, s = 0.6, 0.8
+    m = np.array([c, 0, s, 0, 0, 1, 0, 0, -s, 0, c, 0], np.float32)
+    pt, S = _sky_pair(dict(texels=scenes.sky_map(64, 32, seed=4), m34=m))
+    g, o, frac = _compare(pt, S, 2)
+    assert frac >= 0.97 and relmse(g, o) <= 1e-3, (frac, relmse(g, o))
+    pt.close()
+
+
+def test_sky_scene_aabb_matches_oracle():
+    """SceneAABB (and from it the sky's scene diameter) equals the oracle's."""
+    pt, S = _sky_pair(dict(texels=scenes.sky_map(16, 8, seed=0)))
+    assert np.array_equal(pt.acc.scene_aabb(), S.scene_aabb())
+    pt.close()
