@@ -214,6 +214,11 @@ typedef struct mrg_pt_params
     float    fov[2];             /* radians, x and y */
     float    nearFar[2];
     uint32_t sampleStart;        /* index of the first sample (continue an accumulation) */
+    uint32_t partitionByMaterial;/* group paths by work key (miss, light, material
+                                    group) before every shade, as MRay's
+                                    RayPartitioner does: 1 always, 0 never
+                                    (shade in hit order), 2 when the scene has
+                                    more than one material group or a skysphere */
 } mrg_pt_params;
 
 /* Surface description of an instance, the equivalent of attaching a
@@ -239,6 +244,24 @@ typedef struct mrg_pt_material
 mrg_status mrg_pt_set_material(mrg_ctx* ctx, uint32_t instance_id, const mrg_pt_material* material);
 mrg_status mrg_pt_set_area_light(mrg_ctx* ctx, uint32_t instance_id, const float radiance[3],
                                  uint32_t two_sided);
+
+/* ---- Ray partitioning ---------------------------------------------------- */
+/* RayPartitioner::MultiPartition (Source/Tracer/RayPartitioner.cu:263-411):
+ * a stable sort of the n (key, index) pairs by the key's batch bits and, unless
+ * only_sort_for_batches, its data bits below them (bit ranges [begin, end)),
+ * then the runs of equal batch bits: *d_partition_count runs, run i starting at
+ * d_partition_offsets[i] with key d_partition_keys[i] (the sorted key there),
+ * and d_partition_offsets[count] = n.  Entries past max_partitions are not
+ * written (the count is still exact; offsets[count] is written only when
+ * count <= max_partitions).  d_indices == NULL sorts the identity 0..n-1.
+ * Inputs are not modified.  Device buffers; stream-ordered, no host
+ * synchronisation.  n <= 2^28. */
+mrg_status mrg_multi_partition(mrg_ctx* ctx, const uint32_t* d_keys, const uint32_t* d_indices, uint32_t n,
+                               const uint32_t key_data_bits[2], const uint32_t key_batch_bits[2],
+                               uint32_t only_sort_for_batches,
+                               uint32_t* d_sorted_keys, uint32_t* d_sorted_indices,
+                               uint32_t* d_partition_count, uint32_t* d_partition_offsets,
+                               uint32_t* d_partition_keys, uint32_t max_partitions, void* stream);
 
 /* Skysphere boundary light (LightGroupSkysphere<SphericalCoordConverter>,
  * Source/Tracer/LightsDefault.hpp:300-420, 700-915): a lat-long radiance map

@@ -30,7 +30,7 @@ EXPORTED = [
     "mrg_cast_visibility", "mrg_cast_closest_host", "mrg_scene_aabb", "mrg_get_stats",
     "mrg_sync_status", "mrg_cast_closest_stats", "mrg_cast_closest_host_noalloc",
     "mrg_pt_set_lambert", "mrg_pt_set_area_light", "mrg_pt_camera_frame", "mrg_pt_render",
-    "mrg_pt_set_material", "mrg_pt_set_env",
+    "mrg_pt_set_material", "mrg_pt_set_env", "mrg_multi_partition",
 ]
 
 MRG_MAT_LAMBERT, MRG_MAT_REFLECT, MRG_MAT_REFRACT, MRG_MAT_UNREAL = 0, 1, 2, 3
@@ -51,7 +51,8 @@ class MrgPtParams(C.Structure):
                 ("samplesPerPass", C.c_uint32), ("rrStart", C.c_uint32), ("maxDepth", C.c_uint32),
                 ("sampleMode", C.c_uint32), ("seed", C.c_uint32), ("filterRadius", C.c_float),
                 ("camPos", C.c_float * 3), ("camGaze", C.c_float * 3), ("camUp", C.c_float * 3),
-                ("fov", C.c_float * 2), ("nearFar", C.c_float * 2), ("sampleStart", C.c_uint32)]
+                ("fov", C.c_float * 2), ("nearFar", C.c_float * 2), ("sampleStart", C.c_uint32),
+                ("partitionByMaterial", C.c_uint32)]
 
 #: capacity of mrg_cast_closest_host_noalloc (rays per call)
 MRG_NOALLOC_MAX_RAYS = 262144
@@ -103,6 +104,7 @@ def _declare(lib):
         "mrg_pt_set_material": (C.c_int, [vp, u32, C.POINTER(MrgPtMaterial)]),
         "mrg_pt_set_area_light": (C.c_int, [vp, u32, fp, u32]),
         "mrg_pt_set_env": (C.c_int, [vp, u32, u32, vp, vp]),
+        "mrg_multi_partition": (C.c_int, [vp, vp, vp, u32, vp, vp, u32, vp, vp, vp, vp, vp, u32, vp]),
         "mrg_pt_camera_frame": (C.c_int, [C.POINTER(MrgPtParams), fp]),
         "mrg_pt_render": (C.c_int, [vp, C.POINTER(MrgPtParams), vp, vp]),
     }

@@ -4,6 +4,7 @@
 #include "mray_gb300.h"
 #include "mrg_build.h"
 #include "mrg_pt.h"
+#include "mrg_partition.h"
 
 #include <cuda_runtime.h>
 
@@ -83,6 +84,7 @@ struct mrg_ctx
     void*     dPtLights = nullptr;
     void*     dPtTris = nullptr;
     uint32_t  ptSurfaceCount = 0, ptLightCount = 0, ptTriCount = 0;
+    uint32_t  ptMaterialGroups = 0;          // distinct material groups among surfaces
     mrg::PtPaths ptPaths{};
     void*     ptPathMem = nullptr;
     // skysphere boundary light: host copy of the radiance map and transform,
@@ -93,6 +95,10 @@ struct mrg_ctx
     float              ptEnvM[12] = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0 };
     void*              dPtEnv = nullptr;
     mrg::PtEnv         ptEnv{};
+
+    // ray partitioner scratch (grow-only)
+    uint32_t* dPartScratch = nullptr;
+    size_t    partScratchWords = 0;
 
     // staging for the host-buffer cast
     mrg_ray*      dStageRays = nullptr;

@@ -93,8 +93,16 @@ struct PtPaths
     uint32_t* listB;
     uint32_t* shadowList;
     uint32_t* counts;        // [0] list A count, [1] list B count, [2] shadow count, [3] pad
+    uint32_t* workKeys;      // work key per alive entry (partitioning)
+    uint32_t* workKeysOut;
+    uint32_t* listSorted;    // alive list grouped by work key
+    uint32_t* sortHist;      // multi-split count table
     uint32_t  capacity;
 };
+
+// Work keys of the partition before shading: miss, light, then one per
+// material group (PtMaterial).
+constexpr uint32_t kPtWorkKeyBits = 3;
 
 cudaError_t pt_raygen(const PtLaunch& L, const PtPaths& P, uint32_t* aliveList, uint32_t* aliveCount,
                       int smCount, cudaStream_t st);
@@ -102,6 +110,8 @@ cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSurface* 
                           const PtLight* lights, const float4* tris, uint32_t nTris,
                           const uint32_t* aliveList, const uint32_t* aliveCount,
                           uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st);
+cudaError_t pt_work_keys(const PtPaths& P, const PtSurface* surfaces, uint32_t nSurfaces,
+                         const uint32_t* aliveList, const uint32_t* aliveCount, int smCount, cudaStream_t st);
 cudaError_t pt_resolve(const PtLaunch& L, const PtPaths& P, uint32_t depth, int smCount, cudaStream_t st);
 cudaError_t pt_film(const PtLaunch& L, const PtPaths& P, float4* image, cudaStream_t st);
 

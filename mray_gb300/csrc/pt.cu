@@ -792,6 +792,28 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
     }
 }
 
+// Work key of every alive path (KCGenerateSurfaceWorkKeysIndirect,
+// RendererCommon.h:14): 0 miss (boundary light), 1 area light, 2 + material
+// group.
+__global__ void __launch_bounds__(kPtTPB)
+k_work_keys(PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t nSurfaces,
+            const uint32_t* __restrict__ aliveList, const uint32_t* __restrict__ aliveCount)
+{
+    const uint32_t n = *aliveCount;
+    for(uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    {
+        const uint4 hk = P.hits[aliveList[k]];
+        const uint32_t s = hk.z & 0x00FFFFFFu;
+        uint32_t key = 0u;
+        if(hk.x != kMissMark && s < nSurfaces)
+        {
+            const uint4 info = surfaces[s].info;
+            key = info.x ? 1u : 2u + min(info.w, 5u);
+        }
+        P.workKeys[k] = key;
+    }
+}
+
 // Adds the radiance of every shadow ray that reached its light
 // (KCAccumulateShadowRaysPT; the depth limit was applied when it was cast).
 __global__ void __launch_bounds__(kPtTPB)
@@ -852,6 +874,13 @@ cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSurface* 
 {
     k_shade<<<(unsigned)smCount * 8u, kPtTPB, 0, st>>>(L, P, surfaces, nSurfaces, lights, tris, nTris,
                                                      aliveList, aliveCount, nextList, nextCount);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_work_keys(const PtPaths& P, const PtSurface* surfaces, uint32_t nSurfaces,
+                         const uint32_t* aliveList, const uint32_t* aliveCount, int smCount, cudaStream_t st)
+{
+    k_work_keys<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, surfaces, nSurfaces, aliveList, aliveCount);
     return cudaGetLastError();
 }
 

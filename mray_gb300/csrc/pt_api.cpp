@@ -263,6 +263,10 @@ mrg_status pt_prepare(mrg_ctx* c)
     c->ptSurfaceCount = ni;
     c->ptLightCount = (uint32_t)lights.size();
     c->ptTriCount = maxPrim;
+    uint32_t groups = 0;
+    for(uint32_t i = 0; i < ni; i++)
+        if(c->ptDesc[i].kind == 1) groups |= 1u << std::min<uint32_t>(c->ptDesc[i].material, 31u);
+    c->ptMaterialGroups = (uint32_t)__builtin_popcount(groups);
     mrg_status es = env_prepare(c);
     if(es != MRG_OK) return es;
     c->ptDirty = false;
@@ -278,8 +282,9 @@ mrg_status pt_paths(mrg_ctx* c, uint32_t slots)
     const size_t n = slots;
     const size_t words = (n + 31) / 32;
     // one allocation, every array 256-byte aligned
-    const size_t sizes[13] = { n * 32, n * 16, n * 8, n * 16, n * 16, n * 4, n * 32, n * 16,
-                               words * 4, n * 4, n * 4, n * 4, 64 };
+    const size_t sizes[17] = { n * 32, n * 16, n * 8, n * 16, n * 16, n * 4, n * 32, n * 16,
+                               words * 4, n * 4, n * 4, n * 4, 64, n * 4, n * 4, n * 4,
+                               4 * mrg::multisplit_hist_words(slots, mrg::kPtWorkKeyBits) };
     size_t need = 0;
     for(size_t sz : sizes) need += (sz + 255) & ~size_t(255);
     char* base = nullptr;
@@ -302,6 +307,10 @@ mrg_status pt_paths(mrg_ctx* c, uint32_t slots)
     P.listB = reinterpret_cast<uint32_t*>(take());
     P.shadowList = reinterpret_cast<uint32_t*>(take());
     P.counts = reinterpret_cast<uint32_t*>(take());
+    P.workKeys = reinterpret_cast<uint32_t*>(take());
+    P.workKeysOut = reinterpret_cast<uint32_t*>(take());
+    P.listSorted = reinterpret_cast<uint32_t*>(take());
+    P.sortHist = reinterpret_cast<uint32_t*>(take());
     P.capacity = slots;
     return MRG_OK;
 }
@@ -393,8 +402,9 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
     if(!c->built) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_pt_render: call mrg_build first");
     if(p->width == 0 || p->height == 0 || p->spp == 0)
         return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: empty image or zero samples");
-    if(p->maxDepth == 0 || p->maxDepth > 255 || p->sampleMode > MRG_PT_NEE_MIS)
-        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: maxDepth must be in [1, 255], sampleMode in [0, 2]");
+    if(p->maxDepth == 0 || p->maxDepth > 255 || p->sampleMode > MRG_PT_NEE_MIS || p->partitionByMaterial > 2u)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: maxDepth must be in [1, 255], sampleMode and "
+                                                   "partitionByMaterial in [0, 2]");
     const uint64_t wh = (uint64_t)p->width * p->height;
     uint32_t spp = p->samplesPerPass ? p->samplesPerPass : std::max<uint32_t>(1, (uint32_t)std::min<uint64_t>(p->spp, (1ull << 22) / wh));
     spp = std::min(spp, p->spp);
@@ -422,6 +432,8 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
     L.filterSigma = p->filterRadius * 0.285714f;
     camera_frame(*p, L.cam);
     mrg::PtPaths& P = c->ptPaths;
+    const bool partition = p->partitionByMaterial == 1u ||
+                           (p->partitionByMaterial == 2u && (c->ptMaterialGroups > 1u || c->ptEnvSet));
     mrg::TraceScratch scr;
     scr.workCounter = c->dScratch;
     scr.errorFlag = c->dScratch + 1;
@@ -443,7 +455,18 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
             PT_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), st), "reset");
             PT_TRY(mrg::launch_closest(c->scene, scr, P.rays, alive, 0, P.hits, P.meta, c->smCount, st,
                                        aliveCount), "closest hit");
-            PT_TRY(mrg::pt_shade_impl(L, P, surf, c->ptSurfaceCount, lights, tris, c->ptTriCount, alive,
+            const uint32_t* shadeList = alive;
+            if(partition)
+            {
+                mrg::DigitSpec ks;
+                ks.batchShift = 0; ks.batchWidth = mrg::kPtWorkKeyBits;
+                ks.digitShift = 0; ks.digitBits = mrg::kPtWorkKeyBits;
+                PT_TRY(mrg::pt_work_keys(P, surf, c->ptSurfaceCount, alive, aliveCount, c->smCount, st), "work keys");
+                PT_TRY(mrg::multisplit_pass(P.workKeys, alive, P.workKeysOut, P.listSorted, aliveCount, slots, ks,
+                                            P.sortHist, st), "partition");
+                shadeList = P.listSorted;
+            }
+            PT_TRY(mrg::pt_shade_impl(L, P, surf, c->ptSurfaceCount, lights, tris, c->ptTriCount, shadeList,
                                       aliveCount, next, nextCount, c->smCount, st), "shade");
             PT_TRY(mrg::launch_visibility(c->scene, scr, P.visBits, P.shadowRays, P.shadowList, 0,
                                           c->smCount, st, P.counts + 2), "shadow rays");

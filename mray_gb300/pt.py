@@ -70,13 +70,14 @@ class PathTracer:
 
     @staticmethod
     def params(width, height, spp, camera, max_depth=8, rr_start=3, sample_mode=N.MRG_PT_NEE_MIS,
-               seed=0, filter_radius=1.0, samples_per_pass=0, sample_start=0):
+               seed=0, filter_radius=1.0, samples_per_pass=0, sample_start=0, partition="auto"):
         p = N.MrgPtParams()
         p.width, p.height, p.spp = width, height, spp
         p.samplesPerPass = samples_per_pass
         p.rrStart, p.maxDepth = rr_start, max_depth
         p.sampleMode, p.seed = sample_mode, seed
         p.filterRadius = filter_radius
+        p.partitionByMaterial = 2 if partition == "auto" else (1 if partition else 0)
         p.camPos[:] = [float(x) for x in camera["pos"]]
         p.camGaze[:] = [float(x) for x in camera["gaze"]]
         p.camUp[:] = [float(x) for x in camera["up"]]

@@ -421,3 +421,33 @@ class PtScene:
                              C.byref(self.env) if self.env is not None else None,
                              _vp(img), threads or default_threads())
         return img
+
+
+def multi_partition(keys, indices=None, key_data_bits=(0, 0), key_batch_bits=(0, 32),
+                    only_sort_for_batches=False):
+    """RayPartitioner::MultiPartition (Source/Tracer/RayPartitioner.cu:263-411):
+    stable radix sort of (key, index) by the data bits then the batch bits
+    (one sort over the joined range when they are contiguous; the batch bits
+    alone when only_sort_for_batches), then KCFindSplits (:19-49) marks where
+    the batch portion changes and KCFindBinMatIds (:51-75) gathers each run's
+    start offset and key.  Returns (count, offsets[count + 1], keys[count],
+    sorted indices, sorted keys)."""
+    k = np.asarray(keys, np.uint64).ravel()
+    n = k.shape[0]
+    idx = np.arange(n, dtype=np.uint64) if indices is None else np.asarray(indices, np.uint64).ravel()
+
+    def bits(v, r):
+        w = r[1] - r[0]
+        return (v >> np.uint64(r[0])) & np.uint64((1 << w) - 1)
+
+    comp = bits(k, key_batch_bits)
+    if not only_sort_for_batches:
+        comp = (comp << np.uint64(key_data_bits[1] - key_data_bits[0])) | bits(k, key_data_bits)
+    order = np.argsort(comp, kind="stable")
+    sk, si = k[order], idx[order]
+    if n == 0:
+        return 0, np.zeros(1, np.uint32), np.zeros(0, np.uint32), si.astype(np.uint32), sk.astype(np.uint32)
+    b = bits(sk, key_batch_bits)
+    starts = np.concatenate([[0], np.nonzero(b[1:] != b[:-1])[0] + 1]).astype(np.uint32)
+    offsets = np.concatenate([starts, [n]]).astype(np.uint32)
+    return (len(starts), offsets, sk[starts].astype(np.uint32), si.astype(np.uint32), sk.astype(np.uint32))

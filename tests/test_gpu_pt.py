@@ -143,3 +143,17 @@ def test_sky_scene_aabb_matches_oracle():
     pt, S = _sky_pair(dict(texels=scenes.sky_map(16, 8, seed=0)))
     assert np.array_equal(pt.acc.scene_aabb(), S.scene_aabb())
     pt.close()
+
+
+def test_partition_by_material_is_invisible():
+    """Grouping paths by work key before shading changes only the order of
+    work, never a path: images with and without it are bit-identical."""
+    pt = PathTracer(0)
+    load_box_scene(pt, scenes.box_scene_mixed(0))
+    pt.set_env(scenes.sky_map(32, 16, seed=1))
+    cam = scenes.box_camera()
+    for mode in (0, 2):
+        a = pt.render(PathTracer.params(80, 60, 8, cam, sample_mode=mode, seed=2, partition=True))
+        b = pt.render(PathTracer.params(80, 60, 8, cam, sample_mode=mode, seed=2, partition=False))
+        assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
+    pt.close()
