@@ -274,6 +274,20 @@ mrg_status mrg_multi_partition(mrg_ctx* ctx, const uint32_t* d_keys, const uint3
 mrg_status mrg_pt_set_env(mrg_ctx* ctx, uint32_t width, uint32_t height, const float* rgba,
                           const float m3x4[12]);
 
+/* Spectral rendering (SpectrumContextJakob2019, Source/Tracer/SpectrumContext.{h,hpp,cu};
+ * SpectraPerSpectrum = 4, hyperbolic wavelength sampling, the renderer's
+ * default): lut = the float data of an MR_SPECTRA file (9 * lut_res^3 floats,
+ * [table][coefficient][z][y][x]); the CIE 1931 observer (cie_count x 3 from
+ * 360 nm in 1 nm steps), its integrals, the colour space's illuminant SPD and
+ * normalisation factor, and the XYZ -> RGB matrix (row-major), as MRay's
+ * colour tables hold them.  Everything is copied.  lut_res = 0 returns to RGB
+ * rendering.  Albedos and emissions stay RGB in the scene description and are
+ * converted per path (Converter::ConvertAlbedo / ConvertRadiance). */
+mrg_status mrg_pt_set_spectral(mrg_ctx* ctx, uint32_t lut_res, const float* lut, uint32_t cie_count,
+                               const float* cie_xyz, const float cie_integrals[3],
+                               const float* illuminant_spd, float illuminant_norm,
+                               const float xyz_to_rgb[9]);
+
 /* The pinhole frame MRay derives from the camera parameters
  * (CameraPinhole ctor, Source/Tracer/CamerasDefault.hpp:6-30): out = position[3],
  * bottomLeft[3], right[3], up[3], planeSize[2], near, far. */

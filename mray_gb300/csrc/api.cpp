@@ -128,6 +128,7 @@ mrg_status mrg_destroy(mrg_ctx* c)
     cudaFree(c->dStats);
     cudaFree(c->dPtSurfaces); cudaFree(c->dPtLights); cudaFree(c->dPtTris); cudaFree(c->ptPathMem);
     cudaFree(c->dPtEnv);
+    cudaFree(c->dPtSpec);
     cudaFree(c->dPartScratch);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);

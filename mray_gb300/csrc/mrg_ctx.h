@@ -95,6 +95,9 @@ struct mrg_ctx
     float              ptEnvM[12] = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0 };
     void*              dPtEnv = nullptr;
     mrg::PtEnv         ptEnv{};
+    // spectral context: device block [lut | observer | illuminant]
+    void*              dPtSpec = nullptr;
+    mrg::PtSpectral    ptSpec{};
 
     // ray partitioner scratch (grow-only)
     uint32_t* dPartScratch = nullptr;

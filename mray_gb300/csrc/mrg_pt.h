@@ -52,6 +52,18 @@ struct PtEnv
     uint32_t      enabled;
 };
 
+// Spectral context (Jakob & Hanika 2019 RGB -> spectrum, 4 wavelengths per
+// path; Source/Tracer/SpectrumContext.{h,hpp,cu}).
+struct PtSpectral
+{
+    const float* lut;            // 9 * res^3: [table][coefficient][z][y][x]
+    const float* observer;       // cieCount * 3, divided by the CIE integrals
+    const float* illuminant;     // cieCount, scaled by Y integral / norm factor
+    float        xyzToRgb[9];
+    uint32_t     lutRes, cieCount;
+    uint32_t     enabled;
+};
+
 struct PtCamera
 {
     float pos[3];
@@ -75,6 +87,7 @@ struct PtLaunch
     float    filterSigma;
     PtCamera cam;
     PtEnv    env;
+    PtSpectral spec;
 };
 
 // Path state, structure of arrays (device).
@@ -83,8 +96,11 @@ struct PtPaths
     float4*   rays;          // 2 per slot (RayGMem)
     uint4*    hits;          // HitKeyPack per slot
     float2*   meta;          // MetaHit per slot
-    float4*   thr;           // throughput xyz, w = pdf of the last BxDF sample
-    float4*   rad;           // radiance xyz, w = film weight
+    float4*   thr;           // throughput (RGB in xyz, or 4 wavelengths)
+    float4*   rad;           // radiance (RGB in xyz, or 4 wavelengths)
+    float*    prevPdf;       // pdf of the last BxDF sample (MIS)
+    float4*   waves;         // spectral: wavelengths of the path
+    float4*   wavePdf;       // spectral: their sampling pdfs
     uint32_t* state;         // depth | type << 8
     float4*   shadowRays;    // 2 per slot
     float4*   shadowRad;

@@ -1,4 +1,5 @@
-// pt.cu -- wavefront path tracer kernels (RGB, NEE + MIS, Russian roulette).
+// pt.cu -- wavefront path tracer kernels (RGB or 4-wavelength spectral, NEE +
+// MIS, Russian roulette).
 //
 // The estimator is MRay's (Source/TracerDLL/PathTracerRendererShaders.h:
 // 203-300 BxDF sample + RR, 354-445 NEE, 450-517 light hits with MIS;
@@ -184,14 +185,30 @@ __device__ __forceinline__ float unreal_ratio(const PtSurface& m, float avg)
     const float total = add(specR, integ);
     return (total == 0.0f) ? 0.0f : __fdiv_rn(integ, total);
 }
-__device__ __forceinline__ float avg_albedo(const PtSurface& m)
+
+// Channel values of a colour: RGB (3) or 4 sampled wavelengths.
+struct Chan { float v[4]; };
+
+__device__ __forceinline__ Chan chan(float a, float b, float c, float d)
 {
-    return mul(add(add(m.albedo.x, m.albedo.y), m.albedo.z), 0.3333f);
+    Chan r; r.v[0] = a; r.v[1] = b; r.v[2] = c; r.v[3] = d; return r;
 }
-__device__ __forceinline__ float specularity(const PtSurface& m)
+__device__ __forceinline__ Chan chan(float4 f) { return chan(f.x, f.y, f.z, f.w); }
+__device__ __forceinline__ float4 f4(const Chan& c) { return make_float4(c.v[0], c.v[1], c.v[2], c.v[3]); }
+
+// albedo.Sum() * 0.3333 over the Spectrum's channels (MaterialsDefault.hpp:548)
+template<int NC>
+__device__ __forceinline__ float avg_albedo(const Chan& a)
+{
+    float s = add(add(a.v[0], a.v[1]), a.v[2]);
+    if(NC == 4) s = add(s, a.v[3]);
+    return mul(s, 0.3333f);
+}
+template<int NC>
+__device__ __forceinline__ float specularity(const PtSurface& m, const Chan& alb)
 {
     if(m.info.w == kMatReflect || m.info.w == kMatRefract) return 1.0f;
-    if(m.info.w == kMatUnreal) return sub(1.0f, unreal_ratio(m, avg_albedo(m)));
+    if(m.info.w == kMatUnreal) return sub(1.0f, unreal_ratio(m, avg_albedo<NC>(alb)));
     return 0.0f;
 }
 __device__ __forceinline__ float f0_of(const PtSurface& m, float alb)
@@ -199,7 +216,8 @@ __device__ __forceinline__ float f0_of(const PtSurface& m, float alb)
     return add(mul(mul(m.mat.y, 0.08f), sub(1.0f, m.mat.x)), mul(alb, m.mat.x));
 }
 // UnrealMaterial::Evaluate + Pdf (V, L in the tangent frame).
-__device__ __forceinline__ float3 unreal_eval(const PtSurface& m, float3 V, float3 L, float& pdfOut)
+template<int NC>
+__device__ __forceinline__ Chan unreal_eval(const PtSurface& m, const Chan& alb, float3 V, float3 L, float& pdfOut)
 {
     const float rough = m.albedo.w;
     const float alpha = mul(rough, rough);
@@ -216,24 +234,23 @@ __device__ __forceinline__ float3 unreal_eval(const PtSurface& m, float3 V, floa
     G = (vdh == 0.0f) ? 0.0f : G;
     const float ndl = fmaxf(0.0f, L.z);
     const float corr = burley(ndl, ndv, ldh, rough);
-    const float alb[3] = { m.albedo.x, m.albedo.y, m.albedo.z };
-    float out[3];
+    Chan out = chan(0, 0, 0, 0);
 #pragma unroll
-    for(int k = 0; k < 3; k++)
+    for(int k = 0; k < NC; k++)
     {
-        const float F = schlick1(vdh, f0_of(m, alb[k]));
+        const float F = schlick1(vdh, f0_of(m, alb.v[k]));
         const float spec = (ndv == 0.0f) ? 0.0f : __fdiv_rn(mul(mul(mul(Dn, F), G), 0.25f), ndv);
-        const float diff = mul(mul(mul(ndl, mul(sub(1.0f, m.mat.x), alb[k])), kInvPi), corr);
-        out[k] = add(diff, spec);
+        const float diff = mul(mul(mul(ndl, mul(sub(1.0f, m.mat.x), alb.v[k])), kInvPi), corr);
+        out.v[k] = add(diff, spec);
     }
-    const float ratio = unreal_ratio(m, avg_albedo(m));
+    const float ratio = unreal_ratio(m, avg_albedo<NC>(alb));
     float pd = mul(L.z, kInvPi);
     pd = (pd <= 1.0e-5f) ? 0.0f : pd;
     float ps = vndf_pdf(V, H, alpha);
     ps = dBad ? 0.0f : ps;
     ps = (vdh == 0.0f) ? 0.0f : __fdiv_rn(ps, mul(4.0f, vdh));
     pdfOut = add(mul(pd, ratio), mul(ps, sub(1.0f, ratio)));
-    return make_float3(out[0], out[1], out[2]);
+    return out;
 }
 __device__ __forceinline__ float fresnel_dielectric(float cosF, float etaF, float etaB)
 {
@@ -381,6 +398,172 @@ __device__ float3 env_sample(const PtEnv& E, float xi0, float xi1, float& pdf)
     return rows_apply(E.m, make_float3(mul(sT, sP), cP, mul(cT, sP)));
 }
 
+// ---------------------------------------------------------------------------
+// Spectral (SpectrumContext.hpp:36-152, SpectrumContext.cu:40-170): the host
+// backend's linear texture reads (texel = uv * n - 0.5, modf with negative
+// fractions made absolute, clamp), MRay's arithmetic order.
+// ---------------------------------------------------------------------------
+constexpr float kCieStart = 360.0f;
+
+__device__ __forceinline__ void tex_axis(float uv, uint32_t n, int32_t& i0, int32_t& i1, float& frac)
+{
+    const float t = sub(mul(uv, (float)n), 0.5f);
+    float b;
+    float f = modff(t, &b);
+    int32_t s = (int32_t)b;
+    if(f < 0.0f) { s -= 1; f = fabsf(f); }
+    const int32_t hi = (int32_t)n - 1;
+    i0 = s < 0 ? 0 : (s > hi ? hi : s);
+    i1 = (s + 1) < 0 ? 0 : ((s + 1) > hi ? hi : (s + 1));
+    frac = f;
+}
+__device__ __forceinline__ float lerp_(float a, float b, float t) { return add(mul(a, sub(1.0f, t)), mul(b, t)); }
+
+__device__ __forceinline__ float tex3d(const PtSpectral& S, uint32_t tex, float u, float v, float w)
+{
+    const uint32_t n = S.lutRes;
+    const float* t = S.lut + (size_t)tex * n * n * n;
+    int32_t a0, a1, b0, b1, c0, c1;
+    float fx, fy, fz;
+    tex_axis(u, n, a0, a1, fx);
+    tex_axis(v, n, b0, b1, fy);
+    tex_axis(w, n, c0, c1, fz);
+    auto T = [&](int32_t x, int32_t y, int32_t z) { return __ldg(&t[((size_t)z * n + (size_t)y) * n + (size_t)x]); };
+    const float p0 = lerp_(T(a0, b0, c0), T(a1, b0, c0), fx);
+    const float p1 = lerp_(T(a0, b1, c0), T(a1, b1, c0), fx);
+    const float p2 = lerp_(T(a0, b0, c1), T(a1, b0, c1), fx);
+    const float p3 = lerp_(T(a0, b1, c1), T(a1, b1, c1), fx);
+    return lerp_(lerp_(p0, p1, fy), lerp_(p2, p3, fy), fz);
+}
+
+__device__ __forceinline__ float inv_smoothstep(float y)
+{
+    return sub(0.5f, sinf(mul(asinf(sub(1.0f, mul(2.0f, y))), 1.0f / 3.0f)));
+}
+
+// SingleSampleSpectrumWavelength, HYPERBOLIC_PBRT (the default mode)
+__device__ __forceinline__ void sample_waves(float xi0, float4& waves, float4& pdf)
+{
+    const float off[4] = { -0.5f, -0.25f, 0.0f, 0.25f };
+    float w[4], p[4];
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+    {
+        float x = add(xi0, off[i]);
+        if(x < 0.0f) x = add(x, 1.0f);
+        if(x >= 1.0f) x = sub(x, 1.0f);
+        const float a = sub(0.85691062f, mul(1.82750197f, x));
+        const float l = sub(538.0f, mul(138.888889f, atanhf(a)));
+        float d = coshf(mul(0.0072f, sub(l, 538.0f)));
+        d = mul(d, d);
+        w[i] = l;
+        p[i] = __fdiv_rn(0.0039398042f, d);
+    }
+    waves = make_float4(w[0], w[1], w[2], w[3]);
+    pdf = make_float4(p[0], p[1], p[2], p[3]);
+}
+
+__device__ Chan convert_albedo(const PtSpectral& S, float r, float g, float b, const float4& waves)
+{
+    const float rgb[3] = { r, g, b };
+    uint32_t maxI = 0;
+    float mx = r;
+    if(g > mx) { mx = g; maxI = 1; }
+    if(b > mx) { mx = b; maxI = 2; }
+    float x = 0.0f, y = 0.0f;
+    if(mx > 1.0e-7f)
+    {
+        const float f = __fdiv_rn(1.0f, mx);
+        x = mul(rgb[(maxI + 1) % 3], f);
+        y = mul(rgb[(maxI + 2) % 3], f);
+    }
+    const float slice = mx < 0.0f ? 0.0f : (mx > 1.0f ? 1.0f : mx);
+    const float z = inv_smoothstep(inv_smoothstep(slice));
+    const float N = (float)S.lutRes;
+    const float A = __fdiv_rn(sub(N, 1.0f), N), B = __fdiv_rn(0.5f, N);
+    const float u = add(mul(x, A), B), v = add(mul(y, A), B), w = add(mul(z, A), B);
+    const float c0 = tex3d(S, 3 * maxI + 0, u, v, w);
+    const float c1 = tex3d(S, 3 * maxI + 1, u, v, w);
+    const float c2 = tex3d(S, 3 * maxI + 2, u, v, w);
+    const float wl[4] = { waves.x, waves.y, waves.z, waves.w };
+    Chan out;
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+    {
+        const float t = __fmaf_rn(c0, wl[i], c1);
+        const float xx = __fmaf_rn(t, wl[i], c2);
+        const float dr = __fdiv_rn(1.0f, __fsqrt_rn(__fmaf_rn(xx, xx, 1.0f)));
+        out.v[i] = __fmaf_rn(mul(0.5f, xx), dr, 0.5f);
+    }
+    return out;
+}
+
+__device__ __forceinline__ float tex1d(const float* tab, uint32_t n, float coord, uint32_t ch, uint32_t c)
+{
+    const float uv = __fdiv_rn(coord, (float)n);
+    int32_t i0, i1;
+    float f;
+    tex_axis(uv, n, i0, i1, f);
+    return lerp_(__ldg(&tab[(size_t)i0 * ch + c]), __ldg(&tab[(size_t)i1 * ch + c]), f);
+}
+
+__device__ Chan convert_radiance(const PtSpectral& S, float r, float g, float b, const float4& waves)
+{
+    float mx = r;
+    if(g > mx) mx = g;
+    if(b > mx) mx = b;
+    const float scale = mul(mx, 2.0f);
+    float c[3] = { 0.0f, 0.0f, 0.0f };
+    if(scale != 0.0f) { c[0] = __fdiv_rn(r, scale); c[1] = __fdiv_rn(g, scale); c[2] = __fdiv_rn(b, scale); }
+    Chan out = convert_albedo(S, c[0], c[1], c[2], waves);
+    const float wl[4] = { waves.x, waves.y, waves.z, waves.w };
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+        out.v[i] = mul(out.v[i], tex1d(S.illuminant, S.cieCount, add(wl[i], 0.5f - kCieStart), 1, 0));
+#pragma unroll
+    for(int i = 0; i < 4; i++) out.v[i] = mul(out.v[i], scale);
+    return out;
+}
+
+// ConvertSpectraToRGBSingle (no dispersion)
+__device__ float3 spectrum_to_rgb(const PtSpectral& S, const float4& value, const float4& waves, const float4& pdf)
+{
+    const float val[4] = { value.x, value.y, value.z, value.w };
+    const float wl[4] = { waves.x, waves.y, waves.z, waves.w };
+    const float pd[4] = { pdf.x, pdf.y, pdf.z, pdf.w };
+    float xyz[3] = { 0.0f, 0.0f, 0.0f };
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+    {
+        const float coord = add(wl[i], 0.5f - kCieStart);
+        const float v = (pd[i] == 0.0f) ? 0.0f : __fdiv_rn(val[i], pd[i]);
+#pragma unroll
+        for(int k = 0; k < 3; k++) xyz[k] = add(xyz[k], mul(tex1d(S.observer, S.cieCount, coord, 3, k), v));
+    }
+#pragma unroll
+    for(int k = 0; k < 3; k++) xyz[k] = mul(xyz[k], 0.25f);
+    float rgb[3];
+#pragma unroll
+    for(int r = 0; r < 3; r++)
+        rgb[r] = __fmaf_rn(S.xyzToRgb[3 * r + 2], xyz[2],
+                           __fmaf_rn(S.xyzToRgb[3 * r + 1], xyz[1], mul(S.xyzToRgb[3 * r], xyz[0])));
+    return make_float3(rgb[0], rgb[1], rgb[2]);
+}
+
+// The colour of an RGB triple on this path: itself, or its spectrum.
+template<bool SPEC>
+__device__ __forceinline__ Chan albedo_of(const PtSpectral& S, float r, float g, float b, const float4& waves)
+{
+    if(SPEC) return convert_albedo(S, r, g, b, waves);
+    return chan(r, g, b, 0.0f);
+}
+template<bool SPEC>
+__device__ __forceinline__ Chan radiance_of(const PtSpectral& S, float r, float g, float b, const float4& waves)
+{
+    if(SPEC) return convert_radiance(S, r, g, b, waves);
+    return chan(r, g, b, 0.0f);
+}
+
 __device__ __forceinline__ uint32_t slot_pixel(const PtLaunch& L, uint32_t i) { return i % (L.width * L.height); }
 __device__ __forceinline__ uint32_t slot_sample(const PtLaunch& L, uint32_t i)
 {
@@ -389,8 +572,10 @@ __device__ __forceinline__ uint32_t slot_sample(const PtLaunch& L, uint32_t i)
 
 // ---------------------------------------------------------------------------
 // Camera rays: pinhole (CamerasDefault.hpp:94-140), Gaussian film filter
-// sampled with Box-Muller (filter / pdf = 1 per sample, Filters.h:195-233).
+// sampled with Box-Muller (filter / pdf = 1 per sample, Filters.h:195-233);
+// spectral paths also draw their 4 wavelengths here.
 // ---------------------------------------------------------------------------
+template<bool SPEC>
 __global__ void __launch_bounds__(kPtTPB)
 k_raygen(PtLaunch L, PtPaths P, uint32_t* aliveList, uint32_t* aliveCount)
 {
@@ -416,17 +601,26 @@ k_raygen(PtLaunch L, PtPaths P, uint32_t* aliveList, uint32_t* aliveCount)
         P.rays[2 * (size_t)i] = make_float4(L.cam.pos[0], L.cam.pos[1], L.cam.pos[2], L.cam.nearT);
         P.rays[2 * (size_t)i + 1] = make_float4(d.x, d.y, d.z, L.cam.farT);
         P.hits[i].x = kMissMark;
-        P.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-        P.rad[i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        P.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+        P.rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        P.prevPdf[i] = 0.0f;
         P.state[i] = 0u;
+        if(SPEC)
+        {
+            float4 w, p;
+            sample_waves(rnd(key, 0, 9), w, p);
+            P.waves[i] = w;
+            P.wavePdf[i] = p;
+        }
         aliveList[i] = i;
     }
 }
 
 // ---------------------------------------------------------------------------
-// Shade: light hits (emission with MIS), surface hits (NEE + Lambert sample +
-// Russian roulette).  Live paths and shadow rays are appended to their lists
-// with one atomic per warp.
+// Shade: light hits (emission with MIS), misses (skysphere with MIS), surface
+// hits (NEE + BxDF sample + Russian roulette).  Live paths and shadow rays
+// are appended to their lists with one atomic per warp.  NC colour channels:
+// 3 (RGB) or 4 (wavelengths).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void warp_append(bool pred, uint32_t value, uint32_t* list, uint32_t* count)
 {
@@ -440,14 +634,33 @@ __device__ __forceinline__ void warp_append(bool pred, uint32_t value, uint32_t*
     if(pred) list[base + __popc(m & ((1u << lane) - 1u))] = value;
 }
 
+// throughput * prevPdf / (prevPdf + lightPdf): the balance heuristic with the
+// BxDF pdf cancelled (BalanceCancelled, DistributionFunctions.h:957).
+template<int NC>
+__device__ __forceinline__ Chan mis_weighted(Chan tp, float prevPdf, float lightPdf)
+{
+    const float misPdf = add(prevPdf, lightPdf);
+#pragma unroll
+    for(int k = 0; k < NC; k++) tp.v[k] = mul(tp.v[k], prevPdf);
+    if(misPdf == 0.0f) return chan(0, 0, 0, 0);
+    const float inv = __fdiv_rn(1.0f, misPdf);
+#pragma unroll
+    for(int k = 0; k < NC; k++) tp.v[k] = mul(tp.v[k], inv);
+    return tp;
+}
+
+template<bool SPEC>
 __global__ void __launch_bounds__(kPtTPB)
 k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t nSurfaces,
         const PtLight* __restrict__ lights, const float4* __restrict__ tris, uint32_t nTris,
         const uint32_t* __restrict__ aliveList, const uint32_t* __restrict__ aliveCount,
         uint32_t* nextList, uint32_t* nextCount)
 {
+    constexpr int NC = SPEC ? 4 : 3;
     const uint32_t n = *aliveCount;
     const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t nAll = L.nLights + (L.env.enabled ? 1u : 0u);
+    const float invN = nAll ? __fdiv_rn(1.0f, (float)nAll) : 0.0f;
     // warp-uniform trip count so every lane reaches the ballots
     const uint32_t first = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
     for(uint32_t base = first; base < n; base += stride)
@@ -464,6 +677,7 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
             uint32_t type = (st >> 8) & 3u;
             const uint32_t key = path_key(L.seed, slot_pixel(L, i), slot_sample(L, i));
             const uint32_t surfIdx = hk.z & 0x00FFFFFFu;
+            const float4 waves = SPEC ? P.waves[i] : make_float4(0, 0, 0, 0);
             if(hk.x != kMissMark && surfIdx < nSurfaces)
             {
                 const float4 r0 = P.rays[2 * (size_t)i], r1 = P.rays[2 * (size_t)i + 1];
@@ -492,10 +706,9 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                 gn.y = add(add(mul(sf.inv[0].y, nl.x), mul(sf.inv[1].y, nl.y)), mul(sf.inv[2].y, nl.z));
                 gn.z = add(add(mul(sf.inv[0].z, nl.x), mul(sf.inv[1].z, nl.y)), mul(sf.inv[2].z, nl.z));
                 gn = normalize3(gn);
-                const uint32_t nAll = L.nLights + (L.env.enabled ? 1u : 0u);
-                const float invN = nAll ? __fdiv_rn(1.0f, (float)nAll) : 0.0f;
-                float4 thr = P.thr[i];
-                float4 rad = P.rad[i];
+                Chan thr = chan(P.thr[i]);
+                const float prevPdf = P.prevPdf[i];
+                Chan rad = chan(P.rad[i]);
 
                 if(sf.info.x)
                 {
@@ -504,7 +717,7 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                     const bool neeOnly = (L.sampleMode == 1u && type == 1u);
                     if(!neeOnly)
                     {
-                        float3 tp = f3(thr);
+                        Chan tp = thr;
                         if(L.sampleMode == 2u && type == 1u)
                         {
                             float ndl = -dot3(f3(lt.n), dir);
@@ -513,22 +726,15 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                             float lpdf = (ndl == 0.0f) ? 0.0f : __fdiv_rn(__fdiv_rn(1.0f, lt.p0.w), ndl);
                             lpdf = mul(lpdf, dot3(dd, dd));
                             lpdf = mul(lpdf, invN);
-                            const float misPdf = add(thr.w, lpdf);
-                            tp = make_float3(mul(tp.x, thr.w), mul(tp.y, thr.w), mul(tp.z, thr.w));
-                            if(misPdf == 0.0f) tp = make_float3(0, 0, 0);
-                            else
-                            {
-                                const float inv = __fdiv_rn(1.0f, misPdf);
-                                tp = make_float3(mul(tp.x, inv), mul(tp.y, inv), mul(tp.z, inv));
-                            }
+                            tp = mis_weighted<NC>(tp, prevPdf, lpdf);
                         }
                         const float3 wo = make_float3(-dir.x, -dir.y, -dir.z);
                         const bool emits = (lt.n.w != 0.0f) || (dot3(f3(lt.n), wo) > 0.0f);
                         if(emits && depth + 1u <= L.maxDepth)
                         {
-                            rad.x = add(rad.x, mul(lt.radiance.x, tp.x));
-                            rad.y = add(rad.y, mul(lt.radiance.y, tp.y));
-                            rad.z = add(rad.z, mul(lt.radiance.z, tp.z));
+                            const Chan lr = radiance_of<SPEC>(L.spec, lt.radiance.x, lt.radiance.y, lt.radiance.z, waves);
+#pragma unroll
+                            for(int k = 0; k < NC; k++) rad.v[k] = add(rad.v[k], mul(lr.v[k], tp.v[k]));
                         }
                     }
                 }
@@ -543,7 +749,8 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                     onb(nrm, tng, btg);
                     const float3 wo = make_float3(-dir.x, -dir.y, -dir.z);
                     const float3 V = make_float3(dot3(wo, tng), dot3(wo, btg), dot3(wo, nrm));
-                    const bool isSpec = specularity(sf) >= kSpecularThreshold;
+                    const Chan alb = albedo_of<SPEC>(L.spec, sf.albedo.x, sf.albedo.y, sf.albedo.z, waves);
+                    const bool isSpec = specularity<NC>(sf, alb) >= kSpecularThreshold;
                     const uint32_t mt = sf.info.w;
                     // ---- NEE (WorkFunctionNEE); specular materials cast none ----
                     if(L.sampleMode != 0u && nAll > 0u && !isSpec && depth + 2u <= L.maxDepth)
@@ -551,7 +758,8 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                         const float dXi = rnd(key, depth, 3);
                         uint32_t li = (uint32_t)mul(dXi, (float)nAll);
                         li = min(li, nAll - 1u);
-                        float3 lp, emis;
+                        float3 lp;
+                        Chan emis = chan(0, 0, 0, 0);
                         float lightPdf;
                         if(li == L.nLights)
                         {
@@ -562,7 +770,8 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                                              add(pos.y, mul(wd.y, L.env.sceneDiameter)),
                                              add(pos.z, mul(wd.z, L.env.sceneDiameter)));
                             const float3 sd = normalize3(make_float3(sub(pos.x, lp.x), sub(pos.y, lp.y), sub(pos.z, lp.z)));
-                            emis = env_emit(L.env, make_float3(-sd.x, -sd.y, -sd.z));
+                            const float3 er = env_emit(L.env, make_float3(-sd.x, -sd.y, -sd.z));
+                            emis = radiance_of<SPEC>(L.spec, er.x, er.y, er.z, waves);
                             lightPdf = mul(invN, spdf);
                         }
                         else
@@ -582,42 +791,42 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                             ppdf = mul(ppdf, distSq);
                             lightPdf = mul(invN, ppdf);
                             const bool emits = (lt.n.w != 0.0f) || (dot3(f3(lt.n), sd) > 0.0f);
-                            emis = emits ? f3(lt.radiance) : make_float3(0, 0, 0);
+                            if(emits) emis = radiance_of<SPEC>(L.spec, lt.radiance.x, lt.radiance.y, lt.radiance.z, waves);
                         }
                         const float3 sdir = normalize3(make_float3(sub(lp.x, pos.x), sub(lp.y, pos.y), sub(lp.z, pos.z)));
                         const float3 lpn = nudge(lp, make_float3(-sdir.x, -sdir.y, -sdir.z));
                         const float3 seg = make_float3(sub(lpn.x, pos.x), sub(lpn.y, pos.y), sub(lpn.z, pos.z));
                         const float length = __fsqrt_rn(dot3(seg, seg));
                         const float3 Ls = make_float3(dot3(sdir, tng), dot3(sdir, btg), dot3(sdir, nrm));
-                        float3 refl;
+                        Chan refl = chan(0, 0, 0, 0);
                         float bpdf;
-                        if(mt == kMatUnreal) refl = unreal_eval(sf, V, Ls, bpdf);
+                        if(mt == kMatUnreal) refl = unreal_eval<NC>(sf, alb, V, Ls, bpdf);
                         else
                         {
                             const float cw = mul(fmaxf(Ls.z, 0.0f), kInvPi);
-                            refl = make_float3(mul(sf.albedo.x, cw), mul(sf.albedo.y, cw), mul(sf.albedo.z, cw));
+#pragma unroll
+                            for(int k = 0; k < NC; k++) refl.v[k] = mul(alb.v[k], cw);
                             bpdf = mul(Ls.z, kInvPi);
                             bpdf = (bpdf <= 1.0e-5f) ? 0.0f : bpdf;
                         }
                         const float pdf = (L.sampleMode == 2u) ? add(bpdf, lightPdf) : lightPdf;
-                        float3 srad = make_float3(mul(mul(thr.x, refl.x), emis.x),
-                                                  mul(mul(thr.y, refl.y), emis.y),
-                                                  mul(mul(thr.z, refl.z), emis.z));
-                        if(pdf == 0.0f) srad = make_float3(0, 0, 0);
-                        else
+                        Chan srad = chan(0, 0, 0, 0);
+                        if(pdf != 0.0f)
                         {
                             const float inv = __fdiv_rn(1.0f, pdf);
-                            srad = make_float3(mul(srad.x, inv), mul(srad.y, inv), mul(srad.z, inv));
+#pragma unroll
+                            for(int k = 0; k < NC; k++) srad.v[k] = mul(mul(mul(thr.v[k], refl.v[k]), emis.v[k]), inv);
                         }
                         const float3 so = nudge(pos, nrm);
                         P.shadowRays[2 * (size_t)i] = make_float4(so.x, so.y, so.z, 1.0e-5f);
                         P.shadowRays[2 * (size_t)i + 1] = make_float4(sdir.x, sdir.y, sdir.z,
                                                                       mul(length, sub(1.0f, 1.0e-4f)));
-                        P.shadowRad[i] = make_float4(srad.x, srad.y, srad.z, 0.0f);
+                        P.shadowRad[i] = f4(srad);
                         shadow = true;
                     }
                     // ---- BxDF sample + Russian roulette (WorkFunction) ----
-                    float3 Ll, refl;
+                    float3 Ll;
+                    Chan refl = chan(0, 0, 0, 0);
                     float bpdf;
                     bool passed = false;
                     float3 pre = pos;
@@ -625,7 +834,7 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                     {
                         Ll = normalize3(make_float3(-V.x, -V.y, sub(mul(2.0f, V.z), V.z)));
                         bpdf = 1.0f;
-                        refl = make_float3(1.0f, 1.0f, 1.0f);
+                        refl = chan(1.0f, 1.0f, 1.0f, 1.0f);
                     }
                     else if(mt == kMatRefract)
                     {
@@ -645,7 +854,7 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                                              add(mul(eta, -V.z), sub(mul(eta, cosIn), cosOut)));
                         }
                         bpdf = doRefl ? f : sub(1.0f, f);
-                        refl = make_float3(bpdf, bpdf, bpdf);
+                        refl = chan(bpdf, bpdf, bpdf, bpdf);
                         passed = !doRefl;
                         pre = nudge(pos, nrm);
                     }
@@ -653,7 +862,7 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                     {
                         const float rough = sf.albedo.w;
                         const float alpha = mul(rough, rough);
-                        const float ratio = unreal_ratio(sf, avg_albedo(sf));
+                        const float ratio = unreal_ratio(sf, avg_albedo<NC>(alb));
                         const float sXi = rnd(key, depth, 0), x0 = rnd(key, depth, 1), x1 = rnd(key, depth, 2);
                         float3 H;
                         float pd, ps;
@@ -692,17 +901,14 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                         if(dBad) ps = 1.0f;
                         const float ndl = fmaxf(0.0f, Ll.z);
                         const float corr = burley(ndl, ndv, ldh, rough);
-                        const float alb[3] = { sf.albedo.x, sf.albedo.y, sf.albedo.z };
-                        float rr[3];
 #pragma unroll
-                        for(int k = 0; k < 3; k++)
+                        for(int k = 0; k < NC; k++)
                         {
-                            const float F = schlick1(vdh, f0_of(sf, alb[k]));
+                            const float F = schlick1(vdh, f0_of(sf, alb.v[k]));
                             float spec = (ndv == 0.0f) ? 0.0f : __fdiv_rn(mul(mul(mul(D, F), G), 0.25f), ndv);
                             if(dBad) spec = __fdiv_rn(mul(G, F), gs);
-                            rr[k] = add(mul(mul(mul(ndl, mul(sub(1.0f, sf.mat.x), alb[k])), kInvPi), corr), spec);
+                            refl.v[k] = add(mul(mul(mul(ndl, mul(sub(1.0f, sf.mat.x), alb.v[k])), kInvPi), corr), spec);
                         }
-                        refl = make_float3(rr[0], rr[1], rr[2]);
                         bpdf = add(mul(pd, ratio), mul(ps, sub(1.0f, ratio)));
                     }
                     else
@@ -713,48 +919,54 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                         Ll.z = __fsqrt_rn(fmaxf(0.0f, sub(1.0f, add(mul(Ll.x, Ll.x), mul(Ll.y, Ll.y)))));
                         bpdf = mul(Ll.z, kInvPi);
                         const float cw = mul(fmaxf(Ll.z, 0.0f), kInvPi);
-                        refl = make_float3(mul(sf.albedo.x, cw), mul(sf.albedo.y, cw), mul(sf.albedo.z, cw));
+#pragma unroll
+                        for(int k = 0; k < NC; k++) refl.v[k] = mul(alb.v[k], cw);
                     }
                     float3 wi = make_float3(add(add(mul(tng.x, Ll.x), mul(btg.x, Ll.y)), mul(nrm.x, Ll.z)),
                                             add(add(mul(tng.y, Ll.x), mul(btg.y, Ll.y)), mul(nrm.y, Ll.z)),
                                             add(add(mul(tng.z, Ll.x), mul(btg.z, Ll.y)), mul(nrm.z, Ll.z)));
                     wi = normalize3(wi);
-                    thr.x = mul(thr.x, refl.x); thr.y = mul(thr.y, refl.y); thr.z = mul(thr.z, refl.z);
+#pragma unroll
+                    for(int k = 0; k < NC; k++) thr.v[k] = mul(thr.v[k], refl.v[k]);
                     depth += 1u;
                     bool dead = depth >= L.maxDepth;
                     if(!dead && depth >= L.rrStart && !isSpec)
                     {
-                        float pr = mul(add(add(thr.x, thr.y), thr.z), 0.33333333f);
+                        // throughput.Sum() * ChannelCountInv (PathTracerRendererShaders.h:250-256)
+                        float pr = add(add(thr.v[0], thr.v[1]), thr.v[2]);
+                        pr = (NC == 4) ? mul(add(pr, thr.v[3]), 0.25f) : mul(pr, 0.33333333f);
                         pr = fminf(fmaxf(pr, 0.1f), 1.0f);
                         const float xr = rnd(key, depth - 1u, 8);
                         if(xr >= pr) dead = true;
                         else
                         {
                             const float inv = __fdiv_rn(1.0f, pr);
-                            thr.x = mul(thr.x, inv); thr.y = mul(thr.y, inv); thr.z = mul(thr.z, inv);
+#pragma unroll
+                            for(int k = 0; k < NC; k++) thr.v[k] = mul(thr.v[k], inv);
                         }
                     }
                     type = isSpec ? 2u : 1u;
                     if(!dead)
                     {
-                        if(bpdf == 0.0f) { thr.x = 0.0f; thr.y = 0.0f; thr.z = 0.0f; }
+                        if(bpdf == 0.0f) thr = chan(0, 0, 0, 0);
                         else
                         {
                             const float inv = __fdiv_rn(1.0f, bpdf);
-                            thr.x = mul(thr.x, inv); thr.y = mul(thr.y, inv); thr.z = mul(thr.z, inv);
+#pragma unroll
+                            for(int k = 0; k < NC; k++) thr.v[k] = mul(thr.v[k], inv);
                         }
-                        thr.w = bpdf;
                         const float3 nn = passed ? make_float3(-nrm.x, -nrm.y, -nrm.z) : nrm;
                         const float3 no = nudge(pre, nn);
                         P.rays[2 * (size_t)i] = make_float4(no.x, no.y, no.z, 1.0e-4f);
                         P.rays[2 * (size_t)i + 1] = make_float4(wi.x, wi.y, wi.z, 3.402823466e+38f);
                         P.hits[i].x = kMissMark;
-                        P.thr[i] = thr;
+                        P.thr[i] = f4(thr);
+                        P.prevPdf[i] = bpdf;
                         P.state[i] = depth | (type << 8);
                         alive = true;
                     }
                 }
-                P.rad[i] = rad;
+                P.rad[i] = f4(rad);
             }
             else if(hk.x == kMissMark && L.env.enabled)
             {
@@ -763,27 +975,15 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                 if(!neeOnly && depth + 1u <= L.maxDepth)
                 {
                     const float3 dir = f3(P.rays[2 * (size_t)i + 1]);
-                    const float4 thr = P.thr[i];
-                    float4 rad = P.rad[i];
-                    float3 tp = f3(thr);
+                    Chan tp = chan(P.thr[i]);
+                    Chan rad = chan(P.rad[i]);
                     if(L.sampleMode == 2u && type == 1u)
-                    {
-                        const float invN = __fdiv_rn(1.0f, (float)(L.nLights + 1u));
-                        const float lpdf = mul(env_pdf(L.env, dir), invN);
-                        const float misPdf = add(thr.w, lpdf);
-                        tp = make_float3(mul(tp.x, thr.w), mul(tp.y, thr.w), mul(tp.z, thr.w));
-                        if(misPdf == 0.0f) tp = make_float3(0, 0, 0);
-                        else
-                        {
-                            const float inv = __fdiv_rn(1.0f, misPdf);
-                            tp = make_float3(mul(tp.x, inv), mul(tp.y, inv), mul(tp.z, inv));
-                        }
-                    }
-                    const float3 em = env_emit(L.env, dir);
-                    rad.x = add(rad.x, mul(em.x, tp.x));
-                    rad.y = add(rad.y, mul(em.y, tp.y));
-                    rad.z = add(rad.z, mul(em.z, tp.z));
-                    P.rad[i] = rad;
+                        tp = mis_weighted<NC>(tp, P.prevPdf[i], mul(env_pdf(L.env, dir), invN));
+                    const float3 er = env_emit(L.env, dir);
+                    const Chan em = radiance_of<SPEC>(L.spec, er.x, er.y, er.z, waves);
+#pragma unroll
+                    for(int k = 0; k < NC; k++) rad.v[k] = add(rad.v[k], mul(em.v[k], tp.v[k]));
+                    P.rad[i] = f4(rad);
                 }
             }
         }
@@ -827,13 +1027,15 @@ k_resolve(PtPaths P)
         {
             const float4 s = P.shadowRad[i];
             float4 r = P.rad[i];
-            r.x = add(r.x, s.x); r.y = add(r.y, s.y); r.z = add(r.z, s.z);
+            r.x = add(r.x, s.x); r.y = add(r.y, s.y); r.z = add(r.z, s.z); r.w = add(r.w, s.w);
             P.rad[i] = r;
         }
     }
 }
 
-// Film: every pixel sums its samples of the pass (slots p, p + WH, ...).
+// Film: every pixel sums its samples of the pass (slots p, p + WH, ...);
+// spectral samples are converted to RGB first (KCConvertSpectrumToRGBIndirect).
+template<bool SPEC>
 __global__ void __launch_bounds__(kPtTPB)
 k_film(PtLaunch L, PtPaths P, float4* __restrict__ image)
 {
@@ -843,9 +1045,11 @@ k_film(PtLaunch L, PtPaths P, float4* __restrict__ image)
         float4 acc = image[p];
         for(uint32_t k = 0; k < L.samplesPerPass; k++)
         {
-            const float4 r = P.rad[p + (size_t)k * wh];
-            acc.x = add(acc.x, r.x); acc.y = add(acc.y, r.y); acc.z = add(acc.z, r.z);
-            acc.w = add(acc.w, r.w);
+            const size_t slot = p + (size_t)k * wh;
+            const float4 r = P.rad[slot];
+            const float3 c = SPEC ? spectrum_to_rgb(L.spec, r, P.waves[slot], P.wavePdf[slot]) : f3(r);
+            acc.x = add(acc.x, c.x); acc.y = add(acc.y, c.y); acc.z = add(acc.z, c.z);
+            acc.w = add(acc.w, 1.0f);
         }
         image[p] = acc;
     }
@@ -863,7 +1067,8 @@ inline unsigned grid_for(uint32_t n, int smCount)
 cudaError_t pt_raygen(const PtLaunch& L, const PtPaths& P, uint32_t* aliveList, uint32_t* aliveCount,
                       int smCount, cudaStream_t st)
 {
-    k_raygen<<<grid_for(L.slots, smCount), kPtTPB, 0, st>>>(L, P, aliveList, aliveCount);
+    if(L.spec.enabled) k_raygen<true><<<grid_for(L.slots, smCount), kPtTPB, 0, st>>>(L, P, aliveList, aliveCount);
+    else k_raygen<false><<<grid_for(L.slots, smCount), kPtTPB, 0, st>>>(L, P, aliveList, aliveCount);
     return cudaGetLastError();
 }
 
@@ -872,8 +1077,12 @@ cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSurface* 
                           const uint32_t* aliveList, const uint32_t* aliveCount,
                           uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st)
 {
-    k_shade<<<(unsigned)smCount * 8u, kPtTPB, 0, st>>>(L, P, surfaces, nSurfaces, lights, tris, nTris,
-                                                     aliveList, aliveCount, nextList, nextCount);
+    if(L.spec.enabled)
+        k_shade<true><<<(unsigned)smCount * 8u, kPtTPB, 0, st>>>(L, P, surfaces, nSurfaces, lights, tris, nTris,
+                                                               aliveList, aliveCount, nextList, nextCount);
+    else
+        k_shade<false><<<(unsigned)smCount * 8u, kPtTPB, 0, st>>>(L, P, surfaces, nSurfaces, lights, tris, nTris,
+                                                                aliveList, aliveCount, nextList, nextCount);
     return cudaGetLastError();
 }
 
@@ -892,7 +1101,8 @@ cudaError_t pt_resolve(const PtLaunch&, const PtPaths& P, uint32_t, int smCount,
 
 cudaError_t pt_film(const PtLaunch& L, const PtPaths& P, float4* image, cudaStream_t st)
 {
-    k_film<<<grid_for(L.width * L.height, 152), kPtTPB, 0, st>>>(L, P, image);
+    if(L.spec.enabled) k_film<true><<<grid_for(L.width * L.height, 152), kPtTPB, 0, st>>>(L, P, image);
+    else k_film<false><<<grid_for(L.width * L.height, 152), kPtTPB, 0, st>>>(L, P, image);
     return cudaGetLastError();
 }
 

@@ -282,9 +282,10 @@ mrg_status pt_paths(mrg_ctx* c, uint32_t slots)
     const size_t n = slots;
     const size_t words = (n + 31) / 32;
     // one allocation, every array 256-byte aligned
-    const size_t sizes[17] = { n * 32, n * 16, n * 8, n * 16, n * 16, n * 4, n * 32, n * 16,
+    const size_t sizes[20] = { n * 32, n * 16, n * 8, n * 16, n * 16, n * 4, n * 32, n * 16,
                                words * 4, n * 4, n * 4, n * 4, 64, n * 4, n * 4, n * 4,
-                               4 * mrg::multisplit_hist_words(slots, mrg::kPtWorkKeyBits) };
+                               4 * mrg::multisplit_hist_words(slots, mrg::kPtWorkKeyBits),
+                               n * 4, n * 16, n * 16 };
     size_t need = 0;
     for(size_t sz : sizes) need += (sz + 255) & ~size_t(255);
     char* base = nullptr;
@@ -311,6 +312,9 @@ mrg_status pt_paths(mrg_ctx* c, uint32_t slots)
     P.workKeysOut = reinterpret_cast<uint32_t*>(take());
     P.listSorted = reinterpret_cast<uint32_t*>(take());
     P.sortHist = reinterpret_cast<uint32_t*>(take());
+    P.prevPdf = reinterpret_cast<float*>(take());
+    P.waves = reinterpret_cast<float4*>(take());
+    P.wavePdf = reinterpret_cast<float4*>(take());
     P.capacity = slots;
     return MRG_OK;
 }
@@ -385,6 +389,55 @@ mrg_status mrg_pt_set_env(mrg_ctx* c, uint32_t width, uint32_t height, const flo
     return MRG_OK;
 }
 
+mrg_status mrg_pt_set_spectral(mrg_ctx* c, uint32_t lutRes, const float* lut, uint32_t cieCount,
+                               const float* cieXyz, const float integrals[3], const float* spd, float norm,
+                               const float xyzToRgb[9])
+{
+    if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_spectral: null context");
+    DevGuard g(c->device);
+    if(lutRes == 0)
+    {
+        cudaFree(c->dPtSpec);
+        c->dPtSpec = nullptr;
+        c->ptSpec = mrg::PtSpectral{};
+        return MRG_OK;
+    }
+    if(!lut || !cieXyz || !integrals || !spd || !xyzToRgb || cieCount < 2)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_spectral: null table or fewer than 2 observer samples");
+    if(lutRes < 2 || lutRes > 256) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_spectral: LUT resolution out of [2, 256]");
+    const size_t lutN = 9ull * lutRes * lutRes * lutRes;
+    // SpectrumContext.cu:400-420: observer / CIE integrals, illuminant * Y / norm
+    std::vector<float> obs(3ull * cieCount), ill(cieCount);
+    const float w[3] = { 1.0f / integrals[0], 1.0f / integrals[1], 1.0f / integrals[2] };
+    const float f = integrals[1] / norm;
+    for(uint32_t i = 0; i < cieCount; i++)
+    {
+        for(int k = 0; k < 3; k++) obs[3ull * i + k] = cieXyz[3ull * i + k] * w[k];
+        ill[i] = spd[i] * f;
+    }
+    const size_t lutBytes = (sizeof(float) * lutN + 255) & ~size_t(255);
+    const size_t obsBytes = (sizeof(float) * obs.size() + 255) & ~size_t(255);
+    cudaFree(c->dPtSpec);
+    c->dPtSpec = nullptr;
+    c->ptSpec = mrg::PtSpectral{};
+    PT_TRY(cudaMalloc(&c->dPtSpec, lutBytes + obsBytes + sizeof(float) * ill.size()), "mrg_pt_set_spectral");
+    char* base = static_cast<char*>(c->dPtSpec);
+    PT_TRY(cudaMemcpy(base, lut, sizeof(float) * lutN, cudaMemcpyHostToDevice), "mrg_pt_set_spectral: upload");
+    PT_TRY(cudaMemcpy(base + lutBytes, obs.data(), sizeof(float) * obs.size(), cudaMemcpyHostToDevice),
+           "mrg_pt_set_spectral: upload");
+    PT_TRY(cudaMemcpy(base + lutBytes + obsBytes, ill.data(), sizeof(float) * ill.size(), cudaMemcpyHostToDevice),
+           "mrg_pt_set_spectral: upload");
+    mrg::PtSpectral& S = c->ptSpec;
+    S.lut = reinterpret_cast<const float*>(base);
+    S.observer = reinterpret_cast<const float*>(base + lutBytes);
+    S.illuminant = reinterpret_cast<const float*>(base + lutBytes + obsBytes);
+    std::memcpy(S.xyzToRgb, xyzToRgb, sizeof(S.xyzToRgb));
+    S.lutRes = lutRes;
+    S.cieCount = cieCount;
+    S.enabled = 1u;
+    return MRG_OK;
+}
+
 mrg_status mrg_pt_camera_frame(const mrg_pt_params* p, float out[16])
 {
     if(!p || !out) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_camera_frame: null pointer");
@@ -429,6 +482,7 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
     L.sampleMode = p->sampleMode; L.seed = p->seed;
     L.nLights = c->ptLightCount;
     L.env = c->ptEnv;
+    L.spec = c->ptSpec;
     L.filterSigma = p->filterRadius * 0.285714f;
     camera_frame(*p, L.cam);
     mrg::PtPaths& P = c->ptPaths;

@@ -65,6 +65,23 @@ class PathTracer:
         N.check(N.lib().mrg_pt_set_env(self.acc._h, t.shape[1], t.shape[0], t.ctypes.data,
                                        None if m is None else m.ctypes.data))
 
+    def set_spectral(self, lut_res, lut, tables):
+        """4-wavelength spectral rendering with an MR_SPECTRA LUT and MRay's
+        colour tables (see mray_gb300.spectral); lut_res = 0 returns to RGB."""
+        if not lut_res:
+            N.check(N.lib().mrg_pt_set_spectral(self.acc._h, 0, None, 0, None, None, None, 0.0, None))
+            return
+        self._spec_keep = [np.ascontiguousarray(lut, np.float32),
+                           np.ascontiguousarray(tables["cie_xyz"], np.float32),
+                           np.ascontiguousarray(tables["cie_integrals"], np.float32),
+                           np.ascontiguousarray(tables["illuminant"], np.float32),
+                           np.ascontiguousarray(tables["xyz_to_rgb"], np.float32)]
+        k = self._spec_keep
+        N.check(N.lib().mrg_pt_set_spectral(self.acc._h, lut_res, k[0].ctypes.data, k[1].shape[0], k[1].ctypes.data,
+                                            k[2].ctypes.data, k[3].ctypes.data,
+                                            float(np.asarray(tables["illuminant_norm"]).ravel()[0]),
+                                            k[4].ctypes.data))
+
     def build(self):
         self.acc.construct()
 

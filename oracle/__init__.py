@@ -56,7 +56,12 @@ def lib():
             getattr(L, f).argtypes = [vp, vp, vp, u32, vp, vp, vp, C.c_int]
         L.orc_cast_visibility.argtypes = [vp, vp, vp, u32, vp, C.c_int]
         L.orc_scene_stats.argtypes = [vp, vp]
-        L.orc_pt_render.argtypes = [vp, vp, vp, vp, u32, vp, vp, C.c_int]
+        L.orc_pt_render.argtypes = [vp, vp, vp, vp, u32, vp, vp, vp, C.c_int]
+        L.orc_spec_prepare.argtypes = [vp, vp, vp, C.c_float, u32, vp, vp]
+        L.orc_spec_sample_waves.argtypes = [C.c_float, vp, vp]
+        L.orc_spec_convert_albedo.argtypes = [vp, vp, vp, vp]
+        L.orc_spec_convert_radiance.argtypes = [vp, vp, vp, vp]
+        L.orc_spec_to_rgb.argtypes = [vp, vp, vp, vp, vp]
         L.orc_scene_aabb.argtypes = [vp, vp]
         L.orc_scene_diameter.argtypes = [vp]
         L.orc_scene_diameter.restype = C.c_float
@@ -328,13 +333,83 @@ def env_uv_to_dir(uv):
     return out
 
 
+class OrcSpectral(C.Structure):
+    _fields_ = [("lutRes", C.c_uint32), ("lut", C.c_void_p), ("cieCount", C.c_uint32),
+                ("observer", C.c_void_p), ("illuminant", C.c_void_p), ("xyzToRgb", C.c_float * 9)]
+
+
+def read_mrspectra(path):
+    """MRay's MR_SPECTRA LUT file (SpectraLUTGen/main.cpp:596-606): the ten
+    characters MR_SPECTRA, uint32 resolution, uint32 mode (1 = float), then
+    9 * res^3 floats."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    if raw[:10] != b"MR_SPECTRA":
+        raise ValueError("not an MR_SPECTRA file")
+    res, mode = np.frombuffer(raw[10:18], np.uint32)
+    if mode != 1:
+        raise ValueError("only float MR_SPECTRA files are supported")
+    lut = np.frombuffer(raw[18:], np.float32)
+    if lut.size != 9 * int(res) ** 3:
+        raise ValueError("truncated MR_SPECTRA file")
+    return int(res), lut.copy()
+
+
+class Spectral:
+    """Spectral context of the oracle from a LUT file and the colour tables
+    (tests/golden fixtures written from the MRay tree)."""
+
+    def __init__(self, lut_path, tables_path):
+        self.res, self.lut = read_mrspectra(lut_path)
+        t = np.load(tables_path)
+        n = int(t["cie_xyz"].shape[0])
+        self.raw = {k: t[k] for k in t.files}
+        self.observer = np.zeros((n, 3), np.float32)
+        self.illuminant = np.zeros(n, np.float32)
+        lib().orc_spec_prepare(_vp(np.ascontiguousarray(t["cie_xyz"], np.float32)),
+                               _vp(np.ascontiguousarray(t["cie_integrals"], np.float32)),
+                               _vp(np.ascontiguousarray(t["illuminant"], np.float32)),
+                               float(t["illuminant_norm"][0]), n, _vp(self.observer), _vp(self.illuminant))
+        c = OrcSpectral()
+        c.lutRes, c.lut, c.cieCount = self.res, self.lut.ctypes.data, n
+        c.observer, c.illuminant = self.observer.ctypes.data, self.illuminant.ctypes.data
+        c.xyzToRgb[:] = [float(x) for x in t["xyz_to_rgb"]]
+        self.c = c
+
+    def sample_waves(self, xi0):
+        w = np.zeros(4, np.float32)
+        p = np.zeros(4, np.float32)
+        lib().orc_spec_sample_waves(float(xi0), _vp(w), _vp(p))
+        return w, p
+
+    def convert_albedo(self, rgb, waves):
+        out = np.zeros(4, np.float32)
+        lib().orc_spec_convert_albedo(C.byref(self.c), _vp(np.ascontiguousarray(rgb, np.float32)),
+                                      _vp(np.ascontiguousarray(waves, np.float32)), _vp(out))
+        return out
+
+    def convert_radiance(self, rgb, waves):
+        out = np.zeros(4, np.float32)
+        lib().orc_spec_convert_radiance(C.byref(self.c), _vp(np.ascontiguousarray(rgb, np.float32)),
+                                        _vp(np.ascontiguousarray(waves, np.float32)), _vp(out))
+        return out
+
+    def to_rgb(self, value, waves, pdf):
+        out = np.zeros(3, np.float32)
+        lib().orc_spec_to_rgb(C.byref(self.c), _vp(np.ascontiguousarray(value, np.float32)),
+                              _vp(np.ascontiguousarray(waves, np.float32)),
+                              _vp(np.ascontiguousarray(pdf, np.float32)), _vp(out))
+        return out
+
+
 class PtScene:
     """The CPU path-tracer oracle over a list of surfaces (dicts with pos,
     idx, m34, kind, albedo / radiance), keyed like mray_gb300.pt.PathTracer:
     dense primitive keys, instance id = surface index."""
 
-    def __init__(self, surfaces, cull=True, env=None):
+    def __init__(self, surfaces, cull=True, env=None, spectral=None):
         self.L = lib()
+        self.spectral = spectral
         self.S = Scene()
         self._keep = []
         prim = 0
@@ -419,6 +494,7 @@ class PtScene:
         img = np.zeros((p.height, p.width, 4), np.float32) if image is None else image
         self.L.orc_pt_render(self.S._h, C.byref(p), self.surf, self.lights, self.n_lights,
                              C.byref(self.env) if self.env is not None else None,
+                             C.byref(self.spectral.c) if self.spectral is not None else None,
                              _vp(img), threads or default_threads())
         return img
 

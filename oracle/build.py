@@ -72,6 +72,50 @@ def build_ref(force=False, verbose=False):
     return REF_LIB
 
 
+def _mray_cmake_header(gen_dir):
+    """The configure_file output the MRay sources include (mray_cmake.h.in),
+    with fixed values: this recipe does not run CMake."""
+    os.makedirs(gen_dir, exist_ok=True)
+    h = os.path.join(gen_dir, "mray_cmake.h")
+    if not os.path.exists(h):
+        with open(h, "w") as f:
+            f.write("#pragma once\n#include <string_view>\nusing namespace std::string_view_literals;\n"
+                    "#define MRAY_VERSION_MAJOR 1\n#define MRAY_VERSION_MINOR 0\n#define MRAY_VERSION_PATCH 0\n"
+                    "#define MRAY_BUILD_VISOR 0\n#define MRAY_HOST_ARCH_BASIC\n"
+                    "#define MRAY_PROJECT_NAME \"MRay\"sv\n#define MRAY_PROJECT_DESCRIPTION \"\"sv\n"
+                    "#define MRAY_PLATFORM_NAME \"Linux\"sv\n#define MRAY_COMPILER_NAME \"gcc\"sv\n"
+                    "#define MRAY_GPU_PLATFORM_NAME \"none\"sv\n#define MRAY_GPU_COMPILER_NAME \"none\"sv\n")
+    return gen_dir
+
+
+def build_ref_spectra(force=False, verbose=False):
+    """The reference's spectral tools, compiled from the MRay tree: the LUT
+    generator (SpectraLUTGen/main.cpp) as ``oracle/_ref/spectra_lut_gen`` and
+    the colour-table accessors (spectra_driver.cpp) as
+    ``oracle/_ref/libmray_ref_spectra.so``.  Returns (generator, library) or
+    None without the MRay tree."""
+    src_dir = reference_source_dir()
+    if src_dir is None:
+        return None
+    gen = _mray_cmake_header(os.path.join(REF_DIR, "gen"))
+    color = os.path.join(src_dir, "Core", "ColorFunctions.cpp")
+    flags = ["-std=c++20", "-O2", "-ffp-contract=off", "-DMRAY_GCC", "-DMRAY_LINUX", "-I", gen, "-I", src_dir]
+    exe = os.path.join(REF_DIR, "spectra_lut_gen")
+    lib = os.path.join(REF_DIR, "libmray_ref_spectra.so")
+    drv = os.path.join(HERE, "spectra_driver.cpp")
+    if force or not os.path.exists(exe):
+        cmd = ["g++"] + flags + ["-pthread", "-o", exe, os.path.join(src_dir, "SpectraLUTGen", "main.cpp"), color]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.run(cmd, check=True)
+    if force or not _newer(lib, [drv]):
+        cmd = ["g++"] + flags + ["-fPIC", "-shared", "-o", lib, drv, color]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.run(cmd, check=True)
+    return exe, lib
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True, verbose=True))
     print(build_ref(force=True, verbose=True))

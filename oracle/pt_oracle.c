@@ -111,12 +111,12 @@ static float g_correlated(const float o[3], const float i[3], float alpha)
     return 1.0f / (lambda_smith(o, alpha) + lambda_smith(i, alpha) + 1.0f);
 }
 /* BxDF::FSchlick (:502-511) */
-static void f_schlick(float vdh, const float f0[3], float out[3])
+static void f_schlick(float vdh, const float* f0, float* out, int nc)
 {
     float pw = 1.0f - vdh;
     float pw2 = pw * pw;
     float pw5 = pw2 * pw2 * pw;
-    for(int k = 0; k < 3; k++) out[k] = (1.0f - f0[k]) * pw5 + f0[k];
+    for(int k = 0; k < nc; k++) out[k] = (1.0f - f0[k]) * pw5 + f0[k];
 }
 /* BxDF::VNDFGGXSmithPDF (:515-527) */
 static float vndf_pdf(const float V[3], const float H[3], float alpha)
@@ -176,20 +176,24 @@ static float unreal_mis_ratio(const orc_pt_surface* m, float avgAlbedo)
     float total = specR + integ;
     return (total == 0.0f) ? 0.0f : integ / total;
 }
-static float specularity(const orc_pt_surface* m)
+/* albedo.Sum() * 0.3333 over the Spectrum's channels (RGB: 3, spectral: 4;
+ * MaterialsDefault.hpp:548) */
+static inline float avg_albedo(const float* alb, int nc)
+{
+    float s = alb[0] + alb[1] + alb[2];
+    if(nc == 4) s += alb[3];
+    return s * 0.3333f;
+}
+static float specularity(const orc_pt_surface* m, const float* alb, int nc)
 {
     if(m->matType == ORC_MAT_REFLECT || m->matType == ORC_MAT_REFRACT) return 1.0f;
-    if(m->matType == ORC_MAT_UNREAL)
-    {
-        float avg = (m->albedo[0] + m->albedo[1] + m->albedo[2]) * 0.3333f;
-        return 1.0f - unreal_mis_ratio(m, avg);
-    }
+    if(m->matType == ORC_MAT_UNREAL) return 1.0f - unreal_mis_ratio(m, avg_albedo(alb, nc));
     return 0.0f;
 }
 /* UnrealMaterial::Evaluate / Pdf (MaterialsDefault.hpp:628-720) in the
  * tangent frame; V, L unit vectors. */
-static void unreal_eval(const orc_pt_surface* m, const float V[3], const float L[3],
-                        float refl[3], float* pdfOut)
+static void unreal_eval(const orc_pt_surface* m, const float* alb, int nc, const float V[3], const float L[3],
+                        float* refl, float* pdfOut)
 {
     float alpha = m->roughness * m->roughness;
     float H[3] = { L[0] + V[0], L[1] + V[1], L[2] + V[2] };
@@ -204,20 +208,19 @@ static void unreal_eval(const orc_pt_surface* m, const float V[3], const float L
     float G = g_correlated(V, L, alpha);
     G = (ldh == 0.0f) ? 0.0f : G;
     G = (vdh == 0.0f) ? 0.0f : G;
-    float f0[3];
-    for(int k = 0; k < 3; k++) f0[k] = (m->specular * 0.08f) * (1.0f - m->metallic) + m->albedo[k] * m->metallic;
-    float F[3];
-    f_schlick(vdh, f0, F);
+    float f0[4];
+    for(int k = 0; k < nc; k++) f0[k] = (m->specular * 0.08f) * (1.0f - m->metallic) + alb[k] * m->metallic;
+    float F[4];
+    f_schlick(vdh, f0, F, nc);
     float ndl = fmaxf(0.0f, L[2]);
     float corr = burley(ndl, ndv, ldh, m->roughness);
-    for(int k = 0; k < 3; k++)
+    for(int k = 0; k < nc; k++)
     {
         float spec = (ndv == 0.0f) ? 0.0f : Dn * F[k] * G * 0.25f / ndv;
-        float diff = ndl * ((1.0f - m->metallic) * m->albedo[k]) * INV_PI_F * corr;
+        float diff = ndl * ((1.0f - m->metallic) * alb[k]) * INV_PI_F * corr;
         refl[k] = diff + spec;
     }
-    float avg = (m->albedo[0] + m->albedo[1] + m->albedo[2]) * 0.3333f;
-    float ratio = unreal_mis_ratio(m, avg);
+    float ratio = unreal_mis_ratio(m, avg_albedo(alb, nc));
     float pd = L[2] * INV_PI_F;
     pd = (pd <= 1.0e-5f) ? 0.0f : pd;
     float ps = vndf_pdf(V, H, alpha);
@@ -454,6 +457,158 @@ static void env_sample(const orc_pt_env* E, float xi0, float xi1, float wdir[3],
     rows_apply(E->m, dy, wdir);
 }
 
+/* ------------------------------------------------------------------------ */
+/* Spectral (Source/Tracer/SpectrumContext.{hpp,cu}, host backend)           */
+/* ------------------------------------------------------------------------ */
+#define CIE_START 360.0f
+
+void orc_spec_prepare(const float* cieXyz, const float integrals[3], const float* spd, float normFactor,
+                      uint32_t cieCount, float* observer, float* illuminant)
+{
+    /* SpectrumContext.cu:405-420: WEIGHT = 1 / CIE_SUM; factor = Y / norm */
+    float w[3] = { 1.0f / integrals[0], 1.0f / integrals[1], 1.0f / integrals[2] };
+    float f = integrals[1] / normFactor;
+    for(uint32_t i = 0; i < cieCount; i++)
+    {
+        for(int k = 0; k < 3; k++) observer[3 * i + k] = cieXyz[3 * i + k] * w[k];
+        illuminant[i] = spd[i] * f;
+    }
+}
+
+/* The host texture view's linear read of fraction and base index for one
+ * axis: texel = uv * n - 0.5, modf, negative fractions made absolute; CLAMP
+ * edge resolve. */
+static inline void tex_axis(float uv, uint32_t n, int32_t* i0, int32_t* i1, float* frac)
+{
+    float t = uv * (float)n - 0.5f, b;
+    float f = modff(t, &b);
+    int32_t s = (int32_t)b;
+    if(f < 0.0f) { s -= 1; f = fabsf(f); }
+    int32_t hi = (int32_t)n - 1;
+    *i0 = s < 0 ? 0 : (s > hi ? hi : s);
+    *i1 = (s + 1) < 0 ? 0 : ((s + 1) > hi ? hi : (s + 1));
+    *frac = f;
+}
+
+static inline float lerpf_(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+
+/* 1D table read at a texel coordinate (normCoordinates = false). */
+static void tex1d(const float* tab, uint32_t n, uint32_t ch, float coord, float* out)
+{
+    float uv = coord / (float)n;
+    int32_t i0, i1; float f;
+    tex_axis(uv, n, &i0, &i1, &f);
+    for(uint32_t c = 0; c < ch; c++) out[c] = lerpf_(tab[(size_t)i0 * ch + c], tab[(size_t)i1 * ch + c], f);
+}
+
+/* Trilinear read of LUT texture `tex` (0..8) at normalised uvw. */
+static float tex3d(const orc_spectral* S, uint32_t tex, const float uvw[3])
+{
+    const uint32_t n = S->lutRes;
+    const float* t = S->lut + (size_t)tex * n * n * n;
+    int32_t a0, a1, b0, b1, c0, c1; float fx, fy, fz;
+    tex_axis(uvw[0], n, &a0, &a1, &fx);
+    tex_axis(uvw[1], n, &b0, &b1, &fy);
+    tex_axis(uvw[2], n, &c0, &c1, &fz);
+#define T3(x, y, z) t[((size_t)(z) * n + (size_t)(y)) * n + (size_t)(x)]
+    float p0 = lerpf_(T3(a0, b0, c0), T3(a1, b0, c0), fx);
+    float p1 = lerpf_(T3(a0, b1, c0), T3(a1, b1, c0), fx);
+    float p2 = lerpf_(T3(a0, b0, c1), T3(a1, b0, c1), fx);
+    float p3 = lerpf_(T3(a0, b1, c1), T3(a1, b1, c1), fx);
+#undef T3
+    float q0 = lerpf_(p0, p1, fy), q1 = lerpf_(p2, p3, fy);
+    return lerpf_(q0, q1, fz);
+}
+
+static inline float inv_smoothstep(float y)
+{
+    return 0.5f - sinf(asinf(1.0f - 2.0f * y) * (1.0f / 3.0f));
+}
+
+void orc_spec_sample_waves(float xi0, float waves[4], float pdf[4])
+{
+    static const float OFF[4] = { -0.5f, -0.25f, 0.0f, 0.25f };
+    for(int i = 0; i < 4; i++)
+    {
+        float x = xi0 + OFF[i];
+        if(x < 0.0f) x += 1.0f;
+        if(x >= 1.0f) x -= 1.0f;
+        float a = 0.85691062f - 1.82750197f * x;
+        float l = 538.0f - 138.888889f * atanhf(a);
+        float d = coshf(0.0072f * (l - 538.0f));
+        d = d * d;
+        waves[i] = l;
+        pdf[i] = 0.0039398042f / d;
+    }
+}
+
+/* Converter::ConvertAlbedo (SpectrumContext.hpp:36-130) */
+void orc_spec_convert_albedo(const orc_spectral* S, const float rgb[3], const float waves[4], float out[4])
+{
+    uint32_t maxI = 0;
+    float mx = rgb[0];
+    for(uint32_t i = 1; i < 3; i++) if(rgb[i] > mx) { mx = rgb[i]; maxI = i; }
+    float xyz[3] = { 0.0f, 0.0f, 0.0f };
+    if(mx > 1.0e-7f)
+    {
+        float f = 1.0f / mx;
+        xyz[0] = rgb[(maxI + 1) % 3] * f;
+        xyz[1] = rgb[(maxI + 2) % 3] * f;
+    }
+    float slice = mx < 0.0f ? 0.0f : (mx > 1.0f ? 1.0f : mx);
+    xyz[2] = inv_smoothstep(inv_smoothstep(slice));
+    const float N = (float)S->lutRes;
+    const float A = (N - 1.0f) / N, B = 0.5f / N;
+    float uvw[3];
+    for(int k = 0; k < 3; k++) uvw[k] = xyz[k] * A + B;
+    float c[3];
+    for(uint32_t k = 0; k < 3; k++) c[k] = tex3d(S, 3 * maxI + k, uvw);
+    for(int i = 0; i < 4; i++)
+    {
+        float t = fmaf(c[0], waves[i], c[1]);
+        float x = fmaf(t, waves[i], c[2]);
+        float dr = 1.0f / sqrtf(fmaf(x, x, 1.0f));
+        out[i] = fmaf(0.5f * x, dr, 0.5f);
+    }
+}
+
+/* Converter::ConvertRadiance (SpectrumContext.hpp:132-152) */
+void orc_spec_convert_radiance(const orc_spectral* S, const float rgb[3], const float waves[4], float out[4])
+{
+    uint32_t maxI = 0;
+    float mx = rgb[0];
+    for(uint32_t i = 1; i < 3; i++) if(rgb[i] > mx) { mx = rgb[i]; maxI = i; }
+    (void)maxI;
+    float scale = mx * 2.0f;
+    float c[3] = { 0.0f, 0.0f, 0.0f };
+    if(scale != 0.0f) for(int k = 0; k < 3; k++) c[k] = rgb[k] / scale;
+    orc_spec_convert_albedo(S, c, waves, out);
+    for(int i = 0; i < 4; i++)
+    {
+        float il;
+        tex1d(S->illuminant, S->cieCount, 1, waves[i] + (0.5f - CIE_START), &il);
+        out[i] *= il;
+    }
+    for(int i = 0; i < 4; i++) out[i] *= scale;
+}
+
+/* ConvertSpectraToRGBSingle (SpectrumContext.cu:137-170), no dispersion */
+void orc_spec_to_rgb(const orc_spectral* S, const float value[4], const float waves[4], const float pdf[4],
+                     float rgb[3])
+{
+    float xyz[3] = { 0.0f, 0.0f, 0.0f };
+    for(int i = 0; i < 4; i++)
+    {
+        float f[3];
+        tex1d(S->observer, S->cieCount, 3, waves[i] + (0.5f - CIE_START), f);
+        float v = (pdf[i] == 0.0f) ? 0.0f : value[i] / pdf[i];
+        for(int k = 0; k < 3; k++) xyz[k] += f[k] * v;
+    }
+    for(int k = 0; k < 3; k++) xyz[k] *= 0.25f;
+    for(int r = 0; r < 3; r++)
+        rgb[r] = fmaf(S->xyzToRgb[3 * r + 2], xyz[2], fmaf(S->xyzToRgb[3 * r + 1], xyz[1], S->xyzToRgb[3 * r] * xyz[0]));
+}
+
 typedef struct
 {
     const orc_scene*          scene;
@@ -462,6 +617,7 @@ typedef struct
     const orc_pt_light_tri*   lights;
     uint32_t                  nLights;      /* triangle lights */
     const orc_pt_env*         env;          /* boundary light (last), or NULL */
+    const orc_spectral*       spec;         /* NULL: RGB */
     float*                    image;
     atomic_uint               nextRow;
 } pt_job;
@@ -534,8 +690,13 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
     normalize3f(dir);
     float tmin = P->nearT, tmax = P->farT;
 
-    float thr[3] = { 1.0f, 1.0f, 1.0f };
-    float rad[3] = { 0.0f, 0.0f, 0.0f };
+    float thr[4] = { 1.0f, 1.0f, 1.0f, 1.0f };
+    float rad[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+    /* spectral: 4 wavelengths per path, sampled at the camera */
+    const orc_spectral* S = J->spec;
+    const int nc = S ? 4 : 3;
+    float waves[4] = { 0, 0, 0, 0 }, wpdf[4] = { 1, 1, 1, 1 };
+    if(S) orc_spec_sample_waves(rnd(key, 0, 9), waves, wpdf);
     uint32_t depth = 0;
     int type = 0;           /* 0 camera, 1 path (diffuse) */
     float prevPdf = 0.0f;
@@ -551,19 +712,20 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
             /* miss: boundary light work (LightWorkFunction[WithNEE] with the
              * skysphere, PathTracerRendererShaders.h:308-345, 450-517) */
             if(!E || (P->sampleMode == ORC_PT_NEE && type == 1)) break;
-            float tp[3] = { thr[0], thr[1], thr[2] };
+            float tp[4] = { thr[0], thr[1], thr[2], thr[3] };
             if(P->sampleMode == ORC_PT_NEE_MIS && type == 1)
             {
                 float lpdf = env_pdf(E, dir) * invN;
                 float misPdf = prevPdf + lpdf;
-                for(int k = 0; k < 3; k++) tp[k] *= prevPdf;
-                if(misPdf == 0.0f) { tp[0] = tp[1] = tp[2] = 0.0f; }
-                else { float inv = 1.0f / misPdf; for(int k = 0; k < 3; k++) tp[k] *= inv; }
+                for(int k = 0; k < nc; k++) tp[k] *= prevPdf;
+                if(misPdf == 0.0f) { tp[0] = tp[1] = tp[2] = tp[3] = 0.0f; }
+                else { float inv = 1.0f / misPdf; for(int k = 0; k < nc; k++) tp[k] *= inv; }
             }
-            float em[3];
+            float em[4];
             env_emit(E, dir, em);
+            if(S) { float c[3] = { em[0], em[1], em[2] }; orc_spec_convert_radiance(S, c, waves, em); }
             if(depth + 1u <= P->maxDepth)
-                for(int k = 0; k < 3; k++) rad[k] += em[k] * tp[k];
+                for(int k = 0; k < nc; k++) rad[k] += em[k] * tp[k];
             break;
         }
         const orc_pt_surface* sf = &J->surfaces[inst];
@@ -579,7 +741,7 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
         {
             /* NEE-only mode: only camera and specular rays see emission */
             if(P->sampleMode == ORC_PT_NEE && type == 1) break;
-            float tp[3] = { thr[0], thr[1], thr[2] };
+            float tp[4] = { thr[0], thr[1], thr[2], thr[3] };
             if(P->sampleMode == ORC_PT_NEE_MIS && type == 1)
             {
                 const orc_pt_light_tri* L = &J->lights[sf->lightBase + localPrim];
@@ -591,16 +753,18 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
                 lpdf *= dot3f(dd, dd);
                 lpdf *= invN;
                 float misPdf = prevPdf + lpdf;
-                for(int k = 0; k < 3; k++) tp[k] *= prevPdf;
-                if(misPdf == 0.0f) { tp[0] = tp[1] = tp[2] = 0.0f; }
-                else { float inv = 1.0f / misPdf; for(int k = 0; k < 3; k++) tp[k] *= inv; }
+                for(int k = 0; k < nc; k++) tp[k] *= prevPdf;
+                if(misPdf == 0.0f) { tp[0] = tp[1] = tp[2] = tp[3] = 0.0f; }
+                else { float inv = 1.0f / misPdf; for(int k = 0; k < nc; k++) tp[k] *= inv; }
             }
             const orc_pt_light_tri* L = &J->lights[sf->lightBase + localPrim];
             float wo[3] = { -dir[0], -dir[1], -dir[2] };
             float ndl = dot3f(L->n, wo);
             int emits = L->twoSided ? 1 : (ndl > 0.0f);
+            float lr[4] = { L->radiance[0], L->radiance[1], L->radiance[2], 0.0f };
+            if(S) orc_spec_convert_radiance(S, L->radiance, waves, lr);
             if(emits && depth + 1u <= P->maxDepth)
-                for(int k = 0; k < 3; k++) rad[k] += L->radiance[k] * tp[k];
+                for(int k = 0; k < nc; k++) rad[k] += lr[k] * tp[k];
             break;
         }
 
@@ -612,7 +776,9 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
         onb(nrm, tng, btg);
         const float wo[3] = { -dir[0], -dir[1], -dir[2] };
         const float V[3] = { dot3f(wo, tng), dot3f(wo, btg), dot3f(wo, nrm) };
-        const int isSpec = specularity(sf) >= SPECULAR_THRESHOLD;
+        float alb[4] = { sf->albedo[0], sf->albedo[1], sf->albedo[2], 0.0f };
+        if(S) orc_spec_convert_albedo(S, sf->albedo, waves, alb);
+        const int isSpec = specularity(sf, alb, nc) >= SPECULAR_THRESHOLD;
 
         /* ---- NEE (WorkFunctionNEE); no shadow ray for specular materials ---- */
         if(P->sampleMode != ORC_PT_PURE && nAll > 0 && !isSpec)
@@ -621,7 +787,7 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
             uint32_t li = (uint32_t)(dXi * (float)nAll);
             if(li > nAll - 1u) li = nAll - 1u;
             float lp[3], lightPdf;
-            float emis[3] = { 0, 0, 0 };
+            float emis[4] = { 0, 0, 0, 0 };
             if(li == J->nLights)
             {
                 /* skysphere: a point sceneDiameter away along the sampled direction */
@@ -632,6 +798,7 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
                 normalize3f(sd);
                 float toward[3] = { -sd[0], -sd[1], -sd[2] };
                 env_emit(E, toward, emis);
+                if(S) { float c[3] = { emis[0], emis[1], emis[2] }; orc_spec_convert_radiance(S, c, waves, emis); }
                 lightPdf = invN * spdf;
             }
             else
@@ -649,7 +816,10 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
                 ppdf *= distSq;
                 lightPdf = invN * ppdf;
                 if(L->twoSided || dot3f(L->n, sd) > 0.0f)
+                {
                     for(int k = 0; k < 3; k++) emis[k] = L->radiance[k];
+                    if(S) orc_spec_convert_radiance(S, L->radiance, waves, emis);
+                }
             }
             float sdir[3] = { lp[0] - pos[0], lp[1] - pos[1], lp[2] - pos[2] };
             normalize3f(sdir);
@@ -658,31 +828,31 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
             orc_nudge(lp, nd, lpn);
             float seg[3] = { lpn[0] - pos[0], lpn[1] - pos[1], lpn[2] - pos[2] };
             float length = sqrtf(dot3f(seg, seg));
-            float refl[3], bpdf;
+            float refl[4] = { 0, 0, 0, 0 }, bpdf;
             const float Ls[3] = { dot3f(sdir, tng), dot3f(sdir, btg), dot3f(sdir, nrm) };
             if(sf->matType == ORC_MAT_UNREAL)
-                unreal_eval(sf, V, Ls, refl, &bpdf);
+                unreal_eval(sf, alb, nc, V, Ls, refl, &bpdf);
             else
             {
                 float cw = fmaxf(Ls[2], 0.0f) * INV_PI_F;
-                for(int k = 0; k < 3; k++) refl[k] = sf->albedo[k] * cw;
+                for(int k = 0; k < nc; k++) refl[k] = alb[k] * cw;
                 bpdf = Ls[2] * INV_PI_F;
                 bpdf = (bpdf <= 1.0e-5f) ? 0.0f : bpdf;
             }
             float pdf = (P->sampleMode == ORC_PT_NEE_MIS) ? (bpdf + lightPdf) : lightPdf;
-            float srad[3];
-            for(int k = 0; k < 3; k++) srad[k] = thr[k] * refl[k] * emis[k];
-            if(pdf == 0.0f) srad[0] = srad[1] = srad[2] = 0.0f;
-            else { float inv = 1.0f / pdf; for(int k = 0; k < 3; k++) srad[k] *= inv; }
+            float srad[4] = { 0, 0, 0, 0 };
+            for(int k = 0; k < nc; k++) srad[k] = thr[k] * refl[k] * emis[k];
+            if(pdf == 0.0f) srad[0] = srad[1] = srad[2] = srad[3] = 0.0f;
+            else { float inv = 1.0f / pdf; for(int k = 0; k < nc; k++) srad[k] *= inv; }
             float sorg[3];
             orc_nudge(pos, nrm, sorg);
             if(depth + 2u <= P->maxDepth &&
                visible1(J->scene, sorg, sdir, 1.0e-5f, length * (1.0f - 1.0e-4f)))
-                for(int k = 0; k < 3; k++) rad[k] += srad[k];
+                for(int k = 0; k < nc; k++) rad[k] += srad[k];
         }
 
         /* ---- BxDF sample (WorkFunction) ---- */
-        float Ll[3], refl[3], bpdf;
+        float Ll[3], refl[4] = { 0, 0, 0, 0 }, bpdf;
         int passed = 0;
         float presample[3] = { pos[0], pos[1], pos[2] };    /* ray origin before the final nudge */
         if(sf->matType == ORC_MAT_REFLECT)
@@ -691,7 +861,7 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
             Ll[0] = -V[0]; Ll[1] = -V[1]; Ll[2] = d2 - V[2];
             normalize3f(Ll);
             bpdf = 1.0f;
-            refl[0] = refl[1] = refl[2] = 1.0f;
+            refl[0] = refl[1] = refl[2] = refl[3] = 1.0f;
         }
         else if(sf->matType == ORC_MAT_REFRACT)
         {
@@ -712,15 +882,14 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
                 Ll[2] = eta * -V[2] + (eta * cosIn - cosOut);
             }
             bpdf = doRefl ? f : (1.0f - f);
-            refl[0] = refl[1] = refl[2] = bpdf;
+            refl[0] = refl[1] = refl[2] = refl[3] = bpdf;
             passed = !doRefl;
             orc_nudge(pos, nrm, presample);                 /* SampleBxDF nudges along n first */
         }
         else if(sf->matType == ORC_MAT_UNREAL)
         {
             float alpha = sf->roughness * sf->roughness;
-            float avg = (sf->albedo[0] + sf->albedo[1] + sf->albedo[2]) * 0.3333f;
-            float ratio = unreal_mis_ratio(sf, avg);
+            float ratio = unreal_mis_ratio(sf, avg_albedo(alb, nc));
             float sXi = rnd(key, depth, 0), x0 = rnd(key, depth, 1), x1 = rnd(key, depth, 2);
             float H[3], pd, ps;
             if(sXi < ratio)
@@ -754,21 +923,21 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
             float G = g_correlated(V, Ll, alpha);
             G = (ldh == 0.0f) ? 0.0f : G;
             G = (vdh == 0.0f) ? 0.0f : G;
-            float f0[3], F[3];
-            for(int k = 0; k < 3; k++) f0[k] = (sf->specular * 0.08f) * (1.0f - sf->metallic) + sf->albedo[k] * sf->metallic;
-            f_schlick(vdh, f0, F);
-            float spec[3];
-            for(int k = 0; k < 3; k++) spec[k] = (ndv == 0.0f) ? 0.0f : D * F[k] * G * 0.25f / ndv;
+            float f0[4], F[4];
+            for(int k = 0; k < nc; k++) f0[k] = (sf->specular * 0.08f) * (1.0f - sf->metallic) + alb[k] * sf->metallic;
+            f_schlick(vdh, f0, F, nc);
+            float spec[4];
+            for(int k = 0; k < nc; k++) spec[k] = (ndv == 0.0f) ? 0.0f : D * F[k] * G * 0.25f / ndv;
             if(isinf(D) || isnan(D))
             {
                 float gs = g_single(V, alpha);
-                for(int k = 0; k < 3; k++) spec[k] = G * F[k] / gs;
+                for(int k = 0; k < nc; k++) spec[k] = G * F[k] / gs;
                 ps = 1.0f;
             }
             float ndl = fmaxf(0.0f, Ll[2]);
             float corr = burley(ndl, ndv, ldh, sf->roughness);
-            for(int k = 0; k < 3; k++)
-                refl[k] = ndl * ((1.0f - sf->metallic) * sf->albedo[k]) * INV_PI_F * corr + spec[k];
+            for(int k = 0; k < nc; k++)
+                refl[k] = ndl * ((1.0f - sf->metallic) * alb[k]) * INV_PI_F * corr + spec[k];
             bpdf = pd * ratio + ps * (1.0f - ratio);
         }
         else
@@ -779,26 +948,28 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
             Ll[2] = sqrtf(fmaxf(0.0f, 1.0f - (Ll[0] * Ll[0] + Ll[1] * Ll[1])));
             bpdf = Ll[2] * INV_PI_F;
             float cw = fmaxf(Ll[2], 0.0f) * INV_PI_F;
-            for(int k = 0; k < 3; k++) refl[k] = sf->albedo[k] * cw;
+            for(int k = 0; k < nc; k++) refl[k] = alb[k] * cw;
         }
         float wi[3];
         for(int k = 0; k < 3; k++) wi[k] = tng[k] * Ll[0] + btg[k] * Ll[1] + nrm[k] * Ll[2];
         normalize3f(wi);
-        for(int k = 0; k < 3; k++) thr[k] *= refl[k];
+        for(int k = 0; k < nc; k++) thr[k] *= refl[k];
         depth += 1u;
         int dead = depth >= P->maxDepth;
         if(!dead && depth >= P->rrStart && !isSpec)
         {
-            float pr = (thr[0] + thr[1] + thr[2]) * 0.33333333f;
+            /* throughput.Sum() * ChannelCountInv (PathTracerRendererShaders.h:250-256) */
+            float pr = (nc == 4) ? (thr[0] + thr[1] + thr[2] + thr[3]) * 0.25f
+                                 : (thr[0] + thr[1] + thr[2]) * 0.33333333f;
             pr = fminf(fmaxf(pr, 0.1f), 1.0f);
             float xr = rnd(key, depth - 1u, 8);
             if(xr >= pr) dead = 1;
-            else { float inv = 1.0f / pr; for(int k = 0; k < 3; k++) thr[k] *= inv; }
+            else { float inv = 1.0f / pr; for(int k = 0; k < nc; k++) thr[k] *= inv; }
         }
         type = isSpec ? 2 : 1;
         if(dead) break;
-        if(bpdf == 0.0f) { thr[0] = thr[1] = thr[2] = 0.0f; }
-        else { float inv = 1.0f / bpdf; for(int k = 0; k < 3; k++) thr[k] *= inv; }
+        if(bpdf == 0.0f) { thr[0] = thr[1] = thr[2] = thr[3] = 0.0f; }
+        else { float inv = 1.0f / bpdf; for(int k = 0; k < nc; k++) thr[k] *= inv; }
         prevPdf = bpdf;
         float nn[3] = { nrm[0], nrm[1], nrm[2] };
         if(passed) { nn[0] = -nn[0]; nn[1] = -nn[1]; nn[2] = -nn[2]; }
@@ -807,7 +978,8 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
         tmin = 1.0e-4f;
         tmax = 3.402823466e+38f;
     }
-    outRad[0] = rad[0]; outRad[1] = rad[1]; outRad[2] = rad[2];
+    if(S) orc_spec_to_rgb(S, rad, waves, wpdf, outRad);
+    else { outRad[0] = rad[0]; outRad[1] = rad[1]; outRad[2] = rad[2]; }
 }
 
 static void* pt_worker(void* arg)
@@ -834,13 +1006,14 @@ static void* pt_worker(void* arg)
 
 int orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
                   const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
-                  float* image, int nthreads)
+                  const orc_spectral* spectral, float* image, int nthreads)
 {
     if(!s || !p || !surfaces || !image) return -1;
     pt_job J;
     memset(&J, 0, sizeof(J));
     J.scene = s; J.p = p; J.surfaces = surfaces; J.lights = lights; J.nLights = nLights;
     J.env = env;
+    J.spec = spectral;
     J.image = image;
     atomic_init(&J.nextRow, 0u);
     if(nthreads < 1) nthreads = 1;

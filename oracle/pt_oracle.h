@@ -76,12 +76,38 @@ typedef struct
     float        sceneDiameter; /* orc_scene_diameter */
 } orc_pt_env;
 
+/* Spectral rendering (Jakob & Hanika 2019 RGB -> spectrum, 4 wavelengths per
+ * path; Source/Tracer/SpectrumContext.{h,hpp,cu}).  Tables as MRay prepares
+ * them (SpectrumContext.cu:400-420): the observer already divided by the CIE
+ * integrals, the illuminant already scaled by Y_INTEGRAL / normFactor. */
+typedef struct
+{
+    uint32_t     lutRes;
+    const float* lut;           /* 9 * res^3 floats: [table][coefficient][z][y][x] */
+    uint32_t     cieCount;      /* 471 (360..830 nm) */
+    const float* observer;      /* cieCount * 3 */
+    const float* illuminant;    /* cieCount */
+    float        xyzToRgb[9];
+} orc_spectral;
+
+/* Observer / illuminant preparation of SpectrumContextJakob2019 (from MRay's
+ * raw tables; out arrays of cieCount * 3 and cieCount). */
+void orc_spec_prepare(const float* cieXyz, const float integrals[3], const float* spd, float normFactor,
+                      uint32_t cieCount, float* observer, float* illuminant);
+/* SingleSampleSpectrumWavelength, HYPERBOLIC_PBRT (SpectrumContext.cu:40-135) */
+void orc_spec_sample_waves(float xi0, float waves[4], float pdf[4]);
+void orc_spec_convert_albedo(const orc_spectral* S, const float rgb[3], const float waves[4], float out[4]);
+void orc_spec_convert_radiance(const orc_spectral* S, const float rgb[3], const float waves[4], float out[4]);
+void orc_spec_to_rgb(const orc_spectral* S, const float value[4], const float waves[4], const float pdf[4],
+                     float rgb[3]);
+
 /* Accumulates spp samples per pixel into image (R, G, B, weight) per pixel,
  * row 0 at the bottom of the image plane.  env may be NULL (no boundary
- * light); it is the last light of the uniform light sampler. */
+ * light); it is the last light of the uniform light sampler.  spectral NULL
+ * renders RGB, otherwise 4 wavelengths per path converted to RGB at the film. */
 int  orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
                    const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
-                   float* image, int nthreads);
+                   const orc_spectral* spectral, float* image, int nthreads);
 
 /* Piecewise-constant 2D distribution (Source/Tracer/Distributions.h/.cu). */
 void  orc_pwc2d_build(const float* func, uint32_t w, uint32_t h, float* cdfX, float* cdfY);

@@ -157,3 +157,42 @@ def test_partition_by_material_is_invisible():
         b = pt.render(PathTracer.params(80, 60, 8, cam, sample_mode=mode, seed=2, partition=False))
         assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
     pt.close()
+
+
+# ---- spectral (4 wavelengths per path) -------------------------------------
+
+def _spectral_pair(surf, env=None):
+    import os
+    from mray_gb300 import spectral
+    gold = os.path.join(os.path.dirname(__file__), "golden")
+    res, lut = spectral.read_mrspectra(os.path.join(gold, "REC_709_r32.mrspectra"))
+    tables = spectral.load_tables(os.path.join(gold, "spectral_rec709.npz"))
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    if env is not None:
+        pt.set_env(env["texels"])
+    pt.set_spectral(res, lut, tables)
+    S = oracle.PtScene(surf, env=env, spectral=oracle.Spectral(os.path.join(gold, "REC_709_r32.mrspectra"),
+                                                               os.path.join(gold, "spectral_rec709.npz")))
+    return pt, S
+
+
+@pytest.mark.parametrize("scene,mode", [("box", 2), ("box", 0), ("mixed", 2), ("sky", 2)])
+def test_spectral_per_pixel(scene, mode):
+    """Spectral paths: the LUT upsampling (asin / sin in the inverse
+    smoothstep), hyperbolic wavelength sampling (atanh / cosh) and the
+    observer conversion add library transcendentals whose last ulp can
+    differ between CUDA and the host."""
+    surf = {"box": scenes.box_scene(0), "mixed": scenes.box_scene_mixed(0), "sky": scenes.sky_scene(0)}[scene]
+    env = dict(texels=scenes.sky_map(64, 32, seed=0)) if scene == "sky" else None
+    pt, S = _spectral_pair(surf, env)
+    g, o, frac = _compare(pt, S, mode)
+    print("spectral %s mode %d: close %.4f relMSE %.3g" % (scene, mode, frac, relmse(g, o)))
+    assert frac >= 0.97, frac
+    assert relmse(g, o) <= 1e-3
+    # switching back to RGB renders the RGB image
+    pt.set_spectral(0, None, None)
+    S2 = oracle.PtScene(surf, env=env)
+    g2, o2, frac2 = _compare(pt, S2, mode)
+    assert frac2 >= 0.97
+    pt.close()
