@@ -263,6 +263,40 @@ mrg_status mrg_multi_partition(mrg_ctx* ctx, const uint32_t* d_keys, const uint3
                                uint32_t* d_partition_count, uint32_t* d_partition_offsets,
                                uint32_t* d_partition_keys, uint32_t max_partitions, void* stream);
 
+/* Per-vertex texture coordinates of a mesh (the triangle group's "uv"
+ * attribute, PrimitiveDefaultTriangle.h:22-30): nv x 2 floats, nv equal to
+ * the mesh's vertex count. */
+mrg_status mrg_upload_mesh_uv(mrg_ctx* ctx, uint32_t mesh_id, const float* uv, uint32_t nv);
+
+/* An albedo texture: width x height RGBA texels, format 0 = UNORM8 (read as
+ * v / 255) or 1 = f32; bilinear, wrap addressed, one mip level (MRay's
+ * default "Linear" / "Wrap" texture, Docs/markdown/scene/mrayScene.md:76-77).
+ * borrow = 0 copies host texels; borrow = 1 keeps the DEVICE pointer, which
+ * must stay valid and may be rewritten between renders (a parameter texture
+ * being optimised). */
+#define MRG_TEX_RGBA8 0u
+#define MRG_TEX_RGBA32F 1u
+mrg_status mrg_pt_add_texture(mrg_ctx* ctx, uint32_t width, uint32_t height, uint32_t format,
+                              const void* texels, uint32_t borrow, uint32_t* texture_id);
+/* The instance's albedo comes from the texture at the hit's interpolated uv
+ * (its mesh needs uvs); texture_id = 0xFFFFFFFF returns to the constant. */
+mrg_status mrg_pt_set_albedo_texture(mrg_ctx* ctx, uint32_t instance_id, uint32_t texture_id);
+
+/* ---- Path-replay adjoint (no reference counterpart) ---------------------- */
+/* Gradient of  sum_pixels <d_image_adjoint[p].rgb, I[p].rgb>  with respect to
+ * the RGB texels of f32 texture texture_id (a Lambert albedo), I being the
+ * image of params (RGB mode): I[p] = (sum of the pixel's spp sample
+ * radiances) / spp.  Each pass runs twice with the same paths (counter-based
+ * random numbers): the primal records every path's radiance, the replay adds
+ * at every vertex on the texture  d * (radiance after the vertex) / albedo
+ * into the four texels of its bilinear read (Vicini et al. 2021, "Path Replay
+ * Backpropagation").  d_grad (RGBA f32 per texel, A unused) is ADDED to
+ * (atomics).  Russian roulette probabilities are treated as constants.  When
+ * d_image is not NULL the primal image is accumulated into it as
+ * mrg_pt_render does.  Device buffers, stream-ordered. */
+mrg_status mrg_pt_adjoint(mrg_ctx* ctx, const mrg_pt_params* params, uint32_t texture_id,
+                          const float* d_image_adjoint, float* d_grad, float* d_image, void* stream);
+
 /* Skysphere boundary light (LightGroupSkysphere<SphericalCoordConverter>,
  * Source/Tracer/LightsDefault.hpp:300-420, 700-915): a lat-long radiance map
  * of width x height RGBA f32 texels (row-major, row 0 at v = 0; 1 x 1 = a

@@ -31,6 +31,7 @@ EXPORTED = [
     "mrg_sync_status", "mrg_cast_closest_stats", "mrg_cast_closest_host_noalloc",
     "mrg_pt_set_lambert", "mrg_pt_set_area_light", "mrg_pt_camera_frame", "mrg_pt_render",
     "mrg_pt_set_material", "mrg_pt_set_env", "mrg_multi_partition", "mrg_pt_set_spectral",
+    "mrg_upload_mesh_uv", "mrg_pt_add_texture", "mrg_pt_set_albedo_texture", "mrg_pt_adjoint",
 ]
 
 MRG_MAT_LAMBERT, MRG_MAT_REFLECT, MRG_MAT_REFRACT, MRG_MAT_UNREAL = 0, 1, 2, 3
@@ -105,6 +106,10 @@ def _declare(lib):
         "mrg_pt_set_area_light": (C.c_int, [vp, u32, fp, u32]),
         "mrg_pt_set_env": (C.c_int, [vp, u32, u32, vp, vp]),
         "mrg_pt_set_spectral": (C.c_int, [vp, u32, vp, u32, vp, vp, vp, C.c_float, vp]),
+        "mrg_upload_mesh_uv": (C.c_int, [vp, u32, vp, u32]),
+        "mrg_pt_add_texture": (C.c_int, [vp, u32, u32, u32, vp, u32, C.POINTER(u32)]),
+        "mrg_pt_set_albedo_texture": (C.c_int, [vp, u32, u32]),
+        "mrg_pt_adjoint": (C.c_int, [vp, C.POINTER(MrgPtParams), u32, vp, vp, vp, vp]),
         "mrg_multi_partition": (C.c_int, [vp, vp, vp, u32, vp, vp, u32, vp, vp, vp, vp, vp, u32, vp]),
         "mrg_pt_camera_frame": (C.c_int, [C.POINTER(MrgPtParams), fp]),
         "mrg_pt_render": (C.c_int, [vp, C.POINTER(MrgPtParams), vp, vp]),

@@ -128,6 +128,7 @@ mrg_status mrg_destroy(mrg_ctx* c)
     cudaFree(c->dStats);
     cudaFree(c->dPtSurfaces); cudaFree(c->dPtLights); cudaFree(c->dPtTris); cudaFree(c->ptPathMem);
     cudaFree(c->dPtEnv);
+    cudaFree(c->dPtTexTable); cudaFree(c->dPtTexData); cudaFree(c->dPtUvs); cudaFree(c->dPtRadTotal);
     cudaFree(c->dPtSpec);
     cudaFree(c->dPartScratch);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
@@ -156,6 +157,18 @@ mrg_status mrg_upload_mesh(mrg_ctx* c, const float* pos, uint32_t nv, const uint
     c->meshes.push_back(std::move(m));
     c->built = false;
     if(outId) *outId = (uint32_t)(c->meshes.size() - 1);
+    return MRG_OK;
+}
+
+mrg_status mrg_upload_mesh_uv(mrg_ctx* c, uint32_t mesh, const float* uv, uint32_t nv)
+{
+    if(!c || !uv) return fail(MRG_ERR_INVALID_ARG, "mrg_upload_mesh_uv: null pointer");
+    if(mesh >= c->meshes.size()) return fail(MRG_ERR_INVALID_ARG, "mrg_upload_mesh_uv: bad mesh id");
+    if(3ull * nv != c->meshes[mesh].pos.size())
+        return fail(MRG_ERR_INVALID_ARG, "mrg_upload_mesh_uv: uv count differs from the vertex count");
+    try { c->meshes[mesh].uv.assign(uv, uv + 2ull * nv); }
+    catch(...) { return fail(MRG_ERR_OUT_OF_MEMORY, "mrg_upload_mesh_uv: host allocation"); }
+    c->ptDirty = true;
     return MRG_OK;
 }
 

@@ -38,6 +38,7 @@ struct mrg_ctx
         std::vector<float>    pos;
         std::vector<uint32_t> idx;
         uint32_t              primKeyBase = 0;
+        std::vector<float>    uv;             // per-vertex texture coordinates (optional)
         float                 box[6] = { 0, 0, 0, 0, 0, 0 };
         uint32_t              rootNode = 0;
     };
@@ -77,7 +78,20 @@ struct mrg_ctx
         float    iorFront = 1, iorBack = 1;
         float    radiance[3] = { 0, 0, 0 };
         uint32_t twoSided = 0;
+        uint32_t texture = 0;         // albedo texture id + 1 (0: constant albedo)
     };
+    struct PtTextureDesc
+    {
+        uint32_t             width = 0, height = 0, format = 0;   // 0 RGBA8 unorm, 1 RGBA f32
+        std::vector<uint8_t> host;             // owned copy, or empty when borrowed
+        const void*          borrowed = nullptr;
+    };
+    std::vector<PtTextureDesc> ptTextures;
+    void*     dPtTexTable = nullptr;           // PtTexture per texture
+    void*     dPtTexData = nullptr;            // owned texel copies
+    void*     dPtUvs = nullptr;                // 2 float4 per primitive
+    void*     dPtRadTotal = nullptr;           // adjoint: primal radiance per path slot
+    uint32_t  ptRadTotalCap = 0;
     std::vector<PtSurfaceDesc> ptDesc;       // indexed by instance
     bool      ptDirty = true;
     void*     dPtSurfaces = nullptr;

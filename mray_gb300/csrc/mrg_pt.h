@@ -23,6 +23,16 @@ struct __align__(16) PtSurface
     float4 albedo;      // xyz albedo, w: roughness
     float4 mat;         // x: metallic, y: specular, z: front IoR, w: back IoR
     uint4  info;        // x: 1 if light, y: first light index, z: primitive key base, w: PtMaterial
+    uint4  tex;         // x: albedo texture index + 1 (0: constant albedo)
+};
+
+// Albedo texture: RGBA texels, bilinear, wrap addressed, one level.
+struct __align__(16) PtTexture
+{
+    const void* texels;
+    uint32_t    width, height;
+    uint32_t    format;         // 0 RGBA8 unorm, 1 RGBA f32
+    uint32_t    pad;
 };
 
 // One light per emitting triangle (MRay's primitive-backed lights,
@@ -64,6 +74,20 @@ struct PtSpectral
     uint32_t     enabled;
 };
 
+// Path-replay adjoint of the image with respect to an f32 albedo texture
+// (no reference counterpart): the replay of a pass scatters
+// delta[pixel] * (radiance after the vertex) / albedo * bilinear weight
+// into grad for every Lambert vertex whose albedo is the texture.
+struct PtAdjoint
+{
+    const float4* delta;        // dLoss / dPixel (RGB) per pixel
+    float*        grad;         // RGBA per texel (A unused)
+    const float4* radTotal;     // primal radiance per path slot
+    uint32_t      texIndex;     // texture id + 1
+    float         invSpp;       // 1 / samples per pixel of the image
+    uint32_t      enabled;
+};
+
 struct PtCamera
 {
     float pos[3];
@@ -88,6 +112,7 @@ struct PtLaunch
     PtCamera cam;
     PtEnv    env;
     PtSpectral spec;
+    PtAdjoint  adj;
 };
 
 // Path state, structure of arrays (device).
@@ -122,8 +147,19 @@ constexpr uint32_t kPtWorkKeyBits = 3;
 
 cudaError_t pt_raygen(const PtLaunch& L, const PtPaths& P, uint32_t* aliveList, uint32_t* aliveCount,
                       int smCount, cudaStream_t st);
-cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSurface* surfaces, uint32_t nSurfaces,
-                          const PtLight* lights, const float4* tris, uint32_t nTris,
+// Scene tables the shade kernel reads.
+struct PtSceneTables
+{
+    const PtSurface* surfaces;
+    uint32_t         nSurfaces;
+    const PtLight*   lights;
+    const float4*    tris;        // 3 per primitive key
+    uint32_t         nTris;
+    const float4*    uvs;         // 2 per primitive key, or null
+    const PtTexture* textures;
+};
+
+cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSceneTables& T,
                           const uint32_t* aliveList, const uint32_t* aliveCount,
                           uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st);
 cudaError_t pt_work_keys(const PtPaths& P, const PtSurface* surfaces, uint32_t nSurfaces,

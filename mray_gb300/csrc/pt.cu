@@ -649,14 +649,115 @@ __device__ __forceinline__ Chan mis_weighted(Chan tp, float prevPdf, float light
     return tp;
 }
 
-template<bool SPEC>
+// Albedo texture read: bilinear, wrap addressed, with the host texture view's
+// fraction rule; UNORM8 channels as in * (1 / 255) (NormConversion::FromUNorm).
+__device__ __forceinline__ float3 texel_rgb(const PtTexture& t, size_t i)
+{
+    if(t.format == 0u)
+    {
+        const uchar4 c = __ldg(reinterpret_cast<const uchar4*>(t.texels) + i);
+        const float d = 1.0f / 255.0f;
+        return make_float3(add(0.0f, mul((float)c.x, d)), add(0.0f, mul((float)c.y, d)), add(0.0f, mul((float)c.z, d)));
+    }
+    const float4 c = __ldg(reinterpret_cast<const float4*>(t.texels) + i);
+    return make_float3(c.x, c.y, c.z);
+}
+
+__device__ float3 tex_read(const PtTexture& t, float u, float v)
+{
+    const float tx = sub(mul(u, (float)t.width), 0.5f), ty = sub(mul(v, (float)t.height), 0.5f);
+    float bx, by;
+    float fx = modff(tx, &bx), fy = modff(ty, &by);
+    int32_t sx = (int32_t)bx, sy = (int32_t)by;
+    if(fx < 0.0f) { sx -= 1; fx = fabsf(fx); }
+    if(fy < 0.0f) { sy -= 1; fy = fabsf(fy); }
+    const int32_t x0 = wrap_index(sx, (int32_t)t.width), x1 = wrap_index(sx + 1, (int32_t)t.width);
+    const int32_t y0 = wrap_index(sy, (int32_t)t.height), y1 = wrap_index(sy + 1, (int32_t)t.height);
+    const float3 p00 = texel_rgb(t, (size_t)y0 * t.width + x0), p10 = texel_rgb(t, (size_t)y0 * t.width + x1);
+    const float3 p01 = texel_rgb(t, (size_t)y1 * t.width + x0), p11 = texel_rgb(t, (size_t)y1 * t.width + x1);
+    const float gx = sub(1.0f, fx), gy = sub(1.0f, fy);
+    const float ax = add(mul(p00.x, gx), mul(p10.x, fx)), bxx = add(mul(p01.x, gx), mul(p11.x, fx));
+    const float ay = add(mul(p00.y, gx), mul(p10.y, fx)), byy = add(mul(p01.y, gx), mul(p11.y, fx));
+    const float az = add(mul(p00.z, gx), mul(p10.z, fx)), bzz = add(mul(p01.z, gx), mul(p11.z, fx));
+    return make_float3(add(mul(ax, gy), mul(bxx, fy)), add(mul(ay, gy), mul(byy, fy)),
+                       add(mul(az, gy), mul(bzz, fy)));
+}
+
+// The four texels a bilinear read at (u, v) blends and their weights
+// (derivative of tex_read's value with respect to each texel).
+__device__ __forceinline__ void tex_taps(const PtTexture& t, float u, float v, uint32_t idx[4], float w[4])
+{
+    const float tx = sub(mul(u, (float)t.width), 0.5f), ty = sub(mul(v, (float)t.height), 0.5f);
+    float bx, by;
+    float fx = modff(tx, &bx), fy = modff(ty, &by);
+    int32_t sx = (int32_t)bx, sy = (int32_t)by;
+    if(fx < 0.0f) { sx -= 1; fx = fabsf(fx); }
+    if(fy < 0.0f) { sy -= 1; fy = fabsf(fy); }
+    const int32_t x0 = wrap_index(sx, (int32_t)t.width), x1 = wrap_index(sx + 1, (int32_t)t.width);
+    const int32_t y0 = wrap_index(sy, (int32_t)t.height), y1 = wrap_index(sy + 1, (int32_t)t.height);
+    const float gx = sub(1.0f, fx), gy = sub(1.0f, fy);
+    idx[0] = (uint32_t)y0 * t.width + (uint32_t)x0; w[0] = mul(gx, gy);
+    idx[1] = (uint32_t)y0 * t.width + (uint32_t)x1; w[1] = mul(fx, gy);
+    idx[2] = (uint32_t)y1 * t.width + (uint32_t)x0; w[2] = mul(gx, fy);
+    idx[3] = (uint32_t)y1 * t.width + (uint32_t)x1; w[3] = mul(fx, fy);
+}
+
+// Texture coordinates at a hit (GenerateSurface, PrimitiveDefaultTriangle.hpp:
+// 472-476: uv = uv0 a + uv1 b + uv2 c with a = hit[0], b = hit[1], c = 1 - a - b).
+__device__ __forceinline__ float2 surface_uv(const PtSceneTables& T, uint32_t gprim, float2 mh)
+{
+    const float4 q0 = T.uvs[2 * (size_t)gprim], q1 = T.uvs[2 * (size_t)gprim + 1];
+    const float a = mh.x, b = mh.y, c = sub(sub(1.0f, a), b);
+    return make_float2(add(add(mul(q0.x, a), mul(q0.z, b)), mul(q1.x, c)),
+                       add(add(mul(q0.y, a), mul(q0.w, b)), mul(q1.y, c)));
+}
+
+// Albedo at a hit: constant, or the texture at the hit's uv.
+__device__ __forceinline__ float3 surface_albedo(const PtSceneTables& T, const PtSurface& sf, uint32_t gprim, float2 mh)
+{
+    if(sf.tex.x == 0u || T.uvs == nullptr || gprim >= T.nTris) return make_float3(sf.albedo.x, sf.albedo.y, sf.albedo.z);
+    const float2 uv = surface_uv(T, gprim, mh);
+    return tex_read(T.textures[sf.tex.x - 1u], uv.x, uv.y);
+}
+
+// Path-replay adjoint at a Lambert vertex whose albedo is the parameter
+// texture: every contribution after this vertex is linear in its albedo, so
+// d(path radiance)/d(albedo) = (primal radiance - radiance before the vertex)
+// / albedo, per channel; scattered to the four texels of the read.
+__device__ void adjoint_vertex(const PtLaunch& L, const PtSceneTables& T, const PtSurface& sf, uint32_t slot,
+                               uint32_t gprim, float2 mh, float3 alb, const Chan& radBefore)
+{
+    const float4 tot = L.adj.radTotal[slot];
+    const float4 d = L.adj.delta[slot_pixel(L, slot)];
+    const float s = L.adj.invSpp;
+    const float dd[3] = { d.x, d.y, d.z }, tt[3] = { tot.x, tot.y, tot.z }, aa[3] = { alb.x, alb.y, alb.z };
+    float g[3];
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+        g[k] = (aa[k] > 0.0f) ? mul(mul(dd[k], s), __fdiv_rn(sub(tt[k], radBefore.v[k]), aa[k])) : 0.0f;
+    const float2 uv = surface_uv(T, gprim, mh);
+    uint32_t idx[4];
+    float w[4];
+    tex_taps(T.textures[sf.tex.x - 1u], uv.x, uv.y, idx, w);
+#pragma unroll
+    for(int j = 0; j < 4; j++)
+#pragma unroll
+        for(int k = 0; k < 3; k++)
+            atomicAdd(&L.adj.grad[4 * (size_t)idx[j] + k], mul(g[k], w[j]));
+}
+
+template<bool SPEC, bool ADJ>
 __global__ void __launch_bounds__(kPtTPB)
-k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t nSurfaces,
-        const PtLight* __restrict__ lights, const float4* __restrict__ tris, uint32_t nTris,
+k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
         const uint32_t* __restrict__ aliveList, const uint32_t* __restrict__ aliveCount,
         uint32_t* nextList, uint32_t* nextCount)
 {
     constexpr int NC = SPEC ? 4 : 3;
+    const PtSurface* __restrict__ surfaces = T.surfaces;
+    const uint32_t nSurfaces = T.nSurfaces;
+    const PtLight* __restrict__ lights = T.lights;
+    const float4* __restrict__ tris = T.tris;
+    const uint32_t nTris = T.nTris;
     const uint32_t n = *aliveCount;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t nAll = L.nLights + (L.env.enabled ? 1u : 0u);
@@ -749,7 +850,11 @@ k_shade(PtLaunch L, PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t 
                     onb(nrm, tng, btg);
                     const float3 wo = make_float3(-dir.x, -dir.y, -dir.z);
                     const float3 V = make_float3(dot3(wo, tng), dot3(wo, btg), dot3(wo, nrm));
-                    const Chan alb = albedo_of<SPEC>(L.spec, sf.albedo.x, sf.albedo.y, sf.albedo.z, waves);
+                    const float3 a3 = surface_albedo(T, sf, gprim, mh);
+                    const Chan alb = albedo_of<SPEC>(L.spec, a3.x, a3.y, a3.z, waves);
+                    if(ADJ && sf.tex.x == L.adj.texIndex && sf.info.w == kMatLambert && T.uvs != nullptr &&
+                       gprim < nTris)
+                        adjoint_vertex(L, T, sf, i, gprim, mh, a3, rad);
                     const bool isSpec = specularity<NC>(sf, alb) >= kSpecularThreshold;
                     const uint32_t mt = sf.info.w;
                     // ---- NEE (WorkFunctionNEE); specular materials cast none ----
@@ -1072,17 +1177,17 @@ cudaError_t pt_raygen(const PtLaunch& L, const PtPaths& P, uint32_t* aliveList, 
     return cudaGetLastError();
 }
 
-cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSurface* surfaces, uint32_t nSurfaces,
-                          const PtLight* lights, const float4* tris, uint32_t nTris,
+cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSceneTables& T,
                           const uint32_t* aliveList, const uint32_t* aliveCount,
                           uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st)
 {
-    if(L.spec.enabled)
-        k_shade<true><<<(unsigned)smCount * 8u, kPtTPB, 0, st>>>(L, P, surfaces, nSurfaces, lights, tris, nTris,
-                                                               aliveList, aliveCount, nextList, nextCount);
+    const unsigned grid = (unsigned)smCount * 8u;
+    if(L.adj.enabled)
+        k_shade<false, true><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
+    else if(L.spec.enabled)
+        k_shade<true, false><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
     else
-        k_shade<false><<<(unsigned)smCount * 8u, kPtTPB, 0, st>>>(L, P, surfaces, nSurfaces, lights, tris, nTris,
-                                                                aliveList, aliveCount, nextList, nextCount);
+        k_shade<false, false><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
     return cudaGetLastError();
 }
 

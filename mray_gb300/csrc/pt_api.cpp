@@ -238,6 +238,10 @@ mrg_status pt_prepare(mrg_ctx* c)
         s.albedo = make_float4(d.albedo[0], d.albedo[1], d.albedo[2], d.roughness);
         s.mat = make_float4(d.metallic, d.specular, d.iorFront, d.iorBack);
         s.info = make_uint4(d.kind == 2 ? 1u : 0u, (uint32_t)lights.size(), mesh.primKeyBase, d.material);
+        s.tex = make_uint4(d.kind == 1 ? d.texture : 0u, 0u, 0u, 0u);
+        if(s.tex.x && mesh.uv.empty())
+            return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt: instance " + std::to_string(i) +
+                                  " has an albedo texture but its mesh has no uvs");
         if(d.kind == 2)
         {
             const uint32_t nt = (uint32_t)(mesh.idx.size() / 3);
@@ -263,6 +267,56 @@ mrg_status pt_prepare(mrg_ctx* c)
     c->ptSurfaceCount = ni;
     c->ptLightCount = (uint32_t)lights.size();
     c->ptTriCount = maxPrim;
+    // texture coordinates per primitive key, and the texture table
+    cudaFree(c->dPtUvs); c->dPtUvs = nullptr;
+    bool anyUv = false;
+    for(const auto& m : c->meshes) anyUv |= !m.uv.empty();
+    if(anyUv)
+    {
+        std::vector<float4> uvs(2ull * maxPrim, make_float4(0, 0, 0, 0));
+        for(const auto& m : c->meshes)
+        {
+            if(m.uv.empty()) continue;
+            const uint32_t nt = (uint32_t)(m.idx.size() / 3);
+            for(uint32_t t = 0; t < nt; t++)
+            {
+                const float* a = &m.uv[2ull * m.idx[3ull * t]];
+                const float* b = &m.uv[2ull * m.idx[3ull * t + 1]];
+                const float* d = &m.uv[2ull * m.idx[3ull * t + 2]];
+                const size_t g = 2ull * (m.primKeyBase + t);
+                uvs[g] = make_float4(a[0], a[1], b[0], b[1]);
+                uvs[g + 1] = make_float4(d[0], d[1], 0.0f, 0.0f);
+            }
+        }
+        PT_TRY(cudaMalloc(&c->dPtUvs, sizeof(float4) * uvs.size()), "mrg_pt: uvs");
+        PT_TRY(cudaMemcpy(c->dPtUvs, uvs.data(), sizeof(float4) * uvs.size(), cudaMemcpyHostToDevice), "mrg_pt: uvs");
+    }
+    cudaFree(c->dPtTexTable); c->dPtTexTable = nullptr;
+    cudaFree(c->dPtTexData); c->dPtTexData = nullptr;
+    if(!c->ptTextures.empty())
+    {
+        size_t owned = 0;
+        for(const auto& t : c->ptTextures) owned += (t.host.size() + 255) & ~size_t(255);
+        if(owned) PT_TRY(cudaMalloc(&c->dPtTexData, owned), "mrg_pt: textures");
+        std::vector<mrg::PtTexture> table(c->ptTextures.size());
+        size_t off = 0;
+        for(size_t k = 0; k < c->ptTextures.size(); k++)
+        {
+            const auto& t = c->ptTextures[k];
+            table[k].width = t.width; table[k].height = t.height; table[k].format = t.format; table[k].pad = 0;
+            if(t.borrowed) table[k].texels = t.borrowed;
+            else
+            {
+                char* dst = static_cast<char*>(c->dPtTexData) + off;
+                PT_TRY(cudaMemcpy(dst, t.host.data(), t.host.size(), cudaMemcpyHostToDevice), "mrg_pt: textures");
+                table[k].texels = dst;
+                off += (t.host.size() + 255) & ~size_t(255);
+            }
+        }
+        PT_TRY(cudaMalloc(&c->dPtTexTable, sizeof(mrg::PtTexture) * table.size()), "mrg_pt: textures");
+        PT_TRY(cudaMemcpy(c->dPtTexTable, table.data(), sizeof(mrg::PtTexture) * table.size(), cudaMemcpyHostToDevice),
+               "mrg_pt: textures");
+    }
     uint32_t groups = 0;
     for(uint32_t i = 0; i < ni; i++)
         if(c->ptDesc[i].kind == 1) groups |= 1u << std::min<uint32_t>(c->ptDesc[i].material, 31u);
@@ -438,6 +492,40 @@ mrg_status mrg_pt_set_spectral(mrg_ctx* c, uint32_t lutRes, const float* lut, ui
     return MRG_OK;
 }
 
+mrg_status mrg_pt_add_texture(mrg_ctx* c, uint32_t w, uint32_t h, uint32_t format, const void* texels,
+                              uint32_t borrow, uint32_t* outId)
+{
+    if(!c || !texels || !outId) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_add_texture: null pointer");
+    if(w == 0 || h == 0 || format > MRG_TEX_RGBA32F)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_add_texture: empty texture or unknown format");
+    if((uint64_t)w * h > (1ull << 28)) return mrg::set_error(MRG_ERR_LIMIT, "mrg_pt_add_texture: more than 2^28 texels");
+    mrg_ctx::PtTextureDesc t;
+    t.width = w; t.height = h; t.format = format;
+    if(borrow) t.borrowed = texels;
+    else
+    {
+        const size_t bytes = (size_t)w * h * (format == MRG_TEX_RGBA8 ? 4u : 16u);
+        try { t.host.assign(static_cast<const uint8_t*>(texels), static_cast<const uint8_t*>(texels) + bytes); }
+        catch(...) { return mrg::set_error(MRG_ERR_OUT_OF_MEMORY, "mrg_pt_add_texture: host allocation"); }
+    }
+    c->ptTextures.push_back(std::move(t));
+    *outId = (uint32_t)(c->ptTextures.size() - 1);
+    c->ptDirty = true;
+    return MRG_OK;
+}
+
+mrg_status mrg_pt_set_albedo_texture(mrg_ctx* c, uint32_t inst, uint32_t texId)
+{
+    if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_albedo_texture: null context");
+    if(inst >= c->insts.size()) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_albedo_texture: bad instance");
+    if(texId != 0xFFFFFFFFu && texId >= c->ptTextures.size())
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_albedo_texture: bad texture id");
+    if(c->ptDesc.size() < c->insts.size()) c->ptDesc.resize(c->insts.size());
+    c->ptDesc[inst].texture = (texId == 0xFFFFFFFFu) ? 0u : texId + 1u;
+    c->ptDirty = true;
+    return MRG_OK;
+}
+
 mrg_status mrg_pt_camera_frame(const mrg_pt_params* p, float out[16])
 {
     if(!p || !out) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_camera_frame: null pointer");
@@ -449,35 +537,47 @@ mrg_status mrg_pt_camera_frame(const mrg_pt_params* p, float out[16])
     return MRG_OK;
 }
 
-mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void* stream)
+} // extern "C"
+
+namespace {
+
+// One render's launch description, scene tables and switches.
+struct PtRun
 {
-    if(!c || !p || !dImage) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: null pointer");
-    if(!c->built) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_pt_render: call mrg_build first");
+    mrg::PtLaunch       L{};
+    mrg::PtSceneTables  T{};
+    mrg::TraceScratch   scr{};
+    bool                partition = false;
+    uint32_t            spp = 1;       // samples per pass
+    uint32_t            slots = 0;
+};
+
+mrg_status pt_setup(mrg_ctx* c, const mrg_pt_params* p, PtRun& R, const char* who)
+{
+    const std::string w(who);
+    if(!c->built) return mrg::set_error(MRG_ERR_NOT_BUILT, w + ": call mrg_build first");
     if(p->width == 0 || p->height == 0 || p->spp == 0)
-        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: empty image or zero samples");
+        return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": empty image or zero samples");
     if(p->maxDepth == 0 || p->maxDepth > 255 || p->sampleMode > MRG_PT_NEE_MIS || p->partitionByMaterial > 2u)
-        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: maxDepth must be in [1, 255], sampleMode and "
+        return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": maxDepth must be in [1, 255], sampleMode and "
                                                    "partitionByMaterial in [0, 2]");
     const uint64_t wh = (uint64_t)p->width * p->height;
-    uint32_t spp = p->samplesPerPass ? p->samplesPerPass : std::max<uint32_t>(1, (uint32_t)std::min<uint64_t>(p->spp, (1ull << 22) / wh));
+    uint32_t spp = p->samplesPerPass ? p->samplesPerPass
+                                     : std::max<uint32_t>(1, (uint32_t)std::min<uint64_t>(p->spp, (1ull << 22) / wh));
     spp = std::min(spp, p->spp);
     if(p->spp % spp != 0) spp = 1;
-    if(wh * spp > (1ull << 26))
-        return mrg::set_error(MRG_ERR_LIMIT, "mrg_pt_render: more than 2^26 paths per pass");
-    DevGuard g(c->device);
+    if(wh * spp > (1ull << 26)) return mrg::set_error(MRG_ERR_LIMIT, w + ": more than 2^26 paths per pass");
     for(uint32_t i = 0; i < c->insts.size(); i++)
         if(i >= c->ptDesc.size() || c->ptDesc[i].kind == 0)
-            return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: instance " + std::to_string(i) +
-                                  " has no material or light");
+            return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": instance " + std::to_string(i) + " has no material or light");
     mrg_status s = pt_prepare(c);
     if(s != MRG_OK) return s;
-    const uint32_t slots = (uint32_t)(wh * spp);
-    if((s = pt_paths(c, slots)) != MRG_OK) return s;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-
-    mrg::PtLaunch L{};
+    R.spp = spp;
+    R.slots = (uint32_t)(wh * spp);
+    if((s = pt_paths(c, R.slots)) != MRG_OK) return s;
+    mrg::PtLaunch& L = R.L;
     L.width = p->width; L.height = p->height;
-    L.slots = slots; L.samplesPerPass = spp;
+    L.slots = R.slots; L.samplesPerPass = spp;
     L.rrStart = p->rrStart; L.maxDepth = p->maxDepth;
     L.sampleMode = p->sampleMode; L.seed = p->seed;
     L.nLights = c->ptLightCount;
@@ -485,48 +585,120 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
     L.spec = c->ptSpec;
     L.filterSigma = p->filterRadius * 0.285714f;
     camera_frame(*p, L.cam);
+    R.partition = p->partitionByMaterial == 1u ||
+                  (p->partitionByMaterial == 2u && (c->ptMaterialGroups > 1u || c->ptEnvSet));
+    R.scr.workCounter = c->dScratch;
+    R.scr.errorFlag = c->dScratch + 1;
+    R.scr.stats = c->dStats;
+    R.T.surfaces = static_cast<const mrg::PtSurface*>(c->dPtSurfaces);
+    R.T.nSurfaces = c->ptSurfaceCount;
+    R.T.lights = static_cast<const mrg::PtLight*>(c->dPtLights);
+    R.T.tris = static_cast<const float4*>(c->dPtTris);
+    R.T.nTris = c->ptTriCount;
+    R.T.uvs = static_cast<const float4*>(c->dPtUvs);
+    R.T.textures = static_cast<const mrg::PtTexture*>(c->dPtTexTable);
+    return MRG_OK;
+}
+
+// raygen + maxDepth bounces of the pass at R.L.sampleBase; leaves each slot's
+// radiance in the path state.
+cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, cudaStream_t st)
+{
     mrg::PtPaths& P = c->ptPaths;
-    const bool partition = p->partitionByMaterial == 1u ||
-                           (p->partitionByMaterial == 2u && (c->ptMaterialGroups > 1u || c->ptEnvSet));
-    mrg::TraceScratch scr;
-    scr.workCounter = c->dScratch;
-    scr.errorFlag = c->dScratch + 1;
-    scr.stats = c->dStats;
-    const auto* surf = static_cast<const mrg::PtSurface*>(c->dPtSurfaces);
-    const auto* lights = static_cast<const mrg::PtLight*>(c->dPtLights);
-    const auto* tris = static_cast<const float4*>(c->dPtTris);
-    for(uint32_t pass = 0; pass < p->spp / spp; pass++)
+    const mrg::PtLaunch& L = R.L;
+    cudaError_t e = mrg::pt_raygen(L, P, P.listA, P.counts + 0, c->smCount, st);
+    for(uint32_t depth = 0; depth < L.maxDepth && e == cudaSuccess; depth++)
     {
-        L.sampleBase = p->sampleStart + pass * spp;
-        PT_TRY(mrg::pt_raygen(L, P, P.listA, P.counts + 0, c->smCount, st), "raygen");
-        for(uint32_t depth = 0; depth < p->maxDepth; depth++)
+        uint32_t* alive = (depth & 1u) ? P.listB : P.listA;
+        uint32_t* next = (depth & 1u) ? P.listA : P.listB;
+        uint32_t* aliveCount = P.counts + ((depth & 1u) ? 1 : 0);
+        uint32_t* nextCount = P.counts + ((depth & 1u) ? 0 : 1);
+        e = cudaMemsetAsync(nextCount, 0, sizeof(uint32_t), st);
+        if(e == cudaSuccess) e = cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), st);
+        if(e == cudaSuccess)
+            e = mrg::launch_closest(c->scene, R.scr, P.rays, alive, 0, P.hits, P.meta, c->smCount, st, aliveCount);
+        const uint32_t* shadeList = alive;
+        if(e == cudaSuccess && R.partition)
         {
-            uint32_t* alive = (depth & 1u) ? P.listB : P.listA;
-            uint32_t* next = (depth & 1u) ? P.listA : P.listB;
-            uint32_t* aliveCount = P.counts + ((depth & 1u) ? 1 : 0);
-            uint32_t* nextCount = P.counts + ((depth & 1u) ? 0 : 1);
-            PT_TRY(cudaMemsetAsync(nextCount, 0, sizeof(uint32_t), st), "reset");
-            PT_TRY(cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), st), "reset");
-            PT_TRY(mrg::launch_closest(c->scene, scr, P.rays, alive, 0, P.hits, P.meta, c->smCount, st,
-                                       aliveCount), "closest hit");
-            const uint32_t* shadeList = alive;
-            if(partition)
-            {
-                mrg::DigitSpec ks;
-                ks.batchShift = 0; ks.batchWidth = mrg::kPtWorkKeyBits;
-                ks.digitShift = 0; ks.digitBits = mrg::kPtWorkKeyBits;
-                PT_TRY(mrg::pt_work_keys(P, surf, c->ptSurfaceCount, alive, aliveCount, c->smCount, st), "work keys");
-                PT_TRY(mrg::multisplit_pass(P.workKeys, alive, P.workKeysOut, P.listSorted, aliveCount, slots, ks,
-                                            P.sortHist, st), "partition");
-                shadeList = P.listSorted;
-            }
-            PT_TRY(mrg::pt_shade_impl(L, P, surf, c->ptSurfaceCount, lights, tris, c->ptTriCount, shadeList,
-                                      aliveCount, next, nextCount, c->smCount, st), "shade");
-            PT_TRY(mrg::launch_visibility(c->scene, scr, P.visBits, P.shadowRays, P.shadowList, 0,
-                                          c->smCount, st, P.counts + 2), "shadow rays");
-            PT_TRY(mrg::pt_resolve(L, P, depth, c->smCount, st), "resolve");
+            mrg::DigitSpec ks;
+            ks.batchShift = 0; ks.batchWidth = mrg::kPtWorkKeyBits;
+            ks.digitShift = 0; ks.digitBits = mrg::kPtWorkKeyBits;
+            e = mrg::pt_work_keys(P, R.T.surfaces, R.T.nSurfaces, alive, aliveCount, c->smCount, st);
+            if(e == cudaSuccess)
+                e = mrg::multisplit_pass(P.workKeys, alive, P.workKeysOut, P.listSorted, aliveCount, R.slots, ks,
+                                         P.sortHist, st);
+            shadeList = P.listSorted;
         }
-        PT_TRY(mrg::pt_film(L, P, reinterpret_cast<float4*>(dImage), st), "film");
+        if(e == cudaSuccess)
+            e = mrg::pt_shade_impl(L, P, R.T, shadeList, aliveCount, next, nextCount, c->smCount, st);
+        if(e == cudaSuccess)
+            e = mrg::launch_visibility(c->scene, R.scr, P.visBits, P.shadowRays, P.shadowList, 0, c->smCount, st,
+                                       P.counts + 2);
+        if(e == cudaSuccess) e = mrg::pt_resolve(L, P, depth, c->smCount, st);
+    }
+    return e;
+}
+
+} // namespace
+
+extern "C" {
+
+mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void* stream)
+{
+    if(!c || !p || !dImage) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render: null pointer");
+    DevGuard g(c->device);
+    PtRun R;
+    mrg_status s = pt_setup(c, p, R, "mrg_pt_render");
+    if(s != MRG_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    for(uint32_t pass = 0; pass < p->spp / R.spp; pass++)
+    {
+        R.L.sampleBase = p->sampleStart + pass * R.spp;
+        PT_TRY(pt_bounces(c, R, st), "render pass");
+        PT_TRY(mrg::pt_film(R.L, c->ptPaths, reinterpret_cast<float4*>(dImage), st), "film");
+    }
+    return MRG_OK;
+}
+
+mrg_status mrg_pt_adjoint(mrg_ctx* c, const mrg_pt_params* p, uint32_t texId, const float* dImageAdjoint,
+                          float* dGrad, float* dImage, void* stream)
+{
+    if(!c || !p || !dImageAdjoint || !dGrad) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: null pointer");
+    if(texId >= c->ptTextures.size() || c->ptTextures[texId].format != MRG_TEX_RGBA32F)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: the parameter must be an f32 texture");
+    if(c->ptSpec.enabled) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: RGB rendering only");
+    for(uint32_t i = 0; i < c->insts.size() && i < c->ptDesc.size(); i++)
+        if(c->ptDesc[i].kind == 1 && c->ptDesc[i].texture == texId + 1 && c->ptDesc[i].material != MRG_MAT_LAMBERT)
+            return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: the parameter texture must feed Lambert albedos");
+    DevGuard g(c->device);
+    PtRun R;
+    mrg_status s = pt_setup(c, p, R, "mrg_pt_adjoint");
+    if(s != MRG_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if(c->ptRadTotalCap < R.slots)
+    {
+        cudaFree(c->dPtRadTotal);
+        c->dPtRadTotal = nullptr;
+        c->ptRadTotalCap = 0;
+        PT_TRY(cudaMalloc(&c->dPtRadTotal, sizeof(float4) * (size_t)R.slots), "mrg_pt_adjoint: primal radiance");
+        c->ptRadTotalCap = R.slots;
+    }
+    mrg::PtAdjoint& A = R.L.adj;
+    A.delta = reinterpret_cast<const float4*>(dImageAdjoint);
+    A.grad = dGrad;
+    A.radTotal = static_cast<const float4*>(c->dPtRadTotal);
+    A.texIndex = texId + 1u;
+    A.invSpp = 1.0f / (float)p->spp;
+    for(uint32_t pass = 0; pass < p->spp / R.spp; pass++)
+    {
+        R.L.sampleBase = p->sampleStart + pass * R.spp;
+        A.enabled = 0u;
+        PT_TRY(pt_bounces(c, R, st), "primal pass");
+        if(dImage) PT_TRY(mrg::pt_film(R.L, c->ptPaths, reinterpret_cast<float4*>(dImage), st), "film");
+        PT_TRY(cudaMemcpyAsync(c->dPtRadTotal, c->ptPaths.rad, sizeof(float4) * (size_t)R.slots,
+                               cudaMemcpyDeviceToDevice, st), "primal radiance");
+        A.enabled = 1u;
+        PT_TRY(pt_bounces(c, R, st), "replay pass");
     }
     return MRG_OK;
 }

@@ -21,16 +21,65 @@ class PathTracer:
         self.n_instances = 0
         self._prim_base = 0
 
-    def add_surface(self, pos, idx, m34, cull=True):
+    def add_surface(self, pos, idx, m34, cull=True, uv=None):
         """Adds a mesh instance with dense primitive keys and trans_key =
-        instance id (what the renderer's shading looks up)."""
+        instance id (what the renderer's shading looks up); uv: optional
+        per-vertex texture coordinates."""
         nt = int(np.asarray(idx).reshape(-1, 3).shape[0])
         mesh = self.acc.upload_mesh(pos, idx, prim_key_base=self._prim_base)
+        if uv is not None:
+            u = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+            N.check(N.lib().mrg_upload_mesh_uv(self.acc._h, mesh, u.ctypes.data, u.shape[0]))
         inst = self.n_instances
         self.acc.add_instance(mesh, m34, cull=cull, trans_key=inst, accel_key=inst)
         self._prim_base += nt
         self.n_instances += 1
         return inst
+
+    def add_texture(self, texels):
+        """An albedo texture: a (h, w, 4) uint8 / float32 numpy array (copied)
+        or a float32 CUDA tensor (borrowed: rewrites show in later renders).
+        Returns its id."""
+        out = C.c_uint32()
+        if hasattr(texels, "data_ptr"):
+            if texels.dtype.__str__() != "torch.float32" or texels.dim() != 3 or texels.shape[2] != 4:
+                raise ValueError("device textures are (h, w, 4) float32")
+            if not texels.is_contiguous():
+                raise ValueError("device textures must be contiguous")
+            self._tex_keep = getattr(self, "_tex_keep", []) + [texels]
+            N.check(N.lib().mrg_pt_add_texture(self.acc._h, texels.shape[1], texels.shape[0], 1,
+                                               C.c_void_p(texels.data_ptr()), 1, C.byref(out)))
+            self._tex_shapes = getattr(self, "_tex_shapes", {})
+            self._tex_shapes[out.value] = (texels.shape[0], texels.shape[1])
+            return out.value
+        t = np.ascontiguousarray(texels)
+        if t.ndim != 3 or t.shape[2] != 4 or t.dtype not in (np.uint8, np.float32):
+            raise ValueError("textures are (h, w, 4) uint8 or float32")
+        N.check(N.lib().mrg_pt_add_texture(self.acc._h, t.shape[1], t.shape[0], 0 if t.dtype == np.uint8 else 1,
+                                           t.ctypes.data, 0, C.byref(out)))
+        self._tex_shapes = getattr(self, "_tex_shapes", {})
+        self._tex_shapes[out.value] = (t.shape[0], t.shape[1])
+        return out.value
+
+    def adjoint(self, p, tex_id, image_adjoint, grad=None, image=None, stream=None):
+        """Path-replay adjoint (see mrg_pt_adjoint): image_adjoint is a
+        (h, w, 4) float32 CUDA tensor of dLoss/dPixel; returns grad, a
+        (texH, texW, 4) float32 CUDA tensor the gradient is added to."""
+        import torch
+        t = self._tex_shape(tex_id)
+        if grad is None:
+            grad = torch.zeros((t[0], t[1], 4), dtype=torch.float32, device="cuda:%d" % self.acc.device)
+        N.check(N.lib().mrg_pt_adjoint(self.acc._h, C.byref(p), tex_id, C.c_void_p(image_adjoint.data_ptr()),
+                                       C.c_void_p(grad.data_ptr()),
+                                       None if image is None else C.c_void_p(image.data_ptr()),
+                                       _stream_ptr(stream)))
+        return grad
+
+    def _tex_shape(self, tex_id):
+        return self._tex_shapes[tex_id]
+
+    def set_albedo_texture(self, inst, tex_id):
+        N.check(N.lib().mrg_pt_set_albedo_texture(self.acc._h, inst, 0xFFFFFFFF if tex_id is None else tex_id))
 
     def set_lambert(self, inst, albedo):
         a = (C.c_float * 3)(*[float(x) for x in albedo])
@@ -128,13 +177,19 @@ def load_box_scene(pt, seed=0):
     PathTracer; returns the surface list."""
     from . import scenes
     surf = scenes.box_scene(seed) if isinstance(seed, int) else seed
+    textures = {}
     for s in surf:
-        inst = pt.add_surface(s["pos"], s["idx"], s["m34"], cull=s.get("cull", True))
+        inst = pt.add_surface(s["pos"], s["idx"], s["m34"], cull=s.get("cull", True), uv=s.get("uv"))
         if s["kind"] == "light":
             pt.set_area_light(inst, s["radiance"])
         else:
             pt.set_material(inst, s.get("material", "lambert"), s["albedo"],
                             roughness=s.get("roughness", 0.0), metallic=s.get("metallic", 0.0),
                             specular=s.get("specular", 0.5), ior=s.get("ior", (1.0, 1.5)))
+            if s.get("texture") is not None:
+                key = id(s["texture"])
+                if key not in textures:
+                    textures[key] = pt.add_texture(s["texture"])
+                pt.set_albedo_texture(inst, textures[key])
     pt.build()
     return surf

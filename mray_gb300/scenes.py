@@ -208,6 +208,103 @@ def sky_scene(seed=0):
     return [s[0], s[3], s[5], s[6], s[7]]
 
 
+def value_noise_texture(size=256, seed=0, octaves=4, base=0.15, span=0.7, dtype=np.uint8):
+    """Seeded RGBA texture of fractal gradient ("Perlin") noise, one
+    independent field per colour channel, mapped to [base, base + span];
+    uint8 (RGBA8, alpha 255) or float32 (alpha 1).  Tileable (wraps)."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((size, size, 3), np.float64)
+    y, x = np.meshgrid(np.arange(size) / size, np.arange(size) / size, indexing="ij")
+    for c in range(3):
+        acc = np.zeros((size, size))
+        amp, total = 1.0, 0.0
+        for o in range(octaves):
+            cells = 4 << o
+            ang = rng.random((cells, cells)) * 2 * np.pi
+            gx, gy = np.cos(ang), np.sin(ang)
+            fx, fy = x * cells, y * cells
+            ix, iy = np.floor(fx).astype(np.int64), np.floor(fy).astype(np.int64)
+            tx, ty = fx - ix, fy - iy
+
+            def dot(ox, oy):
+                cx, cy = (ix + ox) % cells, (iy + oy) % cells
+                return gx[cy, cx] * (tx - ox) + gy[cy, cx] * (ty - oy)
+            sx = tx * tx * tx * (tx * (tx * 6 - 15) + 10)
+            sy = ty * ty * ty * (ty * (ty * 6 - 15) + 10)
+            top = dot(0, 0) * (1 - sx) + dot(1, 0) * sx
+            bot = dot(0, 1) * (1 - sx) + dot(1, 1) * sx
+            acc += amp * (top * (1 - sy) + bot * sy)
+            total += amp
+            amp *= 0.5
+        out[..., c] = np.clip(0.5 + acc / total, 0.0, 1.0)
+    val = base + span * out
+    if dtype == np.uint8:
+        t = np.full((size, size, 4), 255, np.uint8)
+        t[..., :3] = np.round(val * 255.0).astype(np.uint8)
+        return t
+    t = np.ones((size, size, 4), np.float32)
+    t[..., :3] = val.astype(np.float32)
+    return t
+
+
+def quad_uv():
+    """Texture coordinates of _quad's four corners."""
+    return np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+
+
+def box_scene_textured(seed=0, size=256):
+    """Box scene with RGBA8 noise textures on the floor, back and left walls
+    (two textures, one shared) and per-vertex uvs on every quad."""
+    s = box_scene(seed)
+    t0 = value_noise_texture(size, seed)
+    t1 = value_noise_texture(size, seed + 1)
+    for k, tex in ((0, t0), (2, t1), (3, t0)):
+        s[k]["uv"] = quad_uv() * 2.0            # two repeats: exercises wrapping
+        s[k]["texture"] = tex
+    return s
+
+
+def uv_sphere(n_theta=128, n_phi=256, radius=1.0, noise=0.0, seed=0):
+    """Latitude-longitude sphere with (n_theta - 1) * n_phi * 2 triangles
+    plus the pole fans (2 * n_phi), uv = (phi / 2pi, theta / pi); optional
+    smooth radial displacement of amplitude noise * radius."""
+    th = np.linspace(0.0, np.pi, n_theta + 1)
+    ph = np.linspace(0.0, 2 * np.pi, n_phi + 1)
+    T, Pp = np.meshgrid(th, ph, indexing="ij")
+    rng = np.random.default_rng(seed)
+    r = np.full(T.shape, radius)
+    if noise:
+        for k in range(1, 4):
+            a, b, c = rng.random(3) * 2 * np.pi
+            r += noise * radius / k * np.sin(k * 3 * T + a) * np.cos(k * 2 * Pp + b + c)
+        r[:, -1] = r[:, 0]
+    pos = np.stack([r * np.sin(T) * np.cos(Pp), r * np.cos(T), r * np.sin(T) * np.sin(Pp)], -1).reshape(-1, 3)
+    uv = np.stack([Pp / (2 * np.pi), T / np.pi], -1).reshape(-1, 2)
+    W = n_phi + 1
+    idx = []
+    for i in range(n_theta):
+        for j in range(n_phi):
+            a, b, c, d = i * W + j, i * W + j + 1, (i + 1) * W + j + 1, (i + 1) * W + j
+            if i != 0:
+                idx.append((a, c, b))
+            if i != n_theta - 1:
+                idx.append((a, d, c))
+    return pos.astype(np.float32), np.array(idx, np.uint32), uv.astype(np.float32)
+
+
+def adjoint_scene(texture, seed=0, n_theta=128, n_phi=256, noise=0.03):
+    """The box scene plus a displaced lat-long sphere (radius 0.15 at
+    (0.35, 0.2, 0.25), clear of both boxes; 65,024 triangles at the default
+    resolution) whose Lambert albedo is `texture` (an f32 RGBA array or
+    tensor): the differentiable-rendering workload."""
+    s = box_scene(seed)
+    pos, idx, uv = uv_sphere(n_theta, n_phi, 0.15, noise=noise, seed=seed)
+    m = np.array([1, 0, 0, 0.35, 0, 1, 0, 0.2, 0, 0, 1, 0.25], np.float32)
+    s.insert(len(s) - 1, dict(pos=pos, idx=idx, uv=uv, m34=m, kind="lambert", albedo=[0.5, 0.5, 0.5],
+                              texture=texture, cull=False))
+    return s
+
+
 def box_camera():
     """Pinhole camera of the box scene (position, gaze point, up, fov radians, near/far)."""
     f = 40.0 * np.pi / 180.0

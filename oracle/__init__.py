@@ -73,6 +73,9 @@ def lib():
         L.orc_env_read.argtypes = [vp, u32, u32, vp, vp]
         L.orc_env_dir_to_uv.argtypes = [vp, vp]
         L.orc_env_uv_to_dir.argtypes = [vp, vp]
+        L.orc_tex_read.argtypes = [vp, u32, u32, u32, vp, vp]
+        L.orc_pt_adjoint.argtypes = [vp, vp, vp, vp, u32, vp, vp, u32, u32, vp, vp, C.c_int]
+        L.orc_pt_adjoint.restype = C.c_int
         L.orc_pt_render.restype = C.c_int
         L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
         L.orc_pt_make_light.argtypes = [vp, vp, vp, C.c_int, vp]
@@ -259,7 +262,8 @@ class PtSurface(C.Structure):
                 ("roughness", C.c_float), ("metallic", C.c_float), ("specular", C.c_float),
                 ("iorFront", C.c_float), ("iorBack", C.c_float), ("lightBase", u32),
                 ("primKeyBase", u32), ("triangles", vp), ("m", C.c_float * 12),
-                ("inv", C.c_float * 12)]
+                ("inv", C.c_float * 12), ("texels", vp), ("texW", u32), ("texH", u32),
+                ("texFormat", u32), ("uvs", vp)]
 
 
 class PtLightTri(C.Structure):
@@ -437,6 +441,17 @@ class PtScene:
             sf.primKeyBase = prim
             sf.triangles = tri.ctypes.data_as(vp)
             sf.m[:] = [float(x) for x in np.asarray(s["m34"], np.float32).reshape(12)]
+            if s.get("texture") is not None:
+                tex = np.ascontiguousarray(s["texture"])
+                if tex.dtype not in (np.uint8, np.float32) or tex.ndim != 3 or tex.shape[2] != 4:
+                    raise ValueError("texture must be (h, w, 4) uint8 or float32")
+                uv = np.ascontiguousarray(s["uv"], np.float32).reshape(-1, 2)
+                uvp = np.ascontiguousarray(uv[idx].reshape(-1, 6), np.float32)
+                self._keep += [tex, uvp]
+                sf.texels = tex.ctypes.data
+                sf.texH, sf.texW = tex.shape[0], tex.shape[1]
+                sf.texFormat = 0 if tex.dtype == np.uint8 else 1
+                sf.uvs = uvp.ctypes.data
             if s["kind"] == "light":
                 rad = (C.c_float * 3)(*[float(x) for x in s["radiance"]])
                 m = np.ascontiguousarray(s["m34"], np.float32).reshape(12)
@@ -470,6 +485,23 @@ class PtScene:
             E.inv[:] = [float(x) for x in inv]
             E.sceneDiameter = self.L.orc_scene_diameter(self.S._h)
             self.env = E
+
+    def adjoint(self, p, surface, delta, threads=None):
+        """FP64 path-replay gradient of sum(delta * image) with respect to the
+        RGB texels of the albedo texture of surface index `surface` (every
+        surface sharing that texture array contributes)."""
+        sf = self.surf[surface]
+        if not sf.texels:
+            raise ValueError("surface has no texture")
+        d = np.ascontiguousarray(delta, np.float32)
+        grad = np.zeros((sf.texH, sf.texW, 4), np.float64)
+        rc = self.L.orc_pt_adjoint(self.S._h, C.byref(p), self.surf, self.lights, self.n_lights,
+                                   C.byref(self.env) if self.env is not None else None,
+                                   C.c_void_p(sf.texels), sf.texW, sf.texH, _vp(d), _vp(grad),
+                                   threads or default_threads())
+        if rc != 0:
+            raise RuntimeError("oracle adjoint failed")
+        return grad
 
     def scene_aabb(self):
         out = np.zeros(6, np.float32)

@@ -346,6 +346,45 @@ static inline int32_t wrap_index(int32_t i, int32_t n)
 /* ReadInterpolatedPixel + FindInterpolants of the host texture view,
  * including its treatment of negative texel coordinates (the fraction of a
  * negative coordinate is its absolute value). */
+static inline void texel_rgb(const void* texels, uint32_t format, size_t i, float out[3])
+{
+    if(format == 0)
+    {
+        const uint8_t* t = (const uint8_t*)texels + 4 * i;
+        /* FromUNorm: MIN + in * (1 / (MAX - MIN)) */
+        const float delta = 1.0f / 255.0f;
+        for(int k = 0; k < 3; k++) out[k] = 0.0f + (float)t[k] * delta;
+    }
+    else
+    {
+        const float* t = (const float*)texels + 4 * i;
+        for(int k = 0; k < 3; k++) out[k] = t[k];
+    }
+}
+
+void orc_tex_read(const void* texels, uint32_t w, uint32_t h, uint32_t format, const float uv[2], float rgb[3])
+{
+    float tx = uv[0] * (float)w - 0.5f, ty = uv[1] * (float)h - 0.5f;
+    float bx, by;
+    float fx = modff(tx, &bx), fy = modff(ty, &by);
+    int32_t sx = (int32_t)bx, sy = (int32_t)by;
+    if(fx < 0.0f) { sx -= 1; fx = fabsf(fx); }
+    if(fy < 0.0f) { sy -= 1; fy = fabsf(fy); }
+    float pix[4][3];
+    for(int j = 0; j < 2; j++)
+        for(int i = 0; i < 2; i++)
+        {
+            int32_t x = wrap_index(sx + i, (int32_t)w), y = wrap_index(sy + j, (int32_t)h);
+            texel_rgb(texels, format, (size_t)y * w + (size_t)x, pix[(j << 1) + i]);
+        }
+    for(int k = 0; k < 3; k++)
+    {
+        float a = pix[0][k] * (1.0f - fx) + pix[1][k] * fx;
+        float b = pix[2][k] * (1.0f - fx) + pix[3][k] * fx;
+        rgb[k] = a * (1.0f - fy) + b * fy;
+    }
+}
+
 void orc_env_read(const float* texels, uint32_t w, uint32_t h, const float uv[2], float rgb[3])
 {
     float tx = uv[0] * (float)w - 0.5f, ty = uv[1] * (float)h - 0.5f;
@@ -618,6 +657,13 @@ typedef struct
     uint32_t                  nLights;      /* triangle lights */
     const orc_pt_env*         env;          /* boundary light (last), or NULL */
     const orc_spectral*       spec;         /* NULL: RGB */
+    /* adjoint (orc_pt_adjoint) */
+    const void*               adjTexels;
+    uint32_t                  adjW, adjH;
+    const float*              adjDelta;
+    double*                   adjGrad;      /* one buffer per worker */
+    int                       adjWorkers;
+    atomic_int                adjNextBuffer;
     float*                    image;
     atomic_uint               nextRow;
 } pt_job;
@@ -665,7 +711,35 @@ static void surface_of(const orc_pt_surface* sf, const float* tri9 /* v0 v1 v2 l
     normalize3f(n);
 }
 
+/* adj: NULL for a primal trace; else {primal radiance[3], delta / spp [3]}
+ * and the worker's gradient buffer. */
+typedef struct { float tot[3]; float d[3]; double* grad; } adj_ctx;
+
+static void tex_taps(uint32_t w, uint32_t h, const float uv[2], size_t idx[4], float wt[4])
+{
+    float tx = uv[0] * (float)w - 0.5f, ty = uv[1] * (float)h - 0.5f;
+    float bx, by;
+    float fx = modff(tx, &bx), fy = modff(ty, &by);
+    int32_t sx = (int32_t)bx, sy = (int32_t)by;
+    if(fx < 0.0f) { sx -= 1; fx = fabsf(fx); }
+    if(fy < 0.0f) { sy -= 1; fy = fabsf(fy); }
+    int32_t x0 = wrap_index(sx, (int32_t)w), x1 = wrap_index(sx + 1, (int32_t)w);
+    int32_t y0 = wrap_index(sy, (int32_t)h), y1 = wrap_index(sy + 1, (int32_t)h);
+    float gx = 1.0f - fx, gy = 1.0f - fy;
+    idx[0] = (size_t)y0 * w + x0; wt[0] = gx * gy;
+    idx[1] = (size_t)y0 * w + x1; wt[1] = fx * gy;
+    idx[2] = (size_t)y1 * w + x0; wt[2] = gx * fy;
+    idx[3] = (size_t)y1 * w + x1; wt[3] = fx * fy;
+}
+
+static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, float outRad[3], adj_ctx* adj);
+
 static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, float outRad[3])
+{
+    trace_sample_adj(J, x, y, sample, outRad, NULL);
+}
+
+static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, float outRad[3], adj_ctx* adj)
 {
     const orc_pt_params* P = J->p;
     const uint32_t pixel = y * P->width + x;
@@ -777,7 +851,31 @@ static void trace_sample(pt_job* J, uint32_t x, uint32_t y, uint32_t sample, flo
         const float wo[3] = { -dir[0], -dir[1], -dir[2] };
         const float V[3] = { dot3f(wo, tng), dot3f(wo, btg), dot3f(wo, nrm) };
         float alb[4] = { sf->albedo[0], sf->albedo[1], sf->albedo[2], 0.0f };
-        if(S) orc_spec_convert_albedo(S, sf->albedo, waves, alb);
+        if(sf->texels)
+        {
+            /* GenerateSurface (PrimitiveDefaultTriangle.hpp:472-476):
+             * uv = uv0 a + uv1 b + uv2 c, a = hit[0], b = hit[1], c = 1 - a - b */
+            const float* q = &sf->uvs[6 * localPrim];
+            float a = mh.bary[0], b = mh.bary[1], c = 1.0f - a - b;
+            float uv[2];
+            for(int k = 0; k < 2; k++) uv[k] = q[k] * a + q[2 + k] * b + q[4 + k] * c;
+            orc_tex_read(sf->texels, sf->texW, sf->texH, sf->texFormat, uv, alb);
+        }
+        if(S) { float c3[3] = { alb[0], alb[1], alb[2] }; orc_spec_convert_albedo(S, c3, waves, alb); }
+        if(adj && sf->texels == J->adjTexels && sf->matType == ORC_MAT_LAMBERT)
+        {
+            const float* q = &sf->uvs[6 * localPrim];
+            float a = mh.bary[0], b = mh.bary[1], c = 1.0f - a - b;
+            float uv[2];
+            for(int k = 0; k < 2; k++) uv[k] = q[k] * a + q[2 + k] * b + q[4 + k] * c;
+            size_t ti[4]; float tw[4];
+            tex_taps(J->adjW, J->adjH, uv, ti, tw);
+            for(int k = 0; k < 3; k++)
+            {
+                float g = (alb[k] > 0.0f) ? adj->d[k] * ((adj->tot[k] - rad[k]) / alb[k]) : 0.0f;
+                for(int j = 0; j < 4; j++) adj->grad[4 * ti[j] + k] += (double)(g * tw[j]);
+            }
+        }
         const int isSpec = specularity(sf, alb, nc) >= SPECULAR_THRESHOLD;
 
         /* ---- NEE (WorkFunctionNEE); no shadow ray for specular materials ---- */
@@ -1002,6 +1100,65 @@ static void* pt_worker(void* arg)
         }
     }
     return NULL;
+}
+
+static void* pt_adj_worker(void* arg)
+{
+    pt_job* J = (pt_job*)arg;
+    const orc_pt_params* P = J->p;
+    int b = atomic_fetch_add(&J->adjNextBuffer, 1);
+    double* grad = J->adjGrad + (size_t)b * 4 * J->adjW * J->adjH;
+    const float invSpp = 1.0f / (float)P->spp;
+    for(;;)
+    {
+        uint32_t y = atomic_fetch_add(&J->nextRow, 1u);
+        if(y >= P->height) break;
+        for(uint32_t x = 0; x < P->width; x++)
+        {
+            const float* d = &J->adjDelta[4ull * (y * P->width + x)];
+            for(uint32_t s = 0; s < P->spp; s++)
+            {
+                adj_ctx A;
+                trace_sample(J, x, y, P->sampleStart + s, A.tot);
+                for(int k = 0; k < 3; k++) A.d[k] = d[k] * invSpp;
+                A.grad = grad;
+                float r[3];
+                trace_sample_adj(J, x, y, P->sampleStart + s, r, &A);
+            }
+        }
+    }
+    return NULL;
+}
+
+int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
+                   const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
+                   const void* texels, uint32_t texW, uint32_t texH, const float* delta,
+                   double* grad, int nthreads)
+{
+    if(!s || !p || !surfaces || !texels || !delta || !grad) return -1;
+    if(nthreads < 1) nthreads = 1;
+    if(nthreads > 64) nthreads = 64;
+    const size_t n = 4ull * texW * texH;
+    double* bufs = (double*)calloc((size_t)nthreads * n, sizeof(double));
+    if(!bufs) return -2;
+    pt_job J;
+    memset(&J, 0, sizeof(J));
+    J.scene = s; J.p = p; J.surfaces = surfaces; J.lights = lights; J.nLights = nLights;
+    J.env = env;
+    J.adjTexels = texels; J.adjW = texW; J.adjH = texH; J.adjDelta = delta; J.adjGrad = bufs;
+    J.adjWorkers = nthreads;
+    atomic_init(&J.nextRow, 0u);
+    atomic_init(&J.adjNextBuffer, 0);
+    pthread_t th[64];
+    int started = 0;
+    for(int t = 1; t < nthreads; t++)
+        if(pthread_create(&th[started], NULL, pt_adj_worker, &J) == 0) started++;
+    pt_adj_worker(&J);
+    for(int t = 0; t < started; t++) pthread_join(th[t], NULL);
+    for(int t = 0; t <= started; t++)
+        for(size_t i = 0; i < n; i++) grad[i] += bufs[(size_t)t * n + i];
+    free(bufs);
+    return 0;
 }
 
 int orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,

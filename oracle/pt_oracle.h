@@ -51,7 +51,17 @@ typedef struct
     const float* triangles;
     float        m[12];
     float        inv[12];
+    /* albedo texture (replaces albedo[] when texels != NULL): RGBA, format
+     * 0 = UNORM8, 1 = f32; bilinear, wrap addressed, single level; the
+     * surface's uvs hold 6 floats (uv0 uv1 uv2) per local primitive */
+    const void*  texels;
+    uint32_t     texW, texH, texFormat;
+    const float* uvs;
 } orc_pt_surface;
+
+/* Bilinear, wrap-addressed albedo read (TextureViewCPU.h:196-375, UNORM8
+ * channels through NormConversion::FromUNorm). */
+void orc_tex_read(const void* texels, uint32_t w, uint32_t h, uint32_t format, const float uv[2], float rgb[3]);
 
 typedef struct
 {
@@ -108,6 +118,17 @@ void orc_spec_to_rgb(const orc_spectral* S, const float value[4], const float wa
 int  orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
                    const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
                    const orc_spectral* spectral, float* image, int nthreads);
+
+/* Path-replay adjoint (project-written reference; MRay has no adjoint):
+ * for every pixel sample, the path is traced twice with the same random
+ * numbers; the replay adds, at each Lambert vertex whose albedo is the texture
+ * `texels`, delta[pixel] / spp * (primal radiance - radiance before the
+ * vertex) / albedo, times each bilinear tap's weight, into grad (double RGBA
+ * per texel, accumulated in FP64).  RGB mode. */
+int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
+                   const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
+                   const void* texels, uint32_t texW, uint32_t texH, const float* delta,
+                   double* grad, int nthreads);
 
 /* Piecewise-constant 2D distribution (Source/Tracer/Distributions.h/.cu). */
 void  orc_pwc2d_build(const float* func, uint32_t w, uint32_t h, float* cdfX, float* cdfY);

@@ -196,3 +196,45 @@ def test_spectral_per_pixel(scene, mode):
     g2, o2, frac2 = _compare(pt, S2, mode)
     assert frac2 >= 0.97
     pt.close()
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_textured_box_per_pixel(mode):
+    """RGBA8 noise albedo textures (bilinear, wrap, uv repeats) on three walls."""
+    surf = scenes.box_scene_textured(0, size=128)
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    g, o, frac = _compare(pt, oracle.PtScene(surf), mode)
+    print("textured mode %d: close %.4f relMSE %.3g" % (mode, frac, relmse(g, o)))
+    assert frac >= 0.97 and relmse(g, o) <= 1e-3
+    pt.close()
+
+
+def test_borrowed_float_texture_updates():
+    """A borrowed f32 device texture: rewriting it changes the next render
+    exactly as the oracle with the new texels."""
+    import torch
+    surf = scenes.box_scene(0)
+    tex = scenes.value_noise_texture(32, seed=5, dtype=np.float32)
+    surf[2]["uv"] = scenes.quad_uv()
+    surf[2]["texture"] = tex
+    pt = PathTracer(0)
+    for k, s in enumerate(surf):
+        inst = pt.add_surface(s["pos"], s["idx"], s["m34"], uv=s.get("uv"))
+        if s["kind"] == "light":
+            pt.set_area_light(inst, s["radiance"])
+        else:
+            pt.set_lambert(inst, s["albedo"])
+    dev = torch.from_numpy(tex.copy()).cuda()
+    tid = pt.add_texture(dev)
+    pt.set_albedo_texture(2, tid)
+    pt.build()
+    g1, o1, f1 = _compare(pt, oracle.PtScene(surf), 2, spp=4)
+    assert f1 >= 0.97
+    tex2 = np.ascontiguousarray(tex[::-1])
+    dev.copy_(torch.from_numpy(tex2))
+    torch.cuda.synchronize()
+    surf[2]["texture"] = tex2
+    g2, o2, f2 = _compare(pt, oracle.PtScene(surf), 2, spp=4)
+    assert f2 >= 0.97 and not np.allclose(g1, g2)
+    pt.close()
