@@ -270,6 +270,9 @@ def gpu_arm(args):
                   "blas_nodes": st["blasNodes"]},
     }
     line["extra"].update(box_scene_pt(args, dev))
+    if not args.no_pt_extras:
+        line["extra"].update(c2_scene_pt(args, dev))
+        line["extra"].update(c3_adjoint(args, dev))
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, idx, m, rays_np, budget_s=args.cpu_seconds)
     if ws > 1:
@@ -305,6 +308,85 @@ def box_scene_pt(args, dev):
     return {"box_pt_ms_per_16spp": round(ms, 3),
             "box_pt_spp_per_s": round(16.0 / (ms * 1e-3), 1),
             "box_pt_mpaths_per_s": round(256 * 256 * 16 / (ms * 1e-3) / 1e6, 1)}
+
+
+def _spectral_inputs():
+    from mray_gb300 import spectral
+    gold = os.path.join(ROOT, "tests", "golden")
+    res, lut = spectral.read_mrspectra(os.path.join(gold, "REC_709_r32.mrspectra"))
+    return res, lut, spectral.load_tables(os.path.join(gold, "spectral_rec709.npz"))
+
+
+def c2_scene_pt(args, dev):
+    """Spectral production scene (199,778 triangles, 509 surfaces, textured
+    Lambert / GGX metal / glass, 8 area lights + a 1024x512 sky): 1920x1080,
+    4 wavelengths per path, depth 12, RR from 3, NEE + MIS; samples per
+    second (the configuration's 64 spp frame is timed in 4-spp steps)."""
+    import torch
+    from mray_gb300.pt import PathTracer, load_box_scene
+    from mray_gb300 import scenes
+    surf, cam = scenes.c2_scene(0)
+    pt = PathTracer(dev.index or 0)
+    load_box_scene(pt, surf)
+    pt.set_env(scenes.sky_map(1024, 512, seed=0))
+    pt.set_spectral(*_spectral_inputs())
+    spp = 4
+    p = PathTracer.params(1920, 1080, spp, cam, max_depth=12, rr_start=3, seed=0)
+    img = pt.render(p)
+    torch.cuda.synchronize(dev)
+    reps = max(3, min(args.steps // 20, 16))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for r in range(reps):
+        p.sampleStart = spp * (r + 1)
+        pt.render(p, image=img)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    pt.close()
+    return {"c2_ms_per_4spp_1080p": round(ms, 2), "c2_spp_per_s_1080p": round(spp / (ms * 1e-3), 1),
+            "c2_mpaths_per_s": round(1920 * 1080 * spp / (ms * 1e-3) / 1e6, 1),
+            "c2_ms_per_64spp_frame": round(ms * 16, 1)}
+
+
+def c3_adjoint(args, dev):
+    """Differentiable workload: box + 65,024-triangle textured sphere, 512^2
+    f32 albedo texture, 512^2 image, 32 spp, depth 6; one primal render plus
+    one path-replay adjoint (primal + replay) per step."""
+    import torch
+    from mray_gb300.pt import PathTracer
+    from mray_gb300 import scenes
+    tex = torch.from_numpy(scenes.value_noise_texture(512, seed=0, dtype=np.float32)).to(dev)
+    surf = scenes.adjoint_scene(None)
+    pt = PathTracer(dev.index or 0)
+    for s in surf:
+        inst = pt.add_surface(s["pos"], s["idx"], s["m34"], cull=s.get("cull", True), uv=s.get("uv"))
+        if s["kind"] == "light":
+            pt.set_area_light(inst, s["radiance"])
+        else:
+            pt.set_lambert(inst, s["albedo"])
+        if "uv" in s:
+            sphere = inst
+    tid = pt.add_texture(tex)
+    pt.set_albedo_texture(sphere, tid)
+    pt.build()
+    p = PathTracer.params(512, 512, 32, scenes.box_camera(), max_depth=6, rr_start=6, seed=0)
+    delta = torch.full((512, 512, 4), 1e-6, dtype=torch.float32, device=dev)
+    grad = torch.zeros((512, 512, 4), dtype=torch.float32, device=dev)
+    pt.adjoint(p, tid, delta, grad=grad)
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record()
+    for _ in range(reps):
+        pt.adjoint(p, tid, delta, grad=grad)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    pt.close()
+    return {"c3_adjoint_ms_512sq_32spp": round(ms, 2)}
 
 
 def oracle_scene(pos, idx, m):
@@ -394,6 +476,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-pt-extras", action="store_true",
+                    help="skip the production-scene and adjoint path-tracing lines")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

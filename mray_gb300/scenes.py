@@ -305,6 +305,71 @@ def adjoint_scene(texture, seed=0, n_theta=128, n_phi=256, noise=0.03):
     return s
 
 
+def c2_scene(seed=0, texture_size=2048, sphere_level=2, spheres=500, ground_quads=141):
+    """The spectral production workload: a displaced ground grid (2 x 141^2 =
+    39,762 triangles) and 500 level-2 icospheres (320 triangles each) --
+    199,762 triangles; half the spheres and the ground Lambert with seeded
+    RGBA8 noise textures (texture_size^2, two textures), a quarter GGX metal
+    (Unreal, metallic 1, roughness ~ U[0.05, 0.5]), a quarter glass (Refract,
+    IoR 1.5); 8 quad area lights.  Returns (surfaces, camera); pair it with
+    sky_map(1024, 512) as the skysphere."""
+    rng = np.random.default_rng(seed)
+    tex = [value_noise_texture(texture_size, seed + 17 + k) for k in range(2)]
+    out = []
+    # ground
+    n = ground_quads
+    g = np.linspace(-20.0, 20.0, n + 1)
+    X, Z = np.meshgrid(g, g, indexing="ij")
+    Y = 0.25 * np.sin(X * 0.45 + 0.3) * np.cos(Z * 0.37 - 0.2) + 0.08 * np.sin(X * 1.9) * np.sin(Z * 2.3)
+    pos = np.stack([X, Y, Z], -1).reshape(-1, 3).astype(np.float32)
+    uv = np.stack([X / 8.0, Z / 8.0], -1).reshape(-1, 2).astype(np.float32)
+    W = n + 1
+    ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    a = (ii * W + jj).ravel()
+    idx = np.concatenate([np.stack([a, a + 1, a + W + 1], 1), np.stack([a, a + W + 1, a + W], 1)]).astype(np.uint32)
+    I34 = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
+    out.append(dict(pos=pos, idx=idx, uv=uv, m34=I34.copy(), kind="lambert", albedo=[0.5, 0.5, 0.5],
+                    texture=tex[0]))
+    # spheres
+    sp, si = icosphere(sphere_level, 1.0)
+    d = sp / np.linalg.norm(sp, axis=1, keepdims=True)
+    suv = np.stack([np.arctan2(d[:, 2], d[:, 0]) / (2 * np.pi) + 0.5, np.arccos(np.clip(d[:, 1], -1, 1)) / np.pi],
+                   1).astype(np.float32)
+    side = int(np.ceil(np.sqrt(spheres)))
+    cells = np.linspace(-18.0, 18.0, side)
+    k = 0
+    for ix in range(side):
+        for iz in range(side):
+            if k == spheres:
+                break
+            r = 0.35 + 0.5 * rng.random()
+            x = cells[ix] + (rng.random() - 0.5) * 0.6
+            z = cells[iz] + (rng.random() - 0.5) * 0.6
+            m = np.array([r, 0, 0, x, 0, r, 0, r + 0.35, 0, 0, r, z], np.float32)
+            kind = k % 4
+            srf = dict(pos=sp, idx=si, m34=m, kind="lambert", albedo=[0.5, 0.5, 0.5])
+            if kind in (0, 1):
+                srf.update(uv=suv, texture=tex[k % 2])
+            elif kind == 2:
+                srf.update(material="unreal", metallic=1.0, roughness=float(0.05 + 0.45 * rng.random()),
+                           specular=0.5, albedo=[float(0.6 + 0.35 * rng.random()) for _ in range(3)])
+            else:
+                srf.update(material="refract", ior=(1.0, 1.5), cull=False)
+            out.append(srf)
+            k += 1
+    # lights
+    for l in range(8):
+        x = -15.0 + 30.0 * (l % 4) / 3.0
+        z = -8.0 + 16.0 * (l // 4)
+        p, i = _quad((x - 0.75, 9.0, z - 0.75), (1.5, 0, 0), (0, 0, 1.5))
+        out.append(dict(pos=p.astype(np.float32), idx=i, m34=I34.copy(), kind="light",
+                        radiance=[40.0, 38.0, 34.0]))
+    f = 50.0 * np.pi / 180.0
+    cam = dict(pos=(0.0, 7.0, -26.0), gaze=(0.0, 0.5, 0.0), up=(0.0, 1.0, 0.0), fov=(f, f * 9.0 / 16.0),
+               near_far=(0.05, 500.0))
+    return out, cam
+
+
 def box_camera():
     """Pinhole camera of the box scene (position, gaze point, up, fov radians, near/far)."""
     f = 40.0 * np.pi / 180.0

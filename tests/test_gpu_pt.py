@@ -238,3 +238,21 @@ def test_borrowed_float_texture_updates():
     g2, o2, f2 = _compare(pt, oracle.PtScene(surf), 2, spp=4)
     assert f2 >= 0.97 and not np.allclose(g1, g2)
     pt.close()
+
+
+def test_c2_scene_spectral_small():
+    """The production scene (textured Lambert, GGX metal, glass, 8 area
+    lights, sky, 4 wavelengths) at a small film against the oracle."""
+    import os
+    surf, cam = scenes.c2_scene(0, texture_size=256)
+    env = dict(texels=scenes.sky_map(128, 64, seed=0))
+    pt, S = _spectral_pair(surf, env)
+    g = _img(pt.render(PathTracer.params(96, 54, 4, cam, max_depth=12, rr_start=3, seed=2)))
+    o = _img(S.render(S.params(96, 54, 4, cam, max_depth=12, rr_start=3, seed=2)))
+    close = (np.abs(g - o) <= 1e-4 * (1.0 + np.abs(o))).all(axis=-1).mean()
+    d = np.abs(g - o).max(axis=-1).ravel()
+    keep = d <= np.quantile(d, 0.98)
+    rel_kept = float(np.mean(((g - o).reshape(-1, 3)[keep]) ** 2 / (o.reshape(-1, 3)[keep] ** 2 + 1e-2)))
+    print("c2 spectral: close %.4f relMSE %.3g kept %.3g" % (close, relmse(g, o), rel_kept))
+    assert close >= 0.95 and rel_kept <= 1e-5
+    pt.close()
