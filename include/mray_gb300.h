@@ -297,6 +297,44 @@ mrg_status mrg_pt_set_albedo_texture(mrg_ctx* ctx, uint32_t instance_id, uint32_
 mrg_status mrg_pt_adjoint(mrg_ctx* ctx, const mrg_pt_params* params, uint32_t texture_id,
                           const float* d_image_adjoint, float* d_grad, float* d_image, void* stream);
 
+/* ---- Radiance cache (no reference counterpart) ----------------------------- */
+/* A multiresolution hash grid (levels x 2 features x 2^log2_table_size fp16
+ * entries per level, resolutions base..max geometrically) feeding a fully
+ * fused MLP of 5 layers, 64 wide, ReLU, BF16 tensor cores with FP32
+ * accumulation (4 x 64x64 + 16x64 weights, no biases), trained online with
+ * Adam on a relative L2 loss.  One cache per context.
+ * Per sample 16 floats: position xyz, roughness | outgoing direction xyz, 0 |
+ * normal xyz, 0 | albedo rgb, 0; positions are normalised to aabb.  Outputs
+ * 4 floats: predicted outgoing radiance rgb, 0. */
+typedef struct mrg_cache_params
+{
+    uint32_t levels;            /* 16 */
+    uint32_t log2_table_size;   /* 19 */
+    uint32_t base_resolution;   /* 16 */
+    uint32_t max_resolution;    /* 2048 */
+    float    learning_rate;     /* 1e-2 */
+    float    beta1, beta2, epsilon;
+    uint32_t seed;              /* initial weights */
+    uint32_t max_batch;         /* training samples per step, <= 2^20 */
+    float    aabb[6];           /* min xyz, max xyz */
+} mrg_cache_params;
+mrg_status mrg_cache_create(mrg_ctx* ctx, const mrg_cache_params* params);
+mrg_status mrg_cache_query(mrg_ctx* ctx, const float* d_inputs, uint32_t n, float* d_out, void* stream);
+/* One Adam step on n <= max_batch samples (targets: 4 floats each, rgb used).
+ * h_loss (optional) receives the batch's mean relative L2 loss and makes the
+ * call synchronous. */
+mrg_status mrg_cache_train(mrg_ctx* ctx, const float* d_inputs, const float* d_targets, uint32_t n,
+                           float* h_loss, void* stream);
+/* Parameters as fp32 host arrays: 17,408 MLP weights (W0..W3 [64][64] then
+ * W4 [16][64], row-major out x in) and levels * 2^log2_table_size * 2 table
+ * features; either pointer may be NULL. */
+mrg_status mrg_cache_get_params(mrg_ctx* ctx, float* h_weights, float* h_table);
+/* The loss gradients of one batch, without an optimiser step (layouts as
+ * mrg_cache_get_params; a gradient check). Synchronous. */
+mrg_status mrg_cache_gradients(mrg_ctx* ctx, const float* d_inputs, const float* d_targets, uint32_t n,
+                               float* h_grad_weights, float* h_grad_table, float* h_loss);
+mrg_status mrg_cache_set_params(mrg_ctx* ctx, const float* h_weights, const float* h_table);
+
 /* Skysphere boundary light (LightGroupSkysphere<SphericalCoordConverter>,
  * Source/Tracer/LightsDefault.hpp:300-420, 700-915): a lat-long radiance map
  * of width x height RGBA f32 texels (row-major, row 0 at v = 0; 1 x 1 = a

@@ -32,6 +32,8 @@ EXPORTED = [
     "mrg_pt_set_lambert", "mrg_pt_set_area_light", "mrg_pt_camera_frame", "mrg_pt_render",
     "mrg_pt_set_material", "mrg_pt_set_env", "mrg_multi_partition", "mrg_pt_set_spectral",
     "mrg_upload_mesh_uv", "mrg_pt_add_texture", "mrg_pt_set_albedo_texture", "mrg_pt_adjoint",
+    "mrg_cache_create", "mrg_cache_query", "mrg_cache_train", "mrg_cache_get_params", "mrg_cache_set_params",
+    "mrg_cache_gradients",
 ]
 
 MRG_MAT_LAMBERT, MRG_MAT_REFLECT, MRG_MAT_REFRACT, MRG_MAT_UNREAL = 0, 1, 2, 3
@@ -57,6 +59,13 @@ class MrgPtParams(C.Structure):
 
 #: capacity of mrg_cast_closest_host_noalloc (rays per call)
 MRG_NOALLOC_MAX_RAYS = 262144
+
+
+class MrgCacheParams(C.Structure):
+    _fields_ = [("levels", C.c_uint32), ("log2_table_size", C.c_uint32), ("base_resolution", C.c_uint32),
+                ("max_resolution", C.c_uint32), ("learning_rate", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("epsilon", C.c_float), ("seed", C.c_uint32), ("max_batch", C.c_uint32),
+                ("aabb", C.c_float * 6)]
 
 
 class MrgParams(C.Structure):
@@ -110,6 +119,12 @@ def _declare(lib):
         "mrg_pt_add_texture": (C.c_int, [vp, u32, u32, u32, vp, u32, C.POINTER(u32)]),
         "mrg_pt_set_albedo_texture": (C.c_int, [vp, u32, u32]),
         "mrg_pt_adjoint": (C.c_int, [vp, C.POINTER(MrgPtParams), u32, vp, vp, vp, vp]),
+        "mrg_cache_create": (C.c_int, [vp, C.POINTER(MrgCacheParams)]),
+        "mrg_cache_query": (C.c_int, [vp, vp, u32, vp, vp]),
+        "mrg_cache_train": (C.c_int, [vp, vp, vp, u32, fp, vp]),
+        "mrg_cache_get_params": (C.c_int, [vp, fp, fp]),
+        "mrg_cache_set_params": (C.c_int, [vp, fp, fp]),
+        "mrg_cache_gradients": (C.c_int, [vp, vp, vp, u32, fp, fp, fp]),
         "mrg_multi_partition": (C.c_int, [vp, vp, vp, u32, vp, vp, u32, vp, vp, vp, vp, vp, u32, vp]),
         "mrg_pt_camera_frame": (C.c_int, [C.POINTER(MrgPtParams), fp]),
         "mrg_pt_render": (C.c_int, [vp, C.POINTER(MrgPtParams), vp, vp]),

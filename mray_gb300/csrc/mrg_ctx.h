@@ -5,6 +5,7 @@
 #include "mrg_build.h"
 #include "mrg_pt.h"
 #include "mrg_partition.h"
+#include "mrg_nrc.h"
 
 #include <cuda_runtime.h>
 
@@ -112,6 +113,11 @@ struct mrg_ctx
     // spectral context: device block [lut | observer | illuminant]
     void*              dPtSpec = nullptr;
     mrg::PtSpectral    ptSpec{};
+
+    // radiance cache (one per context)
+    bool               cacheOn = false;
+    mrg::NrcState      cache{};
+    std::vector<void*> cacheAllocs;
 
     // ray partitioner scratch (grow-only)
     uint32_t* dPartScratch = nullptr;

@@ -1,0 +1,100 @@
+"""Radiance cache on the GPU against the FP64 reference (oracle/nrc.py):
+hash-grid encoding + BF16 tensor-core MLP inference, the loss gradients of
+every weight and table entry, and online training on a synthetic field."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import nrc
+from mray_gb300.cache import RadianceCache
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(n, seed):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, 16), np.float32)
+    x[:, 0:3] = rng.random((n, 3)) * 4.0 - 2.0          # inside the aabb below
+    x[:, 3] = rng.random(n)
+    d = rng.standard_normal((n, 3))
+    x[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    nn = rng.standard_normal((n, 3))
+    x[:, 8:11] = nn / np.linalg.norm(nn, axis=1, keepdims=True)
+    x[:, 12:15] = rng.random((n, 3))
+    return x
+
+
+AABB = (-2.0, -2.0, -2.0, 2.0, 2.0, 2.0)
+
+
+def _cache(levels=16, log2=19):
+    return RadianceCache(levels=levels, log2_table_size=log2, aabb=AABB, max_batch=65536, seed=3)
+
+
+def _random_params(cache, seed):
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(-0.25, 0.25, nrc.WIDTH * nrc.WIDTH * 4 + nrc.OUT * nrc.WIDTH).astype(np.float32)
+    # fp16-representable table values (the GPU reads the fp16 copy)
+    t = rng.uniform(-0.6, 0.6, cache.table_size).astype(np.float16).astype(np.float32)
+    cache.set_params(w, t)
+    return w, t
+
+
+@pytest.mark.parametrize("levels,log2", [(16, 19), (8, 12)])
+def test_query_matches_reference(levels, log2):
+    c = _cache(levels, log2)
+    w, t = _random_params(c, 1)
+    x = _batch(5000, 2)
+    got = c.query(torch.from_numpy(x).cuda()).cpu().numpy()[:, :3]
+    ref = nrc.CacheRef(levels, log2, 16, 2048, AABB)
+    want = ref.query(x, w, t, bf16=True)
+    err = np.abs(got - want).max() / np.abs(want).max()
+    print("query: max |gpu - ref| / max |ref| = %.3g" % err)
+    assert err <= 2e-2
+    assert np.corrcoef(got.ravel(), want.ravel())[0, 1] > 0.9999
+    c.close()
+
+
+def test_gradients_match_reference():
+    c = _cache(16, 19)
+    w, t = _random_params(c, 4)
+    x = _batch(4096, 5)
+    tgt = np.zeros((4096, 4), np.float32)
+    tgt[:, :3] = np.random.default_rng(6).random((4096, 3)) * 2.0
+    loss, gw, gt = c.gradients(torch.from_numpy(x).cuda(), torch.from_numpy(tgt).cuda())
+    ref = nrc.CacheRef(16, 19, 16, 2048, AABB)
+    lref, gwr, gtr = ref.gradients(x, tgt, w, t, bf16=True)
+    assert abs(loss - lref) <= 1e-2 * abs(lref)
+    ew = np.linalg.norm(gw - gwr) / np.linalg.norm(gwr)
+    et = np.linalg.norm(gt - gtr) / np.linalg.norm(gtr)
+    print("gradients: relative L2 error weights %.3g, table %.3g" % (ew, et))
+    assert ew <= 3e-2 and et <= 3e-2
+    c.close()
+
+
+def test_training_fits_a_radiance_field():
+    """Online training on a smooth synthetic radiance field: the relative L2
+    loss falls by at least 10x within 300 Adam steps."""
+    c = _cache(16, 19)
+    rng = np.random.default_rng(7)
+
+    def field(x):
+        p, d = x[:, 0:3], x[:, 4:7]
+        r = np.stack([0.5 + 0.4 * np.sin(2 * p[:, 0]) * np.cos(p[:, 1]),
+                      0.6 + 0.3 * d[:, 1],
+                      0.3 + 0.25 * np.cos(3 * p[:, 2] + d[:, 0])], 1)
+        t = np.zeros((x.shape[0], 4), np.float32)
+        t[:, :3] = r
+        return t
+    first = last = None
+    for step in range(300):
+        x = _batch(16384, 100 + step)
+        l = c.train(torch.from_numpy(x).cuda(), torch.from_numpy(field(x)).cuda())
+        first = l if first is None else first
+        last = l
+    xv = _batch(4096, 9999)
+    pred = c.query(torch.from_numpy(xv).cuda()).cpu().numpy()[:, :3]
+    rel = np.mean((pred - field(xv)[:, :3]) ** 2 / (field(xv)[:, :3] ** 2 + 0.01))
+    print("training: loss %.4g -> %.4g, held-out relMSE %.4g" % (first, last, rel))
+    assert last <= first / 10.0 and rel <= 0.05
+    c.close()
