@@ -273,6 +273,7 @@ def gpu_arm(args):
     if not args.no_pt_extras:
         line["extra"].update(c2_scene_pt(args, dev))
         line["extra"].update(c3_adjoint(args, dev))
+        line["extra"].update(c4_equal_time(args, dev))
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, idx, m, rays_np, budget_s=args.cpu_seconds)
     if ws > 1:
@@ -387,6 +388,64 @@ def c3_adjoint(args, dev):
     ms = e0.elapsed_time(e1) / reps
     pt.close()
     return {"c3_adjoint_ms_512sq_32spp": round(ms, 2)}
+
+
+def c4_equal_time(args, dev):
+    """Radiance cache on the production scene (RGB, 480x270, depth 12):
+    relMSE against a 4096-spp plain render, for plain path tracing at 16 spp
+    and for cache-assisted frames (1 spp + one training step on 32,768
+    training paths each) in the same time, after 64 warm-up frames."""
+    import torch
+    from mray_gb300.pt import PathTracer, load_box_scene
+    from mray_gb300.cache import RadianceCache
+    from mray_gb300 import scenes
+    surf, cam = scenes.c2_scene(0)
+    pt = PathTracer(dev.index or 0)
+    load_box_scene(pt, surf)
+    pt.set_env(scenes.sky_map(1024, 512, seed=0))
+    cache = RadianceCache(owner=pt, aabb=tuple(float(v) for v in pt.acc.scene_aabb()), max_batch=65536)
+    w, h = 480, 270
+
+    def P(spp, seed, start=0, spp_pass=0):
+        return PathTracer.params(w, h, spp, cam, max_depth=12, rr_start=3, seed=seed, sample_start=start,
+                                 samples_per_pass=spp_pass)
+
+    ref = pt.render(P(4096, 1, spp_pass=64))
+    ref = (ref[..., :3] / ref[..., 3:]).double()
+
+    def relmse(img):
+        im = (img[..., :3] / img[..., 3:]).double()
+        return float(torch.mean((im - ref) ** 2 / (ref ** 2 + 1e-2)))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pt.render(P(16, 7))
+    torch.cuda.synchronize(dev)
+    e0.record()
+    plain = pt.render(P(16, 2))
+    e1.record()
+    torch.cuda.synchronize(dev)
+    t_plain = e0.elapsed_time(e1)
+    for f in range(64):
+        pt.render_cached(P(1, 100 + f, start=f), train_paths=32768)
+    torch.cuda.synchronize(dev)
+    e0.record()
+    pt.render_cached(P(1, 300, start=0), train_paths=32768)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    t_frame = e0.elapsed_time(e1)
+    frames = max(1, int(t_plain // t_frame))
+    img = None
+    e0.record()
+    for f in range(frames):
+        img, _ = pt.render_cached(P(1, 1000 + f, start=f), image=img, train_paths=32768)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    t_cached = e0.elapsed_time(e1)
+    out = {"c4_plain_16spp_ms": round(t_plain, 2), "c4_plain_relmse": round(relmse(plain), 5),
+           "c4_cached_frame_ms": round(t_frame, 3), "c4_cached_frames": frames,
+           "c4_cached_ms": round(t_cached, 2), "c4_cached_relmse": round(relmse(img), 5),
+           "c4_workload": "production scene RGB 480x270 depth 12, reference 4096 spp plain"}
+    pt.close()
+    return out
 
 
 def oracle_scene(pos, idx, m):

@@ -335,6 +335,16 @@ mrg_status mrg_cache_gradients(mrg_ctx* ctx, const float* d_inputs, const float*
                                float* h_grad_weights, float* h_grad_table, float* h_loss);
 mrg_status mrg_cache_set_params(mrg_ctx* ctx, const float* h_weights, const float* h_table);
 
+/* One frame of cache-assisted path tracing (RGB): train_paths training paths
+ * from hashed pixels are traced to full depth and their vertices 1..2 give
+ * (inputs, outgoing radiance) samples for one mrg_cache_train step; then
+ * params->spp samples per pixel are rendered with every path ending at its
+ * second vertex on a cache query (Mueller et al. 2021), added to d_image as
+ * mrg_pt_render does.  train_paths = 0 skips training.  Needs
+ * mrg_cache_create with max_batch >= 2 * train_paths. */
+mrg_status mrg_pt_render_cached(mrg_ctx* ctx, const mrg_pt_params* params, float* d_image,
+                                uint32_t train_paths, float* h_loss, void* stream);
+
 /* Skysphere boundary light (LightGroupSkysphere<SphericalCoordConverter>,
  * Source/Tracer/LightsDefault.hpp:300-420, 700-915): a lat-long radiance map
  * of width x height RGBA f32 texels (row-major, row 0 at v = 0; 1 x 1 = a

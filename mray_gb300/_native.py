@@ -33,7 +33,7 @@ EXPORTED = [
     "mrg_pt_set_material", "mrg_pt_set_env", "mrg_multi_partition", "mrg_pt_set_spectral",
     "mrg_upload_mesh_uv", "mrg_pt_add_texture", "mrg_pt_set_albedo_texture", "mrg_pt_adjoint",
     "mrg_cache_create", "mrg_cache_query", "mrg_cache_train", "mrg_cache_get_params", "mrg_cache_set_params",
-    "mrg_cache_gradients",
+    "mrg_cache_gradients", "mrg_pt_render_cached",
 ]
 
 MRG_MAT_LAMBERT, MRG_MAT_REFLECT, MRG_MAT_REFRACT, MRG_MAT_UNREAL = 0, 1, 2, 3
@@ -125,6 +125,7 @@ def _declare(lib):
         "mrg_cache_get_params": (C.c_int, [vp, fp, fp]),
         "mrg_cache_set_params": (C.c_int, [vp, fp, fp]),
         "mrg_cache_gradients": (C.c_int, [vp, vp, vp, u32, fp, fp, fp]),
+        "mrg_pt_render_cached": (C.c_int, [vp, C.POINTER(MrgPtParams), vp, u32, fp, vp]),
         "mrg_multi_partition": (C.c_int, [vp, vp, vp, u32, vp, vp, u32, vp, vp, vp, vp, vp, u32, vp]),
         "mrg_pt_camera_frame": (C.c_int, [C.POINTER(MrgPtParams), fp]),
         "mrg_pt_render": (C.c_int, [vp, C.POINTER(MrgPtParams), vp, vp]),

@@ -131,6 +131,7 @@ mrg_status mrg_destroy(mrg_ctx* c)
     cudaFree(c->dPtTexTable); cudaFree(c->dPtTexData); cudaFree(c->dPtUvs); cudaFree(c->dPtRadTotal);
     cudaFree(c->dPtSpec);
     cudaFree(c->dPartScratch);
+    cudaFree(c->dPtCacheBuf);
     for(void* q : c->cacheAllocs) cudaFree(q);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);

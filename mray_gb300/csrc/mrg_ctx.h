@@ -114,7 +114,9 @@ struct mrg_ctx
     void*              dPtSpec = nullptr;
     mrg::PtSpectral    ptSpec{};
 
-    // radiance cache (one per context)
+    // radiance cache (one per context) and its path-tracer buffers
+    void*              dPtCacheBuf = nullptr;
+    size_t             ptCacheBufBytes = 0;
     bool               cacheOn = false;
     mrg::NrcState      cache{};
     std::vector<void*> cacheAllocs;

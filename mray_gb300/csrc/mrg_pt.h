@@ -88,6 +88,23 @@ struct PtAdjoint
     uint32_t      enabled;
 };
 
+// Radiance-cache use by the path tracer: mode 1 ends every path at its
+// second vertex with a cache query of the outgoing radiance there; mode 2
+// traces training paths (pixels drawn by hash) and records, at vertices
+// 1..recPerPath, the cache inputs, the throughput on arrival and the radiance
+// gathered before the vertex (targets follow from the path's final radiance).
+struct PtCacheUse
+{
+    uint32_t  mode;
+    uint32_t  recPerPath;
+    float4*   queryIn;        // 4 per slot
+    uint32_t* queryList;
+    uint32_t* queryCount;
+    float4*   queryOut;       // per slot
+    float4*   recIn;          // 4 per record (slot * recPerPath + vertex - 1)
+    float4*   recAux;         // 2 per record: throughput (w: 1 = valid), radiance before
+};
+
 struct PtCamera
 {
     float pos[3];
@@ -113,6 +130,7 @@ struct PtLaunch
     PtEnv    env;
     PtSpectral spec;
     PtAdjoint  adj;
+    PtCacheUse cache;
 };
 
 // Path state, structure of arrays (device).
@@ -164,6 +182,12 @@ cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSceneTabl
                           uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st);
 cudaError_t pt_work_keys(const PtPaths& P, const PtSurface* surfaces, uint32_t nSurfaces,
                          const uint32_t* aliveList, const uint32_t* aliveCount, int smCount, cudaStream_t st);
+// rad[slot] += thr[slot] * queryOut[slot] for the queried slots.
+cudaError_t pt_cache_apply(const PtPaths& P, const PtCacheUse& C, int smCount, cudaStream_t st);
+// Training batch from the records of a training pass: target = (final
+// radiance - radiance before) / throughput, valid records compacted.
+cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t paths, float4* batchIn,
+                             float4* batchTarget, uint32_t* batchCount, int smCount, cudaStream_t st);
 cudaError_t pt_resolve(const PtLaunch& L, const PtPaths& P, uint32_t depth, int smCount, cudaStream_t st);
 cudaError_t pt_film(const PtLaunch& L, const PtPaths& P, float4* image, cudaStream_t st);
 

@@ -564,9 +564,15 @@ __device__ __forceinline__ Chan radiance_of(const PtSpectral& S, float r, float 
     return chan(r, g, b, 0.0f);
 }
 
-__device__ __forceinline__ uint32_t slot_pixel(const PtLaunch& L, uint32_t i) { return i % (L.width * L.height); }
+__device__ __forceinline__ uint32_t slot_pixel(const PtLaunch& L, uint32_t i)
+{
+    // training paths start at hashed pixels
+    if(L.cache.mode == 2u) return pcg_hash(i * 0x9E3779B9u + L.sampleBase) % (L.width * L.height);
+    return i % (L.width * L.height);
+}
 __device__ __forceinline__ uint32_t slot_sample(const PtLaunch& L, uint32_t i)
 {
+    if(L.cache.mode == 2u) return L.sampleBase + i;
     return L.sampleBase + i / (L.width * L.height);
 }
 
@@ -746,7 +752,17 @@ __device__ void adjoint_vertex(const PtLaunch& L, const PtSceneTables& T, const 
             atomicAdd(&L.adj.grad[4 * (size_t)idx[j] + k], mul(g[k], w[j]));
 }
 
-template<bool SPEC, bool ADJ>
+// Cache inputs of a surface vertex: position, roughness | outgoing direction |
+// normal | albedo.
+__device__ __forceinline__ void cache_inputs(float4* dst, float3 pos, float rough, float3 wo, float3 nrm, float3 alb)
+{
+    dst[0] = make_float4(pos.x, pos.y, pos.z, rough);
+    dst[1] = make_float4(wo.x, wo.y, wo.z, 0.0f);
+    dst[2] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+    dst[3] = make_float4(alb.x, alb.y, alb.z, 0.0f);
+}
+
+template<bool SPEC, bool ADJ, int CM>
 __global__ void __launch_bounds__(kPtTPB)
 k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
         const uint32_t* __restrict__ aliveList, const uint32_t* __restrict__ aliveCount,
@@ -767,7 +783,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
     for(uint32_t base = first; base < n; base += stride)
     {
         const uint32_t idx = base + (threadIdx.x & 31u);
-        bool alive = false, shadow = false;
+        bool alive = false, shadow = false, query = false;
         uint32_t i = 0;
         if(idx < n)
         {
@@ -857,6 +873,23 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         adjoint_vertex(L, T, sf, i, gprim, mh, a3, rad);
                     const bool isSpec = specularity<NC>(sf, alb) >= kSpecularThreshold;
                     const uint32_t mt = sf.info.w;
+                    const float crough = (mt == kMatLambert) ? 1.0f : ((mt == kMatUnreal) ? sf.albedo.w : 0.0f);
+                    if(CM == 2 && depth >= 1u && depth <= L.cache.recPerPath)
+                    {
+                        const size_t rec = (size_t)i * L.cache.recPerPath + (depth - 1u);
+                        cache_inputs(L.cache.recIn + 4 * rec, pos, crough, wo, nrm, a3);
+                        L.cache.recAux[2 * rec] = make_float4(thr.v[0], thr.v[1], thr.v[2], 1.0f);
+                        L.cache.recAux[2 * rec + 1] = make_float4(rad.v[0], rad.v[1], rad.v[2], 0.0f);
+                    }
+                    const bool terminal = (CM == 1 && depth == 1u);
+                    if(terminal)
+                    {
+                        // the cache stands for the rest of the path
+                        cache_inputs(L.cache.queryIn + 4 * (size_t)i, pos, crough, wo, nrm, a3);
+                        query = true;
+                    }
+                    else
+                    {
                     // ---- NEE (WorkFunctionNEE); specular materials cast none ----
                     if(L.sampleMode != 0u && nAll > 0u && !isSpec && depth + 2u <= L.maxDepth)
                     {
@@ -1070,6 +1103,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         P.state[i] = depth | (type << 8);
                         alive = true;
                     }
+                    }   // not terminal
                 }
                 P.rad[i] = f4(rad);
             }
@@ -1094,6 +1128,60 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
         }
         warp_append(alive, i, nextList, nextCount);
         warp_append(shadow, i, P.shadowList, P.counts + 2);
+        if(CM == 1) warp_append(query, i, L.cache.queryList, L.cache.queryCount);
+    }
+}
+
+__global__ void __launch_bounds__(kPtTPB)
+k_cache_apply(PtPaths P, PtCacheUse C)
+{
+    const uint32_t n = *C.queryCount;
+    for(uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    {
+        const uint32_t i = C.queryList[k];
+        const float4 q = C.queryOut[i], t = P.thr[i];
+        float4 r = P.rad[i];
+        r.x = add(r.x, mul(t.x, fmaxf(q.x, 0.0f)));
+        r.y = add(r.y, mul(t.y, fmaxf(q.y, 0.0f)));
+        r.z = add(r.z, mul(t.z, fmaxf(q.z, 0.0f)));
+        P.rad[i] = r;
+    }
+}
+
+__global__ void __launch_bounds__(kPtTPB)
+k_cache_targets(PtPaths P, PtCacheUse C, uint32_t paths, float4* batchIn, float4* batchTarget, uint32_t* batchCount)
+{
+    const uint32_t total = paths * C.recPerPath;
+    const uint32_t first = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    for(uint32_t base = first; base < total; base += gridDim.x * blockDim.x)
+    {
+        const uint32_t r = base + (threadIdx.x & 31u);
+        bool ok = false;
+        float4 tgt = make_float4(0, 0, 0, 0);
+        if(r < total)
+        {
+            const float4 th = C.recAux[2 * (size_t)r], before = C.recAux[2 * (size_t)r + 1];
+            if(th.w != 0.0f && th.x > 0.0f && th.y > 0.0f && th.z > 0.0f)
+            {
+                const float4 tot = P.rad[r / C.recPerPath];
+                tgt = make_float4(__fdiv_rn(sub(tot.x, before.x), th.x), __fdiv_rn(sub(tot.y, before.y), th.y),
+                                  __fdiv_rn(sub(tot.z, before.z), th.z), 0.0f);
+                ok = isfinite(tgt.x) && isfinite(tgt.y) && isfinite(tgt.z);
+            }
+        }
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+        if(m == 0u) continue;
+        const uint32_t lane = threadIdx.x & 31u;
+        const int leader = __ffs(m) - 1;
+        uint32_t b = 0;
+        if((int)lane == leader) b = atomicAdd(batchCount, (uint32_t)__popc(m));
+        b = __shfl_sync(0xFFFFFFFFu, b, leader);
+        if(ok)
+        {
+            const uint32_t o = b + __popc(m & ((1u << lane) - 1u));
+            for(int j = 0; j < 4; j++) batchIn[4 * (size_t)o + j] = C.recIn[4 * (size_t)r + j];
+            batchTarget[o] = tgt;
+        }
     }
 }
 
@@ -1182,12 +1270,16 @@ cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSceneTabl
                           uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st)
 {
     const unsigned grid = (unsigned)smCount * 8u;
-    if(L.adj.enabled)
-        k_shade<false, true><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
+    if(L.cache.mode == 1u)
+        k_shade<false, false, 1><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
+    else if(L.cache.mode == 2u)
+        k_shade<false, false, 2><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
+    else if(L.adj.enabled)
+        k_shade<false, true, 0><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
     else if(L.spec.enabled)
-        k_shade<true, false><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
+        k_shade<true, false, 0><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
     else
-        k_shade<false, false><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
+        k_shade<false, false, 0><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
     return cudaGetLastError();
 }
 
@@ -1195,6 +1287,19 @@ cudaError_t pt_work_keys(const PtPaths& P, const PtSurface* surfaces, uint32_t n
                          const uint32_t* aliveList, const uint32_t* aliveCount, int smCount, cudaStream_t st)
 {
     k_work_keys<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, surfaces, nSurfaces, aliveList, aliveCount);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_cache_apply(const PtPaths& P, const PtCacheUse& C, int smCount, cudaStream_t st)
+{
+    k_cache_apply<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t paths, float4* batchIn,
+                             float4* batchTarget, uint32_t* batchCount, int smCount, cudaStream_t st)
+{
+    k_cache_targets<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C, paths, batchIn, batchTarget, batchCount);
     return cudaGetLastError();
 }
 

@@ -660,6 +660,88 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
     return MRG_OK;
 }
 
+mrg_status mrg_pt_render_cached(mrg_ctx* c, const mrg_pt_params* p, float* dImage, uint32_t trainPaths,
+                                float* hLoss, void* stream)
+{
+    if(!c || !p || !dImage) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render_cached: null pointer");
+    if(!c->cacheOn) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_pt_render_cached: call mrg_cache_create first");
+    if(c->ptSpec.enabled) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render_cached: RGB rendering only");
+    constexpr uint32_t kRec = 2;
+    if(2ull * trainPaths > c->cache.cap)
+        return mrg::set_error(MRG_ERR_LIMIT, "mrg_pt_render_cached: 2 * train_paths exceeds the cache's max_batch");
+    DevGuard g(c->device);
+    PtRun R;
+    mrg_status s = pt_setup(c, p, R, "mrg_pt_render_cached");
+    if(s != MRG_OK) return s;
+    if(trainPaths > R.slots && (s = pt_paths(c, trainPaths)) != MRG_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // buffers: query in / out / list (per slot), records and batch (per training record), counters
+    const size_t slots = R.slots, recs = (size_t)trainPaths * kRec;
+    const size_t sizes[8] = { slots * 64, slots * 16, slots * 4, recs * 64, recs * 32, recs * 64, recs * 16, 64 };
+    size_t need = 0;
+    for(size_t z : sizes) need += (z + 255) & ~size_t(255);
+    if(c->ptCacheBufBytes < need)
+    {
+        cudaFree(c->dPtCacheBuf);
+        c->dPtCacheBuf = nullptr;
+        c->ptCacheBufBytes = 0;
+        PT_TRY(cudaMalloc(&c->dPtCacheBuf, need), "mrg_pt_render_cached: buffers");
+        c->ptCacheBufBytes = need;
+    }
+    char* base = static_cast<char*>(c->dPtCacheBuf);
+    size_t off = 0;
+    int k = 0;
+    auto take = [&]() { char* q = base + off; off += (sizes[k++] + 255) & ~size_t(255); return q; };
+    mrg::PtCacheUse C{};
+    C.recPerPath = kRec;
+    C.queryIn = reinterpret_cast<float4*>(take());
+    C.queryOut = reinterpret_cast<float4*>(take());
+    C.queryList = reinterpret_cast<uint32_t*>(take());
+    C.recIn = reinterpret_cast<float4*>(take());
+    C.recAux = reinterpret_cast<float4*>(take());
+    float4* batchIn = reinterpret_cast<float4*>(take());
+    float4* batchTarget = reinterpret_cast<float4*>(take());
+    uint32_t* counters = reinterpret_cast<uint32_t*>(take());   // [0] queries, [1] batch
+    C.queryCount = counters;
+    mrg::PtPaths& P = c->ptPaths;
+    // ---- training paths ----
+    if(trainPaths)
+    {
+        PtRun Tr = R;
+        Tr.L.slots = trainPaths;
+        Tr.slots = trainPaths;
+        Tr.L.sampleBase = p->sampleStart * 2654435761u + p->seed;
+        Tr.L.cache = C;
+        Tr.L.cache.mode = 2u;
+        PT_TRY(cudaMemsetAsync(C.recAux, 0, sizes[4], st), "mrg_pt_render_cached: records");
+        PT_TRY(pt_bounces(c, Tr, st), "training paths");
+        PT_TRY(cudaMemsetAsync(counters + 1, 0, sizeof(uint32_t), st), "mrg_pt_render_cached: batch");
+        PT_TRY(mrg::pt_cache_targets(P, Tr.L.cache, trainPaths, batchIn, batchTarget, counters + 1, c->smCount, st),
+               "training targets");
+        PT_TRY(mrg::nrc_train(c->cache, batchIn, batchTarget, counters + 1, (uint32_t)recs, c->smCount, st),
+               "cache training");
+        if(hLoss)
+        {
+            PT_TRY(cudaMemcpyAsync(hLoss, c->cache.loss, sizeof(float), cudaMemcpyDeviceToHost, st), "loss");
+        }
+    }
+    // ---- render with the cache ----
+    R.L.cache = C;
+    R.L.cache.mode = 1u;
+    for(uint32_t pass = 0; pass < p->spp / R.spp; pass++)
+    {
+        R.L.sampleBase = p->sampleStart + pass * R.spp;
+        PT_TRY(cudaMemsetAsync(counters, 0, sizeof(uint32_t), st), "mrg_pt_render_cached: queries");
+        PT_TRY(pt_bounces(c, R, st), "cached pass");
+        PT_TRY(mrg::nrc_query_list(c->cache, C.queryIn, C.queryList, C.queryCount, R.slots, C.queryOut, c->smCount, st),
+               "cache query");
+        PT_TRY(mrg::pt_cache_apply(P, C, c->smCount, st), "cache apply");
+        PT_TRY(mrg::pt_film(R.L, P, reinterpret_cast<float4*>(dImage), st), "film");
+    }
+    if(hLoss) PT_TRY(cudaStreamSynchronize(st), "mrg_pt_render_cached");
+    return MRG_OK;
+}
+
 mrg_status mrg_pt_adjoint(mrg_ctx* c, const mrg_pt_params* p, uint32_t texId, const float* dImageAdjoint,
                           float* dGrad, float* dImage, void* stream)
 {

@@ -61,6 +61,17 @@ class PathTracer:
         self._tex_shapes[out.value] = (t.shape[0], t.shape[1])
         return out.value
 
+    def render_cached(self, p, image=None, train_paths=32768, stream=None, loss=False):
+        """One cache-assisted frame (see mrg_pt_render_cached); needs a
+        RadianceCache created on this tracer.  Returns (image, loss or None)."""
+        import torch
+        if image is None:
+            image = torch.zeros((p.height, p.width, 4), dtype=torch.float32, device="cuda:%d" % self.acc.device)
+        l = C.c_float(0.0)
+        N.check(N.lib().mrg_pt_render_cached(self.acc._h, C.byref(p), C.c_void_p(image.data_ptr()), train_paths,
+                                             C.byref(l) if loss else None, _stream_ptr(stream)))
+        return image, (l.value if loss else None)
+
     def adjoint(self, p, tex_id, image_adjoint, grad=None, image=None, stream=None):
         """Path-replay adjoint (see mrg_pt_adjoint): image_adjoint is a
         (h, w, 4) float32 CUDA tensor of dLoss/dPixel; returns grad, a

@@ -98,3 +98,38 @@ def test_training_fits_a_radiance_field():
     print("training: loss %.4g -> %.4g, held-out relMSE %.4g" % (first, last, rel))
     assert last <= first / 10.0 and rel <= 0.05
     c.close()
+
+
+def test_cached_render_learns_the_scene():
+    """Cache-assisted path tracing of the production scene (RGB): the training
+    loss falls as frames go by, and the cached image approaches a converged
+    plain render (the cache trades variance for a bounded bias)."""
+    from mray_gb300 import scenes
+    from mray_gb300.pt import PathTracer, load_box_scene
+    surf, cam = scenes.c2_scene(0, texture_size=256)
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    pt.set_env(scenes.sky_map(256, 128, seed=0))
+    box = pt.acc.scene_aabb()
+    cache = RadianceCache(owner=pt, aabb=tuple(float(v) for v in box), max_batch=65536)
+    w, h = 160, 90
+    ref = pt.render(PathTracer.params(w, h, 512, cam, max_depth=12, rr_start=3, seed=1, samples_per_pass=64))
+    ref = (ref[..., :3] / ref[..., 3:]).cpu().numpy()
+    losses = []
+    for f in range(60):
+        p = PathTracer.params(w, h, 1, cam, max_depth=12, rr_start=3, seed=100 + f, sample_start=f)
+        _, l = pt.render_cached(p, train_paths=32768, loss=True)
+        losses.append(l)
+    img = None
+    for f in range(16):
+        p = PathTracer.params(w, h, 1, cam, max_depth=12, rr_start=3, seed=500 + f, sample_start=f)
+        img, _ = pt.render_cached(p, image=img, train_paths=32768)
+    img = (img[..., :3] / img[..., 3:]).cpu().numpy()
+    rel = float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+    bias = float(abs(img.mean() - ref.mean()) / ref.mean())
+    print("cache loss %.4g -> %.4g; 16-frame cached relMSE %.4g, mean bias %.3g" %
+          (np.mean(losses[:5]), np.mean(losses[-5:]), rel, bias))
+    assert np.all(np.isfinite(img))
+    assert np.mean(losses[-5:]) < np.mean(losses[:5])
+    assert bias < 0.15 and rel < 0.5
+    pt.close()
