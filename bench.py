@@ -234,13 +234,17 @@ def gpu_arm(args):
     per_ray = (32 + 28 + 80.0 * counts["node_visits"] / counts["rays"] +
                48.0 * counts["tri_tests"] / counts["rays"] + 96.0 * counts["instance_entries"] / counts["rays"])
     achieved = per_ray * n / (kernel_ms * 1e-3) / 1e9
+    # DRAM bytes of one k_trace<closest> launch from the committed ncu summary
+    # (a line "traffic_bytes_per_launch: N")
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "traverse_closest_traffic.json")
+    tp = os.path.join(ROOT, "profiles", "k_trace_closest_bvh_stress.md")
     if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get("bytes_per_launch")
-        except Exception:
-            traffic = None
+        for ln in open(tp):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                try:
+                    traffic = int(ln.split(":", 1)[1].strip())
+                except ValueError:
+                    traffic = None
 
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws,
@@ -390,11 +394,12 @@ def c3_adjoint(args, dev):
     return {"c3_adjoint_ms_512sq_32spp": round(ms, 2)}
 
 
-def c4_equal_time(args, dev):
+def c4_equal_time(args, dev, spp_per_frame=8):
     """Radiance cache on the production scene (RGB, 480x270, depth 12):
     relMSE against a 4096-spp plain render, for plain path tracing at 16 spp
-    and for cache-assisted frames (1 spp + one training step on 32,768
-    training paths each) in the same time, after 64 warm-up frames."""
+    and for cache-assisted frames (spp_per_frame samples per pixel in one
+    pass, ~32,768 of its paths training the cache) in the same time, after 64
+    warm-up frames."""
     import torch
     from mray_gb300.pt import PathTracer, load_box_scene
     from mray_gb300.cache import RadianceCache
@@ -424,11 +429,12 @@ def c4_equal_time(args, dev):
     e1.record()
     torch.cuda.synchronize(dev)
     t_plain = e0.elapsed_time(e1)
+    k = spp_per_frame
     for f in range(64):
-        pt.render_cached(P(1, 100 + f, start=f), train_paths=32768)
+        pt.render_cached(P(k, 100 + f, start=k * f), train_paths=32768)
     torch.cuda.synchronize(dev)
     e0.record()
-    pt.render_cached(P(1, 300, start=0), train_paths=32768)
+    pt.render_cached(P(k, 300, start=0), train_paths=32768)
     e1.record()
     torch.cuda.synchronize(dev)
     t_frame = e0.elapsed_time(e1)
@@ -436,12 +442,12 @@ def c4_equal_time(args, dev):
     img = None
     e0.record()
     for f in range(frames):
-        img, _ = pt.render_cached(P(1, 1000 + f, start=f), image=img, train_paths=32768)
+        img, _ = pt.render_cached(P(k, 1000 + f, start=k * f), image=img, train_paths=32768)
     e1.record()
     torch.cuda.synchronize(dev)
     t_cached = e0.elapsed_time(e1)
     out = {"c4_plain_16spp_ms": round(t_plain, 2), "c4_plain_relmse": round(relmse(plain), 5),
-           "c4_cached_frame_ms": round(t_frame, 3), "c4_cached_frames": frames,
+           "c4_cached_frame_ms": round(t_frame, 3), "c4_cached_frames": frames, "c4_cached_spp_per_frame": k,
            "c4_cached_ms": round(t_cached, 2), "c4_cached_relmse": round(relmse(img), 5),
            "c4_workload": "production scene RGB 480x270 depth 12, reference 4096 spp plain"}
     pt.close()

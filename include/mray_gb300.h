@@ -335,13 +335,14 @@ mrg_status mrg_cache_gradients(mrg_ctx* ctx, const float* d_inputs, const float*
                                float* h_grad_weights, float* h_grad_table, float* h_loss);
 mrg_status mrg_cache_set_params(mrg_ctx* ctx, const float* h_weights, const float* h_table);
 
-/* One frame of cache-assisted path tracing (RGB): train_paths training paths
- * from hashed pixels are traced to full depth and their vertices 1..2 give
- * (inputs, outgoing radiance) samples for one mrg_cache_train step; then
- * params->spp samples per pixel are rendered with every path ending at its
- * second vertex on a cache query (Mueller et al. 2021), added to d_image as
- * mrg_pt_render does.  train_paths = 0 skips training.  Needs
- * mrg_cache_create with max_batch >= 2 * train_paths. */
+/* Cache-assisted path tracing (RGB; Mueller et al. 2021): params->spp
+ * samples per pixel, added to d_image as mrg_pt_render does, every path
+ * ending at its second vertex on a cache query of the outgoing radiance.
+ * About train_paths of each pass's paths (a hashed sparse subset) are training
+ * paths instead: they record vertices 1 and 2 and end at vertex 3 on a cache
+ * query (self-training); after the pass their (inputs, outgoing radiance)
+ * samples, at most the cache's max_batch, make one mrg_cache_train step.
+ * train_paths = 0 renders without training. */
 mrg_status mrg_pt_render_cached(mrg_ctx* ctx, const mrg_pt_params* params, float* d_image,
                                 uint32_t train_paths, float* h_loss, void* stream);
 

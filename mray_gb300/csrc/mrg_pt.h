@@ -88,15 +88,19 @@ struct PtAdjoint
     uint32_t      enabled;
 };
 
-// Radiance-cache use by the path tracer: mode 1 ends every path at its
-// second vertex with a cache query of the outgoing radiance there; mode 2
-// traces training paths (pixels drawn by hash) and records, at vertices
-// 1..recPerPath, the cache inputs, the throughput on arrival and the radiance
-// gathered before the vertex (targets follow from the path's final radiance).
+// Radiance-cache use by the path tracer (mode 1): a path ends at its second
+// vertex with a cache query of the outgoing radiance there, except the sparse
+// training paths (one slot in trainStride, chosen by hash), which record at
+// vertices 1..recPerPath the cache inputs, the throughput on arrival and the
+// radiance gathered before the vertex, and end at vertex recPerPath + 1 on a
+// cache query themselves (self-training); targets follow from each training
+// path's final radiance.
 struct PtCacheUse
 {
     uint32_t  mode;
     uint32_t  recPerPath;
+    uint32_t  trainStride;    // 0: no training paths
+    uint32_t  batchCap;       // training samples kept per pass
     float4*   queryIn;        // 4 per slot
     uint32_t* queryList;
     uint32_t* queryCount;
@@ -184,9 +188,9 @@ cudaError_t pt_work_keys(const PtPaths& P, const PtSurface* surfaces, uint32_t n
                          const uint32_t* aliveList, const uint32_t* aliveCount, int smCount, cudaStream_t st);
 // rad[slot] += thr[slot] * queryOut[slot] for the queried slots.
 cudaError_t pt_cache_apply(const PtPaths& P, const PtCacheUse& C, int smCount, cudaStream_t st);
-// Training batch from the records of a training pass: target = (final
-// radiance - radiance before) / throughput, valid records compacted.
-cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t paths, float4* batchIn,
+// Training batch from the records of a pass: target = (final radiance -
+// radiance before) / throughput, valid records compacted (at most batchCap).
+cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t slots, float4* batchIn,
                              float4* batchTarget, uint32_t* batchCount, int smCount, cudaStream_t st);
 cudaError_t pt_resolve(const PtLaunch& L, const PtPaths& P, uint32_t depth, int smCount, cudaStream_t st);
 cudaError_t pt_film(const PtLaunch& L, const PtPaths& P, float4* image, cudaStream_t st);

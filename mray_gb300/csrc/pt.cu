@@ -564,15 +564,13 @@ __device__ __forceinline__ Chan radiance_of(const PtSpectral& S, float r, float 
     return chan(r, g, b, 0.0f);
 }
 
-__device__ __forceinline__ uint32_t slot_pixel(const PtLaunch& L, uint32_t i)
+__device__ __forceinline__ uint32_t slot_pixel(const PtLaunch& L, uint32_t i) { return i % (L.width * L.height); }
+__device__ __forceinline__ bool training_path(const PtCacheUse& C, uint32_t i, uint32_t sampleBase)
 {
-    // training paths start at hashed pixels
-    if(L.cache.mode == 2u) return pcg_hash(i * 0x9E3779B9u + L.sampleBase) % (L.width * L.height);
-    return i % (L.width * L.height);
+    return C.trainStride != 0u && (pcg_hash(i ^ pcg_hash(sampleBase + 0x5BD1E995u)) % C.trainStride) == 0u;
 }
 __device__ __forceinline__ uint32_t slot_sample(const PtLaunch& L, uint32_t i)
 {
-    if(L.cache.mode == 2u) return L.sampleBase + i;
     return L.sampleBase + i / (L.width * L.height);
 }
 
@@ -874,14 +872,15 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                     const bool isSpec = specularity<NC>(sf, alb) >= kSpecularThreshold;
                     const uint32_t mt = sf.info.w;
                     const float crough = (mt == kMatLambert) ? 1.0f : ((mt == kMatUnreal) ? sf.albedo.w : 0.0f);
-                    if(CM == 2 && depth >= 1u && depth <= L.cache.recPerPath)
+                    const bool trainer = (CM == 1) && training_path(L.cache, i, L.sampleBase);
+                    if(trainer && depth >= 1u && depth <= L.cache.recPerPath)
                     {
                         const size_t rec = (size_t)i * L.cache.recPerPath + (depth - 1u);
                         cache_inputs(L.cache.recIn + 4 * rec, pos, crough, wo, nrm, a3);
                         L.cache.recAux[2 * rec] = make_float4(thr.v[0], thr.v[1], thr.v[2], 1.0f);
                         L.cache.recAux[2 * rec + 1] = make_float4(rad.v[0], rad.v[1], rad.v[2], 0.0f);
                     }
-                    const bool terminal = (CM == 1 && depth == 1u);
+                    const bool terminal = (CM == 1) && depth == (trainer ? L.cache.recPerPath + 1u : 1u);
                     if(terminal)
                     {
                         // the cache stands for the rest of the path
@@ -1179,8 +1178,11 @@ k_cache_targets(PtPaths P, PtCacheUse C, uint32_t paths, float4* batchIn, float4
         if(ok)
         {
             const uint32_t o = b + __popc(m & ((1u << lane) - 1u));
-            for(int j = 0; j < 4; j++) batchIn[4 * (size_t)o + j] = C.recIn[4 * (size_t)r + j];
-            batchTarget[o] = tgt;
+            if(o < C.batchCap)
+            {
+                for(int j = 0; j < 4; j++) batchIn[4 * (size_t)o + j] = C.recIn[4 * (size_t)r + j];
+                batchTarget[o] = tgt;
+            }
         }
     }
 }
@@ -1272,8 +1274,6 @@ cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSceneTabl
     const unsigned grid = (unsigned)smCount * 8u;
     if(L.cache.mode == 1u)
         k_shade<false, false, 1><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
-    else if(L.cache.mode == 2u)
-        k_shade<false, false, 2><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
     else if(L.adj.enabled)
         k_shade<false, true, 0><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
     else if(L.spec.enabled)
@@ -1296,10 +1296,10 @@ cudaError_t pt_cache_apply(const PtPaths& P, const PtCacheUse& C, int smCount, c
     return cudaGetLastError();
 }
 
-cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t paths, float4* batchIn,
+cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t slots, float4* batchIn,
                              float4* batchTarget, uint32_t* batchCount, int smCount, cudaStream_t st)
 {
-    k_cache_targets<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C, paths, batchIn, batchTarget, batchCount);
+    k_cache_targets<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C, slots, batchIn, batchTarget, batchCount);
     return cudaGetLastError();
 }
 

@@ -606,8 +606,10 @@ cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, cudaStream_t st)
 {
     mrg::PtPaths& P = c->ptPaths;
     const mrg::PtLaunch& L = R.L;
+    // with the cache every path has ended by vertex recPerPath + 1
+    const uint32_t loops = (L.cache.mode == 1u) ? std::min(L.maxDepth, L.cache.recPerPath + 2u) : L.maxDepth;
     cudaError_t e = mrg::pt_raygen(L, P, P.listA, P.counts + 0, c->smCount, st);
-    for(uint32_t depth = 0; depth < L.maxDepth && e == cudaSuccess; depth++)
+    for(uint32_t depth = 0; depth < loops && e == cudaSuccess; depth++)
     {
         uint32_t* alive = (depth & 1u) ? P.listB : P.listA;
         uint32_t* next = (depth & 1u) ? P.listA : P.listB;
@@ -667,17 +669,14 @@ mrg_status mrg_pt_render_cached(mrg_ctx* c, const mrg_pt_params* p, float* dImag
     if(!c->cacheOn) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_pt_render_cached: call mrg_cache_create first");
     if(c->ptSpec.enabled) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render_cached: RGB rendering only");
     constexpr uint32_t kRec = 2;
-    if(2ull * trainPaths > c->cache.cap)
-        return mrg::set_error(MRG_ERR_LIMIT, "mrg_pt_render_cached: 2 * train_paths exceeds the cache's max_batch");
     DevGuard g(c->device);
     PtRun R;
     mrg_status s = pt_setup(c, p, R, "mrg_pt_render_cached");
     if(s != MRG_OK) return s;
-    if(trainPaths > R.slots && (s = pt_paths(c, trainPaths)) != MRG_OK) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // buffers: query in / out / list (per slot), records and batch (per training record), counters
-    const size_t slots = R.slots, recs = (size_t)trainPaths * kRec;
-    const size_t sizes[8] = { slots * 64, slots * 16, slots * 4, recs * 64, recs * 32, recs * 64, recs * 16, 64 };
+    // buffers: query in / out / list, per-slot training records, batch, counters
+    const size_t slots = R.slots, recs = slots * kRec, cap = c->cache.cap;
+    const size_t sizes[8] = { slots * 64, slots * 16, slots * 4, recs * 64, recs * 32, cap * 64, cap * 16, 64 };
     size_t need = 0;
     for(size_t z : sizes) need += (z + 255) & ~size_t(255);
     if(c->ptCacheBufBytes < need)
@@ -692,7 +691,8 @@ mrg_status mrg_pt_render_cached(mrg_ctx* c, const mrg_pt_params* p, float* dImag
     size_t off = 0;
     int k = 0;
     auto take = [&]() { char* q = base + off; off += (sizes[k++] + 255) & ~size_t(255); return q; };
-    mrg::PtCacheUse C{};
+    mrg::PtCacheUse& C = R.L.cache;
+    C.mode = 1u;
     C.recPerPath = kRec;
     C.queryIn = reinterpret_cast<float4*>(take());
     C.queryOut = reinterpret_cast<float4*>(take());
@@ -703,42 +703,33 @@ mrg_status mrg_pt_render_cached(mrg_ctx* c, const mrg_pt_params* p, float* dImag
     float4* batchTarget = reinterpret_cast<float4*>(take());
     uint32_t* counters = reinterpret_cast<uint32_t*>(take());   // [0] queries, [1] batch
     C.queryCount = counters;
+    // one slot in `stride` trains, for about trainPaths training paths per pass
+    C.trainStride = trainPaths ? (uint32_t)std::max<size_t>(1, slots / trainPaths) : 0u;
+    C.batchCap = (uint32_t)cap;
     mrg::PtPaths& P = c->ptPaths;
-    // ---- training paths ----
-    if(trainPaths)
-    {
-        PtRun Tr = R;
-        Tr.L.slots = trainPaths;
-        Tr.slots = trainPaths;
-        Tr.L.sampleBase = p->sampleStart * 2654435761u + p->seed;
-        Tr.L.cache = C;
-        Tr.L.cache.mode = 2u;
-        PT_TRY(cudaMemsetAsync(C.recAux, 0, sizes[4], st), "mrg_pt_render_cached: records");
-        PT_TRY(pt_bounces(c, Tr, st), "training paths");
-        PT_TRY(cudaMemsetAsync(counters + 1, 0, sizeof(uint32_t), st), "mrg_pt_render_cached: batch");
-        PT_TRY(mrg::pt_cache_targets(P, Tr.L.cache, trainPaths, batchIn, batchTarget, counters + 1, c->smCount, st),
-               "training targets");
-        PT_TRY(mrg::nrc_train(c->cache, batchIn, batchTarget, counters + 1, (uint32_t)recs, c->smCount, st),
-               "cache training");
-        if(hLoss)
-        {
-            PT_TRY(cudaMemcpyAsync(hLoss, c->cache.loss, sizeof(float), cudaMemcpyDeviceToHost, st), "loss");
-        }
-    }
-    // ---- render with the cache ----
-    R.L.cache = C;
-    R.L.cache.mode = 1u;
     for(uint32_t pass = 0; pass < p->spp / R.spp; pass++)
     {
         R.L.sampleBase = p->sampleStart + pass * R.spp;
-        PT_TRY(cudaMemsetAsync(counters, 0, sizeof(uint32_t), st), "mrg_pt_render_cached: queries");
+        PT_TRY(cudaMemsetAsync(counters, 0, 2 * sizeof(uint32_t), st), "mrg_pt_render_cached: counters");
+        if(C.trainStride) PT_TRY(cudaMemsetAsync(C.recAux, 0, sizes[4], st), "mrg_pt_render_cached: records");
         PT_TRY(pt_bounces(c, R, st), "cached pass");
         PT_TRY(mrg::nrc_query_list(c->cache, C.queryIn, C.queryList, C.queryCount, R.slots, C.queryOut, c->smCount, st),
                "cache query");
         PT_TRY(mrg::pt_cache_apply(P, C, c->smCount, st), "cache apply");
+        if(C.trainStride)
+        {
+            PT_TRY(mrg::pt_cache_targets(P, C, R.slots, batchIn, batchTarget, counters + 1, c->smCount, st),
+                   "training targets");
+            PT_TRY(mrg::nrc_train(c->cache, batchIn, batchTarget, counters + 1, (uint32_t)cap, c->smCount, st),
+                   "cache training");
+        }
         PT_TRY(mrg::pt_film(R.L, P, reinterpret_cast<float4*>(dImage), st), "film");
     }
-    if(hLoss) PT_TRY(cudaStreamSynchronize(st), "mrg_pt_render_cached");
+    if(hLoss)
+    {
+        PT_TRY(cudaMemcpyAsync(hLoss, c->cache.loss, sizeof(float), cudaMemcpyDeviceToHost, st), "loss");
+        PT_TRY(cudaStreamSynchronize(st), "mrg_pt_render_cached");
+    }
     return MRG_OK;
 }
 
