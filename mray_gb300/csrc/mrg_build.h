@@ -19,6 +19,7 @@ struct BuildInput
     uint32_t        count = 0;         // triangles or boxes
     uint32_t        primKeyBase = 0;
     uint32_t        maxLeaf = 3;       // primitives per leaf child (<= 3)
+    bool            ploc = false;      // PLOC clustering instead of the Karras radix tree
 };
 
 struct BuildResult
