@@ -29,7 +29,7 @@ namespace {
 #define MRG_TRACE_REFILL 8           // refill when at least this many lanes are idle
 #endif
 #ifndef MRG_TRACE_STEP_BUDGET
-#define MRG_TRACE_STEP_BUDGET 16     // traversal iterations between refill checks
+#define MRG_TRACE_STEP_BUDGET 24     // traversal iterations between refill checks
 #endif
 #ifndef MRG_TRACE_PREFETCH
 #define MRG_TRACE_PREFETCH 0         // L1 prefetch of the next node
@@ -39,6 +39,12 @@ namespace {
 #endif
 #ifndef MRG_TRACE_POSTPONE
 #define MRG_TRACE_POSTPONE 0         // postpone triangles when fewer lanes want them
+#endif
+#ifndef MRG_TRACE_SMEM_STACK
+#define MRG_TRACE_SMEM_STACK 0       // >0: the first entries of each thread's stack live in shared memory
+#endif
+#ifndef MRG_TRACE_TRI_CHUNK
+#define MRG_TRACE_TRI_CHUNK 2        // >0: at most this many triangles per iteration, the rest go on the stack
 #endif
 
 constexpr int kTraceTPB = 128;
@@ -174,7 +180,26 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
     const uint32_t n = nDevice ? *nDevice : nHost;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t laneLt = (1u << lane) - 1u;
-    uint2 stack[kStackSize];
+    constexpr int kSmemStack = MRG_TRACE_SMEM_STACK;
+    uint2 stack[kStackSize - kSmemStack];
+#if MRG_TRACE_SMEM_STACK > 0
+    __shared__ uint2 sStack[kSmemStack][kTraceTPB];
+#endif
+    // stack entries [0, kSmemStack) in shared memory, the rest in local memory
+    auto push = [&](uint2 v, int& p) {
+#if MRG_TRACE_SMEM_STACK > 0
+        if(p < kSmemStack) sStack[p][threadIdx.x] = v; else
+#endif
+        stack[p - kSmemStack] = v;
+        p++;
+    };
+    auto pop = [&](int& p) -> uint2 {
+        --p;
+#if MRG_TRACE_SMEM_STACK > 0
+        if(p < kSmemStack) return sStack[p][threadIdx.x];
+#endif
+        return stack[p - kSmemStack];
+    };
 
     // Per-lane ray state.
     bool live = false;
@@ -247,7 +272,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                 if(ng.y > 0x00FFFFFFu)
                 {
                     if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); finished = true; break; }
-                    stack[sp++] = ng;
+                    push(ng, sp);
                 }
                 uint32_t cb, tb, im;
                 const uint32_t hm = intersect_node(sc.nodes, ni, lr, tmin, tmax, cb, tb, im);
@@ -278,14 +303,23 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
             if(blasBase >= 0)
             {
                 // triangles of a BLAS leaf group
+                int triDone = 0;
                 while(tg.y != 0u)
                 {
+                    if(MRG_TRACE_TRI_CHUNK > 0 && triDone == MRG_TRACE_TRI_CHUNK && sp < kStackSize)
+                    {
+                        // the rest of the group waits on the stack (as postponed triangles do)
+                        push(tg, sp);
+                        tg.y = 0u;
+                        break;
+                    }
+                    triDone++;
                     // Postpone when few lanes want triangles and this lane has
                     // nodes left: SIMD lanes stay on the wider node work.
                     if(ng.y > 0x00FFFFFFu && __popc(__activemask()) < kPostponeLanes &&
                        sp < kStackSize)
                     {
-                        stack[sp++] = tg;
+                        push(tg, sp);
                         tg.y = 0u;
                         break;
                     }
@@ -345,12 +379,12 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                         if(ng.y > 0x00FFFFFFu)
                         {
                             if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); finished = true; break; }
-                            stack[sp++] = ng;
+                            push(ng, sp);
                         }
                         if(keep != 0u)
                         {
                             if(sp >= kStackSize) { atomicOr(scr.errorFlag, kTraceStackOverflow); finished = true; break; }
-                            stack[sp++] = make_uint2(tg.x, keep);
+                            push(make_uint2(tg.x, keep), sp);
                         }
                         blasBase = sp;
                         const float4 m0 = __ldg(ip), m1 = __ldg(ip + 1), m2 = __ldg(ip + 2);
@@ -375,7 +409,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     setup_level(lr, wox, woy, woz, wdx, wdy, wdz);
                 }
                 if(sp == 0) { finished = true; break; }
-                ng = stack[--sp];
+                ng = pop(sp);
             }
         }
 
