@@ -24,6 +24,17 @@ bool use_ploc()
     return v && std::strcmp(v, "ploc") == 0;
 }
 
+// Optional coherence sort of large closest-hit batches (by direction octant,
+// then origin) before the cast, MRG_CAST_SORT=1.  Off by default: on the
+// stress workload the sort plus the sorted cast took 4.63 ms against 3.13 ms
+// for the cast in the caller's order.
+constexpr uint32_t kCoherenceSortMin = 1u << 18;
+bool cast_sort_enabled()
+{
+    const char* v = std::getenv("MRG_CAST_SORT");
+    return v && std::strcmp(v, "1") == 0;
+}
+
 
 thread_local std::string g_lastError;
 
@@ -360,7 +371,22 @@ mrg_status mrg_cast_closest(mrg_ctx* c, mrg_ray* dRays, const uint32_t* dIdx, ui
        reinterpret_cast<uintptr_t>(dMeta) % 8 != 0)
         return fail(MRG_ERR_INVALID_ARG, "mrg_cast_closest: misaligned buffer");
     DeviceGuard g(c->device);
-    cudaError_t e = mrg::launch_closest(c->scene, scratch_of(c), dRays, dIdx, n, dHits, dMeta,
+    const uint32_t* order = dIdx;
+    if(cast_sort_enabled() && n >= kCoherenceSortMin)
+    {
+        // coherence sort: an index permutation only, results are per ray
+        const size_t words = 4ull * n + mrg::multisplit_hist_words(n, 8);
+        mrg_status s = mrg::partition_scratch(c, words);
+        if(s != MRG_OK) return s;
+        uint32_t* base = c->dPartScratch;
+        uint32_t* sorted = nullptr;
+        cudaError_t e = mrg::ray_coherence_order(dRays, dIdx, n, c->sceneBoxExact, base, base + n, base + 2ull * n,
+                                                 base + 3ull * n, base + 4ull * n, sorted, c->smCount,
+                                                 static_cast<cudaStream_t>(stream));
+        if(e != cudaSuccess) return cuda_fail(e, "mrg_cast_closest: coherence sort");
+        order = sorted;
+    }
+    cudaError_t e = mrg::launch_closest(c->scene, scratch_of(c), dRays, order, n, dHits, dMeta,
                                         c->smCount, static_cast<cudaStream_t>(stream));
     if(e != cudaSuccess) return cuda_fail(e, "mrg_cast_closest");
     return MRG_OK;

@@ -137,5 +137,7 @@ namespace mrg {
 // Records the calling thread's last error message (mrg_last_error) and
 // returns the status.
 mrg_status set_error(mrg_status s, const std::string& msg);
+// Grows the context's partitioner scratch to `words` 32-bit words.
+mrg_status partition_scratch(mrg_ctx* c, size_t words);
 
 } // namespace mrg

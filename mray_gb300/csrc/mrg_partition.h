@@ -41,4 +41,12 @@ cudaError_t multi_partition(const uint32_t* keys, const uint32_t* indices, const
                             uint32_t* hist, uint32_t* count, uint32_t* offsets, uint32_t* binKeys,
                             uint32_t maxPartitions, int smCount, cudaStream_t st);
 
+// Index order that groups rays by direction octant, then by origin (Morton
+// code in `box`): a coherence sort before a cast.  Scratch: 4 arrays of n
+// words and a count table of multisplit_hist_words(n, 8); `order` points at
+// the sorted indices (one of the scratch arrays).
+cudaError_t ray_coherence_order(const void* rays, const uint32_t* idx, uint32_t n, const float box[6],
+                                uint32_t* keysA, uint32_t* valsA, uint32_t* keysB, uint32_t* valsB,
+                                uint32_t* hist, uint32_t*& order, int smCount, cudaStream_t st);
+
 } // namespace mrg

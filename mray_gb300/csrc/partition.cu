@@ -182,6 +182,60 @@ __global__ void k_bins(const uint32_t* __restrict__ splitPos, const uint32_t* __
 
 } // namespace
 
+namespace {
+
+// Coherence key of a ray: direction octant above a 27-bit Morton code of the
+// origin quantised (9 bits per axis) in the scene box.
+__global__ void k_ray_keys(const float4* __restrict__ rays, const uint32_t* __restrict__ idx, uint32_t n,
+                           float3 lo, float3 scale, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals)
+{
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const uint32_t r = idx ? idx[i] : i;
+        const float4 o = __ldg(rays + 2 * (size_t)r), d = __ldg(rays + 2 * (size_t)r + 1);
+        auto q = [](float v, float l, float s) {
+            const float t = fminf(fmaxf((v - l) * s, 0.0f), 511.0f);
+            uint32_t x = (uint32_t)t;
+            x = (x | (x << 16)) & 0x030000FFu;
+            x = (x | (x << 8)) & 0x0300F00Fu;
+            x = (x | (x << 4)) & 0x030C30C3u;
+            x = (x | (x << 2)) & 0x09249249u;
+            return x;
+        };
+        const uint32_t m = q(o.x, lo.x, scale.x) | (q(o.y, lo.y, scale.y) << 1) | (q(o.z, lo.z, scale.z) << 2);
+        const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+        keys[i] = (oct << 27) | m;
+        vals[i] = r;
+    }
+}
+
+} // namespace
+
+cudaError_t ray_coherence_order(const void* rays, const uint32_t* idx, uint32_t n, const float box[6],
+                                uint32_t* keysA, uint32_t* valsA, uint32_t* keysB, uint32_t* valsB,
+                                uint32_t* hist, uint32_t*& order, int smCount, cudaStream_t st)
+{
+    float3 lo = make_float3(box[0], box[1], box[2]), sc;
+    const float ext[3] = { box[3] - box[0], box[4] - box[1], box[5] - box[2] };
+    sc.x = ext[0] > 0.0f ? 511.0f / ext[0] : 0.0f;
+    sc.y = ext[1] > 0.0f ? 511.0f / ext[1] : 0.0f;
+    sc.z = ext[2] > 0.0f ? 511.0f / ext[2] : 0.0f;
+    k_ray_keys<<<std::max(1, smCount * 8), 256, 0, st>>>(static_cast<const float4*>(rays), idx, n, lo, sc, keysA, valsA);
+    cudaError_t e = cudaGetLastError();
+    uint32_t* kin = keysA; uint32_t* vin = valsA;
+    uint32_t* kout = keysB; uint32_t* vout = valsB;
+    for(uint32_t p = 0; p < 4 && e == cudaSuccess; p++)
+    {
+        DigitSpec s;
+        s.batchShift = 0; s.batchWidth = 30;
+        s.digitShift = 8u * p; s.digitBits = (p == 3) ? 6u : 8u;
+        e = multisplit_pass(kin, vin, kout, vout, nullptr, n, s, hist, st);
+        std::swap(kin, kout); std::swap(vin, vout);
+    }
+    order = vin;
+    return e;
+}
+
 size_t multisplit_hist_words(uint32_t nMax, uint32_t digitBits)
 {
     const uint32_t tiles = (nMax + kMsTile - 1) / kMsTile;
