@@ -256,3 +256,25 @@ def test_c2_scene_spectral_small():
     print("c2 spectral: close %.4f relMSE %.3g kept %.3g" % (close, relmse(g, o), rel_kept))
     assert close >= 0.95 and rel_kept <= 1e-5
     pt.close()
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_mray_scene_file_per_pixel(mode):
+    """A scene read from MRay's JSON format (textured floor, mirror, glass,
+    GGX metal, area light, constant sky) renders on the GPU as in the oracle."""
+    import os
+    from mray_gb300 import scene_json
+    path = os.path.join(os.path.dirname(__file__), "scenes", "open_box.json")
+    pt = PathTracer(0)
+    cam, surf = scene_json.load(pt, path)
+    _, _, env = scene_json.read_scene(path)
+    S = oracle.PtScene(surf, env=env)
+    g = _img(pt.render(PathTracer.params(64, 64, 16, cam, sample_mode=mode, seed=4)))
+    o = _img(S.render(S.params(64, 64, 16, cam, sample_mode=mode, seed=4)))
+    close = (np.abs(g - o) <= 1e-4 * (1.0 + np.abs(o))).all(axis=-1).mean()
+    d = np.abs(g - o).max(axis=-1).ravel()
+    keep = d <= np.quantile(d, 0.98)
+    rel_kept = float(np.mean(((g - o).reshape(-1, 3)[keep]) ** 2 / (o.reshape(-1, 3)[keep] ** 2 + 1e-2)))
+    print("scene file mode %d: close %.4f relMSE %.3g kept %.3g" % (mode, close, relmse(g, o), rel_kept))
+    assert close >= 0.95 and rel_kept <= 1e-5
+    pt.close()
