@@ -24,6 +24,18 @@ bool use_ploc()
     return v && std::strcmp(v, "ploc") == 0;
 }
 
+// Triangles per BLAS leaf child (1..3).  One for large meshes (the stress
+// workload's 1.31M-triangle BLAS: 1,317 against 1,243 Mrays/s for three, the
+// tree growing from 73.8 to 93.1 MB), three for small ones, where one wide
+// node then holds the whole mesh (the box scene renders 14% faster);
+// MRG_BVH_LEAF overrides it.
+uint32_t leaf_size(uint32_t triangles)
+{
+    const char* v = std::getenv("MRG_BVH_LEAF");
+    const int k = v ? std::atoi(v) : (triangles > 1024u ? 1 : 3);
+    return (k >= 1 && k <= 3) ? (uint32_t)k : 1u;
+}
+
 // Optional coherence sort of large closest-hit batches (by direction octant,
 // then origin) before the cast, MRG_CAST_SORT=1.  Off by default: on the
 // stress workload the sort plus the sorted cast took 4.63 ms against 3.13 ms
@@ -239,7 +251,7 @@ mrg_status mrg_build(mrg_ctx* c)
         bi.kind = 0; bi.pos = dPos; bi.idx = dIdx;
         bi.count = (uint32_t)(m.idx.size() / 3);
         bi.primKeyBase = m.primKeyBase;
-        bi.maxLeaf = 3;
+        bi.maxLeaf = leaf_size(bi.count);
         bi.ploc = use_ploc();
         bool ok = mrg::build_wide_bvh(bi, blas[mi], st, err);
         cudaFree(dPos); cudaFree(dIdx);
