@@ -533,6 +533,16 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+def only_workload(args):
+    import torch
+    from mray_gb300 import build as B
+    B.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    fn = {"c0": box_scene_pt, "c2": c2_scene_pt, "c3": c3_adjoint, "c4": c4_equal_time}[args.only]
+    print(json.dumps({"workload": args.only, **fn(args, dev)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -543,11 +553,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pt-extras", action="store_true",
                     help="skip the production-scene and adjoint path-tracing lines")
+    ap.add_argument("--only", choices=["c0", "c2", "c3", "c4"], default=None,
+                    help="run one path-tracing workload alone and print its line (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
         reference_arm(args)
+    elif args.only:
+        only_workload(args)
     else:
         gpu_arm(args)
 
