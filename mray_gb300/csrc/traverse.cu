@@ -444,7 +444,6 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
     }
 }
 
-
 template<bool ANY, bool STATS>
 int blocks_for(int smCount)
 {
