@@ -105,6 +105,15 @@ mrg::TraceScratch scratch_of(mrg_ctx* c)
     return s;
 }
 
+// Chunks of the host-buffer cast pipeline: about 512k rays each, at most
+// kHostMaxChunks (MRG_HOST_CHUNKS overrides).
+uint32_t host_chunks(uint32_t n)
+{
+    const char* v = std::getenv("MRG_HOST_CHUNKS");
+    const int want = v ? std::atoi(v) : (int)(n >> 19);
+    return (uint32_t)std::min(std::max(want, 1), mrg_ctx::kHostMaxChunks);
+}
+
 } // namespace
 
 extern "C" {
@@ -168,6 +177,8 @@ mrg_status mrg_destroy(mrg_ctx* c)
     cudaFree(c->dPtCacheBuf);
     for(void* q : c->cacheAllocs) cudaFree(q);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
+    for(cudaStream_t& q : c->hostStreams) if(q) cudaStreamDestroy(q);
+    for(cudaEvent_t& q : c->hostEvents) if(q) cudaEventDestroy(q);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);
     delete c;
     return MRG_OK;
@@ -437,16 +448,37 @@ mrg_status mrg_cast_closest_host(mrg_ctx* c, mrg_ray* hRays, uint32_t n, mrg_hit
         MRG_TRY(cudaMalloc(&c->dStageMeta, sizeof(mrg_meta_hit) * (size_t)n), "mrg_cast_closest_host: staging");
         c->stageCap = n;
     }
-    cudaStream_t st = c->buildStream;
-    MRG_TRY(cudaMemcpyAsync(c->dStageRays, hRays, sizeof(mrg_ray) * (size_t)n, cudaMemcpyHostToDevice, st), "H2D rays");
-    MRG_TRY(cudaMemcpyAsync(c->dStageHits, hHits, sizeof(mrg_hit_keys) * (size_t)n, cudaMemcpyHostToDevice, st), "H2D hits");
-    MRG_TRY(cudaMemcpyAsync(c->dStageMeta, hMeta, sizeof(mrg_meta_hit) * (size_t)n, cudaMemcpyHostToDevice, st), "H2D meta");
-    MRG_TRY(mrg::launch_closest(c->scene, scratch_of(c), c->dStageRays, nullptr, n, c->dStageHits,
-                                c->dStageMeta, c->smCount, st), "cast");
-    MRG_TRY(cudaMemcpyAsync(hRays, c->dStageRays, sizeof(mrg_ray) * (size_t)n, cudaMemcpyDeviceToHost, st), "D2H rays");
-    MRG_TRY(cudaMemcpyAsync(hHits, c->dStageHits, sizeof(mrg_hit_keys) * (size_t)n, cudaMemcpyDeviceToHost, st), "D2H hits");
-    MRG_TRY(cudaMemcpyAsync(hMeta, c->dStageMeta, sizeof(mrg_meta_hit) * (size_t)n, cudaMemcpyDeviceToHost, st), "D2H meta");
-    return mrg_sync_status(c, st);
+    if(!c->hostStreams[0])
+    {
+        for(cudaStream_t& q : c->hostStreams)
+            MRG_TRY(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking), "mrg_cast_closest_host: streams");
+        for(cudaEvent_t& q : c->hostEvents)
+            MRG_TRY(cudaEventCreateWithFlags(&q, cudaEventDisableTiming), "mrg_cast_closest_host: events");
+    }
+    // The ray set goes through in chunks: while chunk k is cast, chunk k+1
+    // is copied in and chunk k-1 copied out (copy engines in both directions
+    // run beside the SMs).  Each chunk owns its slice of the staging buffers.
+    const uint32_t chunks = host_chunks(n);
+    cudaStream_t sIn = c->hostStreams[0], sCast = c->hostStreams[1], sOut = c->hostStreams[2];
+    for(uint32_t k = 0; k < chunks; k++)
+    {
+        const size_t off = (size_t)n * k / chunks, cnt = (size_t)n * (k + 1) / chunks - off;
+        if(cnt == 0) continue;
+        cudaEvent_t copied = c->hostEvents[2 * k], cast = c->hostEvents[2 * k + 1];
+        MRG_TRY(cudaMemcpyAsync(c->dStageRays + off, hRays + off, sizeof(mrg_ray) * cnt, cudaMemcpyHostToDevice, sIn), "H2D rays");
+        MRG_TRY(cudaMemcpyAsync(c->dStageHits + off, hHits + off, sizeof(mrg_hit_keys) * cnt, cudaMemcpyHostToDevice, sIn), "H2D hits");
+        MRG_TRY(cudaMemcpyAsync(c->dStageMeta + off, hMeta + off, sizeof(mrg_meta_hit) * cnt, cudaMemcpyHostToDevice, sIn), "H2D meta");
+        MRG_TRY(cudaEventRecord(copied, sIn), "event");
+        MRG_TRY(cudaStreamWaitEvent(sCast, copied, 0), "event wait");
+        MRG_TRY(mrg::launch_closest(c->scene, scratch_of(c), c->dStageRays + off, nullptr, (uint32_t)cnt,
+                                    c->dStageHits + off, c->dStageMeta + off, c->smCount, sCast), "cast");
+        MRG_TRY(cudaEventRecord(cast, sCast), "event");
+        MRG_TRY(cudaStreamWaitEvent(sOut, cast, 0), "event wait");
+        MRG_TRY(cudaMemcpyAsync(hRays + off, c->dStageRays + off, sizeof(mrg_ray) * cnt, cudaMemcpyDeviceToHost, sOut), "D2H rays");
+        MRG_TRY(cudaMemcpyAsync(hHits + off, c->dStageHits + off, sizeof(mrg_hit_keys) * cnt, cudaMemcpyDeviceToHost, sOut), "D2H hits");
+        MRG_TRY(cudaMemcpyAsync(hMeta + off, c->dStageMeta + off, sizeof(mrg_meta_hit) * cnt, cudaMemcpyDeviceToHost, sOut), "D2H meta");
+    }
+    return mrg_sync_status(c, sOut);
 }
 
 mrg_status mrg_scene_aabb(mrg_ctx* c, float out[6])
@@ -482,6 +514,8 @@ mrg_status mrg_sync_status(mrg_ctx* c, void* stream)
     if(flag)
     {
         MRG_TRY(cudaMemset(c->dScratch + 1, 0, sizeof(uint32_t)), "mrg_sync_status: clear flag");
+        if(flag & mrg::kNrcWaitTimeout)
+            return fail(MRG_ERR_CUDA, "a tensor-core kernel's barrier wait ran out");
         return fail(MRG_ERR_TRAVERSAL, (flag & mrg::kTraceStackOverflow) ? "traversal stack overflow"
                                        : (flag & mrg::kTraceBadIndex) ? "traversal read an out-of-range index"
                                                                       : "traversal step cap reached");

@@ -130,6 +130,11 @@ struct mrg_ctx
     mrg_hit_keys* dStageHits = nullptr;
     mrg_meta_hit* dStageMeta = nullptr;
     size_t        stageCap = 0;
+    // host-buffer cast pipeline: copy-in, cast and copy-out streams, and the
+    // events that chain one chunk through them
+    static constexpr int kHostMaxChunks = 32;
+    cudaStream_t  hostStreams[3] = { nullptr, nullptr, nullptr };
+    cudaEvent_t   hostEvents[2 * kHostMaxChunks] = {};
 };
 
 namespace mrg {

@@ -3,6 +3,7 @@
 // trained online with Adam.  No reference counterpart.
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace mrg {
@@ -41,12 +42,19 @@ struct NrcState
     float     lr, beta1, beta2, eps;
     // training scratch (capacity samples)
     uint16_t* acts;           // [cap][5][64] bf16: x0, a1, a2, a3, a4
-    float*    gz;             // [cap][4][64] fp32: g_z1..g_z4
-    float*    gy;             // [cap][16] fp32
+    uint16_t* g16;            // [cap][5][64] bf16: g_z1..g_z4, then dL/dy in columns 0..15 (16..63 stay 0)
     float4*   y;              // [cap] forward outputs of the training batch
     float*    loss;           // [1]
+    float*    wgPart;         // [partCtas][kNrcWeightCount]: per-CTA weight-gradient partials
+    uint32_t* err;            // sticky error word (a bounded wait that ran out sets kNrcWaitTimeout)
     uint32_t  cap;
+    uint32_t  partCtas;
+    // TMA descriptors of g16 and acts as 2D [cap rows][320 bf16], 64 x 128 boxes, 128-byte swizzle
+    CUtensorMap tmG16;
+    CUtensorMap tmActs;
 };
+
+constexpr uint32_t kNrcWaitTimeout = 8u;   // error bit, shared with the traversal error word
 
 size_t nrc_table_entries(const NrcGrid& g);
 void nrc_make_grid(NrcGrid& g, uint32_t levels, uint32_t log2Table, uint32_t baseRes, uint32_t maxRes,
@@ -68,5 +76,7 @@ cudaError_t nrc_gradients(NrcState& S, const float4* inputs, const float4* targe
                           uint32_t nMax, int smCount, cudaStream_t st);
 // bf16 / fp16 copies from the fp32 masters (after the host set them).
 cudaError_t nrc_sync_copies(const NrcState& S, cudaStream_t st);
+// Encodes S.tmG16 / S.tmActs for the allocated buffers (after g16 / acts / cap are set).
+cudaError_t nrc_make_tensor_maps(NrcState& S);
 
 } // namespace mrg

@@ -28,6 +28,7 @@ constexpr int kPad = 72;                      // padded row of 64 bf16
 constexpr int kPadT4 = 24;                    // padded row of W4^T (16 bf16)
 constexpr int kHiddenRows = 4 * kNrcWidth;    // rows of W0..W3
 constexpr int kActs = 5;                      // stored activations per training sample
+constexpr int kG16Row = kNrcLayers * kNrcWidth;  // bf16 per sample of the gradient rows
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 {
@@ -363,16 +364,17 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
                 }
             }
         }
-        // store gy rows (dW4 = gy x a4)
-        if(v0) { S.gy[(size_t)r0 * 16 + 2 * t] = gy[0][0]; S.gy[(size_t)r0 * 16 + 2 * t + 1] = gy[0][1];
-                 S.gy[(size_t)r0 * 16 + 8 + 2 * t] = gy[1][0]; S.gy[(size_t)r0 * 16 + 9 + 2 * t] = gy[1][1]; }
-        if(v1) { S.gy[(size_t)r1 * 16 + 2 * t] = gy[0][2]; S.gy[(size_t)r1 * 16 + 2 * t + 1] = gy[0][3];
-                 S.gy[(size_t)r1 * 16 + 8 + 2 * t] = gy[1][2]; S.gy[(size_t)r1 * 16 + 9 + 2 * t] = gy[1][3]; }
         uint32_t a[4][4];
         a[0][0] = pack_bf16(gy[0][0], gy[0][1]);
         a[0][1] = pack_bf16(gy[0][2], gy[0][3]);
         a[0][2] = pack_bf16(gy[1][0], gy[1][1]);
         a[0][3] = pack_bf16(gy[1][2], gy[1][3]);
+        // bf16 dL/dy rows for dW4 = gy^T a4 (slot 4, columns 0..15)
+        uint32_t* G16 = reinterpret_cast<uint32_t*>(S.g16);
+        if(v0) { G16[((size_t)r0 * kG16Row + 4 * kNrcWidth + 2 * t) / 2] = a[0][0];
+                 G16[((size_t)r0 * kG16Row + 4 * kNrcWidth + 8 + 2 * t) / 2] = a[0][2]; }
+        if(v1) { G16[((size_t)r1 * kG16Row + 4 * kNrcWidth + 2 * t) / 2] = a[0][1];
+                 G16[((size_t)r1 * kG16Row + 4 * kNrcWidth + 8 + 2 * t) / 2] = a[0][3]; }
         // ---- g_a4 = gy W4 (k = 16) ----
         float acc[8][4];
 #pragma unroll
@@ -406,11 +408,9 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
                     m3 = bf16_to_f((uint16_t)(p >> 16)) > 0.0f ? 1.0f : 0.0f;
                 }
                 acc[nt][0] *= m0; acc[nt][1] *= m1; acc[nt][2] *= m2; acc[nt][3] *= m3;
-                // store g_z{layer+1} (dW_layer = g_z{layer+1} x a_layer)
-                float* G = S.gz + (size_t)layer * kNrcWidth;
-                if(v0) { G[(size_t)r0 * 4 * kNrcWidth + c] = acc[nt][0]; G[(size_t)r0 * 4 * kNrcWidth + c + 1] = acc[nt][1]; }
-                if(v1) { G[(size_t)r1 * 4 * kNrcWidth + c] = acc[nt][2]; G[(size_t)r1 * 4 * kNrcWidth + c + 1] = acc[nt][3]; }
             }
+            // bf16 g_z{layer+1}: the A fragments of g_a_layer below and the rows of
+            // dW_layer = g_z{layer+1}^T a_layer (slot `layer`)
 #pragma unroll
             for(int kt = 0; kt < 4; kt++)
             {
@@ -418,6 +418,9 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
                 a[kt][1] = pack_bf16(acc[2 * kt][2], acc[2 * kt][3]);
                 a[kt][2] = pack_bf16(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
                 a[kt][3] = pack_bf16(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
+                const size_t col = (size_t)layer * kNrcWidth + 16 * kt + 2 * t;
+                if(v0) { G16[((size_t)r0 * kG16Row + col) / 2] = a[kt][0]; G16[((size_t)r0 * kG16Row + col + 8) / 2] = a[kt][2]; }
+                if(v1) { G16[((size_t)r1 * kG16Row + col) / 2] = a[kt][1]; G16[((size_t)r1 * kG16Row + col + 8) / 2] = a[kt][3]; }
             }
             // g_a_layer = g_z{layer+1} W_layer; at layer 0 only the hash columns (0..31) are needed
             const uint16_t* T = sT + layer * kNrcWidth * kPad;
@@ -482,56 +485,239 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
 }
 
 // ---------------------------------------------------------------------------
-// Weight gradients: dW_l[o][i] = sum_b G[b][o] A[b][i] on CUDA cores
+// Weight gradients on the 5th-generation tensor cores:
+//   dW_l[o][i] = sum_b G_l[b][o] A_l[b][i]
+// for the five layers at once.  The batch is the reduction dimension: each CTA
+// takes chunks of 128 samples (blockIdx.x, + gridDim.x, ...), and for every
+// (chunk, layer) item a TMA pair brings the G_l and A_l tiles (128 rows x 64
+// bf16, 128-byte swizzled) into one of four shared-memory stages.  One thread
+// issues tcgen05.mma (kind::f16, M = 64 outputs o, N = 64 inputs i, K = 16
+// samples, both operands MN-major) into the layer's 64 TMEM columns; a
+// tcgen05.commit frees the stage.  At the end every warp reads its TMEM lane
+// quarter (an M = 64 accumulator keeps row r in lane 32 (r / 16) + r % 16) and
+// writes the CTA's partial sums; k_nrc_wgrad_sum adds the partials into gW in
+// a fixed order, so the weight gradient is deterministic.
+// Every mbarrier wait is bounded by a clock deadline; one that runs out sets
+// kNrcWaitTimeout in S.err and the CTA drains its copies, frees its TMEM and
+// returns.
 // ---------------------------------------------------------------------------
-constexpr int kWgTile = 32;
+constexpr uint32_t kWgRows = 128;                        // samples per chunk
+constexpr uint32_t kWgStages = 4;
+constexpr uint32_t kWgTileBytes = kWgRows * kNrcWidth * 2;   // 16 KB
+constexpr uint32_t kWgStageBytes = 2 * kWgTileBytes;
+constexpr size_t kWgSmem = (size_t)kWgStages * kWgStageBytes + 1024;   // + alignment to 1024 B
+constexpr uint32_t kWgTmemCols = 512;                    // 5 layers x 64 fp32 columns, power of two
+constexpr uint32_t kWgThreads = 128;
+constexpr long long kWgWaitCycles = 2000000000ll;        // ~1 s at 2 GHz
+// tcgen05 instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A bf16
+// (bits 7-9 = 1), B bf16 (bits 10-12 = 1), A and B MN-major (bits 15, 16),
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kWgIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+                              ((64u >> 3) << 17) | ((64u >> 4) << 24);
 
-__global__ void __launch_bounds__(256)
-k_nrc_wgrad(NrcState S, const uint32_t* nDevice, uint32_t nMax, uint32_t chunk)
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor of an MN-major operand tile with a 128-byte
+// swizzle: start address >> 4 (bits 0-13), 8-row groups 1024 B apart (stride
+// byte offset, bits 32-45), descriptor version 1 (bit 46), swizzle mode 2 =
+// 128 B (bits 61-63).  The tile is one 64-element atom wide along M/N, so the
+// leading byte offset is unused (0).
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr)
 {
-    __shared__ float sGt[kWgTile][kNrcWidth];
-    __shared__ float sAt[kWgTile][kNrcWidth + 1];
-    const uint32_t layer = blockIdx.y;
-    const uint32_t n = nDevice ? min(*nDevice, nMax) : nMax;
-    const uint32_t b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
-    if(b0 >= b1) return;
-    const uint32_t rows = (layer == 4) ? kNrcOut : kNrcWidth;
-    const uint32_t o = threadIdx.x >> 2, i0 = (threadIdx.x & 3u) * 16u;
-    float acc[16];
-#pragma unroll
-    for(int j = 0; j < 16; j++) acc[j] = 0.0f;
-    for(uint32_t b = b0; b < b1; b += kWgTile)
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(1024u >> 4) << 32) | ((uint64_t)1 << 46) |
+           ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long deadline)
+{
+    for(;;)
     {
-        const uint32_t m = min((uint32_t)kWgTile, b1 - b);
-        for(uint32_t k = threadIdx.x; k < (uint32_t)kWgTile * kNrcWidth; k += 256)
-        {
-            const uint32_t r = k / kNrcWidth, c = k % kNrcWidth;
-            float gv = 0.0f, av = 0.0f;
-            if(r < m)
-            {
-                const size_t s = b + r;
-                if(layer == 4) gv = (c < (uint32_t)kNrcOut) ? S.gy[s * 16 + c] : 0.0f;
-                else gv = S.gz[s * 4 * kNrcWidth + (size_t)layer * kNrcWidth + c];
-                av = bf16_to_f(S.acts[s * kActs * kNrcWidth + (size_t)layer * kNrcWidth + c]);
-            }
-            sGt[r][c] = gv;
-            sAt[r][c] = av;
-        }
-        __syncthreads();
-        if(o < rows)
-            for(uint32_t r = 0; r < m; r++)
-            {
-                const float gv = sGt[r][o];
-#pragma unroll
-                for(int j = 0; j < 16; j++) acc[j] += gv * sAt[r][i0 + j];
-            }
-        __syncthreads();
+        uint32_t ok;
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if(ok) return true;
+        if(clock64() > deadline) return false;
     }
-    if(o < rows)
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                 :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t dTmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile("{ .reg .pred p; setp.ne.b32 p, %4, 0;\n"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }"
+                 :: "r"(dTmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate) : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kWgThreads, 1)
+k_nrc_wgrad_tc(const __grid_constant__ CUtensorMap tmG, const __grid_constant__ CUtensorMap tmA,
+               const uint32_t* __restrict__ nDevice, uint32_t nMax, float* __restrict__ part,
+               uint32_t* __restrict__ err)
+{
+    extern __shared__ uint8_t wgRaw[];
+    uint8_t* tiles = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(wgRaw) + 1023) & ~(uintptr_t)1023);
+    __shared__ uint64_t full[kWgStages], empty[kWgStages], done;
+    __shared__ uint32_t tmemSlot, aborted, issued, consumed;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const uint32_t n = nDevice ? min(*nDevice, nMax) : nMax;
+    const uint32_t chunks = (n + kWgRows - 1) / kWgRows;
+    const uint32_t myChunks = blockIdx.x < chunks ? (chunks - 1 - blockIdx.x) / gridDim.x + 1 : 0u;
+    const uint32_t items = myChunks * kNrcLayers;
+    if(items == 0u) return;
+
+    if(tid == 0u)
     {
-        float* dst = S.gW + (size_t)layer * kNrcWidth * kNrcWidth + (size_t)o * kNrcWidth + i0;
+        for(uint32_t s = 0; s < kWgStages; s++)
+        {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&empty[s])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        aborted = 0u; issued = 0u; consumed = 0u;
+    }
+    if(warp == 0u)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmemSlot)), "r"(kWgTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmemSlot;
+    const long long deadline = clock64() + kWgWaitCycles;
+
+    if(warp == 0u && lane == 0u)
+    {
+        // producer: TMA pairs into the stages
+        for(uint32_t it = 0; it < items; it++)
+        {
+            const uint32_t s = it % kWgStages, round = it / kWgStages;
+            if(!mbar_wait(smem_u32(&empty[s]), (round & 1u) ^ 1u, deadline)) { atomicExch(&aborted, 1u); break; }
+            if(*reinterpret_cast<volatile uint32_t*>(&aborted)) break;
+            const uint32_t chunk = blockIdx.x + (it / kNrcLayers) * gridDim.x, layer = it % kNrcLayers;
+            const uint32_t dst = smem_u32(tiles + s * kWgStageBytes), bar = smem_u32(&full[s]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(kWgStageBytes) : "memory");
+            tma_load_2d(dst, &tmG, (int)(layer * kNrcWidth), (int)(chunk * kWgRows), bar);
+            tma_load_2d(dst + kWgTileBytes, &tmA, (int)(layer * kNrcWidth), (int)(chunk * kWgRows), bar);
+            *reinterpret_cast<volatile uint32_t*>(&issued) = it + 1u;
+        }
+    }
+    else if(warp == 1u)
+    {
+        // MMA issuer: the warp waits and clears ragged rows, lane 0 issues
+        uint32_t it = 0;
+        for(; it < items; it++)
+        {
+            const uint32_t s = it % kWgStages, round = it / kWgStages;
+            if(!mbar_wait(smem_u32(&full[s]), round & 1u, deadline)) { if(lane == 0u) atomicExch(&aborted, 1u); break; }
+            const uint32_t chunk = blockIdx.x + (it / kNrcLayers) * gridDim.x, layer = it % kNrcLayers;
+            uint8_t* st = tiles + s * kWgStageBytes;
+            const uint32_t rows = min(kWgRows, n - chunk * kWgRows);
+            if(rows < kWgRows)
+            {
+                // rows past the batch hold stale samples: zero them in both tiles
+                const uint32_t units = (kWgRows - rows) * 8u;     // 16-byte units per tile
+                for(uint32_t q = lane; q < 2u * units; q += 32u)
+                {
+                    const uint32_t t = q / units, u = q % units;
+                    *reinterpret_cast<uint4*>(st + t * kWgTileBytes + rows * 128u + u * 16u) = make_uint4(0, 0, 0, 0);
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if(lane == 0u)
+            {
+                const uint32_t aG = smem_u32(st), aA = aG + kWgTileBytes;
 #pragma unroll
-        for(int j = 0; j < 16; j++) atomicAdd(dst + j, acc[j]);
+                for(uint32_t k = 0; k < kWgRows / 16u; k++)
+                    umma_f16(tmem + layer * kNrcWidth, umma_desc(aG + k * 2048u), umma_desc(aA + k * 2048u), kWgIdesc,
+                             (it >= (uint32_t)kNrcLayers || k > 0u) ? 1u : 0u);
+                umma_commit(smem_u32(&empty[s]));
+            }
+            __syncwarp();
+        }
+        if(lane == 0u)
+        {
+            *reinterpret_cast<volatile uint32_t*>(&consumed) = it;
+            umma_commit(smem_u32(&done));   // arrives once every MMA issued above has completed
+        }
+    }
+    __syncthreads();
+    const bool finished = mbar_wait(smem_u32(&done), 0u, deadline + kWgWaitCycles);
+    const bool ok = finished && !*reinterpret_cast<volatile uint32_t*>(&aborted);
+    if(!ok)
+    {
+        if(tid == 0u)
+        {
+            atomicOr(err, kNrcWaitTimeout);
+            // copies issued but never consumed may still be landing: wait for them
+            for(uint32_t it = consumed; it < issued; it++)
+                mbar_wait(smem_u32(&full[it % kWgStages]), (it / kWgStages) & 1u, clock64() + kWgWaitCycles);
+        }
+    }
+    else
+    {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        float* dst = part + (size_t)blockIdx.x * kNrcWeightCount;
+        const uint32_t row = 16u * warp + lane;          // lanes 0..15 of each quarter hold rows
+        for(uint32_t layer = 0; layer < (uint32_t)kNrcLayers; layer++)
+        {
+            const uint32_t rows = (layer == 4u) ? (uint32_t)kNrcOut : (uint32_t)kNrcWidth;
+#pragma unroll
+            for(uint32_t c = 0; c < (uint32_t)kNrcWidth; c += 16u)
+            {
+                uint32_t r[16];
+                tmem_ld16(tmem + ((32u * warp) << 16) + layer * kNrcWidth + c, r);
+                if(lane < 16u && row < rows)
+                {
+                    float4* o = reinterpret_cast<float4*>(dst + (size_t)layer * kNrcWidth * kNrcWidth +
+                                                          (size_t)row * kNrcWidth + c);
+#pragma unroll
+                    for(int q = 0; q < 4; q++)
+                        o[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
+                                           __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if(warp == 0u)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kWgTmemCols) : "memory");
+}
+
+// gW[i] += sum over the CTAs that had work, in CTA order.
+__global__ void k_nrc_wgrad_sum(const float* __restrict__ part, const uint32_t* __restrict__ nDevice, uint32_t nMax,
+                                uint32_t ctas, float* __restrict__ gW)
+{
+    const uint32_t n = nDevice ? min(*nDevice, nMax) : nMax;
+    const uint32_t used = min(ctas, (n + kWgRows - 1) / kWgRows);
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (uint32_t)kNrcWeightCount; i += gridDim.x * blockDim.x)
+    {
+        float acc = 0.0f;
+        for(uint32_t c = 0; c < used; c++) acc += part[(size_t)c * kNrcWeightCount + i];
+        gW[i] += acc;
     }
 }
 
@@ -667,13 +853,55 @@ cudaError_t nrc_gradients(NrcState& S, const float4* inputs, const float4* targe
         k_nrc_backward<<<grid, kTPB, kBwdSmem, st>>>(S, inputs, S.y, targets, nDevice, nMax);
         e = cudaGetLastError();
     }
-    const uint32_t chunk = 2048;
+    static bool wgConfigured = false;
+    if(e == cudaSuccess && !wgConfigured)
+    {
+        e = cudaFuncSetAttribute(k_nrc_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgSmem);
+        wgConfigured = e == cudaSuccess;
+    }
+    const uint32_t ctas = std::max(1u, std::min(S.partCtas, (nMax + kWgRows - 1) / kWgRows));
     if(e == cudaSuccess)
     {
-        k_nrc_wgrad<<<dim3((nMax + chunk - 1) / chunk, kNrcLayers), 256, 0, st>>>(S, nDevice, nMax, chunk);
+        k_nrc_wgrad_tc<<<ctas, kWgThreads, kWgSmem, st>>>(S.tmG16, S.tmActs, nDevice, nMax, S.wgPart, S.err);
+        e = cudaGetLastError();
+    }
+    if(e == cudaSuccess)
+    {
+        k_nrc_wgrad_sum<<<(kNrcWeightCount + 255) / 256, 256, 0, st>>>(S.wgPart, nDevice, nMax, ctas, S.gW);
         e = cudaGetLastError();
     }
     return e;
+}
+
+cudaError_t nrc_make_tensor_maps(NrcState& S)
+{
+    using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static Encode encode = nullptr;
+    if(!encode)
+    {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if(e != cudaSuccess) return e;
+        if(q != cudaDriverEntryPointSuccess || !fn) return cudaErrorSymbolNotFound;
+        encode = reinterpret_cast<Encode>(fn);
+    }
+    // [cap rows][5 x 64 bf16]: rows 640 B apart; a box is 64 bf16 (128 B, one
+    // swizzle span) by kWgRows rows; rows past cap read as zero.
+    const cuuint64_t dims[2] = { (cuuint64_t)kG16Row, (cuuint64_t)S.cap };
+    const cuuint64_t strides[1] = { (cuuint64_t)kG16Row * 2 };
+    const cuuint32_t box[2] = { (cuuint32_t)kNrcWidth, kWgRows };
+    const cuuint32_t elem[2] = { 1, 1 };
+    void* bases[2] = { S.g16, S.acts };
+    CUtensorMap* maps[2] = { &S.tmG16, &S.tmActs };
+    for(int k = 0; k < 2; k++)
+        if(encode(maps[k], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, bases[k], dims, strides, box, elem,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    return cudaSuccess;
 }
 
 cudaError_t nrc_sync_copies(const NrcState& S, cudaStream_t st)

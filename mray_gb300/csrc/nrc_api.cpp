@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -41,6 +42,22 @@ struct DevScope
     ~DevScope() { if(prev >= 0) cudaSetDevice(prev); }
 };
 
+// The cache kernels' bounded waits report through the context's error word.
+mrg_status wait_flag(mrg_ctx* c, const char* what)
+{
+    uint32_t flag = 0;
+    cudaError_t e = cudaMemcpy(&flag, c->cache.err, sizeof(flag), cudaMemcpyDeviceToHost);
+    if(e != cudaSuccess) return nrc_cuda(e, what);
+    if(flag & mrg::kNrcWaitTimeout)
+    {
+        const uint32_t rest = flag & ~mrg::kNrcWaitTimeout;
+        e = cudaMemcpy(c->cache.err, &rest, sizeof(rest), cudaMemcpyHostToDevice);
+        if(e != cudaSuccess) return nrc_cuda(e, what);
+        return mrg::set_error(MRG_ERR_CUDA, std::string(what) + ": a tensor-core kernel's barrier wait ran out");
+    }
+    return MRG_OK;
+}
+
 } // namespace
 
 extern "C" {
@@ -74,11 +91,17 @@ mrg_status mrg_cache_create(mrg_ctx* c, const mrg_cache_params* p)
     if(e == cudaSuccess) e = alloc(c, S.vT, nt);
     if(e == cudaSuccess) e = alloc(c, S.gT, nt);
     if(e == cudaSuccess) e = alloc(c, S.acts, (size_t)S.cap * 5 * mrg::kNrcWidth);
-    if(e == cudaSuccess) e = alloc(c, S.gz, (size_t)S.cap * 4 * mrg::kNrcWidth);
-    if(e == cudaSuccess) e = alloc(c, S.gy, (size_t)S.cap * 16);
+    if(e == cudaSuccess) e = alloc(c, S.g16, (size_t)S.cap * 5 * mrg::kNrcWidth);
     if(e == cudaSuccess) e = alloc(c, S.y, (size_t)S.cap);
     if(e == cudaSuccess) e = alloc(c, S.loss, 1);
+    S.partCtas = (uint32_t)std::max(1, c->smCount);
+    if(e == cudaSuccess) e = alloc(c, S.wgPart, (size_t)S.partCtas * mrg::kNrcWeightCount);
+    // the gradient rows' unused columns (slot 4, 16..63) must read as zero
+    if(e == cudaSuccess) e = cudaMemset(S.g16, 0, sizeof(uint16_t) * (size_t)S.cap * 5 * mrg::kNrcWidth);
+    if(e == cudaSuccess) e = cudaMemset(S.acts, 0, sizeof(uint16_t) * (size_t)S.cap * 5 * mrg::kNrcWidth);
+    if(e == cudaSuccess) e = mrg::nrc_make_tensor_maps(S);
     if(e != cudaSuccess) return nrc_cuda(e, "mrg_cache_create");
+    S.err = c->dScratch + 1;
     S.lr = p->learning_rate;
     S.beta1 = p->beta1; S.beta2 = p->beta2; S.eps = p->epsilon;
     S.step = 0;
@@ -124,6 +147,7 @@ mrg_status mrg_cache_train(mrg_ctx* c, const float* dIn, const float* dTarget, u
     {
         e = cudaMemcpyAsync(hLoss, c->cache.loss, sizeof(float), cudaMemcpyDeviceToHost, st);
         if(e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if(e == cudaSuccess) return wait_flag(c, "mrg_cache_train");
     }
     return e == cudaSuccess ? MRG_OK : nrc_cuda(e, "mrg_cache_train");
 }
@@ -145,7 +169,7 @@ mrg_status mrg_cache_gradients(mrg_ctx* c, const float* dIn, const float* dTarge
     if(e == cudaSuccess && hLoss) e = cudaMemcpy(hLoss, S.loss, sizeof(float), cudaMemcpyDeviceToHost);
     if(e == cudaSuccess) e = cudaMemset(S.gW, 0, sizeof(float) * mrg::kNrcWeightCount);
     if(e == cudaSuccess) e = cudaMemset(S.gT, 0, sizeof(float) * nt);
-    return e == cudaSuccess ? MRG_OK : nrc_cuda(e, "mrg_cache_gradients");
+    return e == cudaSuccess ? wait_flag(c, "mrg_cache_gradients") : nrc_cuda(e, "mrg_cache_gradients");
 }
 
 mrg_status mrg_cache_get_params(mrg_ctx* c, float* hW, float* hT)

@@ -3,8 +3,8 @@
 Project-written (MRay has no learned cache): the multiresolution hash-grid
 encoding (Mueller et al. 2022), the 5-layer 64-wide ReLU MLP without biases,
 the relative L2 loss and its gradients, in float64 numpy.  ``bf16=True``
-rounds what the GPU holds in BF16 (inputs, weights, activations, deltas) so
-that GPU results can be compared tightly; ``bf16=False`` is the plain FP64
+rounds what the GPU holds in BF16 (inputs, weights, activations, the
+per-sample gradient rows) so that GPU results can be compared tightly; ``bf16=False`` is the plain FP64
 model.
 """
 import numpy as np
@@ -131,12 +131,14 @@ class CacheRef:
         loss = float(np.sum((yy - t) ** 2 / den) / n)
         gy = np.zeros((n, 16))
         gy[:, :3] = 2.0 * (yy - t) / den / n
+        # with bf16, the per-sample gradient rows enter both the weight
+        # gradient and the next layer's data gradient rounded to bf16
         gW = [None] * 5
-        gW[4] = gy.T @ acts[4]
+        gW[4] = r(gy).T @ acts[4]
         g = r(gy) @ W[4]
         for l in range(3, -1, -1):
             g = g * (acts[l + 1] > 0)
-            gW[l] = g.T @ acts[l]
+            gW[l] = r(g).T @ acts[l]
             g = r(g) @ W[l]
         gX = g
         gT = np.zeros(len(np.asarray(table).ravel()))

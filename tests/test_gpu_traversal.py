@@ -184,6 +184,26 @@ def test_host_buffer_entry_point_matches_device():
     compare_closest(ora, (hr, hh, hm))
 
 
+@pytest.mark.parametrize("chunks", ["1", "7", "32"])
+def test_host_buffer_pipeline_chunks(chunks, monkeypatch):
+    """The host-buffer cast moves the rays through in chunks (copy-in, cast,
+    copy-out overlapped); any split gives the device-buffer results, and rays
+    that miss keep the caller's hit and meta values."""
+    pos, idx, m = small(4, 31)
+    acc, _ = build_pair(pos, idx, m)
+    rays = scenes.primary_rays(400, 250, 8, eye=(0, 0, -12), tan_half_fov=0.7)
+    pre = np.full((rays.shape[0], 4), 0xABCD, np.uint32)
+    want = gpu_closest(acc, rays, pre_hits=pre.copy())
+    monkeypatch.setenv("MRG_HOST_CHUNKS", chunks)
+    hr, hh = rays.copy(), pre.copy()
+    hm = np.zeros((rays.shape[0], 2), np.float32)
+    acc.cast_rays_host(hr, hh, hm)
+    assert np.array_equal(hr.view(np.uint32), want[0].view(np.uint32))
+    assert np.array_equal(hh, want[1])
+    assert np.array_equal(hm.view(np.uint32), want[2].view(np.uint32))
+    assert np.any(hh[:, 0] == 0xABCD) and np.any(hh[:, 0] != 0xABCD)
+
+
 def test_stress_scene_full_size_parity():
     """1.31M-triangle icosphere x 64 instances, 1920x1080 primary rays plus
     one diffuse bounce (~4M rays) and shadow rays: bit-exact against the
