@@ -454,6 +454,49 @@ def c4_equal_time(args, dev, spp_per_frame=8):
     return out
 
 
+def cache_micro(args, dev):
+    """Radiance cache alone (16 levels x 2^19 x 2 hash grid, 5 x 64-wide MLP):
+    one optimisation step on 65,536 (input, target) samples (forward,
+    backward, tensor-core weight gradient, Adam) and a 2,073,600-sample query
+    (one 1080p frame), device-timed with CUDA events."""
+    import torch
+    from mray_gb300.cache import RadianceCache
+    rng = np.random.default_rng(0)
+
+    def batch(n):
+        x = np.zeros((n, 16), np.float32)
+        x[:, 0:3] = rng.random((n, 3)) * 4 - 2
+        x[:, 3] = rng.random(n)
+        d = rng.standard_normal((n, 3))
+        x[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+        x[:, 8:11] = x[:, 4:7]
+        x[:, 12:15] = rng.random((n, 3))
+        return torch.from_numpy(x).to(dev)
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps
+
+    c = RadianceCache(device=dev.index or 0, aabb=(-2, -2, -2, 2, 2, 2), max_batch=65536)
+    xb, tb = batch(65536), torch.rand((65536, 4), device=dev)
+    reps = max(3, min(args.steps, 50))
+    train_ms = timed(lambda: c.train(xb, tb, loss=False), reps)
+    xq = batch(2073600)
+    out = torch.empty((2073600, 4), dtype=torch.float32, device=dev)
+    query_ms = timed(lambda: c.query(xq, out=out), reps)
+    c.close()
+    return {"cache_train_step_ms_65536": round(train_ms, 4), "cache_query_ms_2073600": round(query_ms, 4),
+            "cache_query_msamples_per_s": round(2073600 / (query_ms * 1e-3) / 1e6, 1)}
+
+
 def oracle_scene(pos, idx, m):
     import oracle
     S = oracle.Scene()
@@ -539,7 +582,7 @@ def only_workload(args):
     B.build()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    fn = {"c0": box_scene_pt, "c2": c2_scene_pt, "c3": c3_adjoint, "c4": c4_equal_time}[args.only]
+    fn = {"c0": box_scene_pt, "c2": c2_scene_pt, "c3": c3_adjoint, "c4": c4_equal_time, "cache": cache_micro}[args.only]
     print(json.dumps({"workload": args.only, **fn(args, dev)}))
 
 
@@ -553,7 +596,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pt-extras", action="store_true",
                     help="skip the production-scene and adjoint path-tracing lines")
-    ap.add_argument("--only", choices=["c0", "c2", "c3", "c4"], default=None,
+    ap.add_argument("--only", choices=["c0", "c2", "c3", "c4", "cache"], default=None,
                     help="run one path-tracing workload alone and print its line (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":

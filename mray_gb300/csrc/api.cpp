@@ -178,6 +178,7 @@ mrg_status mrg_destroy(mrg_ctx* c)
     for(void* q : c->cacheAllocs) cudaFree(q);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
     for(cudaStream_t& q : c->hostStreams) if(q) cudaStreamDestroy(q);
+    cudaFree(c->dHostCounters);
     for(cudaEvent_t& q : c->hostEvents) if(q) cudaEventDestroy(q);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);
     delete c;
@@ -454,14 +455,21 @@ mrg_status mrg_cast_closest_host(mrg_ctx* c, mrg_ray* hRays, uint32_t n, mrg_hit
             MRG_TRY(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking), "mrg_cast_closest_host: streams");
         for(cudaEvent_t& q : c->hostEvents)
             MRG_TRY(cudaEventCreateWithFlags(&q, cudaEventDisableTiming), "mrg_cast_closest_host: events");
+        MRG_TRY(cudaMalloc(&c->dHostCounters, sizeof(uint32_t) * mrg_ctx::kHostMaxChunks), "mrg_cast_closest_host: counters");
     }
     // The ray set goes through in chunks: while chunk k is cast, chunk k+1
     // is copied in and chunk k-1 copied out (copy engines in both directions
-    // run beside the SMs).  Each chunk owns its slice of the staging buffers.
+    // run beside the SMs).  Casts alternate between two streams, each chunk
+    // with its own ray-claim counter, so chunk k+1's blocks take the SMs that
+    // chunk k's last rays leave idle.  Each chunk owns its slice of the
+    // staging buffers.
     const uint32_t chunks = host_chunks(n);
-    cudaStream_t sIn = c->hostStreams[0], sCast = c->hostStreams[1], sOut = c->hostStreams[2];
+    cudaStream_t sIn = c->hostStreams[0], sOut = c->hostStreams[3];
     for(uint32_t k = 0; k < chunks; k++)
     {
+        cudaStream_t sCast = c->hostStreams[1 + (k & 1u)];
+        mrg::TraceScratch scr = scratch_of(c);
+        scr.workCounter = c->dHostCounters + k;
         const size_t off = (size_t)n * k / chunks, cnt = (size_t)n * (k + 1) / chunks - off;
         if(cnt == 0) continue;
         cudaEvent_t copied = c->hostEvents[2 * k], cast = c->hostEvents[2 * k + 1];
@@ -470,7 +478,7 @@ mrg_status mrg_cast_closest_host(mrg_ctx* c, mrg_ray* hRays, uint32_t n, mrg_hit
         MRG_TRY(cudaMemcpyAsync(c->dStageMeta + off, hMeta + off, sizeof(mrg_meta_hit) * cnt, cudaMemcpyHostToDevice, sIn), "H2D meta");
         MRG_TRY(cudaEventRecord(copied, sIn), "event");
         MRG_TRY(cudaStreamWaitEvent(sCast, copied, 0), "event wait");
-        MRG_TRY(mrg::launch_closest(c->scene, scratch_of(c), c->dStageRays + off, nullptr, (uint32_t)cnt,
+        MRG_TRY(mrg::launch_closest(c->scene, scr, c->dStageRays + off, nullptr, (uint32_t)cnt,
                                     c->dStageHits + off, c->dStageMeta + off, c->smCount, sCast), "cast");
         MRG_TRY(cudaEventRecord(cast, sCast), "event");
         MRG_TRY(cudaStreamWaitEvent(sOut, cast, 0), "event wait");

@@ -133,8 +133,9 @@ struct mrg_ctx
     // host-buffer cast pipeline: copy-in, cast and copy-out streams, and the
     // events that chain one chunk through them
     static constexpr int kHostMaxChunks = 32;
-    cudaStream_t  hostStreams[3] = { nullptr, nullptr, nullptr };
+    cudaStream_t  hostStreams[4] = { nullptr, nullptr, nullptr, nullptr };   // in, cast A, cast B, out
     cudaEvent_t   hostEvents[2 * kHostMaxChunks] = {};
+    uint32_t*     dHostCounters = nullptr;       // one ray-claim counter per chunk
 };
 
 namespace mrg {
