@@ -248,31 +248,73 @@ mrg_status mrg_build(mrg_ctx* c)
     cudaStream_t st = c->buildStream;
     std::string err;
 
-    // 1. one BLAS per mesh
-    std::vector<mrg::BuildResult> blas(c->meshes.size());
-    for(size_t mi = 0; mi < c->meshes.size(); mi++)
+    // 1. BLASes: every mesh in one batched build (PLOC: one build per mesh).
+    //    A piece is a node / triangle block placed into the shared arrays;
+    //    meshRoot[m] is mesh m's root within its piece.
+    struct Piece { mrg::WideNode* nodes; uint32_t nodeCount; mrg::TriRecord* tris; uint32_t payloadCount; };
+    std::vector<Piece> pieces;
+    std::vector<uint32_t> pieceOf(c->meshes.size()), meshRoot(c->meshes.size());
+    auto free_pieces = [&]() { for(auto& p : pieces) { cudaFree(p.nodes); cudaFree(p.tris); } };
     {
-        auto& m = c->meshes[mi];
-        float* dPos = nullptr; uint32_t* dIdx = nullptr;
-        MRG_TRY(cudaMalloc(&dPos, sizeof(float) * m.pos.size()), "mrg_build: mesh upload");
-        cudaError_t e = cudaMalloc(&dIdx, sizeof(uint32_t) * m.idx.size());
-        if(e == cudaSuccess) e = cudaMemcpyAsync(dPos, m.pos.data(), sizeof(float) * m.pos.size(), cudaMemcpyHostToDevice, st);
-        if(e == cudaSuccess) e = cudaMemcpyAsync(dIdx, m.idx.data(), sizeof(uint32_t) * m.idx.size(), cudaMemcpyHostToDevice, st);
-        if(e != cudaSuccess) { cudaFree(dPos); cudaFree(dIdx); return cuda_fail(e, "mrg_build: mesh upload"); }
-        mrg::BuildInput bi;
-        bi.kind = 0; bi.pos = dPos; bi.idx = dIdx;
-        bi.count = (uint32_t)(m.idx.size() / 3);
-        bi.primKeyBase = m.primKeyBase;
-        bi.maxLeaf = leaf_size(bi.count);
-        bi.ploc = use_ploc();
-        bool ok = mrg::build_wide_bvh(bi, blas[mi], st, err);
-        cudaFree(dPos); cudaFree(dIdx);
-        if(!ok)
+        const size_t M = c->meshes.size();
+        std::vector<float*> dPos(M, nullptr);
+        std::vector<uint32_t*> dIdx(M, nullptr);
+        auto free_uploads = [&]() { for(size_t i = 0; i < M; i++) { cudaFreeAsync(dPos[i], st); cudaFreeAsync(dIdx[i], st); } };
+        cudaError_t e = cudaSuccess;
+        for(size_t mi = 0; mi < M && e == cudaSuccess; mi++)
         {
-            for(auto& b : blas) { cudaFree(b.nodes); cudaFree(b.tris); }
-            return fail(MRG_ERR_CUDA, "mrg_build: BLAS build: " + err);
+            auto& m = c->meshes[mi];
+            e = cudaMallocAsync(&dPos[mi], sizeof(float) * m.pos.size(), st);
+            if(e == cudaSuccess) e = cudaMallocAsync(&dIdx[mi], sizeof(uint32_t) * m.idx.size(), st);
+            if(e == cudaSuccess) e = cudaMemcpyAsync(dPos[mi], m.pos.data(), sizeof(float) * m.pos.size(), cudaMemcpyHostToDevice, st);
+            if(e == cudaSuccess) e = cudaMemcpyAsync(dIdx[mi], m.idx.data(), sizeof(uint32_t) * m.idx.size(), cudaMemcpyHostToDevice, st);
         }
-        std::memcpy(m.box, blas[mi].box, sizeof(m.box));
+        if(e != cudaSuccess) { free_uploads(); cudaStreamSynchronize(st); return cuda_fail(e, "mrg_build: mesh upload"); }
+        if(!use_ploc())
+        {
+            std::vector<mrg::BatchMeshInput> in(M);
+            for(size_t mi = 0; mi < M; mi++)
+            {
+                const auto& m = c->meshes[mi];
+                in[mi].pos = dPos[mi]; in[mi].idx = dIdx[mi];
+                in[mi].count = (uint32_t)(m.idx.size() / 3);
+                in[mi].primKeyBase = m.primKeyBase;
+                in[mi].maxLeaf = leaf_size(in[mi].count);
+            }
+            mrg::BatchResult br;
+            const bool ok = mrg::build_wide_bvh_batch(in, br, st, err);
+            free_uploads();
+            if(!ok) { cudaStreamSynchronize(st); return fail(MRG_ERR_CUDA, "mrg_build: BLAS build: " + err); }
+            pieces.push_back(Piece{ br.nodes, br.nodeCount, br.tris, br.payloadCount });
+            for(size_t mi = 0; mi < M; mi++)
+            {
+                pieceOf[mi] = 0; meshRoot[mi] = (uint32_t)mi;
+                std::memcpy(c->meshes[mi].box, &br.boxes[6 * mi], sizeof(c->meshes[mi].box));
+            }
+        }
+        else
+        {
+            for(size_t mi = 0; mi < M; mi++)
+            {
+                auto& m = c->meshes[mi];
+                mrg::BuildInput bi;
+                bi.kind = 0; bi.pos = dPos[mi]; bi.idx = dIdx[mi];
+                bi.count = (uint32_t)(m.idx.size() / 3);
+                bi.primKeyBase = m.primKeyBase;
+                bi.maxLeaf = leaf_size(bi.count);
+                bi.ploc = true;
+                mrg::BuildResult b;
+                if(!mrg::build_wide_bvh(bi, b, st, err))
+                {
+                    free_uploads(); free_pieces(); cudaStreamSynchronize(st);
+                    return fail(MRG_ERR_CUDA, "mrg_build: BLAS build: " + err);
+                }
+                pieceOf[mi] = (uint32_t)pieces.size(); meshRoot[mi] = 0;
+                pieces.push_back(Piece{ b.nodes, b.nodeCount, b.tris, b.payloadCount });
+                std::memcpy(m.box, b.box, sizeof(m.box));
+            }
+            free_uploads();
+        }
     }
 
     // 2. instance world boxes + TLAS
@@ -295,7 +337,7 @@ mrg_status mrg_build(mrg_ctx* c)
         if(e != cudaSuccess)
         {
             cudaFree(dBoxes);
-            for(auto& b : blas) { cudaFree(b.nodes); cudaFree(b.tris); }
+            free_pieces();
             return cuda_fail(e, "mrg_build: instance boxes");
         }
         mrg::BuildInput bi;
@@ -305,14 +347,14 @@ mrg_status mrg_build(mrg_ctx* c)
         cudaFree(dBoxes);
         if(!ok)
         {
-            for(auto& b : blas) { cudaFree(b.nodes); cudaFree(b.tris); }
+            free_pieces();
             return fail(MRG_ERR_CUDA, "mrg_build: TLAS build: " + err);
         }
     }
 
     // 3. place everything in shared arrays
     uint64_t totalNodes = 0, totalTris = 0;
-    for(auto& b : blas) { totalNodes += b.nodeCount; totalTris += b.payloadCount; }
+    for(auto& b : pieces) { totalNodes += b.nodeCount; totalTris += b.payloadCount; }
     const uint64_t tlasOff = totalNodes;
     totalNodes += tlas.nodeCount;
     cudaError_t e = cudaMalloc(&c->dNodes, mrg::kWideNodeBytes * totalNodes);
@@ -320,10 +362,11 @@ mrg_status mrg_build(mrg_ctx* c)
     if(e == cudaSuccess) e = cudaMalloc(&c->dInsts, sizeof(mrg::HostInstRecord) * ni);
     if(e == cudaSuccess) e = cudaMalloc(&c->dTlasLeaf, sizeof(uint32_t) * ni);
     uint64_t nodeOff = 0, triOff = 0;
-    for(size_t mi = 0; mi < blas.size() && e == cudaSuccess; mi++)
+    std::vector<uint64_t> pieceNodeOff(pieces.size());
+    for(size_t pi = 0; pi < pieces.size() && e == cudaSuccess; pi++)
     {
-        auto& b = blas[mi];
-        c->meshes[mi].rootNode = (uint32_t)nodeOff;
+        auto& b = pieces[pi];
+        pieceNodeOff[pi] = nodeOff;
         if(!mrg::relocate_nodes(b.nodes, reinterpret_cast<mrg::WideNode*>(
                                     static_cast<char*>(c->dNodes) + mrg::kWideNodeBytes * nodeOff),
                                 b.nodeCount, (uint32_t)nodeOff, (uint32_t)triOff, st))
@@ -333,6 +376,8 @@ mrg_status mrg_build(mrg_ctx* c)
                                 mrg::kTriRecordBytes * b.payloadCount, cudaMemcpyDeviceToDevice, st);
         nodeOff += b.nodeCount; triOff += b.payloadCount;
     }
+    for(size_t mi = 0; mi < c->meshes.size(); mi++)
+        c->meshes[mi].rootNode = (uint32_t)(pieceNodeOff[pieceOf[mi]] + meshRoot[mi]);
     if(e == cudaSuccess &&
        !mrg::relocate_nodes(tlas.nodes, reinterpret_cast<mrg::WideNode*>(
                                 static_cast<char*>(c->dNodes) + mrg::kWideNodeBytes * tlasOff),
@@ -364,7 +409,7 @@ mrg_status mrg_build(mrg_ctx* c)
     if(e == cudaSuccess)
         e = cudaMemcpyAsync(c->dInsts, recs.data(), sizeof(mrg::HostInstRecord) * ni, cudaMemcpyHostToDevice, st);
     if(e == cudaSuccess) e = cudaStreamSynchronize(st);
-    for(auto& b : blas) { cudaFree(b.nodes); cudaFree(b.tris); }
+    free_pieces();
     cudaFree(tlas.nodes); cudaFree(tlas.leafIds);
     if(e != cudaSuccess) { free_accel(c); return cuda_fail(e, "mrg_build: placement"); }
 

@@ -19,6 +19,7 @@
 
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
+#include <algorithm>
 #include <cfloat>
 #include <vector>
 #include <cstring>
@@ -41,6 +42,32 @@ struct BoxF
     float mn[3];
     float mx[3];
 };
+
+// One mesh of a batched BLAS build: its triangles are leaves
+// [first, first + count) of the concatenated leaf arrays.
+struct MeshSeg
+{
+    const float*    pos;
+    const uint32_t* idx;
+    uint32_t        first;
+    uint32_t        count;
+    uint32_t        primKeyBase;
+    uint32_t        maxLeaf;
+    float           inflate;
+    uint32_t        pad;
+};
+
+// Mesh of sorted leaf position p in a batched build (firsts: nMesh + 1 offsets).
+__device__ __forceinline__ uint32_t mesh_of(const uint32_t* __restrict__ firsts, uint32_t nMesh, uint32_t p)
+{
+    uint32_t lo = 0, hi = nMesh;      // firsts[lo] <= p < firsts[hi]
+    while(hi - lo > 1u)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if(firsts[mid] <= p) lo = mid; else hi = mid;
+    }
+    return lo;
+}
 
 __device__ __forceinline__ uint32_t f2ord(float f)
 {
@@ -138,6 +165,100 @@ __global__ void k_morton(const float* __restrict__ cent, const uint32_t* __restr
     ids[i] = i;
 }
 
+// Batched BLAS build, leaves of every mesh: box, centroid, per-mesh centroid
+// bounds.  A block whose leaves all belong to one mesh reduces in shared
+// memory first; a block that straddles meshes uses per-leaf atomics.
+__global__ void k_leaf_boxes_multi(const MeshSeg* __restrict__ segs, const uint32_t* __restrict__ firsts,
+                                   uint32_t nMesh, uint32_t n, BoxF* __restrict__ boxes, float* __restrict__ cent,
+                                   uint32_t* __restrict__ cbounds, uint32_t* __restrict__ leafMesh)
+{
+    __shared__ uint32_t sb[6];
+    __shared__ uint32_t blockMesh;
+    const uint32_t b0 = blockIdx.x * blockDim.x;
+    const uint32_t b1 = min(n, b0 + blockDim.x) - 1u;
+    if(threadIdx.x < 6) sb[threadIdx.x] = (threadIdx.x < 3) ? 0xFFFFFFFFu : 0u;
+    if(threadIdx.x == 0)
+    {
+        const uint32_t m0 = mesh_of(firsts, nMesh, b0), m1 = mesh_of(firsts, nMesh, b1);
+        blockMesh = (m0 == m1) ? m0 : 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    const uint32_t i = b0 + threadIdx.x;
+    if(i < n)
+    {
+        const uint32_t m = mesh_of(firsts, nMesh, i);
+        const MeshSeg& sg = segs[m];
+        const uint32_t t = i - sg.first;
+        const uint32_t a = sg.idx[3 * t], b = sg.idx[3 * t + 1], c = sg.idx[3 * t + 2];
+        BoxF bx;
+        for(int k = 0; k < 3; k++)
+        {
+            const float va = sg.pos[3 * a + k], vb = sg.pos[3 * b + k], vc = sg.pos[3 * c + k];
+            bx.mn[k] = fminf(va, fminf(vb, vc));
+            bx.mx[k] = fmaxf(va, fmaxf(vb, vc));
+            const float cc = 0.5f * (bx.mn[k] + bx.mx[k]);
+            cent[3 * i + k] = cc;
+            if(blockMesh != 0xFFFFFFFFu)
+            {
+                atomicMin(&sb[k], f2ord(cc));
+                atomicMax(&sb[3 + k], f2ord(cc));
+            }
+            else
+            {
+                atomicMin(&cbounds[6 * m + k], f2ord(cc));
+                atomicMax(&cbounds[6 * m + 3 + k], f2ord(cc));
+            }
+        }
+        boxes[i] = bx;
+        leafMesh[i] = m;
+    }
+    __syncthreads();
+    if(blockMesh != 0xFFFFFFFFu)
+    {
+        if(threadIdx.x < 3) atomicMin(&cbounds[6 * blockMesh + threadIdx.x], sb[threadIdx.x]);
+        else if(threadIdx.x < 6) atomicMax(&cbounds[6 * blockMesh + threadIdx.x], sb[threadIdx.x]);
+    }
+}
+
+// Keys of a batched build: mesh id above a Morton code of `bits` bits per
+// axis, quantised in the mesh's own centroid bounds.  With one mesh (no id
+// bits, 21 bits per axis) the keys equal k_morton's.
+__global__ void k_morton_multi(const float* __restrict__ cent, const uint32_t* __restrict__ cbounds,
+                               const uint32_t* __restrict__ leafMesh, uint32_t n, uint32_t bits,
+                               uint64_t* __restrict__ codes, uint32_t* __restrict__ ids)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    const uint32_t m = leafMesh[i];
+    const float qmax = (float)((1u << bits) - 1u);
+    uint32_t q[3];
+    for(int k = 0; k < 3; k++)
+    {
+        const float lo = ord2f(cbounds[6 * m + k]), hi = ord2f(cbounds[6 * m + 3 + k]);
+        const float ext = hi - lo;
+        const float sc = (ext > 0.0f) ? (qmax / ext) : 0.0f;
+        float v = (cent[3 * i + k] - lo) * sc;
+        v = fminf(fmaxf(v, 0.0f), qmax);
+        q[k] = (uint32_t)v;
+    }
+    const uint64_t morton = expand21(q[0]) | (expand21(q[1]) << 1) | (expand21(q[2]) << 2);
+    codes[i] = ((uint64_t)m << (3u * bits)) | morton;
+    ids[i] = i;
+}
+
+// Root box of every mesh of a batched build (a leaf root for one-triangle meshes).
+__global__ void k_mesh_boxes(const uint32_t* __restrict__ meshRoot, uint32_t nMesh, const BoxF* __restrict__ nodeBoxes,
+                             const BoxF* __restrict__ leafBoxes, const uint32_t* __restrict__ sortedIds, uint32_t n,
+                             BoxF* __restrict__ out, uint32_t* errorFlag)
+{
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if(m >= nMesh) return;
+    const uint32_t r = meshRoot[m];
+    const uint32_t ix = r & ~kLeafBit;
+    if(r == kNoParent || ((r & kLeafBit) ? ix >= n : ix + 1u >= n)) { atomicOr(errorFlag, 1u); return; }
+    out[m] = (r & kLeafBit) ? leafBoxes[sortedIds[ix]] : nodeBoxes[ix];
+}
+
 __device__ __forceinline__ int k_delta(const uint64_t* __restrict__ c, int n, int i, int j)
 {
     if(j < 0 || j >= n) return -1;
@@ -146,9 +267,13 @@ __device__ __forceinline__ int k_delta(const uint64_t* __restrict__ c, int n, in
     return __clzll(a ^ b);
 }
 
-// Karras 2012, "Maximizing parallelism in the construction of BVHs".
+// Karras 2012, "Maximizing parallelism in the construction of BVHs".  In a
+// batched build (firsts != null) the mesh id heads every key, so each mesh's
+// leaves form one subtree; the node whose range is exactly a mesh's leaves
+// is recorded as that mesh's root.
 __global__ void k_karras(const uint64_t* __restrict__ codes, int n, BinNode* __restrict__ nodes,
-                         uint32_t* __restrict__ leafParent)
+                         uint32_t* __restrict__ leafParent, const uint32_t* __restrict__ firsts,
+                         uint32_t nMesh, uint32_t* __restrict__ meshRoot)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= n - 1) return;
@@ -176,6 +301,11 @@ __global__ void k_karras(const uint64_t* __restrict__ codes, int n, BinNode* __r
     if(hi == gamma + 1) { me.right = kLeafBit | (uint32_t)(gamma + 1); leafParent[gamma + 1] = (uint32_t)i; }
     else                { me.right = (uint32_t)(gamma + 1); nodes[gamma + 1].parent = (uint32_t)i; }
     if(i == 0) me.parent = kNoParent;
+    if(firsts)
+    {
+        const uint32_t m = mesh_of(firsts, nMesh, (uint32_t)lo);
+        if((uint32_t)lo == firsts[m] && (uint32_t)hi + 1u == firsts[m + 1]) meshRoot[m] = (uint32_t)i;
+    }
 }
 
 // Bottom-up boxes and leaf counts.  The second thread to reach a node merges
@@ -313,6 +443,7 @@ __global__ void k_ploc_compact(const uint32_t* __restrict__ keep, const uint32_t
 
 struct CollapseArgs
 {
+    const MeshSeg*  segs;       // batched builds: per-mesh payload, leaf size, inflation (else null)
     const BinNode*  nodes;
     const BoxF*     nodeBoxes;
     const BoxF*     leafBoxes;
@@ -362,30 +493,43 @@ __device__ __forceinline__ float half_area(const BoxF& b)
     return dx * dy + dy * dz + dz * dx;
 }
 
-__device__ __forceinline__ void emit_payload(const CollapseArgs& a, uint32_t leafPos, uint32_t dst)
+__device__ __forceinline__ void emit_payload(const CollapseArgs& a, uint32_t leafPos, uint32_t dst, uint32_t mesh)
 {
     uint32_t prim = a.sortedIds[leafPos];
     if(a.kind == 1) { a.leafIds[dst] = prim; return; }
-    uint32_t i0 = a.idx[3 * prim], i1 = a.idx[3 * prim + 1], i2 = a.idx[3 * prim + 2];
-    float v0x = a.pos[3 * i0], v0y = a.pos[3 * i0 + 1], v0z = a.pos[3 * i0 + 2];
-    float v1x = a.pos[3 * i1], v1y = a.pos[3 * i1 + 1], v1z = a.pos[3 * i1 + 2];
-    float v2x = a.pos[3 * i2], v2y = a.pos[3 * i2 + 1], v2z = a.pos[3 * i2 + 2];
+    const float* pos = a.pos;
+    const uint32_t* idx = a.idx;
+    uint32_t keyBase = a.primKeyBase;
+    if(a.segs)
+    {
+        const MeshSeg& m = a.segs[mesh];
+        prim -= m.first;
+        pos = m.pos; idx = m.idx; keyBase = m.primKeyBase;
+    }
+    uint32_t i0 = idx[3 * prim], i1 = idx[3 * prim + 1], i2 = idx[3 * prim + 2];
+    float v0x = pos[3 * i0], v0y = pos[3 * i0 + 1], v0z = pos[3 * i0 + 2];
+    float v1x = pos[3 * i1], v1y = pos[3 * i1 + 1], v1z = pos[3 * i1 + 2];
+    float v2x = pos[3 * i2], v2y = pos[3 * i2 + 1], v2z = pos[3 * i2 + 2];
     TriRecord r;
-    r.v0 = make_float4(v0x, v0y, v0z, __uint_as_float(a.primKeyBase + prim));
+    r.v0 = make_float4(v0x, v0y, v0z, __uint_as_float(keyBase + prim));
     r.e0 = make_float4(__fsub_rn(v1x, v0x), __fsub_rn(v1y, v0y), __fsub_rn(v1z, v0z), 0.0f);
     r.e1 = make_float4(__fsub_rn(v2x, v0x), __fsub_rn(v2y, v0y), __fsub_rn(v2z, v0z), 0.0f);
     a.tris[dst] = r;
 }
 
-// One thread per wide node of the current level.
-__global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint32_t qn,
-                           uint2* __restrict__ nextQueue)
+// One thread per wide node of the current level.  Queue items: binary node
+// (or leaf) reference, wide node index, mesh of a batched build.
+__global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint32_t qn,
+                           uint4* __restrict__ nextQueue)
 {
     uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if(w >= qn) return;
-    uint2 item = queue[w];
+    uint4 item = queue[w];
     uint32_t root = item.x;
     uint32_t wideIdx = item.y;
+    const uint32_t mesh = item.z;
+    const uint32_t maxLeaf = a.segs ? a.segs[mesh].maxLeaf : a.maxLeaf;
+    const float inflate = a.segs ? a.segs[mesh].inflate : a.inflate;
 
     uint32_t cand[8];
     BoxF cbox[8];
@@ -393,7 +537,7 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
     int nc = 0;
     BoxF nbox; uint32_t ncnt;
     ref_box(a, root, nbox, ncnt);
-    if((root & kLeafBit) || ncnt <= a.maxLeaf)
+    if((root & kLeafBit) || ncnt <= maxLeaf)
     {
         cand[0] = root; cbox[0] = nbox; ccnt[0] = ncnt; nc = 1;
     }
@@ -408,7 +552,7 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
             int best = -1; float bestA = -1.0f;
             for(int c = 0; c < nc; c++)
             {
-                if((cand[c] & kLeafBit) || ccnt[c] <= a.maxLeaf) continue;
+                if((cand[c] & kLeafBit) || ccnt[c] <= maxLeaf) continue;
                 float ar = half_area(cbox[c]);
                 if(ar > bestA) { bestA = ar; best = c; }
             }
@@ -430,8 +574,8 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
     float invS[3];
     for(int k = 0; k < 3; k++)
     {
-        float lo = __fsub_rd(nbox.mn[k], a.inflate);
-        float hi = __fadd_ru(nbox.mx[k], a.inflate);
+        float lo = __fsub_rd(nbox.mn[k], inflate);
+        float hi = __fadd_ru(nbox.mx[k], inflate);
         float ext = __fsub_ru(hi, lo);
         float x = __fdiv_ru(ext, 252.0f);
         uint32_t bits = __float_as_uint(x);
@@ -478,7 +622,7 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
     uint32_t numInternal = 0, numPayload = 0;
     for(int c = 0; c < nc; c++)
     {
-        bool leaf = (cand[c] & kLeafBit) || ccnt[c] <= a.maxLeaf;
+        bool leaf = (cand[c] & kLeafBit) || ccnt[c] <= maxLeaf;
         if(leaf) numPayload += ccnt[c]; else numInternal++;
     }
     uint32_t childBase = numInternal ? atomicAdd(&a.counters[0], numInternal) : 0u;
@@ -505,19 +649,19 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
         }
         for(int k = 0; k < 3; k++)
         {
-            float lo = __fsub_rd(cbox[c].mn[k], a.inflate);
-            float hi = __fadd_ru(cbox[c].mx[k], a.inflate);
+            float lo = __fsub_rd(cbox[c].mn[k], inflate);
+            float hi = __fadd_ru(cbox[c].mx[k], inflate);
             float ql = floorf(__fmul_rd(__fsub_rd(lo, px[k]), invS[k])) - 1.0f;
             float qh = ceilf(__fmul_ru(__fsub_ru(hi, px[k]), invS[k])) + 1.0f;
             qlo[k][s] = (uint8_t)fminf(fmaxf(ql, 0.0f), 255.0f);
             qhi[k][s] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
         }
-        bool leaf = (cand[c] & kLeafBit) || ccnt[c] <= a.maxLeaf;
+        bool leaf = (cand[c] & kLeafBit) || ccnt[c] <= maxLeaf;
         if(!leaf)
         {
             imask |= 1u << s;
             meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
-            nextQueue[qBase + rank] = make_uint2(cand[c], childBase + rank);
+            nextQueue[qBase + rank] = make_uint4(cand[c], childBase + rank, mesh, 0u);
             rank++;
         }
         else
@@ -533,7 +677,7 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ queue, uint
                 if(!ref_ok(a, r)) continue;
                 if(r & kLeafBit)
                 {
-                    if(m < k) emit_payload(a, r & ~kLeafBit, triBase + triOff + m);
+                    if(m < k) emit_payload(a, r & ~kLeafBit, triBase + triOff + m, mesh);
                     else atomicOr(&a.counters[3], 4u);
                     m++;
                 }
@@ -594,7 +738,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     uint64_t* dCodes[2] = { nullptr, nullptr }; uint32_t* dIds[2] = { nullptr, nullptr };
     void* dTemp = nullptr; size_t tempBytes = 0;
     BinNode* dNodes = nullptr; BoxF* dNodeBoxes = nullptr; uint32_t* dLeafParent = nullptr;
-    uint32_t* dCnt = nullptr; uint2* dQ[2] = { nullptr, nullptr };
+    uint32_t* dCnt = nullptr; uint4* dQ[2] = { nullptr, nullptr };
     uint32_t* dCounters = nullptr;
     WideNode* dW = nullptr;
     const uint32_t nInt = (n > 1) ? (n - 1) : 1;
@@ -606,7 +750,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     cub::DoubleBuffer<uint32_t> vb;
     uint32_t qn = 1;
     int cur = 0;
-    uint2 rootItem;
+    uint4 rootItem;
     CollapseArgs ca;
     float ext;
 
@@ -621,8 +765,8 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     MRG_CK(cudaMallocAsync(&dNodeBoxes, sizeof(BoxF) * nInt, st));
     MRG_CK(cudaMallocAsync(&dLeafParent, sizeof(uint32_t) * n, st));
     MRG_CK(cudaMallocAsync(&dCnt, sizeof(uint32_t) * nInt, st));
-    MRG_CK(cudaMallocAsync(&dQ[0], sizeof(uint2) * wideCap, st));
-    MRG_CK(cudaMallocAsync(&dQ[1], sizeof(uint2) * wideCap, st));
+    MRG_CK(cudaMallocAsync(&dQ[0], sizeof(uint4) * wideCap, st));
+    MRG_CK(cudaMallocAsync(&dQ[1], sizeof(uint4) * wideCap, st));
     MRG_CK(cudaMallocAsync(&dCounters, sizeof(uint32_t) * 4, st));
     MRG_CK(cudaMallocAsync(&dW, sizeof(WideNode) * wideCap, st));
     if(in.kind == 0) MRG_CK(cudaMallocAsync(&out.tris, sizeof(TriRecord) * n, st));
@@ -693,13 +837,13 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
         cudaFreeAsync(dNN, st); cudaFreeAsync(dKeep, st); cudaFreeAsync(dPos, st); cudaFreeAsync(dScanTemp, st);
         if(!okP) { err = "PLOC clustering failed"; goto fail; }
         MRG_CK(cudaMemcpyAsync(&rootBox, dNodeBoxes + rootRef, sizeof(BoxF), cudaMemcpyDeviceToHost, st));
-        rootItem = make_uint2(rootRef, 0u);
+        rootItem = make_uint4(rootRef, 0u, 0u, 0u);
     }
     else if(n > 1)
     {
         MRG_CK(cudaMemsetAsync(dNodes, 0xFF, sizeof(BinNode) * nInt, st));
         MRG_CK(cudaMemsetAsync(dLeafParent, 0xFF, sizeof(uint32_t) * n, st));
-        k_karras<<<gridFor(n - 1), kTPB, 0, st>>>(kb.Current(), (int)n, dNodes, dLeafParent);
+        k_karras<<<gridFor(n - 1), kTPB, 0, st>>>(kb.Current(), (int)n, dNodes, dLeafParent, nullptr, 0u, nullptr);
         MRG_CK(cudaGetLastError());
         MRG_CK(cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * nInt, st));
         MRG_CK(cudaMemsetAsync(dCounters, 0, sizeof(uint32_t) * 4, st));
@@ -707,12 +851,12 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
                                                  dNodeBoxes, dCnt, (int)n, dCounters + 3);
         MRG_CK(cudaGetLastError());
         MRG_CK(cudaMemcpyAsync(&rootBox, dNodeBoxes, sizeof(BoxF), cudaMemcpyDeviceToHost, st));
-        rootItem = make_uint2(0u, 0u);
+        rootItem = make_uint4(0u, 0u, 0u, 0u);
     }
     else
     {
         MRG_CK(cudaMemcpyAsync(&rootBox, dLeafBoxes, sizeof(BoxF), cudaMemcpyDeviceToHost, st));
-        rootItem = make_uint2(kLeafBit | 0u, 0u);
+        rootItem = make_uint4(kLeafBit | 0u, 0u, 0u, 0u);
     }
     MRG_CK(cudaMemcpyAsync(hostCounters, dCounters, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st));
     MRG_CK(cudaStreamSynchronize(st));
@@ -728,6 +872,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
         ext = (ext > sp) ? ext : sp;
     }
 
+    ca.segs = nullptr;
     ca.nodes = dNodes; ca.nodeBoxes = dNodeBoxes; ca.leafBoxes = dLeafBoxes;
     ca.sortedIds = vb.Current(); ca.pos = in.pos; ca.idx = in.idx;
     ca.primKeyBase = in.primKeyBase; ca.kind = in.kind; ca.maxLeaf = in.maxLeaf;
@@ -737,7 +882,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
 
     hostCounters[0] = 1; hostCounters[1] = 0; hostCounters[2] = 0; hostCounters[3] = 0;
     MRG_CK(cudaMemcpyAsync(dCounters, hostCounters, sizeof(hostCounters), cudaMemcpyHostToDevice, st));
-    MRG_CK(cudaMemcpyAsync(dQ[0], &rootItem, sizeof(uint2), cudaMemcpyHostToDevice, st));
+    MRG_CK(cudaMemcpyAsync(dQ[0], &rootItem, sizeof(uint4), cudaMemcpyHostToDevice, st));
     for(int level = 0; qn > 0; level++)
     {
         if(level > 64) { err = "wide BVH deeper than 64 levels"; goto fail; }
@@ -773,6 +918,183 @@ fail:
     cudaFree(dLeafParent); cudaFree(dCnt); cudaFree(dQ[0]); cudaFree(dQ[1]); cudaFree(dCounters);
     cudaFree(dW); cudaFree(out.nodes); cudaFree(out.tris); cudaFree(out.leafIds);
     out = BuildResult{};
+    return false;
+}
+
+bool build_wide_bvh_batch(const std::vector<BatchMeshInput>& meshes, BatchResult& out, cudaStream_t st,
+                          std::string& err)
+{
+    out = BatchResult{};
+    const uint32_t M = (uint32_t)meshes.size();
+    if(M == 0) { err = "empty batch"; return false; }
+    std::vector<uint32_t> firsts(M + 1);
+    std::vector<MeshSeg> segs(M);
+    uint64_t total = 0;
+    for(uint32_t m = 0; m < M; m++)
+    {
+        const BatchMeshInput& in = meshes[m];
+        if(in.count == 0 || !in.pos || !in.idx) { err = "empty mesh in batch"; return false; }
+        firsts[m] = (uint32_t)total;
+        segs[m] = MeshSeg{ in.pos, in.idx, (uint32_t)total, in.count, in.primKeyBase,
+                           std::min(3u, std::max(1u, in.maxLeaf)), 0.0f, 0u };
+        total += in.count;
+        if(total >= (1ull << 31)) { err = "batch larger than 2^31 triangles"; return false; }
+    }
+    firsts[M] = (uint32_t)total;
+    const uint32_t n = (uint32_t)total;
+    const uint32_t nInt = (n > 1) ? (n - 1) : 1;
+    const uint32_t wideCap = n;
+    // key layout: mesh id bits above 3 x `bits` Morton bits
+    uint32_t mbits = 0;
+    while(mbits < 32 && (1ull << mbits) < M) mbits++;
+    const uint32_t bits = std::min(21u, (64u - mbits) / 3u);
+    const int endBit = (int)(mbits + 3u * bits);
+
+    MeshSeg* dSegs = nullptr; uint32_t* dFirsts = nullptr; uint32_t* dCB = nullptr; uint32_t* dLeafMesh = nullptr;
+    BoxF* dLeafBoxes = nullptr; float* dCent = nullptr;
+    uint64_t* dCodes[2] = { nullptr, nullptr }; uint32_t* dIds[2] = { nullptr, nullptr };
+    void* dTemp = nullptr; size_t tempBytes = 0;
+    BinNode* dNodes = nullptr; BoxF* dNodeBoxes = nullptr; uint32_t* dLeafParent = nullptr;
+    uint32_t* dCnt = nullptr; uint4* dQ[2] = { nullptr, nullptr };
+    uint32_t* dCounters = nullptr; uint32_t* dMeshRoot = nullptr; BoxF* dMeshBoxes = nullptr;
+    WideNode* dW = nullptr;
+    std::vector<uint32_t> cbInit(6ull * M), meshRoot(M);
+    std::vector<BoxF> meshBoxes(M);
+    std::vector<uint4> seeds(M);
+    uint32_t hostCounters[4] = { 0, 0, 0, 0 };
+    cub::DoubleBuffer<uint64_t> kb;
+    cub::DoubleBuffer<uint32_t> vb;
+    CollapseArgs ca;
+    uint32_t qn = M;
+    int cur = 0;
+
+    for(uint32_t m = 0; m < M; m++)
+    {
+        for(int k = 0; k < 3; k++) { cbInit[6 * m + k] = 0xFFFFFFFFu; cbInit[6 * m + 3 + k] = 0u; }
+        meshRoot[m] = (segs[m].count == 1u) ? (kLeafBit | segs[m].first) : kNoParent;
+    }
+    MRG_CK(cudaMallocAsync(&dSegs, sizeof(MeshSeg) * M, st));
+    MRG_CK(cudaMallocAsync(&dFirsts, sizeof(uint32_t) * (M + 1), st));
+    MRG_CK(cudaMallocAsync(&dCB, sizeof(uint32_t) * 6 * M, st));
+    MRG_CK(cudaMallocAsync(&dLeafMesh, sizeof(uint32_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dLeafBoxes, sizeof(BoxF) * n, st));
+    MRG_CK(cudaMallocAsync(&dCent, sizeof(float) * 3 * n, st));
+    MRG_CK(cudaMallocAsync(&dCodes[0], sizeof(uint64_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dCodes[1], sizeof(uint64_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dIds[0], sizeof(uint32_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dIds[1], sizeof(uint32_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dNodes, sizeof(BinNode) * nInt, st));
+    MRG_CK(cudaMallocAsync(&dNodeBoxes, sizeof(BoxF) * nInt, st));
+    MRG_CK(cudaMallocAsync(&dLeafParent, sizeof(uint32_t) * n, st));
+    MRG_CK(cudaMallocAsync(&dCnt, sizeof(uint32_t) * nInt, st));
+    MRG_CK(cudaMallocAsync(&dQ[0], sizeof(uint4) * wideCap, st));
+    MRG_CK(cudaMallocAsync(&dQ[1], sizeof(uint4) * wideCap, st));
+    MRG_CK(cudaMallocAsync(&dCounters, sizeof(uint32_t) * 4, st));
+    MRG_CK(cudaMallocAsync(&dMeshRoot, sizeof(uint32_t) * M, st));
+    MRG_CK(cudaMallocAsync(&dMeshBoxes, sizeof(BoxF) * M, st));
+    MRG_CK(cudaMallocAsync(&dW, sizeof(WideNode) * wideCap, st));
+    MRG_CK(cudaMallocAsync(&out.tris, sizeof(TriRecord) * n, st));
+
+    MRG_CK(cudaMemcpyAsync(dSegs, segs.data(), sizeof(MeshSeg) * M, cudaMemcpyHostToDevice, st));
+    MRG_CK(cudaMemcpyAsync(dFirsts, firsts.data(), sizeof(uint32_t) * (M + 1), cudaMemcpyHostToDevice, st));
+    MRG_CK(cudaMemcpyAsync(dCB, cbInit.data(), sizeof(uint32_t) * 6 * M, cudaMemcpyHostToDevice, st));
+    MRG_CK(cudaMemcpyAsync(dMeshRoot, meshRoot.data(), sizeof(uint32_t) * M, cudaMemcpyHostToDevice, st));
+    MRG_CK(cudaMemsetAsync(dCounters, 0, sizeof(uint32_t) * 4, st));
+    k_leaf_boxes_multi<<<gridFor(n), kTPB, 0, st>>>(dSegs, dFirsts, M, n, dLeafBoxes, dCent, dCB, dLeafMesh);
+    MRG_CK(cudaGetLastError());
+    k_morton_multi<<<gridFor(n), kTPB, 0, st>>>(dCent, dCB, dLeafMesh, n, bits, dCodes[0], dIds[0]);
+    MRG_CK(cudaGetLastError());
+    kb = cub::DoubleBuffer<uint64_t>(dCodes[0], dCodes[1]);
+    vb = cub::DoubleBuffer<uint32_t>(dIds[0], dIds[1]);
+    MRG_CK(cub::DeviceRadixSort::SortPairs(nullptr, tempBytes, kb, vb, (int)n, 0, endBit, st));
+    MRG_CK(cudaMallocAsync(&dTemp, tempBytes, st));
+    MRG_CK(cub::DeviceRadixSort::SortPairs(dTemp, tempBytes, kb, vb, (int)n, 0, endBit, st));
+    if(n > 1)
+    {
+        MRG_CK(cudaMemsetAsync(dNodes, 0xFF, sizeof(BinNode) * nInt, st));
+        MRG_CK(cudaMemsetAsync(dLeafParent, 0xFF, sizeof(uint32_t) * n, st));
+        k_karras<<<gridFor(n - 1), kTPB, 0, st>>>(kb.Current(), (int)n, dNodes, dLeafParent, dFirsts, M, dMeshRoot);
+        MRG_CK(cudaGetLastError());
+        MRG_CK(cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * nInt, st));
+        k_bottom_up<<<gridFor(n), kTPB, 0, st>>>(dLeafParent, vb.Current(), dLeafBoxes, dNodes,
+                                                 dNodeBoxes, dCnt, (int)n, dCounters + 3);
+        MRG_CK(cudaGetLastError());
+    }
+    k_mesh_boxes<<<gridFor(M), kTPB, 0, st>>>(dMeshRoot, M, dNodeBoxes, dLeafBoxes, vb.Current(), n, dMeshBoxes,
+                                              dCounters + 3);
+    MRG_CK(cudaGetLastError());
+    MRG_CK(cudaMemcpyAsync(meshRoot.data(), dMeshRoot, sizeof(uint32_t) * M, cudaMemcpyDeviceToHost, st));
+    MRG_CK(cudaMemcpyAsync(meshBoxes.data(), dMeshBoxes, sizeof(BoxF) * M, cudaMemcpyDeviceToHost, st));
+    MRG_CK(cudaMemcpyAsync(hostCounters, dCounters, sizeof(hostCounters), cudaMemcpyDeviceToHost, st));
+    MRG_CK(cudaStreamSynchronize(st));
+    if(hostCounters[3] != 0) { err = "batched binary tree construction produced an invalid node"; goto fail; }
+
+    // per-mesh box, inflation (1e-5 of the mesh's extent, as a single build) and collapse seed
+    out.boxes.resize(6ull * M);
+    for(uint32_t m = 0; m < M; m++)
+    {
+        const BoxF& b = meshBoxes[m];
+        float ext = 0.0f;
+        for(int k = 0; k < 3; k++)
+        {
+            out.boxes[6ull * m + k] = b.mn[k];
+            out.boxes[6ull * m + 3 + k] = b.mx[k];
+            const float e = fabsf(b.mx[k]) > fabsf(b.mn[k]) ? fabsf(b.mx[k]) : fabsf(b.mn[k]);
+            ext = (ext > e) ? ext : e;
+            const float sp = b.mx[k] - b.mn[k];
+            ext = (ext > sp) ? ext : sp;
+        }
+        segs[m].inflate = ext * 1.0e-5f + 1.0e-30f;
+        seeds[m] = make_uint4(meshRoot[m], m, m, 0u);
+    }
+    MRG_CK(cudaMemcpyAsync(dSegs, segs.data(), sizeof(MeshSeg) * M, cudaMemcpyHostToDevice, st));
+    MRG_CK(cudaMemcpyAsync(dQ[0], seeds.data(), sizeof(uint4) * M, cudaMemcpyHostToDevice, st));
+
+    ca.segs = dSegs;
+    ca.nodes = dNodes; ca.nodeBoxes = dNodeBoxes; ca.leafBoxes = dLeafBoxes;
+    ca.sortedIds = vb.Current(); ca.pos = nullptr; ca.idx = nullptr;
+    ca.primKeyBase = 0; ca.kind = 0; ca.maxLeaf = 3; ca.inflate = 0.0f;
+    ca.wnodes = dW; ca.tris = out.tris; ca.leafIds = nullptr; ca.counters = dCounters;
+    ca.leafCount = n; ca.wideCap = wideCap;
+    hostCounters[0] = M; hostCounters[1] = 0; hostCounters[2] = 0; hostCounters[3] = 0;
+    MRG_CK(cudaMemcpyAsync(dCounters, hostCounters, sizeof(hostCounters), cudaMemcpyHostToDevice, st));
+    for(int level = 0; qn > 0; level++)
+    {
+        if(level > 64) { err = "wide BVH deeper than 64 levels"; goto fail; }
+        MRG_CK(cudaMemsetAsync(dCounters + 2, 0, sizeof(uint32_t), st));
+        k_collapse<<<gridFor(qn, 128), 128, 0, st>>>(ca, dQ[cur], qn, dQ[cur ^ 1]);
+        MRG_CK(cudaGetLastError());
+        MRG_CK(cudaMemcpyAsync(hostCounters, dCounters, sizeof(hostCounters), cudaMemcpyDeviceToHost, st));
+        MRG_CK(cudaStreamSynchronize(st));
+        if(hostCounters[3] != 0) { err = "wide BVH collapse reported an invalid tree"; goto fail; }
+        if(hostCounters[0] > wideCap) { err = "wide node capacity exceeded"; goto fail; }
+        qn = hostCounters[2];
+        cur ^= 1;
+    }
+    if(hostCounters[1] != n) { err = "payload count mismatch"; goto fail; }
+    out.nodeCount = hostCounters[0];
+    MRG_CK(cudaMallocAsync(&out.nodes, sizeof(WideNode) * out.nodeCount, st));
+    MRG_CK(cudaMemcpyAsync(out.nodes, dW, sizeof(WideNode) * out.nodeCount, cudaMemcpyDeviceToDevice, st));
+    out.payloadCount = n;
+
+    cudaFreeAsync(dSegs, st); cudaFreeAsync(dFirsts, st); cudaFreeAsync(dCB, st); cudaFreeAsync(dLeafMesh, st);
+    cudaFreeAsync(dLeafBoxes, st); cudaFreeAsync(dCent, st);
+    cudaFreeAsync(dCodes[0], st); cudaFreeAsync(dCodes[1], st);
+    cudaFreeAsync(dIds[0], st); cudaFreeAsync(dIds[1], st); cudaFreeAsync(dTemp, st);
+    cudaFreeAsync(dNodes, st); cudaFreeAsync(dNodeBoxes, st); cudaFreeAsync(dLeafParent, st);
+    cudaFreeAsync(dCnt, st); cudaFreeAsync(dQ[0], st); cudaFreeAsync(dQ[1], st);
+    cudaFreeAsync(dCounters, st); cudaFreeAsync(dMeshRoot, st); cudaFreeAsync(dMeshBoxes, st); cudaFreeAsync(dW, st);
+    if(cudaStreamSynchronize(st) != cudaSuccess) { err = "stream sync failed"; return false; }
+    return true;
+
+fail:
+    cudaStreamSynchronize(st);
+    cudaFree(dSegs); cudaFree(dFirsts); cudaFree(dCB); cudaFree(dLeafMesh);
+    cudaFree(dLeafBoxes); cudaFree(dCent); cudaFree(dCodes[0]); cudaFree(dCodes[1]);
+    cudaFree(dIds[0]); cudaFree(dIds[1]); cudaFree(dTemp); cudaFree(dNodes); cudaFree(dNodeBoxes);
+    cudaFree(dLeafParent); cudaFree(dCnt); cudaFree(dQ[0]); cudaFree(dQ[1]); cudaFree(dCounters);
+    cudaFree(dMeshRoot); cudaFree(dMeshBoxes); cudaFree(dW); cudaFree(out.nodes); cudaFree(out.tris);
+    out = BatchResult{};
     return false;
 }
 

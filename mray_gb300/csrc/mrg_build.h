@@ -2,6 +2,7 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 
 namespace mrg {
@@ -33,6 +34,31 @@ struct BuildResult
 };
 
 bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std::string& err);
+
+// Batched BLAS build (the counterpart of MRay's segmented multi-build,
+// Source/Tracer/AcceleratorLBVH.hpp:585-899): every mesh in one pass of
+// leaf boxes, keys, sort, radix tree, bottom-up boxes and level-by-level
+// collapse.  Wide node m is the root of mesh m.
+struct BatchMeshInput
+{
+    const float*    pos = nullptr;     // device, 3 floats per vertex
+    const uint32_t* idx = nullptr;     // device, 3 per triangle (local to the mesh)
+    uint32_t        count = 0;         // triangles (>= 1)
+    uint32_t        primKeyBase = 0;
+    uint32_t        maxLeaf = 3;       // triangles per leaf child (<= 3)
+};
+
+struct BatchResult
+{
+    WideNode*          nodes = nullptr;     // device, nodeCount (child bases local to the batch)
+    uint32_t           nodeCount = 0;
+    TriRecord*         tris = nullptr;      // device, payloadCount records
+    uint32_t           payloadCount = 0;
+    std::vector<float> boxes;               // 6 per mesh: exact root box
+};
+
+bool build_wide_bvh_batch(const std::vector<BatchMeshInput>& meshes, BatchResult& out, cudaStream_t st,
+                          std::string& err);
 bool relocate_nodes(const WideNode* src, WideNode* dst, uint32_t n, uint32_t nodeOff,
                     uint32_t triOff, cudaStream_t st);
 

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle
-from mray_gb300 import MRGError, scenes
+from mray_gb300 import Accelerator, MRGError, scenes
 from parity_util import (MISS, build_pair, compare_closest, gpu_closest, gpu_visibility,
                          stress_workload)
 
@@ -34,6 +34,48 @@ def test_closest_small_scenes(level, ninst, cull):
     gpu = gpu_closest(acc, rays)
     n, hits, ties = compare_closest(ora, gpu)
     assert hits > 0
+
+
+def _mesh_of(ntri, seed):
+    """A random triangle soup of ntri triangles inside a unit cube."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-1, 1, (ntri, 1, 3))
+    pos = (c + rng.uniform(-0.35, 0.35, (ntri, 3, 3))).reshape(-1, 3).astype(np.float32)
+    return pos, np.arange(3 * ntri, dtype=np.uint32).reshape(-1, 3)
+
+
+def test_batched_blas_build_mixed_mesh_sizes():
+    """All BLASes are built in one batch: meshes of 1, 2, 3, 7, 100 and 5,000
+    triangles (leaf roots, tiny trees, one-triangle and three-triangle leaf
+    sizes) side by side, each instanced, against the oracle's per-mesh
+    builds; per-mesh prim keys and world boxes must survive the batching."""
+    sizes = [1, 2, 3, 7, 100, 5000, 1, 40]
+    acc = Accelerator(0)
+    S = oracle.Scene()
+    rng = np.random.default_rng(3)
+    inst = 0
+    for k, nt in enumerate(sizes):
+        pos, idx = _mesh_of(nt, 10 + k)
+        base = 0x10000000 + 0x10000 * k
+        mid = acc.upload_mesh(pos, idx, prim_key_base=base)
+        oid = S.add_mesh(pos, idx, prim_key_base=base)
+        for j in range(2):
+            m = np.zeros((3, 4), np.float32)
+            m[:, :3] = np.eye(3) * rng.uniform(0.8, 1.5)
+            m[:, 3] = rng.uniform(-5, 5, 3)
+            m = m.reshape(12)
+            acc.add_instance(mid, m, light_or_mat_key=inst, trans_key=(1 << 24) | inst, accel_key=(2 << 20) | inst)
+            S.add_instance(oid, m, lm_key=inst, trans_key=(1 << 24) | inst, accel_key=(2 << 20) | inst)
+            inst += 1
+    acc.construct()
+    S.build()
+    rays = scenes.primary_rays(160, 120, 4, eye=(0, 0, -16), tan_half_fov=0.45)
+    ora = S.cast_closest(rays)
+    gpu = gpu_closest(acc, rays)
+    n, hits, ties = compare_closest(ora, gpu)
+    assert hits > 1000
+    keys = gpu[1][:, 0][gpu[1][:, 0] != MISS]
+    assert len(np.unique(keys >> 16)) >= len(sizes) - 2   # nearly every mesh is hit somewhere
 
 
 def _general_rotations(n=12, seed=5):
