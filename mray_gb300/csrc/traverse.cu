@@ -207,7 +207,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
     float wox = 0, woy = 0, woz = 0, wdx = 0, wdy = 0, wdz = 0, tmin = 0, tmax = 0;
     float wix = 0, wiy = 0, wiz = 0;   // IEEE 1/dir of the world ray (exact leaf slab test)
     LevelRay lr;
-    float3 lo = make_float3(0, 0, 0), ld = make_float3(0, 0, 0);
+    float3 ld = make_float3(0, 0, 0);   // local direction (the local origin is lr.ox/oy/oz)
     uint2 ng = make_uint2(0, 0), tg = make_uint2(0, 0);
     int sp = 0, blasBase = -1;
     uint32_t curInst = kInvalidIndex, hitPrim = 0, hitInst = kInvalidIndex;
@@ -331,7 +331,8 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     const float4 v0 = __ldg(tp), e0 = __ldg(tp + 1), e1 = __ldg(tp + 2);
                     if(STATS) statTris++;
                     float t, u, v;
-                    if(intersect_tri_exact(lo, ld, v0, e0, e1, cull, t, u, v) && t >= tmin && t < tmax)
+                    if(intersect_tri_exact(make_float3(lr.ox, lr.oy, lr.oz), ld, v0, e0, e1, cull, t, u, v) &&
+                       t >= tmin && t < tmax)
                     {
                         tmax = t; hitU = u; hitV = v;
                         hitPrim = __float_as_uint(v0.w);
@@ -388,6 +389,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                         }
                         blasBase = sp;
                         const float4 m0 = __ldg(ip), m1 = __ldg(ip + 1), m2 = __ldg(ip + 2);
+                        float3 lo;
                         const uint4 keys = __ldg(reinterpret_cast<const uint4*>(ip + 3));
                         transform_ray_exact(m0, m1, m2, make_float3(wox, woy, woz),
                                             make_float3(wdx, wdy, wdz), lo, ld);
