@@ -161,16 +161,18 @@ __device__ void encode_sample(const NrcState& S, const float4* in, bool valid, u
 // ---------------------------------------------------------------------------
 // Forward: inference (out) or training (stores activations and outputs)
 // ---------------------------------------------------------------------------
-template<bool TRAIN, bool LIST>
-__global__ void __launch_bounds__(kTPB)
+// WARPS warps per CTA share one shared-memory copy of the weights; more warps
+// per CTA keep more hash-grid gathers in flight per SM.
+template<bool TRAIN, bool LIST, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
 k_nrc_forward(NrcState S, const float4* __restrict__ inputs, const uint32_t* __restrict__ list,
               const uint32_t* nDevice, uint32_t nMax, float4* __restrict__ out)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t* sW = reinterpret_cast<uint16_t*>(smem);                       // (256 + 16) x kPad
-    uint16_t* sX = sW + (kHiddenRows + kNrcOut) * kPad;                      // kWarps x 16 x kPad
-    float* sO = reinterpret_cast<float*>(sX + kWarps * 16 * kPad);           // kWarps x 16 x 4
-    for(uint32_t i = threadIdx.x; i < (uint32_t)kNrcWeightCount; i += kTPB)
+    uint16_t* sX = sW + (kHiddenRows + kNrcOut) * kPad;                      // WARPS x 16 x kPad
+    float* sO = reinterpret_cast<float*>(sX + WARPS * 16 * kPad);            // WARPS x 16 x 4
+    for(uint32_t i = threadIdx.x; i < (uint32_t)kNrcWeightCount; i += WARPS * 32)
         sW[(i / kNrcWidth) * kPad + (i % kNrcWidth)] = S.w16[i];
     __syncthreads();
     const uint32_t n = nDevice ? min(*nDevice, nMax) : nMax;
@@ -178,7 +180,7 @@ k_nrc_forward(NrcState S, const float4* __restrict__ inputs, const uint32_t* __r
     const uint32_t g = lane >> 2, t = lane & 3u;
     uint16_t* xw = sX + warp * 16 * kPad;
     float* ow = sO + warp * 64;
-    for(uint32_t base = (blockIdx.x * kWarps + warp) * 16u; base < n; base += gridDim.x * kWarps * 16u)
+    for(uint32_t base = (blockIdx.x * WARPS + warp) * 16u; base < n; base += gridDim.x * WARPS * 16u)
     {
         // ---- encode 16 samples ----
         {
@@ -753,8 +755,13 @@ __global__ void k_copy_params(const float* __restrict__ w, uint16_t* __restrict_
     }
 }
 
-constexpr size_t kFwdSmem = (size_t)(kHiddenRows + kNrcOut) * kPad * 2 + (size_t)kWarps * 16 * kPad * 2 +
-                            (size_t)kWarps * 64 * 4;
+#ifndef MRG_NRC_QUERY_WARPS
+#define MRG_NRC_QUERY_WARPS 16       // warps per CTA of the inference forward
+#endif
+constexpr size_t fwd_smem(int warps)
+{
+    return (size_t)(kHiddenRows + kNrcOut) * kPad * 2 + (size_t)warps * 16 * kPad * 2 + (size_t)warps * 64 * 4;
+}
 constexpr size_t kBwdSmem = (size_t)kHiddenRows * kPad * 2 + (size_t)kNrcWidth * kPadT4 * 2 +
                             (size_t)kWarps * 16 * 33 * 4;
 
@@ -762,17 +769,25 @@ template<bool TRAIN, bool LIST>
 cudaError_t launch_forward(const NrcState& S, const float4* in, const uint32_t* list, const uint32_t* nDevice,
                            uint32_t nMax, float4* out, int smCount, cudaStream_t st)
 {
+    // training batches keep 4-warp CTAs (their activation stores dominate);
+    // inference uses MRG_NRC_QUERY_WARPS
+    constexpr int W = TRAIN ? 4 : MRG_NRC_QUERY_WARPS;
+    constexpr size_t smem = fwd_smem(W);
     static bool configured = false;
+    static int perSM = 1;
     if(!configured)
     {
-        cudaError_t e = cudaFuncSetAttribute(k_nrc_forward<TRAIN, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kFwdSmem);
+        cudaError_t e = cudaFuncSetAttribute(k_nrc_forward<TRAIN, LIST, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
         if(e != cudaSuccess) return e;
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_nrc_forward<TRAIN, LIST, W>, W * 32, smem) != cudaSuccess ||
+           perSM < 1)
+            perSM = 1;
         configured = true;
     }
-    const uint32_t tiles = (nMax + 16 * kWarps - 1) / (16 * kWarps);
-    const uint32_t grid = std::max(1u, std::min(tiles, (uint32_t)smCount * 8u));
-    k_nrc_forward<TRAIN, LIST><<<grid, kTPB, kFwdSmem, st>>>(S, in, list, nDevice, nMax, out);
+    const uint32_t tiles = (nMax + 16 * W - 1) / (16 * W);
+    const uint32_t grid = std::max(1u, std::min(tiles, (uint32_t)smCount * (uint32_t)perSM * 2u));
+    k_nrc_forward<TRAIN, LIST, W><<<grid, W * 32, smem, st>>>(S, in, list, nDevice, nMax, out);
     return cudaGetLastError();
 }
 

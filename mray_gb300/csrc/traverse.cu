@@ -316,7 +316,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     triDone++;
                     // Postpone when few lanes want triangles and this lane has
                     // nodes left: SIMD lanes stay on the wider node work.
-                    if(ng.y > 0x00FFFFFFu && __popc(__activemask()) < kPostponeLanes &&
+                    if(kPostponeLanes > 0 && ng.y > 0x00FFFFFFu && __popc(__activemask()) < kPostponeLanes &&
                        sp < kStackSize)
                     {
                         push(tg, sp);
