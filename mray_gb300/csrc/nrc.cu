@@ -22,8 +22,6 @@ namespace mrg {
 
 namespace {
 
-constexpr int kTPB = 128;                     // 4 warps
-constexpr int kWarps = kTPB / 32;
 constexpr int kPad = 72;                      // padded row of 64 bf16
 constexpr int kPadT4 = 24;                    // padded row of W4^T (16 bf16)
 constexpr int kHiddenRows = 4 * kNrcWidth;    // rows of W0..W3
@@ -302,7 +300,8 @@ k_nrc_forward(NrcState S, const float4* __restrict__ inputs, const uint32_t* __r
 // ---------------------------------------------------------------------------
 // Backward: relative L2 loss, deltas through the MLP, hash-grid scatter
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTPB)
+template<int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
 k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __restrict__ y,
                const float4* __restrict__ targets, const uint32_t* nDevice, uint32_t nMax)
 {
@@ -310,14 +309,14 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
     // transposed weights: W0^T..W3^T [64 in][64 out] and W4^T [64 in][16 out]
     uint16_t* sT = reinterpret_cast<uint16_t*>(smem);                        // 4 x 64 x kPad
     uint16_t* sT4 = sT + kHiddenRows * kPad;                                  // 64 x kPadT4
-    float* sG = reinterpret_cast<float*>(sT4 + kNrcWidth * kPadT4);           // kWarps x 16 x 33
-    for(uint32_t i = threadIdx.x; i < (uint32_t)(kHiddenRows * kNrcWidth); i += kTPB)
+    float* sG = reinterpret_cast<float*>(sT4 + kNrcWidth * kPadT4);           // WARPS x 16 x 33
+    for(uint32_t i = threadIdx.x; i < (uint32_t)(kHiddenRows * kNrcWidth); i += WARPS * 32)
     {
         const uint32_t layer = i / (kNrcWidth * kNrcWidth), r = (i / kNrcWidth) % kNrcWidth, c = i % kNrcWidth;
         // W[layer][out = r][in = c] -> T[layer][in = c][out = r]
         sT[(layer * kNrcWidth + c) * kPad + r] = S.w16[i];
     }
-    for(uint32_t i = threadIdx.x; i < (uint32_t)(kNrcOut * kNrcWidth); i += kTPB)
+    for(uint32_t i = threadIdx.x; i < (uint32_t)(kNrcOut * kNrcWidth); i += WARPS * 32)
     {
         const uint32_t r = i / kNrcWidth, c = i % kNrcWidth;
         sT4[c * kPadT4 + r] = S.w16[kHiddenRows * kNrcWidth + i];
@@ -330,7 +329,7 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
     const uint32_t g = lane >> 2, t = lane & 3u;
     float* gw = sG + warp * 16 * 33;
     float lossAcc = 0.0f;
-    for(uint32_t base = (blockIdx.x * kWarps + warp) * 16u; base < n; base += gridDim.x * kWarps * 16u)
+    for(uint32_t base = (blockIdx.x * WARPS + warp) * 16u; base < n; base += gridDim.x * WARPS * 16u)
     {
         const uint32_t r0 = base + g, r1 = base + g + 8;
         const bool v0 = r0 < n, v1 = r1 < n;
@@ -762,16 +761,20 @@ constexpr size_t fwd_smem(int warps)
 {
     return (size_t)(kHiddenRows + kNrcOut) * kPad * 2 + (size_t)warps * 16 * kPad * 2 + (size_t)warps * 64 * 4;
 }
-constexpr size_t kBwdSmem = (size_t)kHiddenRows * kPad * 2 + (size_t)kNrcWidth * kPadT4 * 2 +
-                            (size_t)kWarps * 16 * 33 * 4;
+#ifndef MRG_NRC_TRAIN_WARPS
+#define MRG_NRC_TRAIN_WARPS 16       // warps per CTA of the training forward and backward
+#endif
+constexpr size_t bwd_smem(int warps)
+{
+    return (size_t)kHiddenRows * kPad * 2 + (size_t)kNrcWidth * kPadT4 * 2 + (size_t)warps * 16 * 33 * 4;
+}
 
 template<bool TRAIN, bool LIST>
 cudaError_t launch_forward(const NrcState& S, const float4* in, const uint32_t* list, const uint32_t* nDevice,
                            uint32_t nMax, float4* out, int smCount, cudaStream_t st)
 {
-    // training batches keep 4-warp CTAs (their activation stores dominate);
-    // inference uses MRG_NRC_QUERY_WARPS
-    constexpr int W = TRAIN ? 4 : MRG_NRC_QUERY_WARPS;
+    // warps per CTA: MRG_NRC_TRAIN_WARPS for training batches, MRG_NRC_QUERY_WARPS for inference
+    constexpr int W = TRAIN ? MRG_NRC_TRAIN_WARPS : MRG_NRC_QUERY_WARPS;
     constexpr size_t smem = fwd_smem(W);
     static bool configured = false;
     static int perSM = 1;
@@ -851,21 +854,27 @@ cudaError_t nrc_gradients(NrcState& S, const float4* inputs, const float4* targe
                           uint32_t nMax, int smCount, cudaStream_t st)
 {
     if(nMax > S.cap) return cudaErrorInvalidValue;
+    constexpr int W = MRG_NRC_TRAIN_WARPS;
+    constexpr size_t bsmem = bwd_smem(W);
     static bool configured = false;
+    static int perSM = 1;
     if(!configured)
     {
-        cudaError_t e = cudaFuncSetAttribute(k_nrc_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+        cudaError_t e = cudaFuncSetAttribute(k_nrc_backward<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
         if(e != cudaSuccess) return e;
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_nrc_backward<W>, W * 32, bsmem) != cudaSuccess ||
+           perSM < 1)
+            perSM = 1;
         configured = true;
     }
     cudaError_t e = cudaMemsetAsync(S.loss, 0, sizeof(float), st);
     // the forward stores the activations and the outputs of the batch
     if(e == cudaSuccess) e = launch_forward<true, false>(S, inputs, nullptr, nDevice, nMax, S.y, smCount, st);
-    const uint32_t tiles = (nMax + 16 * kWarps - 1) / (16 * kWarps);
-    const uint32_t grid = std::max(1u, std::min(tiles, (uint32_t)smCount * 8u));
+    const uint32_t tiles = (nMax + 16 * W - 1) / (16 * W);
+    const uint32_t grid = std::max(1u, std::min(tiles, (uint32_t)smCount * (uint32_t)perSM * 2u));
     if(e == cudaSuccess)
     {
-        k_nrc_backward<<<grid, kTPB, kBwdSmem, st>>>(S, inputs, S.y, targets, nDevice, nMax);
+        k_nrc_backward<W><<<grid, W * 32, bsmem, st>>>(S, inputs, S.y, targets, nDevice, nMax);
         e = cudaGetLastError();
     }
     static bool wgConfigured = false;
