@@ -178,6 +178,9 @@ mrg_status mrg_destroy(mrg_ctx* c)
     for(void* q : c->cacheAllocs) cudaFree(q);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
     for(cudaStream_t& q : c->hostStreams) if(q) cudaStreamDestroy(q);
+    if(c->ptSideStream) cudaStreamDestroy(c->ptSideStream);
+    if(c->ptEvShaded) cudaEventDestroy(c->ptEvShaded);
+    if(c->ptEvResolved) cudaEventDestroy(c->ptEvResolved);
     cudaFree(c->dHostCounters);
     for(cudaEvent_t& q : c->hostEvents) if(q) cudaEventDestroy(q);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);

@@ -101,6 +101,9 @@ struct mrg_ctx
     uint32_t  ptSurfaceCount = 0, ptLightCount = 0, ptTriCount = 0;
     uint32_t  ptMaterialGroups = 0;          // distinct material groups among surfaces
     mrg::PtPaths ptPaths{};
+    // shadow casts of bounce d overlap the closest-hit cast of bounce d + 1
+    cudaStream_t ptSideStream = nullptr;
+    cudaEvent_t  ptEvShaded = nullptr, ptEvResolved = nullptr;
     void*     ptPathMem = nullptr;
     // skysphere boundary light: host copy of the radiance map and transform,
     // device block [texels | cdfX | cdfY]

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -602,10 +603,35 @@ mrg_status pt_setup(mrg_ctx* c, const mrg_pt_params* p, PtRun& R, const char* wh
 
 // raygen + maxDepth bounces of the pass at R.L.sampleBase; leaves each slot's
 // radiance in the path state.
+// Shadow casts overlap the next closest-hit cast (MRG_PT_OVERLAP=0: one stream).
+bool pt_overlap()
+{
+    const char* v = std::getenv("MRG_PT_OVERLAP");
+    return !(v && v[0] == '0');
+}
+
+// One pass of bounces.  Per bounce: closest-hit cast of the alive paths,
+// optional material-key partition, shading (continuations, NEE shadow rays),
+// shadow cast and resolve.  The shadow cast and resolve of bounce d run on a
+// side stream, beside the closest-hit cast and partition of bounce d + 1;
+// shading of bounce d + 1 waits for them, since it rewrites the shadow rays,
+// list and count and adds to the same path radiance.  The two casts claim
+// rays through separate counters.
 cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, cudaStream_t st)
 {
     mrg::PtPaths& P = c->ptPaths;
     const mrg::PtLaunch& L = R.L;
+    const bool overlap = pt_overlap();
+    if(overlap && !c->ptSideStream)
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&c->ptSideStream, cudaStreamNonBlocking);
+        if(e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ptEvShaded, cudaEventDisableTiming);
+        if(e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ptEvResolved, cudaEventDisableTiming);
+        if(e != cudaSuccess) return e;
+    }
+    cudaStream_t side = overlap ? c->ptSideStream : st;
+    mrg::TraceScratch shadowScr = R.scr;
+    if(overlap) shadowScr.workCounter = c->dScratch + 2;
     // with the cache every path has ended by vertex recPerPath + 1
     const uint32_t loops = (L.cache.mode == 1u) ? std::min(L.maxDepth, L.cache.recPerPath + 2u) : L.maxDepth;
     cudaError_t e = mrg::pt_raygen(L, P, P.listA, P.counts + 0, c->smCount, st);
@@ -616,7 +642,6 @@ cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, cudaStream_t st)
         uint32_t* aliveCount = P.counts + ((depth & 1u) ? 1 : 0);
         uint32_t* nextCount = P.counts + ((depth & 1u) ? 0 : 1);
         e = cudaMemsetAsync(nextCount, 0, sizeof(uint32_t), st);
-        if(e == cudaSuccess) e = cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), st);
         if(e == cudaSuccess)
             e = mrg::launch_closest(c->scene, R.scr, P.rays, alive, 0, P.hits, P.meta, c->smCount, st, aliveCount);
         const uint32_t* shadeList = alive;
@@ -631,13 +656,19 @@ cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, cudaStream_t st)
                                          P.sortHist, st);
             shadeList = P.listSorted;
         }
+        if(e == cudaSuccess && overlap && depth > 0) e = cudaStreamWaitEvent(st, c->ptEvResolved, 0);
+        if(e == cudaSuccess) e = cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), st);
         if(e == cudaSuccess)
             e = mrg::pt_shade_impl(L, P, R.T, shadeList, aliveCount, next, nextCount, c->smCount, st);
+        if(e == cudaSuccess && overlap) e = cudaEventRecord(c->ptEvShaded, st);
+        if(e == cudaSuccess && overlap) e = cudaStreamWaitEvent(side, c->ptEvShaded, 0);
         if(e == cudaSuccess)
-            e = mrg::launch_visibility(c->scene, R.scr, P.visBits, P.shadowRays, P.shadowList, 0, c->smCount, st,
+            e = mrg::launch_visibility(c->scene, shadowScr, P.visBits, P.shadowRays, P.shadowList, 0, c->smCount, side,
                                        P.counts + 2);
-        if(e == cudaSuccess) e = mrg::pt_resolve(L, P, depth, c->smCount, st);
+        if(e == cudaSuccess) e = mrg::pt_resolve(L, P, depth, c->smCount, side);
+        if(e == cudaSuccess && overlap) e = cudaEventRecord(c->ptEvResolved, side);
     }
+    if(e == cudaSuccess && overlap) e = cudaStreamWaitEvent(st, c->ptEvResolved, 0);
     return e;
 }
 
