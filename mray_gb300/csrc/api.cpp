@@ -178,9 +178,11 @@ mrg_status mrg_destroy(mrg_ctx* c)
     for(void* q : c->cacheAllocs) cudaFree(q);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
     for(cudaStream_t& q : c->hostStreams) if(q) cudaStreamDestroy(q);
-    if(c->ptSideStream) cudaStreamDestroy(c->ptSideStream);
-    if(c->ptEvShaded) cudaEventDestroy(c->ptEvShaded);
-    if(c->ptEvResolved) cudaEventDestroy(c->ptEvResolved);
+    for(cudaStream_t q : { c->ptSideStream, c->ptStream2, c->ptSideStream2 }) if(q) cudaStreamDestroy(q);
+    for(cudaEvent_t q : { c->ptEvShaded, c->ptEvResolved, c->ptEvShaded2, c->ptEvResolved2, c->ptEvFilm,
+                          c->ptEvStart, c->ptEvDone2 })
+        if(q) cudaEventDestroy(q);
+    cudaFree(c->ptPathMem2);
     cudaFree(c->dHostCounters);
     for(cudaEvent_t& q : c->hostEvents) if(q) cudaEventDestroy(q);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);

@@ -104,6 +104,13 @@ struct mrg_ctx
     // shadow casts of bounce d overlap the closest-hit cast of bounce d + 1
     cudaStream_t ptSideStream = nullptr;
     cudaEvent_t  ptEvShaded = nullptr, ptEvResolved = nullptr;
+    // second pass pipeline of mrg_pt_render: its own path state, streams,
+    // events; ptEvFilm orders the film writes of consecutive passes
+    mrg::PtPaths ptPaths2{};
+    void*        ptPathMem2 = nullptr;
+    cudaStream_t ptStream2 = nullptr, ptSideStream2 = nullptr;
+    cudaEvent_t  ptEvShaded2 = nullptr, ptEvResolved2 = nullptr;
+    cudaEvent_t  ptEvFilm = nullptr, ptEvStart = nullptr, ptEvDone2 = nullptr;
     void*     ptPathMem = nullptr;
     // skysphere boundary light: host copy of the radiance map and transform,
     // device block [texels | cdfX | cdfY]

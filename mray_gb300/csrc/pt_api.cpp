@@ -328,12 +328,13 @@ mrg_status pt_prepare(mrg_ctx* c)
     return MRG_OK;
 }
 
-mrg_status pt_paths(mrg_ctx* c, uint32_t slots)
+// Path state of `slots` paths in one allocation (P / mem: one pipeline's).
+mrg_status pt_paths_into(mrg::PtPaths& P, void*& mem, uint32_t slots)
 {
-    if(c->ptPaths.capacity >= slots && c->ptPathMem) return MRG_OK;
-    cudaFree(c->ptPathMem);
-    c->ptPathMem = nullptr;
-    c->ptPaths = mrg::PtPaths{};
+    if(P.capacity >= slots && mem) return MRG_OK;
+    cudaFree(mem);
+    mem = nullptr;
+    P = mrg::PtPaths{};
     const size_t n = slots;
     const size_t words = (n + 31) / 32;
     // one allocation, every array 256-byte aligned
@@ -345,11 +346,10 @@ mrg_status pt_paths(mrg_ctx* c, uint32_t slots)
     for(size_t sz : sizes) need += (sz + 255) & ~size_t(255);
     char* base = nullptr;
     PT_TRY(cudaMalloc(&base, need), "mrg_pt: path state");
-    c->ptPathMem = base;
+    mem = base;
     size_t off = 0;
     int k = 0;
     auto take = [&]() { char* q = base + off; off += (sizes[k++] + 255) & ~size_t(255); return q; };
-    mrg::PtPaths& P = c->ptPaths;
     P.rays = reinterpret_cast<float4*>(take());
     P.hits = reinterpret_cast<uint4*>(take());
     P.meta = reinterpret_cast<float2*>(take());
@@ -373,6 +373,8 @@ mrg_status pt_paths(mrg_ctx* c, uint32_t slots)
     P.capacity = slots;
     return MRG_OK;
 }
+
+mrg_status pt_paths(mrg_ctx* c, uint32_t slots) { return pt_paths_into(c->ptPaths, c->ptPathMem, slots); }
 
 } // namespace
 
@@ -610,6 +612,33 @@ bool pt_overlap()
     return !(v && v[0] == '0');
 }
 
+// One pipeline of passes: path state, the stream its closest-hit casts and
+// shading run on, the side stream of its shadow casts, their events, and the
+// ray-claim counters of its two casts.
+struct PtLane
+{
+    mrg::PtPaths* P;
+    cudaStream_t  st;
+    cudaStream_t  side;          // == st without overlap
+    cudaEvent_t   evShaded, evResolved;
+    uint32_t*     closestCounter;
+    uint32_t*     shadowCounter;
+};
+
+mrg_status pt_lane0(mrg_ctx* c, cudaStream_t st, PtLane& lane)
+{
+    const bool overlap = pt_overlap();
+    if(overlap && !c->ptSideStream)
+    {
+        PT_TRY(cudaStreamCreateWithFlags(&c->ptSideStream, cudaStreamNonBlocking), "mrg_pt: stream");
+        PT_TRY(cudaEventCreateWithFlags(&c->ptEvShaded, cudaEventDisableTiming), "mrg_pt: event");
+        PT_TRY(cudaEventCreateWithFlags(&c->ptEvResolved, cudaEventDisableTiming), "mrg_pt: event");
+    }
+    lane = PtLane{ &c->ptPaths, st, overlap ? c->ptSideStream : st, c->ptEvShaded, c->ptEvResolved,
+                   c->dScratch + 0, c->dScratch + (overlap ? 2 : 0) };
+    return MRG_OK;
+}
+
 // One pass of bounces.  Per bounce: closest-hit cast of the alive paths,
 // optional material-key partition, shading (continuations, NEE shadow rays),
 // shadow cast and resolve.  The shadow cast and resolve of bounce d run on a
@@ -617,21 +646,15 @@ bool pt_overlap()
 // shading of bounce d + 1 waits for them, since it rewrites the shadow rays,
 // list and count and adds to the same path radiance.  The two casts claim
 // rays through separate counters.
-cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, cudaStream_t st)
+cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, const PtLane& lane)
 {
-    mrg::PtPaths& P = c->ptPaths;
+    mrg::PtPaths& P = *lane.P;
     const mrg::PtLaunch& L = R.L;
-    const bool overlap = pt_overlap();
-    if(overlap && !c->ptSideStream)
-    {
-        cudaError_t e = cudaStreamCreateWithFlags(&c->ptSideStream, cudaStreamNonBlocking);
-        if(e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ptEvShaded, cudaEventDisableTiming);
-        if(e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ptEvResolved, cudaEventDisableTiming);
-        if(e != cudaSuccess) return e;
-    }
-    cudaStream_t side = overlap ? c->ptSideStream : st;
-    mrg::TraceScratch shadowScr = R.scr;
-    if(overlap) shadowScr.workCounter = c->dScratch + 2;
+    cudaStream_t st = lane.st, side = lane.side;
+    const bool overlap = side != st;
+    mrg::TraceScratch closestScr = R.scr, shadowScr = R.scr;
+    closestScr.workCounter = lane.closestCounter;
+    shadowScr.workCounter = lane.shadowCounter;
     // with the cache every path has ended by vertex recPerPath + 1
     const uint32_t loops = (L.cache.mode == 1u) ? std::min(L.maxDepth, L.cache.recPerPath + 2u) : L.maxDepth;
     cudaError_t e = mrg::pt_raygen(L, P, P.listA, P.counts + 0, c->smCount, st);
@@ -643,7 +666,7 @@ cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, cudaStream_t st)
         uint32_t* nextCount = P.counts + ((depth & 1u) ? 0 : 1);
         e = cudaMemsetAsync(nextCount, 0, sizeof(uint32_t), st);
         if(e == cudaSuccess)
-            e = mrg::launch_closest(c->scene, R.scr, P.rays, alive, 0, P.hits, P.meta, c->smCount, st, aliveCount);
+            e = mrg::launch_closest(c->scene, closestScr, P.rays, alive, 0, P.hits, P.meta, c->smCount, st, aliveCount);
         const uint32_t* shadeList = alive;
         if(e == cudaSuccess && R.partition)
         {
@@ -656,20 +679,27 @@ cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, cudaStream_t st)
                                          P.sortHist, st);
             shadeList = P.listSorted;
         }
-        if(e == cudaSuccess && overlap && depth > 0) e = cudaStreamWaitEvent(st, c->ptEvResolved, 0);
+        if(e == cudaSuccess && overlap && depth > 0) e = cudaStreamWaitEvent(st, lane.evResolved, 0);
         if(e == cudaSuccess) e = cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), st);
         if(e == cudaSuccess)
             e = mrg::pt_shade_impl(L, P, R.T, shadeList, aliveCount, next, nextCount, c->smCount, st);
-        if(e == cudaSuccess && overlap) e = cudaEventRecord(c->ptEvShaded, st);
-        if(e == cudaSuccess && overlap) e = cudaStreamWaitEvent(side, c->ptEvShaded, 0);
+        if(e == cudaSuccess && overlap) e = cudaEventRecord(lane.evShaded, st);
+        if(e == cudaSuccess && overlap) e = cudaStreamWaitEvent(side, lane.evShaded, 0);
         if(e == cudaSuccess)
             e = mrg::launch_visibility(c->scene, shadowScr, P.visBits, P.shadowRays, P.shadowList, 0, c->smCount, side,
                                        P.counts + 2);
         if(e == cudaSuccess) e = mrg::pt_resolve(L, P, depth, c->smCount, side);
-        if(e == cudaSuccess && overlap) e = cudaEventRecord(c->ptEvResolved, side);
+        if(e == cudaSuccess && overlap) e = cudaEventRecord(lane.evResolved, side);
     }
-    if(e == cudaSuccess && overlap) e = cudaStreamWaitEvent(st, c->ptEvResolved, 0);
+    if(e == cudaSuccess && overlap) e = cudaStreamWaitEvent(st, lane.evResolved, 0);
     return e;
+}
+
+// Passes of mrg_pt_render run two at a time (MRG_PT_PIPELINES=1: one).
+bool pt_two_pipelines()
+{
+    const char* v = std::getenv("MRG_PT_PIPELINES");
+    return !(v && v[0] == '1');
 }
 
 } // namespace
@@ -684,11 +714,43 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
     mrg_status s = pt_setup(c, p, R, "mrg_pt_render");
     if(s != MRG_OK) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    for(uint32_t pass = 0; pass < p->spp / R.spp; pass++)
+    PtLane lanes[2];
+    if((s = pt_lane0(c, st, lanes[0])) != MRG_OK) return s;
+    // Two passes at a time: pass k runs on pipeline k mod 2 (own path state,
+    // streams and counters), so one pass's casts fill the SMs the other's
+    // leave idle.  Film writes stay in pass order (an event chain); the
+    // caller's stream waits for both pipelines at the end.
+    const uint32_t passes = p->spp / R.spp;
+    const bool two = passes >= 2 && pt_two_pipelines();
+    if(two)
     {
+        if((s = pt_paths_into(c->ptPaths2, c->ptPathMem2, R.slots)) != MRG_OK) return s;
+        if(!c->ptStream2)
+        {
+            PT_TRY(cudaStreamCreateWithFlags(&c->ptStream2, cudaStreamNonBlocking), "mrg_pt_render: stream");
+            PT_TRY(cudaStreamCreateWithFlags(&c->ptSideStream2, cudaStreamNonBlocking), "mrg_pt_render: stream");
+            for(cudaEvent_t* q : { &c->ptEvShaded2, &c->ptEvResolved2, &c->ptEvFilm, &c->ptEvStart, &c->ptEvDone2 })
+                PT_TRY(cudaEventCreateWithFlags(q, cudaEventDisableTiming), "mrg_pt_render: event");
+        }
+        const bool overlap = lanes[0].side != lanes[0].st;
+        lanes[1] = PtLane{ &c->ptPaths2, c->ptStream2, overlap ? c->ptSideStream2 : c->ptStream2, c->ptEvShaded2,
+                           c->ptEvResolved2, c->dScratch + 3, c->dScratch + (overlap ? 4 : 3) };
+        PT_TRY(cudaEventRecord(c->ptEvStart, st), "mrg_pt_render: event");
+        PT_TRY(cudaStreamWaitEvent(c->ptStream2, c->ptEvStart, 0), "mrg_pt_render: event wait");
+    }
+    for(uint32_t pass = 0; pass < passes; pass++)
+    {
+        const PtLane& lane = lanes[two ? (pass & 1u) : 0u];
         R.L.sampleBase = p->sampleStart + pass * R.spp;
-        PT_TRY(pt_bounces(c, R, st), "render pass");
-        PT_TRY(mrg::pt_film(R.L, c->ptPaths, reinterpret_cast<float4*>(dImage), st), "film");
+        PT_TRY(pt_bounces(c, R, lane), "render pass");
+        if(two && pass > 0) PT_TRY(cudaStreamWaitEvent(lane.st, c->ptEvFilm, 0), "film order");
+        PT_TRY(mrg::pt_film(R.L, *lane.P, reinterpret_cast<float4*>(dImage), lane.st), "film");
+        if(two) PT_TRY(cudaEventRecord(c->ptEvFilm, lane.st), "film order");
+    }
+    if(two)
+    {
+        PT_TRY(cudaEventRecord(c->ptEvDone2, c->ptStream2), "mrg_pt_render: event");
+        PT_TRY(cudaStreamWaitEvent(st, c->ptEvDone2, 0), "mrg_pt_render: event wait");
     }
     return MRG_OK;
 }
@@ -738,12 +800,14 @@ mrg_status mrg_pt_render_cached(mrg_ctx* c, const mrg_pt_params* p, float* dImag
     C.trainStride = trainPaths ? (uint32_t)std::max<size_t>(1, slots / trainPaths) : 0u;
     C.batchCap = (uint32_t)cap;
     mrg::PtPaths& P = c->ptPaths;
+    PtLane lane;
+    if((s = pt_lane0(c, st, lane)) != MRG_OK) return s;
     for(uint32_t pass = 0; pass < p->spp / R.spp; pass++)
     {
         R.L.sampleBase = p->sampleStart + pass * R.spp;
         PT_TRY(cudaMemsetAsync(counters, 0, 2 * sizeof(uint32_t), st), "mrg_pt_render_cached: counters");
         if(C.trainStride) PT_TRY(cudaMemsetAsync(C.recAux, 0, sizes[4], st), "mrg_pt_render_cached: records");
-        PT_TRY(pt_bounces(c, R, st), "cached pass");
+        PT_TRY(pt_bounces(c, R, lane), "cached pass");
         PT_TRY(mrg::nrc_query_list(c->cache, C.queryIn, C.queryList, C.queryCount, R.slots, C.queryOut, c->smCount, st),
                "cache query");
         PT_TRY(mrg::pt_cache_apply(P, C, c->smCount, st), "cache apply");
@@ -793,16 +857,18 @@ mrg_status mrg_pt_adjoint(mrg_ctx* c, const mrg_pt_params* p, uint32_t texId, co
     A.radTotal = static_cast<const float4*>(c->dPtRadTotal);
     A.texIndex = texId + 1u;
     A.invSpp = 1.0f / (float)p->spp;
+    PtLane lane;
+    if((s = pt_lane0(c, st, lane)) != MRG_OK) return s;
     for(uint32_t pass = 0; pass < p->spp / R.spp; pass++)
     {
         R.L.sampleBase = p->sampleStart + pass * R.spp;
         A.enabled = 0u;
-        PT_TRY(pt_bounces(c, R, st), "primal pass");
+        PT_TRY(pt_bounces(c, R, lane), "primal pass");
         if(dImage) PT_TRY(mrg::pt_film(R.L, c->ptPaths, reinterpret_cast<float4*>(dImage), st), "film");
         PT_TRY(cudaMemcpyAsync(c->dPtRadTotal, c->ptPaths.rad, sizeof(float4) * (size_t)R.slots,
                                cudaMemcpyDeviceToDevice, st), "primal radiance");
         A.enabled = 1u;
-        PT_TRY(pt_bounces(c, R, st), "replay pass");
+        PT_TRY(pt_bounces(c, R, lane), "replay pass");
     }
     return MRG_OK;
 }

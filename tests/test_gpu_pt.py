@@ -159,10 +159,11 @@ def test_partition_by_material_is_invisible():
     pt.close()
 
 
-def test_shadow_cast_overlap_is_invisible(monkeypatch):
+def test_stream_overlap_is_invisible(monkeypatch):
     """The shadow cast and resolve of a bounce run beside the next bounce's
-    closest-hit cast on a second stream; images are bit-identical to the
-    single-stream order (MRG_PT_OVERLAP=0), RGB and spectral."""
+    closest-hit cast on a second stream, and consecutive passes run on two
+    pipelines; images are bit-identical to the single-stream order
+    (MRG_PT_OVERLAP=0, MRG_PT_PIPELINES=1), RGB and spectral."""
     pt = PathTracer(0)
     load_box_scene(pt, scenes.box_scene_mixed(0))
     pt.set_env(scenes.sky_map(32, 16, seed=1))
@@ -174,14 +175,23 @@ def test_shadow_cast_overlap_is_invisible(monkeypatch):
                      for mode in (0, 1, 2)]
     for a, b in zip(out["0"], out["1"]):
         assert np.array_equal(a, b)
+    # several passes: pass k runs on pipeline k mod 2 unless MRG_PT_PIPELINES=1
+    multi = {}
+    for pipes in ("1", "2"):
+        monkeypatch.setenv("MRG_PT_PIPELINES", pipes)
+        multi[pipes] = pt.render(PathTracer.params(80, 60, 8, cam, sample_mode=2, seed=5, max_depth=10,
+                                                   samples_per_pass=2)).cpu().numpy()
+    assert np.array_equal(multi["1"], multi["2"])
     pt.close()
     surf, cam = scenes.c2_scene(0, texture_size=128)
     pt, _ = _spectral_pair(surf, dict(texels=scenes.sky_map(64, 32, seed=0)))
     imgs = []
-    for flag in ("0", "1"):
+    for flag, pipes in (("0", "1"), ("1", "1"), ("1", "2")):
         monkeypatch.setenv("MRG_PT_OVERLAP", flag)
-        imgs.append(pt.render(PathTracer.params(64, 36, 4, cam, max_depth=12, rr_start=3, seed=4)).cpu().numpy())
-    assert np.array_equal(imgs[0], imgs[1])
+        monkeypatch.setenv("MRG_PT_PIPELINES", pipes)
+        imgs.append(pt.render(PathTracer.params(64, 36, 8, cam, max_depth=12, rr_start=3, seed=4,
+                                                samples_per_pass=2)).cpu().numpy())
+    assert np.array_equal(imgs[0], imgs[1]) and np.array_equal(imgs[0], imgs[2])
     pt.close()
 
 
