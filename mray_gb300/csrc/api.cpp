@@ -183,6 +183,7 @@ mrg_status mrg_destroy(mrg_ctx* c)
                           c->ptEvStart, c->ptEvDone2 })
         if(q) cudaEventDestroy(q);
     cudaFree(c->ptPathMem2);
+    cudaFree(c->dPtRadTotal2);
     cudaFree(c->dHostCounters);
     for(cudaEvent_t& q : c->hostEvents) if(q) cudaEventDestroy(q);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);

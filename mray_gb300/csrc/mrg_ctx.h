@@ -111,6 +111,8 @@ struct mrg_ctx
     cudaStream_t ptStream2 = nullptr, ptSideStream2 = nullptr;
     cudaEvent_t  ptEvShaded2 = nullptr, ptEvResolved2 = nullptr;
     cudaEvent_t  ptEvFilm = nullptr, ptEvStart = nullptr, ptEvDone2 = nullptr;
+    void*        dPtRadTotal2 = nullptr;      // adjoint: primal radiance of the second pipeline
+    uint32_t     ptRadTotalCap2 = 0;
     void*     ptPathMem = nullptr;
     // skysphere boundary light: host copy of the radiance map and transform,
     // device block [texels | cdfX | cdfY]

@@ -695,11 +695,41 @@ cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, const PtLane& lane)
     return e;
 }
 
-// Passes of mrg_pt_render run two at a time (MRG_PT_PIPELINES=1: one).
+// Passes of mrg_pt_render and mrg_pt_adjoint run two at a time
+// (MRG_PT_PIPELINES=1: one).
 bool pt_two_pipelines()
 {
     const char* v = std::getenv("MRG_PT_PIPELINES");
     return !(v && v[0] == '1');
+}
+
+// The second pipeline: its path state, streams and events (created once),
+// counters 3 and 4; it starts after the caller's earlier work on st.
+mrg_status pt_lane1(mrg_ctx* c, uint32_t slots, cudaStream_t st, const PtLane& lane0, PtLane& lane1)
+{
+    mrg_status s = pt_paths_into(c->ptPaths2, c->ptPathMem2, slots);
+    if(s != MRG_OK) return s;
+    if(!c->ptStream2)
+    {
+        PT_TRY(cudaStreamCreateWithFlags(&c->ptStream2, cudaStreamNonBlocking), "mrg_pt: stream");
+        PT_TRY(cudaStreamCreateWithFlags(&c->ptSideStream2, cudaStreamNonBlocking), "mrg_pt: stream");
+        for(cudaEvent_t* q : { &c->ptEvShaded2, &c->ptEvResolved2, &c->ptEvFilm, &c->ptEvStart, &c->ptEvDone2 })
+            PT_TRY(cudaEventCreateWithFlags(q, cudaEventDisableTiming), "mrg_pt: event");
+    }
+    const bool overlap = lane0.side != lane0.st;
+    lane1 = PtLane{ &c->ptPaths2, c->ptStream2, overlap ? c->ptSideStream2 : c->ptStream2, c->ptEvShaded2,
+                    c->ptEvResolved2, c->dScratch + 3, c->dScratch + (overlap ? 4 : 3) };
+    PT_TRY(cudaEventRecord(c->ptEvStart, st), "mrg_pt: event");
+    PT_TRY(cudaStreamWaitEvent(c->ptStream2, c->ptEvStart, 0), "mrg_pt: event wait");
+    return MRG_OK;
+}
+
+// The caller's stream waits for the second pipeline.
+mrg_status pt_join(mrg_ctx* c, cudaStream_t st)
+{
+    PT_TRY(cudaEventRecord(c->ptEvDone2, c->ptStream2), "mrg_pt: event");
+    PT_TRY(cudaStreamWaitEvent(st, c->ptEvDone2, 0), "mrg_pt: event wait");
+    return MRG_OK;
 }
 
 } // namespace
@@ -722,22 +752,7 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
     // caller's stream waits for both pipelines at the end.
     const uint32_t passes = p->spp / R.spp;
     const bool two = passes >= 2 && pt_two_pipelines();
-    if(two)
-    {
-        if((s = pt_paths_into(c->ptPaths2, c->ptPathMem2, R.slots)) != MRG_OK) return s;
-        if(!c->ptStream2)
-        {
-            PT_TRY(cudaStreamCreateWithFlags(&c->ptStream2, cudaStreamNonBlocking), "mrg_pt_render: stream");
-            PT_TRY(cudaStreamCreateWithFlags(&c->ptSideStream2, cudaStreamNonBlocking), "mrg_pt_render: stream");
-            for(cudaEvent_t* q : { &c->ptEvShaded2, &c->ptEvResolved2, &c->ptEvFilm, &c->ptEvStart, &c->ptEvDone2 })
-                PT_TRY(cudaEventCreateWithFlags(q, cudaEventDisableTiming), "mrg_pt_render: event");
-        }
-        const bool overlap = lanes[0].side != lanes[0].st;
-        lanes[1] = PtLane{ &c->ptPaths2, c->ptStream2, overlap ? c->ptSideStream2 : c->ptStream2, c->ptEvShaded2,
-                           c->ptEvResolved2, c->dScratch + 3, c->dScratch + (overlap ? 4 : 3) };
-        PT_TRY(cudaEventRecord(c->ptEvStart, st), "mrg_pt_render: event");
-        PT_TRY(cudaStreamWaitEvent(c->ptStream2, c->ptEvStart, 0), "mrg_pt_render: event wait");
-    }
+    if(two && (s = pt_lane1(c, R.slots, st, lanes[0], lanes[1])) != MRG_OK) return s;
     for(uint32_t pass = 0; pass < passes; pass++)
     {
         const PtLane& lane = lanes[two ? (pass & 1u) : 0u];
@@ -747,12 +762,7 @@ mrg_status mrg_pt_render(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void
         PT_TRY(mrg::pt_film(R.L, *lane.P, reinterpret_cast<float4*>(dImage), lane.st), "film");
         if(two) PT_TRY(cudaEventRecord(c->ptEvFilm, lane.st), "film order");
     }
-    if(two)
-    {
-        PT_TRY(cudaEventRecord(c->ptEvDone2, c->ptStream2), "mrg_pt_render: event");
-        PT_TRY(cudaStreamWaitEvent(st, c->ptEvDone2, 0), "mrg_pt_render: event wait");
-    }
-    return MRG_OK;
+    return two ? pt_join(c, st) : MRG_OK;
 }
 
 mrg_status mrg_pt_render_cached(mrg_ctx* c, const mrg_pt_params* p, float* dImage, uint32_t trainPaths,
@@ -854,23 +864,47 @@ mrg_status mrg_pt_adjoint(mrg_ctx* c, const mrg_pt_params* p, uint32_t texId, co
     mrg::PtAdjoint& A = R.L.adj;
     A.delta = reinterpret_cast<const float4*>(dImageAdjoint);
     A.grad = dGrad;
-    A.radTotal = static_cast<const float4*>(c->dPtRadTotal);
     A.texIndex = texId + 1u;
     A.invSpp = 1.0f / (float)p->spp;
-    PtLane lane;
-    if((s = pt_lane0(c, st, lane)) != MRG_OK) return s;
-    for(uint32_t pass = 0; pass < p->spp / R.spp; pass++)
+    // passes (primal + replay each) on two pipelines as in mrg_pt_render; the
+    // gradient is a sum of atomic adds, so its value does not depend on it
+    PtLane lanes[2];
+    if((s = pt_lane0(c, st, lanes[0])) != MRG_OK) return s;
+    const uint32_t passes = p->spp / R.spp;
+    const bool two = passes >= 2 && pt_two_pipelines();
+    if(two)
     {
+        if(c->ptRadTotalCap2 < R.slots)
+        {
+            cudaFree(c->dPtRadTotal2);
+            c->dPtRadTotal2 = nullptr;
+            c->ptRadTotalCap2 = 0;
+            PT_TRY(cudaMalloc(&c->dPtRadTotal2, sizeof(float4) * (size_t)R.slots), "mrg_pt_adjoint: primal radiance");
+            c->ptRadTotalCap2 = R.slots;
+        }
+        if((s = pt_lane1(c, R.slots, st, lanes[0], lanes[1])) != MRG_OK) return s;
+    }
+    for(uint32_t pass = 0; pass < passes; pass++)
+    {
+        const uint32_t li = two ? (pass & 1u) : 0u;
+        const PtLane& lane = lanes[li];
+        float4* radTotal = static_cast<float4*>(li ? c->dPtRadTotal2 : c->dPtRadTotal);
         R.L.sampleBase = p->sampleStart + pass * R.spp;
+        A.radTotal = radTotal;
         A.enabled = 0u;
         PT_TRY(pt_bounces(c, R, lane), "primal pass");
-        if(dImage) PT_TRY(mrg::pt_film(R.L, c->ptPaths, reinterpret_cast<float4*>(dImage), st), "film");
-        PT_TRY(cudaMemcpyAsync(c->dPtRadTotal, c->ptPaths.rad, sizeof(float4) * (size_t)R.slots,
-                               cudaMemcpyDeviceToDevice, st), "primal radiance");
+        if(dImage)
+        {
+            if(two && pass > 0) PT_TRY(cudaStreamWaitEvent(lane.st, c->ptEvFilm, 0), "film order");
+            PT_TRY(mrg::pt_film(R.L, *lane.P, reinterpret_cast<float4*>(dImage), lane.st), "film");
+            if(two) PT_TRY(cudaEventRecord(c->ptEvFilm, lane.st), "film order");
+        }
+        PT_TRY(cudaMemcpyAsync(radTotal, lane.P->rad, sizeof(float4) * (size_t)R.slots,
+                               cudaMemcpyDeviceToDevice, lane.st), "primal radiance");
         A.enabled = 1u;
         PT_TRY(pt_bounces(c, R, lane), "replay pass");
     }
-    return MRG_OK;
+    return two ? pt_join(c, st) : MRG_OK;
 }
 
 } // extern "C"

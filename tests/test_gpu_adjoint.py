@@ -38,13 +38,15 @@ def _img(t):
     return t[..., :3] / t[..., 3:]
 
 
-def test_adjoint_matches_oracle_small():
+@pytest.mark.parametrize("spp_pass", [0, 1])
+def test_adjoint_matches_oracle_small(spp_pass):
+    """spp_pass 1: four passes, primal + replay each, on two pipelines."""
     tex = scenes.value_noise_texture(8, seed=0, dtype=np.float32)
     tgt_tex = scenes.value_noise_texture(8, seed=1, dtype=np.float32)
     dev = torch.from_numpy(tex.copy()).cuda()
     pt, tid, sphere = _tracer(dev, 12, 24)
     cam = scenes.box_camera()
-    p = PathTracer.params(16, 16, 4, cam, max_depth=4, rr_start=4, seed=5)
+    p = PathTracer.params(16, 16, 4, cam, max_depth=4, rr_start=4, seed=5, samples_per_pass=spp_pass)
     img = _img(pt.render(p))
     dev.copy_(torch.from_numpy(tgt_tex))
     tgt = _img(pt.render(p))
