@@ -516,12 +516,23 @@ mrg_status mrg_cast_closest_host(mrg_ctx* c, mrg_ray* hRays, uint32_t n, mrg_hit
     // staging buffers.
     const uint32_t chunks = host_chunks(n);
     cudaStream_t sIn = c->hostStreams[0], sOut = c->hostStreams[3];
+    // Chunk k covers rays [edge(k), edge(k + 1)).  With three or more chunks the
+    // first and last weigh a quarter of the others: the copy-in before the
+    // first cast and the copy-out after the last one are not overlapped.
+    const double wEnd = (chunks >= 3) ? 0.25 : 1.0;
+    const double wSum = (chunks >= 3) ? 2.0 * wEnd + (double)(chunks - 2) : (double)chunks;
+    auto edge = [&](uint32_t k) -> size_t {
+        if(k == 0) return 0;
+        if(k >= chunks) return n;
+        const double w = (chunks >= 3) ? wEnd + (double)(k - 1) : (double)k;
+        return std::min((size_t)n, (size_t)((double)n * w / wSum));
+    };
     for(uint32_t k = 0; k < chunks; k++)
     {
         cudaStream_t sCast = c->hostStreams[1 + (k & 1u)];
         mrg::TraceScratch scr = scratch_of(c);
         scr.workCounter = c->dHostCounters + k;
-        const size_t off = (size_t)n * k / chunks, cnt = (size_t)n * (k + 1) / chunks - off;
+        const size_t off = edge(k), cnt = edge(k + 1) - off;
         if(cnt == 0) continue;
         cudaEvent_t copied = c->hostEvents[2 * k], cast = c->hostEvents[2 * k + 1];
         MRG_TRY(cudaMemcpyAsync(c->dStageRays + off, hRays + off, sizeof(mrg_ray) * cnt, cudaMemcpyHostToDevice, sIn), "H2D rays");
