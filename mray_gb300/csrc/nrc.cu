@@ -11,6 +11,7 @@
 // never leave registers between layers.  Weights live in shared memory with
 // rows padded to 72 elements (conflict-free fragment loads).
 #include "mrg_nrc.h"
+#include "mrg_launch.h"
 
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -776,17 +777,18 @@ cudaError_t launch_forward(const NrcState& S, const float4* in, const uint32_t* 
     // warps per CTA: MRG_NRC_TRAIN_WARPS for training batches, MRG_NRC_QUERY_WARPS for inference
     constexpr int W = TRAIN ? MRG_NRC_TRAIN_WARPS : MRG_NRC_QUERY_WARPS;
     constexpr size_t smem = fwd_smem(W);
-    static bool configured = false;
-    static int perSM = 1;
-    if(!configured)
+    static int perSMOf[kMaxDevices] = {};          // 0: not configured on that device yet
+    int& perSM = perSMOf[launch_device()];
+    if(perSM == 0)
     {
         cudaError_t e = cudaFuncSetAttribute(k_nrc_forward<TRAIN, LIST, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if(e != cudaSuccess) return e;
-        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_nrc_forward<TRAIN, LIST, W>, W * 32, smem) != cudaSuccess ||
-           perSM < 1)
-            perSM = 1;
-        configured = true;
+        int b = 0;
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_nrc_forward<TRAIN, LIST, W>, W * 32, smem) != cudaSuccess ||
+           b < 1)
+            b = 1;
+        perSM = b;
     }
     const uint32_t tiles = (nMax + 16 * W - 1) / (16 * W);
     const uint32_t grid = std::max(1u, std::min(tiles, (uint32_t)smCount * (uint32_t)perSM * 2u));
@@ -856,16 +858,17 @@ cudaError_t nrc_gradients(NrcState& S, const float4* inputs, const float4* targe
     if(nMax > S.cap) return cudaErrorInvalidValue;
     constexpr int W = MRG_NRC_TRAIN_WARPS;
     constexpr size_t bsmem = bwd_smem(W);
-    static bool configured = false;
-    static int perSM = 1;
-    if(!configured)
+    static int perSMOf[kMaxDevices] = {};          // 0: not configured on that device yet
+    const int dev = launch_device();
+    int& perSM = perSMOf[dev];
+    if(perSM == 0)
     {
         cudaError_t e = cudaFuncSetAttribute(k_nrc_backward<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
         if(e != cudaSuccess) return e;
-        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_nrc_backward<W>, W * 32, bsmem) != cudaSuccess ||
-           perSM < 1)
-            perSM = 1;
-        configured = true;
+        int b = 0;
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_nrc_backward<W>, W * 32, bsmem) != cudaSuccess || b < 1)
+            b = 1;
+        perSM = b;
     }
     cudaError_t e = cudaMemsetAsync(S.loss, 0, sizeof(float), st);
     // the forward stores the activations and the outputs of the batch
@@ -877,11 +880,11 @@ cudaError_t nrc_gradients(NrcState& S, const float4* inputs, const float4* targe
         k_nrc_backward<W><<<grid, W * 32, bsmem, st>>>(S, inputs, S.y, targets, nDevice, nMax);
         e = cudaGetLastError();
     }
-    static bool wgConfigured = false;
-    if(e == cudaSuccess && !wgConfigured)
+    static bool wgConfigured[kMaxDevices] = {};
+    if(e == cudaSuccess && !wgConfigured[dev])
     {
         e = cudaFuncSetAttribute(k_nrc_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgSmem);
-        wgConfigured = e == cudaSuccess;
+        wgConfigured[dev] = e == cudaSuccess;
     }
     const uint32_t ctas = std::max(1u, std::min(S.partCtas, (nMax + kWgRows - 1) / kWgRows));
     if(e == cudaSuccess)

@@ -16,6 +16,7 @@
 // bit-exact restatements of MRay's host arithmetic (see mrg_device.cuh).
 #include "mrg_build.h"
 #include "mrg_device.cuh"
+#include "mrg_launch.h"
 
 namespace mrg {
 
@@ -449,7 +450,8 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
 template<bool ANY, bool STATS>
 int blocks_for(int smCount)
 {
-    static int perSM = 0;
+    static int perSMOf[kMaxDevices] = {};          // 0: not queried on that device yet
+    int& perSM = perSMOf[launch_device()];
     if(perSM == 0)
     {
         int b = 0;
