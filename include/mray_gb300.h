@@ -125,6 +125,17 @@ mrg_status mrg_add_instance(mrg_ctx* ctx, uint32_t mesh_id, const float m3x4[12]
  * Synchronous. */
 mrg_status mrg_build(mrg_ctx* ctx);
 
+/* Local cast.  Replaces BaseAcceleratorI::CastLocalRays
+ * (Source/Tracer/AcceleratorC.h:407-421; KCLocalRayCast,
+ * Source/Tracer/AcceleratorWork.kt.h:179-244).  For i in [0, n):
+ * r = d_ray_idx ? d_ray_idx[i] : i; ray r is cast against instance
+ * d_inst_ids[i] only (its BLAS, in the instance's local space, no instance-box
+ * test).  Writes as mrg_cast_closest (instance keys of d_inst_ids[i]).  An id
+ * >= the instance count skips the ray; mrg_sync_status reports it. */
+mrg_status mrg_cast_local(mrg_ctx* ctx, mrg_ray* d_rays, const uint32_t* d_ray_idx,
+                          const uint32_t* d_inst_ids, uint32_t n, mrg_hit_keys* d_hits,
+                          mrg_meta_hit* d_meta, void* stream);
+
 /* Closest hit.  Replaces BaseAcceleratorI::CastRays
  * (Source/Tracer/AcceleratorC.h:391-398; Source/Tracer/AcceleratorLBVH.cu:760-896).
  * For i in [0, n): r = d_ray_idx ? d_ray_idx[i] : i.  On a hit in

@@ -26,7 +26,7 @@ MRG_INSTANCE_CORRECTED_INVERSE = 0x2
 #: every function declared in include/mray_gb300.h
 EXPORTED = [
     "mrg_create", "mrg_destroy", "mrg_last_error", "mrg_status_string",
-    "mrg_upload_mesh", "mrg_add_instance", "mrg_build", "mrg_cast_closest",
+    "mrg_upload_mesh", "mrg_add_instance", "mrg_build", "mrg_cast_closest", "mrg_cast_local",
     "mrg_cast_visibility", "mrg_cast_closest_host", "mrg_scene_aabb", "mrg_get_stats",
     "mrg_sync_status", "mrg_cast_closest_stats", "mrg_cast_closest_host_noalloc",
     "mrg_pt_set_lambert", "mrg_pt_set_area_light", "mrg_pt_camera_frame", "mrg_pt_render",
@@ -103,6 +103,7 @@ def _declare(lib):
         "mrg_add_instance": (C.c_int, [vp, u32, fp, u32, u32, u32, u32, u32p]),
         "mrg_build": (C.c_int, [vp]),
         "mrg_cast_closest": (C.c_int, [vp, vp, vp, u32, vp, vp, vp]),
+        "mrg_cast_local": (C.c_int, [vp, vp, vp, vp, u32, vp, vp, vp]),
         "mrg_cast_visibility": (C.c_int, [vp, vp, vp, vp, u32, vp]),
         "mrg_cast_closest_host": (C.c_int, [vp, vp, u32, vp, vp]),
         "mrg_cast_closest_host_noalloc": (C.c_int, [vp, vp, u32, vp, vp]),

@@ -100,6 +100,16 @@ class Accelerator:
         N.check(self._lib.mrg_cast_closest(self._h, _ptr(rays), _ptr(ray_idx), n, _ptr(hits),
                                            _ptr(meta), _stream_ptr(stream)))
 
+    def cast_local_rays(self, rays, hits, meta, inst_ids, ray_idx=None, stream=None):
+        """Local cast on device buffers (CastLocalRays): listed ray i against
+        instance inst_ids[i] only.  inst_ids: int32/uint32 [n], n = the list
+        length (ray_idx) or the ray count."""
+        n = int(ray_idx.numel()) if ray_idx is not None else int(rays.shape[0])
+        if int(inst_ids.numel()) != n:
+            raise ValueError("cast_local_rays: one instance id per listed ray")
+        N.check(self._lib.mrg_cast_local(self._h, _ptr(rays), _ptr(ray_idx), _ptr(inst_ids), n, _ptr(hits),
+                                         _ptr(meta), _stream_ptr(stream)))
+
     def cast_visibility_rays(self, visible_bits, rays, ray_idx=None, count=None, stream=None):
         """Any hit (CastVisibilityRays) into a device bitspan of 32-bit words."""
         n = int(ray_idx.numel()) if ray_idx is not None else int(rays.shape[0])

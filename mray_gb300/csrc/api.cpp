@@ -435,6 +435,22 @@ mrg_status mrg_build(mrg_ctx* c)
     return MRG_OK;
 }
 
+mrg_status mrg_cast_local(mrg_ctx* c, mrg_ray* dRays, const uint32_t* dIdx, const uint32_t* dInst, uint32_t n,
+                          mrg_hit_keys* dHits, mrg_meta_hit* dMeta, void* stream)
+{
+    if(!c) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_local: null context");
+    if(!c->built) return fail(MRG_ERR_NOT_BUILT, "mrg_cast_local: call mrg_build first");
+    if(n == 0) return MRG_OK;
+    if(!dRays || !dInst || !dHits || !dMeta) return fail(MRG_ERR_INVALID_ARG, "mrg_cast_local: null buffer");
+    if(reinterpret_cast<uintptr_t>(dRays) % 32 != 0 || reinterpret_cast<uintptr_t>(dHits) % 16 != 0 ||
+       reinterpret_cast<uintptr_t>(dMeta) % 8 != 0)
+        return fail(MRG_ERR_INVALID_ARG, "mrg_cast_local: misaligned buffer");
+    DeviceGuard g(c->device);
+    MRG_TRY(mrg::launch_local(c->scene, scratch_of(c), dRays, dIdx, dInst, n, dHits, dMeta, c->smCount,
+                              static_cast<cudaStream_t>(stream)), "mrg_cast_local");
+    return MRG_OK;
+}
+
 mrg_status mrg_cast_closest(mrg_ctx* c, mrg_ray* dRays, const uint32_t* dIdx, uint32_t n,
                             mrg_hit_keys* dHits, mrg_meta_hit* dMeta, void* stream)
 {

@@ -91,6 +91,9 @@ enum TraceErrorBits : uint32_t
 
 // nDevice (optional): device word holding the ray count, read by the kernel
 // (device-driven wavefronts); when given, n is ignored.
+// Listed ray i against instance instIds[i] only (CastLocalRays).
+cudaError_t launch_local(const TraceScene& sc, const TraceScratch& scr, void* rays, const uint32_t* rayIdx,
+                         const uint32_t* instIds, uint32_t n, void* hits, void* meta, int smCount, cudaStream_t st);
 cudaError_t launch_closest(const TraceScene& sc, const TraceScratch& scr, void* rays,
                            const uint32_t* rayIdx, uint32_t n, void* hits, void* meta,
                            int smCount, cudaStream_t st, const uint32_t* nDevice = nullptr);

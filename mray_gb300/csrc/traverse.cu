@@ -170,11 +170,14 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
     return hm;
 }
 
-template<bool ANY, bool STATS>
+// LOCAL: listed ray i starts inside instance instIds[i] (its BLAS, in the
+// instance's space) and ends when that BLAS is exhausted: CastLocalRays.
+template<bool ANY, bool STATS, bool LOCAL = false>
 __global__ void __launch_bounds__(kTraceTPB, MRG_TRACE_MIN_BLOCKS)
 k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
         const uint32_t* __restrict__ rayIdx, uint32_t nHost, const uint32_t* __restrict__ nDevice,
-        uint4* __restrict__ hits, float2* __restrict__ meta, uint32_t* __restrict__ visBits)
+        uint4* __restrict__ hits, float2* __restrict__ meta, uint32_t* __restrict__ visBits,
+        const uint32_t* __restrict__ instIds = nullptr)
 {
     // The ray count comes from the host or, for casts inside a device-driven
     // wavefront, from device memory written by the previous kernel.
@@ -251,6 +254,26 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     steps = 0;
                     if(STATS) { statNodes = 0; statTris = 0; statInst = 0; statTlasNodes = 0; statDry = 0; }
                     live = true;
+                    if(LOCAL)
+                    {
+                        const uint32_t inst = __ldg(instIds + i);
+                        if(inst >= sc.instCount) { atomicOr(scr.errorFlag, kTraceBadIndex); live = false; }
+                        else
+                        {
+                            // enter the instance as at a TLAS leaf, with an empty world stack
+                            const float4* ip = reinterpret_cast<const float4*>(sc.insts + inst);
+                            const float4 m0 = __ldg(ip), m1 = __ldg(ip + 1), m2 = __ldg(ip + 2);
+                            const uint4 keys = __ldg(reinterpret_cast<const uint4*>(ip + 3));
+                            float3 lo;
+                            transform_ray_exact(m0, m1, m2, make_float3(wox, woy, woz), make_float3(wdx, wdy, wdz),
+                                                lo, ld);
+                            setup_level(lr, lo.x, lo.y, lo.z, ld.x, ld.y, ld.z);
+                            cull = (keys.w & kCullBit) != 0u;
+                            curInst = inst;
+                            blasBase = 0;
+                            ng = make_uint2(keys.w & ~kCullBit, (1u << (24u + lr.oct7)) | 1u);
+                        }
+                    }
                 }
             }
         }
@@ -447,7 +470,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
     }
 }
 
-template<bool ANY, bool STATS>
+template<bool ANY, bool STATS, bool LOCAL = false>
 int blocks_for(int smCount)
 {
     static int perSMOf[kMaxDevices] = {};          // 0: not queried on that device yet
@@ -455,7 +478,8 @@ int blocks_for(int smCount)
     if(perSM == 0)
     {
         int b = 0;
-        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<ANY, STATS>, kTraceTPB, 0) != cudaSuccess || b < 1)
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<ANY, STATS, LOCAL>, kTraceTPB, 0) != cudaSuccess ||
+           b < 1)
             b = 4;
         perSM = b;
     }
@@ -474,6 +498,18 @@ cudaError_t launch_closest(const TraceScene& sc, const TraceScratch& scr, void* 
     k_trace<false, false><<<blocks_for<false, false>(smCount), kTraceTPB, 0, st>>>(
         sc, scr, static_cast<float4*>(rays), rayIdx, n, nDevice, static_cast<uint4*>(hits),
         static_cast<float2*>(meta), nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_local(const TraceScene& sc, const TraceScratch& scr, void* rays, const uint32_t* rayIdx,
+                         const uint32_t* instIds, uint32_t n, void* hits, void* meta, int smCount, cudaStream_t st)
+{
+    if(n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(scr.workCounter, 0, sizeof(uint32_t), st);
+    if(e != cudaSuccess) return e;
+    k_trace<false, false, true><<<blocks_for<false, false, true>(smCount), kTraceTPB, 0, st>>>(
+        sc, scr, static_cast<float4*>(rays), rayIdx, n, nullptr, static_cast<uint4*>(hits),
+        static_cast<float2*>(meta), nullptr, instIds);
     return cudaGetLastError();
 }
 

@@ -55,6 +55,7 @@ def lib():
         for f in ("orc_cast_closest", "orc_cast_closest_linear"):
             getattr(L, f).argtypes = [vp, vp, vp, u32, vp, vp, vp, C.c_int]
         L.orc_cast_visibility.argtypes = [vp, vp, vp, u32, vp, C.c_int]
+        L.orc_cast_local.argtypes = [vp, vp, vp, vp, u32, vp, vp, C.c_int]
         L.orc_scene_stats.argtypes = [vp, vp]
         L.orc_pt_render.argtypes = [vp, vp, vp, vp, u32, vp, vp, vp, C.c_int]
         L.orc_spec_prepare.argtypes = [vp, vp, vp, C.c_float, u32, vp, vp]
@@ -144,6 +145,21 @@ class Scene:
         f(self._h, _vp(rays), _vp(ridx), n, _vp(hits), _vp(meta), _vp(inst),
           threads or default_threads())
         return rays, hits, meta, inst
+
+    def cast_local(self, rays, inst_ids, ray_idx=None, hits=None, meta=None, threads=None):
+        """CastLocalRays: listed ray i against instance inst_ids[i] only.
+        Returns (rays (tMax updated), hits [N,4] u32, meta [N,2] f32)."""
+        rays = np.array(rays, np.float32, copy=True, order="C")
+        n_total = rays.shape[0]
+        hits = np.zeros((n_total, 4), np.uint32) if hits is None else np.array(hits, np.uint32, copy=True)
+        meta = np.zeros((n_total, 2), np.float32) if meta is None else np.array(meta, np.float32, copy=True)
+        ridx = None if ray_idx is None else np.ascontiguousarray(ray_idx, np.uint32)
+        ids = np.ascontiguousarray(inst_ids, np.uint32)
+        n = n_total if ridx is None else ridx.shape[0]
+        assert ids.shape[0] == n
+        self._L.orc_cast_local(self._h, _vp(rays), _vp(ridx), _vp(ids), n, _vp(hits), _vp(meta),
+                               threads or default_threads())
+        return rays, hits, meta
 
     def cast_visibility(self, rays, ray_idx=None, bits=None, threads=None):
         rays = np.ascontiguousarray(rays, np.float32)

@@ -800,7 +800,8 @@ typedef struct
     orc_meta_hit*       meta;
     uint32_t*           hitInst;
     uint32_t*           vis;
-    int                 mode;     /* 0 closest, 1 linear, 2 visibility */
+    const uint32_t*     instIds;  /* mode 3: instance of each listed ray */
+    int                 mode;     /* 0 closest, 1 linear, 2 visibility, 3 local */
     atomic_uint         next;
 } cast_job;
 
@@ -825,7 +826,28 @@ static void* cast_worker(void* arg)
                 continue;
             }
             scene_hit h; memset(&h, 0, sizeof(h));
-            int got = (j->mode == 0) ? scene_cast(j->s, &j->rays[ri], 0, &h)
+            int got;
+            if(j->mode == 3)
+            {
+                /* KCLocalRayCast (AcceleratorWork.kt.h:179-244): the listed
+                 * instance only, the ray moved to its local space, ClosestHit
+                 * of its BLAS in [tMin, tMax); no instance-box test. */
+                const uint32_t ii = j->instIds[i];
+                if(ii >= j->s->instCount) continue;
+                const orc_inst* in = &j->s->insts[ii];
+                float ld[3], lp[3];
+                orc_transform_ray(in->inv, j->rays[ri].dir, j->rays[ri].pos, ld, lp);
+                float tmm[2] = { j->rays[ri].tMin, j->rays[ri].tMax };
+                blas_hit bh; memset(&bh, 0, sizeof(bh));
+                got = blas_traverse(&j->s->meshes[in->mesh], in->cull, ld, lp, tmm, 0, &bh);
+                if(got)
+                {
+                    h.hit = 1; h.t = bh.t; h.prim = bh.prim; h.inst = ii;
+                    h.bary[0] = bh.bary[0]; h.bary[1] = bh.bary[1]; h.bary[2] = bh.bary[2];
+                }
+            }
+            else
+                got = (j->mode == 0) ? scene_cast(j->s, &j->rays[ri], 0, &h)
                                      : scene_cast_linear(j->s, &j->rays[ri], &h);
             if(!got)
             {
@@ -877,6 +899,15 @@ void orc_cast_closest_linear(const orc_scene* s, orc_ray_gmem* rays, const uint3
     cast_job j; memset(&j, 0, sizeof(j));
     j.s = s; j.rays = rays; j.ridx = ridx; j.n = n; j.hits = hits; j.meta = meta;
     j.hitInst = hitInst; j.mode = 1;
+    run_job(&j, nthreads);
+}
+
+void orc_cast_local(const orc_scene* s, orc_ray_gmem* rays, const uint32_t* ridx, const uint32_t* inst_ids,
+                    uint32_t n, orc_hit_keys* hits, orc_meta_hit* meta, int nthreads)
+{
+    cast_job j; memset(&j, 0, sizeof(j));
+    j.s = s; j.rays = rays; j.ridx = ridx; j.instIds = inst_ids; j.n = n; j.hits = hits; j.meta = meta;
+    j.mode = 3;
     run_job(&j, nthreads);
 }
 

@@ -73,6 +73,12 @@ void orc_cast_closest(const orc_scene*, orc_ray_gmem* rays, const uint32_t* ray_
 void orc_cast_closest_linear(const orc_scene*, orc_ray_gmem* rays, const uint32_t* ray_idx,
                              uint32_t n, orc_hit_keys* hits, orc_meta_hit* meta,
                              uint32_t* hit_inst, int nthreads);
+/* Local cast: BaseAcceleratorI::CastLocalRays semantics (AcceleratorC.h:407-421,
+ * KCLocalRayCast AcceleratorWork.kt.h:179-244).  Listed ray i is cast against
+ * instance inst_ids[i] only (its BLAS, local space, no instance-box test);
+ * hits / meta / tMax as orc_cast_closest.  Out-of-range ids are skipped. */
+void orc_cast_local(const orc_scene*, orc_ray_gmem* rays, const uint32_t* ray_idx, const uint32_t* inst_ids,
+                    uint32_t n, orc_hit_keys* hits, orc_meta_hit* meta, int nthreads);
 /* Any hit: CastVisibilityRays semantics.  visible_bits has one bit per ray
  * index (set = visible); bits of the listed rays are set then cleared on a hit. */
 void orc_cast_visibility(const orc_scene*, const orc_ray_gmem* rays, const uint32_t* ray_idx,

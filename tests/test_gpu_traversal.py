@@ -214,6 +214,45 @@ def test_zero_rays_and_not_built_errors():
         acc.add_instance(5, m[0])
 
 
+@pytest.mark.parametrize("cull", [True, False])
+def test_local_cast_matches_oracle(cull):
+    """mrg_cast_local (CastLocalRays): random instance per listed ray, an index
+    list over part of the rays, prefilled hits that misses keep; bit-exact
+    against the oracle.  An out-of-range instance id skips its ray and is
+    reported by mrg_sync_status."""
+    import torch
+    pos, idx, m = small(3, 8, seed=2)
+    acc, S = build_pair(pos, idx, m, cull=cull)
+    rays = scenes.primary_rays(96, 64, 9, eye=(0, 0, -10), tan_half_fov=0.35)   # ~29% of rays hit
+    n = rays.shape[0]
+    rng = np.random.default_rng(4)
+    sel = np.sort(rng.permutation(n)[: n * 3 // 4]).astype(np.uint32)
+    # two thirds: the instance of the ray's closest hit (when it hits); the rest random
+    own = S.cast_closest(rays)[3][sel]
+    ids = rng.integers(0, m.shape[0], sel.shape[0]).astype(np.uint32)
+    take = (own != MISS) & (rng.random(sel.shape[0]) < 2.0 / 3.0)
+    ids[take] = own[take]
+    pre = np.full((n, 4), 0x5A5A5A5A, np.uint32)
+    ora = S.cast_local(rays, ids, ray_idx=sel, hits=pre)
+    dr = torch.from_numpy(rays.copy()).cuda()
+    dh = torch.from_numpy(pre.view(np.int32).copy()).cuda()
+    dm = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
+    di = torch.from_numpy(ids.view(np.int32)).cuda()
+    ds = torch.from_numpy(sel.view(np.int32)).cuda()
+    acc.cast_local_rays(dr, dh, dm, di, ray_idx=ds)
+    acc.sync_status()
+    got = (dr.cpu().numpy(), dh.cpu().numpy().view(np.uint32), dm.cpu().numpy())
+    assert np.array_equal(got[0].view(np.uint32), ora[0].view(np.uint32))
+    assert np.array_equal(got[1], ora[1])
+    hit = ora[1][:, 0] != 0x5A5A5A5A
+    assert hit.sum() > 400
+    assert np.array_equal(got[2][hit].view(np.uint32), ora[2][hit].view(np.uint32))
+    bad = torch.full((n,), m.shape[0], dtype=torch.int32, device="cuda")
+    acc.cast_local_rays(dr, dh, dm, bad)
+    with pytest.raises(MRGError):
+        acc.sync_status()
+
+
 def test_host_buffer_entry_point_matches_device():
     pos, idx, m = small(4, 27)
     acc, S = build_pair(pos, idx, m)

@@ -52,6 +52,34 @@ def test_hit_keys_and_misses_untouched(built_libs):
     assert (r[hit, 7] < rays[hit, 7]).all()
 
 
+def test_local_cast(built_libs):
+    """CastLocalRays: given the instance of its closest hit, a ray finds the
+    same hit locally; given another instance, a hit is never closer than the
+    scene's closest and carries that instance's keys; misses stay untouched."""
+    S, *_ = small_scene(ninst=8)
+    rays = scenes.primary_rays(40, 40, 5, eye=(0, 0, -12), tan_half_fov=0.5)
+    r, h, m, inst = S.cast_closest(rays)
+    hit = inst != MISS
+    own = np.where(hit, inst, 0).astype(np.uint32)
+    r2, h2, m2 = S.cast_local(rays, own, threads=2)
+    assert np.array_equal(h2[hit], h[hit]) and np.array_equal(r2[hit], r[hit]) and np.array_equal(m2[hit], m[hit])
+    rng = np.random.default_rng(1)
+    other = rng.integers(0, 8, rays.shape[0]).astype(np.uint32)
+    pre = np.full((rays.shape[0], 4), 0xABCDEF, np.uint32)
+    r3, h3, m3 = S.cast_local(rays, other, hits=pre, threads=2)
+    got = h3[:, 0] != 0xABCDEF
+    assert got.any() and (~got).any()
+    assert np.array_equal(r3[~got], rays[~got])
+    assert np.array_equal(h3[got, 1], 100 + other[got])
+    assert np.array_equal(h3[got, 3], (2 << 20) | other[got])
+    closer = got & hit
+    assert (r3[closer, 7] >= r[closer, 7]).all()
+    # out-of-range instance ids skip the ray
+    bad = np.full(rays.shape[0], 8, np.uint32)
+    r4, h4, _ = S.cast_local(rays, bad, hits=pre, threads=2)
+    assert (h4 == 0xABCDEF).all() and np.array_equal(r4, rays)
+
+
 def test_indirection_and_visibility(built_libs):
     S, *_ = small_scene()
     rays = scenes.primary_rays(40, 40, 3, eye=(0, 0, -12), tan_half_fov=0.5)
