@@ -73,14 +73,17 @@ typedef struct mrg_params
     uint32_t reserved[7];
 } mrg_params;
 
+/* Accelerator figures: BaseAcceleratorI::GPUMemoryUsage, TotalAccelCount,
+ * TotalInstanceCount (Source/Tracer/AcceleratorC.h:425-428) and build data. */
 typedef struct mrg_accel_stats
 {
     uint64_t blasNodes;        /* 8-wide nodes over all BLASes */
     uint64_t blasTriangles;    /* triangle records */
     uint64_t tlasNodes;
-    uint64_t instances;
-    uint64_t deviceBytes;      /* accelerator bytes resident on the device */
+    uint64_t instances;        /* TotalInstanceCount */
+    uint64_t deviceBytes;      /* accelerator bytes resident on the device (GPUMemoryUsage) */
     double   buildMs;          /* last mrg_build wall time */
+    uint64_t accelerators;     /* BLASes, one per uploaded mesh (TotalAccelCount) */
 } mrg_accel_stats;
 
 typedef struct mrg_ctx mrg_ctx;

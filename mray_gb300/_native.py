@@ -75,7 +75,7 @@ class MrgParams(C.Structure):
 class MrgAccelStats(C.Structure):
     _fields_ = [("blasNodes", C.c_uint64), ("blasTriangles", C.c_uint64),
                 ("tlasNodes", C.c_uint64), ("instances", C.c_uint64),
-                ("deviceBytes", C.c_uint64), ("buildMs", C.c_double)]
+                ("deviceBytes", C.c_uint64), ("buildMs", C.c_double), ("accelerators", C.c_uint64)]
 
 
 class MRGError(RuntimeError):

@@ -586,6 +586,7 @@ mrg_status mrg_get_stats(mrg_ctx* c, mrg_accel_stats* out)
                        mrg::kTriRecordBytes * c->blasTris +
                        (sizeof(mrg::HostInstRecord) + 4) * c->insts.size();
     out->buildMs = c->buildMs;
+    out->accelerators = c->built ? c->meshes.size() : 0;
     return MRG_OK;
 }
 

@@ -69,6 +69,9 @@ def test_batched_blas_build_mixed_mesh_sizes():
             inst += 1
     acc.construct()
     S.build()
+    st = acc.stats()
+    assert st["accelerators"] == len(sizes) and st["instances"] == 2 * len(sizes)
+    assert st["blasTriangles"] == sum(sizes)
     rays = scenes.primary_rays(160, 120, 4, eye=(0, 0, -16), tan_half_fov=0.45)
     ora = S.cast_closest(rays)
     gpu = gpu_closest(acc, rays)
@@ -303,4 +306,4 @@ def test_stress_scene_full_size_parity():
     shadow = scenes.shadow_rays(bounce, (0.0, 80.0, -60.0))
     assert np.array_equal(gpu_visibility(acc, shadow), S.cast_visibility(shadow))
     st = acc.stats()
-    assert st["blasTriangles"] == 1310720 and st["instances"] == 64
+    assert st["blasTriangles"] == 1310720 and st["instances"] == 64 and st["accelerators"] == 1
