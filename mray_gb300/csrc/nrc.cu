@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 namespace mrg {
 
@@ -572,12 +573,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
 __global__ void __launch_bounds__(kWgThreads, 1)
 k_nrc_wgrad_tc(const __grid_constant__ CUtensorMap tmG, const __grid_constant__ CUtensorMap tmA,
                const uint32_t* __restrict__ nDevice, uint32_t nMax, float* __restrict__ part,
-               uint32_t* __restrict__ err)
+               uint32_t* __restrict__ err, uint32_t stallItem)
 {
     extern __shared__ uint8_t wgRaw[];
     uint8_t* tiles = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(wgRaw) + 1023) & ~(uintptr_t)1023);
     __shared__ uint64_t full[kWgStages], empty[kWgStages], done;
-    __shared__ uint32_t tmemSlot, aborted, issued, consumed;
+    __shared__ uint32_t tmemSlot, aborted, issued, consumed, skipped;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
     const uint32_t n = nDevice ? min(*nDevice, nMax) : nMax;
     const uint32_t chunks = (n + kWgRows - 1) / kWgRows;
@@ -594,7 +595,7 @@ k_nrc_wgrad_tc(const __grid_constant__ CUtensorMap tmG, const __grid_constant__ 
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&done)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        aborted = 0u; issued = 0u; consumed = 0u;
+        aborted = 0u; issued = 0u; consumed = 0u; skipped = 0xFFFFFFFFu;
     }
     if(warp == 0u)
     {
@@ -616,6 +617,13 @@ k_nrc_wgrad_tc(const __grid_constant__ CUtensorMap tmG, const __grid_constant__ 
             const uint32_t s = it % kWgStages, round = it / kWgStages;
             if(!mbar_wait(smem_u32(&empty[s]), (round & 1u) ^ 1u, deadline)) { atomicExch(&aborted, 1u); break; }
             if(*reinterpret_cast<volatile uint32_t*>(&aborted)) break;
+            if(it == stallItem && blockIdx.x == 0u)
+            {
+                // test hook: this stage's copy is never issued, so the MMA
+                // warp's bounded wait on it runs out (no fault, no trap)
+                *reinterpret_cast<volatile uint32_t*>(&skipped) = it;
+                continue;
+            }
             const uint32_t chunk = blockIdx.x + (it / kNrcLayers) * gridDim.x, layer = it % kNrcLayers;
             const uint32_t dst = smem_u32(tiles + s * kWgStageBytes), bar = smem_u32(&full[s]);
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(kWgStageBytes) : "memory");
@@ -631,7 +639,9 @@ k_nrc_wgrad_tc(const __grid_constant__ CUtensorMap tmG, const __grid_constant__ 
         for(; it < items; it++)
         {
             const uint32_t s = it % kWgStages, round = it / kWgStages;
-            if(!mbar_wait(smem_u32(&full[s]), round & 1u, deadline)) { if(lane == 0u) atomicExch(&aborted, 1u); break; }
+            // warp-uniform: every lane leaves together if any lane's wait ran out
+            const bool landed = mbar_wait(smem_u32(&full[s]), round & 1u, deadline);
+            if(!__all_sync(0xFFFFFFFFu, landed)) { if(lane == 0u) atomicExch(&aborted, 1u); break; }
             const uint32_t chunk = blockIdx.x + (it / kNrcLayers) * gridDim.x, layer = it % kNrcLayers;
             uint8_t* st = tiles + s * kWgStageBytes;
             const uint32_t rows = min(kWgRows, n - chunk * kWgRows);
@@ -675,7 +685,8 @@ k_nrc_wgrad_tc(const __grid_constant__ CUtensorMap tmG, const __grid_constant__ 
             atomicOr(err, kNrcWaitTimeout);
             // copies issued but never consumed may still be landing: wait for them
             for(uint32_t it = consumed; it < issued; it++)
-                mbar_wait(smem_u32(&full[it % kWgStages]), (it / kWgStages) & 1u, clock64() + kWgWaitCycles);
+                if(it != skipped)
+                    mbar_wait(smem_u32(&full[it % kWgStages]), (it / kWgStages) & 1u, clock64() + kWgWaitCycles);
         }
     }
     else
@@ -889,7 +900,11 @@ cudaError_t nrc_gradients(NrcState& S, const float4* inputs, const float4* targe
     const uint32_t ctas = std::max(1u, std::min(S.partCtas, (nMax + kWgRows - 1) / kWgRows));
     if(e == cudaSuccess)
     {
-        k_nrc_wgrad_tc<<<ctas, kWgThreads, kWgSmem, st>>>(S.tmG16, S.tmActs, nDevice, nMax, S.wgPart, S.err);
+        // MRG_TEST_WGRAD_STALL=1 (tests only): CTA 0 never issues its first copy
+        const char* stall = std::getenv("MRG_TEST_WGRAD_STALL");
+        const uint32_t stallItem = (stall && stall[0] == '1') ? 0u : 0xFFFFFFFFu;
+        k_nrc_wgrad_tc<<<ctas, kWgThreads, kWgSmem, st>>>(S.tmG16, S.tmActs, nDevice, nMax, S.wgPart, S.err,
+                                                         stallItem);
         e = cudaGetLastError();
     }
     if(e == cudaSuccess)

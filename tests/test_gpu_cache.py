@@ -97,6 +97,29 @@ def test_weight_gradients_ragged_batches(n):
     c.close()
 
 
+def test_weight_gradient_wait_timeout_is_reported(monkeypatch):
+    """A copy the tensor-core weight-gradient kernel waits for never arrives
+    (test hook: the first stage of CTA 0 is not issued).  The bounded wait runs
+    out (about a second), the kernel drains its other copies, frees its TMEM and
+    returns; the call reports the error and the next call is correct."""
+    from mray_gb300 import MRGError
+    c = _cache(8, 12)
+    w, t = _random_params(c, 11)
+    x = _batch(4096, 12)
+    tgt = np.zeros((4096, 4), np.float32)
+    tgt[:, :3] = np.random.default_rng(13).random((4096, 3))
+    xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(tgt).cuda()
+    monkeypatch.setenv("MRG_TEST_WGRAD_STALL", "1")
+    with pytest.raises(MRGError, match="barrier wait ran out"):
+        c.gradients(xd, td)
+    monkeypatch.delenv("MRG_TEST_WGRAD_STALL")
+    _, gw, _ = c.gradients(xd, td)
+    ref = nrc.CacheRef(8, 12, 16, 2048, AABB)
+    _, gwr, _ = ref.gradients(x, tgt, w, t, bf16=True)
+    assert np.linalg.norm(gw - gwr) / np.linalg.norm(gwr) <= 2e-2
+    c.close()
+
+
 def test_training_fits_a_radiance_field():
     """Online training on a smooth synthetic radiance field: the relative L2
     loss falls by at least 10x within 300 Adam steps."""
