@@ -198,6 +198,39 @@ def test_edge_rays():
     assert np.array_equal(gpu_visibility(acc, rays), S.cast_visibility(rays))
 
 
+def test_scale_extremes():
+    """Instances scaled by 1e-3 .. 1e3 in one scene (TLAS quantisation and box
+    inflation across six orders of magnitude) and a mesh placed 1e5 away from
+    its own origin (BLAS quantisation frames with large exponents)."""
+    pos, idx = scenes.icosphere(3, 1.0, 0.05, 4.0, 5)
+    far = (pos + np.float32(1.0e5)).astype(np.float32)
+    acc = Accelerator(0)
+    S = oracle.Scene()
+    ids = []
+    for k, p in enumerate((pos, far)):
+        ids.append((acc.upload_mesh(p, idx, prim_key_base=0x10000000 + 0x100000 * k),
+                    S.add_mesh(p, idx, prim_key_base=0x10000000 + 0x100000 * k)))
+    mats = []
+    for i, (sc, t) in enumerate(((1e-3, (0.0, 0.0, 0.0)), (1.0, (3.0, 0.0, 0.0)), (1e3, (0.0, 0.0, 3000.0)),
+                                  (1e-2, (0.01, 0.005, 0.0)), (1.0, (-1.0e5 - 3.0, -1.0e5, -1.0e5)))):
+        m = np.zeros((3, 4), np.float32)
+        m[:, :3] = np.eye(3) * sc
+        m[:, 3] = t
+        mats.append((1 if i == 4 else 0, m.reshape(12)))
+    for i, (mesh, m) in enumerate(mats):
+        acc.add_instance(ids[mesh][0], m, light_or_mat_key=i, trans_key=(1 << 24) | i, accel_key=i)
+        S.add_instance(ids[mesh][1], m, lm_key=i, trans_key=(1 << 24) | i, accel_key=i)
+    acc.construct()
+    S.build()
+    rays = []
+    for eye, fov in (((0, 0, -0.01), 0.3), ((0, 0, -10), 0.5), ((0, 0, -1.0e4), 0.4)):
+        rays.append(scenes.primary_rays(80, 60, 3, eye=eye, tan_half_fov=fov))
+    rays = np.ascontiguousarray(np.vstack(rays))
+    n, hits, ties = compare_closest(S.cast_closest(rays), gpu_closest(acc, rays))
+    assert hits > 1000
+    assert np.array_equal(gpu_visibility(acc, rays), S.cast_visibility(rays))
+
+
 def test_zero_rays_and_not_built_errors():
     import torch
     from mray_gb300 import Accelerator
