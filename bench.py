@@ -397,11 +397,16 @@ def c3_adjoint(args, dev):
 
 
 def c4_equal_time(args, dev, spp_per_frame=8):
-    """Radiance cache on the production scene (RGB, 480x270, depth 12):
-    relMSE against a 4096-spp plain render, for plain path tracing at 16 spp
-    and for cache-assisted frames (spp_per_frame samples per pixel in one
-    pass, ~32,768 of its paths training the cache) in the same time, after 64
-    warm-up frames."""
+    """Radiance cache on the production scene (RGB, 1920x1080, depth 12; 16
+    levels x 2 x 2^19 hash grid, 5 hidden 64-wide layers, lr 1e-2, about
+    32,768 training paths = up to 65,536 training samples per frame, paths
+    end in the cache after one bounce), relMSE against a 4096-spp plain
+    render, after 64 warm-up frames:
+    - equal time: cache-assisted frames of spp_per_frame samples in the time
+      of a 16-spp plain render;
+    - time to quality: the cheapest single cache-assisted frame (1, 2, 4 or
+      8 spp) whose relMSE is at most the 16-spp plain render's, and the
+      plain render's time over it."""
     import torch
     from mray_gb300.pt import PathTracer, load_box_scene
     from mray_gb300.cache import RadianceCache
@@ -411,47 +416,58 @@ def c4_equal_time(args, dev, spp_per_frame=8):
     load_box_scene(pt, surf)
     pt.set_env(scenes.sky_map(1024, 512, seed=0))
     cache = RadianceCache(owner=pt, aabb=tuple(float(v) for v in pt.acc.scene_aabb()), max_batch=65536)
-    w, h = 480, 270
+    w, h = 1920, 1080
 
     def P(spp, seed, start=0, spp_pass=0):
         return PathTracer.params(w, h, spp, cam, max_depth=12, rr_start=3, seed=seed, sample_start=start,
                                  samples_per_pass=spp_pass)
 
-    ref = pt.render(P(4096, 1, spp_pass=64))
+    ref = pt.render(P(4096, 1, spp_pass=16))
     ref = (ref[..., :3] / ref[..., 3:]).double()
 
     def relmse(img):
         im = (img[..., :3] / img[..., 3:]).double()
         return float(torch.mean((im - ref) ** 2 / (ref ** 2 + 1e-2)))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return out, e0.elapsed_time(e1)
+
     pt.render(P(16, 7))
-    torch.cuda.synchronize(dev)
-    e0.record()
-    plain = pt.render(P(16, 2))
-    e1.record()
-    torch.cuda.synchronize(dev)
-    t_plain = e0.elapsed_time(e1)
+    plain, t_plain = timed(lambda: pt.render(P(16, 2)))
+    plain_rel = relmse(plain)
     k = spp_per_frame
     for f in range(64):
         pt.render_cached(P(k, 100 + f, start=k * f), train_paths=32768)
-    torch.cuda.synchronize(dev)
-    e0.record()
-    pt.render_cached(P(k, 300, start=0), train_paths=32768)
-    e1.record()
-    torch.cuda.synchronize(dev)
-    t_frame = e0.elapsed_time(e1)
+    _, t_frame = timed(lambda: pt.render_cached(P(k, 300, start=0), train_paths=32768))
     frames = max(1, int(t_plain // t_frame))
-    img = None
-    e0.record()
-    for f in range(frames):
-        img, _ = pt.render_cached(P(k, 1000 + f, start=k * f), image=img, train_paths=32768)
-    e1.record()
-    torch.cuda.synchronize(dev)
-    t_cached = e0.elapsed_time(e1)
-    out = {"c4_plain_16spp_ms": round(t_plain, 2), "c4_plain_relmse": round(relmse(plain), 5),
+
+    def run_frames():
+        img = None
+        for f in range(frames):
+            img, _ = pt.render_cached(P(k, 1000 + f, start=k * f), image=img, train_paths=32768)
+        return img
+    img, t_cached = timed(run_frames)
+    out = {"c4_plain_16spp_ms": round(t_plain, 2), "c4_plain_relmse": round(plain_rel, 5),
            "c4_cached_frame_ms": round(t_frame, 3), "c4_cached_frames": frames, "c4_cached_spp_per_frame": k,
-           "c4_cached_ms": round(t_cached, 2), "c4_cached_relmse": round(relmse(img), 5),
-           "c4_workload": "production scene RGB 480x270 depth 12, reference 4096 spp plain"}
+           "c4_cached_ms": round(t_cached, 2), "c4_cached_relmse": round(relmse(img), 5)}
+    best = None
+    for spp in (1, 2, 4, 8):
+        one, t_one = timed(lambda: pt.render_cached(P(spp, 2000 + spp, start=0), train_paths=32768)[0])
+        rel = relmse(one)
+        out["c4_cached_%dspp_ms" % spp] = round(t_one, 3)
+        out["c4_cached_%dspp_relmse" % spp] = round(rel, 5)
+        if best is None and rel <= plain_rel:
+            best = (spp, t_one)
+    if best is not None:
+        out["c4_time_to_plain_quality_ms"] = round(best[1], 3)
+        out["c4_time_to_plain_quality_speedup"] = round(t_plain / best[1], 2)
+    out["c4_workload"] = "production scene RGB 1920x1080 depth 12, reference 4096 spp plain"
     pt.close()
     return out
 

@@ -314,8 +314,9 @@ mrg_status mrg_pt_adjoint(mrg_ctx* ctx, const mrg_pt_params* params, uint32_t te
 /* ---- Radiance cache (no reference counterpart) ----------------------------- */
 /* A multiresolution hash grid (levels x 2 features x 2^log2_table_size fp16
  * entries per level, resolutions base..max geometrically) feeding a fully
- * fused MLP of 5 layers, 64 wide, ReLU, BF16 tensor cores with FP32
- * accumulation (4 x 64x64 + 16x64 weights, no biases), trained online with
+ * fused MLP of 5 hidden 64-wide ReLU layers and a 16-wide output layer, BF16
+ * tensor cores with FP32 accumulation (5 x 64x64 + 16x64 weights, no
+ * biases), trained online with
  * Adam on a relative L2 loss.  One cache per context.
  * Per sample 16 floats: position xyz, roughness | outgoing direction xyz, 0 |
  * normal xyz, 0 | albedo rgb, 0; positions are normalised to aabb.  Outputs
@@ -339,8 +340,8 @@ mrg_status mrg_cache_query(mrg_ctx* ctx, const float* d_inputs, uint32_t n, floa
  * call synchronous. */
 mrg_status mrg_cache_train(mrg_ctx* ctx, const float* d_inputs, const float* d_targets, uint32_t n,
                            float* h_loss, void* stream);
-/* Parameters as fp32 host arrays: 17,408 MLP weights (W0..W3 [64][64] then
- * W4 [16][64], row-major out x in) and levels * 2^log2_table_size * 2 table
+/* Parameters as fp32 host arrays: 21,504 MLP weights (hidden W0..W4 [64][64]
+ * then output W5 [16][64], row-major out x in) and levels * 2^log2_table_size * 2 table
  * features; either pointer may be NULL. */
 mrg_status mrg_cache_get_params(mrg_ctx* ctx, float* h_weights, float* h_table);
 /* The loss gradients of one batch, without an optimiser step (layouts as

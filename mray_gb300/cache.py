@@ -8,7 +8,7 @@ import numpy as np
 from . import _native as N
 from .accel import _stream_ptr
 
-WEIGHTS = 4 * 64 * 64 + 16 * 64
+WEIGHTS = 5 * 64 * 64 + 16 * 64          # hidden W0..W4 [64][64], output W5 [16][64]
 
 
 class RadianceCache:

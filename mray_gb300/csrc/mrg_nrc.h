@@ -1,5 +1,6 @@
 // mrg_nrc.h -- radiance cache: multiresolution hash-grid encoding + fully
-// fused 5-layer, 64-wide ReLU MLP (BF16 tensor cores, FP32 accumulation),
+// fused MLP of 5 hidden 64-wide ReLU layers and a 16-wide output layer
+// (BF16 tensor cores, FP32 accumulation),
 // trained online with Adam.  No reference counterpart.
 #pragma once
 #include <cstdint>
@@ -10,10 +11,11 @@ namespace mrg {
 
 constexpr int kNrcWidth = 64;          // hidden width = input width
 constexpr int kNrcOut = 16;            // output rows (RGB in the first 3)
-constexpr int kNrcLayers = 5;          // 4 hidden (64x64) + output (16x64)
+constexpr int kNrcHidden = 5;          // hidden layers, each 64x64 with ReLU
+constexpr int kNrcLayers = kNrcHidden + 1;   // + the 16x64 output layer
 constexpr int kNrcHashFeatures = 32;   // levels * features per level
 constexpr int kNrcInputFloats = 16;    // per sample: pos, rough | dir | normal | albedo
-constexpr int kNrcWeightCount = 4 * kNrcWidth * kNrcWidth + kNrcOut * kNrcWidth;   // 17,408
+constexpr int kNrcWeightCount = kNrcHidden * kNrcWidth * kNrcWidth + kNrcOut * kNrcWidth;   // 21,504
 
 struct NrcGrid
 {
@@ -31,7 +33,7 @@ struct NrcState
 {
     NrcGrid   grid;
     // parameters: MLP master weights (fp32) + bf16 copies, table master (fp32) + fp16 copy
-    float*    w32;            // kNrcWeightCount: W0..W3 [64][64] row-major (out, in), W4 [16][64]
+    float*    w32;            // kNrcWeightCount: W0..W4 [64][64] row-major (out, in), W5 [16][64]
     uint16_t* w16;            // bf16 bits of w32
     float*    t32;            // levels * 2^log2Table * featuresPerLevel
     uint16_t* t16;            // fp16 bits of t32
@@ -41,8 +43,8 @@ struct NrcState
     uint32_t  step;
     float     lr, beta1, beta2, eps;
     // training scratch (capacity samples)
-    uint16_t* acts;           // [cap][5][64] bf16: x0, a1, a2, a3, a4
-    uint16_t* g16;            // [cap][5][64] bf16: g_z1..g_z4, then dL/dy in columns 0..15 (16..63 stay 0)
+    uint16_t* acts;           // [cap][6][64] bf16: x0, a1 .. a5
+    uint16_t* g16;            // [cap][6][64] bf16: g_z1..g_z5, then dL/dy in columns 0..15 (16..63 stay 0)
     float4*   y;              // [cap] forward outputs of the training batch
     float*    loss;           // [1]
     float*    wgPart;         // [partCtas][kNrcWeightCount]: per-CTA weight-gradient partials

@@ -25,10 +25,11 @@ namespace mrg {
 namespace {
 
 constexpr int kPad = 72;                      // padded row of 64 bf16
-constexpr int kPadT4 = 24;                    // padded row of W4^T (16 bf16)
-constexpr int kHiddenRows = 4 * kNrcWidth;    // rows of W0..W3
-constexpr int kActs = 5;                      // stored activations per training sample
+constexpr int kPadT4 = 24;                    // padded row of the output layer's W^T (16 bf16)
+constexpr int kHiddenRows = kNrcHidden * kNrcWidth;   // rows of the hidden weight matrices
+constexpr int kActs = kNrcHidden + 1;         // stored activations per training sample: x0, a1 ..
 constexpr int kG16Row = kNrcLayers * kNrcWidth;  // bf16 per sample of the gradient rows
+static_assert(kActs == kNrcLayers, "activation and gradient rows share one tensor-map shape");
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 {
@@ -221,9 +222,9 @@ k_nrc_forward(NrcState S, const float4* __restrict__ inputs, const uint32_t* __r
             }
         }
         __syncwarp();
-        // ---- 4 hidden layers ----
+        // ---- hidden layers ----
 #pragma unroll 1
-        for(int layer = 0; layer < 4; layer++)
+        for(int layer = 0; layer < kNrcHidden; layer++)
         {
             const uint16_t* W = sW + layer * kNrcWidth * kPad;
             float acc[8][4];
@@ -308,7 +309,7 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
                const float4* __restrict__ targets, const uint32_t* nDevice, uint32_t nMax)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    // transposed weights: W0^T..W3^T [64 in][64 out] and W4^T [64 in][16 out]
+    // transposed weights: hidden W0^T..W4^T [64 in][64 out], output W5^T [64 in][16 out]
     uint16_t* sT = reinterpret_cast<uint16_t*>(smem);                        // 4 x 64 x kPad
     uint16_t* sT4 = sT + kHiddenRows * kPad;                                  // 64 x kPadT4
     float* sG = reinterpret_cast<float*>(sT4 + kNrcWidth * kPadT4);           // WARPS x 16 x 33
@@ -372,13 +373,13 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
         a[0][1] = pack_bf16(gy[0][2], gy[0][3]);
         a[0][2] = pack_bf16(gy[1][0], gy[1][1]);
         a[0][3] = pack_bf16(gy[1][2], gy[1][3]);
-        // bf16 dL/dy rows for dW4 = gy^T a4 (slot 4, columns 0..15)
+        // bf16 dL/dy rows for the output layer's dW = gy^T a5 (slot kNrcHidden, columns 0..15)
         uint32_t* G16 = reinterpret_cast<uint32_t*>(S.g16);
-        if(v0) { G16[((size_t)r0 * kG16Row + 4 * kNrcWidth + 2 * t) / 2] = a[0][0];
-                 G16[((size_t)r0 * kG16Row + 4 * kNrcWidth + 8 + 2 * t) / 2] = a[0][2]; }
-        if(v1) { G16[((size_t)r1 * kG16Row + 4 * kNrcWidth + 2 * t) / 2] = a[0][1];
-                 G16[((size_t)r1 * kG16Row + 4 * kNrcWidth + 8 + 2 * t) / 2] = a[0][3]; }
-        // ---- g_a4 = gy W4 (k = 16) ----
+        if(v0) { G16[((size_t)r0 * kG16Row + kNrcHidden * kNrcWidth + 2 * t) / 2] = a[0][0];
+                 G16[((size_t)r0 * kG16Row + kNrcHidden * kNrcWidth + 8 + 2 * t) / 2] = a[0][2]; }
+        if(v1) { G16[((size_t)r1 * kG16Row + kNrcHidden * kNrcWidth + 2 * t) / 2] = a[0][1];
+                 G16[((size_t)r1 * kG16Row + kNrcHidden * kNrcWidth + 8 + 2 * t) / 2] = a[0][3]; }
+        // ---- g_a5 = gy W5 (k = 16) ----
         float acc[8][4];
 #pragma unroll
         for(int nt = 0; nt < 8; nt++)
@@ -389,7 +390,7 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
         }
         const uint16_t* acts = S.acts;
 #pragma unroll 1
-        for(int layer = 3; layer >= 0; layer--)
+        for(int layer = kNrcHidden - 1; layer >= 0; layer--)
         {
             // mask with the ReLU of activation a_{layer+1} (stored at index layer + 1)
             const size_t aoff = (size_t)(layer + 1) * kNrcWidth;
@@ -490,7 +491,7 @@ k_nrc_backward(NrcState S, const float4* __restrict__ inputs, const float4* __re
 // ---------------------------------------------------------------------------
 // Weight gradients on the 5th-generation tensor cores:
 //   dW_l[o][i] = sum_b G_l[b][o] A_l[b][i]
-// for the five layers at once.  The batch is the reduction dimension: each CTA
+// for all six layers at once.  The batch is the reduction dimension: each CTA
 // takes chunks of 128 samples (blockIdx.x, + gridDim.x, ...), and for every
 // (chunk, layer) item a TMA pair brings the G_l and A_l tiles (128 rows x 64
 // bf16, 128-byte swizzled) into one of four shared-memory stages.  One thread
@@ -509,7 +510,8 @@ constexpr uint32_t kWgStages = 4;
 constexpr uint32_t kWgTileBytes = kWgRows * kNrcWidth * 2;   // 16 KB
 constexpr uint32_t kWgStageBytes = 2 * kWgTileBytes;
 constexpr size_t kWgSmem = (size_t)kWgStages * kWgStageBytes + 1024;   // + alignment to 1024 B
-constexpr uint32_t kWgTmemCols = 512;                    // 5 layers x 64 fp32 columns, power of two
+constexpr uint32_t kWgTmemCols = 512;                    // kNrcLayers x 64 fp32 columns, power of two
+static_assert(kNrcLayers * kNrcWidth <= (int)kWgTmemCols, "layer accumulators exceed the TMEM allocation");
 constexpr uint32_t kWgThreads = 128;
 constexpr long long kWgWaitCycles = 2000000000ll;        // ~1 s at 2 GHz
 // tcgen05 instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A bf16
@@ -696,7 +698,7 @@ k_nrc_wgrad_tc(const __grid_constant__ CUtensorMap tmG, const __grid_constant__ 
         const uint32_t row = 16u * warp + lane;          // lanes 0..15 of each quarter hold rows
         for(uint32_t layer = 0; layer < (uint32_t)kNrcLayers; layer++)
         {
-            const uint32_t rows = (layer == 4u) ? (uint32_t)kNrcOut : (uint32_t)kNrcWidth;
+            const uint32_t rows = (layer == (uint32_t)kNrcHidden) ? (uint32_t)kNrcOut : (uint32_t)kNrcWidth;
 #pragma unroll
             for(uint32_t c = 0; c < (uint32_t)kNrcWidth; c += 16u)
             {

@@ -90,15 +90,15 @@ mrg_status mrg_cache_create(mrg_ctx* c, const mrg_cache_params* p)
     if(e == cudaSuccess) e = alloc(c, S.mT, nt);
     if(e == cudaSuccess) e = alloc(c, S.vT, nt);
     if(e == cudaSuccess) e = alloc(c, S.gT, nt);
-    if(e == cudaSuccess) e = alloc(c, S.acts, (size_t)S.cap * 5 * mrg::kNrcWidth);
-    if(e == cudaSuccess) e = alloc(c, S.g16, (size_t)S.cap * 5 * mrg::kNrcWidth);
+    if(e == cudaSuccess) e = alloc(c, S.acts, (size_t)S.cap * mrg::kNrcLayers * mrg::kNrcWidth);
+    if(e == cudaSuccess) e = alloc(c, S.g16, (size_t)S.cap * mrg::kNrcLayers * mrg::kNrcWidth);
     if(e == cudaSuccess) e = alloc(c, S.y, (size_t)S.cap);
     if(e == cudaSuccess) e = alloc(c, S.loss, 1);
     S.partCtas = (uint32_t)std::max(1, c->smCount);
     if(e == cudaSuccess) e = alloc(c, S.wgPart, (size_t)S.partCtas * mrg::kNrcWeightCount);
-    // the gradient rows' unused columns (slot 4, 16..63) must read as zero
-    if(e == cudaSuccess) e = cudaMemset(S.g16, 0, sizeof(uint16_t) * (size_t)S.cap * 5 * mrg::kNrcWidth);
-    if(e == cudaSuccess) e = cudaMemset(S.acts, 0, sizeof(uint16_t) * (size_t)S.cap * 5 * mrg::kNrcWidth);
+    // the gradient rows' unused columns (output slot, 16..63) must read as zero
+    if(e == cudaSuccess) e = cudaMemset(S.g16, 0, sizeof(uint16_t) * (size_t)S.cap * mrg::kNrcLayers * mrg::kNrcWidth);
+    if(e == cudaSuccess) e = cudaMemset(S.acts, 0, sizeof(uint16_t) * (size_t)S.cap * mrg::kNrcLayers * mrg::kNrcWidth);
     if(e == cudaSuccess) e = mrg::nrc_make_tensor_maps(S);
     if(e != cudaSuccess) return nrc_cuda(e, "mrg_cache_create");
     S.err = c->dScratch + 1;
@@ -110,7 +110,8 @@ mrg_status mrg_cache_create(mrg_ctx* c, const mrg_cache_params* p)
     std::vector<float> w(nw);
     const float lim = std::sqrt(6.0f / (64.0f + 64.0f)), limOut = std::sqrt(6.0f / (64.0f + 16.0f));
     std::uniform_real_distribution<float> U(-1.0f, 1.0f);
-    for(size_t i = 0; i < nw; i++) w[i] = U(rng) * (i < 4u * 4096u ? lim : limOut);
+    const size_t hiddenWeights = (size_t)mrg::kNrcHidden * mrg::kNrcWidth * mrg::kNrcWidth;
+    for(size_t i = 0; i < nw; i++) w[i] = U(rng) * (i < hiddenWeights ? lim : limOut);
     std::vector<float> t(nt);
     for(size_t i = 0; i < nt; i++) t[i] = U(rng) * 1e-4f;
     e = cudaMemcpy(S.w32, w.data(), sizeof(float) * nw, cudaMemcpyHostToDevice);

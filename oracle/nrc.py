@@ -1,15 +1,17 @@
 """FP64 reference of the radiance cache (TEST INFRASTRUCTURE ONLY).
 
 Project-written (MRay has no learned cache): the multiresolution hash-grid
-encoding (Mueller et al. 2022), the 5-layer 64-wide ReLU MLP without biases,
-the relative L2 loss and its gradients, in float64 numpy.  ``bf16=True``
-rounds what the GPU holds in BF16 (inputs, weights, activations, the
-per-sample gradient rows) so that GPU results can be compared tightly; ``bf16=False`` is the plain FP64
-model.
+encoding (Mueller et al. 2022), the MLP of 5 hidden 64-wide ReLU layers and a
+16-wide output layer without biases, the relative L2 loss and its gradients,
+in float64 numpy.  ``bf16=True`` rounds what the GPU holds in BF16 (inputs,
+weights, activations, the per-sample gradient rows) so that GPU results can
+be compared tightly; ``bf16=False`` is the plain FP64 model.
 """
 import numpy as np
 
-WIDTH, OUT, LAYERS = 64, 16, 5
+WIDTH, OUT, HIDDEN = 64, 16, 5
+LAYERS = HIDDEN + 1                       # hidden layers + the output layer
+WEIGHTS = HIDDEN * WIDTH * WIDTH + OUT * WIDTH
 PRIMES = (1, 2654435761, 805459861)
 
 
@@ -23,8 +25,8 @@ def round_bf16(a):
 
 def split_weights(w):
     w = np.asarray(w, np.float64)
-    mats = [w[i * 4096:(i + 1) * 4096].reshape(64, 64) for i in range(4)]
-    mats.append(w[4 * 4096:4 * 4096 + 1024].reshape(16, 64))
+    mats = [w[i * 4096:(i + 1) * 4096].reshape(64, 64) for i in range(HIDDEN)]
+    mats.append(w[HIDDEN * 4096:HIDDEN * 4096 + 1024].reshape(16, 64))
     return mats
 
 
@@ -107,10 +109,10 @@ class CacheRef:
         W = [r(m) for m in split_weights(weights)]
         acts = [r(X)]
         a = acts[0]
-        for l in range(4):
+        for l in range(HIDDEN):
             a = r(np.maximum(a @ W[l].T, 0.0))
             acts.append(a)
-        y = a @ W[4].T
+        y = a @ W[HIDDEN].T
         return y, acts, W
 
     def query(self, inputs, weights, table, bf16=False):
@@ -133,10 +135,10 @@ class CacheRef:
         gy[:, :3] = 2.0 * (yy - t) / den / n
         # with bf16, the per-sample gradient rows enter both the weight
         # gradient and the next layer's data gradient rounded to bf16
-        gW = [None] * 5
-        gW[4] = r(gy).T @ acts[4]
-        g = r(gy) @ W[4]
-        for l in range(3, -1, -1):
+        gW = [None] * LAYERS
+        gW[HIDDEN] = r(gy).T @ acts[HIDDEN]
+        g = r(gy) @ W[HIDDEN]
+        for l in range(HIDDEN - 1, -1, -1):
             g = g * (acts[l + 1] > 0)
             gW[l] = r(g).T @ acts[l]
             g = r(g) @ W[l]

@@ -23,7 +23,7 @@ def _batch(n, seed):
 def test_reference_gradients_match_finite_differences():
     ref = nrc.CacheRef(levels=4, log2_table=8, base=4, max_res=32)
     rng = np.random.default_rng(0)
-    w = rng.uniform(-0.3, 0.3, nrc.WIDTH * nrc.WIDTH * 4 + nrc.OUT * nrc.WIDTH)
+    w = rng.uniform(-0.3, 0.3, nrc.WEIGHTS)
     tab = rng.uniform(-0.5, 0.5, 4 * 256 * 2)
     x, t = _batch(64, 1)
     loss, gw, gt = ref.gradients(x, t, w, tab)

@@ -33,7 +33,7 @@ def _cache(levels=16, log2=19):
 
 def _random_params(cache, seed):
     rng = np.random.default_rng(seed)
-    w = rng.uniform(-0.25, 0.25, nrc.WIDTH * nrc.WIDTH * 4 + nrc.OUT * nrc.WIDTH).astype(np.float32)
+    w = rng.uniform(-0.25, 0.25, nrc.WEIGHTS).astype(np.float32)
     # fp16-representable table values (the GPU reads the fp16 copy)
     t = rng.uniform(-0.6, 0.6, cache.table_size).astype(np.float16).astype(np.float32)
     cache.set_params(w, t)
