@@ -82,11 +82,21 @@ def test_adjoint_finite_differences_full_size():
     delta = torch.zeros((512, 512, 4), dtype=torch.float32, device="cuda")
     delta[..., :3] = (2.0 * (img - tgt) / npix).float()
     grad = pt.adjoint(p, tid, delta).cpu().numpy().astype(np.float64)
+    # the same gradient through torch.autograd (backward = the adjoint)
+    from mray_gb300.adjoint import render_albedo
+    dev.requires_grad_(True)
+    ag_loss = torch.sum((render_albedo(dev, pt, tid, p).double() - tgt) ** 2) / npix
+    ag_loss.backward()
+    assert np.array_equal(dev.grad.cpu().numpy(), grad.astype(np.float32)[..., :dev.shape[-1]]) or \
+        np.abs(dev.grad.cpu().numpy() - grad[..., :dev.shape[-1]]).max() <= 1e-6 * np.abs(grad).max()
+    dev.requires_grad_(False)
+    dev.grad = None
 
     def loss():
         return float(torch.sum((_img(pt.render(p)).double() - tgt) ** 2) / npix)
 
     # 64 seeded texels among those the adjoint says matter
+    dev = dev.detach()
     g3 = np.abs(grad[..., :3]).ravel()
     live = np.nonzero(g3 > np.quantile(g3[g3 > 0], 0.5))[0]
     picks = rng.choice(live, 64, replace=False)
