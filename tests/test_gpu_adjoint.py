@@ -2,7 +2,8 @@
 FP64 replay on a small case, and against central finite differences of the
 GPU's own renders on the differentiable-rendering workload (box + 65k-triangle
 displaced sphere with a 512^2 f32 albedo texture, L2 loss over a 512^2
-image, 32 spp, depth 6, finite-difference step 1e-3 on 64 seeded texels).
+image, 32 spp, depth 6, finite-difference step 1e-3 on 64 seeded texels,
+within 2%).
 Russian roulette is off (rr_start = max_depth): with it on, its
 throughput-dependent probability is treated as a constant by the adjoint."""
 import numpy as np
@@ -101,7 +102,7 @@ def test_adjoint_finite_differences_full_size():
     live = np.nonzero(g3 > np.quantile(g3[g3 > 0], 0.5))[0]
     picks = rng.choice(live, 64, replace=False)
     h = 1e-3
-    bad = []
+    bad, rel = [], []
     for flat in picks:
         y, x, k = np.unravel_index(flat, (512, 512, 3))
         v = float(tex[y, x, k])
@@ -112,8 +113,10 @@ def test_adjoint_finite_differences_full_size():
         dev[y, x, k] = v
         fd = (lp - lm) / (2 * h)
         g = grad[y, x, k]
-        if abs(fd - g) > 0.05 * abs(g) + 1e-9:
+        rel.append(abs(fd - g) / max(abs(g), 1e-30))
+        if abs(fd - g) > 0.02 * abs(g) + 1e-9:
             bad.append((int(y), int(x), int(k), fd, g))
-    print("finite differences: %d of 64 outside 5%%" % len(bad), bad[:4])
+    print("finite differences: %d of 64 outside 2%%; relative error median %.2g, max %.2g"
+          % (len(bad), float(np.median(rel)), float(np.max(rel))), bad[:4])
     assert len(bad) <= 3, bad[:8]
     pt.close()
