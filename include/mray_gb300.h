@@ -298,18 +298,26 @@ mrg_status mrg_pt_set_albedo_texture(mrg_ctx* ctx, uint32_t instance_id, uint32_
 
 /* ---- Path-replay adjoint (no reference counterpart) ---------------------- */
 /* Gradient of  sum_pixels <d_image_adjoint[p].rgb, I[p].rgb>  with respect to
- * the RGB texels of f32 texture texture_id (a Lambert albedo), I being the
- * image of params (RGB mode): I[p] = (sum of the pixel's spp sample
- * radiances) / spp.  Each pass runs twice with the same paths (counter-based
- * random numbers): the primal records every path's radiance, the replay adds
- * at every vertex on the texture  d * (radiance after the vertex) / albedo
- * into the four texels of its bilinear read (Vicini et al. 2021, "Path Replay
- * Backpropagation").  d_grad (RGBA f32 per texel, A unused) is ADDED to
- * (atomics).  Russian roulette probabilities are treated as constants.  When
- * d_image is not NULL the primal image is accumulated into it as
+ * the RGB texels of f32 texture texture_id (a Lambert albedo) and to the RGB
+ * radiance of every area light, I being the image of params (RGB mode):
+ * I[p] = (sum of the pixel's spp sample radiances) / spp.  Each pass runs
+ * twice with the same paths (counter-based random numbers): the primal records
+ * every path's radiance, the replay adds at every vertex on the texture
+ * d * (radiance after the vertex) / albedo  into the four texels of its
+ * bilinear read (Vicini et al. 2021, "Path Replay Backpropagation"), and, for
+ * every emission it gathers (a light hit, or a visible NEE sample), d * (the
+ * contribution / the light's radiance) into the light's instance.
+ * d_grad (RGBA f32 per texel, A unused) and d_grad_emission (RGBA f32 per
+ * instance, A unused; entries of instances that are not area lights stay
+ * untouched) are ADDED to (atomics).  texture_id = MRG_PT_NO_TEXTURE asks for
+ * the emission gradient alone (d_grad may then be NULL); d_grad_emission =
+ * NULL skips it.  Russian roulette probabilities are treated as constants.
+ * When d_image is not NULL the primal image is accumulated into it as
  * mrg_pt_render does.  Device buffers, stream-ordered. */
+#define MRG_PT_NO_TEXTURE 0xFFFFFFFFu
 mrg_status mrg_pt_adjoint(mrg_ctx* ctx, const mrg_pt_params* params, uint32_t texture_id,
-                          const float* d_image_adjoint, float* d_grad, float* d_image, void* stream);
+                          const float* d_image_adjoint, float* d_grad, float* d_grad_emission, float* d_image,
+                          void* stream);
 
 /* ---- Radiance cache (no reference counterpart) ----------------------------- */
 /* A multiresolution hash grid (levels x 2 features x 2^log2_table_size fp16

@@ -119,7 +119,7 @@ def _declare(lib):
         "mrg_upload_mesh_uv": (C.c_int, [vp, u32, vp, u32]),
         "mrg_pt_add_texture": (C.c_int, [vp, u32, u32, u32, vp, u32, C.POINTER(u32)]),
         "mrg_pt_set_albedo_texture": (C.c_int, [vp, u32, u32]),
-        "mrg_pt_adjoint": (C.c_int, [vp, C.POINTER(MrgPtParams), u32, vp, vp, vp, vp]),
+        "mrg_pt_adjoint": (C.c_int, [vp, C.POINTER(MrgPtParams), u32, vp, vp, vp, vp, vp]),
         "mrg_cache_create": (C.c_int, [vp, C.POINTER(MrgCacheParams)]),
         "mrg_cache_query": (C.c_int, [vp, vp, u32, vp, vp]),
         "mrg_cache_train": (C.c_int, [vp, vp, vp, u32, fp, vp]),

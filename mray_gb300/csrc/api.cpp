@@ -184,6 +184,7 @@ mrg_status mrg_destroy(mrg_ctx* c)
         if(q) cudaEventDestroy(q);
     cudaFree(c->ptPathMem2);
     cudaFree(c->dPtRadTotal2);
+    cudaFree(c->dPtGradEmission);
     cudaFree(c->dHostCounters);
     for(cudaEvent_t& q : c->hostEvents) if(q) cudaEventDestroy(q);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);

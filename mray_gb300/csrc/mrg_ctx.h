@@ -113,6 +113,8 @@ struct mrg_ctx
     cudaEvent_t  ptEvFilm = nullptr, ptEvStart = nullptr, ptEvDone2 = nullptr;
     void*        dPtRadTotal2 = nullptr;      // adjoint: primal radiance of the second pipeline
     uint32_t     ptRadTotalCap2 = 0;
+    double*      dPtGradEmission = nullptr;   // adjoint: FP64 emission-gradient sums, RGBA per instance
+    uint32_t     ptGradEmissionCap = 0;       // instances
     void*     ptPathMem = nullptr;
     // skysphere boundary light: host copy of the radiance map and transform,
     // device block [texels | cdfX | cdfY]

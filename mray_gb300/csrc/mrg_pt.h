@@ -40,7 +40,7 @@ struct __align__(16) PtTexture
 struct __align__(16) PtLight
 {
     float4 p0;          // w: area
-    float4 p1;
+    float4 p1;          // w: instance index (uint32 bits), for emission gradients
     float4 p2;
     float4 n;           // geometric normal, w: two-sided (0/1)
     float4 radiance;
@@ -83,9 +83,10 @@ struct PtAdjoint
     const float4* delta;        // dLoss / dPixel (RGB) per pixel
     float*        grad;         // RGBA per texel (A unused)
     const float4* radTotal;     // primal radiance per path slot
-    uint32_t      texIndex;     // texture id + 1
+    uint32_t      texIndex;     // texture id + 1 (0: no texture parameter)
     float         invSpp;       // 1 / samples per pixel of the image
     uint32_t      enabled;
+    double*       gradEmission; // RGBA per instance: dLoss / d(area-light radiance), FP64 sums, or null
 };
 
 // Radiance-cache use by the path tracer (mode 1): a path ends at its second
@@ -155,6 +156,7 @@ struct PtPaths
     uint32_t* listA;         // alive lists (ping-pong)
     uint32_t* listB;
     uint32_t* shadowList;
+    uint32_t* shadowLight;   // adjoint: area light of the slot's NEE sample (~0u: the skysphere)
     uint32_t* counts;        // [0] list A count, [1] list B count, [2] shadow count, [3] pad
     uint32_t* workKeys;      // work key per alive entry (partitioning)
     uint32_t* workKeysOut;
@@ -192,7 +194,10 @@ cudaError_t pt_cache_apply(const PtPaths& P, const PtCacheUse& C, int smCount, c
 // radiance before) / throughput, valid records compacted (at most batchCap).
 cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t slots, float4* batchIn,
                              float4* batchTarget, uint32_t* batchCount, int smCount, cudaStream_t st);
-cudaError_t pt_resolve(const PtLaunch& L, const PtPaths& P, uint32_t depth, int smCount, cudaStream_t st);
+cudaError_t pt_resolve(const PtLaunch& L, const PtPaths& P, const PtLight* lights, uint32_t depth, int smCount,
+                       cudaStream_t st);
+// out[i] += acc[i] (f32 from the FP64 emission-gradient sums), n entries.
+cudaError_t pt_add_emission_grad(const double* acc, float* out, uint32_t n, cudaStream_t st);
 cudaError_t pt_film(const PtLaunch& L, const PtPaths& P, float4* image, cudaStream_t st);
 
 } // namespace mrg

@@ -724,6 +724,39 @@ __device__ __forceinline__ float3 surface_albedo(const PtSceneTables& T, const P
     return tex_read(T.textures[sf.tex.x - 1u], uv.x, uv.y);
 }
 
+// Adds an emission-gradient contribution (RGB) to the light instance's FP64
+// sums: the active lanes of the warp that share the instance sum their values
+// first, and one lane of each group issues the atomics, so a light seen by
+// every path costs a few atomics per warp rather than one per lane.  Every
+// active lane runs the same number of shuffles (one per active lane).
+__device__ void add_emission_grad(double* acc, uint32_t inst, float gx, float gy, float gz)
+{
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, inst);
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for(unsigned m = act; m != 0u; m &= m - 1u)
+    {
+        const int src = __ffs(m) - 1;
+        const float vx = __shfl_sync(act, gx, src);
+        const float vy = __shfl_sync(act, gy, src);
+        const float vz = __shfl_sync(act, gz, src);
+        if((grp >> src) & 1u) { sx += (double)vx; sy += (double)vy; sz += (double)vz; }
+    }
+    if((int)(threadIdx.x & 31u) == __ffs(grp) - 1)
+    {
+        double* a = acc + 4 * (size_t)inst;
+        atomicAdd(a + 0, sx);
+        atomicAdd(a + 1, sy);
+        atomicAdd(a + 2, sz);
+    }
+}
+
+__global__ void k_add_emission_grad(const double* __restrict__ acc, float* __restrict__ out, uint32_t n)
+{
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = add(out[i], (float)acc[i]);
+}
+
 // Path-replay adjoint at a Lambert vertex whose albedo is the parameter
 // texture: every contribution after this vertex is linear in its albedo, so
 // d(path radiance)/d(albedo) = (primal radiance - radiance before the vertex)
@@ -850,6 +883,15 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                             const Chan lr = radiance_of<SPEC>(L.spec, lt.radiance.x, lt.radiance.y, lt.radiance.z, waves);
 #pragma unroll
                             for(int k = 0; k < NC; k++) rad.v[k] = add(rad.v[k], mul(lr.v[k], tp.v[k]));
+                            if(ADJ && L.adj.gradEmission)
+                            {
+                                // the emission enters linearly: d(contribution) / d(radiance) = tp
+                                const float4 d = L.adj.delta[slot_pixel(L, i)];
+                                const float sc = L.adj.invSpp;
+                                add_emission_grad(L.adj.gradEmission, __float_as_uint(lt.p1.w),
+                                                  mul(mul(d.x, sc), tp.v[0]), mul(mul(d.y, sc), tp.v[1]),
+                                                  mul(mul(d.z, sc), tp.v[2]));
+                            }
                         }
                     }
                 }
@@ -866,8 +908,8 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                     const float3 V = make_float3(dot3(wo, tng), dot3(wo, btg), dot3(wo, nrm));
                     const float3 a3 = surface_albedo(T, sf, gprim, mh);
                     const Chan alb = albedo_of<SPEC>(L.spec, a3.x, a3.y, a3.z, waves);
-                    if(ADJ && sf.tex.x == L.adj.texIndex && sf.info.w == kMatLambert && T.uvs != nullptr &&
-                       gprim < nTris)
+                    if(ADJ && L.adj.texIndex != 0u && sf.tex.x == L.adj.texIndex && sf.info.w == kMatLambert &&
+                       T.uvs != nullptr && gprim < nTris)
                         adjoint_vertex(L, T, sf, i, gprim, mh, a3, rad);
                     const bool isSpec = specularity<NC>(sf, alb) >= kSpecularThreshold;
                     const uint32_t mt = sf.info.w;
@@ -959,6 +1001,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         P.shadowRays[2 * (size_t)i + 1] = make_float4(sdir.x, sdir.y, sdir.z,
                                                                       mul(length, sub(1.0f, 1.0e-4f)));
                         P.shadowRad[i] = f4(srad);
+                        if(ADJ) P.shadowLight[i] = (li < L.nLights) ? li : 0xFFFFFFFFu;
                         shadow = true;
                     }
                     // ---- BxDF sample + Russian roulette (WorkFunction) ----
@@ -1211,8 +1254,13 @@ k_work_keys(PtPaths P, const PtSurface* __restrict__ surfaces, uint32_t nSurface
 
 // Adds the radiance of every shadow ray that reached its light
 // (KCAccumulateShadowRaysPT; the depth limit was applied when it was cast).
+// Resolve: visible NEE samples add their radiance.  In an adjoint replay with
+// emission gradients (ADJ) each also adds delta / spp * (its radiance / the
+// light's radiance), its derivative by the light's radiance, to the light's
+// instance.
+template<bool ADJ>
 __global__ void __launch_bounds__(kPtTPB)
-k_resolve(PtPaths P)
+k_resolve(PtPaths P, PtLaunch L, const PtLight* __restrict__ lights)
 {
     const uint32_t n = P.counts[2];
     for(uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
@@ -1224,6 +1272,20 @@ k_resolve(PtPaths P)
             float4 r = P.rad[i];
             r.x = add(r.x, s.x); r.y = add(r.y, s.y); r.z = add(r.z, s.z); r.w = add(r.w, s.w);
             P.rad[i] = r;
+            if(ADJ)
+            {
+                const uint32_t li = P.shadowLight[i];
+                if(li < L.nLights)
+                {
+                    const PtLight lt = lights[li];
+                    const float4 d = L.adj.delta[slot_pixel(L, i)];
+                    const float sc = L.adj.invSpp;
+                    add_emission_grad(L.adj.gradEmission, __float_as_uint(lt.p1.w),
+                        (lt.radiance.x > 0.0f) ? mul(mul(d.x, sc), __fdiv_rn(s.x, lt.radiance.x)) : 0.0f,
+                        (lt.radiance.y > 0.0f) ? mul(mul(d.y, sc), __fdiv_rn(s.y, lt.radiance.y)) : 0.0f,
+                        (lt.radiance.z > 0.0f) ? mul(mul(d.z, sc), __fdiv_rn(s.z, lt.radiance.z)) : 0.0f);
+                }
+            }
         }
     }
 }
@@ -1303,9 +1365,18 @@ cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t slo
     return cudaGetLastError();
 }
 
-cudaError_t pt_resolve(const PtLaunch&, const PtPaths& P, uint32_t, int smCount, cudaStream_t st)
+cudaError_t pt_add_emission_grad(const double* acc, float* out, uint32_t n, cudaStream_t st)
 {
-    k_resolve<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P);
+    if(n == 0) return cudaSuccess;
+    k_add_emission_grad<<<(n + 255u) / 256u, 256, 0, st>>>(acc, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_resolve(const PtLaunch& L, const PtPaths& P, const PtLight* lights, uint32_t, int smCount,
+                       cudaStream_t st)
+{
+    if(L.adj.enabled && L.adj.gradEmission) k_resolve<true><<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, L, lights);
+    else k_resolve<false><<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, L, lights);
     return cudaGetLastError();
 }
 

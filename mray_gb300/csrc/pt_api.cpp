@@ -73,7 +73,7 @@ void camera_frame(const mrg_pt_params& p, mrg::PtCamera& c)
 // Light triangle in world space: ApplyP with MRay's 4-term fma Dot
 // (TransformsDefault.hpp:19-23), Triangle::Normal / Area (ShapeFunctions.h:60-73).
 void make_light(const float m[12], const float v[9], const float radiance[3], uint32_t twoSided,
-                mrg::PtLight& out)
+                uint32_t instance, mrg::PtLight& out)
 {
     float w[3][3];
     for(int c = 0; c < 3; c++)
@@ -94,7 +94,9 @@ void make_light(const float m[12], const float v[9], const float radiance[3], ui
     const float area = len * 0.5f;
     const float inv = 1.0f / len;
     out.p0 = make_float4(w[0][0], w[0][1], w[0][2], area);
-    out.p1 = make_float4(w[1][0], w[1][1], w[1][2], 0.0f);
+    float instBits;
+    std::memcpy(&instBits, &instance, sizeof(instBits));
+    out.p1 = make_float4(w[1][0], w[1][1], w[1][2], instBits);
     out.p2 = make_float4(w[2][0], w[2][1], w[2][2], 0.0f);
     out.n = make_float4(cr[0] * inv, cr[1] * inv, cr[2] * inv, twoSided ? 1.0f : 0.0f);
     out.radiance = make_float4(radiance[0], radiance[1], radiance[2], 0.0f);
@@ -252,7 +254,7 @@ mrg_status pt_prepare(mrg_ctx* c)
                 for(int k = 0; k < 3; k++)
                     for(int q = 0; q < 3; q++) v[3 * k + q] = mesh.pos[3ull * mesh.idx[3ull * t + k] + q];
                 mrg::PtLight L;
-                make_light(in.m, v, d.radiance, d.twoSided, L);
+                make_light(in.m, v, d.radiance, d.twoSided, i, L);
                 lights.push_back(L);
             }
         }
@@ -338,10 +340,10 @@ mrg_status pt_paths_into(mrg::PtPaths& P, void*& mem, uint32_t slots)
     const size_t n = slots;
     const size_t words = (n + 31) / 32;
     // one allocation, every array 256-byte aligned
-    const size_t sizes[20] = { n * 32, n * 16, n * 8, n * 16, n * 16, n * 4, n * 32, n * 16,
+    const size_t sizes[21] = { n * 32, n * 16, n * 8, n * 16, n * 16, n * 4, n * 32, n * 16,
                                words * 4, n * 4, n * 4, n * 4, 64, n * 4, n * 4, n * 4,
                                4 * mrg::multisplit_hist_words(slots, mrg::kPtWorkKeyBits),
-                               n * 4, n * 16, n * 16 };
+                               n * 4, n * 16, n * 16, n * 4 };
     size_t need = 0;
     for(size_t sz : sizes) need += (sz + 255) & ~size_t(255);
     char* base = nullptr;
@@ -370,6 +372,7 @@ mrg_status pt_paths_into(mrg::PtPaths& P, void*& mem, uint32_t slots)
     P.prevPdf = reinterpret_cast<float*>(take());
     P.waves = reinterpret_cast<float4*>(take());
     P.wavePdf = reinterpret_cast<float4*>(take());
+    P.shadowLight = reinterpret_cast<uint32_t*>(take());
     P.capacity = slots;
     return MRG_OK;
 }
@@ -688,7 +691,7 @@ cudaError_t pt_bounces(mrg_ctx* c, PtRun& R, const PtLane& lane)
         if(e == cudaSuccess)
             e = mrg::launch_visibility(c->scene, shadowScr, P.visBits, P.shadowRays, P.shadowList, 0, c->smCount, side,
                                        P.counts + 2);
-        if(e == cudaSuccess) e = mrg::pt_resolve(L, P, depth, c->smCount, side);
+        if(e == cudaSuccess) e = mrg::pt_resolve(L, P, R.T.lights, depth, c->smCount, side);
         if(e == cudaSuccess && overlap) e = cudaEventRecord(lane.evResolved, side);
     }
     if(e == cudaSuccess && overlap) e = cudaStreamWaitEvent(st, lane.evResolved, 0);
@@ -839,14 +842,19 @@ mrg_status mrg_pt_render_cached(mrg_ctx* c, const mrg_pt_params* p, float* dImag
 }
 
 mrg_status mrg_pt_adjoint(mrg_ctx* c, const mrg_pt_params* p, uint32_t texId, const float* dImageAdjoint,
-                          float* dGrad, float* dImage, void* stream)
+                          float* dGrad, float* dGradEmission, float* dImage, void* stream)
 {
-    if(!c || !p || !dImageAdjoint || !dGrad) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: null pointer");
-    if(texId >= c->ptTextures.size() || c->ptTextures[texId].format != MRG_TEX_RGBA32F)
+    const bool texParam = texId != MRG_PT_NO_TEXTURE;
+    if(!c || !p || !dImageAdjoint || (texParam && !dGrad))
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: null pointer");
+    if(!texParam && !dGradEmission)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: no parameter (no texture and no emission gradient)");
+    if(texParam && (texId >= c->ptTextures.size() || c->ptTextures[texId].format != MRG_TEX_RGBA32F))
         return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: the parameter must be an f32 texture");
     if(c->ptSpec.enabled) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: RGB rendering only");
     for(uint32_t i = 0; i < c->insts.size() && i < c->ptDesc.size(); i++)
-        if(c->ptDesc[i].kind == 1 && c->ptDesc[i].texture == texId + 1 && c->ptDesc[i].material != MRG_MAT_LAMBERT)
+        if(texParam && c->ptDesc[i].kind == 1 && c->ptDesc[i].texture == texId + 1 &&
+           c->ptDesc[i].material != MRG_MAT_LAMBERT)
             return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: the parameter texture must feed Lambert albedos");
     DevGuard g(c->device);
     PtRun R;
@@ -864,7 +872,22 @@ mrg_status mrg_pt_adjoint(mrg_ctx* c, const mrg_pt_params* p, uint32_t texId, co
     mrg::PtAdjoint& A = R.L.adj;
     A.delta = reinterpret_cast<const float4*>(dImageAdjoint);
     A.grad = dGrad;
-    A.texIndex = texId + 1u;
+    A.texIndex = texParam ? texId + 1u : 0u;
+    A.gradEmission = nullptr;
+    const uint32_t nInst = (uint32_t)c->insts.size();
+    if(dGradEmission)
+    {
+        if(c->ptGradEmissionCap < nInst)
+        {
+            cudaFree(c->dPtGradEmission);
+            c->dPtGradEmission = nullptr;
+            c->ptGradEmissionCap = 0;
+            PT_TRY(cudaMalloc(&c->dPtGradEmission, sizeof(double) * 4 * (size_t)nInst), "mrg_pt_adjoint: emission sums");
+            c->ptGradEmissionCap = nInst;
+        }
+        PT_TRY(cudaMemsetAsync(c->dPtGradEmission, 0, sizeof(double) * 4 * (size_t)nInst, st), "emission sums");
+        A.gradEmission = c->dPtGradEmission;
+    }
     A.invSpp = 1.0f / (float)p->spp;
     // passes (primal + replay each) on two pipelines as in mrg_pt_render; the
     // gradient is a sum of atomic adds, so its value does not depend on it
@@ -904,7 +927,10 @@ mrg_status mrg_pt_adjoint(mrg_ctx* c, const mrg_pt_params* p, uint32_t texId, co
         A.enabled = 1u;
         PT_TRY(pt_bounces(c, R, lane), "replay pass");
     }
-    return two ? pt_join(c, st) : MRG_OK;
+    if(two && (s = pt_join(c, st)) != MRG_OK) return s;
+    if(dGradEmission)
+        PT_TRY(mrg::pt_add_emission_grad(c->dPtGradEmission, dGradEmission, 4 * nInst, st), "emission gradient");
+    return MRG_OK;
 }
 
 } // extern "C"

@@ -72,16 +72,26 @@ class PathTracer:
                                              C.byref(l) if loss else None, _stream_ptr(stream)))
         return image, (l.value if loss else None)
 
-    def adjoint(self, p, tex_id, image_adjoint, grad=None, image=None, stream=None):
+    def adjoint(self, p, tex_id, image_adjoint, grad=None, image=None, stream=None, grad_emission=None):
         """Path-replay adjoint (see mrg_pt_adjoint): image_adjoint is a
         (h, w, 4) float32 CUDA tensor of dLoss/dPixel; returns grad, a
-        (texH, texW, 4) float32 CUDA tensor the gradient is added to."""
+        (texH, texW, 4) float32 CUDA tensor the texture gradient is added to
+        (None when tex_id is None: emission only).  grad_emission, a
+        (n_instances, 4) float32 CUDA tensor, receives dLoss / d(radiance)
+        of every area-light instance when given."""
         import torch
-        t = self._tex_shape(tex_id)
-        if grad is None:
-            grad = torch.zeros((t[0], t[1], 4), dtype=torch.float32, device="cuda:%d" % self.acc.device)
-        N.check(N.lib().mrg_pt_adjoint(self.acc._h, C.byref(p), tex_id, C.c_void_p(image_adjoint.data_ptr()),
-                                       C.c_void_p(grad.data_ptr()),
+        dev = "cuda:%d" % self.acc.device
+        if grad_emission is not None and (tuple(grad_emission.shape) != (self.n_instances, 4) or
+                                          grad_emission.dtype != torch.float32 or
+                                          not grad_emission.is_cuda or not grad_emission.is_contiguous()):
+            raise ValueError("grad_emission must be a contiguous (n_instances, 4) float32 CUDA tensor")
+        if tex_id is not None and grad is None:
+            t = self._tex_shape(tex_id)
+            grad = torch.zeros((t[0], t[1], 4), dtype=torch.float32, device=dev)
+        N.check(N.lib().mrg_pt_adjoint(self.acc._h, C.byref(p), 0xFFFFFFFF if tex_id is None else tex_id,
+                                       C.c_void_p(image_adjoint.data_ptr()),
+                                       None if grad is None else C.c_void_p(grad.data_ptr()),
+                                       None if grad_emission is None else C.c_void_p(grad_emission.data_ptr()),
                                        None if image is None else C.c_void_p(image.data_ptr()),
                                        _stream_ptr(stream)))
         return grad

@@ -75,7 +75,7 @@ def lib():
         L.orc_env_dir_to_uv.argtypes = [vp, vp]
         L.orc_env_uv_to_dir.argtypes = [vp, vp]
         L.orc_tex_read.argtypes = [vp, u32, u32, u32, vp, vp]
-        L.orc_pt_adjoint.argtypes = [vp, vp, vp, vp, u32, vp, vp, u32, u32, vp, vp, C.c_int]
+        L.orc_pt_adjoint.argtypes = [vp, vp, vp, vp, u32, vp, vp, u32, u32, vp, vp, vp, u32, C.c_int]
         L.orc_pt_adjoint.restype = C.c_int
         L.orc_pt_render.restype = C.c_int
         L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
@@ -285,7 +285,7 @@ class PtSurface(C.Structure):
 class PtLightTri(C.Structure):
     _fields_ = [("p0", C.c_float * 3), ("p1", C.c_float * 3), ("p2", C.c_float * 3),
                 ("n", C.c_float * 3), ("area", C.c_float), ("radiance", C.c_float * 3),
-                ("twoSided", C.c_int)]
+                ("twoSided", C.c_int), ("instance", C.c_uint32)]
 
 
 class PtEnv(C.Structure):
@@ -474,6 +474,7 @@ class PtScene:
                 for t in range(tri.shape[0]):
                     lt = PtLightTri()
                     self.L.orc_pt_make_light(_vp(m), _vp(tri[t]), rad, 0, C.byref(lt))
+                    lt.instance = k
                     lights.append(lt)
             prim += idx.shape[0]
         self.S.build()
@@ -502,22 +503,29 @@ class PtScene:
             E.sceneDiameter = self.L.orc_scene_diameter(self.S._h)
             self.env = E
 
-    def adjoint(self, p, surface, delta, threads=None):
+    def adjoint(self, p, surface, delta, threads=None, emission=False):
         """FP64 path-replay gradient of sum(delta * image) with respect to the
         RGB texels of the albedo texture of surface index `surface` (every
-        surface sharing that texture array contributes)."""
-        sf = self.surf[surface]
-        if not sf.texels:
-            raise ValueError("surface has no texture")
+        surface sharing that texture array contributes; None: no texture).
+        With emission=True returns (texture gradient or None, (n_surfaces, 4)
+        gradient by each area light's radiance)."""
         d = np.ascontiguousarray(delta, np.float32)
-        grad = np.zeros((sf.texH, sf.texW, 4), np.float64)
+        grad, texels, tw, th = None, None, 0, 0
+        if surface is not None:
+            sf = self.surf[surface]
+            if not sf.texels:
+                raise ValueError("surface has no texture")
+            grad = np.zeros((sf.texH, sf.texW, 4), np.float64)
+            texels, tw, th = C.c_void_p(sf.texels), sf.texW, sf.texH
+        n = len(self.surf)
+        ge = np.zeros((n, 4), np.float64) if emission else None
         rc = self.L.orc_pt_adjoint(self.S._h, C.byref(p), self.surf, self.lights, self.n_lights,
                                    C.byref(self.env) if self.env is not None else None,
-                                   C.c_void_p(sf.texels), sf.texW, sf.texH, _vp(d), _vp(grad),
-                                   threads or default_threads())
+                                   texels, tw, th, _vp(d), None if grad is None else _vp(grad),
+                                   None if ge is None else _vp(ge), n, threads or default_threads())
         if rc != 0:
             raise RuntimeError("oracle adjoint failed")
-        return grad
+        return (grad, ge) if emission else grad
 
     def scene_aabb(self):
         out = np.zeros(6, np.float32)

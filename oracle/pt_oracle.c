@@ -662,6 +662,8 @@ typedef struct
     uint32_t                  adjW, adjH;
     const float*              adjDelta;
     double*                   adjGrad;      /* one buffer per worker */
+    double*                   adjGradE;     /* one buffer per worker, or NULL */
+    uint32_t                  adjInstances;
     int                       adjWorkers;
     atomic_int                adjNextBuffer;
     float*                    image;
@@ -713,7 +715,7 @@ static void surface_of(const orc_pt_surface* sf, const float* tri9 /* v0 v1 v2 l
 
 /* adj: NULL for a primal trace; else {primal radiance[3], delta / spp [3]}
  * and the worker's gradient buffer. */
-typedef struct { float tot[3]; float d[3]; double* grad; } adj_ctx;
+typedef struct { float tot[3]; float d[3]; double* grad; double* gradE; } adj_ctx;
 
 static void tex_taps(uint32_t w, uint32_t h, const float uv[2], size_t idx[4], float wt[4])
 {
@@ -838,7 +840,12 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             float lr[4] = { L->radiance[0], L->radiance[1], L->radiance[2], 0.0f };
             if(S) orc_spec_convert_radiance(S, L->radiance, waves, lr);
             if(emits && depth + 1u <= P->maxDepth)
+            {
                 for(int k = 0; k < nc; k++) rad[k] += lr[k] * tp[k];
+                /* the emission enters linearly: d(contribution) / d(radiance) = tp */
+                if(adj && adj->gradE)
+                    for(int k = 0; k < 3; k++) adj->gradE[4 * (size_t)L->instance + k] += (double)(adj->d[k] * tp[k]);
+            }
             break;
         }
 
@@ -862,7 +869,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             orc_tex_read(sf->texels, sf->texW, sf->texH, sf->texFormat, uv, alb);
         }
         if(S) { float c3[3] = { alb[0], alb[1], alb[2] }; orc_spec_convert_albedo(S, c3, waves, alb); }
-        if(adj && sf->texels == J->adjTexels && sf->matType == ORC_MAT_LAMBERT)
+        if(adj && J->adjTexels && sf->texels == J->adjTexels && sf->matType == ORC_MAT_LAMBERT)
         {
             const float* q = &sf->uvs[6 * localPrim];
             float a = mh.bary[0], b = mh.bary[1], c = 1.0f - a - b;
@@ -946,7 +953,16 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             orc_nudge(pos, nrm, sorg);
             if(depth + 2u <= P->maxDepth &&
                visible1(J->scene, sorg, sdir, 1.0e-5f, length * (1.0f - 1.0e-4f)))
+            {
                 for(int k = 0; k < nc; k++) rad[k] += srad[k];
+                if(adj && adj->gradE && li < J->nLights)
+                {
+                    const orc_pt_light_tri* L = &J->lights[li];
+                    for(int k = 0; k < 3; k++)
+                        if(L->radiance[k] > 0.0f)
+                            adj->gradE[4 * (size_t)L->instance + k] += (double)(adj->d[k] * (srad[k] / L->radiance[k]));
+                }
+            }
         }
 
         /* ---- BxDF sample (WorkFunction) ---- */
@@ -1108,6 +1124,7 @@ static void* pt_adj_worker(void* arg)
     const orc_pt_params* P = J->p;
     int b = atomic_fetch_add(&J->adjNextBuffer, 1);
     double* grad = J->adjGrad + (size_t)b * 4 * J->adjW * J->adjH;
+    double* gradE = J->adjGradE ? J->adjGradE + (size_t)b * 4 * J->adjInstances : NULL;
     const float invSpp = 1.0f / (float)P->spp;
     for(;;)
     {
@@ -1122,6 +1139,7 @@ static void* pt_adj_worker(void* arg)
                 trace_sample(J, x, y, P->sampleStart + s, A.tot);
                 for(int k = 0; k < 3; k++) A.d[k] = d[k] * invSpp;
                 A.grad = grad;
+                A.gradE = gradE;
                 float r[3];
                 trace_sample_adj(J, x, y, P->sampleStart + s, r, &A);
             }
@@ -1133,19 +1151,23 @@ static void* pt_adj_worker(void* arg)
 int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
                    const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
                    const void* texels, uint32_t texW, uint32_t texH, const float* delta,
-                   double* grad, int nthreads)
+                   double* grad, double* gradEmission, uint32_t nInstances, int nthreads)
 {
-    if(!s || !p || !surfaces || !texels || !delta || !grad) return -1;
+    if(!s || !p || !surfaces || !delta || (texels && !grad) || (!texels && !gradEmission)) return -1;
     if(nthreads < 1) nthreads = 1;
     if(nthreads > 64) nthreads = 64;
-    const size_t n = 4ull * texW * texH;
-    double* bufs = (double*)calloc((size_t)nthreads * n, sizeof(double));
+    if(!texels) texW = texH = 0;
+    const size_t n = 4ull * texW * texH, ne = gradEmission ? 4ull * nInstances : 0;
+    double* bufs = (double*)calloc((size_t)nthreads * (n + ne) + 1, sizeof(double));
     if(!bufs) return -2;
+    double* bufsE = bufs + (size_t)nthreads * n;
     pt_job J;
     memset(&J, 0, sizeof(J));
     J.scene = s; J.p = p; J.surfaces = surfaces; J.lights = lights; J.nLights = nLights;
     J.env = env;
     J.adjTexels = texels; J.adjW = texW; J.adjH = texH; J.adjDelta = delta; J.adjGrad = bufs;
+    J.adjGradE = gradEmission ? bufsE : NULL;
+    J.adjInstances = nInstances;
     J.adjWorkers = nthreads;
     atomic_init(&J.nextRow, 0u);
     atomic_init(&J.adjNextBuffer, 0);
@@ -1156,7 +1178,10 @@ int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surf
     pt_adj_worker(&J);
     for(int t = 0; t < started; t++) pthread_join(th[t], NULL);
     for(int t = 0; t <= started; t++)
+    {
         for(size_t i = 0; i < n; i++) grad[i] += bufs[(size_t)t * n + i];
+        for(size_t i = 0; i < ne; i++) gradEmission[i] += bufsE[(size_t)t * ne + i];
+    }
     free(bufs);
     return 0;
 }
@@ -1252,4 +1277,5 @@ void orc_pt_make_light(const float m[12], const float* v9, const float radiance[
     out->n[0] = c[0] * inv; out->n[1] = c[1] * inv; out->n[2] = c[2] * inv;
     memcpy(out->radiance, radiance, 12);
     out->twoSided = twoSided;
+    out->instance = 0u;
 }

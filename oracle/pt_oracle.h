@@ -70,6 +70,7 @@ typedef struct
     float    area;
     float    radiance[3];
     int      twoSided;
+    uint32_t instance;          /* the light's instance (emission gradients) */
 } orc_pt_light_tri;
 
 /* Skysphere boundary light with a spherical (lat-long) radiance map
@@ -124,11 +125,15 @@ int  orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surf
  * numbers; the replay adds, at each Lambert vertex whose albedo is the texture
  * `texels`, delta[pixel] / spp * (primal radiance - radiance before the
  * vertex) / albedo, times each bilinear tap's weight, into grad (double RGBA
- * per texel, accumulated in FP64).  RGB mode. */
+ * per texel, accumulated in FP64).  With gradEmission (double RGBA per
+ * instance, nInstances entries) it also adds, for every emission the path
+ * gathers from an area light (a hit, or a visible NEE sample), delta / spp *
+ * (the contribution / the light's radiance) into the light's instance.
+ * texels = NULL: no texture parameter.  RGB mode. */
 int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
                    const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
                    const void* texels, uint32_t texW, uint32_t texH, const float* delta,
-                   double* grad, int nthreads);
+                   double* grad, double* gradEmission, uint32_t nInstances, int nthreads);
 
 /* Piecewise-constant 2D distribution (Source/Tracer/Distributions.h/.cu). */
 void  orc_pwc2d_build(const float* func, uint32_t w, uint32_t h, float* cdfX, float* cdfY);

@@ -3,7 +3,7 @@ FP64 replay on a small case, and against central finite differences of the
 GPU's own renders on the differentiable-rendering workload (box + 65k-triangle
 displaced sphere with a 512^2 f32 albedo texture, L2 loss over a 512^2
 image, 32 spp, depth 6, finite-difference step 1e-3 on 64 seeded texels,
-within 2%).
+within 2%); the same for the area light's radiance (d(loss)/d(emission)).
 Russian roulette is off (rr_start = max_depth): with it on, its
 throughput-dependent probability is treated as a constant by the adjoint."""
 import numpy as np
@@ -119,4 +119,92 @@ def test_adjoint_finite_differences_full_size():
     print("finite differences: %d of 64 outside 2%%; relative error median %.2g, max %.2g"
           % (len(bad), float(np.median(rel)), float(np.max(rel))), bad[:4])
     assert len(bad) <= 3, bad[:8]
+    pt.close()
+
+
+def _light(n_theta, n_phi):
+    surf = scenes.adjoint_scene(None, n_theta=n_theta, n_phi=n_phi)
+    lights = [k for k, s in enumerate(surf) if s["kind"] == "light"]
+    assert len(lights) == 1
+    return len(surf), lights[0], np.array(surf[lights[0]]["radiance"], np.float64)
+
+
+def test_emission_gradient_matches_oracle_small():
+    """d(loss)/d(area-light radiance) beside the texture gradient, and alone
+    (no texture parameter), against the oracle's FP64 replay."""
+    tex = scenes.value_noise_texture(8, seed=0, dtype=np.float32)
+    dev = torch.from_numpy(tex.copy()).cuda()
+    pt, tid, sphere = _tracer(dev, 12, 24)
+    n, light, _ = _light(12, 24)
+    cam = scenes.box_camera()
+    p = PathTracer.params(16, 16, 4, cam, max_depth=4, rr_start=4, seed=5, samples_per_pass=1)
+    img = _img(pt.render(p))
+    tgt = 0.8 * torch.flip(img, dims=[0])
+    delta = torch.zeros((16, 16, 4), dtype=torch.float32, device="cuda")
+    delta[..., :3] = 2.0 * (img - tgt) / (16 * 16)
+    ge = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    g = pt.adjoint(p, tid, delta, grad_emission=ge).cpu().numpy().astype(np.float64)
+    ge_only = torch.zeros_like(ge)
+    assert pt.adjoint(p, None, delta, grad_emission=ge_only) is None
+    ge, ge_only = ge.cpu().numpy().astype(np.float64), ge_only.cpu().numpy().astype(np.float64)
+    S = oracle.PtScene(scenes.adjoint_scene(tex, n_theta=12, n_phi=24))
+    go, geo = S.adjoint(oracle.PtScene.params(16, 16, 4, cam, max_depth=4, rr_start=4, seed=5), sphere,
+                        delta.cpu().numpy(), emission=True)
+    assert np.abs(geo[light, :3]).min() > 0
+    assert not np.delete(ge, light, axis=0).any()
+    err = np.abs(ge[:, :3] - geo[:, :3]).max() / np.abs(geo[:, :3]).max()
+    print("emission gradient vs oracle: max |diff| / max |grad| = %.3g" % err, ge[light], geo[light])
+    assert err <= 1e-3
+    assert np.allclose(ge_only, ge, rtol=1e-5, atol=0)
+    terr = np.abs(g[..., :3] - go[..., :3]).max() / np.abs(go[..., :3]).max()
+    assert terr <= 1e-3
+    pt.close()
+
+
+def test_emission_gradient_full_size():
+    """On the differentiable-rendering workload (512^2, 32 spp, depth 6): the
+    image is linear in the light's radiance, so radiance * gradient equals
+    sum(delta * image) per channel, and central differences of the GPU's own
+    renders (radiance +- 1%) agree within 0.5%."""
+    tex = scenes.value_noise_texture(512, seed=0, dtype=np.float32)
+    dev = torch.from_numpy(tex.copy()).cuda()
+    pt, tid, _ = _tracer(dev, 128, 256)
+    n, light, rad = _light(128, 256)
+    cam = scenes.box_camera()
+    p = PathTracer.params(512, 512, 32, cam, max_depth=6, rr_start=6, seed=7)
+    img = _img(pt.render(p)).double()
+    tgt = 0.8 * torch.flip(img, dims=[0])
+    npix = 512 * 512
+    delta = torch.zeros((512, 512, 4), dtype=torch.float32, device="cuda")
+    delta[..., :3] = (2.0 * (img - tgt) / npix).float()
+    ge = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    assert pt.adjoint(p, None, delta, grad_emission=ge) is None
+    ge = ge.cpu().numpy().astype(np.float64)
+    lin = (delta[..., :3].double() * img).sum(dim=(0, 1)).cpu().numpy()
+    print("radiance * gradient", ge[light, :3] * rad, "sum(delta * image)", lin)
+    assert np.allclose(ge[light, :3] * rad, lin, rtol=1e-4, atol=0)
+    # the same gradients through torch.autograd (backward = the adjoint)
+    from mray_gb300.adjoint import render_scene
+    dev.requires_grad_(True)
+    em = torch.tensor(rad[None, :], dtype=torch.float64, requires_grad=True)
+    ag_loss = torch.sum((render_scene(dev, em, pt, tid, [light], p).double() - tgt) ** 2) / npix
+    ag_loss.backward()
+    assert np.allclose(em.grad.numpy()[0], ge[light, :3], rtol=1e-5, atol=0)
+    assert float(dev.grad.abs().max()) > 0
+    dev.requires_grad_(False)
+
+    def loss(r):
+        pt.set_area_light(light, r)
+        out = float(torch.sum((_img(pt.render(p)).double() - tgt) ** 2) / npix)
+        pt.set_area_light(light, rad)
+        return out
+
+    for k in range(3):
+        h = 1e-2 * rad[k]
+        rp, rm = rad.copy(), rad.copy()
+        rp[k] += h
+        rm[k] -= h
+        fd = (loss(rp) - loss(rm)) / (2 * h)
+        print("channel %d: finite difference %.6g, adjoint %.6g" % (k, fd, ge[light, k]))
+        assert abs(fd - ge[light, k]) <= 5e-3 * abs(ge[light, k])
     pt.close()
