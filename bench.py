@@ -359,8 +359,9 @@ def c2_scene_pt(args, dev):
 
 def c3_adjoint(args, dev):
     """Differentiable workload: box + 65,024-triangle textured sphere, 512^2
-    f32 albedo texture, 512^2 image, 32 spp, depth 6; one primal render plus
-    one path-replay adjoint (primal + replay) per step."""
+    f32 albedo texture, 512^2 image, 32 spp, depth 6; one path-replay adjoint
+    (primal + replay) per step giving d(loss)/d(texture) and d(loss)/d(area-light
+    emission)."""
     import torch
     from mray_gb300.pt import PathTracer
     from mray_gb300 import scenes
@@ -381,14 +382,15 @@ def c3_adjoint(args, dev):
     p = PathTracer.params(512, 512, 32, scenes.box_camera(), max_depth=6, rr_start=6, seed=0)
     delta = torch.full((512, 512, 4), 1e-6, dtype=torch.float32, device=dev)
     grad = torch.zeros((512, 512, 4), dtype=torch.float32, device=dev)
-    pt.adjoint(p, tid, delta, grad=grad)
+    grad_em = torch.zeros((pt.n_instances, 4), dtype=torch.float32, device=dev)
+    pt.adjoint(p, tid, delta, grad=grad, grad_emission=grad_em)
     torch.cuda.synchronize(dev)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     reps = 3
     e0.record()
     for _ in range(reps):
-        pt.adjoint(p, tid, delta, grad=grad)
+        pt.adjoint(p, tid, delta, grad=grad, grad_emission=grad_em)
     e1.record()
     torch.cuda.synchronize(dev)
     ms = e0.elapsed_time(e1) / reps

@@ -90,7 +90,7 @@ def build(force=False, verbose=False, ptxas_verbose=False, defines=None, lib_pat
         jobs.append((cmd, o))
     for f in cpp:
         o = os.path.join(obj, f + ".o")
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"] + dflags + [
                "-I", CSRC, "-I", INCLUDE, "-I", os.path.join(home, "include"),
                "-c", os.path.join(CSRC, f), "-o", o]
         jobs.append((cmd, o))

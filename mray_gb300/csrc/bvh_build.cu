@@ -577,7 +577,18 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
         float lo = __fsub_rd(nbox.mn[k], inflate);
         float hi = __fadd_ru(nbox.mx[k], inflate);
         float ext = __fsub_ru(hi, lo);
-        float x = __fdiv_ru(ext, 252.0f);
+#if MRG_NODE_F16
+        // fp16 frame: p = inflated min, 2^e the smallest power of two with
+        // ext * 2^-e <= 2^15 (every offset fits fp16 exactly scaled)
+        uint32_t bits = __float_as_uint(ext);
+        int ex = (int)((bits >> 23) & 0xFF);
+        int e = (ex == 0) ? -126 : ex - 127 + (((bits & 0x7FFFFFu) != 0u) ? 1 : 0) - 15;
+        e = max(-126, min(e, 126));
+        eb[k] = (uint32_t)(e + 127);
+        px[k] = lo;
+        invS[k] = __uint_as_float((uint32_t)(127 - e) << 23);
+#else
+        float x = __fdiv_ru(ext, MRG_NODE_EXACT_Q ? 255.0f : 252.0f);
         uint32_t bits = __float_as_uint(x);
         int ex = (int)((bits >> 23) & 0xFF);
         int e;
@@ -585,8 +596,9 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
         else e = ex - 127 + (((bits & 0x7FFFFFu) != 0u) ? 1 : 0);
         e = max(-126, min(e, 126));
         eb[k] = (uint32_t)(e + 127);
-        px[k] = __fsub_rd(lo, __uint_as_float((uint32_t)(e + 127) << 23));
+        px[k] = MRG_NODE_EXACT_Q ? lo : __fsub_rd(lo, __uint_as_float((uint32_t)(e + 127) << 23));
         invS[k] = __uint_as_float((uint32_t)(127 - e) << 23);
+#endif
     }
 
     // Slot assignment by direction: slot s holds the child whose centre lies
@@ -635,7 +647,12 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
         return;
     }
 
-    uint8_t meta[8], qlo[3][8], qhi[3][8];
+    uint8_t meta[8];
+#if MRG_NODE_F16
+    __half hlo[3][8], hhi[3][8];
+#else
+    uint8_t qlo[3][8], qhi[3][8];
+#endif
     uint32_t imask = 0;
     uint32_t rank = 0, triOff = 0;
     for(int s = 0; s < 8; s++)
@@ -644,17 +661,30 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
         if(c < 0)
         {
             meta[s] = 0;
+#if MRG_NODE_F16
+            for(int k = 0; k < 3; k++) { hlo[k][s] = __float2half(0.0f); hhi[k][s] = __float2half(0.0f); }
+#else
             for(int k = 0; k < 3; k++) { qlo[k][s] = 0; qhi[k][s] = 0; }
+#endif
             continue;
         }
         for(int k = 0; k < 3; k++)
         {
             float lo = __fsub_rd(cbox[c].mn[k], inflate);
             float hi = __fadd_ru(cbox[c].mx[k], inflate);
-            float ql = floorf(__fmul_rd(__fsub_rd(lo, px[k]), invS[k])) - 1.0f;
-            float qh = ceilf(__fmul_ru(__fsub_ru(hi, px[k]), invS[k])) + 1.0f;
+#if MRG_NODE_F16
+            // offsets rounded outward at every step (the scale is a power of two)
+            const float vl = fmaxf(__fmul_rd(__fsub_rd(lo, px[k]), invS[k]), 0.0f);
+            const float vh = __fmul_ru(__fsub_ru(hi, px[k]), invS[k]);
+            hlo[k][s] = __float2half_rd(vl);
+            hhi[k][s] = __float2half_ru(vh);
+#else
+            const float pad = MRG_NODE_EXACT_Q ? 0.0f : 1.0f;
+            float ql = floorf(__fmul_rd(__fsub_rd(lo, px[k]), invS[k])) - pad;
+            float qh = ceilf(__fmul_ru(__fsub_ru(hi, px[k]), invS[k])) + pad;
             qlo[k][s] = (uint8_t)fminf(fmaxf(ql, 0.0f), 255.0f);
             qhi[k][s] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
+#endif
         }
         bool leaf = (cand[c] & kLeafBit) || ccnt[c] <= maxLeaf;
         if(!leaf)
@@ -694,6 +724,18 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
     uint32_t m0 = meta[0] | (meta[1] << 8) | (meta[2] << 16) | ((uint32_t)meta[3] << 24);
     uint32_t m1 = meta[4] | (meta[5] << 8) | (meta[6] << 16) | ((uint32_t)meta[7] << 24);
     out.w1 = make_uint4(childBase, triBase, m0, m1);
+#if MRG_NODE_F16
+    auto pack2 = [](__half a, __half b) -> uint32_t {
+        return (uint32_t)__half_as_ushort(a) | ((uint32_t)__half_as_ushort(b) << 16);
+    };
+    for(int k = 0; k < 3; k++)
+    {
+        out.h[k] = make_uint4(pack2(hlo[k][0], hlo[k][1]), pack2(hlo[k][2], hlo[k][3]),
+                              pack2(hlo[k][4], hlo[k][5]), pack2(hlo[k][6], hlo[k][7]));
+        out.h[3 + k] = make_uint4(pack2(hhi[k][0], hhi[k][1]), pack2(hhi[k][2], hhi[k][3]),
+                                  pack2(hhi[k][4], hhi[k][5]), pack2(hhi[k][6], hhi[k][7]));
+    }
+#else
     uint32_t qw[12];
     for(int k = 0; k < 3; k++)
     {
@@ -705,6 +747,7 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
     out.q[0] = make_uint4(qw[0], qw[1], qw[2], qw[3]);
     out.q[1] = make_uint4(qw[4], qw[5], qw[6], qw[7]);
     out.q[2] = make_uint4(qw[8], qw[9], qw[10], qw[11]);
+#endif
     a.wnodes[wideIdx] = out;
 }
 

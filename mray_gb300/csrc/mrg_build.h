@@ -7,6 +7,17 @@
 
 namespace mrg {
 
+// Child-plane encoding of the 8-wide node: 0 = 8-bit quantised offsets
+// (80-byte nodes), 1 = fp16 offsets (128-byte nodes).
+#ifndef MRG_NODE_F16
+#define MRG_NODE_F16 0
+#endif
+// 8-bit planes decoded exactly (byte - 2^23 after the biased conversion, one
+// add on the FMA pipe per plane), so child boxes need no padding quantum.
+#ifndef MRG_NODE_EXACT_Q
+#define MRG_NODE_EXACT_Q 0
+#endif
+
 struct WideNode;
 struct TriRecord;
 struct InstRecord;

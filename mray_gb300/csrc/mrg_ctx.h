@@ -23,7 +23,7 @@ struct HostInstRecord
     float    wmax[4];
 };
 static_assert(sizeof(HostInstRecord) == 96, "instance record is 96 bytes");
-constexpr size_t kWideNodeBytes = 80;
+constexpr size_t kWideNodeBytes = MRG_NODE_F16 ? 128 : 80;
 constexpr size_t kTriRecordBytes = 48;
 
 } // namespace mrg

@@ -12,6 +12,9 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+#include "mrg_build.h"
 
 namespace mrg {
 
@@ -21,10 +24,17 @@ struct __align__(16) WideNode
     float4 w0;
     // w1: childBase, triBase, meta[0..3], meta[4..7]
     uint4  w1;
+#if MRG_NODE_F16
+    // h[a]: the 8 children's planes as fp16 offsets (plane - p) * 2^-e, a =
+    // 0, 1, 2: lower x, y, z; 3, 4, 5: upper x, y, z (lower rounded down,
+    // upper rounded up)
+    uint4  h[6];
+#else
     // q[0]: qlo_x[0..7] qlo_y[0..7]; q[1]: qlo_z qhi_x; q[2]: qhi_y qhi_z
     uint4  q[3];
+#endif
 };
-static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
+static_assert(sizeof(WideNode) == (MRG_NODE_F16 ? 128 : 80), "wide node size");
 
 struct __align__(16) TriRecord
 {

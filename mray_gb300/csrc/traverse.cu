@@ -97,10 +97,139 @@ __device__ __forceinline__ float min3f(float a, float b, float c)
 }
 
 // Byte k of w plus 2^23, as a float (exact): the quantised plane index,
-// biased.  The bias is folded into the per-axis offset of the node.
+// biased.  The bias is folded into the per-axis offset of the node, or (exact
+// decode) subtracted again, which leaves the byte's value exactly.
 __device__ __forceinline__ float qbias(uint32_t w, uint32_t k)
 {
+#if MRG_NODE_EXACT_Q
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k)), 8388608.0f);
+#else
     return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k));
+#endif
+}
+
+#ifndef MRG_TRACE_RECOMPUTE_WINV
+#define MRG_TRACE_RECOMPUTE_WINV 0  // 1: the world ray's 1/dir is recomputed at TLAS leaves, not kept
+#endif
+#if MRG_NODE_F16
+// Tests the ray against the 8 children of node `ni` (fp16 child planes).
+// Returns the hit mask: bits 24..31 = internal children keyed by
+// (slot ^ oct7) so that the highest key is the nearest corner, bits 0..23 =
+// payload slots of leaf children (relative to the node's payload base).  A
+// plane at p + h * 2^e is reached at t = h * (2^e / d) + (p - o) / d, one fma
+// per plane; the stored planes are rounded outward and every box carries the
+// builder's inflation, which covers the rounding of that evaluation.
+__device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ nodes, uint32_t ni,
+                                                   const LevelRay& r, float tmin, float tmax,
+                                                   uint32_t& childBase, uint32_t& triBase,
+                                                   uint32_t& imask)
+{
+    const uint4* np = reinterpret_cast<const uint4*>(nodes + ni);
+    const uint4 a = __ldg(np + 0);
+    const uint4 b = __ldg(np + 1);
+    // near planes: the upper ones on axes the ray runs down
+    const uint32_t nxo = (r.oct7 & 1u) ? 0u : 3u, nyo = (r.oct7 & 2u) ? 0u : 3u, nzo = (r.oct7 & 4u) ? 0u : 3u;
+    const uint2* pnX = reinterpret_cast<const uint2*>(np + 2 + nxo);
+    const uint2* pfX = reinterpret_cast<const uint2*>(np + 5 - nxo);
+    const uint2* pnY = reinterpret_cast<const uint2*>(np + 3 + nyo);
+    const uint2* pfY = reinterpret_cast<const uint2*>(np + 6 - nyo);
+    const uint2* pnZ = reinterpret_cast<const uint2*>(np + 4 + nzo);
+    const uint2* pfZ = reinterpret_cast<const uint2*>(np + 7 - nzo);
+    const uint32_t packed = a.w;
+    const float sx = __uint_as_float((packed & 0xFFu) << 23) * r.ix;
+    const float sy = __uint_as_float(((packed >> 8) & 0xFFu) << 23) * r.iy;
+    const float sz = __uint_as_float(((packed >> 16) & 0xFFu) << 23) * r.iz;
+    const float ax = (__uint_as_float(a.x) - r.ox) * r.ix;
+    const float ay = (__uint_as_float(a.y) - r.oy) * r.iy;
+    const float az = (__uint_as_float(a.z) - r.oz) * r.iz;
+    imask = packed >> 24;
+    childBase = b.x;
+    triBase = b.y;
+
+    uint32_t hm = 0;
+#pragma unroll
+    for(uint32_t h = 0; h < 2; h++)
+    {
+        // children 4h .. 4h + 3: 8 bytes of each plane vector
+        const uint2 nX = __ldg(pnX + h), fX = __ldg(pfX + h);
+        const uint2 nY = __ldg(pnY + h), fY = __ldg(pfY + h);
+        const uint2 nZ = __ldg(pnZ + h), fZ = __ldg(pfZ + h);
+        const uint32_t nx4[2] = { nX.x, nX.y }, fx4[2] = { fX.x, fX.y };
+        const uint32_t ny4[2] = { nY.x, nY.y }, fy4[2] = { fY.x, fY.y };
+        const uint32_t nz4[2] = { nZ.x, nZ.y }, fz4[2] = { fZ.x, fZ.y };
+        // meta byte: internal = 0b001_11sss (24 + slot), leaf = unary count << 5 | offset,
+        // empty = 0.  For internal children xor the slot bits with oct7.
+        const uint32_t meta4 = h ? b.w : b.z;
+        const uint32_t inner4 = ((meta4 & (meta4 << 1)) & 0x10101010u) >> 4;   // 1 per internal byte
+        const uint32_t bitIdx4 = (meta4 ^ (r.octRep & (inner4 * 0xFFu))) & 0x1F1F1F1Fu;
+        const uint32_t bits4 = (meta4 >> 5) & 0x07070707u;
+#pragma unroll
+        for(uint32_t w = 0; w < 2; w++)
+        {
+            const uint32_t wnx = nx4[w], wfx = fx4[w], wny = ny4[w], wfy = fy4[w], wnz = nz4[w], wfz = fz4[w];
+            const float2 tnx2 = __half22float2(*reinterpret_cast<const __half2*>(&wnx));
+            const float2 tfx2 = __half22float2(*reinterpret_cast<const __half2*>(&wfx));
+            const float2 tny2 = __half22float2(*reinterpret_cast<const __half2*>(&wny));
+            const float2 tfy2 = __half22float2(*reinterpret_cast<const __half2*>(&wfy));
+            const float2 tnz2 = __half22float2(*reinterpret_cast<const __half2*>(&wnz));
+            const float2 tfz2 = __half22float2(*reinterpret_cast<const __half2*>(&wfz));
+#pragma unroll
+            for(uint32_t c = 0; c < 2; c++)
+            {
+                const uint32_t k = 2 * w + c;
+                const float tnx = fmaf(c ? tnx2.y : tnx2.x, sx, ax);
+                const float tny = fmaf(c ? tny2.y : tny2.x, sy, ay);
+                const float tnz = fmaf(c ? tnz2.y : tnz2.x, sz, az);
+                const float tfx = fmaf(c ? tfx2.y : tfx2.x, sx, ax);
+                const float tfy = fmaf(c ? tfy2.y : tfy2.x, sy, ay);
+                const float tfz = fmaf(c ? tfz2.y : tfz2.x, sz, az);
+                const float tn = fmaxf(max3f(tnx, tny, tnz), tmin);
+                const float tf = fminf(min3f(tfx, tfy, tfz), tmax);
+                const uint32_t cb = (bits4 >> (8u * k)) & 0xFFu;
+                const uint32_t bi = (bitIdx4 >> (8u * k)) & 0xFFu;
+                hm |= (tn <= tf) ? (cb << bi) : 0u;
+            }
+        }
+    }
+    return hm;
+}
+#else
+#ifndef MRG_NODE_FFMA2
+#define MRG_NODE_FFMA2 0            // 1: plane distances of two children per packed fp32x2 fma
+#endif
+
+// Two planes at once: (q0, q1) * s + a, both lanes of one fp32x2 fma (and,
+// with exact decode, the 2^23 bias removed by one fp32x2 subtract first).
+__device__ __forceinline__ float2 plane2(uint32_t w, uint32_t k0, uint32_t k1, float s, float a)
+{
+    const float b0 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k0));
+    const float b1 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k1));
+    float r0, r1;
+#if MRG_NODE_EXACT_Q
+    asm("{\n\t.reg .b64 q, b, s, a, t, d;\n\t"
+        "mov.b64 q, {%2, %3};\n\tmov.b64 b, {%4, %4};\n\tmov.b64 s, {%5, %5};\n\tmov.b64 a, {%6, %6};\n\t"
+        "sub.rn.f32x2 t, q, b;\n\tfma.rn.f32x2 d, t, s, a;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r0), "=f"(r1) : "f"(b0), "f"(b1), "f"(8388608.0f), "f"(s), "f"(a));
+#else
+    asm("{\n\t.reg .b64 q, s, a, d;\n\t"
+        "mov.b64 q, {%2, %3};\n\tmov.b64 s, {%4, %4};\n\tmov.b64 a, {%5, %5};\n\t"
+        "fma.rn.f32x2 d, q, s, a;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r0), "=f"(r1) : "f"(b0), "f"(b1), "f"(s), "f"(a));
+#endif
+    return make_float2(r0, r1);
+}
+
+// The x and y planes of child k: (qx, qy) * (sx, sy) + (ax, ay), one fp32x2 fma.
+__device__ __forceinline__ float2 planes_xy(uint32_t wx, uint32_t wy, uint32_t k, float sx, float sy,
+                                            float ax, float ay)
+{
+    const float bx = qbias(wx, k), by = qbias(wy, k);
+    float r0, r1;
+    asm("{\n\t.reg .b64 q, s, a, d;\n\t"
+        "mov.b64 q, {%2, %3};\n\tmov.b64 s, {%4, %5};\n\tmov.b64 a, {%6, %7};\n\t"
+        "fma.rn.f32x2 d, q, s, a;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r0), "=f"(r1) : "f"(bx), "f"(by), "f"(sx), "f"(sy), "f"(ax), "f"(ay));
+    return make_float2(r0, r1);
 }
 
 // Tests the ray against the 8 children of node `ni`.  Returns the hit mask:
@@ -124,9 +253,15 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
     const float sx = __uint_as_float((packed & 0xFFu) << 23) * r.ix;
     const float sy = __uint_as_float(((packed >> 8) & 0xFFu) << 23) * r.iy;
     const float sz = __uint_as_float(((packed >> 16) & 0xFFu) << 23) * r.iz;
+#if MRG_NODE_EXACT_Q
+    const float ax = (__uint_as_float(a.x) - r.ox) * r.ix;
+    const float ay = (__uint_as_float(a.y) - r.oy) * r.iy;
+    const float az = (__uint_as_float(a.z) - r.oz) * r.iz;
+#else
     const float ax = fmaf(-8388608.0f, sx, (__uint_as_float(a.x) - r.ox) * r.ix);
     const float ay = fmaf(-8388608.0f, sy, (__uint_as_float(a.y) - r.oy) * r.iy);
     const float az = fmaf(-8388608.0f, sz, (__uint_as_float(a.z) - r.oz) * r.iz);
+#endif
     imask = packed >> 24;
     childBase = b.x;
     triBase = b.y;
@@ -151,6 +286,39 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
         const uint32_t inner4 = ((meta4 & (meta4 << 1)) & 0x10101010u) >> 4;   // 1 per internal byte
         const uint32_t bitIdx4 = (meta4 ^ (r.octRep & (inner4 * 0xFFu))) & 0x1F1F1F1Fu;
         const uint32_t bits4 = (meta4 >> 5) & 0x07070707u;
+#if MRG_NODE_FFMA2 == 2
+#pragma unroll
+        for(uint32_t k = 0; k < 4; k++)
+        {
+            // x and y planes of one child per fp32x2 fma, z alone
+            const float2 nxy = planes_xy(nearX, nearY, k, sx, sy, ax, ay);
+            const float2 fxy = planes_xy(farX, farY, k, sx, sy, ax, ay);
+            const float tnz = fmaf(qbias(nearZ, k), sz, az);
+            const float tfz = fmaf(qbias(farZ, k), sz, az);
+            const float tn = fmaxf(max3f(nxy.x, nxy.y, tnz), tmin);
+            const float tf = fminf(min3f(fxy.x, fxy.y, tfz), tmax);
+            const uint32_t cb = (bits4 >> (8u * k)) & 0xFFu;
+            const uint32_t bi = (bitIdx4 >> (8u * k)) & 0xFFu;
+            hm |= (tn <= tf) ? (cb << bi) : 0u;
+        }
+#elif MRG_NODE_FFMA2
+#pragma unroll
+        for(uint32_t k = 0; k < 4; k += 2)
+        {
+            const float2 nx2 = plane2(nearX, k, k + 1, sx, ax), fx2 = plane2(farX, k, k + 1, sx, ax);
+            const float2 ny2 = plane2(nearY, k, k + 1, sy, ay), fy2 = plane2(farY, k, k + 1, sy, ay);
+            const float2 nz2 = plane2(nearZ, k, k + 1, sz, az), fz2 = plane2(farZ, k, k + 1, sz, az);
+#pragma unroll
+            for(uint32_t c = 0; c < 2; c++)
+            {
+                const float tn = fmaxf(max3f(c ? nx2.y : nx2.x, c ? ny2.y : ny2.x, c ? nz2.y : nz2.x), tmin);
+                const float tf = fminf(min3f(c ? fx2.y : fx2.x, c ? fy2.y : fy2.x, c ? fz2.y : fz2.x), tmax);
+                const uint32_t cb = (bits4 >> (8u * (k + c))) & 0xFFu;
+                const uint32_t bi = (bitIdx4 >> (8u * (k + c))) & 0xFFu;
+                hm |= (tn <= tf) ? (cb << bi) : 0u;
+            }
+        }
+#else
 #pragma unroll
         for(uint32_t k = 0; k < 4; k++)
         {
@@ -166,9 +334,12 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
             const uint32_t bi = (bitIdx4 >> (8u * k)) & 0xFFu;
             hm |= (tn <= tf) ? (cb << bi) : 0u;
         }
+#endif
     }
     return hm;
 }
+
+#endif
 
 // LOCAL: listed ray i starts inside instance instIds[i] (its BLAS, in the
 // instance's space) and ends when that BLAS is exhausted: CastLocalRays.
@@ -209,7 +380,9 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
     bool live = false;
     uint32_t ri = 0;
     float wox = 0, woy = 0, woz = 0, wdx = 0, wdy = 0, wdz = 0, tmin = 0, tmax = 0;
+#if !MRG_TRACE_RECOMPUTE_WINV
     float wix = 0, wiy = 0, wiz = 0;   // IEEE 1/dir of the world ray (exact leaf slab test)
+#endif
     LevelRay lr;
     float3 ld = make_float3(0, 0, 0);   // local direction (the local origin is lr.ox/oy/oz)
     uint2 ng = make_uint2(0, 0), tg = make_uint2(0, 0);
@@ -245,7 +418,9 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     const float4 r1 = rays[2 * (size_t)ri + 1];
                     wox = r0.x; woy = r0.y; woz = r0.z; tmin = r0.w;
                     wdx = r1.x; wdy = r1.y; wdz = r1.z; tmax = r1.w;
+#if !MRG_TRACE_RECOMPUTE_WINV
                     wix = __frcp_rn(wdx); wiy = __frcp_rn(wdy); wiz = __frcp_rn(wdz);
+#endif
                     setup_level(lr, wox, woy, woz, wdx, wdy, wdz);
                     ng = make_uint2(sc.tlasRoot, (1u << (24u + lr.oct7)) | 1u);
                     tg = make_uint2(0u, 0u);
@@ -375,6 +550,10 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                 // the stack, to be re-tested against the shrunken tMax.
                 if(tg.y != 0u)
                 {
+#if MRG_TRACE_RECOMPUTE_WINV
+                    // IEEE 1/dir of the world ray, recomputed here to keep registers free
+                    const float wix = __frcp_rn(wdx), wiy = __frcp_rn(wdy), wiz = __frcp_rn(wdz);
+#endif
                     uint32_t keep = 0u, best = 32u;
                     float bestT = 0.0f;
                     for(uint32_t cand = tg.y; cand != 0u; cand &= cand - 1u)

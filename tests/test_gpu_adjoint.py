@@ -208,3 +208,37 @@ def test_emission_gradient_full_size():
         print("channel %d: finite difference %.6g, adjoint %.6g" % (k, fd, ge[light, k]))
         assert abs(fd - ge[light, k]) <= 5e-3 * abs(ge[light, k])
     pt.close()
+
+
+def test_emission_gradient_many_lights_with_sky():
+    """The production scene (eight quad lights, a skysphere, Lambert / GGX /
+    glass surfaces, RGBA8 textures) at 64x36, RGB, 2 spp, depth 5: every
+    light's gradient against the oracle's; skysphere NEE samples add none."""
+    from mray_gb300.pt import load_box_scene
+    surf, cam = scenes.c2_scene(0, texture_size=64)
+    env = dict(texels=scenes.sky_map(64, 32, seed=0))
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    pt.set_env(env["texels"])
+    p = PathTracer.params(64, 36, 2, cam, max_depth=5, rr_start=5, seed=3, samples_per_pass=1)
+    img = _img(pt.render(p))
+    delta = torch.zeros((36, 64, 4), dtype=torch.float32, device="cuda")
+    delta[..., :3] = 2.0 * (img - 0.8 * torch.flip(img, dims=[0])) / (64 * 36)
+    ge = torch.zeros((pt.n_instances, 4), dtype=torch.float32, device="cuda")
+    assert pt.adjoint(p, None, delta, grad_emission=ge) is None
+    ge = ge.cpu().numpy().astype(np.float64)
+    S = oracle.PtScene(surf, env=env)
+    _, geo = S.adjoint(oracle.PtScene.params(64, 36, 2, cam, max_depth=5, rr_start=5, seed=3), None,
+                       delta.cpu().numpy(), emission=True)
+    lights = [k for k, s in enumerate(surf) if s["kind"] == "light"]
+    assert len(lights) == 8
+    assert not np.delete(geo, lights, axis=0).any() and not np.delete(ge, lights, axis=0).any()
+    assert np.count_nonzero(np.abs(geo[lights, :3]).max(axis=1)) >= 6
+    err = np.abs(ge[:, :3] - geo[:, :3]).max() / np.abs(geo[:, :3]).max()
+    print("8 lights: emission gradient vs oracle, max |diff| / max |grad| = %.3g" % err)
+    assert err <= 1e-3
+    # per light, against that light's own scale (gradients span four decades)
+    for k in lights:
+        scale = np.abs(geo[k, :3]).max()
+        assert np.abs(ge[k, :3] - geo[k, :3]).max() <= 1e-3 * scale + 1e-6 * np.abs(geo).max(), (k, ge[k], geo[k])
+    pt.close()
