@@ -751,6 +751,34 @@ __device__ void add_emission_grad(double* acc, uint32_t inst, float gx, float gy
     }
 }
 
+// A thread's run of emission-gradient terms for one light instance: terms of
+// the same instance are summed in registers and reach the FP64 sums (through
+// the warp-aggregated add) only when the instance changes and once at the
+// end of the thread's work, so a scene with few lights costs few atomics.
+constexpr uint32_t kNoEmission = 0xFFFFFFFFu;
+struct EmisRun
+{
+    uint32_t inst;
+    float    x, y, z;
+};
+
+__device__ __forceinline__ void emis_flush(EmisRun& r, double* acc)
+{
+    if(r.inst != kNoEmission) add_emission_grad(acc, r.inst, r.x, r.y, r.z);
+    r.inst = kNoEmission;
+}
+
+__device__ __forceinline__ void emis_push(EmisRun& r, double* acc, uint32_t inst, float gx, float gy, float gz)
+{
+    if(inst != r.inst)
+    {
+        emis_flush(r, acc);
+        r.inst = inst;
+        r.x = 0.0f; r.y = 0.0f; r.z = 0.0f;
+    }
+    r.x = add(r.x, gx); r.y = add(r.y, gy); r.z = add(r.z, gz);
+}
+
 __global__ void k_add_emission_grad(const double* __restrict__ acc, float* __restrict__ out, uint32_t n)
 {
     for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -809,6 +837,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t nAll = L.nLights + (L.env.enabled ? 1u : 0u);
     const float invN = nAll ? __fdiv_rn(1.0f, (float)nAll) : 0.0f;
+    EmisRun emis{ kNoEmission, 0.0f, 0.0f, 0.0f };
     // warp-uniform trip count so every lane reaches the ballots
     const uint32_t first = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
     for(uint32_t base = first; base < n; base += stride)
@@ -888,9 +917,9 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                                 // the emission enters linearly: d(contribution) / d(radiance) = tp
                                 const float4 d = L.adj.delta[slot_pixel(L, i)];
                                 const float sc = L.adj.invSpp;
-                                add_emission_grad(L.adj.gradEmission, __float_as_uint(lt.p1.w),
-                                                  mul(mul(d.x, sc), tp.v[0]), mul(mul(d.y, sc), tp.v[1]),
-                                                  mul(mul(d.z, sc), tp.v[2]));
+                                emis_push(emis, L.adj.gradEmission, __float_as_uint(lt.p1.w),
+                                          mul(mul(d.x, sc), tp.v[0]), mul(mul(d.y, sc), tp.v[1]),
+                                          mul(mul(d.z, sc), tp.v[2]));
                             }
                         }
                     }
@@ -1172,6 +1201,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
         warp_append(shadow, i, P.shadowList, P.counts + 2);
         if(CM == 1) warp_append(query, i, L.cache.queryList, L.cache.queryCount);
     }
+    if(ADJ && L.adj.gradEmission) emis_flush(emis, L.adj.gradEmission);
 }
 
 __global__ void __launch_bounds__(kPtTPB)
@@ -1263,6 +1293,7 @@ __global__ void __launch_bounds__(kPtTPB)
 k_resolve(PtPaths P, PtLaunch L, const PtLight* __restrict__ lights)
 {
     const uint32_t n = P.counts[2];
+    EmisRun emis{ kNoEmission, 0.0f, 0.0f, 0.0f };
     for(uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
     {
         const uint32_t i = P.shadowList[k];
@@ -1280,7 +1311,7 @@ k_resolve(PtPaths P, PtLaunch L, const PtLight* __restrict__ lights)
                     const PtLight lt = lights[li];
                     const float4 d = L.adj.delta[slot_pixel(L, i)];
                     const float sc = L.adj.invSpp;
-                    add_emission_grad(L.adj.gradEmission, __float_as_uint(lt.p1.w),
+                    emis_push(emis, L.adj.gradEmission, __float_as_uint(lt.p1.w),
                         (lt.radiance.x > 0.0f) ? mul(mul(d.x, sc), __fdiv_rn(s.x, lt.radiance.x)) : 0.0f,
                         (lt.radiance.y > 0.0f) ? mul(mul(d.y, sc), __fdiv_rn(s.y, lt.radiance.y)) : 0.0f,
                         (lt.radiance.z > 0.0f) ? mul(mul(d.z, sc), __fdiv_rn(s.z, lt.radiance.z)) : 0.0f);
@@ -1288,6 +1319,7 @@ k_resolve(PtPaths P, PtLaunch L, const PtLight* __restrict__ lights)
             }
         }
     }
+    if(ADJ) emis_flush(emis, L.adj.gradEmission);
 }
 
 // Film: every pixel sums its samples of the pass (slots p, p + WH, ...);
