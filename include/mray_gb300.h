@@ -319,6 +319,23 @@ mrg_status mrg_pt_adjoint(mrg_ctx* ctx, const mrg_pt_params* params, uint32_t te
                           const float* d_image_adjoint, float* d_grad, float* d_grad_emission, float* d_image,
                           void* stream);
 
+/* ---- ZSobol random numbers ---------------------------------------------------
+ * MRay's RNGGroupZSobol (Source/Tracer/Random.h:454-523, Random.cu:1147-1380):
+ * mrg_zsobol_seeds replaces its constructor's per-pixel seeds (the i-th output
+ * of std::mt19937 seeded with (seed >> 32) ^ (seed & 0xFFFFFFFF), pixels in
+ * row-major order, Random.cu:1149-1230) for a width x height image.
+ * mrg_zsobol_generate replaces GenerateNumbers (KCGenRandomNumbersGeneric,
+ * Random.cu:536-556) for one sample index of every pixel: `requests` is an
+ * RNRequestList (request r = bits 2r..2r+1, 1..3 numbers, request_count of
+ * them); request r reads dimension dim_start + (numbers before it) through
+ * ZSobol::Next / Next2D / Next3D, and number k of pixel i lands at
+ * d_out[i + width * height * k].  initial_max_spp is the group's
+ * initialMaxSampleCount.  Device buffers, stream-ordered. */
+mrg_status mrg_zsobol_seeds(uint32_t width, uint32_t height, uint64_t seed, uint32_t* h_seeds);
+mrg_status mrg_zsobol_generate(uint32_t width, uint32_t height, const uint32_t* d_seeds, uint32_t initial_max_spp,
+                               uint32_t sample_index, uint32_t dim_start, uint64_t requests,
+                               uint32_t request_count, uint32_t* d_out, void* stream);
+
 /* ---- Radiance cache (no reference counterpart) ----------------------------- */
 /* A multiresolution hash grid (levels x 2 features x 2^log2_table_size fp16
  * entries per level, resolutions base..max geometrically) feeding a fully

@@ -32,6 +32,7 @@ EXPORTED = [
     "mrg_pt_set_lambert", "mrg_pt_set_area_light", "mrg_pt_camera_frame", "mrg_pt_render",
     "mrg_pt_set_material", "mrg_pt_set_env", "mrg_multi_partition", "mrg_pt_set_spectral",
     "mrg_upload_mesh_uv", "mrg_pt_add_texture", "mrg_pt_set_albedo_texture", "mrg_pt_adjoint",
+    "mrg_zsobol_seeds", "mrg_zsobol_generate",
     "mrg_cache_create", "mrg_cache_query", "mrg_cache_train", "mrg_cache_get_params", "mrg_cache_set_params",
     "mrg_cache_gradients", "mrg_pt_render_cached",
 ]
@@ -120,6 +121,8 @@ def _declare(lib):
         "mrg_pt_add_texture": (C.c_int, [vp, u32, u32, u32, vp, u32, C.POINTER(u32)]),
         "mrg_pt_set_albedo_texture": (C.c_int, [vp, u32, u32]),
         "mrg_pt_adjoint": (C.c_int, [vp, C.POINTER(MrgPtParams), u32, vp, vp, vp, vp, vp]),
+        "mrg_zsobol_seeds": (C.c_int, [u32, u32, C.c_uint64, vp]),
+        "mrg_zsobol_generate": (C.c_int, [u32, u32, vp, u32, u32, u32, C.c_uint64, u32, vp, vp]),
         "mrg_cache_create": (C.c_int, [vp, C.POINTER(MrgCacheParams)]),
         "mrg_cache_query": (C.c_int, [vp, vp, u32, vp, vp]),
         "mrg_cache_train": (C.c_int, [vp, vp, vp, u32, fp, vp]),

@@ -77,6 +77,13 @@ def lib():
         L.orc_tex_read.argtypes = [vp, u32, u32, u32, vp, vp]
         L.orc_pt_adjoint.argtypes = [vp, vp, vp, vp, u32, vp, vp, u32, u32, vp, vp, vp, u32, C.c_int]
         L.orc_pt_adjoint.restype = C.c_int
+        L.orc_zs_tables.argtypes = [vp, vp]
+        L.orc_mt19937.argtypes = [u32, u32, vp]
+        L.orc_zs_res_max_bits.argtypes = [u32, u32]
+        L.orc_zs_res_max_bits.restype = u32
+        L.orc_zs_seeds.argtypes = [u32, u32, C.c_uint64, vp]
+        L.orc_zs_generate.argtypes = [u32, u32, vp, u32, u32, u32, C.c_uint64, u32, vp]
+        L.orc_zs_generate.restype = C.c_int
         L.orc_pt_render.restype = C.c_int
         L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
         L.orc_pt_make_light.argtypes = [vp, vp, vp, C.c_int, vp]
@@ -583,3 +590,40 @@ def multi_partition(keys, indices=None, key_data_bits=(0, 0), key_batch_bits=(0,
     starts = np.concatenate([[0], np.nonzero(b[1:] != b[:-1])[0] + 1]).astype(np.uint32)
     offsets = np.concatenate([starts, [n]]).astype(np.uint32)
     return (len(starts), offsets, sk[starts].astype(np.uint32), si.astype(np.uint32), sk.astype(np.uint32))
+
+
+# ---- ZSobol random-number group (zsobol_oracle.c) ----------------------------
+def zsobol_tables():
+    """(3 x 52 uint32 Sobol matrices, 24 x 4 uint8 digit permutations)."""
+    m = np.zeros((3, 52), np.uint32)
+    p = np.zeros((24, 4), np.uint8)
+    lib().orc_zs_tables(_vp(m), _vp(p))
+    return m, p
+
+
+def mt19937(seed, count):
+    out = np.zeros(count, np.uint32)
+    lib().orc_mt19937(seed, count, _vp(out))
+    return out
+
+
+def zsobol_seeds(width, height, seed):
+    out = np.zeros(width * height, np.uint32)
+    lib().orc_zs_seeds(width, height, seed, _vp(out))
+    return out
+
+
+def zsobol_generate(width, height, seeds, initial_max_spp, sample_index, dim_start, requests):
+    """requests: list of request sizes (1..3).  Returns (numbers, width*height)
+    uint32 in MRay's strided order (number k of pixel i at [k, i])."""
+    enc = 0
+    for r, d in enumerate(requests):
+        enc |= int(d) << (2 * r)
+    total = int(sum(requests))
+    out = np.zeros((total, width * height), np.uint32)
+    sd = np.ascontiguousarray(seeds, np.uint32)
+    rc = lib().orc_zs_generate(width, height, _vp(sd), initial_max_spp, sample_index, dim_start, enc,
+                               len(requests), _vp(out))
+    if rc != 0:
+        raise ValueError("zsobol_generate: bad arguments")
+    return out

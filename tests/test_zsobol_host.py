@@ -1,0 +1,79 @@
+"""ZSobol oracle (oracle/zsobol_oracle.c), CPU: the MT19937 restatement
+against the C++ standard's known answer, the generated Sobol matrices and
+digit permutations against MRay's own tables (read from its source when the
+source tree is present), the product's seeds against the oracle's, and
+properties of the generator's outputs."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+
+REF_RANDOM = "/root/reference/Source/Tracer/Random.cu"
+
+
+def test_mt19937_known_answer():
+    # [rand.predef]: the 10000th consecutive output of a default-seeded
+    # std::mt19937 (seed 5489) is 4123659995
+    assert int(oracle.mt19937(5489, 10000)[-1]) == 4123659995
+
+
+@pytest.mark.skipif(not os.path.exists(REF_RANDOM), reason="MRay source tree not present")
+def test_tables_match_reference_source():
+    m, p = oracle.zsobol_tables()
+    src = open(REF_RANDOM).read()
+    for d in range(3):
+        blk = re.search(r"SOBOL_32_JOE_KUO_DIM_%d\s*=\s*\{(.*?)\};" % d, src, re.S).group(1)
+        ref = np.array([int(x, 16) for x in re.findall(r"0x([0-9A-Fa-f]+)u", blk)], np.uint32)
+        assert np.array_equal(ref, m[d]), d
+    blk = re.search(r"TABLE\s*=\s*\{(.*?)\};", src, re.S).group(1)
+    rows = re.findall(r"COMPOSE_48x2\((.*?)\),?\s*(?://|\})", blk + "}", re.S)
+    table = np.array([[int(v) for v in re.findall(r"(\d+)ull", r)] for r in rows])
+    assert table.shape == (4, 24)
+    assert np.array_equal(table.T, p)
+
+
+def test_seeds_are_the_mt19937_stream():
+    s = oracle.zsobol_seeds(7, 5, (3 << 32) | 11)
+    assert np.array_equal(s, oracle.mt19937(3 ^ 11, 35))
+
+
+def test_product_seeds_match_oracle():
+    from mray_gb300 import zsobol
+    try:
+        got = zsobol.seeds(33, 17, 0x123456789)
+    except OSError:
+        pytest.skip("library not built")
+    assert np.array_equal(got, oracle.zsobol_seeds(33, 17, 0x123456789))
+
+
+@pytest.mark.parametrize("spp", [4, 8])
+def test_samples_of_a_pixel_are_distinct(spp):
+    """For a fixed dimension the samples of one pixel read distinct Sobol
+    indices of the pixel's block, and the scramble is a bijection, so their
+    numbers are distinct."""
+    w, h = 16, 12
+    seeds = oracle.zsobol_seeds(w, h, 7)
+    for dim in (0, 5):
+        vals = np.stack([oracle.zsobol_generate(w, h, seeds, spp, s, dim, [2])
+                         for s in range(spp)])            # (spp, 2, pixels)
+        for k in range(2):
+            for px in range(0, w * h, 37):
+                assert len(set(vals[:, k, px].tolist())) == spp
+
+
+def test_request_layout():
+    """Request r reads dimension dim_start + (numbers before it); a 2D request
+    equals the first two numbers of a 3D request only in its first number's
+    Sobol dimension, so check the layout through 1D requests: request list
+    [1, 1] at dim_start d gives Next(d), Next(d + 1)."""
+    w, h = 8, 8
+    seeds = oracle.zsobol_seeds(w, h, 1)
+    a = oracle.zsobol_generate(w, h, seeds, 16, 3, 4, [1, 1])
+    b0 = oracle.zsobol_generate(w, h, seeds, 16, 3, 4, [1])
+    b1 = oracle.zsobol_generate(w, h, seeds, 16, 3, 5, [1])
+    assert np.array_equal(a[0], b0[0]) and np.array_equal(a[1], b1[0])
+    c = oracle.zsobol_generate(w, h, seeds, 16, 3, 4, [2, 3, 1])
+    assert c.shape == (6, 64)
