@@ -10,8 +10,9 @@ import numpy as np
 import pytest
 
 import oracle
+from oracle.build import reference_source_dir
 
-REF_RANDOM = "/root/reference/Source/Tracer/Random.cu"
+REF_RANDOM = os.path.join(reference_source_dir(), "Tracer", "Random.cu")
 
 
 def test_mt19937_known_answer():
