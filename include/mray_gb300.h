@@ -233,7 +233,13 @@ typedef struct mrg_pt_params
                                     RayPartitioner does: 1 always, 0 never
                                     (shade in hit order), 2 when the scene has
                                     more than one material group or a skysphere */
+    uint32_t sampler;            /* MRG_PT_SAMPLER_*: the paths' random numbers */
+    uint32_t samplerMaxSpp;      /* ZSobol initialMaxSampleCount (0: sampleStart + spp) */
 } mrg_pt_params;
+/* Samplers: counter-based independent numbers (the default), or MRay's ZSobol
+ * group (see mrg_zsobol_generate) with seeds from params.seed. */
+#define MRG_PT_SAMPLER_INDEPENDENT 0u
+#define MRG_PT_SAMPLER_ZSOBOL      1u
 
 /* Surface description of an instance, the equivalent of attaching a
  * material / light group to a surface (TracerI::CreateSurface, CreateLightSurface).

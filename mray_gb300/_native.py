@@ -56,7 +56,7 @@ class MrgPtParams(C.Structure):
                 ("sampleMode", C.c_uint32), ("seed", C.c_uint32), ("filterRadius", C.c_float),
                 ("camPos", C.c_float * 3), ("camGaze", C.c_float * 3), ("camUp", C.c_float * 3),
                 ("fov", C.c_float * 2), ("nearFar", C.c_float * 2), ("sampleStart", C.c_uint32),
-                ("partitionByMaterial", C.c_uint32)]
+                ("partitionByMaterial", C.c_uint32), ("sampler", C.c_uint32), ("samplerMaxSpp", C.c_uint32)]
 
 #: capacity of mrg_cast_closest_host_noalloc (rays per call)
 MRG_NOALLOC_MAX_RAYS = 262144

@@ -185,6 +185,8 @@ mrg_status mrg_destroy(mrg_ctx* c)
     cudaFree(c->ptPathMem2);
     cudaFree(c->dPtRadTotal2);
     cudaFree(c->dPtGradEmission);
+    cudaFree(c->dZsTables);
+    cudaFree(c->dZsSeeds);
     cudaFree(c->dHostCounters);
     for(cudaEvent_t& q : c->hostEvents) if(q) cudaEventDestroy(q);
     if(c->buildStream) cudaStreamDestroy(c->buildStream);

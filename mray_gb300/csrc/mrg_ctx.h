@@ -114,6 +114,9 @@ struct mrg_ctx
     void*        dPtRadTotal2 = nullptr;      // adjoint: primal radiance of the second pipeline
     uint32_t     ptRadTotalCap2 = 0;
     double*      dPtGradEmission = nullptr;   // adjoint: FP64 emission-gradient sums, RGBA per instance
+    uint32_t*    dZsTables = nullptr;         // ZSobol sampler: matrices and digit permutations
+    uint32_t*    dZsSeeds = nullptr;          // ZSobol sampler: per-pixel seeds of (zsW, zsH, zsSeed)
+    uint32_t     zsW = 0, zsH = 0, zsSeed = 0;
     uint32_t     ptGradEmissionCap = 0;       // instances
     void*     ptPathMem = nullptr;
     // skysphere boundary light: host copy of the radiance map and transform,

@@ -20,6 +20,7 @@
 // multiply-add), so both render the same paths up to the library's sin / cos
 // / log, which differ between CUDA and the host C library by a few ulps.
 #include "mrg_pt.h"
+#include "zsobol.cuh"
 #include "mrg_device.cuh"
 
 namespace mrg {
@@ -574,6 +575,38 @@ __device__ __forceinline__ uint32_t slot_sample(const PtLaunch& L, uint32_t i)
     return L.sampleBase + i / (L.width * L.height);
 }
 
+// Random number k of bounce b of slot i's path: the counter-based hash, or
+// MRay's ZSobol group (sampler 1) under this dimension plan: the film-filter
+// offset (k 6, 7) = Next2D(0), the wavelengths (k 9) = Next(2); bounce b from
+// dimension 3 + 7b: k 0..2 (lobe choice and direction) = Next3D(+0), light
+// choice (k 3) = Next(+3), light point (k 4, 5) = Next2D(+4), Russian
+// roulette (k 8) = Next(+6).
+// Kept out of line so the default sampler's kernels keep their registers.
+__device__ __noinline__ float rnd_zsobol(const PtLaunch& L, uint32_t i, uint32_t bounce, uint32_t k)
+{
+    uint32_t dim, size, comp;
+    if(k == 6u || k == 7u) { dim = 0u; size = 2u; comp = k - 6u; }
+    else if(k == 9u) { dim = 2u; size = 1u; comp = 0u; }
+    else
+    {
+        const uint32_t b = 3u + 7u * bounce;
+        if(k <= 2u) { dim = b; size = 3u; comp = k; }
+        else if(k == 3u) { dim = b + 3u; size = 1u; comp = 0u; }
+        else if(k <= 5u) { dim = b + 4u; size = 2u; comp = k - 4u; }
+        else { dim = b + 6u; size = 1u; comp = 0u; }
+    }
+    const uint32_t pixel = slot_pixel(L, i);
+    const ZsGen g = zs_make(pixel % L.width, pixel / L.width, __ldg(L.zsSeeds + pixel), slot_sample(L, i),
+                            L.zsMaxSpp, L.zsResBits);
+    const uint64_t* perm = reinterpret_cast<const uint64_t*>(L.zsTables + 3 * kZsWidth);
+    return zs_to_float01(zs_number(g, L.zsTables, perm, dim, size, comp));
+}
+
+__device__ __forceinline__ float rnd_s(const PtLaunch& L, uint32_t key, uint32_t i, uint32_t bounce, uint32_t k)
+{
+    return (L.sampler == 0u) ? rnd(key, bounce, k) : rnd_zsobol(L, i, bounce, k);
+}
+
 // ---------------------------------------------------------------------------
 // Camera rays: pinhole (CamerasDefault.hpp:94-140), Gaussian film filter
 // sampled with Box-Muller (filter / pdf = 1 per sample, Filters.h:195-233);
@@ -589,7 +622,7 @@ k_raygen(PtLaunch L, PtPaths P, uint32_t* aliveList, uint32_t* aliveCount)
         const uint32_t pixel = slot_pixel(L, i);
         const uint32_t x = pixel % L.width, y = pixel / L.width;
         const uint32_t key = path_key(L.seed, pixel, slot_sample(L, i));
-        const float u1 = rnd(key, 0, 6), u2 = rnd(key, 0, 7);
+        const float u1 = rnd_s(L, key, i, 0, 6), u2 = rnd_s(L, key, i, 0, 7);
         const float r = mul(L.filterSigma, __fsqrt_rn(mul(-2.0f, logf(sub(1.0f, u1)))));
         const float ang = mul(mul(2.0f, kPi), u2);
         const float ox = mul(r, cosf(ang)), oy = mul(r, sinf(ang));
@@ -612,7 +645,7 @@ k_raygen(PtLaunch L, PtPaths P, uint32_t* aliveList, uint32_t* aliveCount)
         if(SPEC)
         {
             float4 w, p;
-            sample_waves(rnd(key, 0, 9), w, p);
+            sample_waves(rnd_s(L, key, i, 0, 9), w, p);
             P.waves[i] = w;
             P.wavePdf[i] = p;
         }
@@ -963,7 +996,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                     // ---- NEE (WorkFunctionNEE); specular materials cast none ----
                     if(L.sampleMode != 0u && nAll > 0u && !isSpec && depth + 2u <= L.maxDepth)
                     {
-                        const float dXi = rnd(key, depth, 3);
+                        const float dXi = rnd_s(L, key, i, depth, 3);
                         uint32_t li = (uint32_t)mul(dXi, (float)nAll);
                         li = min(li, nAll - 1u);
                         float3 lp;
@@ -973,7 +1006,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         {
                             // skysphere: a point sceneDiameter away along the sampled direction
                             float spdf;
-                            const float3 wd = env_sample(L.env, rnd(key, depth, 4), rnd(key, depth, 5), spdf);
+                            const float3 wd = env_sample(L.env, rnd_s(L, key, i, depth, 4), rnd_s(L, key, i, depth, 5), spdf);
                             lp = make_float3(add(pos.x, mul(wd.x, L.env.sceneDiameter)),
                                              add(pos.y, mul(wd.y, L.env.sceneDiameter)),
                                              add(pos.z, mul(wd.z, L.env.sceneDiameter)));
@@ -985,7 +1018,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         else
                         {
                             const PtLight lt = lights[li];
-                            const float r1 = __fsqrt_rn(rnd(key, depth, 4)), r2 = rnd(key, depth, 5);
+                            const float r1 = __fsqrt_rn(rnd_s(L, key, i, depth, 4)), r2 = rnd_s(L, key, i, depth, 5);
                             const float a = sub(1.0f, r1), b = mul(sub(1.0f, r2), r1), c = mul(r1, r2);
                             lp = make_float3(add(add(mul(lt.p0.x, a), mul(lt.p1.x, b)), mul(lt.p2.x, c)),
                                              add(add(mul(lt.p0.y, a), mul(lt.p1.y, b)), mul(lt.p2.y, c)),
@@ -1050,7 +1083,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         float fromEta = sf.mat.z, toEta = sf.mat.w;
                         if(backSide) { const float t = fromEta; fromEta = toEta; toEta = t; }
                         const float f = fresnel_dielectric(fabsf(V.z), fromEta, toEta);
-                        const bool doRefl = rnd(key, depth, 0) < f;
+                        const bool doRefl = rnd_s(L, key, i, depth, 0) < f;
                         if(doRefl) Ll = make_float3(-V.x, -V.y, sub(mul(2.0f, V.z), V.z));
                         else
                         {
@@ -1072,7 +1105,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         const float rough = sf.albedo.w;
                         const float alpha = mul(rough, rough);
                         const float ratio = unreal_ratio(sf, avg_albedo<NC>(alb));
-                        const float sXi = rnd(key, depth, 0), x0 = rnd(key, depth, 1), x1 = rnd(key, depth, 2);
+                        const float sXi = rnd_s(L, key, i, depth, 0), x0 = rnd_s(L, key, i, depth, 1), x1 = rnd_s(L, key, i, depth, 2);
                         float3 H;
                         float pd, ps;
                         if(sXi < ratio)
@@ -1122,7 +1155,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                     }
                     else
                     {
-                        const float xi0 = rnd(key, depth, 0), xi1 = rnd(key, depth, 1);
+                        const float xi0 = rnd_s(L, key, i, depth, 0), xi1 = rnd_s(L, key, i, depth, 1);
                         const float ang = mul(mul(2.0f, kPi), xi1), sr = __fsqrt_rn(xi0);
                         Ll.x = mul(sr, cosf(ang)); Ll.y = mul(sr, sinf(ang));
                         Ll.z = __fsqrt_rn(fmaxf(0.0f, sub(1.0f, add(mul(Ll.x, Ll.x), mul(Ll.y, Ll.y)))));
@@ -1145,7 +1178,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         float pr = add(add(thr.v[0], thr.v[1]), thr.v[2]);
                         pr = (NC == 4) ? mul(add(pr, thr.v[3]), 0.25f) : mul(pr, 0.33333333f);
                         pr = fminf(fmaxf(pr, 0.1f), 1.0f);
-                        const float xr = rnd(key, depth - 1u, 8);
+                        const float xr = rnd_s(L, key, i, depth - 1u, 8);
                         if(xr >= pr) dead = true;
                         else
                         {

@@ -2,6 +2,7 @@
 // "Path tracer" section): surface / light description, camera frame, and the
 // host-side enqueue of device-driven render passes.
 #include "mrg_ctx.h"
+#include "zsobol.cuh"
 #include "host_math.h"
 
 #include <cuda_runtime.h>
@@ -196,6 +197,43 @@ mrg_status env_prepare(mrg_ctx* c)
     const float sz = c->sceneBoxExact[5] - c->sceneBoxExact[2];
     E.sceneDiameter = std::sqrt(std::fma(sz, sz, sx * sx));
     E.enabled = 1u;
+    return MRG_OK;
+}
+
+// ZSobol state of a render: the tables (once per context) and the per-pixel
+// seeds of (width, height, seed), kept while those stay the same.
+mrg_status pt_zsobol(mrg_ctx* c, const mrg_pt_params& p, mrg::PtLaunch& L, const std::string& w)
+{
+    if(!c->dZsTables)
+    {
+        uint32_t t[mrg::kZsTableWords];
+        mrg::zsobol_tables(t);
+        PT_TRY(cudaMalloc(&c->dZsTables, sizeof(t)), "ZSobol tables");
+        PT_TRY(cudaMemcpy(c->dZsTables, t, sizeof(t), cudaMemcpyHostToDevice), "ZSobol tables");
+    }
+    if(!c->dZsSeeds || c->zsW != p.width || c->zsH != p.height || c->zsSeed != p.seed)
+    {
+        std::vector<uint32_t> seeds((size_t)p.width * p.height);
+        mrg_status s = mrg_zsobol_seeds(p.width, p.height, p.seed, seeds.data());
+        if(s != MRG_OK) return s;
+        cudaFree(c->dZsSeeds);
+        c->dZsSeeds = nullptr;
+        PT_TRY(cudaMalloc(&c->dZsSeeds, sizeof(uint32_t) * seeds.size()), "ZSobol seeds");
+        PT_TRY(cudaMemcpy(c->dZsSeeds, seeds.data(), sizeof(uint32_t) * seeds.size(), cudaMemcpyHostToDevice),
+               "ZSobol seeds");
+        c->zsW = p.width; c->zsH = p.height; c->zsSeed = p.seed;
+    }
+    const uint64_t maxSpp = p.samplerMaxSpp ? p.samplerMaxSpp : (uint64_t)p.sampleStart + p.spp;
+    if(maxSpp == 0 || maxSpp > 0x80000000ull) return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": ZSobol sample count");
+    const uint32_t m = std::max(p.width, p.height);
+    uint32_t pow2 = 1;
+    while(pow2 < m) pow2 <<= 1;
+    uint32_t bits = 0;
+    while((1u << bits) < pow2) bits++;
+    L.zsMaxSpp = (uint32_t)maxSpp;
+    L.zsResBits = bits;
+    L.zsSeeds = c->dZsSeeds;
+    L.zsTables = c->dZsTables;
     return MRG_OK;
 }
 
@@ -590,6 +628,9 @@ mrg_status pt_setup(mrg_ctx* c, const mrg_pt_params* p, PtRun& R, const char* wh
     L.env = c->ptEnv;
     L.spec = c->ptSpec;
     L.filterSigma = p->filterRadius * 0.285714f;
+    if(p->sampler > MRG_PT_SAMPLER_ZSOBOL) return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": unknown sampler");
+    L.sampler = p->sampler;
+    if(L.sampler == MRG_PT_SAMPLER_ZSOBOL && (s = pt_zsobol(c, *p, L, w)) != MRG_OK) return s;
     camera_frame(*p, L.cam);
     R.partition = p->partitionByMaterial == 1u ||
                   (p->partitionByMaterial == 2u && (c->ptMaterialGroups > 1u || c->ptEnvSet));

@@ -157,8 +157,11 @@ class PathTracer:
 
     @staticmethod
     def params(width, height, spp, camera, max_depth=8, rr_start=3, sample_mode=N.MRG_PT_NEE_MIS,
-               seed=0, filter_radius=1.0, samples_per_pass=0, sample_start=0, partition="auto"):
+               seed=0, filter_radius=1.0, samples_per_pass=0, sample_start=0, partition="auto",
+               sampler="independent", sampler_max_spp=0):
         p = N.MrgPtParams()
+        p.sampler = {"independent": 0, "zsobol": 1}[sampler]
+        p.samplerMaxSpp = sampler_max_spp
         p.width, p.height, p.spp = width, height, spp
         p.samplesPerPass = samples_per_pass
         p.rrStart, p.maxDepth = rr_start, max_depth

@@ -277,7 +277,7 @@ class PtParams(C.Structure):
                 ("filterRadius", C.c_float), ("camPos", C.c_float * 3),
                 ("camBottomLeft", C.c_float * 3), ("camRight", C.c_float * 3),
                 ("camUp", C.c_float * 3), ("planeSize", C.c_float * 2),
-                ("nearT", C.c_float), ("farT", C.c_float)]
+                ("nearT", C.c_float), ("farT", C.c_float), ("sampler", u32), ("samplerMaxSpp", u32)]
 
 
 class PtSurface(C.Structure):
@@ -541,8 +541,9 @@ class PtScene:
 
     @staticmethod
     def params(width, height, spp, camera, max_depth=8, rr_start=3, sample_mode=PT_NEE_MIS, seed=0,
-               filter_radius=1.0, sample_start=0):
+               filter_radius=1.0, sample_start=0, sampler=0, sampler_max_spp=0):
         p = PtParams()
+        p.sampler, p.samplerMaxSpp = sampler, sampler_max_spp
         p.width, p.height, p.spp, p.sampleStart = width, height, spp, sample_start
         p.rrStart, p.maxDepth, p.sampleMode, p.seed = rr_start, max_depth, sample_mode, seed
         p.filterRadius = filter_radius

@@ -29,6 +29,7 @@
  */
 #include "mrg_oracle.h"
 #include "pt_oracle.h"
+#include "zsobol_oracle.h"
 
 #include <math.h>
 #include <pthread.h>
@@ -54,6 +55,36 @@ static inline float rnd(uint32_t key, uint32_t bounce, uint32_t dim)
 {
     uint32_t h = pcg_hash(key ^ pcg_hash((bounce << 4) | dim));
     return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
+/* The sample's random-number source: the counter-based hash, or MRay's ZSobol
+ * group under the path tracer's dimension plan (film-filter offset = Next2D(0),
+ * wavelengths = Next(2); bounce b from dimension 3 + 7b: k 0..2 = Next3D(+0),
+ * k 3 = Next(+3), k 4, 5 = Next2D(+4), k 8 = Next(+6)), converted as
+ * RNGFunctions::ToFloat01 does (Source/Tracer/Random.h:100-119). */
+typedef struct
+{
+    uint32_t key, px, py, sample, seed, sampler, maxSpp, resBits;
+} smp_ctx;
+
+static float urnd(const smp_ctx* c, uint32_t bounce, uint32_t k)
+{
+    if(c->sampler == 0u) return rnd(c->key, bounce, k);
+    uint32_t dim, size, comp;
+    if(k == 6u || k == 7u) { dim = 0u; size = 2u; comp = k - 6u; }
+    else if(k == 9u) { dim = 2u; size = 1u; comp = 0u; }
+    else
+    {
+        const uint32_t b = 3u + 7u * bounce;
+        if(k <= 2u) { dim = b; size = 3u; comp = k; }
+        else if(k == 3u) { dim = b + 3u; size = 1u; comp = 0u; }
+        else if(k <= 5u) { dim = b + 4u; size = 2u; comp = k - 4u; }
+        else { dim = b + 6u; size = 1u; comp = 0u; }
+    }
+    uint32_t v = orc_zs_number(c->px, c->py, c->seed, c->sample, c->maxSpp, c->resBits, dim, size, comp);
+    float f = (float)v * 0x1p-32f;
+    const float prev1 = 0x1.fffffep-1f;
+    return f < prev1 ? f : prev1;
 }
 
 static inline float dot3f(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
@@ -668,6 +699,8 @@ typedef struct
     atomic_int                adjNextBuffer;
     float*                    image;
     atomic_uint               nextRow;
+    uint32_t*                 zsSeeds;      /* ZSobol per-pixel seeds, or NULL */
+    uint32_t                  zsResBits;
 } pt_job;
 
 /* One ray cast through the oracle accelerator. */
@@ -746,11 +779,13 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
     const orc_pt_params* P = J->p;
     const uint32_t pixel = y * P->width + x;
     const uint32_t key = path_key(P->seed, pixel, sample);
+    smp_ctx SC = { key, x, y, sample, J->zsSeeds ? J->zsSeeds[pixel] : 0u, J->zsSeeds ? 1u : 0u,
+                   P->samplerMaxSpp ? P->samplerMaxSpp : P->sampleStart + P->spp, J->zsResBits };
     outRad[0] = outRad[1] = outRad[2] = 0.0f;
 
     /* camera ray: Gaussian offset by Box-Muller, weight filter/pdf = 1 */
     float sigma = P->filterRadius * 0.285714f;
-    float u1 = rnd(key, 0, 6), u2 = rnd(key, 0, 7);
+    float u1 = urnd(&SC, 0, 6), u2 = urnd(&SC, 0, 7);
     float rr = sigma * sqrtf(-2.0f * logf(1.0f - u1));
     float ox = rr * cosf(2.0f * PI_F * u2), oy = rr * sinf(2.0f * PI_F * u2);
     float dx = P->planeSize[0] / (float)P->width, dy = P->planeSize[1] / (float)P->height;
@@ -772,7 +807,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
     const orc_spectral* S = J->spec;
     const int nc = S ? 4 : 3;
     float waves[4] = { 0, 0, 0, 0 }, wpdf[4] = { 1, 1, 1, 1 };
-    if(S) orc_spec_sample_waves(rnd(key, 0, 9), waves, wpdf);
+    if(S) orc_spec_sample_waves(urnd(&SC, 0, 9), waves, wpdf);
     uint32_t depth = 0;
     int type = 0;           /* 0 camera, 1 path (diffuse) */
     float prevPdf = 0.0f;
@@ -888,7 +923,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
         /* ---- NEE (WorkFunctionNEE); no shadow ray for specular materials ---- */
         if(P->sampleMode != ORC_PT_PURE && nAll > 0 && !isSpec)
         {
-            float dXi = rnd(key, depth, 3);
+            float dXi = urnd(&SC, depth, 3);
             uint32_t li = (uint32_t)(dXi * (float)nAll);
             if(li > nAll - 1u) li = nAll - 1u;
             float lp[3], lightPdf;
@@ -897,7 +932,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             {
                 /* skysphere: a point sceneDiameter away along the sampled direction */
                 float wd[3], spdf;
-                env_sample(E, rnd(key, depth, 4), rnd(key, depth, 5), wd, &spdf);
+                env_sample(E, urnd(&SC, depth, 4), urnd(&SC, depth, 5), wd, &spdf);
                 for(int k = 0; k < 3; k++) lp[k] = pos[k] + wd[k] * E->sceneDiameter;
                 float sd[3] = { pos[0] - lp[0], pos[1] - lp[1], pos[2] - lp[2] };
                 normalize3f(sd);
@@ -909,7 +944,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             else
             {
                 const orc_pt_light_tri* L = &J->lights[li];
-                float r1 = sqrtf(rnd(key, depth, 4)), r2 = rnd(key, depth, 5);
+                float r1 = sqrtf(urnd(&SC, depth, 4)), r2 = urnd(&SC, depth, 5);
                 float a = 1.0f - r1, b = (1.0f - r2) * r1, c = r1 * r2;
                 for(int k = 0; k < 3; k++) lp[k] = L->p0[k] * a + L->p1[k] * b + L->p2[k] * c;
                 float sd[3] = { pos[0] - lp[0], pos[1] - lp[1], pos[2] - lp[2] };
@@ -983,7 +1018,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             if(backSide) { float t = fromEta; fromEta = toEta; toEta = t; }
             float cosT = fabsf(V[2]);
             float f = fresnel_dielectric(cosT, fromEta, toEta);
-            int doRefl = rnd(key, depth, 0) < f;
+            int doRefl = urnd(&SC, depth, 0) < f;
             if(doRefl) { Ll[0] = -V[0]; Ll[1] = -V[1]; Ll[2] = 2.0f * V[2] - V[2]; }
             else
             {
@@ -1004,7 +1039,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
         {
             float alpha = sf->roughness * sf->roughness;
             float ratio = unreal_mis_ratio(sf, avg_albedo(alb, nc));
-            float sXi = rnd(key, depth, 0), x0 = rnd(key, depth, 1), x1 = rnd(key, depth, 2);
+            float sXi = urnd(&SC, depth, 0), x0 = urnd(&SC, depth, 1), x1 = urnd(&SC, depth, 2);
             float H[3], pd, ps;
             if(sXi < ratio)
             {
@@ -1056,7 +1091,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
         }
         else
         {
-            float xi0 = rnd(key, depth, 0), xi1 = rnd(key, depth, 1);
+            float xi0 = urnd(&SC, depth, 0), xi1 = urnd(&SC, depth, 1);
             float ang = 2.0f * PI_F * xi1, sr = sqrtf(xi0);
             Ll[0] = sr * cosf(ang); Ll[1] = sr * sinf(ang);
             Ll[2] = sqrtf(fmaxf(0.0f, 1.0f - (Ll[0] * Ll[0] + Ll[1] * Ll[1])));
@@ -1076,7 +1111,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             float pr = (nc == 4) ? (thr[0] + thr[1] + thr[2] + thr[3]) * 0.25f
                                  : (thr[0] + thr[1] + thr[2]) * 0.33333333f;
             pr = fminf(fmaxf(pr, 0.1f), 1.0f);
-            float xr = rnd(key, depth - 1u, 8);
+            float xr = urnd(&SC, depth - 1u, 8);
             if(xr >= pr) dead = 1;
             else { float inv = 1.0f / pr; for(int k = 0; k < nc; k++) thr[k] *= inv; }
         }
@@ -1148,6 +1183,18 @@ static void* pt_adj_worker(void* arg)
     return NULL;
 }
 
+/* ZSobol sampler state of a job (seeds of the whole image). */
+static int job_sampler(pt_job* J, const orc_pt_params* p)
+{
+    J->zsSeeds = NULL;
+    if(p->sampler != 1u) return 0;
+    J->zsSeeds = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)p->width * p->height);
+    if(!J->zsSeeds) return -2;
+    orc_zs_seeds(p->width, p->height, (uint64_t)p->seed, J->zsSeeds);
+    J->zsResBits = orc_zs_res_max_bits(p->width, p->height);
+    return 0;
+}
+
 int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
                    const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
                    const void* texels, uint32_t texW, uint32_t texH, const float* delta,
@@ -1169,6 +1216,7 @@ int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surf
     J.adjGradE = gradEmission ? bufsE : NULL;
     J.adjInstances = nInstances;
     J.adjWorkers = nthreads;
+    if(job_sampler(&J, p) != 0) { free(bufs); return -2; }
     atomic_init(&J.nextRow, 0u);
     atomic_init(&J.adjNextBuffer, 0);
     pthread_t th[64];
@@ -1183,6 +1231,7 @@ int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surf
         for(size_t i = 0; i < ne; i++) gradEmission[i] += bufsE[(size_t)t * ne + i];
     }
     free(bufs);
+    free(J.zsSeeds);
     return 0;
 }
 
@@ -1197,6 +1246,7 @@ int orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surfa
     J.env = env;
     J.spec = spectral;
     J.image = image;
+    if(job_sampler(&J, p) != 0) return -2;
     atomic_init(&J.nextRow, 0u);
     if(nthreads < 1) nthreads = 1;
     if(nthreads > 256) nthreads = 256;
@@ -1206,6 +1256,7 @@ int orc_pt_render(const orc_scene* s, const orc_pt_params* p, const orc_pt_surfa
         if(pthread_create(&th[started], NULL, pt_worker, &J) == 0) started++;
     pt_worker(&J);
     for(int t = 0; t < started; t++) pthread_join(th[t], NULL);
+    free(J.zsSeeds);
     return 0;
 }
 

@@ -282,3 +282,18 @@ int orc_zs_generate(uint32_t width, uint32_t height, const uint32_t* seeds, uint
     }
     return 0;
 }
+
+uint32_t orc_zs_number(uint32_t px, uint32_t py, uint32_t seed, uint32_t sampleIndex, uint32_t initialMaxSpp,
+                       uint32_t resMaxBits, uint32_t dim, uint32_t size, uint32_t comp)
+{
+    zs_init();
+    zs_gen g = zs_make(morton2(px, py), sampleIndex, seed, initialMaxSpp, resMaxBits);
+    const uint64_t a = zs_index(&g, dim);
+    const uint64_t h = hash_dim_seed(dim, seed);
+    uint32_t scr;
+    if(size == 1u) scr = (uint32_t)h;
+    else if(size == 2u) scr = comp ? (uint32_t)(h >> 32) : (uint32_t)h;
+    else scr = (comp == 0u) ? (uint32_t)(h & 0x1FFFFFull)
+             : (comp == 1u) ? (uint32_t)((h >> 21) & 0x1FFFFFull) : (uint32_t)(h >> 42);
+    return owen_fast(mat_mul((int)comp, a), scr);
+}
