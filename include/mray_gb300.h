@@ -236,8 +236,9 @@ typedef struct mrg_pt_params
     uint32_t sampler;            /* MRG_PT_SAMPLER_*: the paths' random numbers */
     uint32_t samplerMaxSpp;      /* ZSobol initialMaxSampleCount (0: sampleStart + spp) */
 } mrg_pt_params;
-/* Samplers: counter-based independent numbers (the default), or MRay's ZSobol
- * group (see mrg_zsobol_generate) with seeds from params.seed. */
+/* Samplers (TracerParameters::samplerType, Source/Core/TracerI.h:56):
+ * counter-based independent numbers (the default), or MRay's ZSobol group (see
+ * mrg_zsobol_generate) with seeds from params.seed. */
 #define MRG_PT_SAMPLER_INDEPENDENT 0u
 #define MRG_PT_SAMPLER_ZSOBOL      1u
 
