@@ -241,6 +241,10 @@ typedef struct mrg_pt_params
  * mrg_zsobol_generate) with seeds from params.seed. */
 #define MRG_PT_SAMPLER_INDEPENDENT 0u
 #define MRG_PT_SAMPLER_ZSOBOL      1u
+/* ZSobol with the scrambled value bit-reversed back (Laine-Karras Owen
+ * scrambling as published), which keeps the Sobol points' stratification that
+ * MRay's ScambleOwenFast (Source/Tracer/Random.cu:141-150) loses. */
+#define MRG_PT_SAMPLER_ZSOBOL_OWEN 2u
 
 /* Surface description of an instance, the equivalent of attaching a
  * material / light group to a surface (TracerI::CreateSurface, CreateLightSurface).

@@ -576,7 +576,8 @@ __device__ __forceinline__ uint32_t slot_sample(const PtLaunch& L, uint32_t i)
 }
 
 // Random number k of bounce b of slot i's path: the counter-based hash, or
-// MRay's ZSobol group (sampler 1) under this dimension plan: the film-filter
+// MRay's ZSobol group (sampler 1; sampler 2 with the scramble's bit reversal
+// undone, which keeps the stratification) under this dimension plan: the film-filter
 // offset (k 6, 7) = Next2D(0), the wavelengths (k 9) = Next(2); bounce b from
 // dimension 3 + 7b: k 0..2 (lobe choice and direction) = Next3D(+0), light
 // choice (k 3) = Next(+3), light point (k 4, 5) = Next2D(+4), Russian
@@ -599,7 +600,7 @@ __device__ __noinline__ float rnd_zsobol(const PtLaunch& L, uint32_t i, uint32_t
     const ZsGen g = zs_make(pixel % L.width, pixel / L.width, __ldg(L.zsSeeds + pixel), slot_sample(L, i),
                             L.zsMaxSpp, L.zsResBits);
     const uint64_t* perm = reinterpret_cast<const uint64_t*>(L.zsTables + 3 * kZsWidth);
-    return zs_to_float01(zs_number(g, L.zsTables, perm, dim, size, comp));
+    return zs_to_float01(zs_number(g, L.zsTables, perm, dim, size, comp, L.sampler == 2u));
 }
 
 __device__ __forceinline__ float rnd_s(const PtLaunch& L, uint32_t key, uint32_t i, uint32_t bounce, uint32_t k)

@@ -628,9 +628,9 @@ mrg_status pt_setup(mrg_ctx* c, const mrg_pt_params* p, PtRun& R, const char* wh
     L.env = c->ptEnv;
     L.spec = c->ptSpec;
     L.filterSigma = p->filterRadius * 0.285714f;
-    if(p->sampler > MRG_PT_SAMPLER_ZSOBOL) return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": unknown sampler");
+    if(p->sampler > MRG_PT_SAMPLER_ZSOBOL_OWEN) return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": unknown sampler");
     L.sampler = p->sampler;
-    if(L.sampler == MRG_PT_SAMPLER_ZSOBOL && (s = pt_zsobol(c, *p, L, w)) != MRG_OK) return s;
+    if(L.sampler != MRG_PT_SAMPLER_INDEPENDENT && (s = pt_zsobol(c, *p, L, w)) != MRG_OK) return s;
     camera_frame(*p, L.cam);
     R.partition = p->partitionByMaterial == 1u ||
                   (p->partitionByMaterial == 2u && (c->ptMaterialGroups > 1u || c->ptEnvSet));

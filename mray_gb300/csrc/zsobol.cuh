@@ -118,9 +118,12 @@ __device__ __forceinline__ uint64_t zs_hash(uint32_t dim, uint32_t seed)
     return zs_hash_pcg64((uint64_t)seed + zs_hash_pcg64((uint64_t)dim));
 }
 
-// Component `comp` of the `size`-number request at dimension `dim`.
+// Component `comp` of the `size`-number request at dimension `dim`.  With
+// `owen` the scrambled value is bit-reversed back (the Laine-Karras form of
+// Owen scrambling, which keeps the Sobol points' stratification); MRay's
+// ScambleOwenFast leaves it reversed.
 __device__ __forceinline__ uint32_t zs_number(const ZsGen& g, const uint32_t* mat, const uint64_t* perm,
-                                              uint32_t dim, uint32_t size, uint32_t comp)
+                                              uint32_t dim, uint32_t size, uint32_t comp, bool owen = false)
 {
     const uint64_t a = zs_sample_index(g, perm, dim);
     const uint64_t h = zs_hash(dim, g.seed);
@@ -129,7 +132,8 @@ __device__ __forceinline__ uint32_t zs_number(const ZsGen& g, const uint32_t* ma
     else if(size == 2u) scr = comp ? (uint32_t)(h >> 32) : (uint32_t)h;
     else scr = (comp == 0u) ? (uint32_t)(h & 0x1FFFFFull)
              : (comp == 1u) ? (uint32_t)((h >> 21) & 0x1FFFFFull) : (uint32_t)(h >> 42);
-    return zs_owen_fast(zs_mat_mul(mat, (int)comp, a), scr);
+    const uint32_t v = zs_owen_fast(zs_mat_mul(mat, (int)comp, a), scr);
+    return owen ? __brev(v) : v;
 }
 
 // RNGFunctions::ToFloat01<float, uint32_t> (Source/Tracer/Random.h:100-119).

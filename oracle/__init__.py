@@ -84,6 +84,8 @@ def lib():
         L.orc_zs_seeds.argtypes = [u32, u32, C.c_uint64, vp]
         L.orc_zs_generate.argtypes = [u32, u32, vp, u32, u32, u32, C.c_uint64, u32, vp]
         L.orc_zs_generate.restype = C.c_int
+        L.orc_zs_number.argtypes = [u32, u32, u32, u32, u32, u32, u32, u32, u32, C.c_int]
+        L.orc_zs_number.restype = u32
         L.orc_pt_render.restype = C.c_int
         L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
         L.orc_pt_make_light.argtypes = [vp, vp, vp, C.c_int, vp]
@@ -628,3 +630,9 @@ def zsobol_generate(width, height, seeds, initial_max_spp, sample_index, dim_sta
     if rc != 0:
         raise ValueError("zsobol_generate: bad arguments")
     return out
+
+
+def zsobol_number(px, py, seed, sample_index, initial_max_spp, res_max_bits, dim, size, comp, owen=False):
+    """One ZSobol number (component comp of a size-number request)."""
+    return int(lib().orc_zs_number(px, py, seed, sample_index, initial_max_spp, res_max_bits, dim, size, comp,
+                                   1 if owen else 0))

@@ -81,7 +81,8 @@ static float urnd(const smp_ctx* c, uint32_t bounce, uint32_t k)
         else if(k <= 5u) { dim = b + 4u; size = 2u; comp = k - 4u; }
         else { dim = b + 6u; size = 1u; comp = 0u; }
     }
-    uint32_t v = orc_zs_number(c->px, c->py, c->seed, c->sample, c->maxSpp, c->resBits, dim, size, comp);
+    uint32_t v = orc_zs_number(c->px, c->py, c->seed, c->sample, c->maxSpp, c->resBits, dim, size, comp,
+                               c->sampler == 2u);
     float f = (float)v * 0x1p-32f;
     const float prev1 = 0x1.fffffep-1f;
     return f < prev1 ? f : prev1;
@@ -779,7 +780,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
     const orc_pt_params* P = J->p;
     const uint32_t pixel = y * P->width + x;
     const uint32_t key = path_key(P->seed, pixel, sample);
-    smp_ctx SC = { key, x, y, sample, J->zsSeeds ? J->zsSeeds[pixel] : 0u, J->zsSeeds ? 1u : 0u,
+    smp_ctx SC = { key, x, y, sample, J->zsSeeds ? J->zsSeeds[pixel] : 0u, J->zsSeeds ? P->sampler : 0u,
                    P->samplerMaxSpp ? P->samplerMaxSpp : P->sampleStart + P->spp, J->zsResBits };
     outRad[0] = outRad[1] = outRad[2] = 0.0f;
 
@@ -1187,7 +1188,7 @@ static void* pt_adj_worker(void* arg)
 static int job_sampler(pt_job* J, const orc_pt_params* p)
 {
     J->zsSeeds = NULL;
-    if(p->sampler != 1u) return 0;
+    if(p->sampler != 1u && p->sampler != 2u) return 0;
     J->zsSeeds = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)p->width * p->height);
     if(!J->zsSeeds) return -2;
     orc_zs_seeds(p->width, p->height, (uint64_t)p->seed, J->zsSeeds);

@@ -284,7 +284,7 @@ int orc_zs_generate(uint32_t width, uint32_t height, const uint32_t* seeds, uint
 }
 
 uint32_t orc_zs_number(uint32_t px, uint32_t py, uint32_t seed, uint32_t sampleIndex, uint32_t initialMaxSpp,
-                       uint32_t resMaxBits, uint32_t dim, uint32_t size, uint32_t comp)
+                       uint32_t resMaxBits, uint32_t dim, uint32_t size, uint32_t comp, int owen)
 {
     zs_init();
     zs_gen g = zs_make(morton2(px, py), sampleIndex, seed, initialMaxSpp, resMaxBits);
@@ -295,5 +295,6 @@ uint32_t orc_zs_number(uint32_t px, uint32_t py, uint32_t seed, uint32_t sampleI
     else if(size == 2u) scr = comp ? (uint32_t)(h >> 32) : (uint32_t)h;
     else scr = (comp == 0u) ? (uint32_t)(h & 0x1FFFFFull)
              : (comp == 1u) ? (uint32_t)((h >> 21) & 0x1FFFFFull) : (uint32_t)(h >> 42);
-    return owen_fast(mat_mul((int)comp, a), scr);
+    const uint32_t v = owen_fast(mat_mul((int)comp, a), scr);
+    return owen ? brev32(v) : v;
 }

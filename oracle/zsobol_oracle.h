@@ -21,9 +21,10 @@ int      orc_zs_generate(uint32_t width, uint32_t height, const uint32_t* seeds,
                          uint32_t* out);
 
 /* Component comp of the size-number request at dimension dim of one
- * pixel's sample (ZSobol::Next / Next2D / Next3D). */
+ * pixel's sample (ZSobol::Next / Next2D / Next3D); owen != 0 reverses the
+ * scrambled value's bits back (Laine-Karras Owen scrambling as published). */
 uint32_t orc_zs_number(uint32_t px, uint32_t py, uint32_t seed, uint32_t sampleIndex, uint32_t initialMaxSpp,
-                       uint32_t resMaxBits, uint32_t dim, uint32_t size, uint32_t comp);
+                       uint32_t resMaxBits, uint32_t dim, uint32_t size, uint32_t comp, int owen);
 
 #ifdef __cplusplus
 }

@@ -93,3 +93,24 @@ def test_oracle_render_with_zsobol_is_statistically_equal():
     assert not np.array_equal(a, b)
     assert abs(a.mean() - b.mean()) <= 0.03 * a.mean()
     assert float(np.mean((a - b) ** 2 / (a ** 2 + 1e-2))) <= 0.05
+
+
+def test_owen_variant_keeps_stratification():
+    """16 samples of one pixel, a 2D request: with the scramble's reversal
+    undone every cell of the 4x4 grid (and of the 16x1 and 1x16 grids) holds
+    one point, as a scrambled (0, 2)-sequence must; MRay's form does not keep
+    that for every pixel."""
+    def points(owen, px, py, seed):
+        return np.array([[oracle.zsobol_number(px, py, seed, s, 16, 6, 0, 2, c, owen) for c in range(2)]
+                         for s in range(16)], np.uint64)
+
+    strat_mray = 0
+    for px, py, seed in ((3, 5, 11), (40, 7, 12345), (0, 0, 99), (63, 63, 7)):
+        p = points(True, px, py, seed)
+        for bx, by in ((2, 2), (4, 0), (0, 4)):
+            cells = (p[:, 0] >> np.uint64(32 - bx)) * (1 << by) + (p[:, 1] >> np.uint64(32 - by))
+            assert len(set(cells.tolist())) == 16, (px, py, bx, by)
+        q = points(False, px, py, seed)
+        cells = (q[:, 0] >> np.uint64(30)) * 4 + (q[:, 1] >> np.uint64(30))
+        strat_mray += len(set(cells.tolist())) == 16
+    assert strat_mray < 4
