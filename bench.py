@@ -296,23 +296,31 @@ def box_scene_pt(args, dev):
     pt = PathTracer(dev.index or 0)
     load_box_scene(pt, 0)
     cam = scenes.box_camera()
-    p = PathTracer.params(256, 256, 16, cam, max_depth=8, rr_start=3, seed=0)
-    img = pt.render(p)
-    torch.cuda.synchronize(dev)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
     reps = max(3, min(args.steps, 20))
-    e0.record()
-    for r in range(reps):
-        p.sampleStart = 16 * (r + 1)
-        pt.render(p, image=img)
-    e1.record()
-    torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1) / reps
+
+    def timed(sampler):
+        # the ZSobol group's initial sample count covers every timed call
+        p = PathTracer.params(256, 256, 16, cam, max_depth=8, rr_start=3, seed=0, sampler=sampler,
+                              sampler_max_spp=16 * (reps + 1))
+        img = pt.render(p)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for r in range(reps):
+            p.sampleStart = 16 * (r + 1)
+            pt.render(p, image=img)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps
+
+    ms = timed("independent")
+    ms_zs = timed("zsobol-owen")
     pt.close()
     return {"box_pt_ms_per_16spp": round(ms, 3),
             "box_pt_spp_per_s": round(16.0 / (ms * 1e-3), 1),
-            "box_pt_mpaths_per_s": round(256 * 256 * 16 / (ms * 1e-3) / 1e6, 1)}
+            "box_pt_mpaths_per_s": round(256 * 256 * 16 / (ms * 1e-3) / 1e6, 1),
+            "box_pt_zsobol_ms_per_16spp": round(ms_zs, 3)}
 
 
 def _spectral_inputs():

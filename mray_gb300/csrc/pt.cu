@@ -608,6 +608,35 @@ __device__ __forceinline__ float rnd_s(const PtLaunch& L, uint32_t key, uint32_t
     return (L.sampler == 0u) ? rnd(key, bounce, k) : rnd_zsobol(L, i, bounce, k);
 }
 
+// The bounce's numbers k 0..2 (one Next3D request) or k 4, 5 (one Next2D
+// request) at once; each equals rnd_s of that k.
+__device__ __noinline__ float4 rnd_zsobol_group(const PtLaunch& L, uint32_t i, uint32_t bounce, uint32_t k0)
+{
+    const uint32_t b = 3u + 7u * bounce;
+    const uint32_t dim = (k0 == 0u) ? b : b + 4u, size = (k0 == 0u) ? 3u : 2u;
+    const uint32_t pixel = slot_pixel(L, i);
+    const ZsGen g = zs_make(pixel % L.width, pixel / L.width, __ldg(L.zsSeeds + pixel), slot_sample(L, i),
+                            L.zsMaxSpp, L.zsResBits);
+    const uint64_t* perm = reinterpret_cast<const uint64_t*>(L.zsTables + 3 * kZsWidth);
+    uint32_t v[3] = { 0u, 0u, 0u };
+    zs_numbers(g, L.zsTables, perm, dim, size, v, L.sampler == 2u);
+    return make_float4(zs_to_float01(v[0]), zs_to_float01(v[1]), zs_to_float01(v[2]), 0.0f);
+}
+
+__device__ __forceinline__ float3 rnd_s3(const PtLaunch& L, uint32_t key, uint32_t i, uint32_t bounce)
+{
+    if(L.sampler == 0u) return make_float3(rnd(key, bounce, 0), rnd(key, bounce, 1), rnd(key, bounce, 2));
+    const float4 r = rnd_zsobol_group(L, i, bounce, 0u);
+    return make_float3(r.x, r.y, r.z);
+}
+
+__device__ __forceinline__ float2 rnd_s45(const PtLaunch& L, uint32_t key, uint32_t i, uint32_t bounce)
+{
+    if(L.sampler == 0u) return make_float2(rnd(key, bounce, 4), rnd(key, bounce, 5));
+    const float4 r = rnd_zsobol_group(L, i, bounce, 4u);
+    return make_float2(r.x, r.y);
+}
+
 // ---------------------------------------------------------------------------
 // Camera rays: pinhole (CamerasDefault.hpp:94-140), Gaussian film filter
 // sampled with Box-Muller (filter / pdf = 1 per sample, Filters.h:195-233);
@@ -1007,7 +1036,8 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         {
                             // skysphere: a point sceneDiameter away along the sampled direction
                             float spdf;
-                            const float3 wd = env_sample(L.env, rnd_s(L, key, i, depth, 4), rnd_s(L, key, i, depth, 5), spdf);
+                            const float2 u45 = rnd_s45(L, key, i, depth);
+                            const float3 wd = env_sample(L.env, u45.x, u45.y, spdf);
                             lp = make_float3(add(pos.x, mul(wd.x, L.env.sceneDiameter)),
                                              add(pos.y, mul(wd.y, L.env.sceneDiameter)),
                                              add(pos.z, mul(wd.z, L.env.sceneDiameter)));
@@ -1019,7 +1049,8 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         else
                         {
                             const PtLight lt = lights[li];
-                            const float r1 = __fsqrt_rn(rnd_s(L, key, i, depth, 4)), r2 = rnd_s(L, key, i, depth, 5);
+                            const float2 u45 = rnd_s45(L, key, i, depth);
+                            const float r1 = __fsqrt_rn(u45.x), r2 = u45.y;
                             const float a = sub(1.0f, r1), b = mul(sub(1.0f, r2), r1), c = mul(r1, r2);
                             lp = make_float3(add(add(mul(lt.p0.x, a), mul(lt.p1.x, b)), mul(lt.p2.x, c)),
                                              add(add(mul(lt.p0.y, a), mul(lt.p1.y, b)), mul(lt.p2.y, c)),
@@ -1106,7 +1137,8 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         const float rough = sf.albedo.w;
                         const float alpha = mul(rough, rough);
                         const float ratio = unreal_ratio(sf, avg_albedo<NC>(alb));
-                        const float sXi = rnd_s(L, key, i, depth, 0), x0 = rnd_s(L, key, i, depth, 1), x1 = rnd_s(L, key, i, depth, 2);
+                        const float3 u3 = rnd_s3(L, key, i, depth);
+                        const float sXi = u3.x, x0 = u3.y, x1 = u3.z;
                         float3 H;
                         float pd, ps;
                         if(sXi < ratio)
@@ -1156,7 +1188,8 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                     }
                     else
                     {
-                        const float xi0 = rnd_s(L, key, i, depth, 0), xi1 = rnd_s(L, key, i, depth, 1);
+                        const float3 u3 = rnd_s3(L, key, i, depth);
+                        const float xi0 = u3.x, xi1 = u3.y;
                         const float ang = mul(mul(2.0f, kPi), xi1), sr = __fsqrt_rn(xi0);
                         Ll.x = mul(sr, cosf(ang)); Ll.y = mul(sr, sinf(ang));
                         Ll.z = __fsqrt_rn(fmaxf(0.0f, sub(1.0f, add(mul(Ll.x, Ll.x), mul(Ll.y, Ll.y)))));

@@ -136,6 +136,25 @@ __device__ __forceinline__ uint32_t zs_number(const ZsGen& g, const uint32_t* ma
     return owen ? __brev(v) : v;
 }
 
+// Components 0 .. size-1 of the request at `dim` (sample index and hash
+// computed once); each equals zs_number's result for that component.
+__device__ __forceinline__ void zs_numbers(const ZsGen& g, const uint32_t* mat, const uint64_t* perm, uint32_t dim,
+                                           uint32_t size, uint32_t* out, bool owen = false)
+{
+    const uint64_t a = zs_sample_index(g, perm, dim);
+    const uint64_t h = zs_hash(dim, g.seed);
+    for(uint32_t comp = 0; comp < size; comp++)
+    {
+        uint32_t scr;
+        if(size == 1u) scr = (uint32_t)h;
+        else if(size == 2u) scr = comp ? (uint32_t)(h >> 32) : (uint32_t)h;
+        else scr = (comp == 0u) ? (uint32_t)(h & 0x1FFFFFull)
+                 : (comp == 1u) ? (uint32_t)((h >> 21) & 0x1FFFFFull) : (uint32_t)(h >> 42);
+        const uint32_t v = zs_owen_fast(zs_mat_mul(mat, (int)comp, a), scr);
+        out[comp] = owen ? __brev(v) : v;
+    }
+}
+
 // RNGFunctions::ToFloat01<float, uint32_t> (Source/Tracer/Random.h:100-119).
 __device__ __forceinline__ float zs_to_float01(uint32_t v)
 {
