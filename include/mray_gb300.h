@@ -168,12 +168,16 @@ mrg_status mrg_cast_closest_host(mrg_ctx* ctx, mrg_ray* h_rays, uint32_t n,
  * or a real-time / plugin thread that may not grow the device heap): the
  * device staging for rays, hit keys and meta hits plus the kernel's work
  * counter and error flag live in one static __device__ array of the library
- * (about 14 MiB, held by every GPU that loads the library until exit).  It
- * calls no cudaMalloc / cudaFree and nothing that allocates.
+ * (about 14 MiB).  The driver allocates that array on a device when the
+ * library's module loads there; mrg_create forces the load and looks up the
+ * array's device address (with the device current), so the array is resident
+ * from the first context on a device until the process exits.  The call
+ * itself calls no cudaMalloc / cudaFree and nothing that allocates.
  *  - n must be <= MRG_NOALLOC_MAX_RAYS, otherwise MRG_ERR_LIMIT;
- *  - the first call on a device looks up the array's device address (once
- *    per device, with that device current); make that first call before any
- *    stream capture;
+ *  - the device address is cached per process and refreshed by every
+ *    mrg_create; after a device reset (cudaDeviceReset or a primary-context
+ *    reset by the application) contexts created before the reset are invalid
+ *    and a new one must be created;
  *  - every call shares the one array and leaves its contents behind, so calls
  *    that overlap on the GPU (other threads, other contexts on the same
  *    device) race: serialise them.

@@ -158,6 +158,13 @@ mrg_status mrg_create(const mrg_params* params, mrg_ctx** out)
         mrg_destroy(c);
         return s;
     }
+    // the allocation-free cast's static array and kernel are loaded here,
+    // where allocating is allowed, not in its first call
+    if(mrg_status s = mrg::noalloc_prepare(dev); s != MRG_OK)
+    {
+        mrg_destroy(c);
+        return s;
+    }
     *out = c;
     return MRG_OK;
 }

@@ -111,6 +111,9 @@ cudaError_t launch_closest(const TraceScene& sc, const TraceScratch& scr, void* 
 cudaError_t launch_visibility(const TraceScene& sc, const TraceScratch& scr, uint32_t* visBits,
                               const void* rays, const uint32_t* rayIdx, uint32_t n,
                               int smCount, cudaStream_t st, const uint32_t* nDevice = nullptr);
+// Loads the closest-hit traversal kernel on the current device (a function
+// attribute query forces a lazily loaded module in).
+cudaError_t preload_closest();
 cudaError_t launch_closest_stats(const TraceScene& sc, const TraceScratch& scr, const void* rays,
                                  uint32_t n, int smCount, cudaStream_t st);
 

@@ -162,5 +162,11 @@ namespace mrg {
 mrg_status set_error(mrg_status s, const std::string& msg);
 // Grows the context's partitioner scratch to `words` 32-bit words.
 mrg_status partition_scratch(mrg_ctx* c, size_t words);
+// Called by mrg_create with `device` current: loads the module that holds the
+// allocation-free cast's static array and the closest-hit kernel (both are
+// allocated by the driver when their module loads) and records the array's
+// device address, so that mrg_cast_closest_host_noalloc itself never makes the
+// driver allocate.
+mrg_status noalloc_prepare(int device);
 
 } // namespace mrg

@@ -25,35 +25,48 @@ constexpr size_t kMaxRays = MRG_NOALLOC_MAX_RAYS;
 constexpr size_t kScratchBytes = kCtrlBytes + kMaxRays * (kRayBytes + kHitBytes + kMetaBytes);
 
 // Layout: [0, 256) control words (u32 work counter, u32 error flag);
-// then rays[kMaxRays], hits[kMaxRays], meta[kMaxRays].  Every GPU that loads
-// the library holds these ~14 MiB until the process exits.
+// then rays[kMaxRays], hits[kMaxRays], meta[kMaxRays].  The driver allocates
+// these ~14 MiB on a device when the module loads there (at the latest in the
+// first mrg_create on that device) and holds them until the process exits.
 static __device__ __align__(256) unsigned char g_noallocScratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setupMutex;
 unsigned char* g_scratchAddr[kMaxDevices] = {};
 
-// Device address of g_noallocScratch on `device`, looked up once per device
-// with that device current.  In host code the symbol name is only a host-side
-// stand-in, so kernels and copies must use this address.
+// Looks up the device address of g_noallocScratch on `device` (which must be
+// current) and records it.  In host code the symbol name is only a host-side
+// stand-in, so kernels and copies must use this address.  The lookup also
+// loads the module that holds the array, which is when the driver allocates
+// it.  mrg_create calls this for every new context, so a context created
+// after a device reset sees the re-loaded array's address.
+mrg_status resolve_scratch(int device)
+{
+    if(device < 0 || device >= kMaxDevices)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_cast_closest_host_noalloc: device ordinal out of range");
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+    if(e != cudaSuccess || p == nullptr)
+    {
+        cudaGetLastError();
+        return mrg::set_error(MRG_ERR_CUDA, std::string("mrg_cast_closest_host_noalloc: "
+                              "cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+    }
+    std::lock_guard<std::mutex> lock(g_setupMutex);
+    g_scratchAddr[device] = static_cast<unsigned char*>(p);
+    return MRG_OK;
+}
+
 mrg_status scratch_address(int device, unsigned char** out)
 {
     if(device < 0 || device >= kMaxDevices)
         return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_cast_closest_host_noalloc: device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_setupMutex);
-    if(g_scratchAddr[device] == nullptr)
     {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
-        if(e != cudaSuccess || p == nullptr)
-        {
-            cudaGetLastError();
-            return mrg::set_error(MRG_ERR_CUDA, std::string("mrg_cast_closest_host_noalloc: "
-                                  "cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
-        }
-        g_scratchAddr[device] = static_cast<unsigned char*>(p);
+        std::lock_guard<std::mutex> lock(g_setupMutex);
+        *out = g_scratchAddr[device];
     }
-    *out = g_scratchAddr[device];
+    if(*out == nullptr)   // every context comes from mrg_create, which resolves it
+        return mrg::set_error(MRG_ERR_CUDA, "mrg_cast_closest_host_noalloc: staging array not set up on this device");
     return MRG_OK;
 }
 
@@ -65,6 +78,15 @@ mrg_status cuda_err(cudaError_t e, const char* what)
 }
 
 } // namespace
+
+mrg_status mrg::noalloc_prepare(int device)
+{
+    mrg_status s = resolve_scratch(device);
+    if(s != MRG_OK) return s;
+    cudaError_t e = mrg::preload_closest();
+    if(e != cudaSuccess) return cuda_err(e, "loading the closest-hit kernel");
+    return MRG_OK;
+}
 
 extern "C" mrg_status mrg_cast_closest_host_noalloc(mrg_ctx* c, mrg_ray* hRays, uint32_t n,
                                                     mrg_hit_keys* hHits, mrg_meta_hit* hMeta)

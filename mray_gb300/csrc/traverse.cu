@@ -667,6 +667,12 @@ int blocks_for(int smCount)
 
 } // namespace
 
+cudaError_t preload_closest()
+{
+    cudaFuncAttributes a;
+    return cudaFuncGetAttributes(&a, k_trace<false, false>);
+}
+
 cudaError_t launch_closest(const TraceScene& sc, const TraceScratch& scr, void* rays,
                            const uint32_t* rayIdx, uint32_t n, void* hits, void* meta,
                            int smCount, cudaStream_t st, const uint32_t* nDevice)

@@ -24,8 +24,9 @@ def reduce_film(image, group=None):
 def render_sharded(render, total_spp, rank, world, group=None):
     """render(sample_start, spp) -> film tensor of this rank's samples;
     returns the film of all total_spp samples (identical on every rank)."""
+    # checked from the arguments every rank has, so all ranks raise together
+    # and none is left waiting in the all-reduce
+    if int(total_spp) < int(world):
+        raise ValueError("more ranks (%d) than samples (%d)" % (world, total_spp))
     start, count = sample_range(total_spp, rank, world)
-    img = render(start, count) if count else None
-    if img is None:
-        raise ValueError("more ranks than samples")
-    return reduce_film(img, group)
+    return reduce_film(render(start, count), group)

@@ -52,3 +52,12 @@ def test_two_rank_film_equals_single_render(tmp_path):
     want = S.render(S.params(24, 20, 8, scenes.box_camera(), seed=3), threads=2)
     np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-6)
     assert np.all(got[..., 3] == 8.0)
+
+
+def test_more_ranks_than_samples_raises_on_every_rank():
+    # every rank must raise before any of them reaches the film all-reduce
+    calls = []
+    for rank in range(4):
+        with pytest.raises(ValueError):
+            replicas.render_sharded(lambda s, c: calls.append((s, c)), 3, rank, 4)
+    assert calls == []

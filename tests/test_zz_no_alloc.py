@@ -6,7 +6,12 @@ that may not grow the device heap -- use this entry point: its device staging
 and control words live in a static __device__ array inside the library.  Its
 results must equal the allocating host-buffer entry point's (bit for bit, the
 tolerance of every hit test here) on two calls in a row, since the array
-keeps the previous call's contents.  This file is collected last on purpose.
+keeps the previous call's contents.  The call must also leave the device's
+free memory unchanged: its whole point is that nothing is allocated.
+
+The file name sorts last so that a run which stops at the first failure has
+already run every other test when this one runs; it also passes alone in a
+fresh process (its fixtures build the library and the scene it needs).
 """
 import ctypes as C
 
@@ -37,12 +42,18 @@ def test_noalloc_cast_matches_allocating_entry_point(cuda_lib, built_libs):
     acc.construct()
     L = N.lib()
     h = acc._h
+    import torch
     for seed, (w, hgt) in ((1, (512, 400)), (2, (300, 211))):      # two calls in a row
         rays = scenes.primary_rays(w, hgt, seed, eye=(0, 0, -10), tan_half_fov=0.45)
         assert rays.shape[0] <= N.MRG_NOALLOC_MAX_RAYS
         st0, r0, h0, m0 = _cast(L.mrg_cast_closest_host, h, rays)
+        free0 = torch.cuda.mem_get_info(0)[0]
         st1, r1, h1, m1 = _cast(L.mrg_cast_closest_host_noalloc, h, rays)
+        free1 = torch.cuda.mem_get_info(0)[0]
         assert st0 == N.MRG_OK and st1 == N.MRG_OK, L.mrg_last_error()
+        # the allocating call ran the same kernel just before, so any lazy
+        # driver set-up is done: the no-allocation call must not move free memory
+        assert free1 == free0, (free0, free1)
         assert np.array_equal(r0.view(np.uint32), r1.view(np.uint32))
         assert np.array_equal(h0, h1)
         assert np.array_equal(m0.view(np.uint32), m1.view(np.uint32))
