@@ -48,19 +48,24 @@ __device__ __forceinline__ float rnd(uint32_t key, uint32_t bounce, uint32_t dim
     return __fmul_rn((float)(h >> 8), 1.0f / 16777216.0f);
 }
 
-// Unfused a*b + c and friends (the oracle is compiled without contraction).
+// Unfused a*b + c and friends (the oracle is compiled without contraction);
+// fma only where MRay's own code calls it.
 __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+// Math::Dot (Source/Core/Math.h:1585-1596): r = 0; r = fma(a_i, b_i, r).
 __device__ __forceinline__ float dot3(float3 a, float3 b)
 {
-    return add(add(mul(a.x, b.x), mul(a.y, b.y)), mul(a.z, b.z));
+    return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmaf_rn(a.x, b.x, 0.0f)));
 }
+// LengthSqr of a 2-vector with the same fma chain.
+__device__ __forceinline__ float len2_2(float x, float y) { return __fmaf_rn(y, y, __fmaf_rn(x, x, 0.0f)); }
+// Math::Cross (Math.h:1627-1633): one fma per component.
 __device__ __forceinline__ float3 cross3(float3 a, float3 b)
 {
-    return make_float3(sub(mul(a.y, b.z), mul(a.z, b.y)),
-                       sub(mul(a.z, b.x), mul(a.x, b.z)),
-                       sub(mul(a.x, b.y), mul(a.y, b.x)));
+    return make_float3(__fmaf_rn(a.y, b.z, -mul(a.z, b.y)),
+                       __fmaf_rn(a.z, b.x, -mul(a.x, b.z)),
+                       __fmaf_rn(a.x, b.y, -mul(a.y, b.x)));
 }
 __device__ __forceinline__ float3 normalize3(float3 v)
 {
@@ -144,7 +149,7 @@ __device__ __forceinline__ float vndf_pdf(float3 V, float3 H, float alpha)
 __device__ __forceinline__ float3 vndf_sample(float3 V, float a, float xi0, float xi1)
 {
     float3 vh = normalize3(make_float3(mul(a, V.x), mul(a, V.y), V.z));
-    const float len2 = add(mul(vh.x, vh.x), mul(vh.y, vh.y));
+    const float len2 = len2_2(vh.x, vh.y);        // LengthSqr(Vector2(VHemi))
     float3 T1;
     if(len2 > 0.0f)
     {
@@ -174,8 +179,9 @@ __device__ __forceinline__ float burley(float ndl, float ndv, float ldh, float r
 {
     const float fd90 = add(0.5f, mul(mul(mul(2.0f, rough), ldh), ldh));
     const float p1 = sub(1.0f, ndl), p2 = sub(1.0f, ndv);
-    const float a = add(1.0f, mul(sub(fd90, 1.0f), mul(mul(mul(mul(p1, p1), p1), p1), p1)));
-    const float b = add(1.0f, mul(sub(fd90, 1.0f), mul(mul(mul(mul(p2, p2), p2), p2), p2)));
+    const float p1s = mul(p1, p1), p2s = mul(p2, p2);      // pw5 = pw2 * pw2 * pw
+    const float a = add(1.0f, mul(sub(fd90, 1.0f), mul(mul(p1s, p1s), p1)));
+    const float b = add(1.0f, mul(sub(fd90, 1.0f), mul(mul(p2s, p2s), p2)));
     return mul(a, b);
 }
 __device__ __forceinline__ float unreal_ratio(const PtSurface& m, float avg)
@@ -639,9 +645,24 @@ __device__ __forceinline__ float2 rnd_s45(const PtLaunch& L, uint32_t key, uint3
 
 // ---------------------------------------------------------------------------
 // Camera rays: pinhole (CamerasDefault.hpp:94-140), Gaussian film filter
-// sampled with Box-Muller (filter / pdf = 1 per sample, Filters.h:195-233);
-// spectral paths also draw their 4 wavelengths here.
+// sampled per axis by inverting its CDF (GaussianFilter::Sample,
+// Filters.h:209-219; film weight Evaluate / pdf = 1 per sample); spectral
+// paths also draw their 4 wavelengths here.
 // ---------------------------------------------------------------------------
+// Common::SampleGaussian with mu = 0 (DistributionFunctions.h:686-705):
+// sqrt(2) sigma erfinv(2 xi - 1), clamped to 3.5 sigma where erfinv is
+// infinite.  MRay's CUDA backend takes Math::InvErrFunc from erfinvf.
+__device__ __forceinline__ float gaussian_offset(float xi, float sigma)
+{
+    const float e = erfinvf(sub(mul(2.0f, xi), 1.0f));
+    float x = mul(mul(1.4142135623730950488f, sigma), e);
+    if(isinf(e))
+    {
+        const float mm = mul(3.5f, sigma);
+        x = fminf(fmaxf(x, -mm), mm);
+    }
+    return x;
+}
 template<bool SPEC>
 __global__ void __launch_bounds__(kPtTPB)
 k_raygen(PtLaunch L, PtPaths P, uint32_t* aliveList, uint32_t* aliveCount)
@@ -652,10 +673,8 @@ k_raygen(PtLaunch L, PtPaths P, uint32_t* aliveList, uint32_t* aliveCount)
         const uint32_t pixel = slot_pixel(L, i);
         const uint32_t x = pixel % L.width, y = pixel / L.width;
         const uint32_t key = path_key(L.seed, pixel, slot_sample(L, i));
-        const float u1 = rnd_s(L, key, i, 0, 6), u2 = rnd_s(L, key, i, 0, 7);
-        const float r = mul(L.filterSigma, __fsqrt_rn(mul(-2.0f, logf(sub(1.0f, u1)))));
-        const float ang = mul(mul(2.0f, kPi), u2);
-        const float ox = mul(r, cosf(ang)), oy = mul(r, sinf(ang));
+        const float ox = gaussian_offset(rnd_s(L, key, i, 0, 6), L.filterSigma);
+        const float oy = gaussian_offset(rnd_s(L, key, i, 0, 7), L.filterSigma);
         const float dx = __fdiv_rn(L.cam.planeSize[0], (float)L.width);
         const float dy = __fdiv_rn(L.cam.planeSize[1], (float)L.height);
         const float sx = mul(add((float)x, add(ox, 0.5f)), dx);
@@ -960,11 +979,20 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         Chan tp = thr;
                         if(L.sampleMode == 2u && type == 1u)
                         {
-                            float ndl = -dot3(f3(lt.n), dir);
+                            // PdfSolidAngle(hit, ray.pos, ray.dir) * 1/N: the light point at
+                            // MRay's hit (a, b) = MetaHit of the world-space light triangle
+                            // (Triangle::SurfaceFromHit, PrimitiveDefaultTriangle.hpp:320-350)
+                            float ndl = dot3(f3(lt.n), make_float3(-dir.x, -dir.y, -dir.z));
                             ndl = (lt.n.w != 0.0f) ? fabsf(ndl) : fmaxf(0.0f, ndl);
-                            const float3 dd = make_float3(sub(org.x, pos.x), sub(org.y, pos.y), sub(org.z, pos.z));
+                            const float a = mh.x, b = mh.y, c = sub(sub(1.0f, a), b);
+                            const bool inside = a >= 0.0f && a <= 1.0f && b >= 0.0f && b <= 1.0f &&
+                                                c >= 0.0f && c <= 1.0f;
+                            const float3 lpos = make_float3(add(add(mul(lt.p0.x, a), mul(lt.p1.x, b)), mul(lt.p2.x, c)),
+                                                            add(add(mul(lt.p0.y, a), mul(lt.p1.y, b)), mul(lt.p2.y, c)),
+                                                            add(add(mul(lt.p0.z, a), mul(lt.p1.z, b)), mul(lt.p2.z, c)));
+                            const float3 dd = make_float3(sub(org.x, lpos.x), sub(org.y, lpos.y), sub(org.z, lpos.z));
                             float lpdf = (ndl == 0.0f) ? 0.0f : __fdiv_rn(__fdiv_rn(1.0f, lt.p0.w), ndl);
-                            lpdf = mul(lpdf, dot3(dd, dd));
+                            lpdf = inside ? mul(lpdf, dot3(dd, dd)) : 0.0f;
                             lpdf = mul(lpdf, invN);
                             tp = mis_weighted<NC>(tp, prevPdf, lpdf);
                         }
@@ -1076,9 +1104,10 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         if(mt == kMatUnreal) refl = unreal_eval<NC>(sf, alb, V, Ls, bpdf);
                         else
                         {
-                            const float cw = mul(fmaxf(Ls.z, 0.0f), kInvPi);
+                            // LambertMaterial::Evaluate: nDotL * albedo * InvPi
+                            const float ndl = fmaxf(Ls.z, 0.0f);
 #pragma unroll
-                            for(int k = 0; k < NC; k++) refl.v[k] = mul(alb.v[k], cw);
+                            for(int k = 0; k < NC; k++) refl.v[k] = mul(mul(ndl, alb.v[k]), kInvPi);
                             bpdf = mul(Ls.z, kInvPi);
                             bpdf = (bpdf <= 1.0e-5f) ? 0.0f : bpdf;
                         }
@@ -1145,7 +1174,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         {
                             const float ang = mul(mul(2.0f, kPi), x1), sr = __fsqrt_rn(x0);
                             Ll.x = mul(sr, cosf(ang)); Ll.y = mul(sr, sinf(ang));
-                            Ll.z = sqrt_max(sub(1.0f, add(mul(Ll.x, Ll.x), mul(Ll.y, Ll.y))));
+                            Ll.z = sqrt_max(sub(1.0f, len2_2(Ll.x, Ll.y)));   // SampleCosDirection
                             pd = mul(Ll.z, kInvPi);
                             H = normalize3(make_float3(add(Ll.x, V.x), add(Ll.y, V.y), add(Ll.z, V.z)));
                             const float vdh = fmaxf(0.0f, dot3(V, H));
@@ -1192,11 +1221,12 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         const float xi0 = u3.x, xi1 = u3.y;
                         const float ang = mul(mul(2.0f, kPi), xi1), sr = __fsqrt_rn(xi0);
                         Ll.x = mul(sr, cosf(ang)); Ll.y = mul(sr, sinf(ang));
-                        Ll.z = __fsqrt_rn(fmaxf(0.0f, sub(1.0f, add(mul(Ll.x, Ll.x), mul(Ll.y, Ll.y)))));
+                        Ll.z = sqrt_max(sub(1.0f, len2_2(Ll.x, Ll.y)));   // SampleCosDirection
                         bpdf = mul(Ll.z, kInvPi);
-                        const float cw = mul(fmaxf(Ll.z, 0.0f), kInvPi);
+                        // reflectance = albedo * nDotL * InvPi
+                        const float ndl = fmaxf(Ll.z, 0.0f);
 #pragma unroll
-                        for(int k = 0; k < NC; k++) refl.v[k] = mul(alb.v[k], cw);
+                        for(int k = 0; k < NC; k++) refl.v[k] = mul(mul(alb.v[k], ndl), kInvPi);
                     }
                     float3 wi = make_float3(add(add(mul(tng.x, Ll.x), mul(btg.x, Ll.y)), mul(nrm.x, Ll.z)),
                                             add(add(mul(tng.y, Ll.x), mul(btg.y, Ll.y)), mul(nrm.y, Ll.z)),

@@ -431,6 +431,69 @@ class Spectral:
         return out
 
 
+# ---- per-function entry points (records of oracle.ref_pt) ---------------
+
+def fx_material(kind, rec):
+    from . import ref_pt
+    rec = np.ascontiguousarray(rec, ref_pt.MAT_IN)
+    out = np.zeros(rec.shape[0], ref_pt.MAT_OUT)
+    lib().orc_fx_material(C.c_int(ref_pt.MATERIALS[kind]), _vp(rec), _vp(out), C.c_uint32(rec.shape[0]))
+    return out
+
+
+def _fx_rows(fn, inp, width_out, dtype=np.float32):
+    inp = np.ascontiguousarray(inp, dtype)
+    out = np.zeros((inp.shape[0], width_out), np.float32)
+    fn(_vp(inp), _vp(out), C.c_uint32(inp.shape[0]))
+    return out
+
+
+def fx_fresnel_dielectric(in3):
+    return _fx_rows(lib().orc_fx_fresnel_dielectric, in3, 1)[:, 0]
+
+
+def fx_vndf_sample(in6):
+    return _fx_rows(lib().orc_fx_vndf_sample, in6, 4)
+
+
+def fx_russian_roulette(in6):
+    return _fx_rows(lib().orc_fx_russian_roulette, in6, 5)
+
+
+def fx_gaussian_filter(in3):
+    return _fx_rows(lib().orc_fx_gaussian_filter, in3, 5)
+
+
+def fx_sample_waves(xi):
+    xi = np.ascontiguousarray(xi, np.uint32)
+    w = np.zeros((xi.shape[0], 4), np.float32)
+    p = np.zeros((xi.shape[0], 4), np.float32)
+    lib().orc_fx_sample_waves(_vp(xi), _vp(w), _vp(p), C.c_uint32(xi.shape[0]))
+    return w, p
+
+
+def fx_spherical_coords(in6):
+    return _fx_rows(lib().orc_fx_spherical_coords, in6, 7)
+
+
+def fx_tri_light(rec):
+    from . import ref_pt
+    rec = np.ascontiguousarray(rec, ref_pt.LIGHT_IN)
+    out = np.zeros(rec.shape[0], ref_pt.LIGHT_OUT)
+    lib().orc_fx_tri_light(_vp(rec), _vp(out), C.c_uint32(rec.shape[0]))
+    return out
+
+
+def fx_camera(cam13, res, pix, off4):
+    cam13 = np.ascontiguousarray(cam13, np.float32)
+    res = np.ascontiguousarray(res, np.uint32)
+    pix = np.ascontiguousarray(pix, np.uint32)
+    off4 = np.ascontiguousarray(off4, np.float32)
+    out = np.zeros((pix.shape[0], 6), np.float32)
+    lib().orc_fx_camera(_vp(cam13), _vp(res), _vp(pix), _vp(off4), _vp(out), C.c_uint32(pix.shape[0]))
+    return out
+
+
 class PtScene:
     """The CPU path-tracer oracle over a list of surfaces (dicts with pos,
     idx, m34, kind, albedo / radiance), keyed like mray_gb300.pt.PathTracer:

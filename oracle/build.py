@@ -5,8 +5,8 @@
 - ``build_ref()`` compiles ``ref_core_driver.cpp`` against the MRay source tree
   (its own ``Source/Core`` headers, unmodified) into
   ``oracle/_ref/libmray_ref_core.so``.  It runs only where the MRay source tree
-  is present (``MRAY_REFERENCE_SRC`` or the default checkout path); elsewhere it
-  is a no-op and tests that need it skip.
+  is present (``MRAY_REFERENCE_SRC``, or a checkout named ``reference`` beside
+  the repository); elsewhere it is a no-op and tests that need it skip.
 
 Both are compiled with ``-ffp-contract=off`` so that only the explicit fma()
 calls of the restated algorithms are fused, matching the reference host build
@@ -26,7 +26,10 @@ ORACLE_SOURCES = ["mrg_oracle.c", "pt_oracle.c", "zsobol_oracle.c"]
 
 
 def reference_source_dir():
-    d = os.environ.get("MRAY_REFERENCE_SRC", "/root/reference/Source")
+    """The MRay ``Source`` directory: ``MRAY_REFERENCE_SRC`` when set, else a
+    checkout named ``reference`` beside this repository's root."""
+    d = os.environ.get("MRAY_REFERENCE_SRC") or os.path.join(os.path.dirname(HERE), os.pardir, "reference", "Source")
+    d = os.path.normpath(d)
     return d if os.path.isdir(os.path.join(d, "Core")) else None
 
 
@@ -116,6 +119,108 @@ def build_ref_spectra(force=False, verbose=False):
     return exe, lib
 
 
+def ref_lut(res=64):
+    """MR_SPECTRA LUT for Rec.709 at resolution `res`, written by MRay's own
+    SpectraLUTGen into ``oracle/_ref/lut<res>/REC_709.mrspectra`` (about
+    9 MB at 64, the converter's compile-time resolution; not committed).
+    None without the MRay tree."""
+    tools = build_ref_spectra()
+    if tools is None:
+        return None
+    out_dir = os.path.join(REF_DIR, "lut%d" % res)
+    path = os.path.join(out_dir, "REC_709.mrspectra")
+    if os.path.exists(path):
+        return path
+    # the generator fails when it has to create the folder itself
+    # (SpectraLUTGen/main.cpp:570 treats "created" as an error)
+    os.makedirs(out_dir, exist_ok=True)
+    subprocess.run([tools[0], str(res), "REC_709", out_dir], check=True, capture_output=True)
+    return path
+
+
+# g++ 13 has no __type_pack_element builtin, and MRay's fallback
+# (Core/TypePack.h:66-75) names a PackElementDetail::TypePackElementT that the
+# tree does not define.  This header, force-included ahead of every source,
+# defines it; no file of the MRay tree is copied or changed.
+_PACK_ELEMENT_PRELUDE = """#pragma once
+#include <cstddef>
+namespace PackElementDetail
+{
+template<std::size_t I, class T0, class... Ts>
+struct TypePackElementT { using Type = typename TypePackElementT<I - 1, Ts...>::Type; };
+template<class T0, class... Ts>
+struct TypePackElementT<0, T0, Ts...> { using Type = T0; };
+}
+"""
+
+REF_PT_LIB = os.path.join(REF_DIR, "libmray_ref_pt.so")
+
+
+def _fmt_include():
+    """fmt headers for MRay's logging (the reference pins fmt v10, header-only
+    use); torch ships a copy in its include directory."""
+    try:
+        import torch
+        d = os.path.join(os.path.dirname(torch.__file__), "include")
+    except ImportError:
+        return None
+    return d if os.path.exists(os.path.join(d, "fmt", "format.h")) else None
+
+
+def build_ref_pt(force=False, verbose=False):
+    """MRay's host-backend path-tracer building blocks (materials, lights,
+    light sampler, camera, film filter, distributions, spectral converter)
+    compiled from the MRay tree with the driver ``ref_pt_driver.cpp`` into
+    ``oracle/_ref/libmray_ref_pt.so``.  Returns None without the MRay tree or
+    the fmt headers."""
+    src_dir = reference_source_dir()
+    fmt = _fmt_include()
+    if src_dir is None or fmt is None:
+        return None
+    gen = _mray_cmake_header(os.path.join(REF_DIR, "gen"))
+    prelude = os.path.join(gen, "pack_element_prelude.h")
+    if not os.path.exists(prelude) or open(prelude).read() != _PACK_ELEMENT_PRELUDE:
+        with open(prelude, "w") as f:
+            f.write(_PACK_ELEMENT_PRELUDE)
+    drv = os.path.join(HERE, "ref_pt_driver.cpp")
+    if not force and _newer(REF_PT_LIB, [drv, __file__]):
+        return REF_PT_LIB
+    tmp = REF_PT_LIB + ".tmp%d" % os.getpid()
+    obj = tmp + ".o"
+    # MRAY_HOST_ARCH_BASIC (no automatic FMA contraction) as in the
+    # reference's host build; FTZ/DAZ is not set (no intermediate here is
+    # subnormal)
+    # NDEBUG as in MRay's release builds: the reference's asserts are off
+    flags = ["g++", "-std=c++20", "-O2", "-fPIC", "-c", "-ffp-contract=off", "-Wno-interference-size", "-DNDEBUG",
+             "-DMRAY_GCC", "-DMRAY_LINUX", "-DMRAY_GPU_BACKEND_CPU", "-DFMT_HEADER_ONLY",
+             "-include", prelude, "-I", gen, "-I", src_dir, "-isystem", fmt]
+    color_obj = tmp + ".color.o"
+    for src, o in ((drv, obj), (os.path.join(src_dir, "Core", "ColorFunctions.cpp"), color_obj)):
+        cmd = flags + ["-o", o, src]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.run(cmd, check=True)
+    # The headers declare MRay's group classes (virtual bookkeeping whose
+    # definitions live in the Device layer).  The driver never reaches them,
+    # so their references are made weak instead of linking that layer: a
+    # first link lists the unresolved, unversioned symbols, objcopy weakens
+    # exactly those, and the second link yields a loadable library.
+    subprocess.run(["g++", "-shared", "-o", tmp, obj, color_obj], check=True)
+    nm = subprocess.run(["nm", "-D", "--undefined-only", tmp], check=True, capture_output=True, text=True)
+    weak = [ln.split()[-1] for ln in nm.stdout.splitlines()
+            if ln.strip() and "@" not in ln and not ln.split()[-1].startswith(("_ITM", "__gmon", "_Jv"))]
+    lst = tmp + ".weak"
+    with open(lst, "w") as f:
+        f.write("\n".join(weak) + "\n")
+    subprocess.run(["objcopy", "--weaken-symbols=" + lst, obj], check=True)
+    subprocess.run(["g++", "-shared", "-o", tmp, obj, color_obj], check=True)
+    for p in (obj, color_obj, lst):
+        os.remove(p)
+    os.replace(tmp, REF_PT_LIB)
+    return REF_PT_LIB
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True, verbose=True))
     print(build_ref(force=True, verbose=True))
+    print(build_ref_pt(force=True, verbose=True))

@@ -88,14 +88,20 @@ static float urnd(const smp_ctx* c, uint32_t bounce, uint32_t k)
     return f < prev1 ? f : prev1;
 }
 
-static inline float dot3f(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+/* Math::Dot (Source/Core/Math.h:1585-1596): r = 0; r = fma(a_i, b_i, r). */
+static inline float dot3f(const float a[3], const float b[3])
+{
+    return fmaf(a[2], b[2], fmaf(a[1], b[1], fmaf(a[0], b[0], 0.0f)));
+}
+/* Math::Cross (Math.h:1627-1633): each component one fma. */
 static inline void cross3f(const float a[3], const float b[3], float o[3])
 {
-    float x = a[1] * b[2] - a[2] * b[1];
-    float y = a[2] * b[0] - a[0] * b[2];
-    float z = a[0] * b[1] - a[1] * b[0];
+    float x = fmaf(a[1], b[2], -(a[2] * b[1]));
+    float y = fmaf(a[2], b[0], -(a[0] * b[2]));
+    float z = fmaf(a[0], b[1], -(a[1] * b[0]));
     o[0] = x; o[1] = y; o[2] = z;
 }
+/* Math::Normalize (Math.h:1618-1624): v * (1 / Length(v)). */
 static inline void normalize3f(float v[3])
 {
     float inv = 1.0f / sqrtf(dot3f(v, v));
@@ -166,7 +172,7 @@ static void vndf_sample(const float V[3], float a, float xi0, float xi1, float H
 {
     float vh[3] = { a * V[0], a * V[1], V[2] };
     normalize3f(vh);
-    float len2 = vh[0] * vh[0] + vh[1] * vh[1];
+    float len2 = fmaf(vh[1], vh[1], fmaf(vh[0], vh[0], 0.0f));   /* LengthSqr(Vector2(VHemi)) */
     float T1[3];
     if(len2 > 0.0f)
     {
@@ -195,8 +201,9 @@ static float burley(float ndl, float ndv, float ldh, float rough)
 {
     float fd90 = 0.5f + 2.0f * rough * ldh * ldh;
     float p1 = 1.0f - ndl, p2 = 1.0f - ndv;
-    float a = 1.0f + (fd90 - 1.0f) * (p1 * p1 * p1 * p1 * p1);
-    float b = 1.0f + (fd90 - 1.0f) * (p2 * p2 * p2 * p2 * p2);
+    float p1s = p1 * p1, p2s = p2 * p2;
+    float a = 1.0f + (fd90 - 1.0f) * (p1s * p1s * p1);
+    float b = 1.0f + (fd90 - 1.0f) * (p2s * p2s * p2);
     return a * b;
 }
 /* UnrealMaterial::MISRatio (MaterialsDefault.hpp:470-478) */
@@ -272,6 +279,137 @@ static float fresnel_dielectric(float cosF, float etaF, float etaB)
     float per = (etaF * cosF - etaB * cosB) / (etaF * cosF + etaB * cosB);
     per = per * per;
     return (par + per) * 0.5f;
+}
+
+/* Common::SampleCosDirection (DistributionFunctions.h:847-870): the
+ * tangent-frame direction and its pdf. */
+static inline void cos_sample(float xi0, float xi1, float L[3], float* pdf)
+{
+    float ang = 2.0f * PI_F * xi1, sr = sqrtf(xi0);
+    L[0] = sr * cosf(ang); L[1] = sr * sinf(ang);
+    L[2] = sqrt_max(1.0f - fmaf(L[1], L[1], fmaf(L[0], L[0], 0.0f)));
+    *pdf = L[2] * INV_PI_F;
+}
+
+/* BxDF sample in the tangent frame (z = shading normal), the SampleBxDF of
+ * each material (MaterialsDefault.hpp: Lambert 29-62, Reflect 150-170,
+ * Refract 263-305, Unreal 535-628).  xi0..xi2 are the dispenser's numbers
+ * 0..2.  L is the sampled direction in the tangent frame (Reflect's is
+ * normalised, as MRay's is); *passed is set for a refraction.  Refract's
+ * one-ulp nudge of the position along the normal is the caller's. */
+static void bxdf_sample(const orc_pt_surface* sf, const float* alb, int nc, int backSide, const float V[3],
+                        float xi0, float xi1, float xi2, float L[3], float refl[4], float* pdfOut, int* passed)
+{
+    refl[0] = refl[1] = refl[2] = refl[3] = 0.0f;
+    *passed = 0;
+    if(sf->matType == ORC_MAT_REFLECT)
+    {
+        float d2 = 2.0f * V[2];
+        L[0] = -V[0]; L[1] = -V[1]; L[2] = d2 - V[2];
+        normalize3f(L);
+        *pdfOut = 1.0f;
+        refl[0] = refl[1] = refl[2] = refl[3] = 1.0f;
+    }
+    else if(sf->matType == ORC_MAT_REFRACT)
+    {
+        float fromEta = sf->iorFront, toEta = sf->iorBack;
+        if(backSide) { float t = fromEta; fromEta = toEta; toEta = t; }
+        float cosT = fabsf(V[2]);
+        float f = fresnel_dielectric(cosT, fromEta, toEta);
+        int doRefl = xi0 < f;
+        if(doRefl) { L[0] = -V[0]; L[1] = -V[1]; L[2] = 2.0f * V[2] - V[2]; }
+        else
+        {
+            float eta = fromEta / toEta;
+            float cosIn = V[2];
+            float sin2 = fmaxf(0.0f, 1.0f - cosIn * cosIn);
+            float sinOut2 = eta * eta * sin2;
+            float cosOut = sqrt_max(1.0f - sinOut2);
+            for(int k = 0; k < 2; k++) L[k] = eta * -V[k];
+            L[2] = eta * -V[2] + (eta * cosIn - cosOut);
+        }
+        float bpdf = doRefl ? f : (1.0f - f);
+        *pdfOut = bpdf;
+        refl[0] = refl[1] = refl[2] = refl[3] = bpdf;
+        *passed = !doRefl;
+    }
+    else if(sf->matType == ORC_MAT_UNREAL)
+    {
+        float alpha = sf->roughness * sf->roughness;
+        float ratio = unreal_mis_ratio(sf, avg_albedo(alb, nc));
+        float sXi = xi0, x0 = xi1, x1 = xi2;
+        float H[3], pd, ps;
+        if(sXi < ratio)
+        {
+            cos_sample(x0, x1, L, &pd);
+            H[0] = L[0] + V[0]; H[1] = L[1] + V[1]; H[2] = L[2] + V[2];
+            normalize3f(H);
+            float vdh = fmaxf(0.0f, dot3f(V, H));
+            ps = vndf_pdf(V, H, alpha);
+            ps = (vdh == 0.0f) ? 0.0f : ps / (4.0f * vdh);
+        }
+        else
+        {
+            vndf_sample(V, alpha, x0, x1, H);
+            float dv = 2.0f * dot3f(V, H);
+            for(int k = 0; k < 3; k++) L[k] = dv * H[k] - V[k];
+            float vdh = fmaxf(0.0f, dot3f(V, H));
+            ps = vndf_pdf(V, H, alpha);
+            ps = (vdh == 0.0f) ? 0.0f : ps / (4.0f * vdh);
+            pd = L[2] * INV_PI_F;
+            pd = (pd <= 1.0e-5f) ? 0.0f : pd;
+        }
+        float vdh = fmaxf(0.0f, dot3f(V, H));
+        float ldh = fmaxf(0.0f, dot3f(L, H));
+        float ndh = fmaxf(0.0f, H[2]);
+        float ndv = fmaxf(0.0f, V[2]);
+        float D = d_ggx(ndh, alpha);
+        float G = g_correlated(V, L, alpha);
+        G = (ldh == 0.0f) ? 0.0f : G;
+        G = (vdh == 0.0f) ? 0.0f : G;
+        float f0[4], F[4];
+        for(int k = 0; k < nc; k++) f0[k] = (sf->specular * 0.08f) * (1.0f - sf->metallic) + alb[k] * sf->metallic;
+        f_schlick(vdh, f0, F, nc);
+        float spec[4];
+        for(int k = 0; k < nc; k++) spec[k] = (ndv == 0.0f) ? 0.0f : D * F[k] * G * 0.25f / ndv;
+        if(isinf(D) || isnan(D))
+        {
+            float gs = g_single(V, alpha);
+            for(int k = 0; k < nc; k++) spec[k] = G * F[k] / gs;
+            ps = 1.0f;
+        }
+        float ndl = fmaxf(0.0f, L[2]);
+        float corr = burley(ndl, ndv, ldh, sf->roughness);
+        for(int k = 0; k < nc; k++)
+            refl[k] = ndl * ((1.0f - sf->metallic) * alb[k]) * INV_PI_F * corr + spec[k];
+        *pdfOut = pd * ratio + ps * (1.0f - ratio);
+    }
+    else
+    {
+        /* reflectance = albedo * nDotL * InvPi, nDotL = max(wI.z, 0) */
+        cos_sample(xi0, xi1, L, pdfOut);
+        float ndl = fmaxf(L[2], 0.0f);
+        for(int k = 0; k < nc; k++) refl[k] = (alb[k] * ndl) * INV_PI_F;
+    }
+}
+
+/* BxDF evaluation and pdf in the tangent frame for the NEE direction L
+ * (Lambert Evaluate / Pdf, MaterialsDefault.hpp:64-86; Unreal 630-720).
+ * Only non-specular materials are evaluated (specular ones take no NEE). */
+static void bxdf_eval(const orc_pt_surface* sf, const float* alb, int nc, const float V[3], const float L[3],
+                      float refl[4], float* pdfOut)
+{
+    refl[0] = refl[1] = refl[2] = refl[3] = 0.0f;
+    if(sf->matType == ORC_MAT_UNREAL)
+        unreal_eval(sf, alb, nc, V, L, refl, pdfOut);
+    else
+    {
+        /* Evaluate: nDotL * albedo * InvPi */
+        float ndl = fmaxf(L[2], 0.0f);
+        for(int k = 0; k < nc; k++) refl[k] = (ndl * alb[k]) * INV_PI_F;
+        float bpdf = L[2] * INV_PI_F;
+        *pdfOut = (bpdf <= 1.0e-5f) ? 0.0f : bpdf;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -747,6 +885,142 @@ static void surface_of(const orc_pt_surface* sf, const float* tri9 /* v0 v1 v2 l
     normalize3f(n);
 }
 
+/* Math::InvErrFunc, host branch (Source/Core/Math.h:787-833): the
+ * single-precision inverse error function of M. Giles, "Approximating the
+ * erfinv function" (GPU Computing Gems, Jade Edition, 2011), evaluated with
+ * fma as MRay writes it.  (MRay's CUDA backend calls erfinvf instead.) */
+static float inv_erf(float x)
+{
+    float t = logf(fmaf(x, 0.0f - x, 1.0f));
+    float p;
+    if(fabsf(t) > 6.125f)
+    {
+        p = 3.03697567e-10f;
+        p = fmaf(p, t, 2.93243101e-8f);
+        p = fmaf(p, t, 1.22150334e-6f);
+        p = fmaf(p, t, 2.84108955e-5f);
+        p = fmaf(p, t, 3.93552968e-4f);
+        p = fmaf(p, t, 3.02698812e-3f);
+        p = fmaf(p, t, 4.83185798e-3f);
+        p = fmaf(p, t, -2.64646143e-1f);
+        p = fmaf(p, t, 8.40016484e-1f);
+    }
+    else
+    {
+        p = 5.438778320e-9f;
+        p = fmaf(p, t, 1.43285448e-7f);
+        p = fmaf(p, t, 1.22774793e-6f);
+        p = fmaf(p, t, 1.12963626e-7f);
+        p = fmaf(p, t, -5.61530760e-5f);
+        p = fmaf(p, t, -1.47697632e-4f);
+        p = fmaf(p, t, 2.31468678e-3f);
+        p = fmaf(p, t, 1.15392581e-2f);
+        p = fmaf(p, t, -2.32015476e-1f);
+        p = fmaf(p, t, 8.86226892e-1f);
+    }
+    return x * p;
+}
+
+/* Math::Gaussian (Math.h:1031-1042) */
+static float gaussian(float x, float sigma)
+{
+    const float invSqrt2Pi = (1.0f / 1.4142135623730950488f) * (1.0f / 1.772453850905516027298f);
+    float sigmaInv = 1.0f / sigma;
+    float r = invSqrt2Pi * sigmaInv;
+    float pw = (x - 0.0f) * sigmaInv;
+    return r * expf(-0.5f * pw * pw);
+}
+
+/* Common::SampleGaussian with mu = 0 (DistributionFunctions.h:686-705):
+ * inverse-CDF sample, clamped to 3.5 sigma where the inverse error function
+ * runs off to infinity. */
+static float sample_gaussian(float xi, float sigma)
+{
+    float x = 1.4142135623730950488f * sigma;
+    float e = inv_erf(2.0f * xi - 1.0f);
+    x = x * e + 0.0f;
+    if(isinf(e))
+    {
+        float mm = 3.5f * sigma;
+        x = x < -mm ? -mm : (x > mm ? mm : x);
+    }
+    return x;
+}
+
+/* GaussianFilter::Sample (Filters.h:195-219): per-axis offsets in pixels,
+ * sigma = radius * 0.285714.  The film weight Evaluate / pdf is the ratio of
+ * equal products, so 1. */
+static void filter_sample(float radius, float xi0, float xi1, float* ox, float* oy)
+{
+    float sigma = radius * 0.285714f;
+    *ox = sample_gaussian(xi0, sigma);
+    *oy = sample_gaussian(xi1, sigma);
+}
+
+/* LightPrim<Triangle>::SampleSolidAngle (LightsDefault.hpp:22-45) with the
+ * triangle's area sampling (Osada et al., PrimitiveDefaultTriangle.hpp:48-80)
+ * towards the shaded point pos, and EmitViaSurfacePoint's side test: lp,
+ * the solid-angle pdf and the emitted RGB (zero from a one-sided light's
+ * back). */
+static void light_tri_sample(const orc_pt_light_tri* L, float xi0, float xi1, const float pos[3], float lp[3],
+                             float* pdf, float emis[3])
+{
+    float r1 = sqrtf(xi0), r2 = xi1;
+    float a = 1.0f - r1, b = (1.0f - r2) * r1, c = r1 * r2;
+    for(int k = 0; k < 3; k++) lp[k] = L->p0[k] * a + L->p1[k] * b + L->p2[k] * c;
+    float sd[3] = { pos[0] - lp[0], pos[1] - lp[1], pos[2] - lp[2] };
+    float distSq = dot3f(sd, sd);
+    normalize3f(sd);
+    float ndl = dot3f(L->n, sd);
+    ndl = L->twoSided ? fabsf(ndl) : fmaxf(0.0f, ndl);
+    float ppdf = (ndl == 0.0f) ? 0.0f : (1.0f / L->area) / ndl;
+    *pdf = ppdf * distSq;
+    emis[0] = emis[1] = emis[2] = 0.0f;
+    if(L->twoSided || dot3f(L->n, sd) > 0.0f)
+        for(int k = 0; k < 3; k++) emis[k] = L->radiance[k];
+}
+
+/* LightPrim<Triangle>::PdfSolidAngle (LightsDefault.hpp:47-66): the light
+ * hit at barycentrics (a, b) of its world-space vertices
+ * (Triangle::SurfaceFromHit, PrimitiveDefaultTriangle.hpp:320-350), seen
+ * from org along dir. */
+static float light_tri_pdf(const orc_pt_light_tri* L, float a, float b, const float org[3], const float dir[3])
+{
+    const float md[3] = { -dir[0], -dir[1], -dir[2] };
+    float ndl = dot3f(L->n, md);
+    ndl = L->twoSided ? fabsf(ndl) : fmaxf(0.0f, ndl);
+    float c = 1.0f - a - b;
+    /* SurfaceFromHit / PdfSurface: no surface outside the triangle */
+    if(a < 0.0f || a > 1.0f || b < 0.0f || b > 1.0f || c < 0.0f || c > 1.0f) return 0.0f;
+    float pos[3];
+    for(int k = 0; k < 3; k++) pos[k] = L->p0[k] * a + L->p1[k] * b + L->p2[k] * c;
+    float dd[3] = { org[0] - pos[0], org[1] - pos[1], org[2] - pos[2] };
+    float lpdf = (ndl == 0.0f) ? 0.0f : (1.0f / L->area) / ndl;
+    return lpdf * dot3f(dd, dd);
+}
+
+/* EmitViaHit's side test (LightsDefault.hpp:125-145): a one-sided light
+ * emits towards wo only when it faces it. */
+static int light_tri_emits(const orc_pt_light_tri* L, const float wo[3])
+{
+    return L->twoSided ? 1 : (dot3f(L->n, wo) > 0.0f);
+}
+
+/* CameraPinhole::EvaluateRay (CamerasDefault.hpp:94-135) for pixel (x, y)
+ * and a film-filter offset (ox, oy) in pixels. */
+static void camera_ray(const orc_pt_params* P, uint32_t x, uint32_t y, float ox, float oy, float dir[3], float org[3])
+{
+    float dx = P->planeSize[0] / (float)P->width, dy = P->planeSize[1] / (float)P->height;
+    float sx = ((float)x + (ox + 0.5f)) * dx, sy = ((float)y + (oy + 0.5f)) * dy;
+    for(int k = 0; k < 3; k++)
+    {
+        float sp = P->camBottomLeft[k] + sx * P->camRight[k] + sy * P->camUp[k];
+        dir[k] = sp - P->camPos[k];
+        org[k] = P->camPos[k];
+    }
+    normalize3f(dir);
+}
+
 /* adj: NULL for a primal trace; else {primal radiance[3], delta / spp [3]}
  * and the worker's gradient buffer. */
 typedef struct { float tot[3]; float d[3]; double* grad; double* gradE; } adj_ctx;
@@ -784,22 +1058,11 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
                    P->samplerMaxSpp ? P->samplerMaxSpp : P->sampleStart + P->spp, J->zsResBits };
     outRad[0] = outRad[1] = outRad[2] = 0.0f;
 
-    /* camera ray: Gaussian offset by Box-Muller, weight filter/pdf = 1 */
-    float sigma = P->filterRadius * 0.285714f;
-    float u1 = urnd(&SC, 0, 6), u2 = urnd(&SC, 0, 7);
-    float rr = sigma * sqrtf(-2.0f * logf(1.0f - u1));
-    float ox = rr * cosf(2.0f * PI_F * u2), oy = rr * sinf(2.0f * PI_F * u2);
-    float dx = P->planeSize[0] / (float)P->width, dy = P->planeSize[1] / (float)P->height;
-    /* (sampleId + (offset + 0.5)) * delta, CamerasDefault.hpp:102-108 */
-    float sx = ((float)x + (ox + 0.5f)) * dx, sy = ((float)y + (oy + 0.5f)) * dy;
-    float sp[3], dir[3], org[3];
-    for(int k = 0; k < 3; k++)
-    {
-        sp[k] = P->camBottomLeft[k] + sx * P->camRight[k] + sy * P->camUp[k];
-        dir[k] = sp[k] - P->camPos[k];
-        org[k] = P->camPos[k];
-    }
-    normalize3f(dir);
+    /* camera ray: Gaussian film-filter offset (weight Evaluate / pdf = 1) */
+    float ox, oy;
+    filter_sample(P->filterRadius, urnd(&SC, 0, 6), urnd(&SC, 0, 7), &ox, &oy);
+    float dir[3], org[3];
+    camera_ray(P, x, y, ox, oy, dir, org);
     float tmin = P->nearT, tmax = P->farT;
 
     float thr[4] = { 1.0f, 1.0f, 1.0f, 1.0f };
@@ -857,13 +1120,8 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             if(P->sampleMode == ORC_PT_NEE_MIS && type == 1)
             {
                 const orc_pt_light_tri* L = &J->lights[sf->lightBase + localPrim];
-                /* PdfSolidAngle(hit, ray.pos, ray.dir) * 1/N */
-                float ndl = -(L->n[0] * dir[0] + L->n[1] * dir[1] + L->n[2] * dir[2]);
-                ndl = L->twoSided ? fabsf(ndl) : fmaxf(0.0f, ndl);
-                float dd[3] = { org[0] - pos[0], org[1] - pos[1], org[2] - pos[2] };
-                float lpdf = (ndl == 0.0f) ? 0.0f : (1.0f / L->area) / ndl;
-                lpdf *= dot3f(dd, dd);
-                lpdf *= invN;
+                /* PdfSolidAngle(hit, ray.pos, ray.dir) * 1/N; the hit is MRay's (a, b) = MetaHit */
+                float lpdf = light_tri_pdf(L, mh.bary[0], mh.bary[1], org, dir) * invN;
                 float misPdf = prevPdf + lpdf;
                 for(int k = 0; k < nc; k++) tp[k] *= prevPdf;
                 if(misPdf == 0.0f) { tp[0] = tp[1] = tp[2] = tp[3] = 0.0f; }
@@ -871,8 +1129,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             }
             const orc_pt_light_tri* L = &J->lights[sf->lightBase + localPrim];
             float wo[3] = { -dir[0], -dir[1], -dir[2] };
-            float ndl = dot3f(L->n, wo);
-            int emits = L->twoSided ? 1 : (ndl > 0.0f);
+            int emits = light_tri_emits(L, wo);
             float lr[4] = { L->radiance[0], L->radiance[1], L->radiance[2], 0.0f };
             if(S) orc_spec_convert_radiance(S, L->radiance, waves, lr);
             if(emits && depth + 1u <= P->maxDepth)
@@ -945,22 +1202,11 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             else
             {
                 const orc_pt_light_tri* L = &J->lights[li];
-                float r1 = sqrtf(urnd(&SC, depth, 4)), r2 = urnd(&SC, depth, 5);
-                float a = 1.0f - r1, b = (1.0f - r2) * r1, c = r1 * r2;
-                for(int k = 0; k < 3; k++) lp[k] = L->p0[k] * a + L->p1[k] * b + L->p2[k] * c;
-                float sd[3] = { pos[0] - lp[0], pos[1] - lp[1], pos[2] - lp[2] };
-                float distSq = dot3f(sd, sd);
-                normalize3f(sd);
-                float ndl = dot3f(L->n, sd);
-                ndl = L->twoSided ? fabsf(ndl) : fmaxf(0.0f, ndl);
-                float ppdf = (ndl == 0.0f) ? 0.0f : (1.0f / L->area) / ndl;
-                ppdf *= distSq;
+                float ppdf;
+                light_tri_sample(L, urnd(&SC, depth, 4), urnd(&SC, depth, 5), pos, lp, &ppdf, emis);
                 lightPdf = invN * ppdf;
-                if(L->twoSided || dot3f(L->n, sd) > 0.0f)
-                {
-                    for(int k = 0; k < 3; k++) emis[k] = L->radiance[k];
-                    if(S) orc_spec_convert_radiance(S, L->radiance, waves, emis);
-                }
+                if(S && (emis[0] != 0.0f || emis[1] != 0.0f || emis[2] != 0.0f))
+                    orc_spec_convert_radiance(S, L->radiance, waves, emis);
             }
             float sdir[3] = { lp[0] - pos[0], lp[1] - pos[1], lp[2] - pos[2] };
             normalize3f(sdir);
@@ -971,15 +1217,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             float length = sqrtf(dot3f(seg, seg));
             float refl[4] = { 0, 0, 0, 0 }, bpdf;
             const float Ls[3] = { dot3f(sdir, tng), dot3f(sdir, btg), dot3f(sdir, nrm) };
-            if(sf->matType == ORC_MAT_UNREAL)
-                unreal_eval(sf, alb, nc, V, Ls, refl, &bpdf);
-            else
-            {
-                float cw = fmaxf(Ls[2], 0.0f) * INV_PI_F;
-                for(int k = 0; k < nc; k++) refl[k] = alb[k] * cw;
-                bpdf = Ls[2] * INV_PI_F;
-                bpdf = (bpdf <= 1.0e-5f) ? 0.0f : bpdf;
-            }
+            bxdf_eval(sf, alb, nc, V, Ls, refl, &bpdf);
             float pdf = (P->sampleMode == ORC_PT_NEE_MIS) ? (bpdf + lightPdf) : lightPdf;
             float srad[4] = { 0, 0, 0, 0 };
             for(int k = 0; k < nc; k++) srad[k] = thr[k] * refl[k] * emis[k];
@@ -1002,104 +1240,12 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
         }
 
         /* ---- BxDF sample (WorkFunction) ---- */
-        float Ll[3], refl[4] = { 0, 0, 0, 0 }, bpdf;
+        float Ll[3], refl[4], bpdf;
         int passed = 0;
         float presample[3] = { pos[0], pos[1], pos[2] };    /* ray origin before the final nudge */
-        if(sf->matType == ORC_MAT_REFLECT)
-        {
-            float d2 = 2.0f * V[2];
-            Ll[0] = -V[0]; Ll[1] = -V[1]; Ll[2] = d2 - V[2];
-            normalize3f(Ll);
-            bpdf = 1.0f;
-            refl[0] = refl[1] = refl[2] = refl[3] = 1.0f;
-        }
-        else if(sf->matType == ORC_MAT_REFRACT)
-        {
-            float fromEta = sf->iorFront, toEta = sf->iorBack;
-            if(backSide) { float t = fromEta; fromEta = toEta; toEta = t; }
-            float cosT = fabsf(V[2]);
-            float f = fresnel_dielectric(cosT, fromEta, toEta);
-            int doRefl = urnd(&SC, depth, 0) < f;
-            if(doRefl) { Ll[0] = -V[0]; Ll[1] = -V[1]; Ll[2] = 2.0f * V[2] - V[2]; }
-            else
-            {
-                float eta = fromEta / toEta;
-                float cosIn = V[2];
-                float sin2 = fmaxf(0.0f, 1.0f - cosIn * cosIn);
-                float sinOut2 = eta * eta * sin2;
-                float cosOut = sqrt_max(1.0f - sinOut2);
-                for(int k = 0; k < 2; k++) Ll[k] = eta * -V[k];
-                Ll[2] = eta * -V[2] + (eta * cosIn - cosOut);
-            }
-            bpdf = doRefl ? f : (1.0f - f);
-            refl[0] = refl[1] = refl[2] = refl[3] = bpdf;
-            passed = !doRefl;
-            orc_nudge(pos, nrm, presample);                 /* SampleBxDF nudges along n first */
-        }
-        else if(sf->matType == ORC_MAT_UNREAL)
-        {
-            float alpha = sf->roughness * sf->roughness;
-            float ratio = unreal_mis_ratio(sf, avg_albedo(alb, nc));
-            float sXi = urnd(&SC, depth, 0), x0 = urnd(&SC, depth, 1), x1 = urnd(&SC, depth, 2);
-            float H[3], pd, ps;
-            if(sXi < ratio)
-            {
-                float ang = 2.0f * PI_F * x1, sr = sqrtf(x0);
-                Ll[0] = sr * cosf(ang); Ll[1] = sr * sinf(ang);
-                Ll[2] = sqrt_max(1.0f - (Ll[0] * Ll[0] + Ll[1] * Ll[1]));
-                pd = Ll[2] * INV_PI_F;
-                H[0] = Ll[0] + V[0]; H[1] = Ll[1] + V[1]; H[2] = Ll[2] + V[2];
-                normalize3f(H);
-                float vdh = fmaxf(0.0f, dot3f(V, H));
-                ps = vndf_pdf(V, H, alpha);
-                ps = (vdh == 0.0f) ? 0.0f : ps / (4.0f * vdh);
-            }
-            else
-            {
-                vndf_sample(V, alpha, x0, x1, H);
-                float dv = 2.0f * dot3f(V, H);
-                for(int k = 0; k < 3; k++) Ll[k] = dv * H[k] - V[k];
-                float vdh = fmaxf(0.0f, dot3f(V, H));
-                ps = vndf_pdf(V, H, alpha);
-                ps = (vdh == 0.0f) ? 0.0f : ps / (4.0f * vdh);
-                pd = Ll[2] * INV_PI_F;
-                pd = (pd <= 1.0e-5f) ? 0.0f : pd;
-            }
-            float vdh = fmaxf(0.0f, dot3f(V, H));
-            float ldh = fmaxf(0.0f, dot3f(Ll, H));
-            float ndh = fmaxf(0.0f, H[2]);
-            float ndv = fmaxf(0.0f, V[2]);
-            float D = d_ggx(ndh, alpha);
-            float G = g_correlated(V, Ll, alpha);
-            G = (ldh == 0.0f) ? 0.0f : G;
-            G = (vdh == 0.0f) ? 0.0f : G;
-            float f0[4], F[4];
-            for(int k = 0; k < nc; k++) f0[k] = (sf->specular * 0.08f) * (1.0f - sf->metallic) + alb[k] * sf->metallic;
-            f_schlick(vdh, f0, F, nc);
-            float spec[4];
-            for(int k = 0; k < nc; k++) spec[k] = (ndv == 0.0f) ? 0.0f : D * F[k] * G * 0.25f / ndv;
-            if(isinf(D) || isnan(D))
-            {
-                float gs = g_single(V, alpha);
-                for(int k = 0; k < nc; k++) spec[k] = G * F[k] / gs;
-                ps = 1.0f;
-            }
-            float ndl = fmaxf(0.0f, Ll[2]);
-            float corr = burley(ndl, ndv, ldh, sf->roughness);
-            for(int k = 0; k < nc; k++)
-                refl[k] = ndl * ((1.0f - sf->metallic) * alb[k]) * INV_PI_F * corr + spec[k];
-            bpdf = pd * ratio + ps * (1.0f - ratio);
-        }
-        else
-        {
-            float xi0 = urnd(&SC, depth, 0), xi1 = urnd(&SC, depth, 1);
-            float ang = 2.0f * PI_F * xi1, sr = sqrtf(xi0);
-            Ll[0] = sr * cosf(ang); Ll[1] = sr * sinf(ang);
-            Ll[2] = sqrtf(fmaxf(0.0f, 1.0f - (Ll[0] * Ll[0] + Ll[1] * Ll[1])));
-            bpdf = Ll[2] * INV_PI_F;
-            float cw = fmaxf(Ll[2], 0.0f) * INV_PI_F;
-            for(int k = 0; k < nc; k++) refl[k] = alb[k] * cw;
-        }
+        bxdf_sample(sf, alb, nc, backSide, V, urnd(&SC, depth, 0), urnd(&SC, depth, 1), urnd(&SC, depth, 2),
+                    Ll, refl, &bpdf, &passed);
+        if(sf->matType == ORC_MAT_REFRACT) orc_nudge(pos, nrm, presample);   /* SampleBxDF nudges along n first */
         float wi[3];
         for(int k = 0; k < 3; k++) wi[k] = tng[k] * Ll[0] + btg[k] * Ll[1] + nrm[k] * Ll[2];
         normalize3f(wi);
@@ -1330,4 +1476,150 @@ void orc_pt_make_light(const float m[12], const float* v9, const float radiance[
     memcpy(out->radiance, radiance, 12);
     out->twoSided = twoSided;
     out->instance = 0u;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Per-function entry points: each runs the helper the path loop above uses */
+/* on one record, so tests can hold it against the same function of MRay's   */
+/* compiled code (oracle/ref_pt_driver.cpp).  Vectors are in the tangent     */
+/* frame; random numbers are the dispenser's uint32 values.                  */
+/* ------------------------------------------------------------------------ */
+
+/* RNGFunctions::ToFloat01 (Source/Tracer/Random.h:102-125) */
+static inline float to_float01(uint32_t v)
+{
+    float f = (float)v * 0x1p-32f;
+    const float prev1 = 0x1.fffffep-1f;
+    return f < prev1 ? f : prev1;
+}
+
+void orc_fx_material(int kind, const orc_fx_mat_in* in, orc_fx_mat_out* out, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const orc_fx_mat_in* q = &in[i];
+        orc_fx_mat_out* o = &out[i];
+        memset(o, 0, sizeof(*o));
+        orc_pt_surface sf;
+        memset(&sf, 0, sizeof(sf));
+        sf.matType = kind;
+        sf.roughness = q->rough; sf.metallic = q->metal; sf.specular = q->spec;
+        sf.iorFront = q->iorF; sf.iorBack = q->iorB;
+        float alb[4] = { q->albedo[0], q->albedo[1], q->albedo[2], 0.0f };
+        float L[3], refl[4], pdf;
+        int passed;
+        bxdf_sample(&sf, alb, 3, (int)q->backSide, q->wo, to_float01(q->xi[0]), to_float01(q->xi[1]),
+                    to_float01(q->xi[2]), L, refl, &pdf, &passed);
+        memcpy(o->wi, L, 12);
+        memcpy(o->wiPos, q->pos, 12);
+        if(kind == ORC_MAT_REFRACT)
+        {
+            const float nz[3] = { 0.0f, 0.0f, 1.0f };
+            orc_nudge(q->pos, nz, o->wiPos);
+        }
+        o->pdf = pdf;
+        memcpy(o->refl, refl, 16);
+        o->passed = (uint32_t)passed;
+        if(kind == ORC_MAT_LAMBERT || kind == ORC_MAT_UNREAL)
+            bxdf_eval(&sf, alb, 3, q->wo, q->wiEval, o->evalRefl, &o->evalPdf);
+        o->specularity = specularity(&sf, alb, 3);
+    }
+}
+
+void orc_fx_fresnel_dielectric(const float* in3, float* out, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++) out[i] = fresnel_dielectric(in3[3 * i], in3[3 * i + 1], in3[3 * i + 2]);
+}
+
+void orc_fx_vndf_sample(const float* in6, float* out4, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in6 + 6 * i;
+        vndf_sample(q, q[3], q[4], q[5], out4 + 4 * i);
+        out4[4 * i + 3] = vndf_pdf(q, out4 + 4 * i, q[3]);
+    }
+}
+
+void orc_fx_russian_roulette(const float* in6, float* out5, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in6 + 6 * i;
+        float* o = out5 + 5 * i;
+        float pr = fminf(fmaxf(q[4], 0.1f), 1.0f);
+        o[0] = (q[5] >= pr) ? 0.0f : 1.0f;
+        float inv = 1.0f / pr;
+        for(int k = 0; k < 4; k++) o[1 + k] = o[0] != 0.0f ? q[k] * inv : 0.0f;
+    }
+}
+
+void orc_fx_tri_light(const orc_fx_light_in* in, orc_fx_light_out* out, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const orc_fx_light_in* q = &in[i];
+        orc_fx_light_out* o = &out[i];
+        memset(o, 0, sizeof(*o));
+        orc_pt_light_tri L;
+        orc_pt_make_light(q->m, q->v9, q->radiance, (int)q->twoSided, &L);
+        float emis[4] = { 0, 0, 0, 0 };
+        light_tri_sample(&L, to_float01(q->xi[0]), to_float01(q->xi[1]), q->distant, o->point, &o->samplePdf,
+                         emis);
+        memcpy(o->emitPoint, emis, 12);
+        o->pdfSolidAngle = light_tri_pdf(&L, q->hit[0], q->hit[1], q->distant, q->dir);
+        if(light_tri_emits(&L, q->wo)) memcpy(o->emitHit, q->radiance, 12);
+        o->area = L.area;
+    }
+}
+
+void orc_fx_camera(const float* cam13, const uint32_t res[2], const uint32_t* pix, const float* off4, float* out6,
+                   uint32_t n)
+{
+    orc_pt_params p;
+    memset(&p, 0, sizeof(p));
+    orc_pt_camera_frame(cam13, cam13 + 3, cam13 + 6, cam13[9], cam13[10], cam13[11], cam13[12], &p);
+    p.width = res[0]; p.height = res[1];
+    for(uint32_t i = 0; i < n; i++)
+        camera_ray(&p, pix[2 * i], pix[2 * i + 1], off4[4 * i], off4[4 * i + 1], out6 + 6 * i, out6 + 6 * i + 3);
+}
+
+/* SphericalCoordConverter (LightsDefault.hpp:174-215) as the skysphere light
+ * uses it: in dir[3], uv[2], pdf -> DirToUV(dir), UVToDir(uv),
+ * ToSolidAnglePdf(pdf, dir), ToSolidAnglePdf(pdf, uv). */
+void orc_fx_spherical_coords(const float* in6, float* out7, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in6 + 6 * i;
+        float* o = out7 + 7 * i;
+        orc_env_dir_to_uv(q, o);
+        orc_env_uv_to_dir(q + 3, o + 2);
+        float cl = (q[1] < -1.0f) ? -1.0f : ((q[1] > 1.0f) ? 1.0f : q[1]);
+        o[5] = env_sa_pdf_sin(q[5], sinf(acosf(cl)));
+        o[6] = env_sa_pdf_sin(q[5], sinf((1.0f - q[4]) * PI_F));
+    }
+}
+
+/* GaussianFilter (Filters.h:195-233): in radius, xi[2] -> offset[2], pdf,
+ * Evaluate(offset), Evaluate / pdf. */
+void orc_fx_gaussian_filter(const float* in3, float* out5, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in3 + 3 * i;
+        float* o = out5 + 5 * i;
+        filter_sample(q[0], q[1], q[2], &o[0], &o[1]);
+        float sigma = q[0] * 0.285714f;
+        o[2] = gaussian(o[0], sigma) * gaussian(o[1], sigma);
+        o[3] = gaussian(o[0], sigma) * gaussian(o[1], sigma);
+        o[4] = o[3] / o[2];
+    }
+}
+
+/* SingleSampleSpectrumWavelength, hyperbolic mode (SpectrumContext.cu:9-130):
+ * uint32 numbers in, wavelengths and pdfs out. */
+void orc_fx_sample_waves(const uint32_t* xi, float* waves4, float* pdf4, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++) orc_spec_sample_waves(to_float01(xi[i]), waves4 + 4 * i, pdf4 + 4 * i);
 }

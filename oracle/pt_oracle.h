@@ -154,6 +154,64 @@ void orc_pt_camera_frame(const float pos[3], const float gaze[3], const float up
 void orc_pt_make_light(const float m[12], const float* v9, const float radiance[3], int twoSided,
                        orc_pt_light_tri* out);
 
+/* Per-function entry points over the helpers the path loop uses (tangent
+ * frame; uint32 random numbers converted as RNGFunctions::ToFloat01).  The
+ * records match oracle/ref_pt_driver.cpp's, which runs MRay's own code. */
+typedef struct
+{
+    float    albedo[3];
+    float    rough, metal, spec, iorF, iorB;
+    uint32_t backSide;
+    float    pos[3];
+    float    wo[3];
+    float    wiEval[3];
+    uint32_t xi[3];
+} orc_fx_mat_in;
+typedef struct
+{
+    float    wi[3];
+    float    wiPos[3];
+    float    pdf;
+    float    refl[4];
+    uint32_t passed;
+    float    evalRefl[4];
+    float    evalPdf;
+    float    specularity;
+} orc_fx_mat_out;
+typedef struct
+{
+    float    m[12];
+    float    v9[9];
+    uint32_t twoSided;
+    float    radiance[3];
+    float    distant[3];
+    uint32_t xi[2];
+    float    hit[2];
+    float    dir[3];
+    float    wo[3];
+} orc_fx_light_in;
+typedef struct
+{
+    float point[3];
+    float samplePdf;
+    float pdfSolidAngle;
+    float emitHit[4];
+    float emitPoint[4];
+    float area;
+} orc_fx_light_out;
+
+/* kind: ORC_MAT_* */
+void orc_fx_material(int kind, const orc_fx_mat_in* in, orc_fx_mat_out* out, uint32_t n);
+void orc_fx_fresnel_dielectric(const float* in3, float* out, uint32_t n);
+void orc_fx_vndf_sample(const float* in6, float* out4, uint32_t n);
+void orc_fx_russian_roulette(const float* in6, float* out5, uint32_t n);
+void orc_fx_tri_light(const orc_fx_light_in* in, orc_fx_light_out* out, uint32_t n);
+void orc_fx_gaussian_filter(const float* in3, float* out5, uint32_t n);
+void orc_fx_sample_waves(const uint32_t* xi, float* waves4, float* pdf4, uint32_t n);
+void orc_fx_spherical_coords(const float* in6, float* out7, uint32_t n);
+void orc_fx_camera(const float* cam13, const uint32_t res[2], const uint32_t* pix, const float* off4, float* out6,
+                   uint32_t n);
+
 #ifdef __cplusplus
 }
 #endif

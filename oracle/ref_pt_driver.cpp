@@ -1,0 +1,496 @@
+// ref_pt_driver.cpp -- test infrastructure only: a thin extern "C" driver over
+// MRay's OWN path-tracer building blocks, compiled from the MRay source tree
+// (host backend, MRAY_GPU_BACKEND_CPU) by oracle/build.py:build_ref_pt().
+// Nothing here restates MRay: every function constructs MRay's types and calls
+// MRay's code, so the fixtures written through it (tests/golden/make_pt_golden.py)
+// are the reference's outputs on fixed inputs.  The project's restatement
+// (oracle/pt_oracle.c) is checked against them in tests/test_oracle_pt_golden.py.
+//
+// Materials are evaluated on a surface whose shading rotation is the identity
+// quaternion, so the tangent frame is the world frame and the BxDF arithmetic
+// is compared without a frame convention in between.
+//
+// Random numbers enter as the uint32 values MRay's RNGDispenser converts
+// (RNGFunctions::ToFloat01, Tracer/Random.h:102-125).
+#include "Tracer/MaterialsDefault.h"
+#include "Tracer/MaterialsDefault.hpp"
+#include "Tracer/LightsDefault.h"
+#include "Tracer/LightsDefault.hpp"
+#include "Tracer/LightSampler.h"
+#include "Tracer/LightSampler.hpp"
+#include "Tracer/CamerasDefault.h"
+#include "Tracer/CamerasDefault.hpp"
+#include "Tracer/Filters.h"
+#include "Tracer/SpectrumContext.h"
+#include "Tracer/Random.h"
+#include "Tracer/DistributionFunctions.h"
+#include "Tracer/Distributions.h"
+#include "Tracer/PrimitiveDefaultTriangle.h"
+#include "Tracer/PrimitiveDefaultTriangle.hpp"
+#include "Tracer/TransformsDefault.h"
+#include "Tracer/TransformsDefault.hpp"
+#include "Tracer/TextureView.hpp"
+#include "Device/CPU/GPUSystemCPU.hpp"
+// the wavelength sampler and the spectrum -> RGB conversion are free device
+// functions of this translation unit of MRay (host backend)
+#include "Tracer/SpectrumContext.cu"
+
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace
+{
+
+Vector3 V3(const float* p) { return Vector3(p[0], p[1], p[2]); }
+void put3(float* o, const Vector3& v) { o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; }
+void put4(float* o, const Spectrum& s) { o[0] = s[0]; o[1] = s[1]; o[2] = s[2]; o[3] = s[3]; }
+
+DefaultSurface tangent_surface(const float* pos, bool backSide)
+{
+    return DefaultSurface
+    {
+        .position = V3(pos),
+        .geoNormal = Vector3(0, 0, 1),
+        .shadingTBN = Quaternion::Identity(),
+        .uv = Vector2(0, 0),
+        .dpdx = Vector2(0, 0),
+        .dpdy = Vector2(0, 0),
+        .backSide = backSide
+    };
+}
+
+// One record of a material query (all vectors in the tangent frame).
+//   in:  albedo[3], rough, metal, spec, iorFront, iorBack, backSide, pos[3],
+//        wo[3], wiEval[3], xi[3] (uint32)
+//   out: wi[3], wiPos[3], pdf, refl[4], passed, evalRefl[4], evalPdf, specularity
+struct MatIn
+{
+    float albedo[3];
+    float rough, metal, spec, iorF, iorB;
+    uint32_t backSide;
+    float pos[3];
+    float wo[3];
+    float wiEval[3];
+    uint32_t xi[3];
+};
+struct MatOut
+{
+    float wi[3];
+    float wiPos[3];
+    float pdf;
+    float refl[4];
+    uint32_t passed;
+    float evalRefl[4];
+    float evalPdf;
+    float specularity;
+};
+static_assert(sizeof(MatIn) == 21 * 4, "MatIn layout");
+static_assert(sizeof(MatOut) == 18 * 4, "MatOut layout");
+
+template<class M>
+void run_material(const M& m, const MatIn& in, MatOut& out)
+{
+    RNGDispenser rng(Span<const uint32_t>(in.xi, 3), 0, 1);
+    BxDFSample s = m.SampleBxDF(V3(in.wo), rng);
+    put3(out.wi, s.wI.dir);
+    put3(out.wiPos, s.wI.pos);
+    out.pdf = s.pdf;
+    put4(out.refl, s.eval.reflectance);
+    out.passed = s.eval.isPassedThrough ? 1u : 0u;
+    Ray wiE(V3(in.wiEval), V3(in.pos));
+    BxDFEval e = m.Evaluate(wiE, V3(in.wo));
+    put4(out.evalRefl, e.reflectance);
+    out.evalPdf = m.Pdf(wiE, V3(in.wo));
+    out.specularity = m.Specularity();
+}
+
+} // namespace
+
+extern "C" {
+
+int ref_pt_abi_version() { return 1; }
+
+// kind: 0 Lambert, 1 Reflect, 2 Refract, 3 Unreal (MaterialsDefault.hpp)
+void ref_material(int kind, const MatIn* in, MatOut* out, uint32_t n)
+{
+    using SC = SpectrumContextIdentity;
+    SC::Converter conv;
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const MatIn& q = in[i];
+        MatOut& o = out[i];
+        std::memset(&o, 0, sizeof(o));
+        DefaultSurface surf = tangent_surface(q.pos, q.backSide != 0);
+        MaterialKey mk = MaterialKey::CombinedKey(0, 0);
+        if(kind == 0)
+        {
+            std::vector<ParamVaryingData<2, Vector3>> alb = { ParamVaryingData<2, Vector3>(V3(q.albedo)) };
+            std::vector<Optional<TracerTexView<2, Vector3>>> nm = { std::nullopt };
+            LambertMatDetail::LambertMatData soa{ Span<const ParamVaryingData<2, Vector3>>(alb.data(), 1),
+                                                  Span<const Optional<TracerTexView<2, Vector3>>>(nm.data(), 1) };
+            LambertMatDetail::LambertMaterial<SC> m(conv, surf, soa, mk);
+            run_material(m, q, o);
+        }
+        else if(kind == 1)
+        {
+            ReflectMatDetail::ReflectMatData soa{};
+            ReflectMatDetail::ReflectMaterial<SC> m(conv, surf, soa, mk);
+            run_material(m, q, o);
+        }
+        else if(kind == 2)
+        {
+            std::vector<Vector3> f = { Vector3(q.iorF, 0, 0) }, b = { Vector3(q.iorB, 0, 0) };
+            RefractMatDetail::RefractMatData soa{ Span<const Vector3>(f.data(), 1), Span<const Vector3>(b.data(), 1) };
+            RefractMatDetail::RefractMaterial<SC> m(conv, surf, soa, mk);
+            run_material(m, q, o);
+        }
+        else
+        {
+            std::vector<ParamVaryingData<2, Vector3>> alb = { ParamVaryingData<2, Vector3>(V3(q.albedo)) };
+            std::vector<Optional<TracerTexView<2, Vector3>>> nm = { std::nullopt };
+            std::vector<ParamVaryingData<2, Float>> r = { ParamVaryingData<2, Float>(q.rough) };
+            std::vector<ParamVaryingData<2, Float>> sp = { ParamVaryingData<2, Float>(q.spec) };
+            std::vector<ParamVaryingData<2, Float>> mt = { ParamVaryingData<2, Float>(q.metal) };
+            UnrealMatDetail::UnrealMatData soa{ Span<const ParamVaryingData<2, Vector3>>(alb.data(), 1),
+                                                Span<const Optional<TracerTexView<2, Vector3>>>(nm.data(), 1),
+                                                Span<const ParamVaryingData<2, Float>>(r.data(), 1),
+                                                Span<const ParamVaryingData<2, Float>>(sp.data(), 1),
+                                                Span<const ParamVaryingData<2, Float>>(mt.data(), 1) };
+            UnrealMatDetail::UnrealMaterial<SC> m(conv, surf, soa, mk);
+            run_material(m, q, o);
+        }
+    }
+}
+
+// BxDF building blocks (DistributionFunctions.h), one call per record:
+// io[0..8] in, outputs after.
+//  fresnel: in cosF, etaF, etaB -> out f
+void ref_fresnel_dielectric(const float* in3, float* out, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+        out[i] = Distribution::BxDF::FresnelDielectric(in3[3 * i], in3[3 * i + 1], in3[3 * i + 2]);
+}
+
+// VNDF sample: in V[3], alpha, xi[2] -> out H[3], pdf
+void ref_vndf_sample(const float* in6, float* out4, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in6 + 6 * i;
+        auto s = Distribution::BxDF::VNDFGGXSmithSample(V3(q), q[3], Vector2(q[4], q[5]));
+        put3(out4 + 4 * i, s.value);
+        out4[4 * i + 3] = s.pdf;
+    }
+}
+
+// Cosine-weighted hemisphere sample: xi[2] -> dir[3], pdf
+void ref_cos_sample(const float* in2, float* out4, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        auto s = Distribution::Common::SampleCosDirection(Vector2(in2[2 * i], in2[2 * i + 1]));
+        put3(out4 + 4 * i, s.value);
+        out4[4 * i + 3] = s.pdf;
+    }
+}
+
+// Russian roulette (Common::RussianRoulette): in thr[4], prob, xi ->
+// out alive, thr'[4]
+void ref_russian_roulette(const float* in6, float* out5, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in6 + 6 * i;
+        Spectrum t(q[0], q[1], q[2], q[3]);
+        auto r = Distribution::Common::RussianRoulette(t, q[4], q[5]);
+        out5[5 * i] = r.has_value() ? 1.0f : 0.0f;
+        if(r.has_value()) put4(out5 + 5 * i + 1, *r);
+        else for(int k = 1; k < 5; k++) out5[5 * i + k] = 0.0f;
+    }
+}
+
+// MIS::BalanceCancelled<2>: in pdf[2], weight[2] -> out
+void ref_balance_cancelled(const float* in4, float* out, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        std::array<Float, 2> p = { in4[4 * i], in4[4 * i + 1] }, w = { in4[4 * i + 2], in4[4 * i + 3] };
+        out[i] = Distribution::MIS::BalanceCancelled<2>(p, w);
+    }
+}
+
+// Ray::Nudge (Core/Ray.hpp:258-300): in pos[3], dir[3] -> out pos[3]
+void ref_nudge(const float* in6, float* out3, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        Ray r(Vector3(0, 0, 1), V3(in6 + 6 * i));
+        put3(out3 + 3 * i, r.Nudge(V3(in6 + 6 * i + 3)).pos);
+    }
+}
+
+// Gaussian film filter (Filters.h:195-233; default radius 1):
+// in radius, xi[2] -> out offset[2], pdf, weight (Evaluate), weight / pdf
+void ref_gaussian_filter(const float* in3, float* out5, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        GaussianFilter f(in3[3 * i]);
+        auto s = f.Sample(Vector2(in3[3 * i + 1], in3[3 * i + 2]));
+        float* o = out5 + 5 * i;
+        o[0] = s.value[0]; o[1] = s.value[1]; o[2] = s.pdf;
+        o[3] = f.Evaluate(s.value);
+        o[4] = o[3] / s.pdf;
+    }
+}
+
+// Primitive-backed area light on one triangle (LightPrim<Triangle<
+// TransformContextSingle>>, LightsDefault.hpp:14-165; Triangle sampling,
+// PrimitiveDefaultTriangle.hpp:48-80).  The triangle's local vertices are
+// moved to world space by the instance's 3x4 transform, as MRay does.
+struct TriLightIn
+{
+    float m[12];            // row-major 3x4 local -> world
+    float v9[9];            // local vertices
+    uint32_t twoSided;
+    float radiance[3];
+    float distant[3];       // the shaded point
+    uint32_t xi[2];
+    float hit[2];           // (a, b) barycentrics of a light hit
+    float dir[3];           // direction of the ray that hit it
+    float wo[3];            // emission direction for EmitViaHit
+};
+struct TriLightOut
+{
+    float point[3];
+    float samplePdf;
+    float pdfSolidAngle;
+    float emitHit[4];
+    float emitPoint[4];     // EmitViaSurfacePoint towards the shaded point
+    float area;
+};
+static_assert(sizeof(TriLightIn) == 38 * 4, "TriLightIn layout");
+static_assert(sizeof(TriLightOut) == 14 * 4, "TriLightOut layout");
+
+void ref_tri_light(const TriLightIn* in, TriLightOut* out, uint32_t n)
+{
+    using namespace DefaultTriangleDetail;
+    using TC = TransformContextSingle;
+    SpectrumContextIdentity::Converter conv;
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const TriLightIn& q = in[i];
+        TriLightOut& o = out[i];
+        std::memset(&o, 0, sizeof(o));
+        Matrix3x4 mt(q.m[0], q.m[1], q.m[2], q.m[3], q.m[4], q.m[5], q.m[6], q.m[7],
+                     q.m[8], q.m[9], q.m[10], q.m[11]);
+        Matrix3x4 inv = mt.Inverse();
+        TransformDetail::SingleTransformSoA tsoa{ Span<const Matrix3x4>(&mt, 1), Span<const Matrix3x4>(&inv, 1) };
+        TC tc(tsoa, TransformKey::CombinedKey(0, 0));
+        Vector3 pos[3] = { V3(q.v9), V3(q.v9 + 3), V3(q.v9 + 6) };
+        Quaternion tbn[3] = { Quaternion::Identity(), Quaternion::Identity(), Quaternion::Identity() };
+        Vector2 uv[3] = { Vector2(0, 0), Vector2(1, 0), Vector2(0, 1) };
+        Vector3ui idx(0, 1, 2);
+        TriangleData td{ Span<const Vector3>(pos, 3), Span<const Quaternion>(tbn, 3),
+                         Span<const Vector2>(uv, 3), Span<const Vector3ui>(&idx, 1) };
+        Triangle<TC> prim(tc, td, PrimitiveKey::CombinedKey(0, 0));
+        std::vector<ParamVaryingData<2, Vector3>> rad = { ParamVaryingData<2, Vector3>(V3(q.radiance)) };
+        bool two[1] = { q.twoSided != 0 };
+        LightDetail::LightData lsoa{ Span<const ParamVaryingData<2, Vector3>>(rad.data(), 1), Span<const bool>(two, 1) };
+        LightDetail::LightPrim<Triangle<TC>, SpectrumContextIdentity> light(conv, prim, lsoa, LightKey::CombinedKey(0, 0));
+        RNGDispenser rng(Span<const uint32_t>(q.xi, 2), 0, 1);
+        SampleT<Vector3> s = light.SampleSolidAngle(rng, V3(q.distant));
+        put3(o.point, s.value);
+        o.samplePdf = s.pdf;
+        o.pdfSolidAngle = light.PdfSolidAngle(Vector2(q.hit[0], q.hit[1]), V3(q.distant), V3(q.dir));
+        put4(o.emitHit, light.EmitViaHit(V3(q.wo), Vector2(q.hit[0], q.hit[1]), RayCone{}));
+        Vector3 wO = Math::Normalize(V3(q.distant) - s.value);
+        put4(o.emitPoint, light.EmitViaSurfacePoint(wO, s.value, RayCone{}));
+        o.area = prim.GetSurfaceArea();
+    }
+}
+
+// Lat-long mapping of the skysphere (SphericalCoordConverter,
+// LightsDefault.hpp:174-215): in dir[3], uv[2], pdf -> out uv[2] (DirToUV),
+// dir[3] (UVToDir), ToSolidAnglePdf(pdf, dir), ToSolidAnglePdf(pdf, uv)
+void ref_spherical_coords(const float* in6, float* out7, uint32_t n)
+{
+    using C = LightDetail::SphericalCoordConverter;
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in6 + 6 * i;
+        float* o = out7 + 7 * i;
+        Vector2 uv = C::DirToUV(V3(q));
+        o[0] = uv[0]; o[1] = uv[1];
+        put3(o + 2, C::UVToDir(Vector2(q[3], q[4])));
+        o[5] = C::ToSolidAnglePdf(q[5], V3(q));
+        o[6] = C::ToSolidAnglePdf(q[5], Vector2(q[3], q[4]));
+    }
+}
+
+// Piecewise-constant 2D distribution sampling (DistributionPwC<2>,
+// Distributions.h:120-270) over given CDFs: cdfX is h rows of w entries
+// (each row's running sum normalised to end at 1), cdfY the h marginal
+// entries.  in xi[2] -> out uv[2], pdf; in uvq[2] -> out PdfUV.
+void ref_pwc2d(const float* cdfX, const float* cdfY, uint32_t w, uint32_t h,
+               const float* xi2, float* out3, const float* uvq2, float* outPdf, uint32_t n)
+{
+    using namespace Distribution;
+    std::vector<DistributionPwC<1>> rows;
+    rows.reserve(h);
+    for(uint32_t r = 0; r < h; r++) rows.emplace_back(Span<const Float>(cdfX + (size_t)r * w, w));
+    DistributionPwC<1> marg(Span<const Float>(cdfY, h));
+    DistributionPwC<2> d2(Span<const DistributionPwC<1>>(rows.data(), h), marg);
+    for(uint32_t i = 0; i < n; i++)
+    {
+        auto s = d2.SampleUV(Vector2(xi2[2 * i], xi2[2 * i + 1]));
+        out3[3 * i] = s.value[0]; out3[3 * i + 1] = s.value[1]; out3[3 * i + 2] = s.pdf;
+        outPdf[i] = d2.PdfUV(Vector2(uvq2[2 * i], uvq2[2 * i + 1]));
+    }
+}
+
+// Pinhole camera (CameraPinhole, CamerasDefault.hpp:8-36 and EvaluateRay
+// :94-135).  cam: pos[3], gaze[3], up[3], fov[2] (radians), near, far.
+// per ray in: pixel[2] (uint32), offset[2], range[2] -> out dir[3], pos[3]
+void ref_camera(const float* cam13, const uint32_t res[2],
+                const uint32_t* pix, const float* off4, float* out6, uint32_t n)
+{
+    using namespace CameraDetail;
+    Vector3 p = V3(cam13), g = V3(cam13 + 3), u = V3(cam13 + 6);
+    Vector4 fp(cam13[9], cam13[10], cam13[11], cam13[12]);
+    CamPinholeData soa{ Span<const Vector4>(&fp, 1), Span<const Vector3>(&p, 1),
+                        Span<const Vector3>(&g, 1), Span<const Vector3>(&u, 1) };
+    CameraPinhole c(soa, CameraKey::CombinedKey(0, 0));
+    for(uint32_t i = 0; i < n; i++)
+    {
+        CameraRaySample r = c.EvaluateRay(Vector2ui(pix[2 * i], pix[2 * i + 1]), Vector2ui(res[0], res[1]),
+                                          Vector2(off4[4 * i], off4[4 * i + 1]),
+                                          Vector2(off4[4 * i + 2], off4[4 * i + 3]));
+        put3(out6 + 6 * i, r.value.ray.dir);
+        put3(out6 + 6 * i + 3, r.value.ray.pos);
+    }
+}
+
+// ---- spectral (Jakob 2019 converter, SpectrumContext.hpp/.cu) ----------
+// The converter's data built exactly as SpectrumContextJakob2019's
+// constructor builds it (SpectrumContext.cu:355-531) for Rec.709, over
+// MRay's CPU texture views of a resolution-64 MR_SPECTRA LUT (the
+// converter's compile-time resolution).
+struct SpecCtx
+{
+    std::vector<float>   lut;                   // 9 * 64^3, file order
+    std::vector<Vector4> observer;              // padded, normalised CIE 1931
+    std::vector<float>   illuminant;            // normalised SPD
+    const Byte*          ptrs[11];
+    TextureInitParams<3> tp3;
+    TextureInitParams<1> tp1;
+    Jakob2019Detail::Data* data = nullptr;
+};
+
+void* ref_spec_create(const float* lut, uint32_t res)
+{
+    constexpr uint32_t N = Jakob2019Detail::Data::N;
+    if(res != N) return nullptr;
+    SpecCtx* c = new SpecCtx();
+    c->lut.assign(lut, lut + 9ull * N * N * N);
+    c->observer.resize(Color::CIE_1931_N);
+    c->illuminant.resize(Color::CIE_1931_N);
+    const auto cs = MRayColorSpaceEnum::MR_REC_709;
+    const auto& spd = Color::SelectIlluminantSPD(cs);
+    Float norm = Color::CIE_1931_Y_INTEGRAL;
+    norm /= Color::SelectIlluminantSPDNormFactor(cs);
+    for(uint32_t i = 0; i < Color::CIE_1931_N; i++)
+    {
+        static constexpr Vector3 SUM = Vector3(Color::CIE_1931_X_INTEGRAL, Color::CIE_1931_Y_INTEGRAL,
+                                               Color::CIE_1931_Z_INTEGRAL);
+        static constexpr Vector3 W = Vector3(1) / SUM;
+        c->observer[i] = Vector4(Color::CIE_1931_XYZ[i] * W, 0);
+        c->illuminant[i] = spd[i] * norm;
+    }
+    c->tp3 = TextureInitParams<3>{ .size = Vector3ui(N), .normIntegers = false,
+                                   .interp = MRayTextureInterpEnum::MR_LINEAR,
+                                   .eResolve = MRayTextureEdgeResolveEnum::MR_CLAMP };
+    c->tp1 = TextureInitParams<1>{ .size = Color::CIE_1931_N, .normIntegers = false, .normCoordinates = false,
+                                   .interp = MRayTextureInterpEnum::MR_LINEAR,
+                                   .eResolve = MRayTextureEdgeResolveEnum::MR_CLAMP };
+    for(int t = 0; t < 9; t++)
+        c->ptrs[t] = reinterpret_cast<const Byte*>(c->lut.data() + (size_t)t * N * N * N);
+    c->ptrs[9] = reinterpret_cast<const Byte*>(c->observer.data());
+    c->ptrs[10] = reinterpret_cast<const Byte*>(c->illuminant.data());
+    using TV3 = TextureView<3, Float>;
+    const auto fEnum = MRayPixelTypeRT(static_cast<MRayPixelEnum>(mray::host::PixelTypeToEnum::template Find<Float>));
+    const auto v4Enum = MRayPixelTypeRT(static_cast<MRayPixelEnum>(mray::host::PixelTypeToEnum::template Find<Vector4>));
+    Matrix3x3 r2x = Color::SelectRGBToXYZMatrix(cs);
+    c->data = new Jakob2019Detail::Data
+    {
+        .RGBToXYZ = r2x,
+        .XYZToRGB = r2x.Inverse(),
+        .lut =
+        {
+            Jakob2019Detail::Data::Table3D{ TV3(&c->ptrs[0], &c->tp3, fEnum), TV3(&c->ptrs[1], &c->tp3, fEnum),
+                                            TV3(&c->ptrs[2], &c->tp3, fEnum) },
+            Jakob2019Detail::Data::Table3D{ TV3(&c->ptrs[3], &c->tp3, fEnum), TV3(&c->ptrs[4], &c->tp3, fEnum),
+                                            TV3(&c->ptrs[5], &c->tp3, fEnum) },
+            Jakob2019Detail::Data::Table3D{ TV3(&c->ptrs[6], &c->tp3, fEnum), TV3(&c->ptrs[7], &c->tp3, fEnum),
+                                            TV3(&c->ptrs[8], &c->tp3, fEnum) },
+        },
+        .spdObserverXYZ = TextureView<1, Vector3>(&c->ptrs[9], &c->tp1, v4Enum),
+        .spdIlluminant = TextureView<1, Float>(&c->ptrs[10], &c->tp1, fEnum)
+    };
+    return c;
+}
+
+void ref_spec_destroy(void* p)
+{
+    SpecCtx* c = static_cast<SpecCtx*>(p);
+    if(!c) return;
+    delete c->data;
+    delete c;
+}
+
+// ConvertAlbedo (radiance = 0) / ConvertRadiance (radiance = 1) of rgb[3] at waves[4]
+void ref_spec_convert(void* p, int radiance, const float* rgb3, const float* waves4, float* out4, uint32_t n)
+{
+    SpecCtx* c = static_cast<SpecCtx*>(p);
+    for(uint32_t i = 0; i < n; i++)
+    {
+        SpectrumWaves w;
+        for(int k = 0; k < 4; k++) w[k] = waves4[4 * i + k];
+        Jakob2019Detail::Converter conv(w, *c->data);
+        Spectrum s = radiance ? conv.ConvertRadiance(V3(rgb3 + 3 * i)) : conv.ConvertAlbedo(V3(rgb3 + 3 * i));
+        put4(out4 + 4 * i, s);
+    }
+}
+
+// SingleSampleSpectrumWavelength (SpectrumContext.cu:9-130):
+// mode 0 uniform, 1 Gaussian MIS, 2 hyperbolic (the renderer default)
+void ref_spec_sample_waves(int mode, const uint32_t* xi, float* waves4, float* pdf4, uint32_t n)
+{
+    WavelengthSampleMode m((mode == 0) ? WavelengthSampleMode::UNIFORM
+                           : (mode == 1) ? WavelengthSampleMode::GAUSSIAN_MIS : WavelengthSampleMode::HYPERBOLIC_PBRT);
+    for(uint32_t i = 0; i < n; i++)
+    {
+        SpectrumWaves w;
+        Spectrum pdf;
+        RNGDispenser rng(Span<const uint32_t>(xi + i, 1), 0, 1);
+        SingleSampleSpectrumWavelength(w, pdf, rng, m);
+        for(int k = 0; k < 4; k++) { waves4[4 * i + k] = w[k]; pdf4[4 * i + k] = pdf[k]; }
+    }
+}
+
+// ConvertSpectraToRGBSingle (SpectrumContext.cu:134-160)
+void ref_spec_to_rgb(void* p, const float* value4, const float* waves4, const float* pdf4, float* rgb3, uint32_t n)
+{
+    SpecCtx* c = static_cast<SpecCtx*>(p);
+    for(uint32_t i = 0; i < n; i++)
+    {
+        Spectrum v, pdf;
+        SpectrumWaves w;
+        for(int k = 0; k < 4; k++) { v[k] = value4[4 * i + k]; pdf[k] = pdf4[4 * i + k]; w[k] = waves4[4 * i + k]; }
+        Spectrum r = ConvertSpectraToRGBSingle(v, w, pdf, c->data->spdObserverXYZ, c->data->XYZToRGB);
+        for(int k = 0; k < 3; k++) rgb3[3 * i + k] = r[k];
+    }
+}
+
+}  // extern "C"

@@ -37,10 +37,16 @@ def test_zsobol_render_matches_oracle(surf_fn, mode, sampler):
     print("zsobol mode %d: close %.4f relMSE %.3g" % (mode, frac, relmse(g, o)))
     assert frac >= 0.97, frac
     assert relmse(g, o) <= 1e-3
-    # a different sampler gives a different (but statistically equal) image
+    # a different sampler gives a different (but statistically equal) image:
+    # image means over four seeds each; pure path tracing (mode 0) of the
+    # small light is several times noisier than NEE, hence its wider bar
     ind = _img(pt.render(PathTracer.params(60, 44, 16, cam, sample_mode=mode, seed=9)))
     assert not np.array_equal(ind, g)
-    assert abs(float(ind.mean()) - float(g.mean())) <= 0.05 * float(ind.mean())
+    mi = np.mean([_img(pt.render(PathTracer.params(60, 44, 16, cam, sample_mode=mode, seed=s))).mean()
+                  for s in range(9, 13)])
+    mz = np.mean([_img(pt.render(PathTracer.params(60, 44, 16, cam, sample_mode=mode, seed=s,
+                                                   sampler=name))).mean() for s in range(9, 13)])
+    assert abs(mi - mz) <= (0.10 if mode == 0 else 0.05) * mi, (mi, mz)
     pt.close()
 
 

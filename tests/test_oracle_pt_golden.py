@@ -1,0 +1,152 @@
+"""The path-tracer oracle pinned to MRay's own code.
+
+tests/golden/pt_math.npz holds seeded inputs and the outputs that MRay's
+compiled path-tracer building blocks give on them (written by
+tests/golden/make_pt_golden.py through oracle/ref_pt_driver.cpp, which calls
+MRay's functions unmodified).  Every function of the project's restatement
+(oracle/pt_oracle.c) that the path loop uses must reproduce them bit for bit:
+materials (Tracer/MaterialsDefault.hpp), the BxDF helpers
+(Tracer/DistributionFunctions.h), Russian roulette, the film filter
+(Tracer/Filters.h), the triangle light (Tracer/LightsDefault.hpp), the
+skysphere's lat-long mapping, the PwC2D sampling (Tracer/Distributions.h), the
+pinhole camera (Tracer/CamerasDefault.hpp) and wavelength sampling
+(Tracer/SpectrumContext.cu).  Both sides use the same host C library for sin,
+cos, log and the like, so there is no tolerance.
+
+Where the MRay tree is present the fixture is also regenerated from MRay's
+code and compared, and the spectral converter is checked against MRay's own
+at its compile-time LUT resolution (64, generated by MRay's SpectraLUTGen).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "pt_math.npz")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return np.load(GOLD)
+
+
+def bits(a):
+    a = np.ascontiguousarray(a, np.float32)
+    # -0 and +0, and NaNs of any payload, are the same value
+    b = a.view(np.uint32).copy()
+    b[a == 0] = 0
+    b[np.isnan(a)] = 0x7FC00000
+    return b
+
+
+def same(a, b):
+    return np.array_equal(bits(a), bits(b))
+
+
+@pytest.mark.parametrize("kind", ["lambert", "reflect", "refract", "unreal"])
+def test_material_sample_eval_pdf_match_mray(g, kind):
+    rin, ref = g["mat_%s_in" % kind], g["mat_%s_out" % kind]
+    got = oracle.fx_material(kind, rin)
+    for f in ("wi", "wiPos", "pdf", "specularity", "passed"):
+        assert same(got[f], ref[f]), f
+    # RGB: MRay's Spectrum has a fourth channel the RGB tracer does not carry
+    assert same(got["refl"][:, :3], ref["refl"][:, :3])
+    if kind in ("lambert", "unreal"):       # specular materials take no NEE
+        assert same(got["evalRefl"][:, :3], ref["evalRefl"][:, :3])
+        assert same(got["evalPdf"], ref["evalPdf"])
+
+
+def test_bxdf_helpers_match_mray(g):
+    assert same(oracle.fx_fresnel_dielectric(g["fresnel_in"]), g["fresnel_out"])
+    assert same(oracle.fx_vndf_sample(g["vndf_in"]), g["vndf_out"])
+    assert same(oracle.fx_russian_roulette(g["rr_in"]), g["rr_out"])
+
+
+def test_film_filter_matches_mray(g):
+    got = oracle.fx_gaussian_filter(g["filter_in"])
+    assert same(got, g["filter_out"])
+    assert np.all(got[:, 4] == 1.0)          # the film weight Evaluate / pdf
+
+
+def test_triangle_light_matches_mray(g):
+    got, ref = oracle.fx_tri_light(g["light_in"]), g["light_out"]
+    for f in ("point", "samplePdf", "pdfSolidAngle", "area"):
+        assert same(got[f], ref[f]), f
+    assert same(got["emitHit"][:, :3], ref["emitHit"][:, :3])
+    assert same(got["emitPoint"][:, :3], ref["emitPoint"][:, :3])
+
+
+def test_skysphere_mapping_and_pwc2d_match_mray(g):
+    assert same(oracle.fx_spherical_coords(g["sph_in"]), g["sph_out"])
+    # Sampling and pdf given CDFs are MRay's DistributionPwC<2>.  The CDFs
+    # are the restatement's construction (MRay builds them in its device
+    # layer, which is not compiled here); the construction is checked
+    # against the properties of MRay's own test in tests/test_oracle_env.py.
+    d = oracle.Pwc2D(g["pwc_func"])
+    uv, pdf = d.sample_uv(g["pwc_xi"])
+    assert same(uv, g["pwc_sample"][:, :2]) and same(pdf, g["pwc_sample"][:, 2])
+    assert same(d.pdf_uv(g["pwc_uvq"]), g["pwc_pdf"])
+
+
+def test_camera_matches_mray(g):
+    got = oracle.fx_camera(g["cam_params"], g["cam_res"], g["cam_pix"], g["cam_off"])
+    assert same(got, g["cam_out"])
+
+
+def test_wavelength_sampling_matches_mray(g):
+    w, p = oracle.fx_sample_waves(g["waves_xi"])
+    assert same(w, g["waves_out"]) and same(p, g["waves_pdf"])
+
+
+# ---- where the MRay tree is present: MRay's code run here -----------------
+
+def _ref():
+    from oracle import ref_pt
+    if ref_pt.load() is None:
+        pytest.skip("the MRay source tree is not present")
+    return ref_pt
+
+
+def test_fixture_is_what_mray_computes(g):
+    """Regenerates the stored outputs from MRay's compiled code."""
+    R = _ref()
+    for kind in ("lambert", "reflect", "refract", "unreal"):
+        ref = R.material(kind, g["mat_%s_in" % kind])
+        for f in ref.dtype.names:
+            assert same(ref[f], g["mat_%s_out" % kind][f]), (kind, f)
+    assert same(R.vndf_sample(g["vndf_in"]), g["vndf_out"])
+    assert same(R.gaussian_filter(g["filter_in"]), g["filter_out"])
+    lo = R.tri_light(g["light_in"])
+    for f in lo.dtype.names:
+        assert same(lo[f], g["light_out"][f]), f
+    assert same(R.camera(g["cam_params"], g["cam_res"], g["cam_pix"], g["cam_off"]), g["cam_out"])
+
+
+def test_spectral_converter_matches_mray():
+    R = _ref()
+    from oracle import build
+    path = build.ref_lut(64)
+    tables = os.path.join(os.path.dirname(__file__), "golden", "spectral_rec709.npz")
+    S = oracle.Spectral(path, tables)
+    res, lut = oracle.read_mrspectra(path)
+    M = R.Spectral(lut, res)
+    rng = np.random.default_rng(5)
+    n = 512
+    rgb = rng.uniform(0, 1, (n, 3)).astype(np.float32)
+    rgb[:8] = 0.0
+    rgb[8:16] = 1.0
+    rgb[16:48] *= 40.0                       # radiances above 1
+    xi = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    waves, pdf = oracle.fx_sample_waves(xi)
+    for radiance in (False, True):
+        want = M.convert(rgb, waves, radiance=radiance)
+        conv = S.convert_radiance if radiance else S.convert_albedo
+        got = np.stack([conv(rgb[i], waves[i]) for i in range(n)])
+        assert same(got, want), radiance
+    val = rng.uniform(0, 5, (n, 4)).astype(np.float32)
+    want = M.to_rgb(val, waves, pdf)
+    got = np.stack([S.to_rgb(val[i], waves[i], pdf[i]) for i in range(n)])
+    assert same(got, want)
+    M.close()

@@ -82,17 +82,25 @@ def test_request_layout():
 
 
 def test_oracle_render_with_zsobol_is_statistically_equal():
-    """The box scene at 24x24, 64 spp: the ZSobol render and the independent
-    render agree in mean radiance within 3% and per pixel in relMSE."""
+    """The box scene at 24x24, 64 spp: the ZSobol renders and the independent
+    renders agree in mean radiance within 2.5% (averaged over eight seeds: one
+    seed's noise is about 1.4% of the mean, so the bar is about 3.5 standard
+    deviations of the difference) and per pixel in
+    relMSE (the 1% largest pixel errors, fireflies, left out)."""
     from mray_gb300 import scenes
     S = oracle.PtScene(scenes.box_scene(0))
     cam = scenes.box_camera()
-    a = S.render(S.params(24, 24, 64, cam, seed=3))
-    b = S.render(S.params(24, 24, 64, cam, seed=3, sampler=1))
-    a, b = a[..., :3] / a[..., 3:], b[..., :3] / b[..., 3:]
-    assert not np.array_equal(a, b)
-    assert abs(a.mean() - b.mean()) <= 0.03 * a.mean()
-    assert float(np.mean((a - b) ** 2 / (a ** 2 + 1e-2))) <= 0.05
+    ma, mb = [], []
+    for seed in range(3, 11):
+        a = S.render(S.params(24, 24, 64, cam, seed=seed))
+        b = S.render(S.params(24, 24, 64, cam, seed=seed, sampler=1))
+        a, b = a[..., :3] / a[..., 3:], b[..., :3] / b[..., 3:]
+        assert not np.array_equal(a, b)
+        e = ((a - b) ** 2 / (a ** 2 + 1e-2)).ravel()
+        assert float(np.mean(np.sort(e)[: int(e.size * 0.99)])) <= 0.05     # fireflies trimmed
+        ma.append(a.mean())
+        mb.append(b.mean())
+    assert abs(np.mean(ma) - np.mean(mb)) <= 0.025 * np.mean(ma)
 
 
 def test_owen_variant_keeps_stratification():
