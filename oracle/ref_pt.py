@@ -133,6 +133,21 @@ def sample_waves(mode, xi):
     return w, p
 
 
+def zsobol(in8):
+    """in8 rows: px, py, seed, sampleIndex, initialMaxSPP, resMaxBits, dim,
+    size -> up to 3 uint32 numbers (ZSobol::Next / Next2D / Next3D)."""
+    in8 = np.ascontiguousarray(in8, np.uint32)
+    out = np.zeros((in8.shape[0], 3), np.uint32)
+    load().ref_zsobol(_p(in8), _p(out), C.c_uint32(in8.shape[0]))
+    return out
+
+
+def zsobol_seeds(seed, count):
+    out = np.zeros(count, np.uint32)
+    load().ref_zsobol_seeds(C.c_uint64(seed), C.c_uint32(count), _p(out))
+    return out
+
+
 class Spectral:
     """MRay's Jakob 2019 converter over a resolution-64 LUT (the converter's
     compile-time resolution)."""

@@ -34,6 +34,8 @@
 // the wavelength sampler and the spectrum -> RGB conversion are free device
 // functions of this translation unit of MRay (host backend)
 #include "Tracer/SpectrumContext.cu"
+// the ZSobol generator (ZSobolDetail::ZSobol) is defined in this unit of MRay
+#include "Tracer/Random.cu"
 
 #include <cstdint>
 #include <cstring>
@@ -491,6 +493,38 @@ void ref_spec_to_rgb(void* p, const float* value4, const float* waves4, const fl
         Spectrum r = ConvertSpectraToRGBSingle(v, w, pdf, c->data->spdObserverXYZ, c->data->XYZToRGB);
         for(int k = 0; k < 3; k++) rgb3[3 * i + k] = r[k];
     }
+}
+
+// ZSobolDetail::ZSobol (Random.cu:265-425): in px, py, seed, sampleIndex,
+// initialMaxSPP, resMaxBits, dim, size (1..3) -> Next / Next2D / Next3D
+// (out[0..size-1]); the pixel's Morton code is Graphics::MortonCode::Compose2D
+// as RNGGroupZSobol computes it (Random.cu:1180-1190).
+void ref_zsobol(const uint32_t* in8, uint32_t* out3, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const uint32_t* q = in8 + 8 * i;
+        using Graphics::MortonCode::Compose2D;
+        ZSobolDetail::LocalState ls{ .pixelMortonCode = Compose2D<uint64_t>(Vector2ui(q[0], q[1])),
+                                     .sampleIndex = q[3], .seed = q[2] };
+        ZSobolDetail::GlobalState gs{ .initialMaxSPP = q[4], .resMaxBits = q[5] };
+        ZSobolDetail::ZSobol z(ls, gs);
+        uint32_t* o = out3 + 3 * i;
+        o[0] = o[1] = o[2] = 0;
+        if(q[7] == 1) o[0] = z.Next(q[6]);
+        else if(q[7] == 2) { Vector2ui v = z.Next2D(q[6]); o[0] = v[0]; o[1] = v[1]; }
+        else { Vector3ui v = z.Next3D(q[6]); o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; }
+    }
+}
+
+// Per-pixel seeds of the ZSobol group (RNGGroupZSobol ctor, Random.cu:
+// 1175-1200): seed32 = hi ^ lo of the 64-bit seed, then the outputs of
+// std::mt19937(seed32) in pixel order.
+void ref_zsobol_seeds(uint64_t seed, uint32_t count, uint32_t* out)
+{
+    uint32_t seed32 = static_cast<uint32_t>((seed >> 32) ^ (seed & 0xFFFFFFFF));
+    std::mt19937 rng(seed32);
+    for(uint32_t i = 0; i < count; i++) out[i] = uint32_t(rng());
 }
 
 }  // extern "C"

@@ -22,6 +22,8 @@ Covered (MRay file:line):
   pwc            DistributionPwC<2>::SampleUV / PdfUV (Tracer/Distributions.h)
   camera         CameraPinhole + EvaluateRay (Tracer/CamerasDefault.hpp)
   waves          SingleSampleSpectrumWavelength (Tracer/SpectrumContext.cu:9)
+  zsobol         ZSobolDetail::ZSobol Next / Next2D / Next3D (Tracer/Random.cu:265-425)
+                 and the group's per-pixel seeds (Random.cu:1175-1200)
 
 Usage: python tests/golden/make_pt_golden.py
 """
@@ -194,12 +196,26 @@ def waves(rng):
     return {"waves_xi": xi, "waves_out": w, "waves_pdf": p}
 
 
+def zsobol(rng):
+    q = np.zeros((N, 8), np.uint32)
+    q[:, 0] = rng.integers(0, 1920, N)
+    q[:, 1] = rng.integers(0, 1080, N)
+    q[:, 2] = rng.integers(0, 2 ** 32, N, dtype=np.uint64).astype(np.uint32)
+    q[:, 3] = rng.integers(0, 300, N)
+    q[:, 4] = rng.choice([1, 4, 16, 64], N)
+    q[:, 5] = rng.choice([6, 8, 11], N)
+    q[:, 6] = rng.integers(0, 90, N)
+    q[:, 7] = rng.integers(1, 4, N)
+    seeds = ref_pt.zsobol_seeds(0x123456789ABCDEF0, 4096)
+    return {"zs_in": q, "zs_out": ref_pt.zsobol(q), "zs_seed64": np.uint64(0x123456789ABCDEF0), "zs_seeds": seeds}
+
+
 def main():
     if ref_pt.load() is None:
         sys.exit("the MRay source tree and fmt headers are needed (MRAY_REFERENCE_SRC)")
     rng = np.random.default_rng(20261204)
     out = {}
-    for f in (materials, building_blocks, lights, distributions, cameras, waves):
+    for f in (materials, building_blocks, lights, distributions, cameras, waves, zsobol):
         out.update(f(rng))
     path = os.path.join(HERE, "pt_math.npz")
     np.savez_compressed(path, **out)

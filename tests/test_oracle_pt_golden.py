@@ -10,7 +10,8 @@ materials (Tracer/MaterialsDefault.hpp), the BxDF helpers
 (Tracer/Filters.h), the triangle light (Tracer/LightsDefault.hpp), the
 skysphere's lat-long mapping, the PwC2D sampling (Tracer/Distributions.h), the
 pinhole camera (Tracer/CamerasDefault.hpp) and wavelength sampling
-(Tracer/SpectrumContext.cu).  Both sides use the same host C library for sin,
+(Tracer/SpectrumContext.cu), and the ZSobol generator with its per-pixel
+seeds (Tracer/Random.cu).  Both sides use the same host C library for sin,
 cos, log and the like, so there is no tolerance.
 
 Where the MRay tree is present the fixture is also regenerated from MRay's
@@ -98,6 +99,16 @@ def test_camera_matches_mray(g):
 def test_wavelength_sampling_matches_mray(g):
     w, p = oracle.fx_sample_waves(g["waves_xi"])
     assert same(w, g["waves_out"]) and same(p, g["waves_pdf"])
+
+
+def test_zsobol_numbers_and_seeds_match_mray(g):
+    q, want = g["zs_in"], g["zs_out"]
+    for i in range(q.shape[0]):
+        for c in range(int(q[i, 7])):
+            got = oracle.zsobol_number(*(int(x) for x in q[i, :8]), c)
+            assert got == want[i, c], (i, c)
+    seeds = oracle.zsobol_seeds(64, 64, int(g["zs_seed64"]))
+    assert np.array_equal(np.asarray(seeds, np.uint32).ravel(), g["zs_seeds"])
 
 
 # ---- where the MRay tree is present: MRay's code run here -----------------
