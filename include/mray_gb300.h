@@ -67,10 +67,21 @@ typedef struct mrg_meta_hit
     float bary[2];
 } mrg_meta_hit;
 
+/* Triangle test of a context's casts.  MRG_TRI_MOLLER_TRUMBORE (0, the
+ * default) is MRay's Ray::IntersectsTriangle (Source/Core/Ray.hpp:121-167),
+ * bit for bit.  MRG_TRI_WATERTIGHT (1) has no counterpart in the reference:
+ * the watertight test of Woop, Benthin and Wald (JCGT 2013), under which a ray
+ * through an edge shared by two triangles hits one of them; same outputs
+ * (t > 1e-7, MetaHit weights of v0 and v1, back-face culling), but hits can
+ * differ from MRay's on edges and at grazing angles. */
+#define MRG_TRI_MOLLER_TRUMBORE 0u
+#define MRG_TRI_WATERTIGHT      1u
+
 typedef struct mrg_params
 {
     int      device;           /* CUDA device ordinal */
-    uint32_t reserved[7];
+    uint32_t triangle_test;    /* MRG_TRI_* */
+    uint32_t reserved[6];
 } mrg_params;
 
 /* Accelerator figures: BaseAcceleratorI::GPUMemoryUsage, TotalAccelCount,
@@ -390,9 +401,13 @@ mrg_status mrg_cache_gradients(mrg_ctx* ctx, const float* d_inputs, const float*
                                float* h_grad_weights, float* h_grad_table, float* h_loss);
 mrg_status mrg_cache_set_params(mrg_ctx* ctx, const float* h_weights, const float* h_table);
 
-/* Cache-assisted path tracing (RGB; Mueller et al. 2021): params->spp
- * samples per pixel, added to d_image as mrg_pt_render does, every path
- * ending at its second vertex on a cache query of the outgoing radiance.
+/* Cache-assisted path tracing (Mueller et al. 2021): params->spp samples
+ * per pixel, added to d_image as mrg_pt_render does, every path ending at its
+ * second vertex on a cache query of the outgoing radiance.  The cache learns
+ * RGB radiance; with a spectral context (mrg_pt_set_spectral) a path takes the
+ * answer at its 4 wavelengths through the radiance conversion, and its
+ * training targets are its wavelength estimates converted to RGB as the film
+ * converts a sample.
  * About train_paths of each pass's paths (a hashed sparse subset) are training
  * paths instead: they record vertices 1 and 2 and end at vertex 3 on a cache
  * query (self-training); after the pass their (inputs, outgoing radiance)

@@ -69,8 +69,12 @@ class MrgCacheParams(C.Structure):
                 ("aabb", C.c_float * 6)]
 
 
+MRG_TRI_MOLLER_TRUMBORE = 0
+MRG_TRI_WATERTIGHT = 1
+
+
 class MrgParams(C.Structure):
-    _fields_ = [("device", C.c_int), ("reserved", C.c_uint32 * 7)]
+    _fields_ = [("device", C.c_int), ("triangle_test", C.c_uint32), ("reserved", C.c_uint32 * 6)]
 
 
 class MrgAccelStats(C.Structure):

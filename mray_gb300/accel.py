@@ -32,9 +32,13 @@ def _stream_ptr(stream):
 class Accelerator:
     """Two-level 8-wide BVH accelerator on one GPU."""
 
-    def __init__(self, device=0):
+    def __init__(self, device=0, watertight=False):
+        """watertight: the watertight triangle test (Woop, Benthin and Wald
+        2013) instead of MRay's Moller-Trumbore test for every cast of this
+        accelerator."""
         self._lib = N.lib()
-        p = N.MrgParams(device=device)
+        p = N.MrgParams(device=device,
+                        triangle_test=N.MRG_TRI_WATERTIGHT if watertight else N.MRG_TRI_MOLLER_TRUMBORE)
         h = C.c_void_p()
         N.check(self._lib.mrg_create(C.byref(p), C.byref(h)))
         self._h = h

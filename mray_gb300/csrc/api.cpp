@@ -147,6 +147,13 @@ mrg_status mrg_create(const mrg_params* params, mrg_ctx** out)
     mrg_ctx* c = new(std::nothrow) mrg_ctx();
     if(!c) return fail(MRG_ERR_OUT_OF_MEMORY, "mrg_create: host allocation");
     c->device = dev;
+    const uint32_t test = params ? params->triangle_test : MRG_TRI_MOLLER_TRUMBORE;
+    if(test != MRG_TRI_MOLLER_TRUMBORE && test != MRG_TRI_WATERTIGHT)
+    {
+        delete c;
+        return fail(MRG_ERR_INVALID_ARG, "mrg_create: unknown triangle_test");
+    }
+    c->watertight = (test == MRG_TRI_WATERTIGHT);
     DeviceGuard g(dev);
     if((e = cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
        (e = cudaStreamCreateWithFlags(&c->buildStream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -296,6 +303,7 @@ mrg_status mrg_build(mrg_ctx* c)
                 in[mi].count = (uint32_t)(m.idx.size() / 3);
                 in[mi].primKeyBase = m.primKeyBase;
                 in[mi].maxLeaf = leaf_size(in[mi].count);
+                in[mi].rawVerts = c->watertight;
             }
             mrg::BatchResult br;
             const bool ok = mrg::build_wide_bvh_batch(in, br, st, err);
@@ -319,6 +327,7 @@ mrg_status mrg_build(mrg_ctx* c)
                 bi.primKeyBase = m.primKeyBase;
                 bi.maxLeaf = leaf_size(bi.count);
                 bi.ploc = true;
+                bi.rawVerts = c->watertight;
                 mrg::BuildResult b;
                 if(!mrg::build_wide_bvh(bi, b, st, err))
                 {
@@ -440,6 +449,7 @@ mrg_status mrg_build(mrg_ctx* c)
     c->scene.instCount = ni;
     c->scene.nodeCount = (uint32_t)totalNodes;
     c->scene.triCount = (uint32_t)totalTris;
+    c->scene.watertight = c->watertight ? 1u : 0u;
     c->built = true;
     c->buildMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return MRG_OK;

@@ -54,7 +54,7 @@ struct MeshSeg
     uint32_t        primKeyBase;
     uint32_t        maxLeaf;
     float           inflate;
-    uint32_t        pad;
+    uint32_t        rawVerts;   // 1: triangle records hold v0, v1, v2 (watertight test)
 };
 
 // Mesh of sorted leaf position p in a batched build (firsts: nMesh + 1 offsets).
@@ -455,6 +455,7 @@ struct CollapseArgs
     int             kind;
     uint32_t        maxLeaf;
     float           inflate;
+    uint32_t        rawVerts;   // single builds: 1 = records hold v0, v1, v2
     // outputs
     WideNode*       wnodes;
     TriRecord*      tris;
@@ -500,11 +501,12 @@ __device__ __forceinline__ void emit_payload(const CollapseArgs& a, uint32_t lea
     const float* pos = a.pos;
     const uint32_t* idx = a.idx;
     uint32_t keyBase = a.primKeyBase;
+    uint32_t raw = a.rawVerts;
     if(a.segs)
     {
         const MeshSeg& m = a.segs[mesh];
         prim -= m.first;
-        pos = m.pos; idx = m.idx; keyBase = m.primKeyBase;
+        pos = m.pos; idx = m.idx; keyBase = m.primKeyBase; raw = m.rawVerts;
     }
     uint32_t i0 = idx[3 * prim], i1 = idx[3 * prim + 1], i2 = idx[3 * prim + 2];
     float v0x = pos[3 * i0], v0y = pos[3 * i0 + 1], v0z = pos[3 * i0 + 2];
@@ -512,8 +514,17 @@ __device__ __forceinline__ void emit_payload(const CollapseArgs& a, uint32_t lea
     float v2x = pos[3 * i2], v2y = pos[3 * i2 + 1], v2z = pos[3 * i2 + 2];
     TriRecord r;
     r.v0 = make_float4(v0x, v0y, v0z, __uint_as_float(keyBase + prim));
-    r.e0 = make_float4(__fsub_rn(v1x, v0x), __fsub_rn(v1y, v0y), __fsub_rn(v1z, v0z), 0.0f);
-    r.e1 = make_float4(__fsub_rn(v2x, v0x), __fsub_rn(v2y, v0y), __fsub_rn(v2z, v0z), 0.0f);
+    if(raw)
+    {
+        // the watertight test reads the shared vertices themselves
+        r.e0 = make_float4(v1x, v1y, v1z, 0.0f);
+        r.e1 = make_float4(v2x, v2y, v2z, 0.0f);
+    }
+    else
+    {
+        r.e0 = make_float4(__fsub_rn(v1x, v0x), __fsub_rn(v1y, v0y), __fsub_rn(v1z, v0z), 0.0f);
+        r.e1 = make_float4(__fsub_rn(v2x, v0x), __fsub_rn(v2y, v0y), __fsub_rn(v2z, v0z), 0.0f);
+    }
     a.tris[dst] = r;
 }
 
@@ -919,6 +930,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     ca.nodes = dNodes; ca.nodeBoxes = dNodeBoxes; ca.leafBoxes = dLeafBoxes;
     ca.sortedIds = vb.Current(); ca.pos = in.pos; ca.idx = in.idx;
     ca.primKeyBase = in.primKeyBase; ca.kind = in.kind; ca.maxLeaf = in.maxLeaf;
+    ca.rawVerts = in.rawVerts ? 1u : 0u;
     ca.inflate = ext * 1.0e-5f + 1.0e-30f;
     ca.wnodes = dW; ca.tris = out.tris; ca.leafIds = out.leafIds; ca.counters = dCounters;
     ca.leafCount = n; ca.wideCap = wideCap;
@@ -979,7 +991,7 @@ bool build_wide_bvh_batch(const std::vector<BatchMeshInput>& meshes, BatchResult
         if(in.count == 0 || !in.pos || !in.idx) { err = "empty mesh in batch"; return false; }
         firsts[m] = (uint32_t)total;
         segs[m] = MeshSeg{ in.pos, in.idx, (uint32_t)total, in.count, in.primKeyBase,
-                           std::min(3u, std::max(1u, in.maxLeaf)), 0.0f, 0u };
+                           std::min(3u, std::max(1u, in.maxLeaf)), 0.0f, in.rawVerts ? 1u : 0u };
         total += in.count;
         if(total >= (1ull << 31)) { err = "batch larger than 2^31 triangles"; return false; }
     }
@@ -1096,7 +1108,7 @@ bool build_wide_bvh_batch(const std::vector<BatchMeshInput>& meshes, BatchResult
     ca.segs = dSegs;
     ca.nodes = dNodes; ca.nodeBoxes = dNodeBoxes; ca.leafBoxes = dLeafBoxes;
     ca.sortedIds = vb.Current(); ca.pos = nullptr; ca.idx = nullptr;
-    ca.primKeyBase = 0; ca.kind = 0; ca.maxLeaf = 3; ca.inflate = 0.0f;
+    ca.primKeyBase = 0; ca.kind = 0; ca.maxLeaf = 3; ca.inflate = 0.0f; ca.rawVerts = 0u;
     ca.wnodes = dW; ca.tris = out.tris; ca.leafIds = nullptr; ca.counters = dCounters;
     ca.leafCount = n; ca.wideCap = wideCap;
     hostCounters[0] = M; hostCounters[1] = 0; hostCounters[2] = 0; hostCounters[3] = 0;

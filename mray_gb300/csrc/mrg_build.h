@@ -32,6 +32,7 @@ struct BuildInput
     uint32_t        primKeyBase = 0;
     uint32_t        maxLeaf = 3;       // primitives per leaf child (<= 3)
     bool            ploc = false;      // PLOC clustering instead of the Karras radix tree
+    bool            rawVerts = false;  // triangle records hold v0, v1, v2 (watertight test)
 };
 
 struct BuildResult
@@ -57,6 +58,7 @@ struct BatchMeshInput
     uint32_t        count = 0;         // triangles (>= 1)
     uint32_t        primKeyBase = 0;
     uint32_t        maxLeaf = 3;       // triangles per leaf child (<= 3)
+    bool            rawVerts = false;  // triangle records hold v0, v1, v2 (watertight test)
 };
 
 struct BatchResult
@@ -84,6 +86,7 @@ struct TraceScene
     uint32_t          instCount = 0;
     uint32_t          nodeCount = 0;       // bounds for every index read from the tree
     uint32_t          triCount = 0;
+    uint32_t          watertight = 0;      // 1: records hold v0, v1, v2; the watertight test runs
 };
 
 struct TraceScratch

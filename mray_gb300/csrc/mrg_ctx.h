@@ -32,6 +32,7 @@ struct mrg_ctx
 {
     int device = 0;
     int smCount = 0;
+    bool watertight = false;          // triangle test: watertight instead of MRay's Moller-Trumbore
     cudaStream_t buildStream = nullptr;
 
     struct Mesh

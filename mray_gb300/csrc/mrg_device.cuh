@@ -121,6 +121,63 @@ __device__ __forceinline__ bool intersect_tri_exact(const float3& o, const float
     return true;
 }
 
+// Watertight ray/triangle test (S. Woop, C. Benthin, I. Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013), the opt-in alternative to
+// MRay's Moller-Trumbore test.  The ray is sheared to run along +z; the
+// triangle's scaled barycentrics are 2D edge functions of the sheared
+// vertices, so two triangles sharing an edge evaluate it from the same two
+// vertices and a ray through the edge hits one of them.  Edge functions that
+// round to exactly 0 are recomputed in double.  The record holds the three
+// vertices (v0, v1 = e0 slot, v2 = e1 slot).  Same outputs as the MT test:
+// t > SmallEpsilon, (u, v) = weights of v1 and v2, back faces where MT's
+// determinant is negative; the MetaHit pair is (U, V) / det, both computed.
+// IEEE round-to-nearest operations only, in the oracle's order
+// (orc_intersect_triangle_wt).
+__device__ __forceinline__ bool intersect_tri_watertight(const float3& o, const float3& d,
+                                                         const float4& v0, const float4& v1,
+                                                         const float4& v2, bool cull,
+                                                         float& tOut, float& uOut, float& wOut)
+{
+    const float dd[3] = { d.x, d.y, d.z };
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    const int kz = (ax >= ay) ? ((ax >= az) ? 0 : 2) : ((ay >= az) ? 1 : 2);
+    int kx = (kz == 2) ? 0 : kz + 1;
+    int ky = (kx == 2) ? 0 : kx + 1;
+    if(dd[kz] < 0.0f) { const int t = kx; kx = ky; ky = t; }
+    const float Sx = __fdiv_rn(dd[kx], dd[kz]), Sy = __fdiv_rn(dd[ky], dd[kz]);
+    const float Sz = __frcp_rn(dd[kz]);
+    const float A[3] = { __fsub_rn(v0.x, o.x), __fsub_rn(v0.y, o.y), __fsub_rn(v0.z, o.z) };
+    const float B[3] = { __fsub_rn(v1.x, o.x), __fsub_rn(v1.y, o.y), __fsub_rn(v1.z, o.z) };
+    const float C[3] = { __fsub_rn(v2.x, o.x), __fsub_rn(v2.y, o.y), __fsub_rn(v2.z, o.z) };
+    const float Ax = __fsub_rn(A[kx], __fmul_rn(Sx, A[kz])), Ay = __fsub_rn(A[ky], __fmul_rn(Sy, A[kz]));
+    const float Bx = __fsub_rn(B[kx], __fmul_rn(Sx, B[kz])), By = __fsub_rn(B[ky], __fmul_rn(Sy, B[kz]));
+    const float Cx = __fsub_rn(C[kx], __fmul_rn(Sx, C[kz])), Cy = __fsub_rn(C[ky], __fmul_rn(Sy, C[kz]));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if(U == 0.0f || V == 0.0f || W == 0.0f)
+    {
+        U = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx)));
+        V = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx)));
+        W = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax)));
+    }
+    const bool allNeg = (U <= 0.0f && V <= 0.0f && W <= 0.0f);
+    const bool allPos = (U >= 0.0f && V >= 0.0f && W >= 0.0f);
+    if(!allNeg && !allPos) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if(det == 0.0f) return false;
+    if(cull && det < 0.0f) return false;
+    const float Az = __fmul_rn(Sz, A[kz]), Bz = __fmul_rn(Sz, B[kz]), Cz = __fmul_rn(Sz, C[kz]);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    const float rcp = __frcp_rn(det);
+    const float t = __fmul_rn(T, rcp);
+    if(t <= kSmallEpsilon) return false;
+    tOut = t;
+    uOut = __fmul_rn(V, rcp);      // weight of v1 (MRay's b0, MetaHit[1])
+    wOut = __fmul_rn(U, rcp);      // weight of v0 (MetaHit[0], computed, not 1 - u - v)
+    return true;
+}
+
 // Matrix3x4::TransformRay (Source/Core/Matrix.hpp:906-913) with the inverse.
 __device__ __forceinline__ void transform_ray_exact(const float4 r0, const float4 r1,
                                                     const float4 r2,

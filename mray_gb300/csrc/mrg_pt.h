@@ -193,12 +193,16 @@ cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSceneTabl
                           uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st);
 cudaError_t pt_work_keys(const PtPaths& P, const PtSurface* surfaces, uint32_t nSurfaces,
                          const uint32_t* aliveList, const uint32_t* aliveCount, int smCount, cudaStream_t st);
-// rad[slot] += thr[slot] * queryOut[slot] for the queried slots.
-cudaError_t pt_cache_apply(const PtPaths& P, const PtCacheUse& C, int smCount, cudaStream_t st);
+// rad[slot] += thr[slot] * queryOut[slot] for the queried slots (a
+// spectral path takes the RGB answer at its wavelengths).
+cudaError_t pt_cache_apply(const PtPaths& P, const PtCacheUse& C, const PtSpectral& S, int smCount,
+                           cudaStream_t st);
 // Training batch from the records of a pass: target = (final radiance -
-// radiance before) / throughput, valid records compacted (at most batchCap).
-cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t slots, float4* batchIn,
-                             float4* batchTarget, uint32_t* batchCount, int smCount, cudaStream_t st);
+// radiance before) / throughput (in RGB; spectral estimates converted as the
+// film converts them), valid records compacted (at most batchCap).
+cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, const PtSpectral& S, uint32_t slots,
+                             float4* batchIn, float4* batchTarget, uint32_t* batchCount, int smCount,
+                             cudaStream_t st);
 cudaError_t pt_resolve(const PtLaunch& L, const PtPaths& P, const PtLight* lights, uint32_t depth, int smCount,
                        cudaStream_t st);
 // out[i] += acc[i] (f32 from the FP64 emission-gradient sums), n entries.

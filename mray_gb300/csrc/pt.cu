@@ -1039,8 +1039,10 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                     {
                         const size_t rec = (size_t)i * L.cache.recPerPath + (depth - 1u);
                         cache_inputs(L.cache.recIn + 4 * rec, pos, crough, wo, nrm, a3);
-                        L.cache.recAux[2 * rec] = make_float4(thr.v[0], thr.v[1], thr.v[2], 1.0f);
-                        L.cache.recAux[2 * rec + 1] = make_float4(rad.v[0], rad.v[1], rad.v[2], 0.0f);
+                        // throughput and radiance so far: RGB (w = 1 marks the record),
+                        // or the 4 wavelengths (a zero marks nothing to learn from)
+                        L.cache.recAux[2 * rec] = make_float4(thr.v[0], thr.v[1], thr.v[2], SPEC ? thr.v[3] : 1.0f);
+                        L.cache.recAux[2 * rec + 1] = make_float4(rad.v[0], rad.v[1], rad.v[2], SPEC ? rad.v[3] : 0.0f);
                     }
                     const bool terminal = (CM == 1) && depth == (trainer ? L.cache.recPerPath + 1u : 1u);
                     if(terminal)
@@ -1301,8 +1303,12 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
     if(ADJ && L.adj.gradEmission) emis_flush(emis, L.adj.gradEmission);
 }
 
+// The cache's RGB radiance, times the path's throughput, ends the path.  A
+// spectral path takes it at its 4 wavelengths through the radiance
+// conversion that emission uses.
+template<bool SPEC>
 __global__ void __launch_bounds__(kPtTPB)
-k_cache_apply(PtPaths P, PtCacheUse C)
+k_cache_apply(PtPaths P, PtCacheUse C, PtSpectral S)
 {
     const uint32_t n = *C.queryCount;
     for(uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
@@ -1310,15 +1316,24 @@ k_cache_apply(PtPaths P, PtCacheUse C)
         const uint32_t i = C.queryList[k];
         const float4 q = C.queryOut[i], t = P.thr[i];
         float4 r = P.rad[i];
-        r.x = add(r.x, mul(t.x, fmaxf(q.x, 0.0f)));
-        r.y = add(r.y, mul(t.y, fmaxf(q.y, 0.0f)));
-        r.z = add(r.z, mul(t.z, fmaxf(q.z, 0.0f)));
+        const Chan lc = radiance_of<SPEC>(S, fmaxf(q.x, 0.0f), fmaxf(q.y, 0.0f), fmaxf(q.z, 0.0f),
+                                          SPEC ? P.waves[i] : make_float4(0, 0, 0, 0));
+        r.x = add(r.x, mul(t.x, lc.v[0]));
+        r.y = add(r.y, mul(t.y, lc.v[1]));
+        r.z = add(r.z, mul(t.z, lc.v[2]));
+        if(SPEC) r.w = add(r.w, mul(t.w, lc.v[3]));
         P.rad[i] = r;
     }
 }
 
+// Training targets: the radiance the path gathered after a recorded vertex,
+// over the throughput up to it.  A spectral path's 4-wavelength estimate is
+// turned into RGB as the film turns a sample (divided by the wavelength
+// pdfs, through the observer), an unbiased RGB target.
+template<bool SPEC>
 __global__ void __launch_bounds__(kPtTPB)
-k_cache_targets(PtPaths P, PtCacheUse C, uint32_t paths, float4* batchIn, float4* batchTarget, uint32_t* batchCount)
+k_cache_targets(PtPaths P, PtCacheUse C, PtSpectral S, uint32_t paths, float4* batchIn, float4* batchTarget,
+                uint32_t* batchCount)
 {
     const uint32_t total = paths * C.recPerPath;
     const uint32_t first = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
@@ -1330,11 +1345,18 @@ k_cache_targets(PtPaths P, PtCacheUse C, uint32_t paths, float4* batchIn, float4
         if(r < total)
         {
             const float4 th = C.recAux[2 * (size_t)r], before = C.recAux[2 * (size_t)r + 1];
-            if(th.w != 0.0f && th.x > 0.0f && th.y > 0.0f && th.z > 0.0f)
+            if(th.w > 0.0f && th.x > 0.0f && th.y > 0.0f && th.z > 0.0f)
             {
-                const float4 tot = P.rad[r / C.recPerPath];
+                const uint32_t path = r / C.recPerPath;
+                const float4 tot = P.rad[path];
                 tgt = make_float4(__fdiv_rn(sub(tot.x, before.x), th.x), __fdiv_rn(sub(tot.y, before.y), th.y),
                                   __fdiv_rn(sub(tot.z, before.z), th.z), 0.0f);
+                if(SPEC)
+                {
+                    tgt.w = __fdiv_rn(sub(tot.w, before.w), th.w);
+                    const float3 rgb = spectrum_to_rgb(S, tgt, P.waves[path], P.wavePdf[path]);
+                    tgt = make_float4(rgb.x, rgb.y, rgb.z, 0.0f);
+                }
                 ok = isfinite(tgt.x) && isfinite(tgt.y) && isfinite(tgt.z);
             }
         }
@@ -1463,7 +1485,9 @@ cudaError_t pt_shade_impl(const PtLaunch& L, const PtPaths& P, const PtSceneTabl
                           uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st)
 {
     const unsigned grid = (unsigned)smCount * 8u;
-    if(L.cache.mode == 1u)
+    if(L.cache.mode == 1u && L.spec.enabled)
+        k_shade<true, false, 1><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
+    else if(L.cache.mode == 1u)
         k_shade<false, false, 1><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
     else if(L.adj.enabled)
         k_shade<false, true, 0><<<grid, kPtTPB, 0, st>>>(L, P, T, aliveList, aliveCount, nextList, nextCount);
@@ -1481,16 +1505,24 @@ cudaError_t pt_work_keys(const PtPaths& P, const PtSurface* surfaces, uint32_t n
     return cudaGetLastError();
 }
 
-cudaError_t pt_cache_apply(const PtPaths& P, const PtCacheUse& C, int smCount, cudaStream_t st)
+cudaError_t pt_cache_apply(const PtPaths& P, const PtCacheUse& C, const PtSpectral& S, int smCount,
+                           cudaStream_t st)
 {
-    k_cache_apply<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C);
+    if(S.enabled) k_cache_apply<true><<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C, S);
+    else k_cache_apply<false><<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C, S);
     return cudaGetLastError();
 }
 
-cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, uint32_t slots, float4* batchIn,
-                             float4* batchTarget, uint32_t* batchCount, int smCount, cudaStream_t st)
+cudaError_t pt_cache_targets(const PtPaths& P, const PtCacheUse& C, const PtSpectral& S, uint32_t slots,
+                             float4* batchIn, float4* batchTarget, uint32_t* batchCount, int smCount,
+                             cudaStream_t st)
 {
-    k_cache_targets<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C, slots, batchIn, batchTarget, batchCount);
+    if(S.enabled)
+        k_cache_targets<true><<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C, S, slots, batchIn, batchTarget,
+                                                                           batchCount);
+    else
+        k_cache_targets<false><<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(P, C, S, slots, batchIn, batchTarget,
+                                                                            batchCount);
     return cudaGetLastError();
 }
 

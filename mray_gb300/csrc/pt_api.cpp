@@ -814,7 +814,6 @@ mrg_status mrg_pt_render_cached(mrg_ctx* c, const mrg_pt_params* p, float* dImag
 {
     if(!c || !p || !dImage) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render_cached: null pointer");
     if(!c->cacheOn) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_pt_render_cached: call mrg_cache_create first");
-    if(c->ptSpec.enabled) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render_cached: RGB rendering only");
     constexpr uint32_t kRec = 2;
     DevGuard g(c->device);
     PtRun R;
@@ -864,10 +863,10 @@ mrg_status mrg_pt_render_cached(mrg_ctx* c, const mrg_pt_params* p, float* dImag
         PT_TRY(pt_bounces(c, R, lane), "cached pass");
         PT_TRY(mrg::nrc_query_list(c->cache, C.queryIn, C.queryList, C.queryCount, R.slots, C.queryOut, c->smCount, st),
                "cache query");
-        PT_TRY(mrg::pt_cache_apply(P, C, c->smCount, st), "cache apply");
+        PT_TRY(mrg::pt_cache_apply(P, C, R.L.spec, c->smCount, st), "cache apply");
         if(C.trainStride)
         {
-            PT_TRY(mrg::pt_cache_targets(P, C, R.slots, batchIn, batchTarget, counters + 1, c->smCount, st),
+            PT_TRY(mrg::pt_cache_targets(P, C, R.L.spec, R.slots, batchIn, batchTarget, counters + 1, c->smCount, st),
                    "training targets");
             PT_TRY(mrg::nrc_train(c->cache, batchIn, batchTarget, counters + 1, (uint32_t)cap, c->smCount, st),
                    "cache training");

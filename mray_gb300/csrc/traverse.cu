@@ -44,6 +44,12 @@ namespace {
 #ifndef MRG_TRACE_SMEM_STACK
 #define MRG_TRACE_SMEM_STACK 0       // >0: the first entries of each thread's stack live in shared memory
 #endif
+#ifndef MRG_NODE_OCTLOAD
+#define MRG_NODE_OCTLOAD 0           // 1: near / far plane vectors loaded by the ray's octant, not selected
+#endif
+#ifndef MRG_NODE_SIGNHIT
+#define MRG_NODE_SIGNHIT 0           // 1: child hit from the sign of tf - tn (FMA pipe) instead of a compare
+#endif
 #ifndef MRG_TRACE_TRI_CHUNK
 #define MRG_TRACE_TRI_CHUNK 2        // >0: at most this many triangles per iteration, the rest go on the stack
 #endif
@@ -246,9 +252,20 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
     const uint4* np = reinterpret_cast<const uint4*>(nodes + ni);
     const uint4 a = __ldg(np + 0);
     const uint4 b = __ldg(np + 1);
+#if MRG_NODE_OCTLOAD
+    // The six 8-byte plane vectors as uint2 [lo_x, lo_y, lo_z, hi_x, hi_y,
+    // hi_z]; the near / far vector of each axis is addressed by the ray's
+    // octant instead of selected after loading.
+    const uint2* qv = reinterpret_cast<const uint2*>(np + 2);
+    const uint32_t nxi = (r.oct7 & 1u) ? 0u : 3u, nyi = (r.oct7 & 2u) ? 1u : 4u, nzi = (r.oct7 & 4u) ? 2u : 5u;
+    const uint2 vnX = __ldg(qv + nxi), vfX = __ldg(qv + (3u - nxi));
+    const uint2 vnY = __ldg(qv + nyi), vfY = __ldg(qv + (5u - nyi));
+    const uint2 vnZ = __ldg(qv + nzi), vfZ = __ldg(qv + (7u - nzi));
+#else
     const uint4 q0 = __ldg(np + 2);
     const uint4 q1 = __ldg(np + 3);
     const uint4 q2 = __ldg(np + 4);
+#endif
     const uint32_t packed = a.w;
     const float sx = __uint_as_float((packed & 0xFFu) << 23) * r.ix;
     const float sy = __uint_as_float(((packed >> 8) & 0xFFu) << 23) * r.iy;
@@ -269,17 +286,25 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
     // q0 = lo_x[0..3], lo_x[4..7], lo_y[0..3], lo_y[4..7]
     // q1 = lo_z[0..3], lo_z[4..7], hi_x[0..3], hi_x[4..7]
     // q2 = hi_y[0..3], hi_y[4..7], hi_z[0..3], hi_z[4..7]
-    const bool nx = !(r.oct7 & 1u), ny = !(r.oct7 & 2u), nz = !(r.oct7 & 4u);
     uint32_t hm = 0;
+#if !MRG_NODE_OCTLOAD
+    const bool nx = !(r.oct7 & 1u), ny = !(r.oct7 & 2u), nz = !(r.oct7 & 4u);
+#endif
 #pragma unroll
     for(uint32_t h = 0; h < 2; h++)
     {
+#if MRG_NODE_OCTLOAD
+        const uint32_t nearX = h ? vnX.y : vnX.x, farX = h ? vfX.y : vfX.x;
+        const uint32_t nearY = h ? vnY.y : vnY.x, farY = h ? vfY.y : vfY.x;
+        const uint32_t nearZ = h ? vnZ.y : vnZ.x, farZ = h ? vfZ.y : vfZ.x;
+#else
         const uint32_t loX = h ? q0.y : q0.x, hiX = h ? q1.w : q1.z;
         const uint32_t loY = h ? q0.w : q0.z, hiY = h ? q2.y : q2.x;
         const uint32_t loZ = h ? q1.y : q1.x, hiZ = h ? q2.w : q2.z;
         const uint32_t nearX = nx ? hiX : loX, farX = nx ? loX : hiX;
         const uint32_t nearY = ny ? hiY : loY, farY = ny ? loY : hiY;
         const uint32_t nearZ = nz ? hiZ : loZ, farZ = nz ? loZ : hiZ;
+#endif
         // meta byte: internal = 0b001_11sss (24 + slot), leaf = unary count << 5 | offset,
         // empty = 0.  For internal children xor the slot bits with oct7.
         const uint32_t meta4 = h ? b.w : b.z;
@@ -332,7 +357,17 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
             const float tf = fminf(min3f(tfx, tfy, tfz), tmax);
             const uint32_t cb = (bits4 >> (8u * k)) & 0xFFu;
             const uint32_t bi = (bitIdx4 >> (8u * k)) & 0xFFu;
+#if MRG_NODE_SIGNHIT
+            // tn <= tf as the sign of tf - tn (the subtraction runs on the FMA
+            // pipe; the all-ones / zero mask from an arithmetic shift then
+            // merges into the hit mask in one logic op).  tf - tn is -0 only
+            // for tf = -0 <= tn = +0, a box that ends at t = 0 and holds no
+            // hit with t > 1e-7.
+            const int32_t miss = __float_as_int(__fsub_rn(tf, tn)) >> 31;
+            hm |= (cb << bi) & ~(uint32_t)miss;
+#else
             hm |= (tn <= tf) ? (cb << bi) : 0u;
+#endif
         }
 #endif
     }
@@ -343,7 +378,8 @@ __device__ __forceinline__ uint32_t intersect_node(const WideNode* __restrict__ 
 
 // LOCAL: listed ray i starts inside instance instIds[i] (its BLAS, in the
 // instance's space) and ends when that BLAS is exhausted: CastLocalRays.
-template<bool ANY, bool STATS, bool LOCAL = false>
+// WT: the watertight triangle test on records that hold the three vertices.
+template<bool ANY, bool STATS, bool LOCAL = false, bool WT = false>
 __global__ void __launch_bounds__(kTraceTPB, MRG_TRACE_MIN_BLOCKS)
 k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
         const uint32_t* __restrict__ rayIdx, uint32_t nHost, const uint32_t* __restrict__ nDevice,
@@ -530,8 +566,11 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
                     const float4 v0 = __ldg(tp), e0 = __ldg(tp + 1), e1 = __ldg(tp + 2);
                     if(STATS) statTris++;
                     float t, u, v;
-                    if(intersect_tri_exact(make_float3(lr.ox, lr.oy, lr.oz), ld, v0, e0, e1, cull, t, u, v) &&
-                       t >= tmin && t < tmax)
+                    const bool isect = WT ? intersect_tri_watertight(make_float3(lr.ox, lr.oy, lr.oz), ld, v0, e0, e1,
+                                                                     cull, t, u, v)
+                                          : intersect_tri_exact(make_float3(lr.ox, lr.oy, lr.oz), ld, v0, e0, e1,
+                                                                cull, t, u, v);
+                    if(isect && t >= tmin && t < tmax)
                     {
                         tmax = t; hitU = u; hitV = v;
                         hitPrim = __float_as_uint(v0.w);
@@ -641,7 +680,8 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
             {
                 const uint4 keys = __ldg(reinterpret_cast<const uint4*>(sc.insts + hitInst) + 3);
                 hits[ri] = make_uint4(hitPrim, keys.x, keys.y, keys.z);
-                const float w = __fsub_rn(__fsub_rn(1.0f, hitU), hitV);
+                // MT: (1 - u - v, u) as MRay forms it; WT: both weights computed
+                const float w = WT ? hitV : __fsub_rn(__fsub_rn(1.0f, hitU), hitV);
                 meta[ri] = make_float2(w, hitU);
                 reinterpret_cast<float*>(rays)[8 * (size_t)ri + 7] = tmax;
             }
@@ -649,7 +689,7 @@ k_trace(TraceScene sc, TraceScratch scr, float4* __restrict__ rays,
     }
 }
 
-template<bool ANY, bool STATS, bool LOCAL = false>
+template<bool ANY, bool STATS, bool LOCAL = false, bool WT = false>
 int blocks_for(int smCount)
 {
     static int perSMOf[kMaxDevices] = {};          // 0: not queried on that device yet
@@ -657,7 +697,7 @@ int blocks_for(int smCount)
     if(perSM == 0)
     {
         int b = 0;
-        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<ANY, STATS, LOCAL>, kTraceTPB, 0) != cudaSuccess ||
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<ANY, STATS, LOCAL, WT>, kTraceTPB, 0) != cudaSuccess ||
            b < 1)
             b = 4;
         perSM = b;
@@ -680,9 +720,14 @@ cudaError_t launch_closest(const TraceScene& sc, const TraceScratch& scr, void* 
     if(n == 0 && nDevice == nullptr) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(scr.workCounter, 0, sizeof(uint32_t), st);
     if(e != cudaSuccess) return e;
-    k_trace<false, false><<<blocks_for<false, false>(smCount), kTraceTPB, 0, st>>>(
-        sc, scr, static_cast<float4*>(rays), rayIdx, n, nDevice, static_cast<uint4*>(hits),
-        static_cast<float2*>(meta), nullptr);
+    if(sc.watertight)
+        k_trace<false, false, false, true><<<blocks_for<false, false, false, true>(smCount), kTraceTPB, 0, st>>>(
+            sc, scr, static_cast<float4*>(rays), rayIdx, n, nDevice, static_cast<uint4*>(hits),
+            static_cast<float2*>(meta), nullptr);
+    else
+        k_trace<false, false><<<blocks_for<false, false>(smCount), kTraceTPB, 0, st>>>(
+            sc, scr, static_cast<float4*>(rays), rayIdx, n, nDevice, static_cast<uint4*>(hits),
+            static_cast<float2*>(meta), nullptr);
     return cudaGetLastError();
 }
 
@@ -692,9 +737,14 @@ cudaError_t launch_local(const TraceScene& sc, const TraceScratch& scr, void* ra
     if(n == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(scr.workCounter, 0, sizeof(uint32_t), st);
     if(e != cudaSuccess) return e;
-    k_trace<false, false, true><<<blocks_for<false, false, true>(smCount), kTraceTPB, 0, st>>>(
-        sc, scr, static_cast<float4*>(rays), rayIdx, n, nullptr, static_cast<uint4*>(hits),
-        static_cast<float2*>(meta), nullptr, instIds);
+    if(sc.watertight)
+        k_trace<false, false, true, true><<<blocks_for<false, false, true, true>(smCount), kTraceTPB, 0, st>>>(
+            sc, scr, static_cast<float4*>(rays), rayIdx, n, nullptr, static_cast<uint4*>(hits),
+            static_cast<float2*>(meta), nullptr, instIds);
+    else
+        k_trace<false, false, true><<<blocks_for<false, false, true>(smCount), kTraceTPB, 0, st>>>(
+            sc, scr, static_cast<float4*>(rays), rayIdx, n, nullptr, static_cast<uint4*>(hits),
+            static_cast<float2*>(meta), nullptr, instIds);
     return cudaGetLastError();
 }
 
@@ -705,9 +755,14 @@ cudaError_t launch_visibility(const TraceScene& sc, const TraceScratch& scr, uin
     if(n == 0 && nDevice == nullptr) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(scr.workCounter, 0, sizeof(uint32_t), st);
     if(e != cudaSuccess) return e;
-    k_trace<true, false><<<blocks_for<true, false>(smCount), kTraceTPB, 0, st>>>(
-        sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), rayIdx, n, nDevice, nullptr,
-        nullptr, visBits);
+    if(sc.watertight)
+        k_trace<true, false, false, true><<<blocks_for<true, false, false, true>(smCount), kTraceTPB, 0, st>>>(
+            sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), rayIdx, n, nDevice, nullptr,
+            nullptr, visBits);
+    else
+        k_trace<true, false><<<blocks_for<true, false>(smCount), kTraceTPB, 0, st>>>(
+            sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), rayIdx, n, nDevice, nullptr,
+            nullptr, visBits);
     return cudaGetLastError();
 }
 
@@ -719,9 +774,14 @@ cudaError_t launch_closest_stats(const TraceScene& sc, const TraceScratch& scr, 
     if(e != cudaSuccess) return e;
     e = cudaMemsetAsync(scr.stats, 0, 8 * sizeof(unsigned long long), st);
     if(e != cudaSuccess) return e;
-    k_trace<false, true><<<blocks_for<false, true>(smCount), kTraceTPB, 0, st>>>(
-        sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), nullptr, n, nullptr, nullptr,
-        nullptr, nullptr);
+    if(sc.watertight)
+        k_trace<false, true, false, true><<<blocks_for<false, true, false, true>(smCount), kTraceTPB, 0, st>>>(
+            sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), nullptr, n, nullptr, nullptr,
+            nullptr, nullptr);
+    else
+        k_trace<false, true><<<blocks_for<false, true>(smCount), kTraceTPB, 0, st>>>(
+            sc, scr, const_cast<float4*>(static_cast<const float4*>(rays)), nullptr, n, nullptr, nullptr,
+            nullptr, nullptr);
     return cudaGetLastError();
 }
 

@@ -42,6 +42,9 @@ def lib():
         L.orc_morton3d_u64.argtypes = [u32, u32, u32]
         L.orc_morton3d_u64.restype = C.c_uint64
         L.orc_nudge.argtypes = [vp, vp, vp]
+        L.orc_scene_set_watertight.argtypes = [vp, C.c_int]
+        L.orc_intersect_triangle_wt.argtypes = [vp] * 5 + [C.c_int, vp, vp, vp]
+        L.orc_intersect_triangle_wt.restype = C.c_int
         L.orc_scene_create.restype = vp
         L.orc_scene_destroy.argtypes = [vp]
         L.orc_scene_add_mesh.argtypes = [vp, vp, u32, vp, u32, u32]
@@ -100,10 +103,14 @@ def default_threads():
 class Scene:
     """Two-level LBVH scene with MRay host-backend semantics."""
 
-    def __init__(self):
+    def __init__(self, watertight=False):
+        """watertight: the restatement's watertight triangle test instead of
+        MRay's Moller-Trumbore test for every mesh."""
         self._L = lib()
         self._h = self._L.orc_scene_create()
         self._keep = []
+        if watertight:
+            self._L.orc_scene_set_watertight(self._h, 1)
 
     def __del__(self):
         try:

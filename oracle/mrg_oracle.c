@@ -96,6 +96,64 @@ int orc_intersect_triangle(const float dir[3], const float pos[3],
 }
 
 /* ------------------------------------------------------------------------ */
+/* Watertight ray/triangle test (S. Woop, C. Benthin, I. Wald, "Watertight   */
+/* Ray/Triangle Intersection", JCGT 2(1), 2013): the ray is sheared so that   */
+/* it runs along +z through the origin, and the triangle's scaled barycentric */
+/* coordinates are 2D edge functions of the sheared vertices.  Two triangles */
+/* that share an edge evaluate that edge's function from the same two        */
+/* vertices, so a ray through the edge cannot miss both.  Edge functions that */
+/* come out exactly 0 in float are recomputed in double.  The project's       */
+/* opt-in alternative to MRay's Moller-Trumbore test: same outputs (MRay's   */
+/* barycentric order, backface flag, t > SmallEpsilon), no epsilon on the    */
+/* determinant.  Plain IEEE operations only (no fma).                        */
+/* ------------------------------------------------------------------------ */
+int orc_intersect_triangle_wt(const float dir[3], const float pos[3],
+                              const float v0[3], const float v1[3], const float v2[3],
+                              int cull, float bary_out[3], float* t_out, int* backface_out)
+{
+    /* largest direction component (first on ties), then the winding-keeping
+     * order of the other two */
+    float ax = fabsf(dir[0]), ay = fabsf(dir[1]), az = fabsf(dir[2]);
+    int kz = (ax >= ay) ? ((ax >= az) ? 0 : 2) : ((ay >= az) ? 1 : 2);
+    int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+    if(dir[kz] < 0.0f) { int t = kx; kx = ky; ky = t; }
+    float Sx = dir[kx] / dir[kz], Sy = dir[ky] / dir[kz], Sz = 1.0f / dir[kz];
+
+    float A[3] = { v0[0] - pos[0], v0[1] - pos[1], v0[2] - pos[2] };
+    float B[3] = { v1[0] - pos[0], v1[1] - pos[1], v1[2] - pos[2] };
+    float C[3] = { v2[0] - pos[0], v2[1] - pos[1], v2[2] - pos[2] };
+    float Ax = A[kx] - Sx * A[kz], Ay = A[ky] - Sy * A[kz];
+    float Bx = B[kx] - Sx * B[kz], By = B[ky] - Sy * B[kz];
+    float Cx = C[kx] - Sx * C[kz], Cy = C[ky] - Sy * C[kz];
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if(U == 0.0f || V == 0.0f || W == 0.0f)
+    {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    int allNeg = (U <= 0.0f && V <= 0.0f && W <= 0.0f);
+    int allPos = (U >= 0.0f && V >= 0.0f && W >= 0.0f);
+    if(!allNeg && !allPos) return 0;
+    float det = U + V + W;
+    if(det == 0.0f) return 0;
+    /* front face: the side MRay's Moller-Trumbore calls front (its det > 0) */
+    int backfaceHit = (det < 0.0f);
+    if(cull && backfaceHit) return 0;
+    float Az = Sz * A[kz], Bz = Sz * B[kz], Cz = Sz * C[kz];
+    float T = U * Az + V * Bz + W * Cz;
+    float rcp = 1.0f / det;
+    float t = T * rcp;
+    if(t <= SMALL_EPS) return 0;
+    bary_out[0] = U * rcp; bary_out[1] = V * rcp; bary_out[2] = W * rcp;
+    *t_out = t;
+    *backface_out = backfaceHit;
+    return 1;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Ray::IntersectsAABB (Source/Core/Ray.hpp:192-219)                         */
 /* ------------------------------------------------------------------------ */
 int orc_intersect_aabb(const float dir[3], const float pos[3],
@@ -276,6 +334,7 @@ typedef struct
     uint32_t*   idx;         /* 3 * nt */
     uint32_t    nt;
     uint32_t    primKeyBase;
+    int         watertight;  /* triangle test: 0 Moller-Trumbore (MRay), 1 watertight */
     lbvh        bvh;
 } orc_mesh;
 
@@ -295,6 +354,7 @@ struct orc_scene
     orc_inst*   insts;   uint32_t instCount, instCap;
     lbvh        tlas;
     int         built;
+    int         watertight;
 };
 
 typedef struct { uint64_t code; uint32_t idx; } code_idx;
@@ -515,7 +575,7 @@ int orc_scene_add_mesh(orc_scene* s, const float* pos, uint32_t nv,
     if(!m->pos || !m->idx) return -1;
     memcpy(m->pos, pos, sizeof(float) * 3 * nv);
     memcpy(m->idx, idx, sizeof(uint32_t) * 3 * nt);
-    m->nv = nv; m->nt = nt; m->primKeyBase = primKeyBase;
+    m->nv = nv; m->nt = nt; m->primKeyBase = primKeyBase; m->watertight = s->watertight;
     s->built = 0;
     return (int)s->meshCount++;
 }
@@ -663,7 +723,9 @@ static inline int isect_check(const orc_mesh* m, uint32_t prim, int cull,
     float v[3][3];
     tri_verts(m, prim, v);
     float bary[3], t; int bf;
-    if(!orc_intersect_triangle(dir, pos, v[0], v[1], v[2], cull, bary, &t, &bf)) return 0;
+    const int hit = m->watertight ? orc_intersect_triangle_wt(dir, pos, v[0], v[1], v[2], cull, bary, &t, &bf)
+                                  : orc_intersect_triangle(dir, pos, v[0], v[1], v[2], cull, bary, &t, &bf);
+    if(!hit) return 0;
     if(!((t >= tmm[0]) && (t < tmm[1]))) return 0;
     out->hit = 1; out->t = t;
     out->bary[0] = bary[0]; out->bary[1] = bary[1]; out->bary[2] = bary[2];
@@ -923,4 +985,12 @@ void orc_cast_visibility(const orc_scene* s, const orc_ray_gmem* rays, const uin
     cast_job j; memset(&j, 0, sizeof(j));
     j.s = s; j.crays = rays; j.ridx = ridx; j.n = n; j.vis = vis; j.mode = 2;
     run_job(&j, nthreads);
+}
+
+/* Selects the triangle test of every mesh of the scene (0 Moller-Trumbore,
+ * MRay's; 1 the watertight test above). */
+void orc_scene_set_watertight(orc_scene* s, int on)
+{
+    s->watertight = on;
+    for(uint32_t i = 0; i < s->meshCount; i++) s->meshes[i].watertight = on;
 }

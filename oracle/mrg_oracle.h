@@ -30,6 +30,10 @@ typedef struct { uint32_t primKey, lmKey, transKey, accelKey; } orc_hit_keys;
 typedef struct { float bary[2]; } orc_meta_hit;
 
 /* ---- core math (pinned against the reference's own headers) ----------- */
+/* Watertight alternative (Woop, Benthin, Wald 2013); same outputs. */
+int  orc_intersect_triangle_wt(const float dir[3], const float pos[3],
+                               const float v0[3], const float v1[3], const float v2[3],
+                               int cull, float bary_out[3], float* t_out, int* backface_out);
 int  orc_intersect_triangle(const float dir[3], const float pos[3],
                             const float v0[3], const float v1[3], const float v2[3],
                             int cull, float bary_out[3], float* t_out, int* backface_out);
@@ -49,6 +53,9 @@ void orc_tri_center(const float v0[3], const float v1[3], const float v2[3], flo
 
 /* ---- scene + two-level LBVH accelerator ------------------------------- */
 typedef struct orc_scene orc_scene;
+/* Triangle test of the scene's meshes: 0 Moller-Trumbore (MRay's, default),
+ * 1 watertight (orc_intersect_triangle_wt). */
+void orc_scene_set_watertight(orc_scene* s, int on);
 orc_scene* orc_scene_create(void);
 void       orc_scene_destroy(orc_scene*);
 /* Returns mesh id (>=0) or -1.  prim keys are prim_key_base + local triangle index. */

@@ -56,10 +56,48 @@ def gpu_visibility(acc, rays, ray_idx=None, pre_bits=None):
     return bits.cpu().numpy().view(np.uint32)
 
 
-def compare_closest(ora, gpu, listed=None):
+def tri_retest(S, rays, pos, idx, prim_base=PRIM_BASE, cull=True, watertight=False,
+               inst_of=lambda keys: int(keys[2] & 0xFFFFFF)):
+    """A re-test for compare_closest: the GPU's reported triangle, intersected
+    by the oracle's triangle test in the reported instance's space (the
+    oracle's own inverse), must give exactly the reported t and barycentrics.
+    Instance = low 24 bits of the transform key (build_pair's keys)."""
+    import ctypes as C
+    L = oracle.lib()
+    vp = C.c_void_p
+    fn = L.orc_intersect_triangle_wt if watertight else L.orc_intersect_triangle
+
+    def check(k, keys, meta, tval):
+        inst = inst_of(keys)
+        prim = int(keys[0]) - prim_base
+        if prim < 0 or prim >= idx.shape[0]:
+            return False
+        inv = np.ascontiguousarray(S.instance_inverse(inst), np.float32)
+        d = np.ascontiguousarray(rays[k, 4:7], np.float32)
+        p = np.ascontiguousarray(rays[k, 0:3], np.float32)
+        ld = np.zeros(3, np.float32)
+        lp = np.zeros(3, np.float32)
+        L.orc_transform_ray(inv.ctypes.data_as(vp), d.ctypes.data_as(vp), p.ctypes.data_as(vp),
+                            ld.ctypes.data_as(vp), lp.ctypes.data_as(vp))
+        v = np.ascontiguousarray(pos[idx[prim]], np.float32)
+        b = np.zeros(3, np.float32)
+        t = np.zeros(1, np.float32)
+        bf = np.zeros(1, np.int32)
+        hit = fn(ld.ctypes.data_as(vp), lp.ctypes.data_as(vp), v[0].ctypes.data_as(vp), v[1].ctypes.data_as(vp),
+                 v[2].ctypes.data_as(vp), 1 if cull else 0, b.ctypes.data_as(vp), t.ctypes.data_as(vp),
+                 bf.ctypes.data_as(vp))
+        return bool(hit) and t.view(np.uint32)[0] == np.float32(tval).view(np.uint32) and \
+            np.array_equal(b[:2].view(np.uint32), np.asarray(meta, np.float32).view(np.uint32))
+    return check
+
+
+def compare_closest(ora, gpu, listed=None, retest=None):
     """ora = (rays, hits, meta, inst) from the oracle; gpu = (rays, hits, meta).
     Returns (n_compared, n_hits, n_ties).  Asserts bit equality except on
-    exact-t ties between different primitives."""
+    exact-t ties between different primitives: the t must be the same, and
+    every such ray is re-tested (retest(k, gpu keys, gpu meta, gpu t), e.g.
+    tri_retest): the GPU's primitive must give exactly its reported t and
+    barycentrics.  Without a re-test no difference is accepted."""
     orays, ohits, ometa, oinst = ora
     grays, ghits, gmeta = gpu
     n = orays.shape[0]
@@ -72,10 +110,14 @@ def compare_closest(ora, gpu, listed=None):
     same_meta = (ometa[sel].view(np.uint32) == gmeta[sel].view(np.uint32)).all(axis=1)
     ok = same_keys & same_meta
     ties = int((~ok).sum())
-    # a difference is only acceptable as a tie: same t, different primitive
+    # a difference is only acceptable as a tie: same t, different primitive,
+    # and the GPU's primitive really is hit at exactly that t
     if ties:
         bad = sel[~ok]
         assert (oinst[bad] != MISS).all()
+        assert retest is not None, "%d key / barycentric differences and no re-test" % ties
+        failed = [int(k) for k in bad if not retest(int(k), ghits[k], gmeta[k], grays[k, 7])]
+        assert not failed, "GPU hits that do not re-test: %s" % failed[:5]
     hitn = int((oinst[sel] != MISS).sum())
     assert ties <= max(2, hitn // 10000), "%d non-tie-looking differences" % ties
     return len(sel), hitn, ties

@@ -2,8 +2,9 @@
 FP64 replay on a small case, and against central finite differences of the
 GPU's own renders on the differentiable-rendering workload (box + 65k-triangle
 displaced sphere with a 512^2 f32 albedo texture, L2 loss over a 512^2
-image, 32 spp, depth 6, finite-difference step 1e-3 on 64 seeded texels,
-within 2%); the same for the area light's radiance (d(loss)/d(emission)).
+image, 32 spp, depth 6, finite-difference step 1e-3 on 64 seeded texels
+drawn uniformly, within 2%, and the host replay at that full size); the same
+for the area light's radiance (d(loss)/d(emission)).
 Russian roulette is off (rr_start = max_depth): with it on, its
 throughput-dependent probability is treated as a constant by the adjoint."""
 import numpy as np
@@ -96,13 +97,13 @@ def test_adjoint_finite_differences_full_size():
     def loss():
         return float(torch.sum((_img(pt.render(p)).double() - tgt) ** 2) / npix)
 
-    # 64 seeded texels among those the adjoint says matter
+    # 64 seeded texel channels drawn uniformly over the whole texture (those
+    # the camera never sees must come out zero on both sides)
     dev = dev.detach()
-    g3 = np.abs(grad[..., :3]).ravel()
-    live = np.nonzero(g3 > np.quantile(g3[g3 > 0], 0.5))[0]
-    picks = rng.choice(live, 64, replace=False)
+    picks = rng.choice(512 * 512 * 3, 64, replace=False)
+    gscale = float(np.abs(grad[..., :3]).max())
     h = 1e-3
-    bad, rel = [], []
+    bad, rel, fds = [], [], []
     for flat in picks:
         y, x, k = np.unravel_index(flat, (512, 512, 3))
         v = float(tex[y, x, k])
@@ -112,13 +113,32 @@ def test_adjoint_finite_differences_full_size():
         lm = loss()
         dev[y, x, k] = v
         fd = (lp - lm) / (2 * h)
+        fds.append(fd)
         g = grad[y, x, k]
-        rel.append(abs(fd - g) / max(abs(g), 1e-30))
-        if abs(fd - g) > 0.02 * abs(g) + 1e-9:
+        if g != 0.0:
+            rel.append(abs(fd - g) / abs(g))
+        # 2% of the gradient, with a floor of 1e-6 of the largest gradient
+        # for channels whose gradient is (near) zero
+        if abs(fd - g) > 0.02 * abs(g) + 1e-6 * gscale:
             bad.append((int(y), int(x), int(k), fd, g))
-    print("finite differences: %d of 64 outside 2%%; relative error median %.2g, max %.2g"
-          % (len(bad), float(np.median(rel)), float(np.max(rel))), bad[:4])
-    assert len(bad) <= 3, bad[:8]
+    live = int(np.sum(grad[..., :3].ravel()[picks] != 0.0))
+    print("finite differences: %d of 64 outside 2%% (%d with a nonzero gradient); relative error median %.2g, "
+          "max %.2g" % (len(bad), live, float(np.median(rel)), float(np.max(rel))), bad[:4])
+    assert live >= 16
+    assert len(bad) <= 1, bad[:8]
+
+    # the project's FP64-accumulated host replay at the full size, on the
+    # same texels and over the whole texture
+    S = oracle.PtScene(scenes.adjoint_scene(tex))
+    sphere = [k for k, s_ in enumerate(scenes.adjoint_scene(None)) if "uv" in s_][0]
+    go = S.adjoint(oracle.PtScene.params(512, 512, 32, cam, max_depth=6, rr_start=6, seed=7), sphere,
+                   delta.cpu().numpy())
+    err_all = float(np.linalg.norm(grad[..., :3] - go[..., :3]) / np.linalg.norm(go[..., :3]))
+    yy, xx, kk = np.unravel_index(picks, (512, 512, 3))
+    err_picks = float(np.abs(grad[yy, xx, kk] - go[yy, xx, kk]).max() / gscale)
+    print("full size against the host replay: relative L2 %.3g over the texture, max %.3g on the 64 texels"
+          % (err_all, err_picks))
+    assert err_all <= 1e-2 and err_picks <= 1e-3
     pt.close()
 
 

@@ -181,3 +181,69 @@ def test_cached_render_learns_the_scene():
     assert np.mean(losses[-5:]) < np.mean(losses[:5])
     assert bias < 0.15 and rel < 0.5
     pt.close()
+
+
+@pytest.mark.parametrize("spectral", [False, True])
+def test_trained_cache_beats_plain_tracer_at_equal_time(spectral):
+    """What the trained network gains over the method without it: on the
+    production scene (a 320x180 film, depth 12, RGB or 4 wavelengths), after
+    training, cache-assisted frames rendered in the device time of a 16-spp
+    plain render have a lower relMSE against a 1,024-spp plain render than
+    that plain render.  The times are CUDA-event measurements of the two
+    renders themselves (training frames before the comparison not counted)."""
+    import os
+    import torch
+    from mray_gb300 import scenes, spectral as sp
+    from mray_gb300.pt import PathTracer, load_box_scene
+    surf, cam = scenes.c2_scene(0, texture_size=256)
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    pt.set_env(scenes.sky_map(256, 128, seed=0))
+    if spectral:
+        gold = os.path.join(os.path.dirname(__file__), "golden")
+        res, lut = sp.read_mrspectra(os.path.join(gold, "REC_709_r32.mrspectra"))
+        pt.set_spectral(res, lut, sp.load_tables(os.path.join(gold, "spectral_rec709.npz")))
+    cache = RadianceCache(owner=pt, aabb=tuple(float(v) for v in pt.acc.scene_aabb()), max_batch=65536)
+    w, h = 320, 180
+
+    def P(spp, seed, start=0, spp_pass=0):
+        return PathTracer.params(w, h, spp, cam, max_depth=12, rr_start=3, seed=seed, sample_start=start,
+                                 samples_per_pass=spp_pass)
+
+    ref = pt.render(P(1024, 1, spp_pass=64))
+    ref = (ref[..., :3] / ref[..., 3:]).double()
+
+    def relmse(img):
+        im = (img[..., :3] / img[..., 3:]).double()
+        return float(torch.mean((im - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    pt.render(P(16, 7))
+    plain, t_plain = timed(lambda: pt.render(P(16, 2)))
+    for f in range(48):
+        pt.render_cached(P(4, 100 + f, start=4 * f), train_paths=16384)
+    _, t_frame = timed(lambda: pt.render_cached(P(4, 300), train_paths=16384))
+    frames = max(1, int(t_plain // t_frame))
+
+    def run():
+        img = None
+        for f in range(frames):
+            img, _ = pt.render_cached(P(4, 1000 + f, start=4 * f), image=img, train_paths=16384)
+        return img
+    img, t_cached = timed(run)
+    rp, rc = relmse(plain), relmse(img)
+    print("%s: plain 16 spp %.2f ms relMSE %.4g; cached %d x 4 spp %.2f ms relMSE %.4g" %
+          ("spectral" if spectral else "RGB", t_plain, rp, frames, t_cached, rc))
+    assert np.isfinite(rc)
+    assert t_cached <= 1.25 * t_plain
+    assert rc < rp
+    cache.close()
+    pt.close()

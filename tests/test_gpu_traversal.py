@@ -7,7 +7,7 @@ import pytest
 
 import oracle
 from mray_gb300 import Accelerator, MRGError, scenes
-from parity_util import (MISS, build_pair, compare_closest, gpu_closest, gpu_visibility,
+from parity_util import (MISS, build_pair, compare_closest, gpu_closest, gpu_visibility, tri_retest,
                          stress_workload)
 
 pytestmark = pytest.mark.gpu
@@ -32,7 +32,7 @@ def test_closest_small_scenes(level, ninst, cull):
     rays = scenes.primary_rays(97, 61, level, eye=(0, 0, -14), tan_half_fov=0.5)
     ora = S.cast_closest(rays)
     gpu = gpu_closest(acc, rays)
-    n, hits, ties = compare_closest(ora, gpu)
+    n, hits, ties = compare_closest(ora, gpu, retest=tri_retest(S, rays, pos, idx, cull=cull))
     assert hits > 0
 
 
@@ -100,7 +100,7 @@ def test_corrected_inverse_mode_general_rotations():
     mats = _general_rotations()
     rays = scenes.primary_rays(80, 80, 9, eye=(0, 0, -12), tan_half_fov=0.5)
     acc, S = build_pair(pos, idx, mats, corrected=True)
-    compare_closest(S.cast_closest(rays), gpu_closest(acc, rays))
+    compare_closest(S.cast_closest(rays), gpu_closest(acc, rays), retest=tri_retest(S, rays, pos, idx))
 
 
 def test_reference_inverse_mode_general_rotations():
@@ -194,7 +194,7 @@ def test_edge_rays():
     rays[200:300, 7] = 0.0           # empty interval
     rays[300:400, 3] = 1.0
     rays[300:400, 7] = 1.0           # [1, 1): empty for a half-open range
-    compare_closest(S.cast_closest(rays), gpu_closest(acc, rays))
+    compare_closest(S.cast_closest(rays), gpu_closest(acc, rays), retest=tri_retest(S, rays, pos, idx, cull=False))
     assert np.array_equal(gpu_visibility(acc, rays), S.cast_visibility(rays))
 
 
@@ -329,14 +329,56 @@ def test_stress_scene_full_size_parity():
     acc, S = build_pair(pos, idx, m)
     ora_p = S.cast_closest(prim)
     gpu_p = gpu_closest(acc, prim)
-    n, hits, ties = compare_closest(ora_p, gpu_p)
+    n, hits, ties = compare_closest(ora_p, gpu_p, retest=tri_retest(S, prim, pos, idx))
     assert hits > 0.8 * n
     bounce, src = scenes.bounce_rays(prim, ora_p[3], ora_p[1][:, 0] - 0x10000000, ora_p[0][:, 7],
                                      pos, idx, m, seed=1)
     ora_b = S.cast_closest(bounce)
     gpu_b = gpu_closest(acc, bounce)
-    compare_closest(ora_b, gpu_b)
+    compare_closest(ora_b, gpu_b, retest=tri_retest(S, bounce, pos, idx))
     shadow = scenes.shadow_rays(bounce, (0.0, 80.0, -60.0))
     assert np.array_equal(gpu_visibility(acc, shadow), S.cast_visibility(shadow))
     st = acc.stats()
     assert st["blasTriangles"] == 1310720 and st["instances"] == 64 and st["accelerators"] == 1
+
+
+def test_watertight_mode_matches_oracle():
+    """The opt-in watertight triangle test: the GPU (records holding the three
+    vertices, the WT kernel instantiation) against the oracle's watertight
+    restatement, bit for bit, on closest and any-hit casts; and the
+    watertightness itself on rays aimed at shared vertices and edges."""
+    from test_watertight_host import _grid_mesh, _rays_at
+    pos, idx, m = small(4, 27, seed=2)
+    acc = Accelerator(0, watertight=True)
+    S = oracle.Scene(watertight=True)
+    mid = acc.upload_mesh(pos, idx, prim_key_base=0x10000000)
+    oid = S.add_mesh(pos, idx, prim_key_base=0x10000000)
+    for i in range(m.shape[0]):
+        acc.add_instance(mid, m[i], light_or_mat_key=i, trans_key=(1 << 24) | i, accel_key=(2 << 20) | i)
+        S.add_instance(oid, m[i], lm_key=i, trans_key=(1 << 24) | i, accel_key=(2 << 20) | i)
+    acc.construct()
+    S.build()
+    rays = scenes.primary_rays(128, 96, 6, eye=(0, 0, -14), tan_half_fov=0.5)
+    n, hits, ties = compare_closest(S.cast_closest(rays), gpu_closest(acc, rays),
+                                    retest=tri_retest(S, rays, pos, idx, watertight=True))
+    assert hits > 1000
+    assert np.array_equal(gpu_visibility(acc, rays), S.cast_visibility(rays))
+    acc.close()
+    # a jittered grid, rays through its shared vertices and edges: the GPU
+    # hits exactly what the oracle's brute force hits (no cracks in either)
+    rng = np.random.default_rng(3)
+    gpos, gidx, nrm = _grid_mesh(24, 1)
+    inner = [j * 25 + i for j in range(1, 24) for i in range(1, 24)]
+    targets = gpos[inner]
+    rays = _rays_at(targets, nrm, rng)
+    acc = Accelerator(0, watertight=True)
+    S = oracle.Scene(watertight=True)
+    acc.add_instance(acc.upload_mesh(gpos, gidx), np.eye(3, 4, dtype=np.float32).reshape(12), cull=False)
+    S.add_instance(S.add_mesh(gpos, gidx), np.eye(3, 4, dtype=np.float32), cull=False)
+    acc.construct()
+    S.build()
+    gr, gh, gm = gpu_closest(acc, rays)
+    assert (gr[:, 7] < 1e29).all()          # every ray through a shared vertex hits
+    lin = S.cast_closest(rays, linear=True)
+    assert np.array_equal(gr[:, 7].view(np.uint32), lin[0][:, 7].view(np.uint32))
+    acc.close()
