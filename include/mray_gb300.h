@@ -260,6 +260,14 @@ typedef struct mrg_pt_params
  * scrambling as published), which keeps the Sobol points' stratification that
  * MRay's ScambleOwenFast (Source/Tracer/Random.cu:141-150) loses. */
 #define MRG_PT_SAMPLER_ZSOBOL_OWEN 2u
+/* MRay's independent group (RNGGroupIndependent, Source/Tracer/Random.cu:
+ * 661-726): one PCG32 stream per pixel (PermutedCG32, Source/Tracer/Random.h:
+ * 235-266), its state GenerateState(i-th output of std::mt19937(seed32)),
+ * seed32 = params.seed.  Number k of bounce b of sample s is the stream's
+ * number at position ((s * (maxDepth + 1) + b) * 16 + k), so that a sample
+ * reads the same numbers however the film is split into passes;
+ * (sampleStart + spp) * (maxDepth + 1) * 16 must not exceed 2^32. */
+#define MRG_PT_SAMPLER_PCG32       3u
 
 /* Surface description of an instance, the equivalent of attaching a
  * material / light group to a surface (TracerI::CreateSurface, CreateLightSurface).

@@ -131,10 +131,10 @@ struct PtLaunch
     uint32_t seed;
     uint32_t nLights;        // triangle lights; the skysphere, if enabled, follows them
     float    filterSigma;
-    uint32_t sampler;        // 0: counter-based independent numbers, 1: ZSobol
+    uint32_t sampler;        // 0: counter-based independent numbers, 1: ZSobol, 2: ZSobol (Owen order), 3: PCG32
     uint32_t zsMaxSpp;       // ZSobol initialMaxSampleCount
     uint32_t zsResBits;      // ZSobol resMaxBits
-    const uint32_t* zsSeeds; // ZSobol per-pixel seeds (row-major)
+    const uint32_t* zsSeeds; // ZSobol / PCG32 per-pixel mt19937 seeds (row-major)
     const uint32_t* zsTables;// ZSobol matrices (3 x 52) then digit permutations (4 x uint64)
     PtCamera cam;
     PtEnv    env;

@@ -609,9 +609,48 @@ __device__ __noinline__ float rnd_zsobol(const PtLaunch& L, uint32_t i, uint32_t
     return zs_to_float01(zs_number(g, L.zsTables, perm, dim, size, comp, L.sampler == 2u));
 }
 
+// MRay's independent group (sampler 3; RNGGroupIndependent, Random.cu:661-726):
+// the pixel's PCG32 stream (PermutedCG32, Random.h:762-842), its state made
+// by GenerateState from the pixel's mt19937 output, read at position
+// ((sample * (maxDepth + 1) + bounce) * 16 + k).  The jump there composes the
+// affine maps of 2^j LCG steps for the set bits of the position (Brown's
+// arbitrary-stride method, as PermutedCG32::Advance does); `count`
+// consecutive positions from k0 follow by single steps.
+constexpr uint32_t kPcgMult = 747796405u, kPcgInc = 2891336453u;
+
+__device__ __forceinline__ uint32_t pcg_permute(uint32_t s)
+{
+    const uint32_t x = ((s >> ((s >> 28) + 4u)) ^ s) * 277803737u;
+    return (x >> 22) ^ x;
+}
+
+__device__ __noinline__ float4 rnd_pcg32(const PtLaunch& L, uint32_t i, uint32_t bounce, uint32_t k0, uint32_t count)
+{
+    const uint32_t pixel = slot_pixel(L, i);
+    uint32_t st = (kPcgInc + __ldg(L.zsSeeds + pixel)) * kPcgMult + kPcgInc;   // GenerateState
+    uint32_t a = 1u, c = 0u, m = kPcgMult, inc = kPcgInc;
+    for(uint32_t n = ((slot_sample(L, i) * (L.maxDepth + 1u) + bounce) << 4) | k0; n; n >>= 1)
+    {
+        if(n & 1u) { a *= m; c = c * m + inc; }
+        inc = (m + 1u) * inc;
+        m *= m;
+    }
+    st = a * st + c;
+    float v[3] = { 0.0f, 0.0f, 0.0f };
+    #pragma unroll
+    for(uint32_t j = 0; j < 3u; j++)
+    {
+        if(j < count) v[j] = zs_to_float01(pcg_permute(st));
+        st = st * kPcgMult + kPcgInc;
+    }
+    return make_float4(v[0], v[1], v[2], 0.0f);
+}
+
 __device__ __forceinline__ float rnd_s(const PtLaunch& L, uint32_t key, uint32_t i, uint32_t bounce, uint32_t k)
 {
-    return (L.sampler == 0u) ? rnd(key, bounce, k) : rnd_zsobol(L, i, bounce, k);
+    if(L.sampler == 0u) return rnd(key, bounce, k);
+    if(L.sampler == 3u) return rnd_pcg32(L, i, bounce, k, 1u).x;
+    return rnd_zsobol(L, i, bounce, k);
 }
 
 // The bounce's numbers k 0..2 (one Next3D request) or k 4, 5 (one Next2D
@@ -632,14 +671,14 @@ __device__ __noinline__ float4 rnd_zsobol_group(const PtLaunch& L, uint32_t i, u
 __device__ __forceinline__ float3 rnd_s3(const PtLaunch& L, uint32_t key, uint32_t i, uint32_t bounce)
 {
     if(L.sampler == 0u) return make_float3(rnd(key, bounce, 0), rnd(key, bounce, 1), rnd(key, bounce, 2));
-    const float4 r = rnd_zsobol_group(L, i, bounce, 0u);
+    const float4 r = (L.sampler == 3u) ? rnd_pcg32(L, i, bounce, 0u, 3u) : rnd_zsobol_group(L, i, bounce, 0u);
     return make_float3(r.x, r.y, r.z);
 }
 
 __device__ __forceinline__ float2 rnd_s45(const PtLaunch& L, uint32_t key, uint32_t i, uint32_t bounce)
 {
     if(L.sampler == 0u) return make_float2(rnd(key, bounce, 4), rnd(key, bounce, 5));
-    const float4 r = rnd_zsobol_group(L, i, bounce, 4u);
+    const float4 r = (L.sampler == 3u) ? rnd_pcg32(L, i, bounce, 4u, 2u) : rnd_zsobol_group(L, i, bounce, 4u);
     return make_float2(r.x, r.y);
 }
 

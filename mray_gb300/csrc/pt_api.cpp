@@ -200,8 +200,10 @@ mrg_status env_prepare(mrg_ctx* c)
     return MRG_OK;
 }
 
-// ZSobol state of a render: the tables (once per context) and the per-pixel
-// seeds of (width, height, seed), kept while those stay the same.
+// ZSobol / PCG32 state of a render: the tables (once per context) and the
+// per-pixel seeds of (width, height, seed), kept while those stay the same.
+// Both groups seed a pixel from the same std::mt19937 output
+// (RNGGroupZSobol, Random.cu:1175-1200; RNGGroupIndependent, Random.cu:683-704).
 mrg_status pt_zsobol(mrg_ctx* c, const mrg_pt_params& p, mrg::PtLaunch& L, const std::string& w)
 {
     if(!c->dZsTables)
@@ -628,7 +630,11 @@ mrg_status pt_setup(mrg_ctx* c, const mrg_pt_params* p, PtRun& R, const char* wh
     L.env = c->ptEnv;
     L.spec = c->ptSpec;
     L.filterSigma = p->filterRadius * 0.285714f;
-    if(p->sampler > MRG_PT_SAMPLER_ZSOBOL_OWEN) return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": unknown sampler");
+    if(p->sampler > MRG_PT_SAMPLER_PCG32) return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": unknown sampler");
+    // a PCG32 stream holds 2^32 numbers: 16 per bounce, maxDepth + 1 bounces per sample
+    if(p->sampler == MRG_PT_SAMPLER_PCG32 &&
+       ((uint64_t)p->sampleStart + p->spp) * ((uint64_t)p->maxDepth + 1u) * 16u > 0x100000000ull)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": samples x depth exceed the PCG32 stream");
     L.sampler = p->sampler;
     if(L.sampler != MRG_PT_SAMPLER_INDEPENDENT && (s = pt_zsobol(c, *p, L, w)) != MRG_OK) return s;
     camera_frame(*p, L.cam);

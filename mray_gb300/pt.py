@@ -160,7 +160,7 @@ class PathTracer:
                seed=0, filter_radius=1.0, samples_per_pass=0, sample_start=0, partition="auto",
                sampler="independent", sampler_max_spp=0):
         p = N.MrgPtParams()
-        p.sampler = {"independent": 0, "zsobol": 1, "zsobol-owen": 2}[sampler]
+        p.sampler = {"independent": 0, "zsobol": 1, "zsobol-owen": 2, "pcg32": 3}[sampler]
         p.samplerMaxSpp = sampler_max_spp
         p.width, p.height, p.spp = width, height, spp
         p.samplesPerPass = samples_per_pass

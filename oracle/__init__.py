@@ -89,6 +89,7 @@ def lib():
         L.orc_zs_generate.restype = C.c_int
         L.orc_zs_number.argtypes = [u32, u32, u32, u32, u32, u32, u32, u32, u32, C.c_int]
         L.orc_zs_number.restype = u32
+        L.orc_pcg32_numbers.argtypes = [vp, vp, u32, vp]
         L.orc_pt_render.restype = C.c_int
         L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
         L.orc_pt_make_light.argtypes = [vp, vp, vp, C.c_int, vp]
@@ -683,6 +684,16 @@ def mt19937(seed, count):
 def zsobol_seeds(width, height, seed):
     out = np.zeros(width * height, np.uint32)
     lib().orc_zs_seeds(width, height, seed, _vp(out))
+    return out
+
+
+def pcg32_numbers(seeds, delta):
+    """Number delta[i] of MRay's PermutedCG32 stream seeded (GenerateState)
+    by seeds[i]."""
+    sd = np.ascontiguousarray(seeds, np.uint32)
+    dl = np.ascontiguousarray(np.broadcast_to(np.asarray(delta, np.uint32), sd.shape))
+    out = np.zeros(sd.shape, np.uint32)
+    lib().orc_pcg32_numbers(_vp(sd), _vp(dl), sd.size, _vp(out))
     return out
 
 

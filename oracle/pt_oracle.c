@@ -57,19 +57,33 @@ static inline float rnd(uint32_t key, uint32_t bounce, uint32_t dim)
     return (float)(h >> 8) * (1.0f / 16777216.0f);
 }
 
-/* The sample's random-number source: the counter-based hash, or MRay's ZSobol
+/* The sample's random-number source: the counter-based hash; MRay's ZSobol
  * group under the path tracer's dimension plan (film-filter offset = Next2D(0),
  * wavelengths = Next(2); bounce b from dimension 3 + 7b: k 0..2 = Next3D(+0),
- * k 3 = Next(+3), k 4, 5 = Next2D(+4), k 8 = Next(+6)), converted as
+ * k 3 = Next(+3), k 4, 5 = Next2D(+4), k 8 = Next(+6)); or MRay's independent
+ * group, the pixel's PCG32 stream read at position
+ * ((sample * (maxDepth + 1) + b) * 16 + k).  Numbers convert as
  * RNGFunctions::ToFloat01 does (Source/Tracer/Random.h:100-119). */
 typedef struct
 {
-    uint32_t key, px, py, sample, seed, sampler, maxSpp, resBits;
+    uint32_t key, px, py, sample, seed, sampler, maxSpp, resBits, maxDepth;
 } smp_ctx;
+
+static float to_unit(uint32_t v)
+{
+    float f = (float)v * 0x1p-32f;
+    const float prev1 = 0x1.fffffep-1f;
+    return f < prev1 ? f : prev1;
+}
 
 static float urnd(const smp_ctx* c, uint32_t bounce, uint32_t k)
 {
     if(c->sampler == 0u) return rnd(c->key, bounce, k);
+    if(c->sampler == 3u)
+    {
+        const uint32_t n = ((c->sample * (c->maxDepth + 1u) + bounce) << 4) | k;
+        return to_unit(orc_pcg32_permute(orc_pcg32_advance(orc_pcg32_state(c->seed), n)));
+    }
     uint32_t dim, size, comp;
     if(k == 6u || k == 7u) { dim = 0u; size = 2u; comp = k - 6u; }
     else if(k == 9u) { dim = 2u; size = 1u; comp = 0u; }
@@ -81,11 +95,8 @@ static float urnd(const smp_ctx* c, uint32_t bounce, uint32_t k)
         else if(k <= 5u) { dim = b + 4u; size = 2u; comp = k - 4u; }
         else { dim = b + 6u; size = 1u; comp = 0u; }
     }
-    uint32_t v = orc_zs_number(c->px, c->py, c->seed, c->sample, c->maxSpp, c->resBits, dim, size, comp,
-                               c->sampler == 2u);
-    float f = (float)v * 0x1p-32f;
-    const float prev1 = 0x1.fffffep-1f;
-    return f < prev1 ? f : prev1;
+    return to_unit(orc_zs_number(c->px, c->py, c->seed, c->sample, c->maxSpp, c->resBits, dim, size, comp,
+                                 c->sampler == 2u));
 }
 
 /* Math::Dot (Source/Core/Math.h:1585-1596): r = 0; r = fma(a_i, b_i, r). */
@@ -1055,7 +1066,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
     const uint32_t pixel = y * P->width + x;
     const uint32_t key = path_key(P->seed, pixel, sample);
     smp_ctx SC = { key, x, y, sample, J->zsSeeds ? J->zsSeeds[pixel] : 0u, J->zsSeeds ? P->sampler : 0u,
-                   P->samplerMaxSpp ? P->samplerMaxSpp : P->sampleStart + P->spp, J->zsResBits };
+                   P->samplerMaxSpp ? P->samplerMaxSpp : P->sampleStart + P->spp, J->zsResBits, P->maxDepth };
     outRad[0] = outRad[1] = outRad[2] = 0.0f;
 
     /* camera ray: Gaussian film-filter offset (weight Evaluate / pdf = 1) */
@@ -1334,7 +1345,7 @@ static void* pt_adj_worker(void* arg)
 static int job_sampler(pt_job* J, const orc_pt_params* p)
 {
     J->zsSeeds = NULL;
-    if(p->sampler != 1u && p->sampler != 2u) return 0;
+    if(p->sampler < 1u || p->sampler > 3u) return 0;
     J->zsSeeds = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)p->width * p->height);
     if(!J->zsSeeds) return -2;
     orc_zs_seeds(p->width, p->height, (uint64_t)p->seed, J->zsSeeds);

@@ -30,7 +30,8 @@ typedef struct
     float    camUp[3];
     float    planeSize[2];
     float    nearT, farT;
-    uint32_t sampler;       /* 0: counter-based independent numbers, 1: ZSobol */
+    uint32_t sampler;       /* 0: counter-based independent numbers, 1: ZSobol, 2: ZSobol with
+                               the Owen bit order, 3: MRay's per-pixel PCG32 streams */
     uint32_t samplerMaxSpp; /* ZSobol initialMaxSampleCount (0: sampleStart + spp) */
 } orc_pt_params;
 

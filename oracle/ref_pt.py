@@ -148,6 +148,24 @@ def zsobol_seeds(seed, count):
     return out
 
 
+def pcg32_jump(seeds, delta):
+    """MRay's PermutedCG32: the number after Advance(delta[i]) of the stream
+    GenerateState(seeds[i]) starts."""
+    sd = np.ascontiguousarray(seeds, np.uint32)
+    dl = np.ascontiguousarray(np.broadcast_to(np.asarray(delta, np.uint32), sd.shape))
+    out = np.zeros(sd.shape, np.uint32)
+    load().ref_pcg32_jump(_p(sd), _p(dl), C.c_uint32(sd.size), _p(out))
+    return out
+
+
+def pcg32_seq(seed, n):
+    """The first n numbers (successive Next calls) of the stream
+    GenerateState(seed) starts."""
+    out = np.zeros(n, np.uint32)
+    load().ref_pcg32_seq(C.c_uint32(seed), C.c_uint32(n), _p(out))
+    return out
+
+
 class Spectral:
     """MRay's Jakob 2019 converter over a resolution-64 LUT (the converter's
     compile-time resolution)."""

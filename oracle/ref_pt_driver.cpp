@@ -527,4 +527,26 @@ void ref_zsobol_seeds(uint64_t seed, uint32_t count, uint32_t* out)
     for(uint32_t i = 0; i < count; i++) out[i] = uint32_t(rng());
 }
 
+// MRay's independent sampler: PermutedCG32 (Random.h:762-842) seeded by
+// GenerateState.  ref_pcg32_jump: out[i] = the number after Advance(delta[i])
+// of the stream seeded by seeds[i]; ref_pcg32_seq: the first n numbers of one
+// stream by successive Next calls.
+void ref_pcg32_jump(const uint32_t* seeds, const uint32_t* delta, uint32_t count, uint32_t* out)
+{
+    for(uint32_t i = 0; i < count; i++)
+    {
+        PermutedCG32::State st = PermutedCG32::GenerateState(seeds[i]);
+        PermutedCG32 rng(st);
+        rng.Advance(delta[i]);
+        out[i] = rng.Next();
+    }
+}
+
+void ref_pcg32_seq(uint32_t seed, uint32_t n, uint32_t* out)
+{
+    PermutedCG32::State st = PermutedCG32::GenerateState(seed);
+    PermutedCG32 rng(st);
+    for(uint32_t i = 0; i < n; i++) out[i] = rng.Next();
+}
+
 }  // extern "C"

@@ -14,6 +14,16 @@
  *   hash:    RNGFunctions::HashPCG64::Hash       Source/Tracer/Random.h:603-633
  *   list:    GenerateRNFromList / RNRequestList  Source/Tracer/Random.cu:426-470,
  *                                                Source/Tracer/Random.h:679-717
+ * and MRay's independent group:
+ *   seeds:   RNGGroupIndependent::RNGGroupIndependent Source/Tracer/Random.cu:661-726
+ *            (the same std::mt19937(seed32) outputs, one per pixel, each
+ *            through PermutedCG32::GenerateState)
+ *   stream:  PermutedCG32 Step / Permute / Next     Source/Tracer/Random.h:762-810
+ *   jump:    PermutedCG32::Advance                  Source/Tracer/Random.h:812-842
+ *            (Brown, "Random Number Generation with Arbitrary Stride",
+ *            Trans. Am. Nucl. Soc. 1994; the LCG constants are PCG's
+ *            published 32-bit multiplier and increment, the output
+ *            permutation PCG's RXS-M-XS)
  * The three 52-column Sobol matrices come from the Sobol recurrence (dims 0-2:
  * the reversed identity; x + 1 with m = {1}; x^2 + x + 1 with m = {1, 3}) and
  * the 24 base-4 digit permutations from the swap-recursive enumeration of the
@@ -297,4 +307,41 @@ uint32_t orc_zs_number(uint32_t px, uint32_t py, uint32_t seed, uint32_t sampleI
              : (comp == 1u) ? (uint32_t)((h >> 21) & 0x1FFFFFull) : (uint32_t)(h >> 42);
     const uint32_t v = owen_fast(mat_mul((int)comp, a), scr);
     return owen ? brev32(v) : v;
+}
+
+/* ---- independent group: PCG32 ------------------------------------------ */
+#define PCG_MULT 747796405u
+#define PCG_INC  2891336453u
+
+static uint32_t pcg_step(uint32_t r) { return r * PCG_MULT + PCG_INC; }
+
+uint32_t orc_pcg32_state(uint32_t seed)
+{
+    return pcg_step(pcg_step(0u) + seed);
+}
+
+uint32_t orc_pcg32_advance(uint32_t state, uint32_t delta)
+{
+    /* Step^delta as one affine map a*x + c, composed from the maps of
+     * Step^(2^i) for the set bits of delta. */
+    uint32_t a = 1u, c = 0u, m = PCG_MULT, k = PCG_INC;
+    for(; delta; delta >>= 1)
+    {
+        if(delta & 1u) { a *= m; c = c * m + k; }
+        k = (m + 1u) * k;
+        m *= m;
+    }
+    return a * state + c;
+}
+
+uint32_t orc_pcg32_permute(uint32_t s)
+{
+    const uint32_t x = ((s >> ((s >> 28) + 4u)) ^ s) * 277803737u;
+    return (x >> 22) ^ x;
+}
+
+void orc_pcg32_numbers(const uint32_t* seeds, const uint32_t* delta, uint32_t count, uint32_t* out)
+{
+    for(uint32_t i = 0; i < count; i++)
+        out[i] = orc_pcg32_permute(orc_pcg32_advance(orc_pcg32_state(seeds[i]), delta[i]));
 }

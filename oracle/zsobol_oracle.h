@@ -1,5 +1,6 @@
 /* zsobol_oracle.h -- TEST INFRASTRUCTURE ONLY: CPU restatement of MRay's
- * ZSobol random-number group (see zsobol_oracle.c for the reference lines). */
+ * ZSobol and independent (PCG32) random-number groups (see zsobol_oracle.c
+ * for the reference lines). */
 #pragma once
 #include <stdint.h>
 
@@ -25,6 +26,15 @@ int      orc_zs_generate(uint32_t width, uint32_t height, const uint32_t* seeds,
  * scrambled value's bits back (Laine-Karras Owen scrambling as published). */
 uint32_t orc_zs_number(uint32_t px, uint32_t py, uint32_t seed, uint32_t sampleIndex, uint32_t initialMaxSpp,
                        uint32_t resMaxBits, uint32_t dim, uint32_t size, uint32_t comp, int owen);
+
+/* MRay's independent sampler (PermutedCG32): the state GenerateState makes
+ * of a per-pixel seed, and number n of that state's stream
+ * (Permute(Step^n(state)), the jump by Brown's arbitrary-stride method). */
+uint32_t orc_pcg32_state(uint32_t seed);
+uint32_t orc_pcg32_advance(uint32_t state, uint32_t delta);
+uint32_t orc_pcg32_permute(uint32_t state);
+/* out[i] = number delta[i] of the stream seeded by seeds[i]. */
+void     orc_pcg32_numbers(const uint32_t* seeds, const uint32_t* delta, uint32_t count, uint32_t* out);
 
 #ifdef __cplusplus
 }

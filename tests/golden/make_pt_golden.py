@@ -24,6 +24,8 @@ Covered (MRay file:line):
   waves          SingleSampleSpectrumWavelength (Tracer/SpectrumContext.cu:9)
   zsobol         ZSobolDetail::ZSobol Next / Next2D / Next3D (Tracer/Random.cu:265-425)
                  and the group's per-pixel seeds (Random.cu:1175-1200)
+  pcg32          PermutedCG32 GenerateState / Advance / Next (Tracer/Random.h:762-842),
+                 the independent group's generator
 
 Usage: python tests/golden/make_pt_golden.py
 """
@@ -210,12 +212,20 @@ def zsobol(rng):
     return {"zs_in": q, "zs_out": ref_pt.zsobol(q), "zs_seed64": np.uint64(0x123456789ABCDEF0), "zs_seeds": seeds}
 
 
+def pcg32(rng):
+    seeds = rng.integers(0, 2 ** 32, N, dtype=np.uint64).astype(np.uint32)
+    delta = rng.integers(0, 2 ** 32, N, dtype=np.uint64).astype(np.uint32)
+    delta[:8] = [0, 1, 2, 15, 16, 1 << 20, 0x7FFFFFFF, 0xFFFFFFFF]
+    return {"pcg_seeds": seeds, "pcg_delta": delta, "pcg_out": ref_pt.pcg32_jump(seeds, delta),
+            "pcg_seq_seed": np.uint32(0x9E3779B9), "pcg_seq": ref_pt.pcg32_seq(0x9E3779B9, 4096)}
+
+
 def main():
     if ref_pt.load() is None:
         sys.exit("the MRay source tree and fmt headers are needed (MRAY_REFERENCE_SRC)")
     rng = np.random.default_rng(20261204)
     out = {}
-    for f in (materials, building_blocks, lights, distributions, cameras, waves, zsobol):
+    for f in (materials, building_blocks, lights, distributions, cameras, waves, zsobol, pcg32):
         out.update(f(rng))
     path = os.path.join(HERE, "pt_math.npz")
     np.savez_compressed(path, **out)

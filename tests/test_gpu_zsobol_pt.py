@@ -1,7 +1,8 @@
-"""The path tracer with MRay's ZSobol sampler (sampler="zsobol") against the
-oracle's render with the same sampler and dimension plan, per pixel, on the
-box scene (three sampling modes) and the textured mixed-material scene; and
-its accumulation across calls (the group's initial sample count fixed)."""
+"""The path tracer with MRay's ZSobol sampler (sampler="zsobol", and the
+Owen-order variant) and MRay's independent PCG32 group (sampler="pcg32")
+against the oracle's render with the same sampler and number plan, per pixel,
+on the box scene (three sampling modes) and the textured mixed-material scene;
+and their accumulation across calls."""
 import numpy as np
 import pytest
 
@@ -23,18 +24,20 @@ def relmse(a, b):
 
 @pytest.mark.parametrize("surf_fn,mode,sampler", [(scenes.box_scene, 0, 1), (scenes.box_scene, 1, 1),
                                                   (scenes.box_scene, 2, 1), (scenes.box_scene_mixed, 2, 1),
-                                                  (scenes.box_scene, 2, 2), (scenes.box_scene_mixed, 2, 2)])
+                                                  (scenes.box_scene, 2, 2), (scenes.box_scene_mixed, 2, 2),
+                                                  (scenes.box_scene, 0, 3), (scenes.box_scene, 2, 3),
+                                                  (scenes.box_scene_mixed, 2, 3)])
 def test_zsobol_render_matches_oracle(surf_fn, mode, sampler):
     pt = PathTracer(0)
     surf = load_box_scene(pt, surf_fn(0))
     S = oracle.PtScene(surf)
     cam = scenes.box_camera()
-    name = {1: "zsobol", 2: "zsobol-owen"}[sampler]
+    name = {1: "zsobol", 2: "zsobol-owen", 3: "pcg32"}[sampler]
     g = _img(pt.render(PathTracer.params(60, 44, 16, cam, sample_mode=mode, seed=9, sampler=name)))
     o = _img(S.render(S.params(60, 44, 16, cam, sample_mode=mode, seed=9, sampler=sampler)))
     close = np.abs(g - o) <= 1e-4 * (1.0 + np.abs(o))
     frac = close.all(axis=-1).mean()
-    print("zsobol mode %d: close %.4f relMSE %.3g" % (mode, frac, relmse(g, o)))
+    print("%s mode %d: close %.4f relMSE %.3g" % (name, mode, frac, relmse(g, o)))
     assert frac >= 0.97, frac
     assert relmse(g, o) <= 1e-3
     # a different sampler gives a different (but statistically equal) image:
@@ -50,11 +53,12 @@ def test_zsobol_render_matches_oracle(surf_fn, mode, sampler):
     pt.close()
 
 
-def test_zsobol_accumulation_across_calls():
+@pytest.mark.parametrize("sampler", ["zsobol", "pcg32"])
+def test_sampler_accumulation_across_calls(sampler):
     pt = PathTracer(0)
     load_box_scene(pt, 0)
     cam = scenes.box_camera()
-    kw = dict(seed=5, samples_per_pass=8, sampler="zsobol", sampler_max_spp=16)
+    kw = dict(seed=5, samples_per_pass=8, sampler=sampler, sampler_max_spp=16)
     one = pt.render(PathTracer.params(48, 40, 16, cam, **kw))
     two = pt.render(PathTracer.params(48, 40, 8, cam, **kw))
     two = pt.render(PathTracer.params(48, 40, 8, cam, sample_start=8, **kw), image=two)

@@ -111,6 +111,15 @@ def test_zsobol_numbers_and_seeds_match_mray(g):
     assert np.array_equal(np.asarray(seeds, np.uint32).ravel(), g["zs_seeds"])
 
 
+def test_pcg32_streams_match_mray(g):
+    got = oracle.pcg32_numbers(g["pcg_seeds"], g["pcg_delta"])
+    assert np.array_equal(got, g["pcg_out"])
+    seq = g["pcg_seq"]
+    got = oracle.pcg32_numbers(np.full(seq.size, int(g["pcg_seq_seed"]), np.uint32),
+                               np.arange(seq.size, dtype=np.uint32))
+    assert np.array_equal(got, seq)
+
+
 # ---- where the MRay tree is present: MRay's code run here -----------------
 
 def _ref():
