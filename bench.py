@@ -504,10 +504,11 @@ def c4_equal_time(args, dev, spp_per_frame=8):
     layers, lr 1e-2, about 32,768 training paths = up to 65,536 training
     samples per frame, paths end in the cache after one bounce), relMSE
     against a 4096-spp plain render:
-    - cold start: from an untrained cache, T training frames (T = 8, 16, 32,
-      64) then one 2-spp cache-assisted frame; the cheapest total (training
-      included) whose frame reaches the 16-spp plain render's relMSE, and the
-      plain render's time over it;
+    - cold start: from an untrained cache, T one-sample training frames
+      (T = 4, 8, 16, 32, 64), then one cache-assisted frame of 1, 2, 4 or 8
+      spp that does not train; the cheapest total (training frames included)
+      whose frame reaches the 16-spp plain render's relMSE, and the plain
+      render's time over it;
     - steady state (after the 64 training frames): equal-time relMSE of
       cache-assisted frames of spp_per_frame samples in the plain render's
       time, and the cheapest single cached frame (1, 2, 4 or 8 spp) that
@@ -552,23 +553,27 @@ def c4_equal_time(args, dev, spp_per_frame=8):
 
     # cold start: a fresh cache, training frames counted
     cache = RadianceCache(owner=pt, aabb=aabb, max_batch=65536)
-    trained, t_train, cold = 0, 0.0, {}
-    for target in (8, 16, 32, 64):
+    trained, t_train, cold = 0, 0.0, []
+    for target in (4, 8, 16, 32, 64):
         def train():
             for f in range(trained, target):
-                pt.render_cached(P(k, 100 + f, start=k * f), train_paths=32768)
+                pt.render_cached(P(1, 100 + f, start=f), train_paths=32768)
         _, dt = timed(train)
         t_train += dt
         trained = target
-        one, t_one = timed(lambda: pt.render_cached(P(2, 5000 + target, start=0), train_paths=0)[0])
-        cold[target] = (t_train + t_one, relmse(one))
-        out["c4_cold_%dtrain_total_ms" % target] = round(t_train + t_one, 2)
-        out["c4_cold_%dtrain_relmse" % target] = round(cold[target][1], 5)
-    ok = [(tt, n) for n, (tt, r) in cold.items() if r <= plain_rel]
-    if ok:
-        tt, n = min(ok)
+        out["c4_cold_%dtrain_ms" % target] = round(t_train, 2)
+        for spp in (1, 2, 4, 8):
+            one, t_one = timed(lambda: pt.render_cached(P(spp, 5000 + target, start=0), train_paths=0)[0])
+            rel = relmse(one)
+            out["c4_cold_%dtrain_%dspp_relmse" % (target, spp)] = round(rel, 5)
+            if rel <= plain_rel:
+                cold.append((t_train + t_one, target, spp))
+                break
+    if cold:
+        tt, n, spp = min(cold)
         out["c4_cold_start_time_to_plain_quality_ms"] = round(tt, 2)
         out["c4_cold_start_training_frames"] = n
+        out["c4_cold_start_frame_spp"] = spp
         out["c4_cold_start_speedup"] = round(t_plain / tt, 3)
 
     # steady state (the cache trained on the 64 frames above)

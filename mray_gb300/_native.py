@@ -83,6 +83,67 @@ class MrgAccelStats(C.Structure):
                 ("deviceBytes", C.c_uint64), ("buildMs", C.c_double), ("accelerators", C.c_uint64)]
 
 
+# ---- include/mray_gb300_tracer.h ----
+TRACER_EXPORTED = [
+    "mrg_tracer_create", "mrg_tracer_destroy", "mrg_tracer_parameters", "mrg_tracer_type_names",
+    "mrg_tracer_attribute_info", "mrg_tracer_group_type_name",
+    "mrg_tracer_create_prim_group", "mrg_tracer_reserve_prim_batches", "mrg_tracer_commit_prim_reservations",
+    "mrg_tracer_is_prim_committed", "mrg_tracer_push_prim_attribute", "mrg_tracer_transform_primitives",
+    "mrg_tracer_create_mat_group", "mrg_tracer_reserve_materials", "mrg_tracer_commit_mat_reservations",
+    "mrg_tracer_is_mat_committed", "mrg_tracer_push_mat_attribute",
+    "mrg_tracer_create_trans_group", "mrg_tracer_reserve_transforms", "mrg_tracer_commit_trans_reservations",
+    "mrg_tracer_is_trans_committed", "mrg_tracer_push_trans_attribute",
+    "mrg_tracer_create_light_group", "mrg_tracer_reserve_lights", "mrg_tracer_commit_light_reservations",
+    "mrg_tracer_is_light_committed", "mrg_tracer_push_light_attribute",
+    "mrg_tracer_create_camera_group", "mrg_tracer_reserve_cameras", "mrg_tracer_commit_cam_reservations",
+    "mrg_tracer_is_cam_committed", "mrg_tracer_push_cam_attribute",
+    "mrg_tracer_create_texture2d", "mrg_tracer_commit_textures", "mrg_tracer_push_texture_data",
+    "mrg_tracer_create_surface", "mrg_tracer_set_boundary_surface", "mrg_tracer_create_light_surface",
+    "mrg_tracer_create_camera_surface", "mrg_tracer_commit_surfaces", "mrg_tracer_get_cam_transform",
+    "mrg_tracer_set_spectral_data", "mrg_tracer_create_renderer", "mrg_tracer_destroy_renderer",
+    "mrg_tracer_push_renderer_attribute", "mrg_tracer_start_render", "mrg_tracer_set_camera_transform",
+    "mrg_tracer_do_render_work", "mrg_tracer_read_film", "mrg_tracer_stop_render", "mrg_tracer_clear_all",
+    "mrg_tracer_flush", "mrg_tracer_device_memory", "mrg_tracer_context",
+]
+
+MRG_KIND_PRIM, MRG_KIND_MATERIAL, MRG_KIND_TRANSFORM, MRG_KIND_CAMERA = 0, 1, 2, 3
+MRG_KIND_MEDIUM, MRG_KIND_LIGHT, MRG_KIND_RENDERER = 4, 5, 6
+MRG_TRACER_SAMPLER_INDEPENDENT, MRG_TRACER_SAMPLER_ZSOBOL = 0, 1
+MRG_PIX_RGBA8_UNORM, MRG_PIX_RGB_FLOAT, MRG_PIX_RGBA_FLOAT = 0, 1, 2
+MRG_ATTR_CONSTANT_ONLY, MRG_ATTR_TEXTURE_OR_CONSTANT, MRG_ATTR_TEXTURE_ONLY = 0, 1, 2
+MRG_DT_NAMES = ["FLOAT", "VECTOR_2", "VECTOR_3", "VECTOR_4", "QUATERNION", "MATRIX_4x4", "UINT32", "VECTOR_2UI",
+                "VECTOR_3UI", "BOOL", "STRING"]
+
+
+class MrgTracerParams(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("device", C.c_int), ("samplerType", C.c_uint32),
+                ("filmFilterRadius", C.c_float), ("triangleTest", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+
+
+class MrgTracerAttribInfo(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("dataType", C.c_uint32), ("elementBytes", C.c_uint32),
+                ("optional", C.c_uint32), ("texturable", C.c_uint32), ("isColor", C.c_uint32)]
+
+
+class MrgTracerSurface(C.Structure):
+    _fields_ = [("count", C.c_uint32), ("primBatches", C.c_uint32 * 8), ("materials", C.c_uint32 * 8),
+                ("alphaMaps", C.c_uint32 * 8), ("cullFace", C.c_uint32 * 8), ("transformId", C.c_uint32)]
+
+
+class MrgTracerCommitResult(C.Structure):
+    _fields_ = [("aabb", C.c_float * 6), ("instanceCount", C.c_uint64), ("acceleratorCount", C.c_uint64)]
+
+
+class MrgTracerRenderInfo(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("totalSpp", C.c_uint32),
+                ("channels", C.c_uint32), ("d_film", C.c_void_p)]
+
+
+class MrgTracerRenderOutput(C.Structure):
+    _fields_ = [("samplesDone", C.c_uint32), ("totalSpp", C.c_uint32), ("finished", C.c_uint32),
+                ("workMs", C.c_float), ("pathsPerSecond", C.c_double)]
+
+
 class MRGError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__("mrg status %d: %s" % (status, msg))
@@ -138,6 +199,56 @@ def _declare(lib):
         "mrg_pt_camera_frame": (C.c_int, [C.POINTER(MrgPtParams), fp]),
         "mrg_pt_render": (C.c_int, [vp, C.POINTER(MrgPtParams), vp, vp]),
     }
+    sz = C.c_size_t
+    sig.update({
+        "mrg_tracer_create": (C.c_int, [C.POINTER(MrgTracerParams), C.POINTER(vp)]),
+        "mrg_tracer_destroy": (C.c_int, [vp]),
+        "mrg_tracer_parameters": (C.c_int, [vp, C.POINTER(MrgTracerParams)]),
+        "mrg_tracer_type_names": (C.c_int, [vp, u32, C.c_char_p, sz, C.POINTER(sz)]),
+        "mrg_tracer_attribute_info": (C.c_int, [vp, u32, C.c_char_p, u32, C.POINTER(MrgTracerAttribInfo), u32p]),
+        "mrg_tracer_group_type_name": (C.c_int, [vp, u32, u32, C.c_char_p, sz]),
+        "mrg_tracer_create_prim_group": (C.c_int, [vp, C.c_char_p, u32p]),
+        "mrg_tracer_reserve_prim_batches": (C.c_int, [vp, u32, vp, u32, vp]),
+        "mrg_tracer_commit_prim_reservations": (C.c_int, [vp, u32]),
+        "mrg_tracer_is_prim_committed": (C.c_int, [vp, u32, u32p]),
+        "mrg_tracer_push_prim_attribute": (C.c_int, [vp, u32, u32, u32, u32, u32, vp, sz]),
+        "mrg_tracer_transform_primitives": (C.c_int, [vp, u32, vp, vp, u32]),
+        "mrg_tracer_set_boundary_surface": (C.c_int, [vp, u32, u32, u32p]),
+        "mrg_tracer_create_light_surface": (C.c_int, [vp, u32, u32, u32p]),
+        "mrg_tracer_create_camera_surface": (C.c_int, [vp, u32, u32, u32p]),
+        "mrg_tracer_create_surface": (C.c_int, [vp, C.POINTER(MrgTracerSurface), u32p]),
+        "mrg_tracer_commit_surfaces": (C.c_int, [vp, C.POINTER(MrgTracerCommitResult)]),
+        "mrg_tracer_get_cam_transform": (C.c_int, [vp, u32, fp]),
+        "mrg_tracer_set_spectral_data": (C.c_int, [vp, u32, vp, u32, vp, vp, vp, C.c_float, vp]),
+        "mrg_tracer_create_renderer": (C.c_int, [vp, C.c_char_p, u32p]),
+        "mrg_tracer_destroy_renderer": (C.c_int, [vp, u32]),
+        "mrg_tracer_push_renderer_attribute": (C.c_int, [vp, u32, u32, vp, sz]),
+        "mrg_tracer_start_render": (C.c_int, [vp, u32, u32, u32, u32, vp, vp, C.POINTER(MrgTracerRenderInfo)]),
+        "mrg_tracer_set_camera_transform": (C.c_int, [vp, u32, fp]),
+        "mrg_tracer_do_render_work": (C.c_int, [vp, C.POINTER(MrgTracerRenderOutput)]),
+        "mrg_tracer_read_film": (C.c_int, [vp, vp, sz]),
+        "mrg_tracer_stop_render": (C.c_int, [vp]),
+        "mrg_tracer_clear_all": (C.c_int, [vp]),
+        "mrg_tracer_flush": (C.c_int, [vp]),
+        "mrg_tracer_device_memory": (C.c_int, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+        "mrg_tracer_context": (vp, [vp]),
+        "mrg_tracer_commit_textures": (C.c_int, [vp]),
+        "mrg_tracer_create_texture2d": (C.c_int, [vp, u32, u32, u32, u32, u32p]),
+        "mrg_tracer_push_texture_data": (C.c_int, [vp, u32, u32, vp, sz]),
+    })
+    for kind in ("mat", "trans", "light", "cam"):
+        sig["mrg_tracer_commit_%s_reservations" % kind] = (C.c_int, [vp, u32])
+        sig["mrg_tracer_is_%s_committed" % kind] = (C.c_int, [vp, u32, u32p])
+    for name in ("mrg_tracer_create_mat_group", "mrg_tracer_create_trans_group", "mrg_tracer_create_camera_group"):
+        sig[name] = (C.c_int, [vp, C.c_char_p, u32p])
+    sig["mrg_tracer_create_light_group"] = (C.c_int, [vp, C.c_char_p, u32, u32p])
+    for name in ("mrg_tracer_reserve_materials", "mrg_tracer_reserve_transforms", "mrg_tracer_reserve_cameras"):
+        sig[name] = (C.c_int, [vp, u32, u32, vp])
+    sig["mrg_tracer_reserve_lights"] = (C.c_int, [vp, u32, u32, vp, vp])
+    for name in ("mrg_tracer_push_mat_attribute", "mrg_tracer_push_light_attribute"):
+        sig[name] = (C.c_int, [vp, u32, u32, u32, u32, vp, sz, vp])
+    for name in ("mrg_tracer_push_trans_attribute", "mrg_tracer_push_cam_attribute"):
+        sig[name] = (C.c_int, [vp, u32, u32, u32, u32, vp, sz])
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
         f.restype = res

@@ -253,8 +253,9 @@ def read_scene(path_or_text, base_dir=None):
         if isinstance(rad, dict):
             raise SceneError("textured area-light radiance is not supported")
         m = _transform(transforms, ls.get("transform"))
+        # light surfaces are not back-face culled (AcceleratorCommon.cu:345-365)
         surfaces.append(dict(pos=pos, idx=idx, m34=_m34(m), kind="light", radiance=[float(x) for x in rad],
-                             cull=True))
+                             cull=False))
     # boundary light
     env = None
     b = j["Boundary"]
@@ -266,7 +267,8 @@ def read_scene(path_or_text, base_dir=None):
             raise SceneError("boundary light %s is not supported (spherical mapping only)" % btyp)
         rad = ba.get("radiance", [1, 1, 1])
         if isinstance(rad, dict):
-            tex = _texture(textures, rad, base_dir).astype(np.float32)
+            tex = _texture(textures, rad, base_dir)
+            tex = tex.astype(np.float32) / 255.0 if tex.dtype == np.uint8 else tex.astype(np.float32)
         else:
             tex = np.ones((1, 1, 4), np.float32)
             tex[0, 0, :3] = [float(x) for x in rad]
@@ -279,20 +281,222 @@ def read_scene(path_or_text, base_dir=None):
     ctyp, ca = cams.get(int(cs["camera"]), (None, None))
     if ctyp != "Pinhole":
         raise SceneError("camera type %s is not supported" % ctyp)
+    fx, fy, near, far = _camera_fnp(ca)
+    cm = _transform(transforms, cs.get("transform"))
+    pos = cm @ np.append(np.asarray(ca["position"], np.float64), 1.0)
+    gaze = cm @ np.append(np.asarray(ca["gaze"], np.float64), 1.0)
+    up = cm[:3, :3] @ np.asarray(ca["up"], np.float64)
+    camera = dict(pos=tuple(pos[:3]), gaze=tuple(gaze[:3]), up=tuple(up), fov=(fx, fy), near_far=(near, far))
+    return surfaces, camera, env
+
+
+def _camera_fnp(ca):
+    """FovAndPlanes of a pinhole camera node (SceneLoaderMRay.cpp:626-644):
+    fov in radians on both axes from fov, isFovX and aspect, then the planes."""
     fov = math.radians(float(ca["fov"]))
     aspect = float(ca.get("aspect", 1.0))
     if ca.get("isFovX", True):
         fx, fy = fov, 2.0 * math.atan(math.tan(fov * 0.5) / aspect)
     else:
         fy, fx = fov, 2.0 * math.atan(math.tan(fov * 0.5) * aspect)
-    cm = _transform(transforms, cs.get("transform"))
-    pos = cm @ np.append(np.asarray(ca["position"], np.float64), 1.0)
-    gaze = cm @ np.append(np.asarray(ca["gaze"], np.float64), 1.0)
-    up = cm[:3, :3] @ np.asarray(ca["up"], np.float64)
     planes = ca.get("planes", [0.01, 1000.0])
-    camera = dict(pos=tuple(pos[:3]), gaze=tuple(gaze[:3]), up=tuple(up), fov=(fx, fy),
-                  near_far=(float(planes[0]), float(planes[1])))
-    return surfaces, camera, env
+    return [fx, fy, float(planes[0]), float(planes[1])]
+
+
+def load_tracer(tracer, path_or_text, base_dir=None, commit=True):
+    """Pushes a scene through the TracerI calls of a mray_gb300.tracer.Tracer
+    the way MRay's SceneLoaderMRay does (SceneLoaderMRay.cpp: one group per
+    type, reservations, commits, attribute pushes, then surfaces, light
+    surfaces, the boundary and camera surfaces) and commits the surfaces.
+    Only what the surfaces reference is loaded.  The type mapping (materials,
+    lights, defaults) happens behind the tracer's C ABI.  Returns
+    {"camera_surfaces": [ids], "commit": commit result or None}; commit=False
+    stops before the surface commit (the first call that needs the device)."""
+    j = load_jsonc(path_or_text)
+    base_dir = base_dir or (os.path.dirname(os.path.abspath(path_or_text)) if os.path.exists(str(path_or_text))
+                            else os.getcwd())
+    for key in ("Cameras", "Lights", "Mediums", "Transforms", "Textures", "Materials", "Primitives", "Boundary",
+                "Surfaces", "LightSurfaces", "CameraSurfaces"):
+        if key not in j:
+            raise SceneError("scene JSON lacks '%s'" % key)
+    cams, lights = _items(j["Cameras"]), _items(j["Lights"])
+    transforms, textures = _items(j["Transforms"]), _items(j["Textures"])
+    materials, prims = _items(j["Materials"]), _items(j["Primitives"])
+
+    def lst(v):
+        return v if isinstance(v, list) else [v]
+
+    # what the surfaces reference
+    used_mats, used_prims, used_trans = set(), set(), set()
+    for sf in j["Surfaces"]:
+        used_mats.update(int(m) for m in lst(sf["material"]))
+        used_prims.update(int(p) for p in lst(sf["primitive"]))
+        used_trans.add(int(sf.get("transform", 0)))
+        if "alphaMap" in sf and any(x != "-" for x in lst(sf["alphaMap"])):
+            raise SceneError("alpha maps are not supported")
+    used_lights = [int(ls["light"]) for ls in j["LightSurfaces"]]
+    used_trans.update(int(ls.get("transform", 0)) for ls in j["LightSurfaces"])
+    b = j["Boundary"]
+    used_trans.add(int(b.get("transform", 0)))
+    used_trans.update(int(cs.get("transform", 0)) for cs in j["CameraSurfaces"])
+    for lid in used_lights:
+        if lid not in lights:
+            raise SceneError("unknown light %d" % lid)
+        if lights[lid][0] != "Primitive":
+            raise SceneError("light surface type %s is not supported" % lights[lid][0])
+        used_prims.add(int(lights[lid][1]["primitive"]))
+
+    # textures: created now, their data pushed after CommitTextures
+    tex_pending, tex_map = [], {}
+
+    def texture(ref):
+        tid = int(ref["texture"])
+        if tid not in tex_map:
+            t = _texture(textures, ref, base_dir)
+            kind = "rgba8_unorm" if t.dtype == np.uint8 else "rgba_float"
+            tex_map[tid] = tracer.create_texture_2d(t.shape[1], t.shape[0], 1, kind)
+            tex_pending.append((tex_map[tid], np.ascontiguousarray(t if t.dtype == np.uint8 else t.astype(np.float32))))
+        return tex_map[tid]
+
+    # transforms: (T)Identity is the implicit transform 0
+    trans_ids, singles = {}, []
+    for tid in sorted(used_trans):
+        if tid not in transforms:
+            raise SceneError("unknown transform %s" % tid)
+        typ = transforms[tid][0]
+        if typ == "Identity":
+            trans_ids[tid] = 0
+        elif typ == "Single":
+            singles.append(tid)
+        else:
+            raise SceneError("transform type %s is not supported" % typ)
+    if singles:
+        g = tracer.create_transform_group("(T)Single")
+        for tid, nid in zip(singles, tracer.reserve_transformations(g, len(singles))):
+            trans_ids[tid] = nid
+        tracer.commit_trans_reservations(g)
+        for tid in singles:
+            m = np.asarray(_transform(transforms, tid), np.float32).reshape(16)
+            tracer.push_trans_attribute(g, (trans_ids[tid], trans_ids[tid]), 0, m)
+
+    # primitives: one (P)Triangle group, a batch per primitive
+    from .tracer import INDEX, POSITION, UV0
+    meshes = {pid: _mesh(prims, pid, base_dir) for pid in sorted(used_prims)}
+    pg = tracer.create_primitive_group("(P)Triangle")
+    order = sorted(meshes)
+    batch = dict(zip(order, tracer.reserve_primitive_batches(
+        pg, [(meshes[p][1].shape[0], meshes[p][0].shape[0]) for p in order])))
+    tracer.commit_prim_reservations(pg)
+    for pid in order:
+        pos, idx, uv = meshes[pid]
+        tracer.push_prim_attribute(pg, batch[pid], POSITION, pos)
+        tracer.push_prim_attribute(pg, batch[pid], INDEX, idx)
+        if uv is not None:
+            tracer.push_prim_attribute(pg, batch[pid], UV0, uv)
+
+    # materials: a group per type
+    by_type = {}
+    for mid in sorted(used_mats):
+        if mid not in materials:
+            raise SceneError("unknown material %s" % mid)
+        by_type.setdefault(materials[mid][0], []).append(mid)
+    mat_ids = {}
+    for typ, mids in by_type.items():
+        if typ not in ("Lambert", "Reflect", "Refract", "Unreal"):
+            raise SceneError("material type %s is not supported" % typ)
+        g = tracer.create_material_group("(Mt)" + typ)
+        for mid, nid in zip(mids, tracer.reserve_materials(g, len(mids))):
+            mat_ids[mid] = nid
+        tracer.commit_mat_reservations(g)
+        for mid in mids:
+            a, r = materials[mid][1], (mat_ids[mid], mat_ids[mid])
+            if typ in ("Lambert", "Unreal"):
+                alb = a.get("albedo", [0.5, 0.5, 0.5])
+                if isinstance(alb, dict):
+                    tracer.push_mat_attribute(g, r, 0, None, [texture(alb)])
+                else:
+                    tracer.push_mat_attribute(g, r, 0, [0.5, 0.5, 0.5] if alb == "-" else alb, [None])
+            if typ == "Unreal":
+                for k, (name, dflt) in enumerate((("roughness", 0.5), ("specular", 0.5), ("metallic", 0.0))):
+                    v = a.get(name, dflt)
+                    if isinstance(v, dict):
+                        raise SceneError("material %s: textured %s is not supported" % (mid, name))
+                    tracer.push_mat_attribute(g, r, 2 + k, [float(v)], [None])
+            if typ == "Refract":
+                tracer.push_mat_attribute(g, r, 0, a.get("cauchyBack", [1.0, 0.0, 0.0]))
+                tracer.push_mat_attribute(g, r, 1, a.get("cauchyFront", [1.0, 0.0, 0.0]))
+
+    # lights: primitive-backed ones in one group, the boundary light
+    light_ids = {}
+    prim_lights = sorted(set(used_lights))
+    if prim_lights:
+        g = tracer.create_light_group("(L)Prim(P)Triangle", pg)
+        ids = tracer.reserve_lights(g, len(prim_lights), [batch[int(lights[l][1]["primitive"])] for l in prim_lights])
+        light_ids.update(zip(prim_lights, ids))
+        tracer.commit_light_reservations(g)
+        for lid in prim_lights:
+            a = lights[lid][1]
+            rad = a.get("radiance", [1, 1, 1])
+            if isinstance(rad, dict):
+                raise SceneError("textured area-light radiance is not supported")
+            r = (light_ids[lid], light_ids[lid])
+            tracer.push_light_attribute(g, r, 0, rad, [None])
+            tracer.push_light_attribute(g, r, 1, [1 if a.get("isTwoSided", False) else 0], dtype=np.uint8)
+    blid = int(b["light"])
+    if blid not in lights:
+        raise SceneError("unknown boundary light")
+    btyp, ba = lights[blid]
+    if btyp == "Null":
+        boundary_light = 0
+    elif btyp in ("Skysphere_Spherical", "Skysphere"):
+        g = tracer.create_light_group("(L)Skysphere_Spherical")
+        boundary_light = tracer.reserve_lights(g, 1)[0]
+        tracer.commit_light_reservations(g)
+        rad = ba.get("radiance", [1, 1, 1])
+        r = (boundary_light, boundary_light)
+        if isinstance(rad, dict):
+            tracer.push_light_attribute(g, r, 0, None, [texture(rad)])
+        else:
+            tracer.push_light_attribute(g, r, 0, rad, [None])
+    else:
+        raise SceneError("boundary light %s is not supported" % btyp)
+
+    # cameras
+    cam_used = sorted({int(cs["camera"]) for cs in j["CameraSurfaces"]})
+    cam_ids = {}
+    if cam_used:
+        for cid in cam_used:
+            if cams.get(cid, (None,))[0] != "Pinhole":
+                raise SceneError("camera type %s is not supported" % cams.get(cid, (None,))[0])
+        g = tracer.create_camera_group("(C)Pinhole")
+        cam_ids = dict(zip(cam_used, tracer.reserve_cameras(g, len(cam_used))))
+        tracer.commit_cam_reservations(g)
+        for cid in cam_used:
+            ca, r = cams[cid][1], (cam_ids[cid], cam_ids[cid])
+            tracer.push_cam_attribute(g, r, 0, _camera_fnp(ca))
+            tracer.push_cam_attribute(g, r, 1, ca["gaze"])
+            tracer.push_cam_attribute(g, r, 2, ca["position"])
+            tracer.push_cam_attribute(g, r, 3, ca["up"])
+
+    tracer.commit_textures()
+    for tid, data in tex_pending:
+        tracer.push_texture_data(tid, 0, data)
+
+    # surfaces, light surfaces, boundary, camera surfaces
+    for sf in j["Surfaces"]:
+        mats, pids = lst(sf["material"]), lst(sf["primitive"])
+        if len(mats) != len(pids):
+            raise SceneError("surface material / primitive counts differ")
+        culls = sf.get("cullFace", True)
+        culls = culls if isinstance(culls, list) else [culls] * len(pids)
+        tracer.create_surface([batch[int(p)] for p in pids], [mat_ids[int(m)] for m in mats],
+                              trans_ids[int(sf.get("transform", 0))], culls)
+    for ls in j["LightSurfaces"]:
+        tracer.create_light_surface(light_ids[int(ls["light"])], trans_ids[int(ls.get("transform", 0))])
+    tracer.set_boundary_surface(boundary_light, trans_ids[int(b.get("transform", 0))])
+    cam_surfaces = [tracer.create_camera_surface(cam_ids[int(cs["camera"])], trans_ids[int(cs.get("transform", 0))])
+                    for cs in j["CameraSurfaces"]]
+    return {"camera_surfaces": cam_surfaces, "commit": tracer.commit_surfaces() if commit else None}
 
 
 def load(pt, path_or_text, base_dir=None):

@@ -1,5 +1,5 @@
 """The C-ABI library builds, loads and exports every symbol declared in
-include/mray_gb300.h; argument checks that need no GPU behave."""
+include/*.h; argument checks that need no GPU behave."""
 import ctypes as C
 import os
 import re
@@ -9,14 +9,20 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "mray_gb300.h")).read()
-    return sorted(set(re.findall(r"\b(mrg_[a-z_]+)\s*\(", src)))
+def declared_symbols(header=None):
+    names = [header] if header else sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h"))
+    out = set()
+    for h in names:
+        src = open(os.path.join(ROOT, "include", h)).read()
+        out |= set(re.findall(r"\b(mrg_[a-z_0-9]+)\s*\(", src))
+    return sorted(out)
 
 
 def test_header_and_binding_list_agree():
     from mray_gb300 import _native as N
-    assert declared_symbols() == sorted(N.EXPORTED)
+    assert declared_symbols("mray_gb300.h") == sorted(N.EXPORTED)
+    tracer = [n for n in declared_symbols("mray_gb300_tracer.h") if n.startswith("mrg_tracer_")]
+    assert tracer == sorted(N.TRACER_EXPORTED)
 
 
 def test_library_exports_every_declared_symbol(cuda_lib):
