@@ -145,6 +145,51 @@ def profile_figures():
     return out
 
 
+def pt_profile_figures():
+    """DRAM and L2 bytes of one render call of the C0 / C2 path-tracing
+    workloads (every kernel of the call summed) from the committed ncu
+    summary: lines '<w>_dram_bytes_per_call: value' and
+    '<w>_l2_bytes_per_call: value'."""
+    out = {}
+    tp = os.path.join(ROOT, "profiles", "pt_workloads_roofline.md")
+    if os.path.exists(tp):
+        for ln in open(tp):
+            for w in ("c0", "c2"):
+                for key in ("dram_bytes_per_call", "l2_bytes_per_call"):
+                    if ln.startswith("%s_%s:" % (w, key)):
+                        try:
+                            out.setdefault(w, {})[key] = int(ln.split(":", 1)[1].strip())
+                        except ValueError:
+                            pass
+    return out
+
+
+def pt_roofline(extra, hbm_peak, l2_peak):
+    """Roofline lines of the C0 and C2 render calls: the profiled DRAM and L2
+    bytes of one call over the call's live time (CUDA events, streams
+    overlapped), against the measured HBM and L2 copy peaks."""
+    prof = pt_profile_figures()
+    out = {}
+    for w, ms_key, paths in (("c0", "box_pt_ms_per_16spp", 256 * 256 * 16),
+                             ("c2", "c2_ms_per_4spp_1080p", 1920 * 1080 * 4)):
+        ms = extra.get(ms_key)
+        f = prof.get(w)
+        if not ms or not f:
+            continue
+        sec = ms * 1e-3
+        line = {"ms_per_call": ms, "paths_per_call": paths, "mpaths_per_s": round(paths / sec / 1e6, 1)}
+        if "dram_bytes_per_call" in f:
+            gbs = f["dram_bytes_per_call"] / sec / 1e9
+            line.update(dram_bytes_per_path=round(f["dram_bytes_per_call"] / paths, 1), dram_gbs=round(gbs, 1),
+                        dram_frac_of_measured_hbm=round(gbs / hbm_peak, 3))
+        if "l2_bytes_per_call" in f:
+            gbs = f["l2_bytes_per_call"] / sec / 1e9
+            line.update(l2_bytes_per_path=round(f["l2_bytes_per_call"] / paths, 1), l2_gbs=round(gbs, 1),
+                        l2_frac_of_measured_l2=round(gbs / l2_peak, 3))
+        out[w] = line
+    return out
+
+
 def make_workload(seed=0):
     from mray_gb300 import scenes
     pos, idx, m = scenes.bvh_stress_scene(seed=seed)
@@ -368,6 +413,7 @@ def gpu_arm(args):
         line["extra"].update(c2_scene_pt(args, dev))
         line["extra"].update(c3_adjoint(args, dev))
         line["extra"].update(c4_equal_time(args, dev))
+    line["extra"]["pt_roofline"] = pt_roofline(line["extra"], peak, l2_peak)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, idx, m, rays_np, budget_s=args.cpu_seconds)
         if not args.no_pt_extras:
@@ -389,6 +435,12 @@ def box_scene_pt(args, dev):
     load_box_scene(pt, 0)
     cam = scenes.box_camera()
     reps = max(3, min(args.steps, 20))
+
+    if getattr(args, "single_call", False):
+        pt.render(PathTracer.params(256, 256, 16, cam, max_depth=8, rr_start=3, seed=0))
+        torch.cuda.synchronize(dev)
+        pt.close()
+        return {"single_call": True}
 
     def timed(sampler):
         # the ZSobol group's initial sample count covers every timed call
@@ -440,6 +492,9 @@ def c2_scene_pt(args, dev):
     p = PathTracer.params(1920, 1080, spp, cam, max_depth=12, rr_start=3, seed=0)
     img = pt.render(p)
     torch.cuda.synchronize(dev)
+    if getattr(args, "single_call", False):
+        pt.close()
+        return {"single_call": True}
     reps = max(3, min(args.steps // 20, 16))
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -792,6 +847,9 @@ def main():
                     help="skip the production-scene and adjoint path-tracing lines")
     ap.add_argument("--only", choices=["c0", "c2", "c3", "c4", "cache"], default=None,
                     help="run one path-tracing workload alone and print its line (for profiling)")
+    ap.add_argument("--single-call", action="store_true",
+                    help="with --only c0 / c2: build the scene and render exactly one call, untimed "
+                         "(the case the path-tracing roofline profile captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

@@ -294,6 +294,39 @@ def test_c2_scene_spectral_small():
     pt.close()
 
 
+def test_c0_configured_size(box):
+    """The C0 bench workload itself: the box scene at 256 x 256, 16 spp,
+    depth 8, Russian roulette from bounce 3, NEE + MIS, per pixel against the
+    oracle (same bars as the small cases)."""
+    pt, S = box
+    cam = scenes.box_camera()
+    p = dict(max_depth=8, rr_start=3, sample_mode=2, seed=19)
+    g = _img(pt.render(PathTracer.params(256, 256, 16, cam, **p)))
+    o = _img(S.render(S.params(256, 256, 16, cam, **p)))
+    frac = (np.abs(g - o) <= 1e-4 * (1.0 + np.abs(o))).all(axis=-1).mean()
+    print("c0 256x256x16: close %.5f relMSE %.3g" % (frac, relmse(g, o)))
+    assert frac >= 0.97, frac
+    assert relmse(g, o) <= 1e-3
+
+
+def test_c2_configured_textures():
+    """The C2 workload's scene as benchmarked -- 2048^2 textures, a 1024 x 512
+    sky, 4 wavelengths, depth 12 -- at a 480 x 270 film and 4 spp against the
+    oracle (the same bars as the small C2 case)."""
+    surf, cam = scenes.c2_scene(0, texture_size=2048)
+    env = dict(texels=scenes.sky_map(1024, 512, seed=0))
+    pt, S = _spectral_pair(surf, env)
+    g = _img(pt.render(PathTracer.params(480, 270, 4, cam, max_depth=12, rr_start=3, seed=6)))
+    o = _img(S.render(S.params(480, 270, 4, cam, max_depth=12, rr_start=3, seed=6)))
+    close = (np.abs(g - o) <= 1e-4 * (1.0 + np.abs(o))).all(axis=-1).mean()
+    d = np.abs(g - o).max(axis=-1).ravel()
+    keep = d <= np.quantile(d, 0.98)
+    rel_kept = float(np.mean(((g - o).reshape(-1, 3)[keep]) ** 2 / (o.reshape(-1, 3)[keep] ** 2 + 1e-2)))
+    print("c2 480x270x4 2048^2 textures: close %.4f relMSE %.3g kept %.3g" % (close, relmse(g, o), rel_kept))
+    assert close >= 0.95 and rel_kept <= 1e-5
+    pt.close()
+
+
 @pytest.mark.parametrize("mode", [0, 2])
 def test_mray_scene_file_per_pixel(mode):
     """A scene read from MRay's JSON format (textured floor, mirror, glass,
