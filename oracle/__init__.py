@@ -90,6 +90,10 @@ def lib():
         L.orc_zs_number.argtypes = [u32, u32, u32, u32, u32, u32, u32, u32, u32, C.c_int]
         L.orc_zs_number.restype = u32
         L.orc_pcg32_numbers.argtypes = [vp, vp, u32, vp]
+        L.orc_guide_lobe_batch.argtypes = [vp, vp, vp, u32]
+        L.orc_conc_octa_batch.argtypes = [vp, vp, vp, vp, u32]
+        L.orc_guide_codes_batch.argtypes = [vp, vp, vp, vp, u32]
+        L.orc_guide_table_batch.argtypes = [vp, u32, vp, u32, u32, vp, vp]
         L.orc_pt_render.restype = C.c_int
         L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
         L.orc_pt_make_light.argtypes = [vp, vp, vp, C.c_int, vp]
@@ -695,6 +699,46 @@ def pcg32_numbers(seeds, delta):
     out = np.zeros(sd.shape, np.uint32)
     lib().orc_pcg32_numbers(_vp(sd), _vp(dl), sd.size, _vp(out))
     return out
+
+
+def guide_lobe(in7, w3):
+    """Gaussian (vMF) lobe records (dir, kappa, xi0, xi1, -) and a direction
+    each -> (alpha, sample dir, pdf of the sample, pdf of w, XOverExp1M,
+    XOverExp1MRecip of -2 kappa)."""
+    a = np.ascontiguousarray(in7, np.float32)
+    w = np.ascontiguousarray(w3, np.float32)
+    out = np.zeros((a.shape[0], 8), np.float32)
+    lib().orc_guide_lobe_batch(_vp(a), _vp(w), _vp(out), a.shape[0])
+    return out
+
+
+def conc_octa(dirs, sts):
+    d = np.ascontiguousarray(dirs, np.float32)
+    s = np.ascontiguousarray(sts, np.float32)
+    st2 = np.zeros((d.shape[0], 2), np.float32)
+    dout = np.zeros((s.shape[0], 3), np.float32)
+    lib().orc_conc_octa_batch(_vp(d), _vp(st2), _vp(s), _vp(dout), d.shape[0])
+    return st2, dout
+
+
+def guide_codes(view15, in6, rng):
+    """(GenCode, GenCodeStochastic) per record; rng: PCG32 states (a copy is
+    advanced)."""
+    v = np.ascontiguousarray(view15, np.float32)
+    q = np.ascontiguousarray(in6, np.float32)
+    r = np.array(rng, np.uint32, copy=True)
+    out = np.zeros((q.shape[0], 2), np.uint64)
+    lib().orc_guide_codes_batch(_vp(v), _vp(q), _vp(r), _vp(out), q.shape[0])
+    return out, r
+
+
+def guide_table(codes, probe, size):
+    c = np.ascontiguousarray(codes, np.uint64)
+    p = np.ascontiguousarray(probe, np.uint64)
+    slots = np.zeros(c.size, np.uint32)
+    found = np.zeros(p.size, np.uint32)
+    lib().orc_guide_table_batch(_vp(c), c.size, _vp(p), p.size, size, _vp(slots), _vp(found))
+    return slots, found
 
 
 def zsobol_generate(width, height, seeds, initial_max_spp, sample_index, dim_start, requests):

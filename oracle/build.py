@@ -22,7 +22,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_LIB = os.path.join(BUILD_DIR, "libmrg_oracle.so")
 REF_LIB = os.path.join(REF_DIR, "libmray_ref_core.so")
 
-ORACLE_SOURCES = ["mrg_oracle.c", "pt_oracle.c", "zsobol_oracle.c"]
+ORACLE_SOURCES = ["mrg_oracle.c", "pt_oracle.c", "zsobol_oracle.c", "guide_oracle.c"]
 
 
 def reference_source_dir():

@@ -166,6 +166,41 @@ def pcg32_seq(seed, n):
     return out
 
 
+def guide_lobe(in7, w3):
+    a = np.ascontiguousarray(in7, np.float32)
+    w = np.ascontiguousarray(w3, np.float32)
+    out = np.zeros((a.shape[0], 8), np.float32)
+    load().ref_guide_lobe(_p(a), _p(w), _p(out), C.c_uint32(a.shape[0]))
+    return out
+
+
+def conc_octa(dirs, sts):
+    d = np.ascontiguousarray(dirs, np.float32)
+    s = np.ascontiguousarray(sts, np.float32)
+    st2 = np.zeros((d.shape[0], 2), np.float32)
+    dout = np.zeros((s.shape[0], 3), np.float32)
+    load().ref_conc_octa(_p(d), _p(st2), _p(s), _p(dout), C.c_uint32(d.shape[0]))
+    return st2, dout
+
+
+def guide_codes(view15, in6, rng):
+    v = np.ascontiguousarray(view15, np.float32)
+    q = np.ascontiguousarray(in6, np.float32)
+    r = np.array(rng, np.uint32, copy=True)
+    out = np.zeros((q.shape[0], 2), np.uint64)
+    load().ref_guide_codes(_p(v), _p(q), _p(r), _p(out), C.c_uint32(q.shape[0]))
+    return out, r
+
+
+def guide_table(codes, probe, size):
+    c = np.ascontiguousarray(codes, np.uint64)
+    p = np.ascontiguousarray(probe, np.uint64)
+    slots = np.zeros(c.size, np.uint32)
+    found = np.zeros(p.size, np.uint32)
+    load().ref_guide_table(_p(c), C.c_uint32(c.size), _p(p), C.c_uint32(p.size), C.c_uint32(size), _p(slots), _p(found))
+    return slots, found
+
+
 class Spectral:
     """MRay's Jakob 2019 converter over a resolution-64 LUT (the converter's
     compile-time resolution)."""

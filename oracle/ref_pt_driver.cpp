@@ -30,6 +30,7 @@
 #include "Tracer/TransformsDefault.h"
 #include "Tracer/TransformsDefault.hpp"
 #include "Tracer/TextureView.hpp"
+#include "Tracer/HashGrid.h"
 #include "Device/CPU/GPUSystemCPU.hpp"
 // the wavelength sampler and the spectrum -> RGB conversion are free device
 // functions of this translation unit of MRay (host backend)
@@ -547,6 +548,77 @@ void ref_pcg32_seq(uint32_t seed, uint32_t n, uint32_t* out)
     PermutedCG32::State st = PermutedCG32::GenerateState(seed);
     PermutedCG32 rng(st);
     for(uint32_t i = 0; i < n; i++) out[i] = rng.Next();
+}
+
+// MRay's guided path tracer's building blocks.
+// Gaussian (vMF) lobe: in7 = dir[3], kappa, xi0, xi1, (unused); w3 = a direction
+// to evaluate.  out8 = alpha, sample dir[3], Pdf(sample), Pdf(w), XOverExp1M(-2 kappa),
+// XOverExp1MRecip(-2 kappa).
+void ref_guide_lobe(const float* in7, const float* w3, float* out8, uint32_t n)
+{
+    using Distribution::GaussianLobe;
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in7 + 7 * i;
+        GaussianLobe l(Vector3(q[0], q[1], q[2]), q[3]);
+        auto s = l.Sample(Vector2(q[4], q[5]));
+        const float* w = w3 + 3 * i;
+        float* o = out8 + 8 * i;
+        o[0] = l.alpha;
+        o[1] = s.value[0]; o[2] = s.value[1]; o[3] = s.value[2];
+        o[4] = s.pdf;
+        o[5] = l.Pdf(Vector3(w[0], w[1], w[2]));
+        o[6] = GaussianLobe::XOverExp1M(-2.0f * q[3]);
+        o[7] = GaussianLobe::XOverExp1MRecip(-2.0f * q[3]);
+    }
+}
+
+// Concentric octahedral mapping: dir3 -> st (DirectionToConcentricOctahedral),
+// st2 -> dir (ConcentricOctahedralToDirection).
+void ref_conc_octa(const float* dir3, float* st2, const float* stIn, float* dirOut, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        Vector2 st = Graphics::DirectionToConcentricOctahedral(Vector3(dir3[3 * i], dir3[3 * i + 1], dir3[3 * i + 2]));
+        st2[2 * i] = st[0]; st2[2 * i + 1] = st[1];
+        Vector3 d = Graphics::ConcentricOctahedralToDirection(Vector2(stIn[2 * i], stIn[2 * i + 1]));
+        dirOut[3 * i] = d[0]; dirOut[3 * i + 1] = d[1]; dirOut[3 * i + 2] = d[2];
+    }
+}
+
+// Hash-grid codes of HashGridView (HashGrid.h): view = the grid's fields as
+// floats / words [cam3, rmin3, rmax3, baseDelta, baseDim, normalDelta,
+// normalDim, maxLevelOffset, tanConeHalfTimes2]; in6 = pos, normal; rng =
+// PermutedCG32 states (updated).  out: GenCode, GenCodeStochastic.
+void ref_guide_codes(const float* view15, const float* in6, uint32_t* rng, uint64_t* out2, uint32_t n)
+{
+    uint32_t counter = 0;
+    HashGridView v{ Span<SpatioDirCode>(), Span<uint32_t, 1>(&counter, 1),
+                    Vector3(view15[0], view15[1], view15[2]),
+                    AABB3(Vector3(view15[3], view15[4], view15[5]), Vector3(view15[6], view15[7], view15[8])),
+                    view15[9], uint32_t(view15[10]), view15[11], uint32_t(view15[12]), uint32_t(view15[13]),
+                    0u, view15[14] };
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in6 + 6 * i;
+        const Vector3 p(q[0], q[1], q[2]), nn(q[3], q[4], q[5]);
+        out2[2 * i] = uint64_t(v.GenCode(p, nn));
+        BackupRNG r(rng[i]);
+        out2[2 * i + 1] = uint64_t(v.GenCodeStochastic(p, nn, r));
+    }
+}
+
+// HashGridView::TryInsert then Search over a table of `size` (a power of two)
+// codes: slots[i] = TryInsert(codes[i]), found[i] = Search(probe[i]).
+void ref_guide_table(const uint64_t* codes, uint32_t n, const uint64_t* probe, uint32_t m, uint32_t size,
+                     uint32_t* slots, uint32_t* found)
+{
+    std::vector<SpatioDirCode> table(size, HashGridView::EMPTY_VAL);
+    uint32_t counter = 0;
+    HashGridView v{ Span<SpatioDirCode>(table.data(), size), Span<uint32_t, 1>(&counter, 1), Vector3::Zero(),
+                    AABB3(Vector3::Zero(), Vector3(1)), 1.0f, 1u, 1.0f, 1u, 0u, size, 1.0f };
+    for(uint32_t i = 0; i < n; i++) slots[i] = v.TryInsert(SpatioDirCode(codes[i])).allocationIndex;
+    for(uint32_t i = 0; i < m; i++) found[i] = v.Search(SpatioDirCode(probe[i])).value_or(0xFFFFFFFFu);
 }
 
 }  // extern "C"

@@ -26,6 +26,10 @@ Covered (MRay file:line):
                  and the group's per-pixel seeds (Random.cu:1175-1200)
   pcg32          PermutedCG32 GenerateState / Advance / Next (Tracer/Random.h:762-842),
                  the independent group's generator
+  guide          the guided path tracer's blocks: Distribution::GaussianLobe
+                 (Tracer/DistributionFunctions.h:230-380), concentric octahedral mapping
+                 (Core/GraphicsFunctions.h:318-384), HashGridView GenCode /
+                 GenCodeStochastic / TryInsert / Search (Tracer/HashGrid.h:230-400)
 
 Usage: python tests/golden/make_pt_golden.py
 """
@@ -220,12 +224,45 @@ def pcg32(rng):
             "pcg_seq_seed": np.uint32(0x9E3779B9), "pcg_seq": ref_pt.pcg32_seq(0x9E3779B9, 4096)}
 
 
+def guide(rng):
+    n = N
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    kap = np.concatenate([np.zeros(8), np.full(8, 1e-8), rng.uniform(0, 0.5, 250), rng.uniform(0.5, 50, 500),
+                          10 ** rng.uniform(1.7, 4, n - 766)]).astype(np.float32)
+    xi = rng.random((n, 2)).astype(np.float32)
+    xi[:4] = [[0, 0], [0.99999994, 0.99999994], [0.5, 0], [0, 0.5]]
+    in7 = np.concatenate([d, kap[:, None], xi, np.zeros((n, 1), np.float32)], 1).astype(np.float32)
+    w = rng.normal(size=(n, 3)).astype(np.float32)
+    w /= np.linalg.norm(w, axis=1, keepdims=True)
+    st = rng.random((n, 2)).astype(np.float32)
+    dd = d.copy()
+    dd[:4] = [[0, 0, 1], [0, 0, -1], [1, 0, 0], [0, -1, 0]]
+    octa_st, octa_dir = ref_pt.conc_octa(dd, st)
+    # a grid over [-1, 2] x [-1, 2.5] x [-1, 3], 2^14 base cells, 4 x 4 normals,
+    # 3 level offsets, a 0.6 degree cone (the guided renderer's defaults)
+    view = np.array([0.5, 0.5, -1.4, -1, -1, -1, 2, 2.5, 3, 16384 / 4.0, 16384, 4, 4, 3, 0], np.float32)
+    view[14] = np.float32(np.tan(np.float32(np.float32(np.pi) / np.float32(180)) * np.float32(0.6) *
+                                 np.float32(0.5))) * np.float32(2)
+    pos = rng.uniform(-1.2, 3.2, (n, 3)).astype(np.float32)
+    in6 = np.concatenate([pos, dd], 1).astype(np.float32)
+    rs = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    codes, rs_after = ref_pt.guide_codes(view, in6, rs)
+    tcodes = rng.integers(0, 2 ** 63, 600, dtype=np.uint64)
+    probe = np.concatenate([tcodes[::3], rng.integers(0, 2 ** 63, 200, dtype=np.uint64)])
+    slots, found = ref_pt.guide_table(tcodes, probe, 1024)
+    return {"gl_in": in7, "gl_w": w, "gl_out": ref_pt.guide_lobe(in7, w), "go_dir": dd, "go_st": st,
+            "go_st_out": octa_st, "go_dir_out": octa_dir, "gc_view": view, "gc_in": in6, "gc_rng": rs,
+            "gc_out": codes, "gc_rng_out": rs_after, "gt_codes": tcodes, "gt_probe": probe, "gt_slots": slots,
+            "gt_found": found}
+
+
 def main():
     if ref_pt.load() is None:
         sys.exit("the MRay source tree and fmt headers are needed (MRAY_REFERENCE_SRC)")
     rng = np.random.default_rng(20261204)
     out = {}
-    for f in (materials, building_blocks, lights, distributions, cameras, waves, zsobol, pcg32):
+    for f in (materials, building_blocks, lights, distributions, cameras, waves, zsobol, pcg32, guide):
         out.update(f(rng))
     path = os.path.join(HERE, "pt_math.npz")
     np.savez_compressed(path, **out)

@@ -120,6 +120,23 @@ def test_pcg32_streams_match_mray(g):
     assert np.array_equal(got, seq)
 
 
+def test_guided_lobe_matches_mray(g):
+    got = oracle.guide_lobe(g["gl_in"], g["gl_w"])
+    assert same(got, g["gl_out"])
+
+
+def test_concentric_octahedral_matches_mray(g):
+    st, d = oracle.conc_octa(g["go_dir"], g["go_st"])
+    assert same(st, g["go_st_out"]) and same(d, g["go_dir_out"])
+
+
+def test_hash_grid_codes_and_table_match_mray(g):
+    codes, rs = oracle.guide_codes(g["gc_view"], g["gc_in"], g["gc_rng"])
+    assert np.array_equal(codes, g["gc_out"]) and np.array_equal(rs, g["gc_rng_out"])
+    slots, found = oracle.guide_table(g["gt_codes"], g["gt_probe"], 1024)
+    assert np.array_equal(slots, g["gt_slots"]) and np.array_equal(found, g["gt_found"])
+
+
 # ---- where the MRay tree is present: MRay's code run here -----------------
 
 def _ref():
