@@ -460,6 +460,54 @@ mrg_status mrg_pt_camera_frame(const mrg_pt_params* params, float out[16]);
  * inside a pass. */
 mrg_status mrg_pt_render(mrg_ctx* ctx, const mrg_pt_params* params, float* d_image, void* stream);
 
+/* ---------------------------------------------------------------------- */
+/* Guided path tracing: MRay's GuidedPTRenderer (Markov-chain mixtures     */
+/* after Alber et al. 2025 on a spatio-directional hash grid;              */
+/* Source/TracerDLL/GuidedPTRenderer.{h,cu}, GuidedPTRendererShaders.h,    */
+/* Source/Tracer/HashGrid.{h,cu}).                                         */
+/* ---------------------------------------------------------------------- */
+/* GuidedPTRDetail::Options (GuidedPTRendererShaders.h:75-133); defaults in
+ * parentheses. */
+typedef struct mrg_guide_params
+{
+    uint32_t entryLimit;        /* cacheEntryLimit (2,000,000): the table holds
+                                   NextPowerOfTwo(entryLimit / 0.6) codes and
+                                   takes new ones up to 60% of them */
+    uint32_t posBits;           /* cachePosBits (14), at most 15 */
+    uint32_t normalBits;        /* cacheNormalBits (2), at most 3 */
+    uint32_t maxLevelOffset;    /* cacheMaxLvlOffset (3) */
+    float    coneAperture;      /* cacheConeAperture, degrees (0.6) */
+    float    lobeProbability;   /* lobeProbablity (0.75) */
+    uint32_t reserved[2];
+} mrg_guide_params;
+mrg_status mrg_guide_defaults(mrg_guide_params* out);
+/* Allocates the context's grid over the scene box of the last mrg_build
+ * (HashGrid::Reset with the accelerator's SceneAABB) and empties it. */
+mrg_status mrg_guide_create(mrg_ctx* ctx, const mrg_guide_params* params);
+/* Empties the grid, its chains and irradiance averages, and restarts the
+ * paths' backup random streams; the next render takes its camera position
+ * (HashGrid::ClearAllEntries, SetCameraPos). */
+mrg_status mrg_guide_clear(mrg_ctx* ctx);
+mrg_status mrg_guide_destroy(mrg_ctx* ctx);
+/* Entries in use and the table size.  Synchronous. */
+mrg_status mrg_guide_stats(mrg_ctx* ctx, uint32_t* used, uint32_t* table_size);
+/* Snapshot of the table: per slot its code (~0: empty), chain state (6
+ * floats: target xyz, cosine, weight, sample count) and irradiance average
+ * (2 floats: value, sample count).  Any pointer may be NULL.  Synchronous. */
+mrg_status mrg_guide_read(mrg_ctx* ctx, uint64_t* h_codes, float* h_chain6, float* h_irr2);
+/* Guided rendering: params->spp samples per pixel ADDED to d_image as
+ * mrg_pt_render does, learning in the grid as it goes (one pass of
+ * samplesPerPass samples per pixel at a time, bounce by bounce).
+ * russianRouletteRange = (rrStart, maxDepth); NEE with MIS always (sampleMode
+ * is not read); samplers MRG_PT_SAMPLER_INDEPENDENT and MRG_PT_SAMPLER_PCG32.
+ * Each path slot (width * height * samplesPerPass of them) has a backup PCG32
+ * stream for the grid's choices, its state GenerateState(output
+ * width * height + slot of std::mt19937(params.seed)), continued from call to
+ * call until mrg_guide_clear.  Irradiance updates of a bounce are applied in
+ * a fixed order (path, NEE, light records, slot by slot per cell), so a
+ * render is reproducible run to run. */
+mrg_status mrg_pt_render_guided(mrg_ctx* ctx, const mrg_pt_params* params, float* d_image, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

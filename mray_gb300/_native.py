@@ -35,6 +35,8 @@ EXPORTED = [
     "mrg_zsobol_seeds", "mrg_zsobol_generate",
     "mrg_cache_create", "mrg_cache_query", "mrg_cache_train", "mrg_cache_get_params", "mrg_cache_set_params",
     "mrg_cache_gradients", "mrg_pt_render_cached",
+    "mrg_guide_defaults", "mrg_guide_create", "mrg_guide_clear", "mrg_guide_destroy", "mrg_guide_stats",
+    "mrg_guide_read", "mrg_pt_render_guided",
 ]
 
 MRG_MAT_LAMBERT, MRG_MAT_REFLECT, MRG_MAT_REFRACT, MRG_MAT_UNREAL = 0, 1, 2, 3
@@ -139,6 +141,12 @@ class MrgTracerRenderInfo(C.Structure):
                 ("channels", C.c_uint32), ("d_film", C.c_void_p)]
 
 
+class MrgGuideParams(C.Structure):
+    _fields_ = [("entryLimit", C.c_uint32), ("posBits", C.c_uint32), ("normalBits", C.c_uint32),
+                ("maxLevelOffset", C.c_uint32), ("coneAperture", C.c_float), ("lobeProbability", C.c_float),
+                ("reserved", C.c_uint32 * 2)]
+
+
 class MrgTracerRenderOutput(C.Structure):
     _fields_ = [("samplesDone", C.c_uint32), ("totalSpp", C.c_uint32), ("finished", C.c_uint32),
                 ("workMs", C.c_float), ("pathsPerSecond", C.c_double)]
@@ -198,6 +206,13 @@ def _declare(lib):
         "mrg_multi_partition": (C.c_int, [vp, vp, vp, u32, vp, vp, u32, vp, vp, vp, vp, vp, u32, vp]),
         "mrg_pt_camera_frame": (C.c_int, [C.POINTER(MrgPtParams), fp]),
         "mrg_pt_render": (C.c_int, [vp, C.POINTER(MrgPtParams), vp, vp]),
+        "mrg_guide_defaults": (C.c_int, [C.POINTER(MrgGuideParams)]),
+        "mrg_guide_create": (C.c_int, [vp, C.POINTER(MrgGuideParams)]),
+        "mrg_guide_clear": (C.c_int, [vp]),
+        "mrg_guide_destroy": (C.c_int, [vp]),
+        "mrg_guide_stats": (C.c_int, [vp, u32p, u32p]),
+        "mrg_guide_read": (C.c_int, [vp, vp, vp, vp]),
+        "mrg_pt_render_guided": (C.c_int, [vp, C.POINTER(MrgPtParams), vp, vp]),
     }
     sz = C.c_size_t
     sig.update({

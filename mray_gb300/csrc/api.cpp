@@ -189,6 +189,8 @@ mrg_status mrg_destroy(mrg_ctx* c)
     cudaFree(c->dPtSpec);
     cudaFree(c->dPartScratch);
     cudaFree(c->dPtCacheBuf);
+    cudaFree(c->dGuideGrid);
+    cudaFree(c->dGuidePaths);
     for(void* q : c->cacheAllocs) cudaFree(q);
     cudaFree(c->dStageRays); cudaFree(c->dStageHits); cudaFree(c->dStageMeta);
     for(cudaStream_t& q : c->hostStreams) if(q) cudaStreamDestroy(q);

@@ -4,6 +4,7 @@
 #include "mray_gb300.h"
 #include "mrg_build.h"
 #include "mrg_pt.h"
+#include "mrg_guide.h"
 #include "mrg_partition.h"
 #include "mrg_nrc.h"
 
@@ -131,6 +132,19 @@ struct mrg_ctx
     // spectral context: device block [lut | observer | illuminant]
     void*              dPtSpec = nullptr;
     mrg::PtSpectral    ptSpec{};
+
+    // guided path tracing: the hash grid block (codes, counter, chain and
+    // irradiance state) and the per-slot guided path state
+    bool               guideOn = false;
+    mrg_guide_params   guidePrm{};
+    void*              dGuideGrid = nullptr;
+    mrg::GuideGrid     guide{};
+    bool               guideCamSet = false;
+    void*              dGuidePaths = nullptr;
+    mrg::GuidePaths    guideQ{};
+    uint32_t           guideCap = 0;              // slots the path state holds
+    bool               guideBkValid = false;      // backup streams of (guideBkSeed, W, H, slots)
+    uint32_t           guideBkSeed = 0, guideBkW = 0, guideBkH = 0;
 
     // radiance cache (one per context) and its path-tracer buffers
     void*              dPtCacheBuf = nullptr;

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -976,6 +977,364 @@ mrg_status mrg_pt_adjoint(mrg_ctx* c, const mrg_pt_params* p, uint32_t texId, co
     if(two && (s = pt_join(c, st)) != MRG_OK) return s;
     if(dGradEmission)
         PT_TRY(mrg::pt_add_emission_grad(c->dPtGradEmission, dGradEmission, 4 * nInst, st), "emission gradient");
+    return MRG_OK;
+}
+
+} // extern "C"
+
+// ---------------------------------------------------------------------------
+// Guided path tracing (GuidedPTRenderer): the hash grid, its per-slot path
+// state and the bounce loop (see mrg_guide.h for the kernel order).
+// ---------------------------------------------------------------------------
+namespace {
+
+uint32_t next_pow2(uint32_t v)
+{
+    uint32_t p = 1;
+    while(p < v) p <<= 1;
+    return p;
+}
+
+// HashGrid::Reset's table size: NextPowerOfTwo(uint32(entries * (1 / 0.6))).
+uint32_t guide_table_size(uint32_t entryLimit)
+{
+    const float mult = 1.0f / 0.6f;
+    return next_pow2((uint32_t)((float)entryLimit * mult));
+}
+
+// HashGrid::View (HashGrid.h:436-460) over the scene box.
+void guide_view(mrg_ctx* c)
+{
+    mrg::GuideGrid& G = c->guide;
+    const mrg_guide_params& p = c->guidePrm;
+    const uint32_t base = 1u << p.posBits;
+    double size[3];
+    int mx = 0;
+    for(int k = 0; k < 3; k++) size[k] = (double)(c->sceneBoxExact[3 + k] - c->sceneBoxExact[k]);
+    for(int k = 1; k < 3; k++)
+        if(size[k] > size[mx]) mx = k;
+    G.baseDelta = (float)((double)base / size[mx]);
+    G.baseDim = base;
+    G.normalDim = 1u << p.normalBits;
+    G.normalDelta = (float)G.normalDim;
+    G.maxLevelOffset = p.maxLevelOffset;
+    const float aperture = (3.1415926535897932384626433f / 180.0f) * p.coneAperture;   // DegToRadCoef
+    G.tanConeHalfTimes2 = std::tan(aperture * 0.5f) * 2.0f;
+    G.maxEntryLimit = (uint32_t)((float)(G.tableMask + 1u) * 0.6f);
+    G.rmin = make_float3(c->sceneBoxExact[0], c->sceneBoxExact[1], c->sceneBoxExact[2]);
+    G.lobeProb = p.lobeProbability;
+}
+
+mrg_status guide_clear(mrg_ctx* c)
+{
+    const mrg::GuideGrid& G = c->guide;
+    const size_t T = (size_t)G.tableMask + 1u;
+    PT_TRY(cudaMemset(G.codes, 0xFF, sizeof(unsigned long long) * T), "mrg_guide: clear");
+    PT_TRY(cudaMemset(G.counter, 0, sizeof(uint32_t)), "mrg_guide: clear");
+    PT_TRY(cudaMemset(G.mcA, 0, sizeof(float4) * T), "mrg_guide: clear");
+    PT_TRY(cudaMemset(G.mcW, 0, sizeof(float) * T), "mrg_guide: clear");
+    PT_TRY(cudaMemset(G.mcN, 0, sizeof(uint32_t) * T), "mrg_guide: clear");
+    PT_TRY(cudaMemset(G.irr, 0, sizeof(float2) * T), "mrg_guide: clear");
+    c->guideCamSet = false;
+    c->guideBkValid = false;
+    return MRG_OK;
+}
+
+// Per-slot guided state for `slots` paths (one allocation, 256-byte aligned
+// arrays); the record keys start empty.
+mrg_status guide_paths(mrg_ctx* c, uint32_t slots)
+{
+    mrg::GuidePaths& Q = c->guideQ;
+    uint32_t lg = 0;
+    while((1u << lg) < c->guide.tableMask + 1u) lg++;
+    if(c->guideCap < slots || !c->dGuidePaths)
+    {
+        cudaFree(c->dGuidePaths);
+        c->dGuidePaths = nullptr;
+        c->guideCap = 0;
+        Q = mrg::GuidePaths{};
+        const size_t n = slots;
+        const size_t sizes[15] = { n * 4, n * 4, n * 4, n * 4, n * 8, n * 4, n * 16, n * 8, n * 8, n * 8,
+                                   n * 8, n * 8, n * 8, n * 8, 4 * mrg::multisplit_hist_words(2u * slots, 8) };
+        size_t need = 0;
+        for(size_t sz : sizes) need += (sz + 255) & ~size_t(255);
+        char* base = nullptr;
+        PT_TRY(cudaMalloc(&base, need), "mrg_pt_render_guided: path state");
+        c->dGuidePaths = base;
+        size_t off = 0;
+        int k = 0;
+        auto take = [&]() { char* q = base + off; off += (sizes[k++] + 255) & ~size_t(255); return q; };
+        Q.bk = reinterpret_cast<uint32_t*>(take());
+        Q.lifted = reinterpret_cast<uint32_t*>(take());
+        Q.prevRefl = reinterpret_cast<float*>(take());
+        Q.scoreSum = reinterpret_cast<float*>(take());
+        Q.prevNormal = reinterpret_cast<float2*>(take());
+        Q.shadowOut = reinterpret_cast<float*>(take());
+        Q.tmpA = reinterpret_cast<float4*>(take());
+        Q.tmpB = reinterpret_cast<float2*>(take());
+        Q.recKey = reinterpret_cast<uint32_t*>(take());
+        Q.recVal = reinterpret_cast<float*>(take());
+        Q.sortKeysA = reinterpret_cast<uint32_t*>(take());
+        Q.sortIdxA = reinterpret_cast<uint32_t*>(take());
+        Q.sortKeysB = reinterpret_cast<uint32_t*>(take());
+        Q.sortIdxB = reinterpret_cast<uint32_t*>(take());
+        Q.sortHist = reinterpret_cast<uint32_t*>(take());
+        c->guideCap = slots;
+        c->guideBkValid = false;
+        // every bounce leaves the records empty again (guide_apply)
+        PT_TRY(cudaMemset(Q.recKey, 0xFF, sizeof(uint32_t) * 2u * n), "mrg_pt_render_guided: records");
+    }
+    if(Q.slots != slots) c->guideBkValid = false;
+    Q.slots = slots;
+    Q.keyBits = lg + 2u;
+    return MRG_OK;
+}
+
+// Backup streams: slot i starts at PermutedCG32::GenerateState of output
+// width * height + i of std::mt19937(seed) (the outputs before it seed the
+// pixels' main streams, as RNGGroupIndependent::Seed orders them,
+// Random.cu:683-724).
+mrg_status guide_backup_streams(mrg_ctx* c, const mrg_pt_params* p, uint32_t slots)
+{
+    if(c->guideBkValid && c->guideBkSeed == p->seed && c->guideBkW == p->width && c->guideBkH == p->height)
+        return MRG_OK;
+    PT_TRY(cudaDeviceSynchronize(), "mrg_pt_render_guided: earlier work");
+    std::mt19937 rng(p->seed);
+    rng.discard((unsigned long long)p->width * p->height);
+    std::vector<uint32_t> st(slots);
+    for(uint32_t i = 0; i < slots; i++)
+        st[i] = ((uint32_t)rng() + mrg::kBackupPcgInc) * mrg::kBackupPcgMult + mrg::kBackupPcgInc;
+    PT_TRY(cudaMemcpy(c->guideQ.bk, st.data(), sizeof(uint32_t) * slots, cudaMemcpyHostToDevice),
+           "mrg_pt_render_guided: backup streams");
+    c->guideBkValid = true;
+    c->guideBkSeed = p->seed; c->guideBkW = p->width; c->guideBkH = p->height;
+    return MRG_OK;
+}
+
+// One pass: raygen, then per bounce closest-hit cast, backprop, chain
+// writes, shade, and on the side stream the shadow cast, resolve and the
+// irradiance records' application.  The next bounce's backprop waits for that
+// application (it reads the averages); its closest-hit cast does not.
+cudaError_t guided_bounces(mrg_ctx* c, PtRun& R, const PtLane& lane)
+{
+    mrg::PtPaths& P = *lane.P;
+    const mrg::PtLaunch& L = R.L;
+    const mrg::GuideGrid& G = c->guide;
+    const mrg::GuidePaths& Q = c->guideQ;
+    cudaStream_t st = lane.st, side = lane.side;
+    const bool overlap = side != st;
+    mrg::TraceScratch closestScr = R.scr, shadowScr = R.scr;
+    closestScr.workCounter = lane.closestCounter;
+    shadowScr.workCounter = lane.shadowCounter;
+    const size_t T = (size_t)G.tableMask + 1u;
+    cudaError_t e = mrg::pt_raygen(L, P, P.listA, P.counts + 0, c->smCount, st);
+    if(e == cudaSuccess) e = cudaMemsetAsync(Q.lifted, 0xFF, sizeof(uint32_t) * (size_t)R.slots, st);
+    for(uint32_t depth = 0; depth < L.maxDepth && e == cudaSuccess; depth++)
+    {
+        uint32_t* alive = (depth & 1u) ? P.listB : P.listA;
+        uint32_t* next = (depth & 1u) ? P.listA : P.listB;
+        uint32_t* aliveCount = P.counts + ((depth & 1u) ? 1 : 0);
+        uint32_t* nextCount = P.counts + ((depth & 1u) ? 0 : 1);
+        e = cudaMemsetAsync(nextCount, 0, sizeof(uint32_t), st);
+        if(e == cudaSuccess) e = cudaMemsetAsync(G.lock, 0xFF, sizeof(uint32_t) * T, st);
+        if(e == cudaSuccess)
+            e = mrg::launch_closest(c->scene, closestScr, P.rays, alive, 0, P.hits, P.meta, c->smCount, st, aliveCount);
+        const uint32_t* shadeList = alive;
+        if(e == cudaSuccess && R.partition)
+        {
+            mrg::DigitSpec ks;
+            ks.batchShift = 0; ks.batchWidth = mrg::kPtWorkKeyBits;
+            ks.digitShift = 0; ks.digitBits = mrg::kPtWorkKeyBits;
+            e = mrg::pt_work_keys(P, R.T.surfaces, R.T.nSurfaces, alive, aliveCount, c->smCount, st);
+            if(e == cudaSuccess)
+                e = mrg::multisplit_pass(P.workKeys, alive, P.workKeysOut, P.listSorted, aliveCount, R.slots, ks,
+                                         P.sortHist, st);
+            shadeList = P.listSorted;
+        }
+        if(e == cudaSuccess && overlap && depth > 0) e = cudaStreamWaitEvent(st, lane.evResolved, 0);
+        if(e == cudaSuccess) e = mrg::guide_backprop(L, P, G, Q, R.T, alive, aliveCount, c->smCount, st);
+        if(e == cudaSuccess) e = mrg::guide_write_mc(P, G, Q, R.T, alive, aliveCount, c->smCount, st);
+        if(e == cudaSuccess) e = cudaMemsetAsync(P.counts + 2, 0, sizeof(uint32_t), st);
+        if(e == cudaSuccess)
+            e = mrg::guide_shade(L, P, G, Q, R.T, shadeList, aliveCount, next, nextCount, c->smCount, st);
+        if(e == cudaSuccess && overlap) e = cudaEventRecord(lane.evShaded, st);
+        if(e == cudaSuccess && overlap) e = cudaStreamWaitEvent(side, lane.evShaded, 0);
+        if(e == cudaSuccess)
+            e = mrg::launch_visibility(c->scene, shadowScr, P.visBits, P.shadowRays, P.shadowList, 0, c->smCount, side,
+                                       P.counts + 2);
+        if(e == cudaSuccess) e = mrg::guide_resolve(P, Q, c->smCount, side);
+        if(e == cudaSuccess) e = mrg::guide_apply(G, Q, c->smCount, side);
+        if(e == cudaSuccess && overlap) e = cudaEventRecord(lane.evResolved, side);
+    }
+    if(e == cudaSuccess && overlap) e = cudaStreamWaitEvent(st, lane.evResolved, 0);
+    return e;
+}
+
+} // namespace
+
+extern "C" {
+
+mrg_status mrg_guide_defaults(mrg_guide_params* out)
+{
+    if(!out) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_guide_defaults: null pointer");
+    *out = mrg_guide_params{};
+    out->entryLimit = 2000000u;
+    out->posBits = 14u;
+    out->normalBits = 2u;
+    out->maxLevelOffset = 3u;
+    out->coneAperture = 0.6f;
+    out->lobeProbability = 0.75f;
+    return MRG_OK;
+}
+
+mrg_status mrg_guide_create(mrg_ctx* c, const mrg_guide_params* p)
+{
+    if(!c || !p) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_guide_create: null pointer");
+    if(!c->built) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_guide_create: call mrg_build first");
+    // HashGrid::Reset's limits (HashGrid.cu:22-36): SpatioDirCode holds 3 normal
+    // bits per axis and levels up to 15
+    if(p->normalBits > 3u || p->posBits > 15u)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_guide_create: normalBits > 3 or posBits > 15");
+    if(p->entryLimit == 0u || p->entryLimit > (1u << 27) || !(p->lobeProbability >= 0.0f && p->lobeProbability <= 1.0f) ||
+       !(p->coneAperture >= 0.0f))
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_guide_create: entryLimit in [1, 2^27], lobeProbability "
+                                                   "in [0, 1], coneAperture >= 0");
+    DevGuard g(c->device);
+    PT_TRY(cudaDeviceSynchronize(), "mrg_guide_create: earlier work");
+    const uint32_t T = guide_table_size(p->entryLimit);
+    cudaFree(c->dGuideGrid);
+    c->dGuideGrid = nullptr;
+    c->guideOn = false;
+    const size_t t = T;
+    const size_t sizes[7] = { t * 8, 256, t * 16, t * 4, t * 4, t * 4, t * 8 };
+    size_t need = 0;
+    for(size_t sz : sizes) need += (sz + 255) & ~size_t(255);
+    char* base = nullptr;
+    PT_TRY(cudaMalloc(&base, need), "mrg_guide_create: grid");
+    c->dGuideGrid = base;
+    size_t off = 0;
+    int k = 0;
+    auto take = [&]() { char* q = base + off; off += (sizes[k++] + 255) & ~size_t(255); return q; };
+    mrg::GuideGrid& G = c->guide;
+    G = mrg::GuideGrid{};
+    G.codes = reinterpret_cast<unsigned long long*>(take());
+    G.counter = reinterpret_cast<uint32_t*>(take());
+    G.mcA = reinterpret_cast<float4*>(take());
+    G.mcW = reinterpret_cast<float*>(take());
+    G.mcN = reinterpret_cast<uint32_t*>(take());
+    G.lock = reinterpret_cast<uint32_t*>(take());
+    G.irr = reinterpret_cast<float2*>(take());
+    G.tableMask = T - 1u;
+    c->guidePrm = *p;
+    guide_view(c);
+    mrg_status s = guide_clear(c);
+    if(s != MRG_OK) return s;
+    c->guideOn = true;
+    return MRG_OK;
+}
+
+mrg_status mrg_guide_clear(mrg_ctx* c)
+{
+    if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_guide_clear: null pointer");
+    if(!c->guideOn) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_guide_clear: call mrg_guide_create first");
+    DevGuard g(c->device);
+    PT_TRY(cudaDeviceSynchronize(), "mrg_guide_clear: earlier work");
+    return guide_clear(c);
+}
+
+mrg_status mrg_guide_destroy(mrg_ctx* c)
+{
+    if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_guide_destroy: null pointer");
+    DevGuard g(c->device);
+    PT_TRY(cudaDeviceSynchronize(), "mrg_guide_destroy: earlier work");
+    cudaFree(c->dGuideGrid);
+    cudaFree(c->dGuidePaths);
+    c->dGuideGrid = nullptr;
+    c->dGuidePaths = nullptr;
+    c->guideCap = 0;
+    c->guideQ = mrg::GuidePaths{};
+    c->guide = mrg::GuideGrid{};
+    c->guideOn = false;
+    c->guideBkValid = false;
+    return MRG_OK;
+}
+
+mrg_status mrg_guide_stats(mrg_ctx* c, uint32_t* used, uint32_t* tableSize)
+{
+    if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_guide_stats: null pointer");
+    if(!c->guideOn) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_guide_stats: call mrg_guide_create first");
+    DevGuard g(c->device);
+    if(used) PT_TRY(cudaMemcpy(used, c->guide.counter, sizeof(uint32_t), cudaMemcpyDeviceToHost), "mrg_guide_stats");
+    if(tableSize) *tableSize = c->guide.tableMask + 1u;
+    return MRG_OK;
+}
+
+mrg_status mrg_guide_read(mrg_ctx* c, uint64_t* hCodes, float* hChain6, float* hIrr2)
+{
+    if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_guide_read: null pointer");
+    if(!c->guideOn) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_guide_read: call mrg_guide_create first");
+    DevGuard g(c->device);
+    const mrg::GuideGrid& G = c->guide;
+    const size_t T = (size_t)G.tableMask + 1u;
+    PT_TRY(cudaDeviceSynchronize(), "mrg_guide_read");
+    if(hCodes) PT_TRY(cudaMemcpy(hCodes, G.codes, 8 * T, cudaMemcpyDeviceToHost), "mrg_guide_read: codes");
+    if(hChain6)
+    {
+        std::vector<float4> a(T);
+        std::vector<float> w(T);
+        std::vector<uint32_t> n(T);
+        PT_TRY(cudaMemcpy(a.data(), G.mcA, 16 * T, cudaMemcpyDeviceToHost), "mrg_guide_read: chains");
+        PT_TRY(cudaMemcpy(w.data(), G.mcW, 4 * T, cudaMemcpyDeviceToHost), "mrg_guide_read: chains");
+        PT_TRY(cudaMemcpy(n.data(), G.mcN, 4 * T, cudaMemcpyDeviceToHost), "mrg_guide_read: chains");
+        for(size_t i = 0; i < T; i++)
+        {
+            float* o = hChain6 + 6 * i;
+            o[0] = a[i].x; o[1] = a[i].y; o[2] = a[i].z; o[3] = a[i].w; o[4] = w[i]; o[5] = (float)n[i];
+        }
+    }
+    if(hIrr2)
+    {
+        std::vector<float2> r(T);
+        PT_TRY(cudaMemcpy(r.data(), G.irr, 8 * T, cudaMemcpyDeviceToHost), "mrg_guide_read: irradiance");
+        for(size_t i = 0; i < T; i++)
+        {
+            uint32_t cnt;
+            std::memcpy(&cnt, &r[i].y, 4);
+            hIrr2[2 * i] = r[i].x;
+            hIrr2[2 * i + 1] = (float)cnt;
+        }
+    }
+    return MRG_OK;
+}
+
+mrg_status mrg_pt_render_guided(mrg_ctx* c, const mrg_pt_params* p, float* dImage, void* stream)
+{
+    if(!c || !p || !dImage) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render_guided: null pointer");
+    if(!c->guideOn) return mrg::set_error(MRG_ERR_NOT_BUILT, "mrg_pt_render_guided: call mrg_guide_create first");
+    if(p->sampler != MRG_PT_SAMPLER_INDEPENDENT && p->sampler != MRG_PT_SAMPLER_PCG32)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_render_guided: samplers INDEPENDENT and PCG32 only");
+    DevGuard g(c->device);
+    PtRun R;
+    mrg_status s = pt_setup(c, p, R, "mrg_pt_render_guided");
+    if(s != MRG_OK) return s;
+    if((s = guide_paths(c, R.slots)) != MRG_OK) return s;
+    if((s = guide_backup_streams(c, p, R.slots)) != MRG_OK) return s;
+    if(!c->guideCamSet)
+    {
+        // GenCameraPosition of the pinhole camera: its position
+        c->guide.cam = make_float3(p->camPos[0], p->camPos[1], p->camPos[2]);
+        c->guideCamSet = true;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    PtLane lane;
+    if((s = pt_lane0(c, st, lane)) != MRG_OK) return s;
+    const uint32_t passes = p->spp / R.spp;
+    for(uint32_t pass = 0; pass < passes; pass++)
+    {
+        R.L.sampleBase = p->sampleStart + pass * R.spp;
+        PT_TRY(guided_bounces(c, R, lane), "guided pass");
+        PT_TRY(mrg::pt_film(R.L, *lane.P, reinterpret_cast<float4*>(dImage), lane.st), "film");
+    }
     return MRG_OK;
 }
 

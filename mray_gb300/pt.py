@@ -192,6 +192,48 @@ class PathTracer:
                                       _stream_ptr(stream)))
         return image
 
+    # ---- guided path tracing (GuidedPTRenderer) ----
+    def guide_create(self, entry_limit=2000000, pos_bits=14, normal_bits=2, max_level_offset=3,
+                     cone_aperture=0.6, lobe_probability=0.75):
+        """Allocates the guiding hash grid over the built scene's box with
+        GuidedPTRenderer's options (cacheEntryLimit, cachePosBits,
+        cacheNormalBits, cacheMaxLvlOffset, cacheConeAperture in degrees,
+        lobeProbablity)."""
+        g = N.MrgGuideParams()
+        N.check(N.lib().mrg_guide_defaults(C.byref(g)))
+        g.entryLimit, g.posBits, g.normalBits = entry_limit, pos_bits, normal_bits
+        g.maxLevelOffset, g.coneAperture, g.lobeProbability = max_level_offset, cone_aperture, lobe_probability
+        N.check(N.lib().mrg_guide_create(self.acc._h, C.byref(g)))
+
+    def guide_clear(self):
+        N.check(N.lib().mrg_guide_clear(self.acc._h))
+
+    def guide_stats(self):
+        """(entries in use, table size)"""
+        used, size = C.c_uint32(), C.c_uint32()
+        N.check(N.lib().mrg_guide_stats(self.acc._h, C.byref(used), C.byref(size)))
+        return used.value, size.value
+
+    def guide_read(self):
+        """The table: codes (uint64, ~0 empty), chains (n, 6: target xyz,
+        cosine, weight, count), irradiance (n, 2: value, count)."""
+        _, size = self.guide_stats()
+        codes = np.empty(size, np.uint64)
+        chain = np.empty((size, 6), np.float32)
+        irr = np.empty((size, 2), np.float32)
+        N.check(N.lib().mrg_guide_read(self.acc._h, codes.ctypes.data, chain.ctypes.data, irr.ctypes.data))
+        return codes, chain, irr
+
+    def render_guided(self, p, image=None, stream=None):
+        """Adds p.spp guided samples per pixel to `image` (see
+        mrg_pt_render_guided) and returns it."""
+        import torch
+        if image is None:
+            image = torch.zeros((p.height, p.width, 4), dtype=torch.float32, device="cuda")
+        N.check(N.lib().mrg_pt_render_guided(self.acc._h, C.byref(p), C.c_void_p(image.data_ptr()),
+                                             _stream_ptr(stream)))
+        return image
+
     def close(self):
         self.acc.close()
 

@@ -94,6 +94,17 @@ def lib():
         L.orc_conc_octa_batch.argtypes = [vp, vp, vp, vp, u32]
         L.orc_guide_codes_batch.argtypes = [vp, vp, vp, vp, u32]
         L.orc_guide_table_batch.argtypes = [vp, u32, vp, u32, u32, vp, vp]
+        L.orc_guide_new.argtypes = [vp, u32, u32, u32, u32, C.c_float, C.c_float]
+        L.orc_guide_new.restype = vp
+        L.orc_guide_delete.argtypes = [vp]
+        L.orc_guide_clear.argtypes = [vp]
+        L.orc_guide_table_size.argtypes = [vp]
+        L.orc_guide_table_size.restype = u32
+        L.orc_guide_used.argtypes = [vp]
+        L.orc_guide_used.restype = u32
+        L.orc_guide_snapshot.argtypes = [vp, vp, vp, vp]
+        L.orc_pt_render_guided.argtypes = [vp, vp, vp, vp, u32, vp, vp, vp, u32, vp]
+        L.orc_pt_render_guided.restype = C.c_int
         L.orc_pt_render.restype = C.c_int
         L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
         L.orc_pt_make_light.argtypes = [vp, vp, vp, C.c_int, vp]
@@ -631,6 +642,24 @@ class PtScene:
                                   float(camera["near_far"][0]), float(camera["near_far"][1]), C.byref(p))
         return p
 
+    def guide(self, entry_limit=2000000, pos_bits=14, normal_bits=2, max_level_offset=3, cone_aperture=0.6,
+              lobe_probability=0.75):
+        """A guided path tracer's state (hash grid, chains, irradiance) over
+        this scene (GuidedPTRenderer options, as mray_gb300.pt.PathTracer.guide_create)."""
+        return GuideState(self, entry_limit, pos_bits, normal_bits, max_level_offset, cone_aperture,
+                          lobe_probability)
+
+    def render_guided(self, p, guide, samples_per_pass, image=None):
+        """Guided samples (single-threaded wavefront) added to image."""
+        img = np.zeros((p.height, p.width, 4), np.float32) if image is None else image
+        rc = self.L.orc_pt_render_guided(self.S._h, C.byref(p), self.surf, self.lights, self.n_lights,
+                                         C.byref(self.env) if self.env is not None else None,
+                                         C.byref(self.spectral.c) if self.spectral is not None else None,
+                                         guide._h, samples_per_pass, _vp(img))
+        if rc != 0:
+            raise RuntimeError("oracle guided render failed (%d)" % rc)
+        return img
+
     def render(self, p, image=None, threads=None):
         img = np.zeros((p.height, p.width, 4), np.float32) if image is None else image
         self.L.orc_pt_render(self.S._h, C.byref(p), self.surf, self.lights, self.n_lights,
@@ -638,6 +667,37 @@ class PtScene:
                              C.byref(self.spectral.c) if self.spectral is not None else None,
                              _vp(img), threads or default_threads())
         return img
+
+
+class GuideState:
+    """orc_guide_state: the oracle's guiding grid, chains, irradiance
+    averages and backup streams."""
+
+    def __init__(self, scene, entry_limit, pos_bits, normal_bits, max_level_offset, cone_aperture, lobe_probability):
+        self.L = lib()
+        self._h = self.L.orc_guide_new(scene.S._h, entry_limit, pos_bits, normal_bits, max_level_offset,
+                                       cone_aperture, lobe_probability)
+        if not self._h:
+            raise MemoryError("orc_guide_new")
+
+    def clear(self):
+        self.L.orc_guide_clear(self._h)
+
+    def stats(self):
+        return self.L.orc_guide_used(self._h), self.L.orc_guide_table_size(self._h)
+
+    def read(self):
+        n = self.L.orc_guide_table_size(self._h)
+        codes = np.empty(n, np.uint64)
+        chain = np.empty((n, 6), np.float32)
+        irr = np.empty((n, 2), np.float32)
+        self.L.orc_guide_snapshot(self._h, _vp(codes), _vp(chain), _vp(irr))
+        return codes, chain, irr
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self.L.orc_guide_delete(self._h)
+            self._h = None
 
 
 def multi_partition(keys, indices=None, key_data_bits=(0, 0), key_batch_bits=(0, 32),

@@ -1634,3 +1634,614 @@ void orc_fx_sample_waves(const uint32_t* xi, float* waves4, float* pdf4, uint32_
 {
     for(uint32_t i = 0; i < n; i++) orc_spec_sample_waves(to_float01(xi[i]), waves4 + 4 * i, pdf4 + 4 * i);
 }
+
+/* ======================================================================== */
+/* Guided path tracing (MRay's GuidedPTRenderer), as a wavefront: every     */
+/* bounce runs its stages over all path slots in slot order, the schedule   */
+/* the GPU renderer's kernels reproduce (closest hit, backprop, chain       */
+/* writes, shade, shadow rays, irradiance records applied per cell in       */
+/* (path, NEE, light) then slot order).  The stages restate                 */
+/*   KCBackpropagateHashGridPath      Source/TracerDLL/GuidedPTRenderer.cu:164-311 */
+/*   KCWriteMarkovChains              GuidedPTRenderer.cu:313-344          */
+/*   WorkFunction / LightWorkFunction GuidedPTRendererShaders.h:588-931    */
+/*   GaussLobeMixtureT                GuidedPTRendererShaders.h:381-450    */
+/*   KCAccumulateShadowRaysGPT, KCBackpropagateIrradNEE / Light            */
+/*                                    GuidedPTRenderer.cu:13-33, 346-430   */
+/* with the building blocks of guide_oracle.c.                             */
+/* ======================================================================== */
+#include "guide_oracle.h"
+
+struct orc_guide_state
+{
+    orc_guide_grid g;
+    float*    mcA;          /* 4 per table slot: target xyz, cosine */
+    float*    mcW;
+    uint32_t* mcN;
+    float*    irr;
+    uint32_t* irrN;
+    uint32_t* lock;
+    float     lobeProb;
+    int       camSet;
+    uint32_t* bk;           /* backup PCG32 state per path slot */
+    uint32_t  bkSlots, bkSeed, bkW, bkH;
+    int       bkValid;
+};
+
+static uint32_t next_pow2_u32(uint32_t v)
+{
+    uint32_t p = 1;
+    while(p < v) p <<= 1;
+    return p;
+}
+
+orc_guide_state* orc_guide_new(const orc_scene* s, uint32_t entryLimit, uint32_t posBits, uint32_t normalBits,
+                               uint32_t maxLevelOffset, float coneDeg, float lobeProb)
+{
+    orc_guide_state* G = (orc_guide_state*)calloc(1, sizeof(orc_guide_state));
+    if(!G) return NULL;
+    const float mult = 1.0f / 0.6f;
+    const uint32_t T = next_pow2_u32((uint32_t)((float)entryLimit * mult));
+    float box[6], cam[3] = { 0, 0, 0 };
+    orc_scene_aabb(s, box);
+    orc_guide_view(&G->g, box, cam, posBits, normalBits, maxLevelOffset, coneDeg, T);
+    G->g.codes = (uint64_t*)malloc(sizeof(uint64_t) * T);
+    G->mcA = (float*)malloc(sizeof(float) * 4 * T);
+    G->mcW = (float*)malloc(sizeof(float) * T);
+    G->mcN = (uint32_t*)malloc(sizeof(uint32_t) * T);
+    G->irr = (float*)malloc(sizeof(float) * T);
+    G->irrN = (uint32_t*)malloc(sizeof(uint32_t) * T);
+    G->lock = (uint32_t*)malloc(sizeof(uint32_t) * T);
+    G->lobeProb = lobeProb;
+    if(!G->g.codes || !G->mcA || !G->mcW || !G->mcN || !G->irr || !G->irrN || !G->lock)
+    {
+        orc_guide_delete(G);
+        return NULL;
+    }
+    orc_guide_clear(G);
+    return G;
+}
+
+void orc_guide_delete(orc_guide_state* G)
+{
+    if(!G) return;
+    free(G->g.codes); free(G->mcA); free(G->mcW); free(G->mcN); free(G->irr); free(G->irrN); free(G->lock);
+    free(G->bk);
+    free(G);
+}
+
+void orc_guide_clear(orc_guide_state* G)
+{
+    const uint32_t T = G->g.tableSize;
+    for(uint32_t i = 0; i < T; i++) G->g.codes[i] = ORC_GUIDE_EMPTY;
+    G->g.counter = 0;
+    memset(G->mcA, 0, sizeof(float) * 4 * T);
+    memset(G->mcW, 0, sizeof(float) * T);
+    memset(G->mcN, 0, sizeof(uint32_t) * T);
+    memset(G->irr, 0, sizeof(float) * T);
+    memset(G->irrN, 0, sizeof(uint32_t) * T);
+    G->camSet = 0;
+    G->bkValid = 0;
+}
+
+uint32_t orc_guide_table_size(const orc_guide_state* G) { return G->g.tableSize; }
+uint32_t orc_guide_used(const orc_guide_state* G) { return G->g.counter; }
+
+void orc_guide_snapshot(const orc_guide_state* G, uint64_t* codes, float* chain6, float* irr2)
+{
+    for(uint32_t i = 0; i < G->g.tableSize; i++)
+    {
+        if(codes) codes[i] = G->g.codes[i];
+        if(chain6)
+        {
+            float* o = chain6 + 6 * (size_t)i;
+            for(int k = 0; k < 4; k++) o[k] = G->mcA[4 * (size_t)i + k];
+            o[4] = G->mcW[i];
+            o[5] = (float)G->mcN[i];
+        }
+        if(irr2) { irr2[2 * (size_t)i] = G->irr[i]; irr2[2 * (size_t)i + 1] = (float)G->irrN[i]; }
+    }
+}
+
+typedef struct
+{
+    smp_ctx  sc;
+    float    org[3], dir[3], tmin, tmax;
+    float    thr[4], rad[4], waves[4], wpdf[4];
+    float    prevPdf;
+    uint32_t depth, type;          /* type 0 camera, 1 path, 2 specular */
+    int      alive;
+    int      hit;                  /* closest hit of this bounce */
+    uint32_t inst;
+    orc_hit_keys hk;
+    orc_meta_hit mh;
+    /* guided state (GuidedPTRDetail::RayState) */
+    uint32_t lifted;
+    float    prevRefl, scoreSum, prevNormal[2], shadowOut;
+    float    tmpA[4], tmpW;
+    uint32_t tmpN;
+    /* shadow ray */
+    int      shadow;
+    float    sorg[3], sdir[3], stmax, srad[4];
+} g_slot;
+
+typedef struct { uint32_t key, pos; } g_rec;
+
+static int g_rec_cmp(const void* a, const void* b)
+{
+    const g_rec* x = (const g_rec*)a;
+    const g_rec* y = (const g_rec*)b;
+    if(x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->pos < y->pos ? -1 : (x->pos > y->pos);
+}
+
+static float g_avg(const float* c, int nc)
+{
+    return (nc == 4) ? (c[0] + c[1] + c[2] + c[3]) * 0.25f : (c[0] + c[1] + c[2]) * 0.33333333f;
+}
+
+static void g_put(uint32_t* recKey, float* recVal, uint32_t pos, uint32_t cell, uint32_t light, float v)
+{
+    recKey[pos] = (cell << 1) | light;
+    recVal[pos] = isfinite(v) ? v : 0.0f;
+}
+
+/* GaussLobeMixtureT::Pdf */
+static float g_mix_pdf(const orc_lobe* lobes, const float* w, float sumW, const float d[3])
+{
+    if(sumW == 0.0f) return 0.0f;
+    float pdf = 0.0f;
+    for(uint32_t j = 0; j < ORC_GUIDE_LOBES; j++)
+        if(w[j] != 0.0f) pdf = pdf + w[j] * orc_lobe_pdf(&lobes[j], d);
+    return pdf / sumW;
+}
+
+static void g_albedo(const orc_pt_surface* sf, uint32_t localPrim, const orc_meta_hit* mh, const orc_spectral* S,
+                     const float waves[4], float alb[4])
+{
+    alb[0] = sf->albedo[0]; alb[1] = sf->albedo[1]; alb[2] = sf->albedo[2]; alb[3] = 0.0f;
+    if(sf->texels)
+    {
+        const float* q = &sf->uvs[6 * localPrim];
+        float a = mh->bary[0], b = mh->bary[1], c = 1.0f - a - b;
+        float uv[2];
+        for(int k = 0; k < 2; k++) uv[k] = q[k] * a + q[2 + k] * b + q[4 + k] * c;
+        orc_tex_read(sf->texels, sf->texW, sf->texH, sf->texFormat, uv, alb);
+    }
+    if(S) { float c3[3] = { alb[0], alb[1], alb[2] }; orc_spec_convert_albedo(S, c3, waves, alb); }
+}
+
+/* Light work of a miss (inst == ~0: the boundary light) or of a light
+ * surface hit: emission with MIS for path rays, and the light-cache radiance
+ * of the previous vertex. */
+static void g_light_work(const orc_pt_params* P, const orc_pt_surface* surfaces, const orc_pt_light_tri* lights,
+                         const orc_pt_env* E, const orc_spectral* S, float invN, g_slot* q, uint32_t i,
+                         uint32_t slots, uint32_t* recKey, float* recVal)
+{
+    const int nc = S ? 4 : 3;
+    float tp[4] = { q->thr[0], q->thr[1], q->thr[2], q->thr[3] };
+    float lcRefl = q->prevRefl;
+    float lpdf = 0.0f;
+    float em[4] = { 0, 0, 0, 0 };
+    if(q->hit)
+    {
+        const orc_pt_surface* sf = &surfaces[q->inst];
+        const orc_pt_light_tri* L = &lights[sf->lightBase + (q->hk.primKey - sf->primKeyBase)];
+        if(q->type == 1u) lpdf = light_tri_pdf(L, q->mh.bary[0], q->mh.bary[1], q->org, q->dir) * invN;
+        const float wo[3] = { -q->dir[0], -q->dir[1], -q->dir[2] };
+        if(light_tri_emits(L, wo))
+        {
+            em[0] = L->radiance[0]; em[1] = L->radiance[1]; em[2] = L->radiance[2];
+            if(S) orc_spec_convert_radiance(S, L->radiance, q->waves, em);
+        }
+    }
+    else if(E)
+    {
+        if(q->type == 1u) lpdf = env_pdf(E, q->dir) * invN;
+        env_emit(E, q->dir, em);
+        if(S) { float c[3] = { em[0], em[1], em[2] }; orc_spec_convert_radiance(S, c, q->waves, em); }
+    }
+    if(q->type == 1u)
+    {
+        const float p0 = q->prevPdf;
+        const float misPdf = p0 + lpdf;
+        for(int k = 0; k < nc; k++) tp[k] *= p0;
+        if(misPdf == 0.0f) tp[0] = tp[1] = tp[2] = tp[3] = 0.0f;
+        else { float inv = 1.0f / misPdf; for(int k = 0; k < nc; k++) tp[k] *= inv; }
+        lcRefl = lcRefl * p0;
+        lcRefl = (misPdf == 0.0f) ? 0.0f : lcRefl / misPdf;
+    }
+    float lcRad = 0.0f;
+    if(q->depth + 1u <= P->maxDepth)
+    {
+        for(int k = 0; k < nc; k++) q->rad[k] += em[k] * tp[k];
+        lcRad = lcRefl * g_avg(em, nc);
+    }
+    if(q->lifted != ORC_GUIDE_INVALID) g_put(recKey, recVal, slots + i, q->lifted, 1u, lcRad);
+    q->alive = 0;
+}
+
+/* WorkFunction of the guided renderer for a surface hit. */
+static void g_surface_work(const orc_scene* scene, const orc_pt_params* P, const orc_pt_surface* surfaces,
+                           const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* E,
+                           const orc_spectral* S, orc_guide_state* G, float invN, uint32_t nAll, g_slot* q,
+                           uint32_t i)
+{
+    const int nc = S ? 4 : 3;
+    const orc_pt_surface* sf = &surfaces[q->inst];
+    const uint32_t localPrim = q->hk.primKey - sf->primKeyBase;
+    const float* tri9 = &sf->triangles[9 * localPrim];
+    const float bu = q->mh.bary[1];
+    const float bv = 1.0f - q->mh.bary[0] - q->mh.bary[1];
+    float pos[3], gn[3];
+    surface_of(sf, tri9, bu, bv, pos, gn);
+    const int backSide = dot3f(gn, q->dir) > 0.0f;
+    if(backSide) { gn[0] = -gn[0]; gn[1] = -gn[1]; gn[2] = -gn[2]; }
+    const float nrm[3] = { gn[0], gn[1], gn[2] };
+    float tng[3], btg[3];
+    onb(nrm, tng, btg);
+    const float wo[3] = { -q->dir[0], -q->dir[1], -q->dir[2] };
+    const float V[3] = { dot3f(wo, tng), dot3f(wo, btg), dot3f(wo, nrm) };
+    float alb[4];
+    g_albedo(sf, localPrim, &q->mh, S, q->waves, alb);
+    const float specv = specularity(sf, alb, nc);
+    const int isSpec = specv >= SPECULAR_THRESHOLD;
+    float woW[3] = { wo[0], wo[1], wo[2] };
+    normalize3f(woW);
+    const uint32_t d = q->depth;
+
+    /* GaussLobeMixtureT::LoadStochastic */
+    orc_lobe lobes[ORC_GUIDE_LOBES];
+    float wts[ORC_GUIDE_LOBES];
+    float sumW = 0.0f, selW = 0.0f;
+    int selected = 0;
+    uint32_t sel = 0, liftedMC = ORC_GUIDE_INVALID;
+    uint32_t* rng = &G->bk[i];
+    float codeN[3] = { woW[0], woW[1], woW[2] };
+    normalize3f(codeN);
+    for(uint32_t j = 0; j < ORC_GUIDE_LOBES; j++)
+    {
+        const uint64_t code = orc_guide_gen_code_stochastic(&G->g, pos, codeN, rng);
+        int ins;
+        const uint32_t slot = orc_guide_try_insert(&G->g, code, &ins);
+        if(slot == ORC_GUIDE_INVALID)
+        {
+            memset(&lobes[j], 0, sizeof(orc_lobe));
+            wts[j] = 0.0f;
+            continue;
+        }
+        orc_mc_state s;
+        for(int k = 0; k < 3; k++) s.target[k] = G->mcA[4 * (size_t)slot + k];
+        s.cosine = G->mcA[4 * (size_t)slot + 3];
+        s.weight = G->mcW[slot];
+        lobes[j] = orc_mc_to_lobe(&s, G->mcN[slot], pos);
+        wts[j] = s.weight;
+        sumW = sumW + wts[j];
+        const float ratio = (sumW != 0.0f) ? wts[j] / sumW : 1.0f;
+        if(orc_guide_next_float(rng) < ratio) { sel = j; selW = wts[j]; selected = 1; liftedMC = slot; }
+    }
+    float coN[2];
+    orc_dir_to_conc_octa(woW, coN);
+
+    /* mixture or material sample, balance-heuristic pdf */
+    float mw0 = 0.0f;
+    if(!isSpec)
+    {
+        float t = 1.0f - specv;
+        t = fminf(fmaxf(t, 0.0f), 1.0f);
+        mw0 = 0.0f * (1.0f - t) + G->lobeProb * t;           /* Math::Lerp(0, p, t) */
+    }
+    const float mw1 = 1.0f - mw0;
+    float refl[4] = { 0, 0, 0, 0 }, pdf0, pdf1, wdir[3], orgOut[3] = { pos[0], pos[1], pos[2] };
+    int passed = 0, lobeSampled = 0;
+    if(urnd(&q->sc, d, 10) < mw0)
+    {
+        float v[3] = { 0.0f, 1.0f, 0.0f }, mpdf = 0.0f;
+        if(selected && selW != 0.0f)
+        {
+            orc_lobe_sample(&lobes[sel], urnd(&q->sc, d, 0), urnd(&q->sc, d, 1), v);
+            mpdf = g_mix_pdf(lobes, wts, sumW, v);
+        }
+        memcpy(wdir, v, 12);
+        float vn[3] = { v[0], v[1], v[2] };
+        normalize3f(vn);
+        const float Ls[3] = { dot3f(vn, tng), dot3f(vn, btg), dot3f(vn, nrm) };
+        float bpdf;
+        bxdf_eval(sf, alb, nc, V, Ls, refl, &bpdf);
+        pdf0 = mpdf;
+        pdf1 = bpdf;
+        lobeSampled = 1;
+    }
+    else
+    {
+        float Ll[3], bpdf;
+        bxdf_sample(sf, alb, nc, backSide, V, urnd(&q->sc, d, 0), urnd(&q->sc, d, 1), urnd(&q->sc, d, 2),
+                    Ll, refl, &bpdf, &passed);
+        if(sf->matType == ORC_MAT_REFRACT) orc_nudge(pos, nrm, orgOut);
+        for(int k = 0; k < 3; k++) wdir[k] = tng[k] * Ll[0] + btg[k] * Ll[1] + nrm[k] * Ll[2];
+        normalize3f(wdir);
+        pdf0 = g_mix_pdf(lobes, wts, sumW, wdir);
+        pdf1 = bpdf;
+    }
+    const float pdfPath = pdf0 * mw0 + pdf1 * mw1;
+
+    /* Russian roulette on the throughput before this vertex */
+    q->depth += 1u;
+    int dead = q->depth >= P->maxDepth;
+    if(!dead && q->depth >= P->rrStart && !isSpec)
+    {
+        float pr = g_avg(q->thr, nc);
+        pr = fminf(fmaxf(pr, 0.1f), 1.0f);
+        if(urnd(&q->sc, d, 8) >= pr) dead = 1;
+        else { float inv = 1.0f / pr; for(int k = 0; k < nc; k++) q->thr[k] *= inv; }
+    }
+    const float avgRefl = g_avg(refl, nc);
+    const float thr[4] = { q->thr[0], q->thr[1], q->thr[2], q->thr[3] };   /* NEE's throughput */
+    q->alive = 0;
+    q->shadow = 0;
+    if(!dead)
+    {
+        float pthr[4] = { 0, 0, 0, 0 };
+        for(int k = 0; k < nc; k++) pthr[k] = thr[k] * refl[k];
+        if(pdfPath == 0.0f) pthr[0] = pthr[1] = pthr[2] = pthr[3] = 0.0f;
+        else { float inv = 1.0f / pdfPath; for(int k = 0; k < nc; k++) pthr[k] *= inv; }
+        float nn[3] = { nrm[0], nrm[1], nrm[2] };
+        if(passed) { nn[0] = -nn[0]; nn[1] = -nn[1]; nn[2] = -nn[2]; }
+        orc_nudge(orgOut, nn, q->org);
+        memcpy(q->dir, wdir, 12);
+        memcpy(q->thr, pthr, 16);
+        q->tmin = 1.0e-4f;
+        q->tmax = 3.402823466e+38f;
+        q->prevPdf = pdfPath;
+        q->type = isSpec ? 2u : 1u;
+        q->prevRefl = avgRefl / fmaxf(pdfPath, 10.0f);
+        q->scoreSum = lobeSampled ? sumW : INFINITY;
+        q->lifted = liftedMC;
+        q->prevNormal[0] = coN[0]; q->prevNormal[1] = coN[1];
+        q->alive = 1;
+    }
+    /* NEE with the mixture / material MIS, then with the light */
+    if(!dead && !isSpec && nAll > 0)
+    {
+        float dXi = urnd(&q->sc, d, 3);
+        uint32_t li = (uint32_t)(dXi * (float)nAll);
+        if(li > nAll - 1u) li = nAll - 1u;
+        float lp[3], lightPdf;
+        float emis[4] = { 0, 0, 0, 0 };
+        if(li == nLights)
+        {
+            float wd[3], spdf;
+            env_sample(E, urnd(&q->sc, d, 4), urnd(&q->sc, d, 5), wd, &spdf);
+            for(int k = 0; k < 3; k++) lp[k] = pos[k] + wd[k] * E->sceneDiameter;
+            float sd[3] = { pos[0] - lp[0], pos[1] - lp[1], pos[2] - lp[2] };
+            normalize3f(sd);
+            float toward[3] = { -sd[0], -sd[1], -sd[2] };
+            env_emit(E, toward, emis);
+            if(S) { float c[3] = { emis[0], emis[1], emis[2] }; orc_spec_convert_radiance(S, c, q->waves, emis); }
+            lightPdf = invN * spdf;
+        }
+        else
+        {
+            const orc_pt_light_tri* L = &lights[li];
+            float ppdf;
+            light_tri_sample(L, urnd(&q->sc, d, 4), urnd(&q->sc, d, 5), pos, lp, &ppdf, emis);
+            lightPdf = invN * ppdf;
+            if(S && (emis[0] != 0.0f || emis[1] != 0.0f || emis[2] != 0.0f))
+                orc_spec_convert_radiance(S, L->radiance, q->waves, emis);
+        }
+        float sdir[3] = { lp[0] - pos[0], lp[1] - pos[1], lp[2] - pos[2] };
+        normalize3f(sdir);
+        float nd[3] = { -sdir[0], -sdir[1], -sdir[2] };
+        float lpn[3];
+        orc_nudge(lp, nd, lpn);
+        float seg[3] = { lpn[0] - pos[0], lpn[1] - pos[1], lpn[2] - pos[2] };
+        const float length = sqrtf(dot3f(seg, seg));
+        const float Ls[3] = { dot3f(sdir, tng), dot3f(sdir, btg), dot3f(sdir, nrm) };
+        float srefl[4] = { 0, 0, 0, 0 }, bpdf;
+        bxdf_eval(sf, alb, nc, V, Ls, srefl, &bpdf);
+        float pdfS = g_mix_pdf(lobes, wts, sumW, sdir) * mw0 + bpdf * mw1;
+        pdfS = pdfS + lightPdf;
+        float srad[4] = { 0, 0, 0, 0 };
+        if(pdfS != 0.0f)
+        {
+            float inv = 1.0f / pdfS;
+            for(int k = 0; k < nc; k++) srad[k] = thr[k] * srefl[k] * emis[k] * inv;
+        }
+        orc_nudge(pos, nrm, q->sorg);
+        memcpy(q->sdir, sdir, 12);
+        q->stmax = length * (1.0f - 1.0e-4f);
+        memcpy(q->srad, srad, 16);
+        const float se = g_avg(srefl, nc) * g_avg(emis, nc);
+        q->shadowOut = se / fmaxf(pdfS, 10.0f);
+        q->shadow = 1;
+    }
+    (void)scene;
+}
+
+int orc_pt_render_guided(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
+                         const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
+                         const orc_spectral* spectral, orc_guide_state* G, uint32_t samplesPerPass, float* image)
+{
+    if(!s || !p || !surfaces || !G || !image || samplesPerPass == 0 || p->spp % samplesPerPass != 0) return -1;
+    if(p->sampler != 0u && p->sampler != 3u) return -1;
+    const uint32_t wh = p->width * p->height;
+    const uint32_t slots = wh * samplesPerPass;
+    const orc_spectral* S = spectral;
+    const int nc = S ? 4 : 3;
+    /* backup streams: GenerateState of output wh + i of std::mt19937(seed) */
+    if(!G->bkValid || G->bkSlots != slots || G->bkSeed != p->seed || G->bkW != p->width || G->bkH != p->height)
+    {
+        uint32_t* mt = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)wh + slots));
+        uint32_t* bk = (uint32_t*)realloc(G->bk, sizeof(uint32_t) * slots);
+        if(!mt || !bk) { free(mt); if(bk) G->bk = bk; return -2; }
+        G->bk = bk;
+        orc_mt19937(p->seed, wh + slots, mt);
+        for(uint32_t i = 0; i < slots; i++) G->bk[i] = orc_pcg32_state(mt[wh + i]);
+        free(mt);
+        G->bkValid = 1; G->bkSlots = slots; G->bkSeed = p->seed; G->bkW = p->width; G->bkH = p->height;
+    }
+    if(!G->camSet)
+    {
+        for(int k = 0; k < 3; k++) G->g.cam[k] = p->camPos[k];
+        G->camSet = 1;
+    }
+    pt_job J;
+    memset(&J, 0, sizeof(J));
+    if(job_sampler(&J, p) != 0) return -2;
+    g_slot* Q = (g_slot*)calloc(slots, sizeof(g_slot));
+    uint32_t* recKey = (uint32_t*)malloc(sizeof(uint32_t) * 2 * (size_t)slots);
+    float* recVal = (float*)malloc(sizeof(float) * 2 * (size_t)slots);
+    g_rec* recs = (g_rec*)malloc(sizeof(g_rec) * 2 * (size_t)slots);
+    if(!Q || !recKey || !recVal || !recs) { free(Q); free(recKey); free(recVal); free(recs); free(J.zsSeeds); return -2; }
+    const uint32_t nAll = nLights + (env ? 1u : 0u);
+    const float invN = nAll ? 1.0f / (float)nAll : 0.0f;
+    const uint32_t T = G->g.tableSize;
+    const uint32_t passes = p->spp / samplesPerPass;
+    for(uint32_t pass = 0; pass < passes; pass++)
+    {
+        const uint32_t sampleBase = p->sampleStart + pass * samplesPerPass;
+        /* raygen */
+        for(uint32_t i = 0; i < slots; i++)
+        {
+            g_slot* q = &Q[i];
+            memset(q, 0, sizeof(*q));
+            const uint32_t pixel = i % wh, sample = sampleBase + i / wh;
+            const uint32_t x = pixel % p->width, y = pixel / p->width;
+            smp_ctx SC = { path_key(p->seed, pixel, sample), x, y, sample, J.zsSeeds ? J.zsSeeds[pixel] : 0u,
+                           J.zsSeeds ? p->sampler : 0u, p->samplerMaxSpp ? p->samplerMaxSpp : p->sampleStart + p->spp,
+                           J.zsResBits, p->maxDepth };
+            q->sc = SC;
+            float ox, oy;
+            filter_sample(p->filterRadius, urnd(&SC, 0, 6), urnd(&SC, 0, 7), &ox, &oy);
+            camera_ray(p, x, y, ox, oy, q->dir, q->org);
+            q->tmin = p->nearT; q->tmax = p->farT;
+            for(int k = 0; k < 4; k++) { q->thr[k] = 1.0f; q->wpdf[k] = 1.0f; }
+            if(S) orc_spec_sample_waves(urnd(&SC, 0, 9), q->waves, q->wpdf);
+            q->alive = 1;
+            q->lifted = ORC_GUIDE_INVALID;
+        }
+        for(uint32_t i = 0; i < 2 * slots; i++) recKey[i] = 0xFFFFFFFFu;
+        for(uint32_t depth = 0; depth < p->maxDepth; depth++)
+        {
+            int any = 0;
+            /* closest hit */
+            for(uint32_t i = 0; i < slots; i++)
+            {
+                g_slot* q = &Q[i];
+                q->shadow = 0;
+                if(!q->alive) continue;
+                any = 1;
+                float t;
+                q->hit = cast1(s, q->org, q->dir, q->tmin, q->tmax, &q->hk, &q->mh, &q->inst, &t);
+                if(q->hit) q->tmax = t;
+            }
+            if(!any) break;
+            /* backprop (KCBackpropagateHashGridPath); locks: smallest slot wins */
+            for(uint32_t c = 0; c < T; c++) G->lock[c] = 0xFFFFFFFFu;
+            for(uint32_t i = 0; i < slots; i++)
+            {
+                g_slot* q = &Q[i];
+                if(!q->alive || !q->hit || surfaces[q->inst].isLight) continue;
+                const uint32_t prev = q->lifted;
+                if(prev == ORC_GUIDE_INVALID) continue;
+                float nextPos[3], wdir[3];
+                for(int k = 0; k < 3; k++) { nextPos[k] = q->org[k] + q->tmax * q->dir[k]; wdir[k] = -q->dir[k]; }
+                normalize3f(wdir);
+                const uint32_t loc = orc_guide_search(&G->g, orc_guide_gen_code(&G->g, nextPos, wdir));
+                if(loc == ORC_GUIDE_INVALID) continue;
+                float out = q->prevRefl * G->irr[loc];
+                if(!isfinite(out)) out = 0.0f;
+                g_put(recKey, recVal, i, prev, 0u, out);
+                uint32_t* rng = &G->bk[i];
+                const float score = q->scoreSum;
+                if(score != INFINITY && orc_guide_next_float(rng) * score > out * (float)ORC_GUIDE_LOBES) continue;
+                float mcN[3];
+                orc_conc_octa_to_dir(q->prevNormal, mcN);
+                const uint64_t mcCode = orc_guide_gen_code_stochastic(&G->g, q->org, mcN, rng);
+                uint32_t ni = orc_guide_search(&G->g, mcCode);
+                if(ni == ORC_GUIDE_INVALID) ni = prev;
+                q->lifted = ni;
+                if(G->lock[ni] < i + 1u) continue;
+                G->lock[ni] = i + 1u;
+                orc_mc_state st;
+                uint32_t cnt;
+                if(score == INFINITY)
+                {
+                    memset(&st, 0, sizeof(st));
+                    cnt = 0u;
+                }
+                else
+                {
+                    for(int k = 0; k < 3; k++) st.target[k] = G->mcA[4 * (size_t)prev + k];
+                    st.cosine = G->mcA[4 * (size_t)prev + 3];
+                    st.weight = G->mcW[prev];
+                    cnt = orc_mc_ema(&st, q->org, nextPos, out, G->mcN[prev]);
+                }
+                if(!isfinite(st.cosine)) st.cosine = 0.0f;
+                if(!isfinite(st.target[0]) || !isfinite(st.target[1]) || !isfinite(st.target[2]))
+                    st.target[0] = st.target[1] = st.target[2] = 0.0f;
+                if(!isfinite(st.weight)) st.weight = 0.0f;
+                for(int k = 0; k < 3; k++) q->tmpA[k] = st.target[k];
+                q->tmpA[3] = st.cosine;
+                q->tmpW = st.weight;
+                q->tmpN = cnt;
+            }
+            /* KCWriteMarkovChains */
+            for(uint32_t i = 0; i < slots; i++)
+            {
+                g_slot* q = &Q[i];
+                if(!q->alive || !q->hit || surfaces[q->inst].isLight) continue;
+                const uint32_t w = q->lifted;
+                if(w == ORC_GUIDE_INVALID || G->lock[w] != i + 1u) continue;
+                for(int k = 0; k < 4; k++) G->mcA[4 * (size_t)w + k] = q->tmpA[k];
+                G->mcW[w] = q->tmpW;
+                G->mcN[w] = q->tmpN;
+            }
+            /* shade */
+            for(uint32_t i = 0; i < slots; i++)
+            {
+                g_slot* q = &Q[i];
+                if(!q->alive) continue;
+                if(!q->hit || surfaces[q->inst].isLight)
+                    g_light_work(p, surfaces, lights, env, S, invN, q, i, slots, recKey, recVal);
+                else
+                    g_surface_work(s, p, surfaces, lights, nLights, env, S, G, invN, nAll, q, i);
+            }
+            /* shadow rays (KCAccumulateShadowRaysGPT) and NEE records */
+            for(uint32_t i = 0; i < slots; i++)
+            {
+                g_slot* q = &Q[i];
+                if(!q->shadow) continue;
+                if(!visible1(s, q->sorg, q->sdir, 1.0e-5f, q->stmax)) continue;
+                for(int k = 0; k < 4; k++) q->rad[k] += q->srad[k];
+                if(q->lifted != ORC_GUIDE_INVALID) g_put(recKey, recVal, slots + i, q->lifted, 0u, q->shadowOut);
+            }
+            /* irradiance records, per cell in (key, position) order */
+            uint32_t nr = 0;
+            for(uint32_t r = 0; r < 2 * slots; r++)
+                if(recKey[r] != 0xFFFFFFFFu) { recs[nr].key = recKey[r]; recs[nr].pos = r; nr++; }
+            qsort(recs, nr, sizeof(g_rec), g_rec_cmp);
+            for(uint32_t r = 0; r < nr; r++)
+            {
+                const uint32_t cell = recs[r].key >> 1;
+                orc_irr_ema(&G->irr[cell], &G->irrN[cell], recVal[recs[r].pos]);
+            }
+            for(uint32_t r = 0; r < 2 * slots; r++) recKey[r] = 0xFFFFFFFFu;
+        }
+        /* film */
+        for(uint32_t px = 0; px < wh; px++)
+        {
+            float* o = &image[4 * (size_t)px];
+            for(uint32_t k = 0; k < samplesPerPass; k++)
+            {
+                const g_slot* q = &Q[px + (size_t)k * wh];
+                float rgb[3];
+                if(S) orc_spec_to_rgb(S, q->rad, q->waves, q->wpdf, rgb);
+                else { rgb[0] = q->rad[0]; rgb[1] = q->rad[1]; rgb[2] = q->rad[2]; }
+                o[0] += rgb[0]; o[1] += rgb[1]; o[2] += rgb[2]; o[3] += 1.0f;
+            }
+        }
+    }
+    (void)nc;
+    free(Q); free(recKey); free(recVal); free(recs); free(J.zsSeeds);
+    return 0;
+}

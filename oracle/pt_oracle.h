@@ -139,6 +139,23 @@ int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surf
                    double* grad, double* gradEmission, uint32_t nInstances, int nthreads);
 
 /* Piecewise-constant 2D distribution (Source/Tracer/Distributions.h/.cu). */
+/* Guided path tracing (GuidedPTRenderer) as a wavefront over the path slots,
+ * in the GPU renderer's stage order.  The state (hash grid, chains,
+ * irradiance averages, the slots' backup streams) persists across calls
+ * until orc_guide_clear. */
+typedef struct orc_guide_state orc_guide_state;
+orc_guide_state* orc_guide_new(const orc_scene* s, uint32_t entryLimit, uint32_t posBits, uint32_t normalBits,
+                               uint32_t maxLevelOffset, float coneDeg, float lobeProb);
+void     orc_guide_delete(orc_guide_state* G);
+void     orc_guide_clear(orc_guide_state* G);
+uint32_t orc_guide_table_size(const orc_guide_state* G);
+uint32_t orc_guide_used(const orc_guide_state* G);
+void     orc_guide_snapshot(const orc_guide_state* G, uint64_t* codes, float* chain6, float* irr2);
+int      orc_pt_render_guided(const orc_scene* s, const orc_pt_params* p, const orc_pt_surface* surfaces,
+                              const orc_pt_light_tri* lights, uint32_t nLights, const orc_pt_env* env,
+                              const orc_spectral* spectral, orc_guide_state* G, uint32_t samplesPerPass,
+                              float* image);
+
 void  orc_pwc2d_build(const float* func, uint32_t w, uint32_t h, float* cdfX, float* cdfY);
 void  orc_pwc2d_sample_uv(const float* cdfX, const float* cdfY, uint32_t w, uint32_t h,
                           const float xi[2], float uv[2], float* pdf);
