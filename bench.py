@@ -460,11 +460,57 @@ def box_scene_pt(args, dev):
 
     ms = timed("independent")
     ms_zs = timed("zsobol-owen")
+
+    # guided path tracing on the same workload: the grid learns across the calls
+    pt.guide_create()
+    p = PathTracer.params(256, 256, 16, cam, max_depth=8, rr_start=3, seed=0, samples_per_pass=16)
+    img = pt.render_guided(p)
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for r in range(reps):
+        p.sampleStart = 16 * (r + 1)
+        pt.render_guided(p, image=img)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms_g = e0.elapsed_time(e1) / reps
+    used, size = pt.guide_stats()
     pt.close()
     return {"box_pt_ms_per_16spp": round(ms, 3),
             "box_pt_spp_per_s": round(16.0 / (ms * 1e-3), 1),
             "box_pt_mpaths_per_s": round(256 * 256 * 16 / (ms * 1e-3) / 1e6, 1),
-            "box_pt_zsobol_ms_per_16spp": round(ms_zs, 3)}
+            "box_pt_zsobol_ms_per_16spp": round(ms_zs, 3),
+            "box_guided_ms_per_16spp": round(ms_g, 3),
+            "box_guided_mpaths_per_s": round(256 * 256 * 16 / (ms_g * 1e-3) / 1e6, 1),
+            "box_guided_grid_entries": int(used), "box_guided_grid_table": int(size)}
+
+
+def box_guided(args, dev):
+    """Guided path tracing on the box workload alone (256x256, 16 spp per
+    call, depth 8, RR from 3): with --single-call, two calls (the second on
+    a grid the first filled), untimed."""
+    import torch
+    from mray_gb300.pt import PathTracer, load_box_scene
+    from mray_gb300 import scenes
+    pt = PathTracer(dev.index or 0)
+    load_box_scene(pt, 0)
+    pt.guide_create()
+    p = PathTracer.params(256, 256, 16, scenes.box_camera(), max_depth=8, rr_start=3, seed=0, samples_per_pass=16)
+    img = pt.render_guided(p)
+    calls = 1 if getattr(args, "single_call", False) else max(3, min(args.steps, 20))
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for r in range(calls):
+        p.sampleStart = 16 * (r + 1)
+        pt.render_guided(p, image=img)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / calls
+    used, _ = pt.guide_stats()
+    pt.close()
+    return {"box_guided_ms_per_16spp": round(ms, 3), "box_guided_grid_entries": int(used)}
 
 
 def _spectral_inputs():
@@ -658,8 +704,35 @@ def c4_equal_time(args, dev, spp_per_frame=8):
     out["c4_workload"] = ("spectral production scene 1920x1080 (4 wavelengths) depth 12, reference 4096 spp plain; "
                           "cold start counts the training frames, steady state does not")
     cache.close()
+    out.update(guided_equal_time(pt, P, relmse, timed, t_plain, plain_rel))
     pt.close()
     return out
+
+
+def guided_equal_time(pt, P, relmse, timed, t_plain, plain_rel, spp=2):
+    """Guided path tracing (GuidedPTRenderer, default options) on the same
+    scene and reference: from an empty grid, frames of `spp` samples per
+    pixel accumulated for the plain 16-spp render's time (learning included),
+    then, the grid trained, one more 16-spp guided frame against the plain
+    16-spp render."""
+    import torch
+    pt.guide_create()
+    pt.render_guided(P(spp, 900, spp_pass=spp))         # allocations, first launches
+    pt.guide_clear()
+    img, spent, frames = None, 0.0, 0
+    while spent < t_plain:
+        img, dt = timed(lambda: pt.render_guided(P(spp, 1000, start=spp * frames, spp_pass=spp), image=img))
+        spent += dt
+        frames += 1
+    used, size = pt.guide_stats()
+    one, t_one = timed(lambda: pt.render_guided(P(16, 3000, spp_pass=spp)))
+    rel_one = relmse(one)
+    return {"guided_equal_time_frames": frames, "guided_equal_time_spp": frames * spp,
+            "guided_equal_time_ms": round(spent, 2), "guided_equal_time_relmse": round(relmse(img), 5),
+            "guided_16spp_ms": round(t_one, 2), "guided_16spp_relmse": round(rel_one, 5),
+            "guided_16spp_vs_plain_relmse": round(rel_one / plain_rel, 3),
+            "guided_16spp_mpaths_per_s": round(1920 * 1080 * 16 / (t_one * 1e-3) / 1e6, 1),
+            "guided_grid_entries": int(used), "guided_grid_table": int(size)}
 
 
 def cache_micro(args, dev):
@@ -831,7 +904,8 @@ def only_workload(args):
     B.build()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    fn = {"c0": box_scene_pt, "c2": c2_scene_pt, "c3": c3_adjoint, "c4": c4_equal_time, "cache": cache_micro}[args.only]
+    fn = {"c0": box_scene_pt, "c2": c2_scene_pt, "c3": c3_adjoint, "c4": c4_equal_time, "cache": cache_micro,
+          "gbox": box_guided}[args.only]
     print(json.dumps({"workload": args.only, **fn(args, dev)}))
 
 
@@ -845,7 +919,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pt-extras", action="store_true",
                     help="skip the production-scene and adjoint path-tracing lines")
-    ap.add_argument("--only", choices=["c0", "c2", "c3", "c4", "cache"], default=None,
+    ap.add_argument("--only", choices=["c0", "c2", "c3", "c4", "cache", "gbox"], default=None,
                     help="run one path-tracing workload alone and print its line (for profiling)")
     ap.add_argument("--single-call", action="store_true",
                     help="with --only c0 / c2: build the scene and render exactly one call, untimed "

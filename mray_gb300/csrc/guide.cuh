@@ -148,12 +148,34 @@ __device__ __forceinline__ uint64_t gen_code(const Grid& g, float3 pos, float3 n
     return compose_code(mcPos, expand2_32(tx) | (expand2_32(ty) << 1), level);
 }
 
-__device__ __forceinline__ uint64_t gen_code_stochastic(const Grid& g, float3 pos, float3 normal, uint32_t& rng)
+// The parts of GenCodeStochastic that do not depend on the random numbers:
+// the cone's base level at pos and the normal's texel and fractions.  Several
+// stochastic codes at one point share them.
+struct CodeBase
+{
+    uint32_t level;
+    float    fx, fy;
+    int32_t  nx, ny;
+};
+
+__device__ __forceinline__ CodeBase code_base(const Grid& g, float3 pos, float3 normal)
+{
+    CodeBase b;
+    b.level = base_level(g, pos);
+    const float2 st = dir_to_conc_octa(make_float3(normal.y, normal.z, normal.x));   // ZUpToYUp
+    float ipx, ipy;
+    b.fx = modff(gmul(st.x, g.normalDelta), &ipx);
+    b.fy = modff(gmul(st.y, g.normalDelta), &ipy);
+    b.nx = (int32_t)ipx;
+    b.ny = (int32_t)ipy;
+    return b;
+}
+
+__device__ __forceinline__ uint64_t gen_code_stochastic(const Grid& g, const CodeBase& b, float3 pos, uint32_t& rng)
 {
     const uint32_t levelMax = required_bits(g.baseDim) - 1u;
-    uint32_t level = base_level(g, pos);
     const uint32_t off = min((uint32_t)(-log2f(gsub(1.0f, next_float(rng)))), g.maxLevelOffset);
-    level = min(level + off, levelMax);
+    const uint32_t level = min(b.level + off, levelMax);
     const float levelDelta = gdiv(g.baseDelta, (float)(1u << level));
     const int32_t edge = (int32_t)(g.baseDim >> level) - 1;
     const float p[3] = { pos.x, pos.y, pos.z }, r[3] = { g.rmin.x, g.rmin.y, g.rmin.z };
@@ -174,16 +196,17 @@ __device__ __forceinline__ uint64_t gen_code_stochastic(const Grid& g, float3 po
         loc[k] = (uint32_t)max(0, min(i, edge));
     }
     const uint64_t mcPos = expand3_64(loc[0]) | (expand3_64(loc[1]) << 1) | (expand3_64(loc[2]) << 2);
-    const float2 st = dir_to_conc_octa(make_float3(normal.y, normal.z, normal.x));
-    float ipx, ipy;
-    const float fx = modff(gmul(st.x, g.normalDelta), &ipx);
-    const float fy = modff(gmul(st.y, g.normalDelta), &ipy);
-    int32_t nx = (int32_t)ipx, ny = (int32_t)ipy;
-    nx += (next_float(rng) > fx) ? 0 : 1;
-    ny += (next_float(rng) > fy) ? 0 : 1;
+    int32_t nx = b.nx, ny = b.ny;
+    nx += (next_float(rng) > b.fx) ? 0 : 1;
+    ny += (next_float(rng) > b.fy) ? 0 : 1;
     int2 t = make_int2(0, 0);
     if(g.normalDim - 1u != 0u) t = conc_octa_wrap_int(nx, ny, (int32_t)g.normalDim);
     return compose_code(mcPos, expand2_32((uint32_t)t.x) | (expand2_32((uint32_t)t.y) << 1), level);
+}
+
+__device__ __forceinline__ uint64_t gen_code_stochastic(const Grid& g, float3 pos, float3 normal, uint32_t& rng)
+{
+    return gen_code_stochastic(g, code_base(g, pos, normal), pos, rng);
 }
 
 __device__ __forceinline__ uint32_t first_slot(const Grid& g, uint64_t code)

@@ -167,15 +167,25 @@ k_guide_write_mc(GuideGrid G, GuidePaths Q, PtPaths P, PtSceneTables T,
     }
 }
 
-// GaussLobeMixtureT::Pdf
-__device__ __forceinline__ float mixture_pdf(const guide::Lobe (&lobes)[guide::kLobes],
-                                             const float (&w)[guide::kLobes], float sumW, float3 d)
+// GaussLobeMixtureT::Pdf; a repeated code's lobe pdf is the earlier one's.
+// The loops stay rolled (the lobes live in local memory): unrolled, the
+// shading kernel outgrows the instruction cache.
+__device__ __noinline__ float mixture_pdf(const guide::Lobe* lobes, const float* w, const uint64_t* codes,
+                                          float sumW, float3 d)
 {
     if(sumW == 0.0f) return 0.0f;
+    float lp[guide::kLobes];
     float pdf = 0.0f;
-#pragma unroll
+#pragma unroll 1
     for(uint32_t j = 0; j < guide::kLobes; j++)
-        if(w[j] != 0.0f) pdf = add(pdf, mul(w[j], guide::lobe_pdf(lobes[j], d)));
+    {
+        lp[j] = 0.0f;
+        if(w[j] == 0.0f) continue;
+        uint32_t q = 0;
+        while(q < j && codes[q] != codes[j]) q++;
+        lp[j] = (q < j) ? lp[q] : guide::lobe_pdf(lobes[j], d);
+        pdf = add(pdf, mul(w[j], lp[j]));
+    }
     return __fdiv_rn(pdf, sumW);
 }
 
@@ -279,44 +289,52 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                 const float3 woW = normalize3(wo);
 
                 // ---- GaussLobeMixtureT::LoadStochastic ----
+                // A code drawn again gives the slot and lobe it gave before
+                // (nothing writes chains while paths shade), so repeats reuse them.
                 guide::Lobe lobes[guide::kLobes];
                 float wts[guide::kLobes];
+                uint64_t codes[guide::kLobes];
+                uint32_t slots[guide::kLobes];
                 float sumW = 0.0f;
-                guide::Lobe sel;
-                sel.dir = make_float3(0, 0, 0); sel.kappa = 0.0f; sel.alpha = 0.0f;
-                float selW = 0.0f;
-                bool selected = false;
-                uint32_t liftedMC = guide::kInvalid;
+                uint32_t sIdx = guide::kInvalid;
                 uint32_t rng = Q.bk[i];
                 const float3 codeN = normalize3(woW);
-#pragma unroll
+                const guide::CodeBase cb = guide::code_base(G, pos, codeN);
+#pragma unroll 1
                 for(uint32_t j = 0; j < guide::kLobes; j++)
                 {
-                    const uint64_t code = guide::gen_code_stochastic(G, pos, codeN, rng);
-                    const uint32_t slot = guide::try_insert(G, code);
-                    if(slot == guide::kInvalid)
+                    codes[j] = guide::gen_code_stochastic(G, cb, pos, rng);
+                    uint32_t q = 0;
+                    while(q < j && codes[q] != codes[j]) q++;
+                    if(q < j)
                     {
-                        lobes[j].dir = make_float3(0, 0, 0); lobes[j].kappa = 0.0f; lobes[j].alpha = 0.0f;
-                        wts[j] = 0.0f;
-                        continue;
+                        slots[j] = slots[q]; lobes[j] = lobes[q]; wts[j] = wts[q];
                     }
-                    guide::Chain s;
-                    const float4 a = G.mcA[slot];
-                    s.target = f3(a);
-                    s.cosine = a.w;
-                    s.weight = G.mcW[slot];
-                    lobes[j] = guide::chain_to_lobe(s, G.mcN[slot], pos);
-                    wts[j] = s.weight;
+                    else
+                    {
+                        slots[j] = guide::try_insert(G, codes[j]);
+                        if(slots[j] == guide::kInvalid)
+                        {
+                            lobes[j].dir = make_float3(0, 0, 0); lobes[j].kappa = 0.0f; lobes[j].alpha = 0.0f;
+                            wts[j] = 0.0f;
+                        }
+                        else
+                        {
+                            guide::Chain s;
+                            const float4 a = G.mcA[slots[j]];
+                            s.target = f3(a);
+                            s.cosine = a.w;
+                            s.weight = G.mcW[slots[j]];
+                            lobes[j] = guide::chain_to_lobe(s, G.mcN[slots[j]], pos);
+                            wts[j] = s.weight;
+                        }
+                    }
+                    if(slots[j] == guide::kInvalid) continue;
                     sumW = add(sumW, wts[j]);
                     const float ratio = (sumW != 0.0f) ? __fdiv_rn(wts[j], sumW) : 1.0f;
-                    if(guide::next_float(rng) < ratio)
-                    {
-                        sel = lobes[j];
-                        selW = wts[j];
-                        selected = true;
-                        liftedMC = slot;
-                    }
+                    if(guide::next_float(rng) < ratio) sIdx = j;
                 }
+                const uint32_t liftedMC = (sIdx != guide::kInvalid) ? slots[sIdx] : guide::kInvalid;
                 Q.bk[i] = rng;
                 const float2 coN = guide::dir_to_conc_octa(woW);
 
@@ -338,11 +356,11 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                     // Y axis with pdf 0
                     float3 v = make_float3(0.0f, 1.0f, 0.0f);
                     float mpdf = 0.0f;
-                    if(selected && selW != 0.0f)
+                    if(sIdx != guide::kInvalid && wts[sIdx] != 0.0f)
                     {
                         const float3 u3 = rnd_s3(L, key, i, depth);
-                        v = guide::lobe_sample(sel, u3.x, u3.y);
-                        mpdf = mixture_pdf(lobes, wts, sumW, v);
+                        v = guide::lobe_sample(lobes[sIdx], u3.x, u3.y);
+                        mpdf = mixture_pdf(lobes, wts, codes, sumW, v);
                     }
                     wdir = v;
                     const float3 vn = normalize3(v);
@@ -363,7 +381,7 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                                                   add(add(mul(tng.y, Ll.x), mul(btg.y, Ll.y)), mul(nrm.y, Ll.z)),
                                                   add(add(mul(tng.z, Ll.x), mul(btg.z, Ll.y)), mul(nrm.z, Ll.z))));
                     orgOut = pre;
-                    pdf0 = mixture_pdf(lobes, wts, sumW, wdir);
+                    pdf0 = mixture_pdf(lobes, wts, codes, sumW, wdir);
                     pdf1 = bpdf;
                 }
                 const float pdfPath = add(mul(pdf0, mw0), mul(pdf1, mw1));     // BalanceCancelled<2>
@@ -425,7 +443,7 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                     const float3 Ls = make_float3(dot3(sdir, tng), dot3(sdir, btg), dot3(sdir, nrm));
                     float bpdf;
                     const Chan srefl = eval_material<NC>(sf, mt, alb, V, Ls, bpdf);
-                    float pdfS = add(mul(mixture_pdf(lobes, wts, sumW, sdir), mw0), mul(bpdf, mw1));
+                    float pdfS = add(mul(mixture_pdf(lobes, wts, codes, sumW, sdir), mw0), mul(bpdf, mw1));
                     pdfS = add(pdfS, lightPdf);
                     Chan srad = chan(0, 0, 0, 0);
                     if(pdfS != 0.0f)
@@ -468,24 +486,98 @@ k_guide_resolve(PtPaths P, GuidePaths Q)
     }
 }
 
-// The sorted records of a bounce: the first record of every cell applies the
-// cell's records in order (MCIrradiance::AtomicEMA's update).
+// MCIrradiance::AtomicEMA's update of record k of a run, split into the part
+// that does not depend on the average (known once the count before the run,
+// n0, and k are): n = min(n0 + k + 1, 128), t = max(1 / n, 0.01),
+// a = 1 - t, b = r t; the average then steps x = x a + b, exactly
+// Math::Lerp(x, r, t) = x (1 - t) + r t.
+__device__ __forceinline__ void ema_terms(uint32_t n0, uint32_t k, float r, float& a, float& b)
+{
+    const uint32_t nn = min(n0 + k + 1u, 128u);
+    const float t = fmaxf(__fdiv_rn(1.0f, (float)nn), 0.01f);
+    a = __fsub_rn(1.0f, t);
+    b = __fmul_rn(r, t);
+}
+
+// The sorted records of a bounce, one warp per window of 32 sorted
+// positions.  Each lane holding a cell's first record applies that cell's
+// records in order, all such cells of the window at once: every lane forms
+// its record's (a, b) terms in parallel, and the first lane of each cell runs
+// the dependent steps x = x a + b, taking the terms by shuffle.  A cell whose
+// records run past the window is finished by its first lane, window by window.
 __global__ void __launch_bounds__(kPtTPB)
 k_guide_apply(GuideGrid G, const uint32_t* __restrict__ keys, const uint32_t* __restrict__ idx,
               const float* __restrict__ vals, uint32_t n)
 {
     const uint32_t tableSize = G.tableMask + 1u;
-    for(uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for(uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c * 32u < n; c += warps)
     {
-        const uint32_t cell = keys[j] >> 1;
-        if(cell >= tableSize) continue;
-        if(j > 0u && (keys[j - 1] >> 1) == cell) continue;
-        const float2 e = G.irr[cell];
-        float v = e.x;
-        uint32_t cnt = __float_as_uint(e.y);
-        for(uint32_t q = j; q < n && (keys[q] >> 1) == cell; q++)
-            guide::irr_ema(v, cnt, vals[idx[q]]);
-        G.irr[cell] = make_float2(v, __uint_as_float(cnt));
+        const uint32_t j = c * 32u + lane;
+        const uint32_t key = (j < n) ? keys[j] : 0xFFFFFFFFu;
+        uint32_t prevKey = __shfl_up_sync(0xFFFFFFFFu, key, 1);
+        if(lane == 0u) prevKey = (j > 0u && j - 1u < n) ? keys[j - 1u] : 0xFFFFFFFFu;
+        const uint32_t cell = key >> 1;
+        const bool ok = cell < tableSize;
+        const bool head = ok && (j == 0u || (prevKey >> 1) != cell);
+        const uint32_t headMask = __ballot_sync(0xFFFFFFFFu, head);
+        if(headMask == 0u) continue;
+        const float r = ok ? vals[idx[j]] : 0.0f;
+        const uint32_t okMask = __ballot_sync(0xFFFFFFFFu, ok);
+        float v = 0.0f;
+        uint32_t cnt = 0;
+        if(head)
+        {
+            const float2 e = G.irr[cell];
+            v = e.x;
+            cnt = __float_as_uint(e.y);
+        }
+        // my cell's first lane in this window (none: a run from an earlier window)
+        const uint32_t mine = headMask & ((lane == 31u) ? 0xFFFFFFFFu : ((2u << lane) - 1u));
+        const uint32_t hl = mine ? 31u - (uint32_t)__clz(mine) : 32u;
+        const uint32_t n0 = __shfl_sync(0xFFFFFFFFu, cnt, hl & 31u);
+        float a = 1.0f, b = 0.0f;
+        if(ok && hl < 32u) ema_terms(n0, lane - hl, r, a, b);
+        // the record after the last one of my cell in this window: the next
+        // first record or empty record, else 32
+        const uint32_t bounds = (headMask | ~okMask) & ((lane == 31u) ? 0u : (0xFFFFFFFFu << (lane + 1u)));
+        const uint32_t segEnd = bounds ? (uint32_t)(__ffs(bounds) - 1) : 32u;
+#pragma unroll
+        for(uint32_t k = 0; k < 32u; k++)
+        {
+            const float ak = __shfl_sync(0xFFFFFFFFu, a, (lane + k) & 31u);
+            const float bk = __shfl_sync(0xFFFFFFFFu, b, (lane + k) & 31u);
+            if(head && lane + k < segEnd) v = __fadd_rn(__fmul_rn(v, ak), bk);
+        }
+        if(head) cnt = min(cnt + (segEnd - lane), 128u);
+        const uint32_t contMask = __ballot_sync(0xFFFFFFFFu, head && segEnd == 32u);
+        if(contMask)
+        {
+            const uint32_t cl = (uint32_t)(__ffs(contMask) - 1);
+            const uint32_t hc = __shfl_sync(0xFFFFFFFFu, cell, cl);
+            for(uint32_t p = c * 32u + 32u;; p += 32u)
+            {
+                const uint32_t q = p + lane;
+                const bool in = q < n && (keys[q] >> 1) == hc;
+                const float rr = in ? vals[idx[q]] : 0.0f;
+                // sorted: the cell's records in this window are a prefix of the lanes
+                const uint32_t len = (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, in));
+                const uint32_t c0 = __shfl_sync(0xFFFFFFFFu, cnt, cl);
+                float aa = 1.0f, bb = 0.0f;
+                if(in) ema_terms(c0, lane, rr, aa, bb);
+#pragma unroll
+                for(uint32_t k = 0; k < 32u; k++)
+                {
+                    const float ak = __shfl_sync(0xFFFFFFFFu, aa, k);
+                    const float bk = __shfl_sync(0xFFFFFFFFu, bb, k);
+                    if(lane == cl && k < len) v = __fadd_rn(__fmul_rn(v, ak), bk);
+                }
+                if(lane == cl) cnt = min(cnt + len, 128u);
+                if(len < 32u) break;
+            }
+        }
+        if(head) G.irr[cell] = make_float2(v, __uint_as_float(cnt));
     }
 }
 

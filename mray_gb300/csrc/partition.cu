@@ -93,6 +93,84 @@ k_ms_scan(uint32_t* __restrict__ hist, uint32_t len)
     }
 }
 
+// Large count tables: a three-kernel scan (per-block sums, one-block scan of
+// the sums, per-block exclusive scan plus its offset), kScanChunk entries per
+// block, 4 per thread.
+constexpr uint32_t kScanChunk = 4u * kScanTPB;
+constexpr uint32_t kSingleBlockScan = 65536u;   // at most this many entries: k_ms_scan
+
+// Exclusive scan of v across the block; the block's total in *total.
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* total)
+{
+    __shared__ uint32_t sWarp[kScanTPB / 32];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for(int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if(lane >= (uint32_t)o) x += y;
+    }
+    if(lane == 31u) sWarp[warp] = x;
+    __syncthreads();
+    if(warp == 0)
+    {
+        uint32_t w = (lane < kScanTPB / 32) ? sWarp[lane] : 0u;
+#pragma unroll
+        for(int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if(lane >= (uint32_t)o) w += y;
+        }
+        if(lane < kScanTPB / 32) sWarp[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t before = (warp ? sWarp[warp - 1] : 0u) + x - v;
+    if(total) *total = sWarp[kScanTPB / 32 - 1];
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(kScanTPB)
+k_scan_sums(const uint32_t* __restrict__ hist, uint32_t len, uint32_t* __restrict__ sums)
+{
+    const uint32_t base = blockIdx.x * kScanChunk + 4u * threadIdx.x;
+    uint32_t v = 0;
+#pragma unroll
+    for(uint32_t k = 0; k < 4u; k++) v += (base + k < len) ? hist[base + k] : 0u;
+    uint32_t total;
+    block_exclusive(v, &total);
+    if(threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanTPB)
+k_scan_top(uint32_t* __restrict__ sums, uint32_t n)
+{
+    uint32_t carry = 0;
+    for(uint32_t b = 0; b < n; b += kScanTPB)
+    {
+        const uint32_t i = b + threadIdx.x;
+        const uint32_t v = (i < n) ? sums[i] : 0u;
+        uint32_t total;
+        const uint32_t ex = block_exclusive(v, &total);
+        if(i < n) sums[i] = carry + ex;
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(kScanTPB)
+k_scan_apply(uint32_t* __restrict__ hist, uint32_t len, const uint32_t* __restrict__ sums)
+{
+    const uint32_t base = blockIdx.x * kScanChunk + 4u * threadIdx.x;
+    uint32_t a[4];
+#pragma unroll
+    for(uint32_t k = 0; k < 4u; k++) a[k] = (base + k < len) ? hist[base + k] : 0u;
+    uint32_t run = sums[blockIdx.x] + block_exclusive(a[0] + a[1] + a[2] + a[3], nullptr);
+#pragma unroll
+    for(uint32_t k = 0; k < 4u; k++)
+        if(base + k < len) { hist[base + k] = run; run += a[k]; }
+}
+
 __global__ void __launch_bounds__(kMsTPB)
 k_ms_scatter(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ idxIn,
              uint32_t* __restrict__ keysOut, uint32_t* __restrict__ idxOut,
@@ -239,7 +317,9 @@ cudaError_t ray_coherence_order(const void* rays, const uint32_t* idx, uint32_t 
 size_t multisplit_hist_words(uint32_t nMax, uint32_t digitBits)
 {
     const uint32_t tiles = (nMax + kMsTile - 1) / kMsTile;
-    return (size_t)(tiles ? tiles : 1u) << digitBits;
+    const size_t len = (size_t)(tiles ? tiles : 1u) << digitBits;
+    // the count table, then the block sums of its scan
+    return len + (len + kScanChunk - 1) / kScanChunk;
 }
 
 cudaError_t multisplit_pass(const uint32_t* keysIn, const uint32_t* idxIn, uint32_t* keysOut, uint32_t* idxOut,
@@ -251,7 +331,15 @@ cudaError_t multisplit_pass(const uint32_t* keysIn, const uint32_t* idxIn, uint3
     if(tiles == 0) tiles = 1;
     const uint32_t len = tiles << spec.digitBits;
     k_ms_hist<<<tiles, kMsTPB, 0, st>>>(keysIn, nDevice, nMax, spec, hist, tiles);
-    k_ms_scan<<<1, kScanTPB, 0, st>>>(hist, len);
+    if(len <= kSingleBlockScan) k_ms_scan<<<1, kScanTPB, 0, st>>>(hist, len);
+    else
+    {
+        const uint32_t blocks = (len + kScanChunk - 1) / kScanChunk;
+        uint32_t* sums = hist + len;
+        k_scan_sums<<<blocks, kScanTPB, 0, st>>>(hist, len, sums);
+        k_scan_top<<<1, kScanTPB, 0, st>>>(sums, blocks);
+        k_scan_apply<<<blocks, kScanTPB, 0, st>>>(hist, len, sums);
+    }
     k_ms_scatter<<<tiles, kMsTPB, 0, st>>>(keysIn, idxIn, keysOut, idxOut, nDevice, nMax, spec, hist, tiles);
     return cudaGetLastError();
 }

@@ -47,15 +47,15 @@ def box():
     return pt, oracle.PtScene(surf)
 
 
-def _render_both(pt, S, calls, w=32, h=32, spp=4, sampler="independent", seed=3, **kw):
-    cam = scenes.box_camera()
+def _render_both(pt, S, calls, w=32, h=32, spp=4, sampler="independent", seed=3, cam=None, depth=8, **kw):
+    cam = cam or scenes.box_camera()
     pt.guide_create(**kw)
     G = S.guide(**kw)
     gi, oi = None, None
     for c in range(calls):
-        pg = PathTracer.params(w, h, spp, cam, max_depth=8, rr_start=2, seed=seed, sample_start=spp * c,
+        pg = PathTracer.params(w, h, spp, cam, max_depth=depth, rr_start=2, seed=seed, sample_start=spp * c,
                                samples_per_pass=spp, sampler=sampler)
-        po = S.params(w, h, spp, cam, max_depth=8, rr_start=2, seed=seed, sample_start=spp * c,
+        po = S.params(w, h, spp, cam, max_depth=depth, rr_start=2, seed=seed, sample_start=spp * c,
                       sampler=3 if sampler == "pcg32" else 0)
         gi = pt.render_guided(pg, image=gi)
         oi = S.render_guided(po, G, spp, image=oi)
@@ -114,6 +114,55 @@ def test_guided_mixed_materials_matches_oracle():
     g, o, gs, os_ = _render_both(pt, S, 2, seed=5)
     _check_images(g, o)
     _check_grids(gs, os_)
+
+
+def _spectral_pair(surf, env=None):
+    import os
+    from mray_gb300 import spectral
+    gold = os.path.join(os.path.dirname(__file__), "golden")
+    res, lut = spectral.read_mrspectra(os.path.join(gold, "REC_709_r32.mrspectra"))
+    tables = spectral.load_tables(os.path.join(gold, "spectral_rec709.npz"))
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    if env is not None:
+        pt.set_env(env["texels"])
+    pt.set_spectral(res, lut, tables)
+    S = oracle.PtScene(surf, env=env, spectral=oracle.Spectral(os.path.join(gold, "REC_709_r32.mrspectra"),
+                                                               os.path.join(gold, "spectral_rec709.npz")))
+    return pt, S
+
+
+def test_guided_spectral_sky_matches_oracle():
+    """MRay's guided renderer is spectral (GuidedPathTracerSpectral): 4
+    wavelengths per path, and a skysphere whose misses feed the light records
+    with MIS against the uniform light sampler."""
+    env = dict(texels=scenes.sky_map(64, 32, seed=0))
+    pt, S = _spectral_pair(scenes.sky_scene(0), env)
+    g, o, gs, os_ = _render_both(pt, S, 2, seed=4)
+    _check_images(g, o)
+    _check_grids(gs, os_)
+    pt.close()
+
+
+def test_guided_c2_scene_small():
+    """The production scene (textured Lambert, GGX metal, glass, 8 area
+    lights, sky, 4 wavelengths) at a small film, depth 12: the same bar as
+    the plain tracer's test of that scene (98% of pixels, the rest may take
+    another path after a flipped decision)."""
+    surf, cam = scenes.c2_scene(0, texture_size=256)
+    env = dict(texels=scenes.sky_map(128, 64, seed=0))
+    pt, S = _spectral_pair(surf, env)
+    g, o, gs, os_ = _render_both(pt, S, 2, w=96, h=54, spp=2, seed=2, cam=cam, depth=12)
+    g, o = _img(g), _img(o)
+    close = (np.abs(g - o) <= 1e-4 * (1.0 + np.abs(o))).all(axis=-1).mean()
+    d = np.abs(g - o).max(axis=-1).ravel()
+    keep = d <= np.quantile(d, 0.98)
+    rel_kept = float(np.mean(((g - o).reshape(-1, 3)[keep]) ** 2 / (o.reshape(-1, 3)[keep] ** 2 + 1e-2)))
+    print("c2 guided: close %.4f relMSE %.3g kept %.3g" % (close, relmse(g, o), rel_kept))
+    assert close >= 0.95 and rel_kept <= 1e-5
+    stats = _check_grids(gs, os_)
+    print("c2 guided grid: entries %d, code differences %d, weights %.4f, irradiance %.4f" % stats)
+    pt.close()
 
 
 def test_guided_reproducible(box):
