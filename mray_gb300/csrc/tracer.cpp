@@ -48,7 +48,7 @@ uint32_t dt_bytes(uint32_t dt)
     return dt <= MRG_DT_STRING ? b[dt] : 0u;
 }
 
-enum : uint32_t { kLightPrim = 1, kLightSky = 2, kRendRGB = 0, kRendSpectral = 1 };
+enum : uint32_t { kLightPrim = 1, kLightSky = 2, kRendRGB = 0, kRendSpectral = 1, kRendGuided = 2 };
 
 struct TypeDef
 {
@@ -92,8 +92,17 @@ const std::vector<TypeDef>& types(uint32_t kind)
         A{ "totalSPP", MRG_DT_UINT32, 0, 0, 0 }, A{ "burstSize", MRG_DT_UINT32, 1, 0, 0 },
         A{ "renderMode", MRG_DT_STRING, 0, 0, 0 }, A{ "sampleMode", MRG_DT_STRING, 0, 0, 0 },
         A{ "rrRange", MRG_DT_VECTOR_2UI, 0, 0, 0 }, A{ "neeSamplerType", MRG_DT_STRING, 0, 0, 0 } };
+    // GuidedPTRenderer::StaticAttributeInfo (GuidedPTRenderer.cu:1273-1292)
+    static const std::vector<Attr> gattr = {
+        A{ "cacheEntryLimit", MRG_DT_UINT32, 1, 0, 0 }, A{ "cachePosBits", MRG_DT_UINT32, 1, 0, 0 },
+        A{ "cacheNormalBits", MRG_DT_UINT32, 1, 0, 0 }, A{ "cacheMaxLvlOffset", MRG_DT_UINT32, 1, 0, 0 },
+        A{ "cacheConeAperture", MRG_DT_FLOAT, 1, 0, 0 }, A{ "rrRange", MRG_DT_VECTOR_2UI, 0, 0, 0 },
+        A{ "totalSPP", MRG_DT_UINT32, 0, 0, 0 }, A{ "lightSampler", MRG_DT_STRING, 1, 0, 0 },
+        A{ "renderMode", MRG_DT_STRING, 0, 0, 0 }, A{ "burstSize", MRG_DT_UINT32, 1, 0, 0 },
+        A{ "lobeProbability", MRG_DT_FLOAT, 1, 0, 0 }, A{ "displayMode", MRG_DT_STRING, 0, 0, 0 } };
     static const std::vector<TypeDef> rend = { { "(R)PathTracerRGB", rattr, kRendRGB, false },
-                                               { "(R)PathTracerSpectral", rattr, kRendSpectral, false } };
+                                               { "(R)PathTracerSpectral", rattr, kRendSpectral, false },
+                                               { "(R)GuidedPathTracerSpectral", gattr, kRendGuided, false } };
     static const std::vector<TypeDef> none;
     switch(kind)
     {
@@ -179,6 +188,7 @@ struct Renderer
     uint32_t totalSpp = 16384, burst = 1;
     uint32_t sampleMode = MRG_PT_PURE;
     uint32_t rrStart = 4, maxDepth = 20;
+    mrg_guide_params guide{};      // the guided renderer's grid options
 };
 
 struct Spectral
@@ -739,6 +749,57 @@ mrg_status push_renderer(mrg_tracer* t, uint32_t rid, uint32_t ai, const void* d
     const std::string str = dt == MRG_DT_STRING ? std::string(static_cast<const char*>(data), bytes) : std::string();
     uint32_t u[2] = { 0, 0 };
     if(dt != MRG_DT_STRING) std::memcpy(u, data, bytes);
+    float f = 0.0f;
+    if(dt == MRG_DT_FLOAT) std::memcpy(&f, data, 4);
+    if(td.code == kRendGuided)
+    {
+        // GuidedPTRenderer::PushAttribute (GuidedPTRenderer.cu:489-540)
+        switch(ai)
+        {
+            case 0:
+                if(u[0] == 0 || u[0] > (1u << 27)) return err("cacheEntryLimit must be in [1, 2^27]");
+                r.guide.entryLimit = u[0];
+                break;
+            case 1:
+                if(u[0] > 15u) return err("cachePosBits exceeds the maximum 15");
+                r.guide.posBits = u[0];
+                break;
+            case 2:
+                if(u[0] > 3u) return err("cacheNormalBits exceeds the maximum 3");
+                r.guide.normalBits = u[0];
+                break;
+            case 3: r.guide.maxLevelOffset = u[0]; break;
+            case 4:
+                if(!(f >= 0.0f)) return err("cacheConeAperture must be >= 0");
+                r.guide.coneAperture = f;
+                break;
+            case 5:
+                if(u[1] == 0 || u[0] > u[1]) return err("rrRange must satisfy start <= end, end > 0");
+                r.rrStart = u[0]; r.maxDepth = u[1];
+                break;
+            case 6:
+                if(u[0] == 0) return err("totalSPP must be positive");
+                r.totalSpp = u[0];
+                break;
+            case 7:
+                if(str != "Uniform") return err("unknown lightSampler \"" + str + "\" (Uniform only)");
+                break;
+            case 8:
+                if(str != "Throughput" && str != "Latency") return err("unknown renderMode \"" + str + "\"");
+                break;
+            case 9: r.burst = std::max(1u, u[0]); break;
+            case 10:
+                if(!(f >= 0.0f && f <= 1.0f)) return err("lobeProbability must be in [0, 1]");
+                r.guide.lobeProbability = f;
+                break;
+            case 11:
+                // the debug displays (Grid, LightCache, MCTarget, ...) are
+                // host-side reads of mrg_guide_read
+                if(str != "Render") return err("displayMode \"" + str + "\": only Render is drawn");
+                break;
+        }
+        return MRG_OK;
+    }
     switch(ai)
     {
         case 0:
@@ -778,11 +839,16 @@ mrg_status start_render(mrg_tracer* t, uint32_t rid, uint32_t csid, uint32_t w, 
     float cam[9], fnp[4];
     mrg_status s = camera_of(t, csid, cam, fnp);
     if(s != MRG_OK) return s;
-    const bool spectral = types(MRG_KIND_RENDERER)[r.type].code == kRendSpectral;
+    const uint32_t code = types(MRG_KIND_RENDERER)[r.type].code;
+    const bool spectral = code == kRendSpectral || code == kRendGuided;
+    if(code == kRendGuided && t->params.samplerType == MRG_TRACER_SAMPLER_ZSOBOL)
+        return err("(R)GuidedPathTracerSpectral: the ZSobol sampler is not supported");
     if(spectral)
     {
         const Spectral& S = t->spectral;
-        if(!S.lutRes) return err("(R)PathTracerSpectral needs the spectral data (mrg_tracer_set_spectral_data)");
+        if(!S.lutRes)
+            return err(std::string(types(MRG_KIND_RENDERER)[r.type].name) +
+                       " needs the spectral data (mrg_tracer_set_spectral_data)");
         s = mrg_pt_set_spectral(t->ctx, S.lutRes, S.lut.data(), S.cieCount, S.cie.data(), S.integrals, S.spd.data(),
                                 S.norm, S.xyzToRgb);
     }
@@ -806,6 +872,9 @@ mrg_status start_render(mrg_tracer* t, uint32_t rid, uint32_t csid, uint32_t w, 
     P.sampler = t->params.samplerType == MRG_TRACER_SAMPLER_ZSOBOL ? MRG_PT_SAMPLER_ZSOBOL : MRG_PT_SAMPLER_PCG32;
     P.samplerMaxSpp = r.totalSpp;
     if((s = cuda_status(cudaSetDevice(t->params.device), "StartRender")) != MRG_OK) return s;
+    // the guided renderer's grid is reset at every StartRender (HashGrid::Reset
+    // over the scene box, GuidedPTRenderer.cu:1146-1161)
+    if(code == kRendGuided && (s = mrg_guide_create(t->ctx, &r.guide)) != MRG_OK) return s;
     const size_t bytes = sizeof(float) * 4 * (size_t)w * h;
     if((s = cuda_status(cudaMalloc(&t->dFilm, bytes), "film")) != MRG_OK) return s;
     if((s = cuda_status(cudaMemset(t->dFilm, 0, bytes), "film")) != MRG_OK) return s;
@@ -837,7 +906,9 @@ mrg_status render_work(mrg_tracer* t, mrg_tracer_render_output* out)
         t->P.sampleStart = t->done;
         mrg_status s;
         if((s = cuda_status(cudaEventRecord(t->ev[0], nullptr), "DoRenderWork")) != MRG_OK) return s;
-        if((s = mrg_pt_render(t->ctx, &t->P, t->dFilm, nullptr)) != MRG_OK) return s;
+        const bool guided = types(MRG_KIND_RENDERER)[t->renderers[t->renderer].type].code == kRendGuided;
+        if((s = guided ? mrg_pt_render_guided(t->ctx, &t->P, t->dFilm, nullptr)
+                       : mrg_pt_render(t->ctx, &t->P, t->dFilm, nullptr)) != MRG_OK) return s;
         if((s = cuda_status(cudaEventRecord(t->ev[1], nullptr), "DoRenderWork")) != MRG_OK) return s;
         if((s = cuda_status(cudaEventSynchronize(t->ev[1]), "DoRenderWork")) != MRG_OK) return s;
         float ms = 0;
@@ -1360,6 +1431,13 @@ mrg_status mrg_tracer_create_renderer(mrg_tracer* t, const char* type_name, uint
     Renderer r;
     r.type = ty;
     r.alive = true;
+    mrg_guide_defaults(&r.guide);
+    if(types(MRG_KIND_RENDERER)[ty].code == kRendGuided)
+    {
+        // GuidedPTRDetail::Options defaults (GuidedPTRendererShaders.h:79-133)
+        r.rrStart = 2;
+        r.maxDepth = 20;
+    }
     *renderer_id = (uint32_t)t->renderers.size();
     t->renderers.push_back(r);
     return MRG_OK;
@@ -1403,8 +1481,14 @@ mrg_status mrg_tracer_set_camera_transform(mrg_tracer* t, uint32_t renderer_id, 
     std::memcpy(t->P.camPos, cam, 12);
     std::memcpy(t->P.camGaze, cam + 3, 12);
     std::memcpy(t->P.camUp, cam + 6, 12);
-    // a moved camera starts the accumulation again
+    // a moved camera starts the accumulation again, and the guided renderer's
+    // grid with it (a new camera resets the hash grid, GuidedPTRenderer.cu:988-1006)
     t->done = 0;
+    if(types(MRG_KIND_RENDERER)[t->renderers[renderer_id].type].code == kRendGuided)
+    {
+        const mrg_status s = mrg_guide_clear(t->ctx);
+        if(s != MRG_OK) return s;
+    }
     return cuda_status(cudaMemset(t->dFilm, 0, sizeof(float) * 4 * (size_t)t->P.width * t->P.height), "film");
 }
 

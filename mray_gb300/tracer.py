@@ -264,13 +264,15 @@ class Tracer:
         self._call("mrg_tracer_destroy_renderer", renderer_id)
 
     def push_renderer_attribute(self, renderer_id, attribute_index, value):
-        """value: an int (totalSPP, burstSize), a str (renderMode, sampleMode,
-        neeSamplerType) or a pair of ints (rrRange)."""
+        """value: an int (totalSPP, burstSize, the guided renderer's cache
+        options), a float (cacheConeAperture, lobeProbability), a str
+        (renderMode, sampleMode, neeSamplerType, lightSampler, displayMode) or
+        a pair of ints (rrRange)."""
         if isinstance(value, str):
             b = value.encode()
             self._call("mrg_tracer_push_renderer_attribute", renderer_id, attribute_index, b, len(b))
             return
-        a = _u32s(value)
+        a = np.ascontiguousarray([value], np.float32) if isinstance(value, float) else _u32s(value)
         self._call("mrg_tracer_push_renderer_attribute", renderer_id, attribute_index, a.ctypes.data, a.nbytes)
 
     def start_render(self, renderer_id, cam_surface_id, width, height, region=None):

@@ -193,6 +193,43 @@ def test_spectral_renderer_matches_direct_path():
     assert np.array_equal(rgb, want_rgb)
 
 
+def test_guided_renderer_matches_direct_path():
+    """(R)GuidedPathTracerSpectral through the tracer calls: the grid is reset
+    at StartRender and learns across the render-work calls, as
+    mrg_guide_create and successive mrg_pt_render_guided calls do."""
+    from mray_gb300 import spectral
+    res, lut = spectral.read_mrspectra(os.path.join(GOLD, "REC_709_r32.mrspectra"))
+    tables = spectral.load_tables(os.path.join(GOLD, "spectral_rec709.npz"))
+    surf = _lights_unculled(scenes.box_scene_mixed(0))
+    cam = scenes.box_camera()
+    total, burst = 12, 4
+    with Tracer(seed=6) as t:
+        t.set_spectral_data(res, lut, tables)
+        cs = push_surfaces(t, surf, cam)
+        t.commit_surfaces()
+        r = t.create_renderer("(R)GuidedPathTracerSpectral")
+        t.push_renderer_attribute(r, 5, (2, 8))
+        t.push_renderer_attribute(r, 6, total)
+        t.push_renderer_attribute(r, 8, "Latency")
+        t.push_renderer_attribute(r, 9, burst)
+        t.push_renderer_attribute(r, 11, "Render")
+        t.start_render(r, cs, 40, 32)
+        while not t.do_render_work()["finished"]:
+            pass
+        film = t.read_film()
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    pt.set_spectral(res, lut, tables)
+    pt.guide_create()
+    img = None
+    for s0 in range(0, total, burst):
+        img = pt.render_guided(PathTracer.params(40, 32, burst, cam, max_depth=8, rr_start=2, seed=6,
+                                                 sample_start=s0, sampler="pcg32"), image=img)
+    pt.close()
+    assert np.isfinite(film).all() and film[..., 3].min() == total
+    assert np.array_equal(film, img.cpu().numpy())
+
+
 def test_spectral_renderer_needs_its_data():
     with Tracer() as t:
         cs = push_surfaces(t, scenes.box_scene(0), scenes.box_camera())

@@ -30,7 +30,7 @@ def test_type_lists(tr):
     assert tr.camera_groups() == ["(C)Pinhole"]
     assert tr.medium_groups() == []
     assert tr.light_groups() == ["(L)Prim(P)Triangle", "(L)Skysphere_Spherical"]
-    assert tr.renderers() == ["(R)PathTracerRGB", "(R)PathTracerSpectral"]
+    assert tr.renderers() == ["(R)PathTracerRGB", "(R)PathTracerSpectral", "(R)GuidedPathTracerSpectral"]
 
 
 def test_attribute_info_follows_mray(tr):
@@ -60,6 +60,14 @@ def test_attribute_info_follows_mray(tr):
     assert [(a["name"], a["data_type"], a["optional"]) for a in r] == [
         ("totalSPP", "UINT32", False), ("burstSize", "UINT32", True), ("renderMode", "STRING", False),
         ("sampleMode", "STRING", False), ("rrRange", "VECTOR_2UI", False), ("neeSamplerType", "STRING", False)]
+    # GuidedPTRenderer::StaticAttributeInfo (GuidedPTRenderer.cu:1273-1292)
+    g = tr.attribute_info("renderer", "(R)GuidedPathTracerSpectral")
+    assert [(a["name"], a["data_type"], a["optional"]) for a in g] == [
+        ("cacheEntryLimit", "UINT32", True), ("cachePosBits", "UINT32", True), ("cacheNormalBits", "UINT32", True),
+        ("cacheMaxLvlOffset", "UINT32", True), ("cacheConeAperture", "FLOAT", True),
+        ("rrRange", "VECTOR_2UI", False), ("totalSPP", "UINT32", False), ("lightSampler", "STRING", True),
+        ("renderMode", "STRING", False), ("burstSize", "UINT32", True), ("lobeProbability", "FLOAT", True),
+        ("displayMode", "STRING", False)]
     with pytest.raises(N.MRGError, match="Unable to find type"):
         tr.attribute_info("material", "(Mt)Nope")
 
@@ -185,6 +193,19 @@ def test_renderer_options(tr):
     tr.destroy_renderer(r)
     with pytest.raises(N.MRGError, match="unknown renderer"):
         tr.push_renderer_attribute(r, 0, 1)
+
+
+def test_guided_renderer_options(tr):
+    r = tr.create_renderer("(R)GuidedPathTracerSpectral")
+    for idx, v in ((0, 500000), (1, 12), (2, 3), (3, 2), (4, 1.5), (5, (2, 12)), (6, 64), (7, "Uniform"),
+                   (8, "Throughput"), (8, "Latency"), (9, 4), (10, 0.5), (11, "Render")):
+        tr.push_renderer_attribute(r, idx, v)
+    for idx, bad, msg in ((1, 16, "cachePosBits"), (2, 4, "cacheNormalBits"), (0, 0, "cacheEntryLimit"),
+                          (4, -1.0, "cacheConeAperture"), (10, 1.5, "lobeProbability"), (5, (9, 3), "rrRange"),
+                          (6, 0, "positive"), (7, "PowerWeighted", "Uniform only"), (11, "MCTarget", "only Render"),
+                          (8, "Fast", "unknown renderMode"), (12, 1, "Unknown attribute index")):
+        with pytest.raises(N.MRGError, match=msg):
+            tr.push_renderer_attribute(r, idx, bad)
 
 
 def test_parameters_and_memory(cuda_lib):

@@ -59,7 +59,8 @@ int main()
     // type lists and attribute information in MRay's types
     const auto mats = tr->MaterialGroups();
     check(mats.size() == 4 && mats[0] == "(Mt)Lambert" && mats[3] == "(Mt)Unreal", "MaterialGroups");
-    check(tr->Renderers().size() == 2 && tr->Renderers()[0] == "(R)PathTracerRGB", "Renderers");
+    check(tr->Renderers().size() == 3 && tr->Renderers()[0] == "(R)PathTracerRGB" &&
+          tr->Renderers()[2] == "(R)GuidedPathTracerSpectral", "Renderers");
     const auto lam = tr->AttributeInfoMat("(Mt)Lambert");
     check(lam.size() == 2 && lam[0].name == "albedo" &&
           lam[0].isTexturable == AttributeTexturable::MR_TEXTURE_OR_CONSTANT &&
@@ -143,6 +144,17 @@ int main()
     check(e.find("unknown sampleMode") != std::string::npos, "bad sampleMode throws");
     const auto rinfo = tr->AttributeInfo(rid);
     check(rinfo.size() == 6 && rinfo[1].isOptional == AttributeOptionality::MR_OPTIONAL, "AttributeInfo(RendererId)");
+    // the guided renderer's options in MRay's types (GuidedPTRenderer.cu:1273-1292)
+    const RendererId gid = tr->CreateRenderer("(R)GuidedPathTracerSpectral");
+    const auto ginfo = tr->AttributeInfo(gid);
+    check(ginfo.size() == 12 && ginfo[4].name == "cacheConeAperture" &&
+          ginfo[4].dataType.Name() == MRayDataEnum::MR_FLOAT && ginfo[5].dataType.Name() == MRayDataEnum::MR_VECTOR_2UI &&
+          ginfo[10].isOptional == AttributeOptionality::MR_OPTIONAL, "AttributeInfo(guided renderer)");
+    tr->PushRendererAttribute(gid, 4, make<Float>({ Float(0.8) }));
+    tr->PushRendererAttribute(gid, 10, make<Float>({ Float(0.5) }));
+    tr->PushRendererAttribute(gid, 11, make_string("Render"));
+    e = throws([&] { tr->PushRendererAttribute(gid, 11, make_string("MCTarget")); });
+    check(e.find("only Render") != std::string::npos, "guided displayMode throws");
 
     // the commit needs a device
     e = throws([&] { tr->CommitSurfaces(); });
