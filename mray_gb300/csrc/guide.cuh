@@ -248,6 +248,25 @@ __device__ __forceinline__ uint32_t try_insert(const Grid& g, uint64_t code)
     return kInvalid;
 }
 
+// TryInsertAtomic's probe from slot `index` whose code was already read as c
+// (the entry-limit test done by the caller).
+__device__ __forceinline__ uint32_t insert_from(const Grid& g, uint64_t code, uint32_t index, unsigned long long c)
+{
+    for(uint32_t i = index;; i = (i + 1u) & g.tableMask)
+    {
+        if(i != index) c = *(volatile unsigned long long*)&g.codes[i];
+        if(c == code) return i;
+        if(c == kEmpty)
+        {
+            const unsigned long long old = atomicCAS(&g.codes[i], kEmpty, (unsigned long long)code);
+            if(old == kEmpty) { atomicAdd(g.counter, 1u); return i; }
+            if(old == code) return i;
+        }
+        if(i == ((index - 1u) & g.tableMask)) break;
+    }
+    return kInvalid;
+}
+
 // ---- Gaussian (vMF) lobe ------------------------------------------------------
 struct Lobe
 {

@@ -167,24 +167,60 @@ k_guide_write_mc(GuideGrid G, GuidePaths Q, PtPaths P, PtSceneTables T,
     }
 }
 
+// A thread's mixture (GaussLobeMixtureSharedT's layout idea,
+// GuidedPTRendererShaders.h:191-214): per lobe its direction, kappa, alpha,
+// weight, code, slot and pdf scratch, one shared-memory word per field, lobe
+// and thread (thread-contiguous, so bank-conflict free).  Kept off the local
+// stack, which spilled to L2 at this occupancy.
+constexpr uint32_t kMixFields = 10;
+constexpr size_t kMixSmem = (size_t)kMixFields * guide::kLobes * kPtTPB * sizeof(float);
+enum : uint32_t { kMxDx = 0, kMxDy, kMxDz, kMxKappa, kMxAlpha, kMxW, kMxCodeLo, kMxCodeHi, kMxSlot, kMxPdf };
+
+struct Mix
+{
+    float* p;
+    __device__ __forceinline__ float& f(uint32_t field, uint32_t j) const
+    {
+        return p[(field * guide::kLobes + j) * kPtTPB + threadIdx.x];
+    }
+    __device__ __forceinline__ uint32_t& u(uint32_t field, uint32_t j) const
+    {
+        return reinterpret_cast<uint32_t&>(f(field, j));
+    }
+    __device__ __forceinline__ guide::Lobe lobe(uint32_t j) const
+    {
+        guide::Lobe l;
+        l.dir = make_float3(f(kMxDx, j), f(kMxDy, j), f(kMxDz, j));
+        l.kappa = f(kMxKappa, j);
+        l.alpha = f(kMxAlpha, j);
+        return l;
+    }
+    __device__ __forceinline__ void set(uint32_t j, const guide::Lobe& l, float w) const
+    {
+        f(kMxDx, j) = l.dir.x; f(kMxDy, j) = l.dir.y; f(kMxDz, j) = l.dir.z;
+        f(kMxKappa, j) = l.kappa; f(kMxAlpha, j) = l.alpha; f(kMxW, j) = w;
+    }
+    __device__ __forceinline__ bool same_code(uint32_t a, uint32_t b) const
+    {
+        return u(kMxCodeLo, a) == u(kMxCodeLo, b) && u(kMxCodeHi, a) == u(kMxCodeHi, b);
+    }
+};
+
 // GaussLobeMixtureT::Pdf; a repeated code's lobe pdf is the earlier one's.
-// The loops stay rolled (the lobes live in local memory): unrolled, the
-// shading kernel outgrows the instruction cache.
-__device__ __noinline__ float mixture_pdf(const guide::Lobe* lobes, const float* w, const uint64_t* codes,
-                                          float sumW, float3 d)
+__device__ __noinline__ float mixture_pdf(Mix m, float sumW, float3 d)
 {
     if(sumW == 0.0f) return 0.0f;
-    float lp[guide::kLobes];
     float pdf = 0.0f;
 #pragma unroll 1
     for(uint32_t j = 0; j < guide::kLobes; j++)
     {
-        lp[j] = 0.0f;
-        if(w[j] == 0.0f) continue;
+        const float w = m.f(kMxW, j);
+        if(w == 0.0f) continue;
         uint32_t q = 0;
-        while(q < j && codes[q] != codes[j]) q++;
-        lp[j] = (q < j) ? lp[q] : guide::lobe_pdf(lobes[j], d);
-        pdf = add(pdf, mul(w[j], lp[j]));
+        while(q < j && !m.same_code(q, j)) q++;
+        const float lp = (q < j) ? m.f(kMxPdf, q) : guide::lobe_pdf(m.lobe(j), d);
+        m.f(kMxPdf, j) = lp;
+        pdf = add(pdf, mul(w, lp));
     }
     return __fdiv_rn(pdf, sumW);
 }
@@ -199,6 +235,7 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                uint32_t* nextList, uint32_t* nextCount)
 {
     constexpr int NC = SPEC ? 4 : 3;
+    extern __shared__ float gmix[];
     const PtLight* __restrict__ lights = T.lights;
     const uint32_t n = *aliveCount;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -291,10 +328,7 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                 // ---- GaussLobeMixtureT::LoadStochastic ----
                 // A code drawn again gives the slot and lobe it gave before
                 // (nothing writes chains while paths shade), so repeats reuse them.
-                guide::Lobe lobes[guide::kLobes];
-                float wts[guide::kLobes];
-                uint64_t codes[guide::kLobes];
-                uint32_t slots[guide::kLobes];
+                const Mix mx{ gmix };
                 float sumW = 0.0f;
                 uint32_t sIdx = guide::kInvalid;
                 uint32_t rng = Q.bk[i];
@@ -303,38 +337,44 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
 #pragma unroll 1
                 for(uint32_t j = 0; j < guide::kLobes; j++)
                 {
-                    codes[j] = guide::gen_code_stochastic(G, cb, pos, rng);
+                    const uint64_t code = guide::gen_code_stochastic(G, cb, pos, rng);
+                    mx.u(kMxCodeLo, j) = (uint32_t)code;
+                    mx.u(kMxCodeHi, j) = (uint32_t)(code >> 32);
                     uint32_t q = 0;
-                    while(q < j && codes[q] != codes[j]) q++;
+                    while(q < j && !mx.same_code(q, j)) q++;
+                    uint32_t slot;
+                    float w;
                     if(q < j)
                     {
-                        slots[j] = slots[q]; lobes[j] = lobes[q]; wts[j] = wts[q];
+                        slot = mx.u(kMxSlot, q);
+                        w = mx.f(kMxW, q);
+                        mx.set(j, mx.lobe(q), w);
                     }
                     else
                     {
-                        slots[j] = guide::try_insert(G, codes[j]);
-                        if(slots[j] == guide::kInvalid)
+                        slot = guide::try_insert(G, code);
+                        guide::Lobe l;
+                        l.dir = make_float3(0, 0, 0); l.kappa = 0.0f; l.alpha = 0.0f;
+                        w = 0.0f;
+                        if(slot != guide::kInvalid)
                         {
-                            lobes[j].dir = make_float3(0, 0, 0); lobes[j].kappa = 0.0f; lobes[j].alpha = 0.0f;
-                            wts[j] = 0.0f;
+                            guide::Chain c;
+                            const float4 a = G.mcA[slot];
+                            c.target = f3(a);
+                            c.cosine = a.w;
+                            c.weight = G.mcW[slot];
+                            l = guide::chain_to_lobe(c, G.mcN[slot], pos);
+                            w = c.weight;
                         }
-                        else
-                        {
-                            guide::Chain s;
-                            const float4 a = G.mcA[slots[j]];
-                            s.target = f3(a);
-                            s.cosine = a.w;
-                            s.weight = G.mcW[slots[j]];
-                            lobes[j] = guide::chain_to_lobe(s, G.mcN[slots[j]], pos);
-                            wts[j] = s.weight;
-                        }
+                        mx.set(j, l, w);
                     }
-                    if(slots[j] == guide::kInvalid) continue;
-                    sumW = add(sumW, wts[j]);
-                    const float ratio = (sumW != 0.0f) ? __fdiv_rn(wts[j], sumW) : 1.0f;
+                    mx.u(kMxSlot, j) = slot;
+                    if(slot == guide::kInvalid) continue;
+                    sumW = add(sumW, w);
+                    const float ratio = (sumW != 0.0f) ? __fdiv_rn(w, sumW) : 1.0f;
                     if(guide::next_float(rng) < ratio) sIdx = j;
                 }
-                const uint32_t liftedMC = (sIdx != guide::kInvalid) ? slots[sIdx] : guide::kInvalid;
+                const uint32_t liftedMC = (sIdx != guide::kInvalid) ? mx.u(kMxSlot, sIdx) : guide::kInvalid;
                 Q.bk[i] = rng;
                 const float2 coN = guide::dir_to_conc_octa(woW);
 
@@ -356,11 +396,11 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                     // Y axis with pdf 0
                     float3 v = make_float3(0.0f, 1.0f, 0.0f);
                     float mpdf = 0.0f;
-                    if(sIdx != guide::kInvalid && wts[sIdx] != 0.0f)
+                    if(sIdx != guide::kInvalid && mx.f(kMxW, sIdx) != 0.0f)
                     {
                         const float3 u3 = rnd_s3(L, key, i, depth);
-                        v = guide::lobe_sample(lobes[sIdx], u3.x, u3.y);
-                        mpdf = mixture_pdf(lobes, wts, codes, sumW, v);
+                        v = guide::lobe_sample(mx.lobe(sIdx), u3.x, u3.y);
+                        mpdf = mixture_pdf(mx, sumW, v);
                     }
                     wdir = v;
                     const float3 vn = normalize3(v);
@@ -381,7 +421,7 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                                                   add(add(mul(tng.y, Ll.x), mul(btg.y, Ll.y)), mul(nrm.y, Ll.z)),
                                                   add(add(mul(tng.z, Ll.x), mul(btg.z, Ll.y)), mul(nrm.z, Ll.z))));
                     orgOut = pre;
-                    pdf0 = mixture_pdf(lobes, wts, codes, sumW, wdir);
+                    pdf0 = mixture_pdf(mx, sumW, wdir);
                     pdf1 = bpdf;
                 }
                 const float pdfPath = add(mul(pdf0, mw0), mul(pdf1, mw1));     // BalanceCancelled<2>
@@ -443,7 +483,7 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                     const float3 Ls = make_float3(dot3(sdir, tng), dot3(sdir, btg), dot3(sdir, nrm));
                     float bpdf;
                     const Chan srefl = eval_material<NC>(sf, mt, alb, V, Ls, bpdf);
-                    float pdfS = add(mul(mixture_pdf(lobes, wts, codes, sumW, sdir), mw0), mul(bpdf, mw1));
+                    float pdfS = add(mul(mixture_pdf(mx, sumW, sdir), mw0), mul(bpdf, mw1));
                     pdfS = add(pdfS, lightPdf);
                     Chan srad = chan(0, 0, 0, 0);
                     if(pdfS != 0.0f)
@@ -504,10 +544,10 @@ __device__ __forceinline__ void ema_terms(uint32_t n0, uint32_t k, float r, floa
 // records in order, all such cells of the window at once: every lane forms
 // its record's (a, b) terms in parallel, and the first lane of each cell runs
 // the dependent steps x = x a + b, taking the terms by shuffle.  A cell whose
-// records run past the window is finished by its first lane, window by window.
+// records run past the window goes to the long-run list instead, whole.
 __global__ void __launch_bounds__(kPtTPB)
-k_guide_apply(GuideGrid G, const uint32_t* __restrict__ keys, const uint32_t* __restrict__ idx,
-              const float* __restrict__ vals, uint32_t n)
+k_guide_apply(GuideGrid G, const uint32_t* __restrict__ keys, const float* __restrict__ vals, uint32_t n,
+              uint2* __restrict__ longRuns, uint32_t* longCount)
 {
     const uint32_t tableSize = G.tableMask + 1u;
     const uint32_t lane = threadIdx.x & 31u;
@@ -523,26 +563,28 @@ k_guide_apply(GuideGrid G, const uint32_t* __restrict__ keys, const uint32_t* __
         const bool head = ok && (j == 0u || (prevKey >> 1) != cell);
         const uint32_t headMask = __ballot_sync(0xFFFFFFFFu, head);
         if(headMask == 0u) continue;
-        const float r = ok ? vals[idx[j]] : 0.0f;
+        // my cell's first lane in this window (none: a run from an earlier window)
+        const uint32_t mine = headMask & ((lane == 31u) ? 0xFFFFFFFFu : ((2u << lane) - 1u));
+        const uint32_t hl = mine ? 31u - (uint32_t)__clz(mine) : 32u;
+        // the record after the last one of my cell in this window: the next
+        // first record or empty record, else 32
         const uint32_t okMask = __ballot_sync(0xFFFFFFFFu, ok);
+        const uint32_t bounds = (headMask | ~okMask) & ((lane == 31u) ? 0u : (0xFFFFFFFFu << (lane + 1u)));
+        const uint32_t segEnd = bounds ? (uint32_t)(__ffs(bounds) - 1) : 32u;
+        const uint32_t hlEnd = __shfl_sync(0xFFFFFFFFu, segEnd, hl & 31u);
+        const bool shortRun = hl < 32u && hlEnd < 32u;        // my record belongs to a run ending here
+        const float r = (ok && shortRun) ? vals[j] : 0.0f;
         float v = 0.0f;
         uint32_t cnt = 0;
-        if(head)
+        if(head && segEnd < 32u)
         {
             const float2 e = G.irr[cell];
             v = e.x;
             cnt = __float_as_uint(e.y);
         }
-        // my cell's first lane in this window (none: a run from an earlier window)
-        const uint32_t mine = headMask & ((lane == 31u) ? 0xFFFFFFFFu : ((2u << lane) - 1u));
-        const uint32_t hl = mine ? 31u - (uint32_t)__clz(mine) : 32u;
         const uint32_t n0 = __shfl_sync(0xFFFFFFFFu, cnt, hl & 31u);
         float a = 1.0f, b = 0.0f;
-        if(ok && hl < 32u) ema_terms(n0, lane - hl, r, a, b);
-        // the record after the last one of my cell in this window: the next
-        // first record or empty record, else 32
-        const uint32_t bounds = (headMask | ~okMask) & ((lane == 31u) ? 0u : (0xFFFFFFFFu << (lane + 1u)));
-        const uint32_t segEnd = bounds ? (uint32_t)(__ffs(bounds) - 1) : 32u;
+        if(ok && shortRun) ema_terms(n0, lane - hl, r, a, b);
 #pragma unroll
         for(uint32_t k = 0; k < 32u; k++)
         {
@@ -550,34 +592,69 @@ k_guide_apply(GuideGrid G, const uint32_t* __restrict__ keys, const uint32_t* __
             const float bk = __shfl_sync(0xFFFFFFFFu, b, (lane + k) & 31u);
             if(head && lane + k < segEnd) v = __fadd_rn(__fmul_rn(v, ak), bk);
         }
-        if(head) cnt = min(cnt + (segEnd - lane), 128u);
-        const uint32_t contMask = __ballot_sync(0xFFFFFFFFu, head && segEnd == 32u);
-        if(contMask)
+        if(head && segEnd < 32u) G.irr[cell] = make_float2(v, __uint_as_float(min(cnt + (segEnd - lane), 128u)));
+        if(head && segEnd == 32u) longRuns[atomicAdd(longCount, 1u)] = make_uint2(j, cell);
+    }
+}
+
+// Runs longer than a window, one block per run: the block forms the (a, b)
+// terms of the next 256 records (and whether they are still the run's) into
+// shared memory while thread 0 runs the dependent chain over the previous 256.
+__global__ void __launch_bounds__(kPtTPB)
+k_guide_apply_long(GuideGrid G, const uint32_t* __restrict__ keys, const float* __restrict__ vals, uint32_t n,
+                   const uint2* __restrict__ longRuns, const uint32_t* longCount)
+{
+    __shared__ __align__(16) float sA[2][kPtTPB];
+    __shared__ __align__(16) float sB[2][kPtTPB];
+    const uint32_t runs = *longCount;
+    for(uint32_t e = blockIdx.x; e < runs; e += gridDim.x)
+    {
+        const uint2 run = longRuns[e];
+        const uint32_t start = run.x, cell = run.y;
+        const float2 e0 = G.irr[cell];
+        const uint32_t n0 = __float_as_uint(e0.y);
+        float v = e0.x;
+        uint32_t total = 0;
+        // terms of chunk ch into buffer ch & 1; returns how many of its records are the run's
+        auto terms = [&](uint32_t ch) -> uint32_t {
+            const uint32_t q = start + ch * kPtTPB + threadIdx.x;
+            const bool in = q < n && (keys[q] >> 1) == cell;
+            float a = 1.0f, b = 0.0f;
+            if(in) ema_terms(n0, q - start, vals[q], a, b);
+            sA[ch & 1u][threadIdx.x] = a;
+            sB[ch & 1u][threadIdx.x] = b;
+            return (uint32_t)__syncthreads_count(in);       // sorted: a prefix of the chunk
+        };
+        uint32_t len = terms(0);
+        for(uint32_t ch = 0;; ch++)
         {
-            const uint32_t cl = (uint32_t)(__ffs(contMask) - 1);
-            const uint32_t hc = __shfl_sync(0xFFFFFFFFu, cell, cl);
-            for(uint32_t p = c * 32u + 32u;; p += 32u)
+            const uint32_t cur = ch & 1u;
+            // the next chunk's terms go into the other buffer meanwhile
+            uint32_t next = 0;
+            if(threadIdx.x == 0)
             {
-                const uint32_t q = p + lane;
-                const bool in = q < n && (keys[q] >> 1) == hc;
-                const float rr = in ? vals[idx[q]] : 0.0f;
-                // sorted: the cell's records in this window are a prefix of the lanes
-                const uint32_t len = (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, in));
-                const uint32_t c0 = __shfl_sync(0xFFFFFFFFu, cnt, cl);
-                float aa = 1.0f, bb = 0.0f;
-                if(in) ema_terms(c0, lane, rr, aa, bb);
-#pragma unroll
-                for(uint32_t k = 0; k < 32u; k++)
+                // four terms per shared-memory load, loads unrolled ahead of the chain
+                const float4* A4 = reinterpret_cast<const float4*>(sA[cur]);
+                const float4* B4 = reinterpret_cast<const float4*>(sB[cur]);
+                const uint32_t quads = len >> 2;
+#pragma unroll 8
+                for(uint32_t k = 0; k < quads; k++)
                 {
-                    const float ak = __shfl_sync(0xFFFFFFFFu, aa, k);
-                    const float bk = __shfl_sync(0xFFFFFFFFu, bb, k);
-                    if(lane == cl && k < len) v = __fadd_rn(__fmul_rn(v, ak), bk);
+                    const float4 a = A4[k], b = B4[k];
+                    v = __fadd_rn(__fmul_rn(v, a.x), b.x);
+                    v = __fadd_rn(__fmul_rn(v, a.y), b.y);
+                    v = __fadd_rn(__fmul_rn(v, a.z), b.z);
+                    v = __fadd_rn(__fmul_rn(v, a.w), b.w);
                 }
-                if(lane == cl) cnt = min(cnt + len, 128u);
-                if(len < 32u) break;
+                for(uint32_t k = quads << 2; k < len; k++) v = __fadd_rn(__fmul_rn(v, sA[cur][k]), sB[cur][k]);
             }
+            total += len;
+            if(len < (uint32_t)kPtTPB) break;           // block-uniform
+            next = terms(ch + 1u);
+            len = next;
         }
-        if(head) G.irr[cell] = make_float2(v, __uint_as_float(cnt));
+        if(threadIdx.x == 0) G.irr[cell] = make_float2(v, __uint_as_float(min(n0 + total, 128u)));
+        __syncthreads();
     }
 }
 
@@ -602,11 +679,24 @@ cudaError_t guide_shade(const PtLaunch& L, const PtPaths& P, const GuideGrid& G,
                         const PtSceneTables& T, const uint32_t* aliveList, const uint32_t* aliveCount,
                         uint32_t* nextList, uint32_t* nextCount, int smCount, cudaStream_t st)
 {
-    const unsigned grid = (unsigned)smCount * 8u;
+    static bool attr = false;
+    if(!attr)
+    {
+        cudaError_t e = cudaFuncSetAttribute(k_shade_guided<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kMixSmem);
+        if(e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_shade_guided<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kMixSmem);
+        if(e != cudaSuccess) return e;
+        attr = true;
+    }
+    const unsigned grid = (unsigned)smCount * 2u;
     if(L.spec.enabled)
-        k_shade_guided<true><<<grid, kPtTPB, 0, st>>>(L, P, G, Q, T, aliveList, aliveCount, nextList, nextCount);
+        k_shade_guided<true><<<grid, kPtTPB, kMixSmem, st>>>(L, P, G, Q, T, aliveList, aliveCount, nextList,
+                                                             nextCount);
     else
-        k_shade_guided<false><<<grid, kPtTPB, 0, st>>>(L, P, G, Q, T, aliveList, aliveCount, nextList, nextCount);
+        k_shade_guided<false><<<grid, kPtTPB, kMixSmem, st>>>(L, P, G, Q, T, aliveList, aliveCount, nextList,
+                                                              nextCount);
     return cudaGetLastError();
 }
 
@@ -620,8 +710,10 @@ cudaError_t guide_apply(const GuideGrid& G, const GuidePaths& Q, int smCount, cu
 {
     const uint32_t n = 2u * Q.slots;
     const uint32_t passes = (Q.keyBits + 7u) / 8u;
+    // the records' values ride along as the sort's payload, so the sorted
+    // values are read in order
     const uint32_t* kIn = Q.recKey;
-    const uint32_t* iIn = nullptr;
+    const uint32_t* iIn = reinterpret_cast<const uint32_t*>(Q.recVal);
     for(uint32_t p = 0; p < passes; p++)
     {
         uint32_t* kOut = (p & 1u) ? Q.sortKeysB : Q.sortKeysA;
@@ -636,8 +728,12 @@ cudaError_t guide_apply(const GuideGrid& G, const GuidePaths& Q, int smCount, cu
         kIn = kOut;
         iIn = iOut;
     }
-    k_guide_apply<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(G, kIn, iIn, Q.recVal, n);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaMemsetAsync(Q.longCount, 0, sizeof(uint32_t), st);
+    if(e != cudaSuccess) return e;
+    const float* vals = reinterpret_cast<const float*>(iIn);
+    k_guide_apply<<<(unsigned)smCount * 4u, kPtTPB, 0, st>>>(G, kIn, vals, n, Q.longRuns, Q.longCount);
+    k_guide_apply_long<<<(unsigned)smCount * 2u, kPtTPB, 0, st>>>(G, kIn, vals, n, Q.longRuns, Q.longCount);
+    e = cudaGetLastError();
     if(e != cudaSuccess) return e;
     return cudaMemsetAsync(Q.recKey, 0xFF, sizeof(uint32_t) * n, st);
 }

@@ -76,6 +76,8 @@ struct GuidePaths
     uint32_t* sortKeysB;
     uint32_t* sortIdxB;
     uint32_t* sortHist;
+    uint2*    longRuns;             // runs of one cell longer than 32 records: (first position, cell)
+    uint32_t* longCount;
     uint32_t  slots;
     uint32_t  keyBits;              // bits of a record key: log2(table) + 2
 };

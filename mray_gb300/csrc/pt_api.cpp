@@ -1054,8 +1054,9 @@ mrg_status guide_paths(mrg_ctx* c, uint32_t slots)
         c->guideCap = 0;
         Q = mrg::GuidePaths{};
         const size_t n = slots;
-        const size_t sizes[15] = { n * 4, n * 4, n * 4, n * 4, n * 8, n * 4, n * 16, n * 8, n * 8, n * 8,
-                                   n * 8, n * 8, n * 8, n * 8, 4 * mrg::multisplit_hist_words(2u * slots, 8) };
+        const size_t sizes[17] = { n * 4, n * 4, n * 4, n * 4, n * 8, n * 4, n * 16, n * 8, n * 8, n * 8,
+                                   n * 8, n * 8, n * 8, n * 8, 4 * mrg::multisplit_hist_words(2u * slots, 8),
+                                   8 * ((2 * n) / 32 + 1), 4 };
         size_t need = 0;
         for(size_t sz : sizes) need += (sz + 255) & ~size_t(255);
         char* base = nullptr;
@@ -1079,6 +1080,8 @@ mrg_status guide_paths(mrg_ctx* c, uint32_t slots)
         Q.sortKeysB = reinterpret_cast<uint32_t*>(take());
         Q.sortIdxB = reinterpret_cast<uint32_t*>(take());
         Q.sortHist = reinterpret_cast<uint32_t*>(take());
+        Q.longRuns = reinterpret_cast<uint2*>(take());
+        Q.longCount = reinterpret_cast<uint32_t*>(take());
         c->guideCap = slots;
         c->guideBkValid = false;
         // every bounce leaves the records empty again (guide_apply)
