@@ -329,6 +329,28 @@ mrg_status mrg_pt_add_texture(mrg_ctx* ctx, uint32_t width, uint32_t height, uin
 /* The instance's albedo comes from the texture at the hit's interpolated uv
  * (its mesh needs uvs); texture_id = 0xFFFFFFFF returns to the constant. */
 mrg_status mrg_pt_set_albedo_texture(mrg_ctx* ctx, uint32_t instance_id, uint32_t texture_id);
+/* A mip chain for a texture (TextureMemory::GenerateMipmaps with the tracer's
+ * mipGenFilter, Source/Tracer/TextureMemory.cpp:491-525,
+ * TextureFilter.cu:124-192, 1006-1100): every level down to 1 x 1, each texel
+ * the normalised sum of 8 x 8 stratified samples of the level above weighted
+ * by a Gaussian filter of filter_radius pixels (MRay's default 2), in the
+ * texture's own format.  Made on the device at the next render (from the
+ * texels of that moment, for a borrowed texture); filter_radius = 0 drops the
+ * chain.  Reads of a texture with a chain take their level from the path's ray
+ * cone (RT Gems I ch. 20; the camera's cone, widened along the path and
+ * refracted by smooth dielectrics, projected on the hit triangle for uv
+ * gradients) and blend the two nearest levels (TextureViewCPU's trilinear
+ * read, the gradients in texels).  mrg_pt_adjoint's texture parameter must have
+ * no chain. */
+mrg_status mrg_pt_generate_mips(mrg_ctx* ctx, uint32_t texture_id, float filter_radius);
+/* Texels of one mip level of a texture (TracerI::PushTextureData with
+ * mipLevel > 0, Source/Core/TracerI.h:243): level in [1, bits(max(w, h))),
+ * max(w >> level, 1) x max(h >> level, 1) texels in the texture's format,
+ * copied.  A given level is kept when the chain is generated (MRay's
+ * validMips, TextureFilter.cu:160-164) and the levels below it are filtered
+ * from it; without a generation filter the chain ends at the last given
+ * level, and every level up to it must be given (else the next render fails). */
+mrg_status mrg_pt_set_texture_mip(mrg_ctx* ctx, uint32_t texture_id, uint32_t level, const void* texels);
 
 /* ---- Path-replay adjoint (no reference counterpart) ---------------------- */
 /* Gradient of  sum_pixels <d_image_adjoint[p].rgb, I[p].rgb>  with respect to

@@ -51,7 +51,9 @@ typedef struct mrg_tracer_params
     uint32_t samplerType;        /* MRG_TRACER_SAMPLER_* */
     float    filmFilterRadius;   /* filmFilter: Gaussian of this radius; 0 = MRay's default 1 */
     uint32_t triangleTest;       /* MRG_TRI_* (MRay: Moller-Trumbore) */
-    uint32_t reserved[4];
+    uint32_t genMips;            /* genMips: every texture gets its full mip chain */
+    float    mipGenFilterRadius; /* mipGenFilter: Gaussian of this radius; 0 = MRay's default 2 */
+    uint32_t reserved[2];
 } mrg_tracer_params;
 
 /* ConstructTracer / DestroyTracer (Source/TracerDLL/EntryPoint.h:12-18). */

@@ -186,6 +186,7 @@ mrg_status mrg_destroy(mrg_ctx* c)
     cudaFree(c->dPtSurfaces); cudaFree(c->dPtLights); cudaFree(c->dPtTris); cudaFree(c->ptPathMem);
     cudaFree(c->dPtEnv);
     cudaFree(c->dPtTexTable); cudaFree(c->dPtTexData); cudaFree(c->dPtUvs); cudaFree(c->dPtRadTotal);
+    cudaFree(c->dPtMipData);
     cudaFree(c->dPtSpec);
     cudaFree(c->dPartScratch);
     cudaFree(c->dPtCacheBuf);

@@ -318,7 +318,9 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                 onb(nrm, tng, btg);
                 const float3 wo = make_float3(-dir.x, -dir.y, -dir.z);
                 const float3 V = make_float3(dot3(wo, tng), dot3(wo, btg), dot3(wo, nrm));
-                const float3 a3 = surface_albedo(T, sf, gprim, mh);
+                const float2 cn = P.cone[i];
+                const Cone cone = cone_advance(Cone{ cn.x, cn.y }, r1.w);
+                const float3 a3 = surface_albedo_cone(T, sf, gprim, mh, pos, nrm, dir, cone);
                 const Chan alb = albedo_of<SPEC>(L.spec, a3.x, a3.y, a3.z, waves);
                 const float specv = specularity<NC>(sf, alb);
                 const bool isSpec = specv >= kSpecularThreshold;
@@ -458,6 +460,8 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                     const float3 no = nudge(orgOut, nn);
                     P.rays[2 * (size_t)i] = make_float4(no.x, no.y, no.z, 1.0e-4f);
                     P.rays[2 * (size_t)i + 1] = make_float4(wdir.x, wdir.y, wdir.z, 3.402823466e+38f);
+                    const Cone co = cone_after_scatter(sf, mt, backSide, cone, wo, nrm, wdir);
+                    P.cone[i] = make_float2(co.aperture, co.width);
                     P.hits[i].x = kMissMark;
                     P.thr[i] = f4(pthr);
                     P.prevPdf[i] = pdfPath;

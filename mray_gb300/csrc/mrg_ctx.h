@@ -88,10 +88,13 @@ struct mrg_ctx
         uint32_t             width = 0, height = 0, format = 0;   // 0 RGBA8 unorm, 1 RGBA f32
         std::vector<uint8_t> host;             // owned copy, or empty when borrowed
         const void*          borrowed = nullptr;
+        float                mipRadius = 0.0f;  // > 0: a mip chain made with this Gaussian radius
+        std::vector<std::vector<uint8_t>> given;  // mip level -> texels set by the caller (level 0 unused)
     };
     std::vector<PtTextureDesc> ptTextures;
     void*     dPtTexTable = nullptr;           // PtTexture per texture
     void*     dPtTexData = nullptr;            // owned texel copies
+    void*     dPtMipData = nullptr;            // mip levels 1.. of the textures that have a chain
     void*     dPtUvs = nullptr;                // 2 float4 per primitive
     void*     dPtRadTotal = nullptr;           // adjoint: primal radiance per path slot
     uint32_t  ptRadTotalCap = 0;

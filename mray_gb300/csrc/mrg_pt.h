@@ -26,13 +26,16 @@ struct __align__(16) PtSurface
     uint4  tex;         // x: albedo texture index + 1 (0: constant albedo)
 };
 
-// Albedo texture: RGBA texels, bilinear, wrap addressed, one level.
+// Albedo texture: RGBA texels, bilinear, wrap addressed; levels 1.. of its
+// mip chain (mipCount > 1) follow one another in `mips`, each max(w >> m, 1) x
+// max(h >> m, 1) texels of the same format (Graphics::TextureMipPixelStart).
 struct __align__(16) PtTexture
 {
     const void* texels;
     uint32_t    width, height;
     uint32_t    format;         // 0 RGBA8 unorm, 1 RGBA f32
-    uint32_t    pad;
+    uint32_t    mipCount;       // 1: level 0 only
+    const void* mips;
 };
 
 // One light per emitting triangle (MRay's primitive-backed lights,
@@ -131,6 +134,7 @@ struct PtLaunch
     uint32_t seed;
     uint32_t nLights;        // triangle lights; the skysphere, if enabled, follows them
     float    filterSigma;
+    float    coneAperture;   // camera rays' cone aperture: 2 tan(fovY / 2) / height
     uint32_t sampler;        // 0: counter-based independent numbers, 1: ZSobol, 2: ZSobol (Owen order), 3: PCG32
     uint32_t zsMaxSpp;       // ZSobol initialMaxSampleCount
     uint32_t zsResBits;      // ZSobol resMaxBits
@@ -149,6 +153,7 @@ struct PtPaths
     float4*   rays;          // 2 per slot (RayGMem)
     uint4*    hits;          // HitKeyPack per slot
     float2*   meta;          // MetaHit per slot
+    float2*   cone;          // ray cone of the path's current ray: aperture, width
     float4*   thr;           // throughput (RGB in xyz, or 4 wavelengths)
     float4*   rad;           // radiance (RGB in xyz, or 4 wavelengths)
     float*    prevPdf;       // pdf of the last BxDF sample (MIS)
@@ -208,5 +213,39 @@ cudaError_t pt_resolve(const PtLaunch& L, const PtPaths& P, const PtLight* light
 // out[i] += acc[i] (f32 from the FP64 emission-gradient sums), n entries.
 cudaError_t pt_add_emission_grad(const double* acc, float* out, uint32_t n, cudaStream_t st);
 cudaError_t pt_film(const PtLaunch& L, const PtPaths& P, float4* image, cudaStream_t st);
+
+// Texels of mip levels 1 .. TextureMipCount - 1 of a w x h texture.
+// Graphics::TextureMipCount: levels of a full chain, bits of max(w, h)
+inline uint32_t mip_level_count(uint32_t w, uint32_t h)
+{
+    uint32_t m = w > h ? w : h, n = 0;
+    for(; m; m >>= 1) n++;
+    return n;
+}
+// Texels of levels 1 .. levels - 1 (all of a full chain by default); the
+// offset of level m in a chain is mip_chain_texels(w, h, m).
+inline size_t mip_chain_texels(uint32_t w, uint32_t h, uint32_t levels = 0xFFFFFFFFu)
+{
+    size_t n = 0;
+    for(uint32_t m = 1; m < levels && ((w >> (m - 1)) > 1u || (h >> (m - 1)) > 1u); m++)
+        n += (size_t)((w >> m) ? (w >> m) : 1u) * ((h >> m) ? (h >> m) : 1u);
+    return n;
+}
+// The 8 per-axis sample offsets (pixels) of KCGenerateMipmaps' stratified
+// accumulation and the Gaussian filter's 1D weights at them (GaussianFilter::
+// Evaluate is their product), made on the host.
+struct MipTaps
+{
+    float off[8];
+    float g[8];
+};
+// Levels 1.. of the texture's mip chain into `mips` (KCGenerateMipmaps,
+// Source/Tracer/TextureFilter.cu:124-192); *count = the chain's level count.
+// Synchronous.
+// Levels 1 .. levels - 1 of a chain, each filtered from its parent; the
+// levels whose bit is set in validMask are already in place and kept
+// (KCGenerateMipmaps' validMips).  Synchronous.
+cudaError_t generate_mips(const void* texels, void* mips, uint32_t w, uint32_t h, uint32_t format, const MipTaps& taps,
+                          uint32_t levels, uint32_t validMask);
 
 } // namespace mrg

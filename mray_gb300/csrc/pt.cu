@@ -21,6 +21,8 @@
 // / log, which differ between CUDA and the host C library by a few ulps.
 #include "pt_device.cuh"
 
+#include <algorithm>
+
 namespace mrg {
 
 namespace {
@@ -50,6 +52,7 @@ k_raygen(PtLaunch L, PtPaths P, uint32_t* aliveList, uint32_t* aliveCount)
         P.rays[2 * (size_t)i + 1] = make_float4(d.x, d.y, d.z, L.cam.farT);
         P.hits[i].x = kMissMark;
         P.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+        P.cone[i] = make_float2(L.coneAperture, 0.0f);     // CameraPinhole: RT Gems I ch. 20 eq. 30
         P.rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         P.prevPdf[i] = 0.0f;
         P.state[i] = 0u;
@@ -180,7 +183,9 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                     onb(nrm, tng, btg);
                     const float3 wo = make_float3(-dir.x, -dir.y, -dir.z);
                     const float3 V = make_float3(dot3(wo, tng), dot3(wo, btg), dot3(wo, nrm));
-                    const float3 a3 = surface_albedo(T, sf, gprim, mh);
+                    const float2 cn = P.cone[i];
+                    const Cone cone = cone_advance(Cone{ cn.x, cn.y }, r1.w);
+                    const float3 a3 = surface_albedo_cone(T, sf, gprim, mh, pos, nrm, dir, cone);
                     const Chan alb = albedo_of<SPEC>(L.spec, a3.x, a3.y, a3.z, waves);
                     if(ADJ && L.adj.texIndex != 0u && sf.tex.x == L.adj.texIndex && sf.info.w == kMatLambert &&
                        T.uvs != nullptr && gprim < nTris)
@@ -282,6 +287,8 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                         const float3 no = nudge(pre, nn);
                         P.rays[2 * (size_t)i] = make_float4(no.x, no.y, no.z, 1.0e-4f);
                         P.rays[2 * (size_t)i + 1] = make_float4(wi.x, wi.y, wi.z, 3.402823466e+38f);
+                        const Cone co = cone_after_scatter(sf, mt, backSide, cone, wo, nrm, wi);
+                        P.cone[i] = make_float2(co.aperture, co.width);
                         P.hits[i].x = kMissMark;
                         P.thr[i] = f4(thr);
                         P.prevPdf[i] = bpdf;
@@ -485,7 +492,90 @@ inline unsigned grid_for(uint32_t n, int smCount)
     return (unsigned)(want < cap ? (want ? want : 1u) : cap);
 }
 
+// One level of a mip chain from the one above it (KCGenerateMipmaps with
+// FilterPixel in ACCUMULATE mode, TextureFilter.cu:62-110, 124-192): per
+// texel the 8 x 8 weighted samples of the parent, each the parent texel
+// nearest to ConvertPixelIndices of the sample point (GraphicsFunctions.h:
+// 527-538), summed in row order and divided by the weight sum.  Texels are
+// read as stored (UNORM8 as 0..255, GenericRead) and written back rounded and
+// clamped (GenericWrite).
+__global__ void __launch_bounds__(kPtTPB)
+k_gen_mip(const void* __restrict__ src, void* __restrict__ dst, uint32_t format, uint32_t pw, uint32_t ph, uint32_t w,
+          uint32_t h, MipTaps taps)
+{
+    const float rx = __fdiv_rn((float)pw, (float)w), ry = __fdiv_rn((float)ph, (float)h);
+    const uint32_t n = w * h;
+    for(uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x)
+    {
+        const uint32_t x = idx % w, y = idx / w;
+        float acc[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+        float wsum = 0.0f;
+        for(int sy = 0; sy < 8; sy++)
+        {
+            float py = sub(mul(add(add((float)y, taps.off[sy]), 0.5f), ry), 0.5f);
+            py = fminf(fmaxf(0.0f, py), (float)(ph - 1u));
+            const uint32_t iy = (uint32_t)lroundf(py);
+            for(int sx = 0; sx < 8; sx++)
+            {
+                float px = sub(mul(add(add((float)x, taps.off[sx]), 0.5f), rx), 0.5f);
+                px = fminf(fmaxf(0.0f, px), (float)(pw - 1u));
+                const uint32_t ix = (uint32_t)lroundf(px);
+                const float wgt = mul(taps.g[sx], taps.g[sy]);
+                const size_t t = (size_t)iy * pw + ix;
+                float v[4];
+                if(format == 0u)
+                {
+                    const uchar4 c = reinterpret_cast<const uchar4*>(src)[t];
+                    v[0] = (float)c.x; v[1] = (float)c.y; v[2] = (float)c.z; v[3] = (float)c.w;
+                }
+                else
+                {
+                    const float4 c = reinterpret_cast<const float4*>(src)[t];
+                    v[0] = c.x; v[1] = c.y; v[2] = c.z; v[3] = c.w;
+                }
+#pragma unroll
+                for(int k = 0; k < 4; k++) acc[k] = add(acc[k], mul(wgt, v[k]));
+                wsum = add(wsum, wgt);
+            }
+        }
+        float o[4];
+#pragma unroll
+        for(int k = 0; k < 4; k++) o[k] = __fdiv_rn(acc[k], wsum);
+        if(format == 0u)
+        {
+            uchar4 c;
+            c.x = (unsigned char)fminf(fmaxf(roundf(o[0]), 0.0f), 255.0f);
+            c.y = (unsigned char)fminf(fmaxf(roundf(o[1]), 0.0f), 255.0f);
+            c.z = (unsigned char)fminf(fmaxf(roundf(o[2]), 0.0f), 255.0f);
+            c.w = (unsigned char)fminf(fmaxf(roundf(o[3]), 0.0f), 255.0f);
+            reinterpret_cast<uchar4*>(dst)[idx] = c;
+        }
+        else reinterpret_cast<float4*>(dst)[idx] = make_float4(o[0], o[1], o[2], o[3]);
+    }
+}
+
 } // namespace
+
+cudaError_t generate_mips(const void* texels, void* mips, uint32_t w, uint32_t h, uint32_t format, const MipTaps& taps,
+                          uint32_t levels, uint32_t validMask)
+{
+    const size_t bpp = (format == 0u) ? 4u : 16u;
+    char* chain = static_cast<char*>(mips);
+    for(uint32_t m = 1; m < levels; m++)
+    {
+        if(validMask & (1u << m)) continue;
+        const uint32_t pw = (w >> (m - 1)) ? (w >> (m - 1)) : 1u, ph = (h >> (m - 1)) ? (h >> (m - 1)) : 1u;
+        const uint32_t cw = (w >> m) ? (w >> m) : 1u, ch = (h >> m) ? (h >> m) : 1u;
+        const uint32_t n = cw * ch;
+        const void* src = (m == 1) ? texels : chain + mip_chain_texels(w, h, m - 1) * bpp;
+        void* out = chain + mip_chain_texels(w, h, m) * bpp;
+        k_gen_mip<<<std::min<uint32_t>((n + kPtTPB - 1) / kPtTPB, 65535u), kPtTPB>>>(src, out, format, pw, ph, cw, ch,
+                                                                                    taps);
+        cudaError_t e = cudaGetLastError();
+        if(e != cudaSuccess) return e;
+    }
+    return cudaDeviceSynchronize();
+}
 
 cudaError_t pt_raygen(const PtLaunch& L, const PtPaths& P, uint32_t* aliveList, uint32_t* aliveCount,
                       int smCount, cudaStream_t st)

@@ -240,6 +240,27 @@ mrg_status pt_zsobol(mrg_ctx* c, const mrg_pt_params& p, mrg::PtLaunch& L, const
     return MRG_OK;
 }
 
+// KCGenerateMipmaps' samples (TextureFilter.cu:62-110, GenerateMipsGeneric
+// :1006-1100): 8 x 8 per texel, xi = (k + 0.5) / 8 per axis, in ACCUMULATE mode
+// at offset xi 2 r - r pixels, weighted by the Gaussian filter of radius r
+// (sigma = 0.285714 r; Math::Gaussian, Core/Math.h:1032-1042).
+mrg::MipTaps mip_taps(float r)
+{
+    mrg::MipTaps t;
+    const float sigma = r * 0.285714f;
+    const float invSqrt2Pi = (1.0f / 1.4142135623730950488f) * (1.0f / 1.772453850905516027298f);
+    for(int k = 0; k < 8; k++)
+    {
+        const float d = 1.0f / 8.0f;
+        const float xi = d * 0.5f + d * (float)k;
+        t.off[k] = xi * 2.0f * r - r;
+        const float sInv = 1.0f / sigma;
+        const float pw = (t.off[k] - 0.0f) * sInv;
+        t.g[k] = (invSqrt2Pi * sInv) * std::exp(-0.5f * pw * pw);
+    }
+    return t;
+}
+
 // Uploads surfaces, lights and the primitive-indexed triangle table.
 mrg_status pt_prepare(mrg_ctx* c)
 {
@@ -337,6 +358,7 @@ mrg_status pt_prepare(mrg_ctx* c)
     }
     cudaFree(c->dPtTexTable); c->dPtTexTable = nullptr;
     cudaFree(c->dPtTexData); c->dPtTexData = nullptr;
+    cudaFree(c->dPtMipData); c->dPtMipData = nullptr;
     if(!c->ptTextures.empty())
     {
         size_t owned = 0;
@@ -347,7 +369,8 @@ mrg_status pt_prepare(mrg_ctx* c)
         for(size_t k = 0; k < c->ptTextures.size(); k++)
         {
             const auto& t = c->ptTextures[k];
-            table[k].width = t.width; table[k].height = t.height; table[k].format = t.format; table[k].pad = 0;
+            table[k].width = t.width; table[k].height = t.height; table[k].format = t.format;
+            table[k].mipCount = 1; table[k].mips = nullptr;
             if(t.borrowed) table[k].texels = t.borrowed;
             else
             {
@@ -355,6 +378,57 @@ mrg_status pt_prepare(mrg_ctx* c)
                 PT_TRY(cudaMemcpy(dst, t.host.data(), t.host.size(), cudaMemcpyHostToDevice), "mrg_pt: textures");
                 table[k].texels = dst;
                 off += (t.host.size() + 255) & ~size_t(255);
+            }
+        }
+        // mip chains (TextureMemory::GenerateMipmaps): levels 1.. of every
+        // texture that has a generation filter or given levels; given levels
+        // are copied in place and kept, the others are filtered on the device
+        // from their parent
+        std::vector<uint32_t> levels(c->ptTextures.size(), 1u);
+        size_t mipBytes = 0;
+        for(size_t k = 0; k < c->ptTextures.size(); k++)
+        {
+            const auto& t = c->ptTextures[k];
+            uint32_t last = 0;
+            for(uint32_t m = 1; m < t.given.size(); m++)
+                if(!t.given[m].empty()) last = m;
+            if(t.mipRadius > 0.0f) levels[k] = mrg::mip_level_count(t.width, t.height);
+            else if(last)
+            {
+                for(uint32_t m = 1; m < last; m++)
+                    if(t.given[m].empty())
+                        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt: texture " + std::to_string(k) + " mip " +
+                                              std::to_string(m) + " has no data and no generation filter");
+                levels[k] = last + 1u;
+            }
+            if(levels[k] > 1u)
+                mipBytes += (mrg::mip_chain_texels(t.width, t.height, levels[k]) * (t.format == MRG_TEX_RGBA8 ? 4u : 16u) +
+                             255) & ~size_t(255);
+        }
+        if(mipBytes)
+        {
+            PT_TRY(cudaMalloc(&c->dPtMipData, mipBytes), "mrg_pt: mips");
+            size_t moff = 0;
+            for(size_t k = 0; k < c->ptTextures.size(); k++)
+            {
+                const auto& t = c->ptTextures[k];
+                if(levels[k] <= 1u) continue;
+                const size_t bpp = t.format == MRG_TEX_RGBA8 ? 4u : 16u;
+                char* dst = static_cast<char*>(c->dPtMipData) + moff;
+                uint32_t valid = 0;
+                for(uint32_t m = 1; m < levels[k] && m < t.given.size(); m++)
+                    if(!t.given[m].empty())
+                    {
+                        PT_TRY(cudaMemcpy(dst + mrg::mip_chain_texels(t.width, t.height, m) * bpp, t.given[m].data(),
+                                          t.given[m].size(), cudaMemcpyHostToDevice), "mrg_pt: mips");
+                        valid |= 1u << m;
+                    }
+                if(t.mipRadius > 0.0f)
+                    PT_TRY(mrg::generate_mips(table[k].texels, dst, t.width, t.height, t.format, mip_taps(t.mipRadius),
+                                              levels[k], valid), "mrg_pt: mips");
+                table[k].mips = dst;
+                table[k].mipCount = levels[k];
+                moff += (mrg::mip_chain_texels(t.width, t.height, levels[k]) * bpp + 255) & ~size_t(255);
             }
         }
         PT_TRY(cudaMalloc(&c->dPtTexTable, sizeof(mrg::PtTexture) * table.size()), "mrg_pt: textures");
@@ -381,10 +455,10 @@ mrg_status pt_paths_into(mrg::PtPaths& P, void*& mem, uint32_t slots)
     const size_t n = slots;
     const size_t words = (n + 31) / 32;
     // one allocation, every array 256-byte aligned
-    const size_t sizes[21] = { n * 32, n * 16, n * 8, n * 16, n * 16, n * 4, n * 32, n * 16,
+    const size_t sizes[22] = { n * 32, n * 16, n * 8, n * 16, n * 16, n * 4, n * 32, n * 16,
                                words * 4, n * 4, n * 4, n * 4, 64, n * 4, n * 4, n * 4,
                                4 * mrg::multisplit_hist_words(slots, mrg::kPtWorkKeyBits),
-                               n * 4, n * 16, n * 16, n * 4 };
+                               n * 4, n * 16, n * 16, n * 4, n * 8 };
     size_t need = 0;
     for(size_t sz : sizes) need += (sz + 255) & ~size_t(255);
     char* base = nullptr;
@@ -414,6 +488,7 @@ mrg_status pt_paths_into(mrg::PtPaths& P, void*& mem, uint32_t slots)
     P.waves = reinterpret_cast<float4*>(take());
     P.wavePdf = reinterpret_cast<float4*>(take());
     P.shadowLight = reinterpret_cast<uint32_t*>(take());
+    P.cone = reinterpret_cast<float2*>(take());
     P.capacity = slots;
     return MRG_OK;
 }
@@ -561,6 +636,34 @@ mrg_status mrg_pt_add_texture(mrg_ctx* c, uint32_t w, uint32_t h, uint32_t forma
     return MRG_OK;
 }
 
+mrg_status mrg_pt_generate_mips(mrg_ctx* c, uint32_t texId, float filterRadius)
+{
+    if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_generate_mips: null pointer");
+    if(texId >= c->ptTextures.size()) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_generate_mips: unknown texture");
+    if(!(filterRadius >= 0.0f) || filterRadius > 64.0f)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_generate_mips: filter radius in [0, 64]");
+    c->ptTextures[texId].mipRadius = filterRadius;
+    c->ptDirty = true;
+    return MRG_OK;
+}
+
+mrg_status mrg_pt_set_texture_mip(mrg_ctx* c, uint32_t texId, uint32_t level, const void* texels)
+{
+    if(!c || !texels) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_texture_mip: null pointer");
+    if(texId >= c->ptTextures.size()) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_texture_mip: unknown texture");
+    auto& t = c->ptTextures[texId];
+    const uint32_t full = mrg::mip_level_count(t.width, t.height);
+    if(level == 0 || level >= full)
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_texture_mip: level in [1, " + std::to_string(full) + ")");
+    const size_t bytes = (size_t)std::max(t.width >> level, 1u) * std::max(t.height >> level, 1u) *
+                         (t.format == MRG_TEX_RGBA8 ? 4u : 16u);
+    if(t.given.size() < full) t.given.resize(full);
+    const uint8_t* b = static_cast<const uint8_t*>(texels);
+    t.given[level].assign(b, b + bytes);
+    c->ptDirty = true;
+    return MRG_OK;
+}
+
 mrg_status mrg_pt_set_albedo_texture(mrg_ctx* c, uint32_t inst, uint32_t texId)
 {
     if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_albedo_texture: null context");
@@ -631,6 +734,8 @@ mrg_status pt_setup(mrg_ctx* c, const mrg_pt_params* p, PtRun& R, const char* wh
     L.env = c->ptEnv;
     L.spec = c->ptSpec;
     L.filterSigma = p->filterRadius * 0.285714f;
+    // CameraPinhole's ray cone (CamerasDefault.hpp:80-86): 2 tan(fovY / 2) / image height
+    L.coneAperture = 2.0f * std::tan(p->fov[1] * 0.5f) / (float)p->height;
     if(p->sampler > MRG_PT_SAMPLER_PCG32) return mrg::set_error(MRG_ERR_INVALID_ARG, w + ": unknown sampler");
     // a PCG32 stream holds 2^32 numbers: 16 per bounce, maxDepth + 1 bounces per sample
     if(p->sampler == MRG_PT_SAMPLER_PCG32 &&
@@ -898,6 +1003,10 @@ mrg_status mrg_pt_adjoint(mrg_ctx* c, const mrg_pt_params* p, uint32_t texId, co
         return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: no parameter (no texture and no emission gradient)");
     if(texParam && (texId >= c->ptTextures.size() || c->ptTextures[texId].format != MRG_TEX_RGBA32F))
         return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: the parameter must be an f32 texture");
+    if(texParam && (c->ptTextures[texId].mipRadius > 0.0f ||
+                    std::any_of(c->ptTextures[texId].given.begin(), c->ptTextures[texId].given.end(),
+                                [](const std::vector<uint8_t>& v) { return !v.empty(); })))
+        return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: the parameter texture must have no mip chain");
     if(c->ptSpec.enabled) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_adjoint: RGB rendering only");
     for(uint32_t i = 0; i < c->insts.size() && i < c->ptDesc.size(); i++)
         if(texParam && c->ptDesc[i].kind == 1 && c->ptDesc[i].texture == texId + 1 &&

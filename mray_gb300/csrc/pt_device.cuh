@@ -780,12 +780,287 @@ __device__ __forceinline__ float2 surface_uv(const PtSceneTables& T, uint32_t gp
                        add(add(mul(q0.y, a), mul(q0.w, b)), mul(q1.y, c)));
 }
 
+// ---------------------------------------------------------------------------
+// Mip-mapped albedo reads and ray cones.
+//   levels      Graphics::TextureMipSize / TextureMipPixelStart
+//               (Source/Core/GraphicsFunctions.h:474-525)
+//   LOD read    TextureViewCPU::operator()(uv, dpdx, dpdy) and (uv, mipLevel)
+//               (Source/Device/CPU/TextureViewCPU.h:405-470), the gradients
+//               taken in texels as a GPU's gradient read takes them
+//   cones       RayCone::Advance / Project, RayConeSurface::ConeAfterScatter
+//               (Source/Tracer/TracerTypes.h:44-66, 323-380); the hit's texture
+//               gradients (Triangle::GenerateSurface, PrimitiveDefaultTriangle.hpp:
+//               491-569); RefractMaterial::RefractRayCone (MaterialsDefault.hpp:
+//               353-462)
+// ---------------------------------------------------------------------------
+constexpr float kConeEps = 1.0e-5f;          // MathConstants::Epsilon
+
+__device__ __forceinline__ uint32_t mip_dim(uint32_t r, uint32_t m) { return max(r >> m, 1u); }
+
+__device__ __forceinline__ float3 texel_rgb_at(uint32_t format, const void* base, size_t i)
+{
+    if(format == 0u)
+    {
+        const uchar4 c = __ldg(reinterpret_cast<const uchar4*>(base) + i);
+        const float d = 1.0f / 255.0f;
+        return make_float3(add(0.0f, mul((float)c.x, d)), add(0.0f, mul((float)c.y, d)), add(0.0f, mul((float)c.z, d)));
+    }
+    const float4 c = __ldg(reinterpret_cast<const float4*>(base) + i);
+    return make_float3(c.x, c.y, c.z);
+}
+
+// Bilinear read of level m (tex_read's arithmetic at the level's size).
+__device__ float3 tex_read_level(const PtTexture& t, uint32_t m, float u, float v)
+{
+    const uint32_t w = mip_dim(t.width, m), h = mip_dim(t.height, m);
+    const void* base = t.texels;
+    if(m > 0u)
+    {
+        size_t start = 0;
+        for(uint32_t k = 1; k < m; k++) start += (size_t)mip_dim(t.width, k) * mip_dim(t.height, k);
+        base = static_cast<const char*>(t.mips) + start * (t.format == 0u ? 4u : 16u);
+    }
+    const float tx = sub(mul(u, (float)w), 0.5f), ty = sub(mul(v, (float)h), 0.5f);
+    float bx, by;
+    float fx = modff(tx, &bx), fy = modff(ty, &by);
+    int32_t sx = (int32_t)bx, sy = (int32_t)by;
+    if(fx < 0.0f) { sx -= 1; fx = fabsf(fx); }
+    if(fy < 0.0f) { sy -= 1; fy = fabsf(fy); }
+    const int32_t x0 = wrap_index(sx, (int32_t)w), x1 = wrap_index(sx + 1, (int32_t)w);
+    const int32_t y0 = wrap_index(sy, (int32_t)h), y1 = wrap_index(sy + 1, (int32_t)h);
+    const float3 p00 = texel_rgb_at(t.format, base, (size_t)y0 * w + x0);
+    const float3 p10 = texel_rgb_at(t.format, base, (size_t)y0 * w + x1);
+    const float3 p01 = texel_rgb_at(t.format, base, (size_t)y1 * w + x0);
+    const float3 p11 = texel_rgb_at(t.format, base, (size_t)y1 * w + x1);
+    const float gx = sub(1.0f, fx), gy = sub(1.0f, fy);
+    const float ax = add(mul(p00.x, gx), mul(p10.x, fx)), bxx = add(mul(p01.x, gx), mul(p11.x, fx));
+    const float ay = add(mul(p00.y, gx), mul(p10.y, fx)), byy = add(mul(p01.y, gx), mul(p11.y, fx));
+    const float az = add(mul(p00.z, gx), mul(p10.z, fx)), bzz = add(mul(p01.z, gx), mul(p11.z, fx));
+    return make_float3(add(mul(ax, gy), mul(bxx, fy)), add(mul(ay, gy), mul(byy, fy)),
+                       add(mul(az, gy), mul(bzz, fy)));
+}
+
+// Level from the uv gradients (in texels), clamped to the chain, and the
+// linear blend of the two nearest levels (Math::Lerp).
+__device__ float3 tex_read_grad(const PtTexture& t, float u, float v, float2 dx, float2 dy)
+{
+    const float sx = (float)t.width, sy = (float)t.height;
+    const float gxx = mul(dx.x, sx), gxy = mul(dx.y, sy), gyx = mul(dy.x, sx), gyy = mul(dy.y, sy);
+    const float maxLenSqr = fmaxf(len2_2(gxx, gxy), len2_2(gyx, gyy));
+    float level = mul(0.5f, log2f(maxLenSqr));
+    level = fminf(fmaxf(0.0f, level), (float)(t.mipCount - 1u));
+    float m0f;
+    const float frac = modff(level, &m0f);
+    const uint32_t m0 = (uint32_t)m0f, m1 = min(m0 + 1u, t.mipCount - 1u);
+    const float3 p0 = tex_read_level(t, m0, u, v);
+    if(m0 == m1) return p0;
+    const float3 p1 = tex_read_level(t, m1, u, v);
+    const float g = sub(1.0f, frac);
+    return make_float3(add(mul(p0.x, g), mul(p1.x, frac)), add(mul(p0.y, g), mul(p1.y, frac)),
+                       add(mul(p0.z, g), mul(p1.z, frac)));
+}
+
+struct Cone
+{
+    float aperture, width;
+};
+
+// RayCone::Advance: the width after distance t (RT Gems I, chapter 20).
+__device__ __forceinline__ Cone cone_advance(Cone c, float t)
+{
+    Cone r;
+    r.aperture = c.aperture;
+    r.width = fminf(fmaxf(kConeEps, add(c.width, mul(c.aperture, t))), 1.0e6f);
+    return r;
+}
+
+// RayCone::Project: the cone's footprint axes on the plane with normal f.
+__device__ void cone_project(Cone c, float3 f, float3 d, float3& a1, float3& a2)
+{
+    const float fDotD = dot3(f, d);
+    if(fabsf(add(fDotD, 1.0f)) < kConeEps)
+        d = make_float3(add(d.x, kConeEps), add(d.y, kConeEps), add(d.z, kConeEps));
+    const float3 h1 = make_float3(sub(d.x, mul(fDotD, f.x)), sub(d.y, mul(fDotD, f.y)), sub(d.z, mul(fDotD, f.z)));
+    const float3 h2 = cross3(f, h1);
+    const float r = mul(c.width, 0.5f);
+    const float3 h[2] = { h1, h2 };
+    float3 out[2];
+#pragma unroll
+    for(int k = 0; k < 2; k++)
+    {
+        const float dh = dot3(d, h[k]);
+        const float3 q = make_float3(sub(h[k].x, mul(dh, d.x)), sub(h[k].y, mul(dh, d.y)), sub(h[k].z, mul(dh, d.z)));
+        const float denom = fmaxf(kConeEps, __fsqrt_rn(dot3(q, q)));
+        const float sc = __fdiv_rn(r, denom);
+        out[k] = make_float3(mul(sc, h[k].x), mul(sc, h[k].y), mul(sc, h[k].z));
+    }
+    a1 = out[0];
+    a2 = out[1];
+}
+
+// uv gradients of a hit along the cone's footprint axes (GenerateSurface,
+// JCGT 2021 Listing 1): P0 and edges E0 = P1 - P0, E1 = P2 - P0 of the
+// triangle in world space, f its normal towards the ray.
+__device__ void tex_gradients(float3 pos, float3 P0, float3 E0, float3 E1, float3 f, float2 uv0, float2 uv1,
+                              float2 uv2, float2 uv, float3 a1, float3 a2, float2& dpdx, float2& dpdy)
+{
+    const float areaRecip = __fdiv_rn(1.0f, dot3(f, cross3(E0, E1)));
+    const float3 off[2] = { a1, a2 };
+    float2 out[2];
+#pragma unroll
+    for(int k = 0; k < 2; k++)
+    {
+        const float3 eP = make_float3(add(sub(pos.x, P0.x), off[k].x), add(sub(pos.y, P0.y), off[k].y),
+                                      add(sub(pos.z, P0.z), off[k].z));
+        const float3 c1 = cross3(eP, E1), c2 = cross3(E0, eP);
+        const float a = dot3(f, make_float3(mul(c1.x, areaRecip), mul(c1.y, areaRecip), mul(c1.z, areaRecip)));
+        const float b = dot3(f, make_float3(mul(c2.x, areaRecip), mul(c2.y, areaRecip), mul(c2.z, areaRecip)));
+        const float c = sub(sub(1.0f, a), b);
+        const float uo = add(add(mul(uv0.x, c), mul(uv1.x, a)), mul(uv2.x, b));
+        const float vo = add(add(mul(uv0.y, c), mul(uv1.y, a)), mul(uv2.y, b));
+        out[k] = make_float2(sub(uo, uv.x), sub(vo, uv.y));
+    }
+    dpdx = out[0];
+    dpdy = out[1];
+}
+
+__device__ __forceinline__ float dot2(float2 a, float2 b) { return __fmaf_rn(a.y, b.y, __fmaf_rn(a.x, b.x, 0.0f)); }
+
+// Graphics::Refract in the plane z = 0 (RefractRayCone's Refract2D): the
+// refracted direction, or on total internal reflection v's component along
+// the boundary, normalised.
+__device__ float2 refract2d(float2 v, float2 n, float fromEta, float toEta)
+{
+    const float etaRatio = __fdiv_rn(fromEta, toEta);
+    // Vector3(n, 0) . Vector3(-v, 0) with the fma chain over three components
+    const float cosIn = __fmaf_rn(0.0f, 0.0f, __fmaf_rn(n.y, -v.y, __fmaf_rn(n.x, -v.x, 0.0f)));
+    const float sinInSqr = fmaxf(0.0f, sub(1.0f, mul(cosIn, cosIn)));
+    const float sinOutSqr = mul(mul(etaRatio, etaRatio), sinInSqr);
+    const float cosOut = sqrt_max(sub(1.0f, sinOutSqr));
+    if(sinOutSqr >= 1.0f)
+    {
+        const float nv = dot2(n, v);
+        const float2 q = make_float2(sub(v.x, mul(n.x, nv)), sub(v.y, mul(n.y, nv)));
+        const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot2(q, q)));
+        return make_float2(mul(q.x, inv), mul(q.y, inv));
+    }
+    const float k = sub(mul(etaRatio, cosIn), cosOut);
+    return make_float2(add(mul(etaRatio, v.x), mul(k, n.x)), add(mul(etaRatio, v.y), mul(k, n.y)));
+}
+
+// RefractMaterial::RefractRayCone (RT Gems II, chapter 10): the cone behind a
+// smooth dielectric, from the cone in front (aperture, width), the surface's
+// curvature term betaN, wo (towards the viewer) and the normal n facing it;
+// false (no change) on total internal reflection of wo.
+__device__ bool refract_cone(Cone front, float betaN, float3 wo, float3 n, float fromEta, float toEta, Cone& back)
+{
+    const float etaRatio = __fdiv_rn(fromEta, toEta);
+    const float cosIn = dot3(n, wo);
+    const float sinInSqr = fmaxf(0.0f, sub(1.0f, mul(cosIn, cosIn)));
+    const float sinOutSqr = mul(mul(etaRatio, etaRatio), sinInSqr);
+    if(sinOutSqr >= 1.0f) return false;
+    const float3 d3 = make_float3(-wo.x, -wo.y, -wo.z);
+    // GSOrthonormalize(d3, n) = Normalize(d3 - n Dot(d3, n))
+    const float dn = dot3(d3, n);
+    const float3 x = normalize3(make_float3(sub(d3.x, mul(n.x, dn)), sub(d3.y, mul(n.y, dn)), sub(d3.z, mul(n.z, dn))));
+    const float2 d = make_float2(dot3(x, d3), dot3(n, d3));
+    const float wSign = (front.width > 0.0f) ? 1.0f : 0.0f;
+    float s, c;
+    sincosf(mul(mul(wSign, front.aperture), 0.5f), &s, &c);
+    const float2 du = make_float2(sub(mul(d.x, c), mul(d.y, s)), add(mul(d.x, s), mul(d.y, c)));
+    const float2 dl = make_float2(add(mul(d.x, c), mul(d.y, s)), add(mul(d.x, -s), mul(d.y, c)));
+    float2 orthoD = make_float2(mul(mul(-d.y, front.width), 0.5f), mul(mul(d.x, front.width), 0.5f));
+    const float uHitX = add(orthoD.x, mul(du.x, __fdiv_rn(-orthoD.y, du.y)));
+    const float lHitX = add(-orthoD.x, mul(dl.x, __fdiv_rn(orthoD.y, dl.y)));
+    const float nSign = (uHitX > lHitX) ? 1.0f : -1.0f;
+    const float dTheta = mul(mul(-betaN, nSign), 0.5f);
+    float ns, nc;
+    sincosf(dTheta, &ns, &nc);
+    // Rotate2D_UL((0, 1), dTheta)
+    const float2 nu = make_float2(sub(mul(0.0f, nc), mul(1.0f, ns)), add(mul(0.0f, ns), mul(1.0f, nc)));
+    const float2 nl = make_float2(add(mul(0.0f, nc), mul(1.0f, ns)), add(mul(0.0f, -ns), mul(1.0f, nc)));
+    const float2 tu = refract2d(du, nu, fromEta, toEta);
+    const float2 tl = refract2d(dl, nl, fromEta, toEta);
+    orthoD = make_float2(-d.y, d.x);
+    float wl = mul(-uHitX, tu.y);
+    wl = __fdiv_rn(wl, dot2(orthoD, make_float2(-tu.y, tu.x)));
+    float wu = mul(lHitX, tl.y);
+    wu = __fdiv_rn(wu, dot2(orthoD, make_float2(-tl.y, tl.x)));
+    const float sgn = copysignf(1.0f, sub(mul(tu.x, tl.y), mul(tu.y, tl.x)));
+    const float cosTheta = fminf(fmaxf(-1.0f, dot2(tu, tl)), 1.0f);
+    float ap = mul(acosf(cosTheta), sgn);
+    ap = fmaxf(ap, kConeEps);
+    back.aperture = add(ap, betaN);
+    back.width = add(wu, wl);
+    return true;
+}
+
 // Albedo at a hit: constant, or the texture at the hit's uv.
 __device__ __forceinline__ float3 surface_albedo(const PtSceneTables& T, const PtSurface& sf, uint32_t gprim, float2 mh)
 {
     if(sf.tex.x == 0u || T.uvs == nullptr || gprim >= T.nTris) return make_float3(sf.albedo.x, sf.albedo.y, sf.albedo.z);
     const float2 uv = surface_uv(T, gprim, mh);
     return tex_read(T.textures[sf.tex.x - 1u], uv.x, uv.y);
+}
+
+// The same with a mip-mapped texture read at the level the path's cone
+// (advanced to the hit) gives: the cone's footprint on the triangle (f: its
+// normal facing the ray, d: the ray's direction) and the uv gradients along
+// its axes.  The triangle's corner and edges go to world space with the
+// instance transform (edges by its linear part).
+__device__ __forceinline__ float3 albedo_lod(const PtSceneTables& T, const PtSurface& sf, uint32_t gprim, float2 uv,
+                                          float3 pos, float3 f, float3 d, Cone cone)
+{
+    const PtTexture tx = T.textures[sf.tex.x - 1u];
+    const float4 v0 = T.tris[3 * (size_t)gprim], e0 = T.tris[3 * (size_t)gprim + 1], e1 = T.tris[3 * (size_t)gprim + 2];
+    float3 P0, E0, E1;
+    P0.x = add(add(add(mul(sf.m[0].x, v0.x), mul(sf.m[0].y, v0.y)), mul(sf.m[0].z, v0.z)), sf.m[0].w);
+    P0.y = add(add(add(mul(sf.m[1].x, v0.x), mul(sf.m[1].y, v0.y)), mul(sf.m[1].z, v0.z)), sf.m[1].w);
+    P0.z = add(add(add(mul(sf.m[2].x, v0.x), mul(sf.m[2].y, v0.y)), mul(sf.m[2].z, v0.z)), sf.m[2].w);
+    E0.x = add(add(mul(sf.m[0].x, e0.x), mul(sf.m[0].y, e0.y)), mul(sf.m[0].z, e0.z));
+    E0.y = add(add(mul(sf.m[1].x, e0.x), mul(sf.m[1].y, e0.y)), mul(sf.m[1].z, e0.z));
+    E0.z = add(add(mul(sf.m[2].x, e0.x), mul(sf.m[2].y, e0.y)), mul(sf.m[2].z, e0.z));
+    E1.x = add(add(mul(sf.m[0].x, e1.x), mul(sf.m[0].y, e1.y)), mul(sf.m[0].z, e1.z));
+    E1.y = add(add(mul(sf.m[1].x, e1.x), mul(sf.m[1].y, e1.y)), mul(sf.m[1].z, e1.z));
+    E1.z = add(add(mul(sf.m[2].x, e1.x), mul(sf.m[2].y, e1.y)), mul(sf.m[2].z, e1.z));
+    float3 a1, a2;
+    cone_project(cone, f, normalize3(d), a1, a2);
+    const float4 q0 = T.uvs[2 * (size_t)gprim], q1 = T.uvs[2 * (size_t)gprim + 1];
+    float2 dpdx, dpdy;
+    tex_gradients(pos, P0, E0, E1, f, make_float2(q0.x, q0.y), make_float2(q0.z, q0.w), make_float2(q1.x, q1.y), uv, a1,
+                  a2, dpdx, dpdy);
+    return tex_read_grad(tx, uv.x, uv.y, dpdx, dpdy);
+}
+
+__device__ __forceinline__ float3 surface_albedo_cone(const PtSceneTables& T, const PtSurface& sf, uint32_t gprim,
+                                                      float2 mh, float3 pos, float3 f, float3 d, Cone cone)
+{
+    if(sf.tex.x == 0u || T.uvs == nullptr || gprim >= T.nTris) return make_float3(sf.albedo.x, sf.albedo.y, sf.albedo.z);
+    const float2 uv = surface_uv(T, gprim, mh);
+    const PtTexture& tx = T.textures[sf.tex.x - 1u];
+    if(tx.mipCount <= 1u) return tex_read(tx, uv.x, uv.y);
+    return albedo_lod(T, sf, gprim, uv, pos, f, d, cone);
+}
+
+// The cone a scattered ray leaves with (RefractRayCone, then
+// ConeAfterScatter; the surfaces here have no vertex normals, so the
+// curvature term betaN is 0): the refracted cone for a dielectric's
+// transmission, the incoming one otherwise.
+__device__ __forceinline__ Cone cone_after_scatter(const PtSurface& sf, uint32_t mt, bool backSide, Cone cone, float3 wo,
+                                                   float3 n, float3 wi)
+{
+    Cone back = cone;
+    if(mt == kMatRefract && dot3(wi, n) <= 0.0f)
+    {
+        float fromEta = sf.mat.z, toEta = sf.mat.w;
+        if(backSide) { const float t = fromEta; fromEta = toEta; toEta = t; }
+        Cone r;
+        if(refract_cone(cone, 0.0f, wo, n, fromEta, toEta, r)) back = r;
+    }
+    Cone out;
+    if(dot3(wi, n) > 0.0f) { out.aperture = add(cone.aperture, mul(2.0f, 0.0f)); out.width = cone.width; }
+    else { out.aperture = sub(back.aperture, 0.0f); out.width = back.width; }
+    return out;
 }
 
 // Adds an emission-gradient contribution (RGB) to the light instance's FP64

@@ -175,6 +175,7 @@ struct Texture
     bool committed = false;
     std::vector<uint8_t> mip0;
     bool mip0Set = false;
+    std::vector<std::vector<uint8_t>> upper;   // pushed levels >= 1 (index = level), empty = not pushed
     uint32_t ptId = 0xFFFFFFFFu;               // the path tracer's texture, after the surface commit
 };
 
@@ -468,25 +469,30 @@ mrg_status transform_of(mrg_tracer* t, uint32_t id, float m34[12])
     return MRG_OK;
 }
 
-mrg_status texture_rgba_f32(mrg_tracer* t, uint32_t tid, std::vector<float>& out, uint32_t& w, uint32_t& h)
+// n texels of a pushed level in the path tracer's RGBA f32 form
+void level_rgba_f32(uint32_t pixel, const uint8_t* data, size_t n, std::vector<float>& out)
 {
-    if(tid == 0 || tid > t->textures.size()) return err("unknown texture " + std::to_string(tid));
-    const Texture& x = t->textures[tid - 1];
-    if(!x.mip0Set) return err("texture " + std::to_string(tid) + " has no data");
-    w = x.w; h = x.h;
-    const size_t n = (size_t)x.w * x.h;
     out.resize(4 * n);
-    if(x.pixel == MRG_PIX_RGBA_FLOAT) std::memcpy(out.data(), x.mip0.data(), 16 * n);
-    else if(x.pixel == MRG_PIX_RGB_FLOAT)
+    if(pixel == MRG_PIX_RGBA_FLOAT) std::memcpy(out.data(), data, 16 * n);
+    else if(pixel == MRG_PIX_RGB_FLOAT)
     {
-        const float* f = reinterpret_cast<const float*>(x.mip0.data());
+        const float* f = reinterpret_cast<const float*>(data);
         for(size_t i = 0; i < n; i++)
         {
             out[4 * i] = f[3 * i]; out[4 * i + 1] = f[3 * i + 1]; out[4 * i + 2] = f[3 * i + 2]; out[4 * i + 3] = 1.0f;
         }
     }
     else
-        for(size_t i = 0; i < 4 * n; i++) out[i] = (float)x.mip0[i] / 255.0f;
+        for(size_t i = 0; i < 4 * n; i++) out[i] = (float)data[i] / 255.0f;
+}
+
+mrg_status texture_rgba_f32(mrg_tracer* t, uint32_t tid, std::vector<float>& out, uint32_t& w, uint32_t& h)
+{
+    if(tid == 0 || tid > t->textures.size()) return err("unknown texture " + std::to_string(tid));
+    const Texture& x = t->textures[tid - 1];
+    if(!x.mip0Set) return err("texture " + std::to_string(tid) + " has no data");
+    w = x.w; h = x.h;
+    level_rgba_f32(x.pixel, x.mip0.data(), (size_t)x.w * x.h, out);
     return MRG_OK;
 }
 
@@ -510,6 +516,28 @@ mrg_status pt_texture(mrg_tracer* t, uint32_t tid, uint32_t& ptId)
         s = mrg_pt_add_texture(t->ctx, x.w, x.h, x.pixel == MRG_PIX_RGBA8_UNORM ? MRG_TEX_RGBA8 : MRG_TEX_RGBA32F,
                                x.mip0.data(), 0, &id);
     if(s != MRG_OK) return s;
+    // mips: TracerParameters::genMips fills every level the texture does not
+    // have with mipGenFilter (TextureMemory.cpp:588-591, 826-830); pushed
+    // levels are kept either way
+    if(t->params.genMips)
+    {
+        const float r = t->params.mipGenFilterRadius > 0.0f ? t->params.mipGenFilterRadius : 2.0f;
+        if((s = mrg_pt_generate_mips(t->ctx, id, r)) != MRG_OK) return s;
+    }
+    for(uint32_t m = 1; m < x.upper.size(); m++)
+    {
+        if(x.upper[m].empty()) continue;
+        const size_t n = (size_t)std::max(x.w >> m, 1u) * std::max(x.h >> m, 1u);
+        if(x.pixel == MRG_PIX_RGB_FLOAT)
+        {
+            std::vector<float> f;
+            level_rgba_f32(x.pixel, x.upper[m].data(), n, f);
+            s = mrg_pt_set_texture_mip(t->ctx, id, m, f.data());
+        }
+        else
+            s = mrg_pt_set_texture_mip(t->ctx, id, m, x.upper[m].data());
+        if(s != MRG_OK) return s;
+    }
     x.ptId = ptId = id;
     return MRG_OK;
 }
@@ -939,6 +967,8 @@ mrg_status mrg_tracer_create(const mrg_tracer_params* params, mrg_tracer** out)
     if(p.triangleTest > MRG_TRI_WATERTIGHT) return err("unknown triangle test");
     if(p.device < 0) return err("bad device ordinal");
     if(!(p.filmFilterRadius >= 0.0f)) return err("film filter radius must be >= 0");
+    if(!(p.mipGenFilterRadius >= 0.0f) || p.mipGenFilterRadius > 64.0f)
+        return err("mip generation filter radius in [0, 64]");
     auto* t = new mrg_tracer;
     t->params = p;
     t->reset_scene();
@@ -1293,6 +1323,11 @@ mrg_status mrg_tracer_push_texture_data(mrg_tracer* t, uint32_t texture_id, uint
     {
         x.mip0.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + bytes);
         x.mip0Set = true;
+    }
+    else
+    {
+        if(x.upper.size() < x.mips) x.upper.resize(x.mips);
+        x.upper[mip_level].assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + bytes);
     }
     return MRG_OK;
 }

@@ -50,7 +50,7 @@ class PathTracer:
             N.check(N.lib().mrg_pt_add_texture(self.acc._h, texels.shape[1], texels.shape[0], 1,
                                                C.c_void_p(texels.data_ptr()), 1, C.byref(out)))
             self._tex_shapes = getattr(self, "_tex_shapes", {})
-            self._tex_shapes[out.value] = (texels.shape[0], texels.shape[1])
+            self._tex_shapes[out.value] = (texels.shape[0], texels.shape[1], np.float32)
             return out.value
         t = np.ascontiguousarray(texels)
         if t.ndim != 3 or t.shape[2] != 4 or t.dtype not in (np.uint8, np.float32):
@@ -58,7 +58,7 @@ class PathTracer:
         N.check(N.lib().mrg_pt_add_texture(self.acc._h, t.shape[1], t.shape[0], 0 if t.dtype == np.uint8 else 1,
                                            t.ctypes.data, 0, C.byref(out)))
         self._tex_shapes = getattr(self, "_tex_shapes", {})
-        self._tex_shapes[out.value] = (t.shape[0], t.shape[1])
+        self._tex_shapes[out.value] = (t.shape[0], t.shape[1], t.dtype.type)
         return out.value
 
     def render_cached(self, p, image=None, train_paths=32768, stream=None, loss=False):
@@ -98,6 +98,23 @@ class PathTracer:
 
     def _tex_shape(self, tex_id):
         return self._tex_shapes[tex_id]
+
+    def generate_mips(self, tex_id, filter_radius=2.0):
+        """A mip chain for the texture (see mrg_pt_generate_mips); 0 drops it."""
+        N.check(N.lib().mrg_pt_generate_mips(self.acc._h, tex_id, float(filter_radius)))
+
+    def set_texture_mip(self, tex_id, level, texels):
+        """Given texels of one mip level (see mrg_pt_set_texture_mip): a
+        (max(h >> level, 1), max(w >> level, 1), 4) array in the texture's
+        format."""
+        a = np.ascontiguousarray(texels)
+        h, w, dt = getattr(self, "_tex_shapes", {}).get(tex_id, (None, None, None))
+        if h is None or level < 1:
+            raise ValueError("unknown texture or level < 1")
+        if a.shape != (max(h >> level, 1), max(w >> level, 1), 4) or a.dtype != dt:
+            raise ValueError("mip level %d of a %d x %d texture is (%d, %d, 4) %s"
+                             % (level, w, h, max(h >> level, 1), max(w >> level, 1), np.dtype(dt).name))
+        N.check(N.lib().mrg_pt_set_texture_mip(self.acc._h, tex_id, level, a.ctypes.data_as(C.c_void_p)))
 
     def set_albedo_texture(self, inst, tex_id):
         N.check(N.lib().mrg_pt_set_albedo_texture(self.acc._h, inst, 0xFFFFFFFF if tex_id is None else tex_id))
@@ -256,6 +273,10 @@ def load_box_scene(pt, seed=0):
                 key = id(s["texture"])
                 if key not in textures:
                     textures[key] = pt.add_texture(s["texture"])
+                    if s.get("mip_radius"):
+                        pt.generate_mips(textures[key], s["mip_radius"])
+                    for lv, texels in sorted(s.get("mips_given", {}).items()):
+                        pt.set_texture_mip(textures[key], lv, texels)
                 pt.set_albedo_texture(inst, textures[key])
     pt.build()
     return surf

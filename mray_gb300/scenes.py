@@ -264,6 +264,16 @@ def box_scene_textured(seed=0, size=256):
     return s
 
 
+def mipmapped(surf, radius=2.0):
+    """Marks every textured surface's texture for a mip chain of the given
+    filter radius (MRay's texture-load option, read at the ray cone's level
+    of detail); returns the surface list."""
+    for s in surf:
+        if s.get("texture") is not None:
+            s["mip_radius"] = float(radius)
+    return surf
+
+
 def uv_sphere(n_theta=128, n_phi=256, radius=1.0, noise=0.0, seed=0):
     """Latitude-longitude sphere with (n_theta - 1) * n_phi * 2 triangles
     plus the pole fans (2 * n_phi), uv = (phi / 2pi, theta / pi); optional

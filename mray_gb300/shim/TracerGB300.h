@@ -165,6 +165,10 @@ class TracerGB300 final : public TracerI
         tp.samplerType = (p.samplerType.e == SamplerType::E::Z_SOBOL) ? MRG_TRACER_SAMPLER_ZSOBOL
                                                                      : MRG_TRACER_SAMPLER_INDEPENDENT;
         tp.filmFilterRadius = p.filmFilter.radius;
+        if(p.genMips && p.mipGenFilter.type != FilterType::E::GAUSSIAN)
+            throw MRayError("mray_gb300: only the Gaussian mip generation filter is available");
+        tp.genMips = p.genMips ? 1u : 0u;
+        tp.mipGenFilterRadius = p.mipGenFilter.radius;
         Check(mrg_tracer_create(&tp, &t));
     }
     ~TracerGB300() override

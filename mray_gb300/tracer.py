@@ -27,13 +27,16 @@ def _u32s(v):
 
 
 class Tracer:
-    def __init__(self, seed=0, device=0, sampler="independent", film_filter_radius=0.0, watertight=False):
+    def __init__(self, seed=0, device=0, sampler="independent", film_filter_radius=0.0, watertight=False,
+                 gen_mips=False, mip_filter_radius=0.0):
         p = N.MrgTracerParams()
         p.seed = int(seed)
         p.device = int(device)
         p.samplerType = SAMPLER[sampler]
         p.filmFilterRadius = float(film_filter_radius)
         p.triangleTest = N.MRG_TRI_WATERTIGHT if watertight else N.MRG_TRI_MOLLER_TRUMBORE
+        p.genMips = 1 if gen_mips else 0
+        p.mipGenFilterRadius = float(mip_filter_radius)
         self._h = C.c_void_p()
         self._L = N.lib()
         N.check(self._L.mrg_tracer_create(C.byref(p), C.byref(self._h)))

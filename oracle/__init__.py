@@ -105,6 +105,10 @@ def lib():
         L.orc_guide_snapshot.argtypes = [vp, vp, vp, vp]
         L.orc_pt_render_guided.argtypes = [vp, vp, vp, vp, u32, vp, vp, vp, u32, vp]
         L.orc_pt_render_guided.restype = C.c_int
+        L.orc_gen_mips.argtypes = [vp, u32, u32, u32, C.c_float, vp]
+        L.orc_gen_mips.restype = u32
+        L.orc_gen_mips_levels.argtypes = [vp, u32, u32, u32, C.c_float, u32, u32, vp]
+        L.orc_gen_mips_levels.restype = u32
         L.orc_pt_render.restype = C.c_int
         L.orc_pt_camera_frame.argtypes = [vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
         L.orc_pt_make_light.argtypes = [vp, vp, vp, C.c_int, vp]
@@ -302,7 +306,8 @@ class PtParams(C.Structure):
                 ("filterRadius", C.c_float), ("camPos", C.c_float * 3),
                 ("camBottomLeft", C.c_float * 3), ("camRight", C.c_float * 3),
                 ("camUp", C.c_float * 3), ("planeSize", C.c_float * 2),
-                ("nearT", C.c_float), ("farT", C.c_float), ("sampler", u32), ("samplerMaxSpp", u32)]
+                ("nearT", C.c_float), ("farT", C.c_float), ("sampler", u32), ("samplerMaxSpp", u32),
+                ("coneAperture", C.c_float)]
 
 
 class PtSurface(C.Structure):
@@ -311,7 +316,7 @@ class PtSurface(C.Structure):
                 ("iorFront", C.c_float), ("iorBack", C.c_float), ("lightBase", u32),
                 ("primKeyBase", u32), ("triangles", vp), ("m", C.c_float * 12),
                 ("inv", C.c_float * 12), ("texels", vp), ("texW", u32), ("texH", u32),
-                ("texFormat", u32), ("uvs", vp)]
+                ("texFormat", u32), ("uvs", vp), ("mips", vp), ("mipCount", u32)]
 
 
 class PtLightTri(C.Structure):
@@ -495,6 +500,14 @@ def fx_sample_waves(xi):
     return w, p
 
 
+def fx_cone(in20):
+    return _fx_rows(lib().orc_fx_cone, in20, 12)
+
+
+def fx_pixel_indices(in6):
+    return _fx_rows(lib().orc_fx_pixel_indices, in6, 2)
+
+
 def fx_spherical_coords(in6):
     return _fx_rows(lib().orc_fx_spherical_coords, in6, 7)
 
@@ -563,6 +576,16 @@ class PtScene:
                 sf.texH, sf.texW = tex.shape[0], tex.shape[1]
                 sf.texFormat = 0 if tex.dtype == np.uint8 else 1
                 sf.uvs = uvp.ctypes.data
+                sf.mipCount = 1
+                if s.get("mip_radius") or s.get("mips_given"):
+                    key = (id(s["texture"]), float(s.get("mip_radius") or 0.0), id(s.get("mips_given")))
+                    mips = getattr(self, "_mips", {})
+                    if key not in mips:
+                        mips[key] = gen_mips(tex, float(s.get("mip_radius") or 0.0), s.get("mips_given"))
+                    self._mips = mips
+                    chain, count = mips[key]
+                    sf.mips = chain.ctypes.data
+                    sf.mipCount = count
             if s["kind"] == "light":
                 rad = (C.c_float * 3)(*[float(x) for x in s["radiance"]])
                 m = np.ascontiguousarray(s["m34"], np.float32).reshape(12)
@@ -667,6 +690,49 @@ class PtScene:
                              C.byref(self.spectral.c) if self.spectral is not None else None,
                              _vp(img), threads or default_threads())
         return img
+
+
+def mip_chain_texels(w, h, levels=None):
+    """Texels of levels 1 .. levels - 1 (all of a full chain by default)."""
+    n, m = 0, 1
+    while ((w >> (m - 1)) > 1 or (h >> (m - 1)) > 1) and (levels is None or m < levels):
+        n += max(w >> m, 1) * max(h >> m, 1)
+        m += 1
+    return n
+
+
+def gen_mips(tex, radius, given=None):
+    """Levels 1.. of a (h, w, 4) uint8 / float32 texture, one after another
+    in a flat array of its dtype; returns (array, level count).  given maps
+    levels to caller texels that are kept (their children filtered from
+    them); with radius 0 the chain ends at the last given level
+    (orc_gen_mips_levels)."""
+    t = np.ascontiguousarray(tex)
+    h, w = t.shape[:2]
+    given = given or {}
+    full = max(w, h).bit_length()
+    if radius > 0:
+        levels = full
+    else:
+        levels = max(given) + 1 if given else 1
+        missing = [m for m in range(1, levels) if m not in given]
+        if missing:
+            raise ValueError("mip levels %s have no data and no generation filter" % missing)
+    out = np.zeros(mip_chain_texels(w, h, levels) * 4, t.dtype)
+    valid = 0
+    for m, texels in given.items():
+        if not 1 <= m < full:
+            raise ValueError("mip level %d out of range" % m)
+        o = mip_chain_texels(w, h, m) * 4
+        a = np.ascontiguousarray(texels, t.dtype).ravel()
+        if a.size != max(w >> m, 1) * max(h >> m, 1) * 4:
+            raise ValueError("mip level %d has the wrong size" % m)
+        out[o:o + a.size] = a
+        valid |= 1 << m
+    if radius > 0:
+        lib().orc_gen_mips_levels(_vp(t), w, h, 0 if t.dtype == np.uint8 else 1, radius, levels, valid,
+                                  _vp(out) if out.size else None)
+    return out, levels
 
 
 class GuideState:

@@ -1017,6 +1017,278 @@ static int light_tri_emits(const orc_pt_light_tri* L, const float wo[3])
     return L->twoSided ? 1 : (dot3f(L->n, wo) > 0.0f);
 }
 
+/* ------------------------------------------------------------------------ */
+/* Mip chains, mip-mapped reads and ray cones.                              */
+/*   KCGenerateMipmaps / FilterPixel     Source/Tracer/TextureFilter.cu:62-192 */
+/*   ConvertPixelIndices, TextureMipSize Source/Core/GraphicsFunctions.h:474-538 */
+/*   TextureViewCPU gradient / LOD read  Source/Device/CPU/TextureViewCPU.h:405-470 */
+/*     (gradients taken in texels)                                          */
+/*   RayCone Advance / Project, ConeAfterScatter  Source/Tracer/TracerTypes.h:323-380 */
+/*   texture gradients of a hit          PrimitiveDefaultTriangle.hpp:491-569 */
+/*   RefractMaterial::RefractRayCone     Source/Tracer/MaterialsDefault.hpp:353-462 */
+/* ------------------------------------------------------------------------ */
+#define CONE_EPS 1.0e-5f
+
+static inline uint32_t mip_dim(uint32_t r, uint32_t m) { return (r >> m) ? (r >> m) : 1u; }
+
+/* texels of levels 1 .. levels - 1 of a w x h chain (the offset of level m is
+ * chain_texels(w, h, m)) */
+static size_t chain_texels(uint32_t w, uint32_t h, uint32_t levels)
+{
+    size_t n = 0;
+    for(uint32_t m = 1; m < levels && (mip_dim(w, m - 1) > 1u || mip_dim(h, m - 1) > 1u); m++)
+        n += (size_t)mip_dim(w, m) * mip_dim(h, m);
+    return n;
+}
+
+uint32_t orc_gen_mips_levels(const void* texels, uint32_t w, uint32_t h, uint32_t format, float radius,
+                             uint32_t levels, uint32_t validMask, void* out)
+{
+    float off[8], g[8];
+    const float sigma = radius * 0.285714f;
+    for(int k = 0; k < 8; k++)
+    {
+        const float d = 1.0f / 8.0f;
+        const float xi = d * 0.5f + d * (float)k;
+        off[k] = xi * 2.0f * radius - radius;
+        g[k] = gaussian(off[k], sigma);
+    }
+    const size_t bpp = (format == 0u) ? 4u : 16u;
+    unsigned char* chain = (unsigned char*)out;
+    for(uint32_t m = 1; m < levels; m++)
+    {
+        if(validMask & (1u << m)) continue;        /* a given level is kept */
+        const uint32_t pw = mip_dim(w, m - 1), ph = mip_dim(h, m - 1);
+        const uint32_t cw = mip_dim(w, m), ch = mip_dim(h, m);
+        const unsigned char* src = (m == 1u) ? (const unsigned char*)texels : chain + chain_texels(w, h, m - 1) * bpp;
+        unsigned char* dst = chain + chain_texels(w, h, m) * bpp;
+        const float rx = (float)pw / (float)cw, ry = (float)ph / (float)ch;
+        for(uint32_t y = 0; y < ch; y++)
+            for(uint32_t x = 0; x < cw; x++)
+            {
+                float acc[4] = { 0, 0, 0, 0 }, wsum = 0.0f;
+                for(int sy = 0; sy < 8; sy++)
+                {
+                    float py = (((float)y + off[sy]) + 0.5f) * ry - 0.5f;
+                    py = fminf(fmaxf(0.0f, py), (float)(ph - 1u));
+                    const uint32_t iy = (uint32_t)lroundf(py);
+                    for(int sx = 0; sx < 8; sx++)
+                    {
+                        float px = (((float)x + off[sx]) + 0.5f) * rx - 0.5f;
+                        px = fminf(fmaxf(0.0f, px), (float)(pw - 1u));
+                        const uint32_t ix = (uint32_t)lroundf(px);
+                        const float wgt = g[sx] * g[sy];
+                        const size_t t = (size_t)iy * pw + ix;
+                        float v[4];
+                        if(format == 0u) for(int k = 0; k < 4; k++) v[k] = (float)src[4 * t + k];
+                        else memcpy(v, src + 16 * t, 16);
+                        for(int k = 0; k < 4; k++) acc[k] = acc[k] + wgt * v[k];
+                        wsum = wsum + wgt;
+                    }
+                }
+                const size_t o = (size_t)y * cw + x;
+                for(int k = 0; k < 4; k++)
+                {
+                    const float r = acc[k] / wsum;
+                    if(format == 0u) dst[4 * o + k] = (unsigned char)fminf(fmaxf(roundf(r), 0.0f), 255.0f);
+                    else memcpy(dst + 16 * o + 4 * k, &r, 4);
+                }
+            }
+    }
+    return levels;
+}
+
+uint32_t orc_gen_mips(const void* texels, uint32_t w, uint32_t h, uint32_t format, float radius, void* out)
+{
+    uint32_t levels = 0;
+    for(uint32_t m = w > h ? w : h; m; m >>= 1) levels++;
+    return orc_gen_mips_levels(texels, w, h, format, radius, levels, 0u, out);
+}
+
+/* level m of a surface's texture: base pointer and size */
+static const void* mip_base(const orc_pt_surface* sf, uint32_t m, uint32_t* w, uint32_t* h)
+{
+    *w = mip_dim(sf->texW, m);
+    *h = mip_dim(sf->texH, m);
+    if(m == 0u) return sf->texels;
+    size_t start = 0;
+    for(uint32_t k = 1; k < m; k++) start += (size_t)mip_dim(sf->texW, k) * mip_dim(sf->texH, k);
+    return (const char*)sf->mips + start * (sf->texFormat == 0u ? 4u : 16u);
+}
+
+static void tex_read_grad(const orc_pt_surface* sf, const float uv[2], const float dx[2], const float dy[2], float rgb[3])
+{
+    const float sx = (float)sf->texW, sy = (float)sf->texH;
+    const float gx0 = dx[0] * sx, gx1 = dx[1] * sy, gy0 = dy[0] * sx, gy1 = dy[1] * sy;
+    const float lx = fmaf(gx1, gx1, fmaf(gx0, gx0, 0.0f)), ly = fmaf(gy1, gy1, fmaf(gy0, gy0, 0.0f));
+    float level = 0.5f * log2f(fmaxf(lx, ly));
+    level = fminf(fmaxf(0.0f, level), (float)(sf->mipCount - 1u));
+    float m0f;
+    const float frac = modff(level, &m0f);
+    const uint32_t m0 = (uint32_t)m0f, m1 = (m0 + 1u < sf->mipCount) ? m0 + 1u : sf->mipCount - 1u;
+    uint32_t w, h;
+    const void* b0 = mip_base(sf, m0, &w, &h);
+    float p0[3];
+    orc_tex_read(b0, w, h, sf->texFormat, uv, p0);
+    if(m0 == m1) { memcpy(rgb, p0, 12); return; }
+    const void* b1 = mip_base(sf, m1, &w, &h);
+    float p1[3];
+    orc_tex_read(b1, w, h, sf->texFormat, uv, p1);
+    for(int k = 0; k < 3; k++) rgb[k] = p0[k] * (1.0f - frac) + p1[k] * frac;
+}
+
+typedef struct { float aperture, width; } cone_t;
+
+static cone_t cone_advance(cone_t c, float t)
+{
+    cone_t r = { c.aperture, fminf(fmaxf(CONE_EPS, c.width + c.aperture * t), 1.0e6f) };
+    return r;
+}
+
+static void cone_project(cone_t c, const float f[3], const float dIn[3], float a1[3], float a2[3])
+{
+    float d[3] = { dIn[0], dIn[1], dIn[2] };
+    const float fDotD = dot3f(f, d);
+    if(fabsf(fDotD + 1.0f) < CONE_EPS) for(int k = 0; k < 3; k++) d[k] = d[k] + CONE_EPS;
+    float h[2][3];
+    for(int k = 0; k < 3; k++) h[0][k] = d[k] - fDotD * f[k];
+    cross3f(f, h[0], h[1]);
+    const float r = c.width * 0.5f;
+    float* out[2] = { a1, a2 };
+    for(int j = 0; j < 2; j++)
+    {
+        const float dh = dot3f(d, h[j]);
+        float q[3];
+        for(int k = 0; k < 3; k++) q[k] = h[j][k] - dh * d[k];
+        const float denom = fmaxf(CONE_EPS, sqrtf(dot3f(q, q)));
+        const float sc = r / denom;
+        for(int k = 0; k < 3; k++) out[j][k] = sc * h[j][k];
+    }
+}
+
+/* Albedo of a textured surface with a mip chain, read at the cone's level:
+ * the triangle's corner and edges in world space (edges by the transform's
+ * linear part), f its normal facing the ray, d the ray direction. */
+static void albedo_lod(const orc_pt_surface* sf, const float* tri9, const float uv[2], const float uvq[6],
+                       const float pos[3], const float f[3], const float d[3], cone_t cone, float rgb[3])
+{
+    const float e0l[3] = { tri9[3] - tri9[0], tri9[4] - tri9[1], tri9[5] - tri9[2] };
+    const float e1l[3] = { tri9[6] - tri9[0], tri9[7] - tri9[1], tri9[8] - tri9[2] };
+    float P0[3], E0[3], E1[3];
+    for(int r = 0; r < 3; r++)
+    {
+        P0[r] = sf->m[4 * r] * tri9[0] + sf->m[4 * r + 1] * tri9[1] + sf->m[4 * r + 2] * tri9[2] + sf->m[4 * r + 3];
+        E0[r] = sf->m[4 * r] * e0l[0] + sf->m[4 * r + 1] * e0l[1] + sf->m[4 * r + 2] * e0l[2];
+        E1[r] = sf->m[4 * r] * e1l[0] + sf->m[4 * r + 1] * e1l[1] + sf->m[4 * r + 2] * e1l[2];
+    }
+    float dn[3] = { d[0], d[1], d[2] };
+    normalize3f(dn);
+    float a[2][3];
+    cone_project(cone, f, dn, a[0], a[1]);
+    float c01[3];
+    cross3f(E0, E1, c01);
+    const float areaRecip = 1.0f / dot3f(f, c01);
+    float grad[2][2];
+    for(int j = 0; j < 2; j++)
+    {
+        float eP[3], c1[3], c2[3];
+        for(int k = 0; k < 3; k++) eP[k] = (pos[k] - P0[k]) + a[j][k];
+        cross3f(eP, E1, c1);
+        cross3f(E0, eP, c2);
+        for(int k = 0; k < 3; k++) { c1[k] = c1[k] * areaRecip; c2[k] = c2[k] * areaRecip; }
+        const float ba = dot3f(f, c1), bb = dot3f(f, c2);
+        const float bc = (1.0f - ba) - bb;
+        for(int k = 0; k < 2; k++) grad[j][k] = (uvq[k] * bc + uvq[2 + k] * ba + uvq[4 + k] * bb) - uv[k];
+    }
+    tex_read_grad(sf, uv, grad[0], grad[1], rgb);
+}
+
+static inline float dot2f(const float a[2], const float b[2]) { return fmaf(a[1], b[1], fmaf(a[0], b[0], 0.0f)); }
+
+static void refract2d(const float v[2], const float n[2], float fromEta, float toEta, float out[2])
+{
+    const float etaRatio = fromEta / toEta;
+    const float cosIn = fmaf(0.0f, 0.0f, fmaf(n[1], -v[1], fmaf(n[0], -v[0], 0.0f)));
+    const float sinInSqr = fmaxf(0.0f, 1.0f - cosIn * cosIn);
+    const float sinOutSqr = etaRatio * etaRatio * sinInSqr;
+    const float cosOut = sqrt_max(1.0f - sinOutSqr);
+    if(sinOutSqr >= 1.0f)
+    {
+        const float nv = dot2f(n, v);
+        float q[2] = { v[0] - n[0] * nv, v[1] - n[1] * nv };
+        const float inv = 1.0f / sqrtf(dot2f(q, q));
+        out[0] = q[0] * inv;
+        out[1] = q[1] * inv;
+        return;
+    }
+    const float k = etaRatio * cosIn - cosOut;
+    out[0] = etaRatio * v[0] + k * n[0];
+    out[1] = etaRatio * v[1] + k * n[1];
+}
+
+static int refract_cone(cone_t front, float betaN, const float wo[3], const float n[3], float fromEta, float toEta,
+                        cone_t* back)
+{
+    const float etaRatio = fromEta / toEta;
+    const float cosIn = dot3f(n, wo);
+    const float sinInSqr = fmaxf(0.0f, 1.0f - cosIn * cosIn);
+    const float sinOutSqr = etaRatio * etaRatio * sinInSqr;
+    if(sinOutSqr >= 1.0f) return 0;
+    const float d3[3] = { -wo[0], -wo[1], -wo[2] };
+    const float dn = dot3f(d3, n);
+    float x[3] = { d3[0] - n[0] * dn, d3[1] - n[1] * dn, d3[2] - n[2] * dn };
+    normalize3f(x);
+    const float d[2] = { dot3f(x, d3), dot3f(n, d3) };
+    const float wSign = (front.width > 0.0f) ? 1.0f : 0.0f;
+    const float alpha = wSign * front.aperture * 0.5f;
+    const float s = sinf(alpha), c = cosf(alpha);
+    const float du[2] = { d[0] * c - d[1] * s, d[0] * s + d[1] * c };
+    const float dl[2] = { d[0] * c + d[1] * s, d[0] * -s + d[1] * c };
+    float orthoD[2] = { -d[1] * front.width * 0.5f, d[0] * front.width * 0.5f };
+    const float uHitX = +orthoD[0] + du[0] * (-orthoD[1] / du[1]);
+    const float lHitX = -orthoD[0] + dl[0] * (+orthoD[1] / dl[1]);
+    const float nSign = (uHitX > lHitX) ? 1.0f : -1.0f;
+    const float dTheta = -betaN * nSign * 0.5f;
+    const float ns = sinf(dTheta), nc = cosf(dTheta);
+    const float nu[2] = { 0.0f * nc - 1.0f * ns, 0.0f * ns + 1.0f * nc };
+    const float nl[2] = { 0.0f * nc + 1.0f * ns, 0.0f * -ns + 1.0f * nc };
+    float tu[2], tl[2];
+    refract2d(du, nu, fromEta, toEta, tu);
+    refract2d(dl, nl, fromEta, toEta, tl);
+    orthoD[0] = -d[1];
+    orthoD[1] = d[0];
+    const float pu[2] = { -tu[1], tu[0] }, pl[2] = { -tl[1], tl[0] };
+    float wl = -uHitX * tu[1];
+    wl /= dot2f(orthoD, pu);
+    float wu = +lHitX * tl[1];
+    wu /= dot2f(orthoD, pl);
+    const float sgn = copysignf(1.0f, tu[0] * tl[1] - tu[1] * tl[0]);
+    const float cosTheta = fminf(fmaxf(-1.0f, dot2f(tu, tl)), 1.0f);
+    float ap = acosf(cosTheta) * sgn;
+    ap = fmaxf(ap, CONE_EPS);
+    back->aperture = ap + betaN;
+    back->width = wu + wl;
+    return 1;
+}
+
+/* RefractRayCone then ConeAfterScatter (betaN = 0: no vertex normals) */
+static cone_t cone_after_scatter(const orc_pt_surface* sf, int backSide, cone_t cone, const float wo[3],
+                                 const float n[3], const float wi[3])
+{
+    cone_t back = cone;
+    if(sf->matType == ORC_MAT_REFRACT && dot3f(wi, n) <= 0.0f)
+    {
+        float fromEta = sf->iorFront, toEta = sf->iorBack;
+        if(backSide) { const float t = fromEta; fromEta = toEta; toEta = t; }
+        cone_t r;
+        if(refract_cone(cone, 0.0f, wo, n, fromEta, toEta, &r)) back = r;
+    }
+    cone_t out;
+    if(dot3f(wi, n) > 0.0f) { out.aperture = cone.aperture + 2.0f * 0.0f; out.width = cone.width; }
+    else { out.aperture = back.aperture - 0.0f; out.width = back.width; }
+    return out;
+}
+
 /* CameraPinhole::EvaluateRay (CamerasDefault.hpp:94-135) for pixel (x, y)
  * and a film-filter offset (ox, oy) in pixels. */
 static void camera_ray(const orc_pt_params* P, uint32_t x, uint32_t y, float ox, float oy, float dir[3], float org[3])
@@ -1075,6 +1347,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
     float dir[3], org[3];
     camera_ray(P, x, y, ox, oy, dir, org);
     float tmin = P->nearT, tmax = P->farT;
+    cone_t cone = { P->coneAperture, 0.0f };
 
     float thr[4] = { 1.0f, 1.0f, 1.0f, 1.0f };
     float rad[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
@@ -1170,7 +1443,8 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             float a = mh.bary[0], b = mh.bary[1], c = 1.0f - a - b;
             float uv[2];
             for(int k = 0; k < 2; k++) uv[k] = q[k] * a + q[2 + k] * b + q[4 + k] * c;
-            orc_tex_read(sf->texels, sf->texW, sf->texH, sf->texFormat, uv, alb);
+            if(sf->mipCount > 1u) albedo_lod(sf, tri9, uv, q, pos, nrm, dir, cone_advance(cone, t), alb);
+            else orc_tex_read(sf->texels, sf->texW, sf->texH, sf->texFormat, uv, alb);
         }
         if(S) { float c3[3] = { alb[0], alb[1], alb[2] }; orc_spec_convert_albedo(S, c3, waves, alb); }
         if(adj && J->adjTexels && sf->texels == J->adjTexels && sf->matType == ORC_MAT_LAMBERT)
@@ -1280,6 +1554,7 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
         prevPdf = bpdf;
         float nn[3] = { nrm[0], nrm[1], nrm[2] };
         if(passed) { nn[0] = -nn[0]; nn[1] = -nn[1]; nn[2] = -nn[2]; }
+        cone = cone_after_scatter(sf, backSide, cone_advance(cone, t), wo, nrm, wi);
         orc_nudge(presample, nn, org);
         memcpy(dir, wi, 12);
         tmin = 1.0e-4f;
@@ -1454,6 +1729,8 @@ void orc_pt_camera_frame(const float pos[3], const float gaze[3], const float up
     p->planeSize[1] = hh * 2.0f;
     p->nearT = nearT;
     p->farT = farT;
+    /* CameraPinhole's ray cone (CamerasDefault.hpp:80-86) */
+    p->coneAperture = 2.0f * tanf(fovY * 0.5f) / (float)p->height;
 }
 
 /* World-space light triangle from instance-space vertices (ApplyP with the
@@ -1630,6 +1907,45 @@ void orc_fx_gaussian_filter(const float* in3, float* out5, uint32_t n)
 
 /* SingleSampleSpectrumWavelength, hyperbolic mode (SpectrumContext.cu:9-130):
  * uint32 numbers in, wavelengths and pdfs out. */
+/* The ray-cone steps on the tangent surface (geometric normal +z), in the
+ * record layout of ref_cone (oracle/ref_pt_driver.cpp). */
+void orc_fx_cone(const float* in20, float* out12, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in20 + 20 * i;
+        float* o = out12 + 12 * i;
+        const cone_t c = { q[0], q[1] };
+        const cone_t adv = cone_advance(c, q[2]);
+        o[0] = adv.aperture; o[1] = adv.width;
+        cone_project(adv, q + 3, q + 6, o + 2, o + 5);
+        const float nz[3] = { 0.0f, 0.0f, 1.0f };
+        float fromEta = q[13], toEta = q[14];
+        if(q[15] != 0.0f) { const float t = fromEta; fromEta = toEta; toEta = t; }
+        cone_t back = adv, r;
+        if(refract_cone(adv, q[9], q + 10, nz, fromEta, toEta, &r)) back = r;
+        o[8] = back.aperture; o[9] = back.width;
+        const float betaN = q[9];
+        if(dot3f(q + 16, nz) > 0.0f) { o[10] = adv.aperture + 2.0f * betaN; o[11] = adv.width; }
+        else { o[10] = back.aperture - betaN; o[11] = back.width; }
+    }
+}
+
+/* Graphics::ConvertPixelIndices, as the mip generation applies it */
+void orc_fx_pixel_indices(const float* in6, float* out2, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in6 + 6 * i;
+        for(int k = 0; k < 2; k++)
+        {
+            const float ratio = q[2 + k] / q[4 + k];
+            const float r = (q[k] + 0.5f) * ratio - 0.5f;
+            out2[2 * i + k] = fminf(fmaxf(0.0f, r), q[2 + k] - 1.0f);
+        }
+    }
+}
+
 void orc_fx_sample_waves(const uint32_t* xi, float* waves4, float* pdf4, uint32_t n)
 {
     for(uint32_t i = 0; i < n; i++) orc_spec_sample_waves(to_float01(xi[i]), waves4 + 4 * i, pdf4 + 4 * i);
@@ -1748,6 +2064,7 @@ typedef struct
     float    org[3], dir[3], tmin, tmax;
     float    thr[4], rad[4], waves[4], wpdf[4];
     float    prevPdf;
+    cone_t   cone;                 /* ray cone of the current ray */
     uint32_t depth, type;          /* type 0 camera, 1 path, 2 specular */
     int      alive;
     int      hit;                  /* closest hit of this bounce */
@@ -1796,7 +2113,8 @@ static float g_mix_pdf(const orc_lobe* lobes, const float* w, float sumW, const 
 }
 
 static void g_albedo(const orc_pt_surface* sf, uint32_t localPrim, const orc_meta_hit* mh, const orc_spectral* S,
-                     const float waves[4], float alb[4])
+                     const float waves[4], const float* tri9, const float pos[3], const float nrm[3],
+                     const float dir[3], cone_t cone, float alb[4])
 {
     alb[0] = sf->albedo[0]; alb[1] = sf->albedo[1]; alb[2] = sf->albedo[2]; alb[3] = 0.0f;
     if(sf->texels)
@@ -1805,7 +2123,8 @@ static void g_albedo(const orc_pt_surface* sf, uint32_t localPrim, const orc_met
         float a = mh->bary[0], b = mh->bary[1], c = 1.0f - a - b;
         float uv[2];
         for(int k = 0; k < 2; k++) uv[k] = q[k] * a + q[2 + k] * b + q[4 + k] * c;
-        orc_tex_read(sf->texels, sf->texW, sf->texH, sf->texFormat, uv, alb);
+        if(sf->mipCount > 1u) albedo_lod(sf, tri9, uv, q, pos, nrm, dir, cone, alb);
+        else orc_tex_read(sf->texels, sf->texW, sf->texH, sf->texFormat, uv, alb);
     }
     if(S) { float c3[3] = { alb[0], alb[1], alb[2] }; orc_spec_convert_albedo(S, c3, waves, alb); }
 }
@@ -1882,7 +2201,8 @@ static void g_surface_work(const orc_scene* scene, const orc_pt_params* P, const
     const float wo[3] = { -q->dir[0], -q->dir[1], -q->dir[2] };
     const float V[3] = { dot3f(wo, tng), dot3f(wo, btg), dot3f(wo, nrm) };
     float alb[4];
-    g_albedo(sf, localPrim, &q->mh, S, q->waves, alb);
+    const cone_t cone = cone_advance(q->cone, q->tmax);
+    g_albedo(sf, localPrim, &q->mh, S, q->waves, tri9, pos, nrm, q->dir, cone, alb);
     const float specv = specularity(sf, alb, nc);
     const int isSpec = specv >= SPECULAR_THRESHOLD;
     float woW[3] = { wo[0], wo[1], wo[2] };
@@ -1986,6 +2306,7 @@ static void g_surface_work(const orc_scene* scene, const orc_pt_params* P, const
         else { float inv = 1.0f / pdfPath; for(int k = 0; k < nc; k++) pthr[k] *= inv; }
         float nn[3] = { nrm[0], nrm[1], nrm[2] };
         if(passed) { nn[0] = -nn[0]; nn[1] = -nn[1]; nn[2] = -nn[2]; }
+        q->cone = cone_after_scatter(sf, backSide, cone, wo, nrm, wdir);
         orc_nudge(orgOut, nn, q->org);
         memcpy(q->dir, wdir, 12);
         memcpy(q->thr, pthr, 16);
@@ -2114,6 +2435,8 @@ int orc_pt_render_guided(const orc_scene* s, const orc_pt_params* p, const orc_p
             filter_sample(p->filterRadius, urnd(&SC, 0, 6), urnd(&SC, 0, 7), &ox, &oy);
             camera_ray(p, x, y, ox, oy, q->dir, q->org);
             q->tmin = p->nearT; q->tmax = p->farT;
+            q->cone.aperture = p->coneAperture;
+            q->cone.width = 0.0f;
             for(int k = 0; k < 4; k++) { q->thr[k] = 1.0f; q->wpdf[k] = 1.0f; }
             if(S) orc_spec_sample_waves(urnd(&SC, 0, 9), q->waves, q->wpdf);
             q->alive = 1;

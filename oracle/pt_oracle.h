@@ -33,6 +33,7 @@ typedef struct
     uint32_t sampler;       /* 0: counter-based independent numbers, 1: ZSobol, 2: ZSobol with
                                the Owen bit order, 3: MRay's per-pixel PCG32 streams */
     uint32_t samplerMaxSpp; /* ZSobol initialMaxSampleCount (0: sampleStart + spp) */
+    float    coneAperture;  /* camera rays' cone aperture 2 tan(fovY / 2) / height (orc_pt_camera_frame) */
 } orc_pt_params;
 
 /* Per instance (surface): Lambert albedo or light, instance-space triangles
@@ -60,7 +61,20 @@ typedef struct
     const void*  texels;
     uint32_t     texW, texH, texFormat;
     const float* uvs;
+    /* the texture's mip levels 1.. (orc_gen_mips), or NULL / 1 for level 0 only */
+    const void*  mips;
+    uint32_t     mipCount;
 } orc_pt_surface;
+
+/* KCGenerateMipmaps (Source/Tracer/TextureFilter.cu:62-192, 1006-1100) with a
+ * Gaussian filter of the given radius: levels 1 .. count - 1 of a w x h
+ * texture (format 0 RGBA8, 1 RGBA f32) into out, one after another;
+ * returns the level count. */
+uint32_t orc_gen_mips(const void* texels, uint32_t w, uint32_t h, uint32_t format, float radius, void* out);
+/* levels 1 .. levels - 1 into out; the levels whose bit is set in validMask
+ * are already in out and kept (their children are filtered from them) */
+uint32_t orc_gen_mips_levels(const void* texels, uint32_t w, uint32_t h, uint32_t format, float radius,
+                             uint32_t levels, uint32_t validMask, void* out);
 
 /* Bilinear, wrap-addressed albedo read (TextureViewCPU.h:196-375, UNORM8
  * channels through NormConversion::FromUNorm). */
@@ -226,6 +240,8 @@ void orc_fx_russian_roulette(const float* in6, float* out5, uint32_t n);
 void orc_fx_tri_light(const orc_fx_light_in* in, orc_fx_light_out* out, uint32_t n);
 void orc_fx_gaussian_filter(const float* in3, float* out5, uint32_t n);
 void orc_fx_sample_waves(const uint32_t* xi, float* waves4, float* pdf4, uint32_t n);
+void orc_fx_cone(const float* in20, float* out12, uint32_t n);
+void orc_fx_pixel_indices(const float* in6, float* out2, uint32_t n);
 void orc_fx_spherical_coords(const float* in6, float* out7, uint32_t n);
 void orc_fx_camera(const float* cam13, const uint32_t res[2], const uint32_t* pix, const float* off4, float* out6,
                    uint32_t n);

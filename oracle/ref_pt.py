@@ -192,6 +192,16 @@ def guide_codes(view15, in6, rng):
     return out, r
 
 
+def cone(in20):
+    """RayCone Advance / Project, RefractRayCone and ConeAfterScatter
+    (record layout of ref_cone in ref_pt_driver.cpp)."""
+    return _rows(load().ref_cone, in20, 12)
+
+
+def pixel_indices(in6):
+    return _rows(load().ref_pixel_indices, in6, 2)
+
+
 def guide_table(codes, probe, size):
     c = np.ascontiguousarray(codes, np.uint64)
     p = np.ascontiguousarray(probe, np.uint64)

@@ -621,4 +621,56 @@ void ref_guide_table(const uint64_t* codes, uint32_t n, const uint64_t* probe, u
     for(uint32_t i = 0; i < m; i++) found[i] = v.Search(SpatioDirCode(probe[i])).value_or(0xFFFFFFFFu);
 }
 
+// Ray cones (RayCone::Advance / Project, RayConeSurface::ConeAfterScatter,
+// Source/Tracer/TracerTypes.h:323-380) and RefractMaterial::RefractRayCone
+// (MaterialsDefault.hpp:353-462) on the tangent surface (geometric normal +z).
+//   in:  aperture, width, t, f[3], d[3], betaN, wo[3], iorFront, iorBack,
+//        backSide, wi[3], 0
+//   out: advanced cone (aperture, width), a1[3], a2[3] (Project of the
+//        advanced cone), the refracted back cone, ConeAfterScatter(wi, +z)
+void ref_cone(const float* in20, float* out12, uint32_t n)
+{
+    using SC = SpectrumContextIdentity;
+    SC::Converter conv;
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in20 + 20 * i;
+        float* o = out12 + 12 * i;
+        RayCone c;
+        c.aperture = q[0];
+        c.width = q[1];
+        const RayCone adv = c.Advance(q[2]);
+        const auto ax = adv.Project(V3(q + 3), V3(q + 6));
+        o[0] = adv.aperture; o[1] = adv.width;
+        put3(o + 2, ax[0]);
+        put3(o + 5, ax[1]);
+        const float zero[3] = { 0, 0, 0 };
+        DefaultSurface surf = tangent_surface(zero, q[15] != 0.0f);
+        std::vector<Vector3> f = { Vector3(q[13], 0, 0) }, b = { Vector3(q[14], 0, 0) };
+        RefractMatDetail::RefractMatData soa{ Span<const Vector3>(f.data(), 1), Span<const Vector3>(b.data(), 1) };
+        RefractMatDetail::RefractMaterial<SC> m(conv, surf, soa, MaterialKey::CombinedKey(0, 0));
+        RayConeSurface rs;
+        rs.rayConeFront = adv;
+        rs.rayConeBack = adv;
+        rs.betaN = q[9];
+        const RayConeSurface rr = m.RefractRayCone(rs, V3(q + 10));
+        o[8] = rr.rayConeBack.aperture; o[9] = rr.rayConeBack.width;
+        const RayCone after = rr.ConeAfterScatter(V3(q + 16), Vector3(0, 0, 1));
+        o[10] = after.aperture; o[11] = after.width;
+    }
+}
+
+// Graphics::ConvertPixelIndices (GraphicsFunctions.h:527-538), 2D:
+// in: index[2], toResolution[2], fromResolution[2] -> out[2]
+void ref_pixel_indices(const float* in6, float* out2, uint32_t n)
+{
+    for(uint32_t i = 0; i < n; i++)
+    {
+        const float* q = in6 + 6 * i;
+        const Vector2 r = Graphics::ConvertPixelIndices(Vector2(q[0], q[1]), Vector2(q[2], q[3]), Vector2(q[4], q[5]));
+        out2[2 * i] = r[0];
+        out2[2 * i + 1] = r[1];
+    }
+}
+
 }  // extern "C"

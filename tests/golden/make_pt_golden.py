@@ -30,6 +30,10 @@ Covered (MRay file:line):
                  (Tracer/DistributionFunctions.h:230-380), concentric octahedral mapping
                  (Core/GraphicsFunctions.h:318-384), HashGridView GenCode /
                  GenCodeStochastic / TryInsert / Search (Tracer/HashGrid.h:230-400)
+  cone           RayCone::Advance / Project, RayConeSurface::ConeAfterScatter
+                 (Tracer/TracerTypes.h:323-380), RefractMaterial::RefractRayCone
+                 (Tracer/MaterialsDefault.hpp:353-462)
+  pix            Graphics::ConvertPixelIndices (Core/GraphicsFunctions.h:529-538)
 
 Usage: python tests/golden/make_pt_golden.py
 """
@@ -257,12 +261,41 @@ def guide(rng):
             "gt_found": found}
 
 
+def cones(rng):
+    """Ray cones: Advance, Project, the refracted cone and ConeAfterScatter,
+    on the tangent surface (normal +z), and the parent-texel lookup of the
+    mip generation."""
+    n = N
+    q = np.zeros((n, 20), np.float32)
+    q[:, 0] = rng.uniform(-0.05, 0.05, n)
+    q[:, 1] = rng.uniform(0.0, 0.2, n)
+    q[:, 2] = rng.uniform(0.0, 30.0, n)
+    q[:16, 1] = 0.0                                  # a camera cone (width 0) ...
+    q[16:32, 2] = 1e8                                # ... and widths past the clamp
+    q[:, 3:6] = unit(rng.normal(size=(n, 3)))
+    q[:, 6:9] = unit(rng.normal(size=(n, 3)))
+    q[:, 9] = rng.choice([0.0, 0.01, -0.02], n)
+    wo = rng.normal(size=(n, 3))
+    wo[:, 2] = np.abs(wo[:, 2]) * rng.choice([1.0, -1.0], n)
+    q[:, 10:13] = unit(wo)
+    q[:, 13] = 1.0
+    q[:, 14] = rng.choice([1.5, 1.33, 2.4], n)
+    q[:, 15] = rng.integers(0, 2, n)
+    q[:, 16:19] = unit(rng.normal(size=(n, 3)))
+    p = np.zeros((n, 6), np.float32)
+    fr = rng.integers(1, 512, (n, 2)).astype(np.float32)
+    p[:, 2:4] = np.maximum(1.0, np.floor(fr / 2))
+    p[:, 4:6] = fr
+    p[:, 0:2] = rng.uniform(-3.0, fr + 3.0)
+    return {"cone_in": q, "cone_out": ref_pt.cone(q), "pix_in": p, "pix_out": ref_pt.pixel_indices(p)}
+
+
 def main():
     if ref_pt.load() is None:
         sys.exit("the MRay source tree and fmt headers are needed (MRAY_REFERENCE_SRC)")
     rng = np.random.default_rng(20261204)
     out = {}
-    for f in (materials, building_blocks, lights, distributions, cameras, waves, zsobol, pcg32, guide):
+    for f in (materials, building_blocks, lights, distributions, cameras, waves, zsobol, pcg32, guide, cones):
         out.update(f(rng))
     path = os.path.join(HERE, "pt_math.npz")
     np.savez_compressed(path, **out)

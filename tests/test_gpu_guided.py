@@ -116,6 +116,18 @@ def test_guided_mixed_materials_matches_oracle():
     _check_grids(gs, os_)
 
 
+def test_guided_mipmapped_textures_match_oracle():
+    """Textured walls with mip chains: the guided shade kernel reads the
+    albedo at the ray cone's level of detail like the plain one."""
+    pt = PathTracer(0)
+    surf = load_box_scene(pt, scenes.mipmapped(scenes.box_scene_textured(0, size=128)))
+    S = oracle.PtScene(surf)
+    g, o, gs, os_ = _render_both(pt, S, 2, seed=5)
+    _check_images(g, o)
+    _check_grids(gs, os_)
+    pt.close()
+
+
 def _spectral_pair(surf, env=None):
     import os
     from mray_gb300 import spectral

@@ -246,6 +246,81 @@ def test_textured_box_per_pixel(mode):
     pt.close()
 
 
+@pytest.mark.parametrize("mode,size,dtype", [(0, 128, np.uint8), (2, 128, np.uint8), (2, 96, np.float32)])
+def test_mipmapped_textured_box_per_pixel(mode, size, dtype):
+    """Mip chains made on the device by MRay's accumulate-mode generation
+    (radius 2) on the textured walls, read at the ray cone's level of detail
+    with trilinear filtering: per pixel against the oracle's chain and cone
+    LOD, and different from the same scene read at level 0."""
+    surf = scenes.box_scene_textured(0, size=size)
+    if dtype == np.float32:
+        for s in surf:
+            if s.get("texture") is not None and s["texture"].dtype == np.uint8:
+                s["texture"] = (s["texture"].astype(np.float32) / 255.0)
+        # the loader keys textures by identity: keep the floor/left-wall share
+        surf[3]["texture"] = surf[0]["texture"]
+    scenes.mipmapped(surf)
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    g, o, frac = _compare(pt, oracle.PtScene(surf), mode)
+    print("mipmapped %s mode %d: close %.4f relMSE %.3g" % (np.dtype(dtype).name, mode, frac, relmse(g, o)))
+    assert frac >= 0.97 and relmse(g, o) <= 1e-3
+    pt.close()
+    flat = [dict(s) for s in surf]
+    for s in flat:
+        s.pop("mip_radius", None)
+    pt = PathTracer(0)
+    load_box_scene(pt, flat)
+    g0, o0, frac0 = _compare(pt, oracle.PtScene(flat), mode)
+    assert frac0 >= 0.97 and not np.allclose(g0, g, rtol=1e-3)
+    pt.close()
+
+
+@pytest.mark.parametrize("radius", [2.0, 0.0])
+def test_given_mip_levels_per_pixel(radius):
+    """Mip levels given by the caller (PushTextureData of levels > 0): kept
+    in the chain, the levels below them filtered from them (radius 2), or
+    the chain ending at the last given level (radius 0)."""
+    surf = scenes.box_scene_textured(0, size=64)
+    tex = surf[2]["texture"]
+    lv1 = np.ascontiguousarray(tex[::2, ::2])                  # a point-sampled level 1
+    lv2 = np.full((16, 16, 4), (30, 200, 90, 255), np.uint8)   # a flat green level 2
+    surf[2]["mips_given"] = {1: lv1, 2: lv2}
+    surf[2]["mip_radius"] = radius
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    g, o, frac = _compare(pt, oracle.PtScene(surf), 2, spp=8)
+    print("given mips radius %.0f: close %.4f relMSE %.3g" % (radius, frac, relmse(g, o)))
+    assert frac >= 0.97 and relmse(g, o) <= 1e-3
+    with pytest.raises(ValueError):
+        pt.set_texture_mip(1, 1, lv2)                          # wrong size for level 1
+    pt.close()
+
+
+def test_generate_mips_errors_and_drop():
+    from mray_gb300 import _native as N
+    surf = scenes.mipmapped(scenes.box_scene_textured(0, size=64))
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    with pytest.raises(N.MRGError):
+        pt.generate_mips(0, -1.0)
+    with pytest.raises(N.MRGError):
+        pt.generate_mips(0, 100.0)
+    with pytest.raises(N.MRGError):
+        pt.generate_mips(7, 2.0)
+    g, o, frac = _compare(pt, oracle.PtScene(surf), 2, spp=4)
+    assert frac >= 0.97
+    # radius 0 drops both chains: the level-0 image
+    pt.generate_mips(0, 0.0)
+    pt.generate_mips(1, 0.0)
+    flat = [dict(s) for s in surf]
+    for s in flat:
+        s.pop("mip_radius", None)
+    g0, o0, frac0 = _compare(pt, oracle.PtScene(flat), 2, spp=4)
+    assert frac0 >= 0.97 and not np.allclose(g0, g, rtol=1e-3)
+    pt.close()
+
+
 def test_borrowed_float_texture_updates():
     """A borrowed f32 device texture: rewriting it changes the next render
     exactly as the oracle with the new texels."""
@@ -276,11 +351,15 @@ def test_borrowed_float_texture_updates():
     pt.close()
 
 
-def test_c2_scene_spectral_small():
+@pytest.mark.parametrize("mips", [False, True])
+def test_c2_scene_spectral_small(mips):
     """The production scene (textured Lambert, GGX metal, glass, 8 area
-    lights, sky, 4 wavelengths) at a small film against the oracle."""
+    lights, sky, 4 wavelengths) at a small film against the oracle; with mip
+    chains the ray cones also cross the glass spheres (refracted cones)."""
     import os
     surf, cam = scenes.c2_scene(0, texture_size=256)
+    if mips:
+        scenes.mipmapped(surf)
     env = dict(texels=scenes.sky_map(128, 64, seed=0))
     pt, S = _spectral_pair(surf, env)
     g = _img(pt.render(PathTracer.params(96, 54, 4, cam, max_depth=12, rr_start=3, seed=2)))
@@ -289,7 +368,7 @@ def test_c2_scene_spectral_small():
     d = np.abs(g - o).max(axis=-1).ravel()
     keep = d <= np.quantile(d, 0.98)
     rel_kept = float(np.mean(((g - o).reshape(-1, 3)[keep]) ** 2 / (o.reshape(-1, 3)[keep] ** 2 + 1e-2)))
-    print("c2 spectral: close %.4f relMSE %.3g kept %.3g" % (close, relmse(g, o), rel_kept))
+    print("c2 spectral mips=%d: close %.4f relMSE %.3g kept %.3g" % (mips, close, relmse(g, o), rel_kept))
     assert close >= 0.95 and rel_kept <= 1e-5
     pt.close()
 

@@ -62,9 +62,11 @@ def push_surfaces(t, surfaces, camera):
                 if s.get("texture") is not None:
                     key = id(s["texture"])
                     if key not in tex:
-                        tex[key] = (t.create_texture_2d(s["texture"].shape[1], s["texture"].shape[0], 1,
+                        given = s.get("mips_given") or {}
+                        tex[key] = (t.create_texture_2d(s["texture"].shape[1], s["texture"].shape[0],
+                                                        1 + max(given, default=0),
                                                         "rgba8_unorm" if s["texture"].dtype == np.uint8
-                                                        else "rgba_float"), s["texture"])
+                                                        else "rgba_float"), s["texture"], given)
                     t.push_mat_attribute(g, r, 0, None, [tex[key][0]])
                 else:
                     t.push_mat_attribute(g, r, 0, s["albedo"], [None])
@@ -93,8 +95,10 @@ def push_surfaces(t, surfaces, camera):
     t.push_cam_attribute(cg, (cid, cid), 2, camera["pos"])
     t.push_cam_attribute(cg, (cid, cid), 3, camera["up"])
     t.commit_textures()
-    for tid, data in tex.values():
+    for tid, data, given in tex.values():
         t.push_texture_data(tid, 0, data)
+        for lv, texels in sorted(given.items()):
+            t.push_texture_data(tid, lv, texels)
     for i, s in enumerate(surfaces):
         if s["kind"] != "light":
             t.create_surface([batches[i]], [mats[i]], trans[i], [s.get("cull", True)])
@@ -151,6 +155,29 @@ def test_tracer_matches_direct_path(scene_fn):
     want = direct_render(pt, cam, 64, 48, 12, 4, seed=21)
     pt.close()
     assert film[..., 3].min() > 0
+    assert np.array_equal(film, want)
+
+
+@pytest.mark.parametrize("gen_mips", [True, False])
+def test_tracer_texture_mips_match_direct_path(gen_mips):
+    """TracerParameters::genMips (every texture's full chain, Gaussian
+    mipGenFilter of radius 1.5) and mip levels pushed by PushTextureData:
+    the tracer's film equals the direct path tracer's with the same chains."""
+    surf = _lights_unculled(scenes.box_scene_textured(0, size=64))
+    tex = surf[2]["texture"]
+    surf[2]["mips_given"] = {1: np.ascontiguousarray(tex[::2, ::2]),
+                             2: np.full((16, 16, 4), (30, 200, 90, 255), np.uint8)}
+    if gen_mips:
+        scenes.mipmapped(surf, 1.5)
+    cam = scenes.box_camera()
+    with Tracer(seed=23, gen_mips=gen_mips, mip_filter_radius=1.5) as t:
+        cs = push_surfaces(t, surf, cam)
+        t.commit_surfaces()
+        film, _ = tracer_render(t, cs, 64, 48, 8, 4)
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    want = direct_render(pt, cam, 64, 48, 8, 4, seed=23)
+    pt.close()
     assert np.array_equal(film, want)
 
 

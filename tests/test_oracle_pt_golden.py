@@ -137,6 +137,15 @@ def test_hash_grid_codes_and_table_match_mray(g):
     assert np.array_equal(slots, g["gt_slots"]) and np.array_equal(found, g["gt_found"])
 
 
+
+def test_ray_cones_match_mray(g):
+    """Advance (with its clamp), Project, the refracted back cone and
+    ConeAfterScatter's front/back choice; the parent-texel lookup of the mip
+    generation."""
+    assert same(oracle.fx_cone(g["cone_in"]), g["cone_out"])
+    assert same(oracle.fx_pixel_indices(g["pix_in"]), g["pix_out"])
+
+
 # ---- where the MRay tree is present: MRay's code run here -----------------
 
 def _ref():
@@ -159,6 +168,7 @@ def test_fixture_is_what_mray_computes(g):
     for f in lo.dtype.names:
         assert same(lo[f], g["light_out"][f]), f
     assert same(R.camera(g["cam_params"], g["cam_res"], g["cam_pix"], g["cam_off"]), g["cam_out"])
+    assert same(R.cone(g["cone_in"]), g["cone_out"])
 
 
 def test_spectral_converter_matches_mray():

@@ -215,6 +215,11 @@ def test_parameters_and_memory(cuda_lib):
         assert p.triangleTest == N.MRG_TRI_WATERTIGHT and p.filmFilterRadius == 1.5
         assert t.device_memory() == (0, 0)                       # no device use before the commit
         assert not t.context()
+    with Tracer(gen_mips=True, mip_filter_radius=3.0) as t:
+        p = t.parameters()
+        assert p.genMips == 1 and p.mipGenFilterRadius == 3.0
+    with pytest.raises(N.MRGError, match="mip generation filter"):
+        Tracer(gen_mips=True, mip_filter_radius=100.0)
 
 
 def test_scene_json_through_the_tracer(tr):
