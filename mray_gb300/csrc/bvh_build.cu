@@ -21,6 +21,7 @@
 #include <cub/device/device_scan.cuh>
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
 #include <vector>
 #include <cstring>
 
@@ -359,6 +360,103 @@ __global__ void k_bottom_up(const uint32_t* __restrict__ leafParent, const uint3
 }
 
 // ---------------------------------------------------------------------------
+// SAH-optimal collapse to 8-wide nodes (Ylitie, Karras and Laine 2017,
+// "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs",
+// section 3.1).  Bottom up over the binary tree, C(n, i) is the least SAH
+// cost of the subtree at n written as a forest of at most i roots (i = 1..8):
+//   C(n, 1) = leaf cost cPrim * P(n) * A(n) when the subtree fits a leaf
+//             child (P(n) <= maxLeaf, the collapse's leaf rule), else
+//             cNode * A(n) + D(n, 8), n as a wide node of its own;
+//   C(n, i) = min(C(n, i - 1), D(n, i)),
+//   D(n, i) = min over k of C(left, k) + C(right, i - k);
+// a binary leaf costs cPrim * A for every i.  The collapse then expands each
+// wide node's root by its recorded choices instead of greedily opening the
+// largest child.
+// ---------------------------------------------------------------------------
+struct WideCost
+{
+    float   c[8];          // C(n, i), i = 1..8
+    uint8_t split[8];      // for i >= 2: 0 = C(n, i - 1), else k of D(n, i)
+    uint32_t fullSplit;    // k of D(n, 8): the split of n opened as a wide node
+};
+
+__device__ __forceinline__ float ref_cost(const WideCost* costs, const BoxF* __restrict__ leafBoxes,
+                                          const uint32_t* __restrict__ sortedIds, uint32_t ref, int i, float cPrim)
+{
+    if(ref & kLeafBit)
+    {
+        const BoxF b = leafBoxes[sortedIds[ref & ~kLeafBit]];
+        const float dx = b.mx[0] - b.mn[0], dy = b.mx[1] - b.mn[1], dz = b.mx[2] - b.mn[2];
+        return cPrim * (dx * dy + dy * dz + dz * dx);
+    }
+    return __ldcg(&costs[ref].c[i - 1]);
+}
+
+__global__ void k_wide_cost(const uint32_t* __restrict__ leafParent, const uint32_t* __restrict__ sortedIds,
+                            const BoxF* __restrict__ leafBoxes, const BinNode* __restrict__ nodes,
+                            const BoxF* __restrict__ nodeBoxes, WideCost* costs, uint32_t* counters, int n,
+                            const uint32_t* __restrict__ firsts, const MeshSeg* __restrict__ segs, uint32_t nMesh,
+                            uint32_t maxLeaf, float cNode, float cPrim, uint32_t* errorFlag)
+{
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if(li >= n) return;
+    const uint32_t nInt = (uint32_t)(n - 1);
+    const uint32_t ml = segs ? segs[mesh_of(firsts, nMesh, (uint32_t)li)].maxLeaf : maxLeaf;
+    uint32_t p = leafParent[li];
+    for(int guard = 0; p != kNoParent; guard++)
+    {
+        if(p >= nInt || guard > n) { atomicOr(errorFlag, 1u); return; }
+        if(atomicAdd(&counters[p], 1u) == 0u) return;
+        __threadfence();
+        const uint32_t ch[2] = { nodes[p].left, nodes[p].right };
+        for(int c = 0; c < 2; c++)
+        {
+            const bool leaf = (ch[c] & kLeafBit) != 0u;
+            const uint32_t ix = ch[c] & ~kLeafBit;
+            if((leaf && ix >= (uint32_t)n) || (!leaf && ix >= nInt)) { atomicOr(errorFlag, 1u); return; }
+        }
+        float cl[8], cr[8];
+        for(int i = 0; i < 8; i++)
+        {
+            cl[i] = ref_cost(costs, leafBoxes, sortedIds, ch[0], i + 1, cPrim);
+            cr[i] = ref_cost(costs, leafBoxes, sortedIds, ch[1], i + 1, cPrim);
+        }
+        WideCost w;
+        float d[8];
+        uint8_t kd[8];
+        d[0] = __int_as_float(0x7f800000);
+        kd[0] = 0;
+        for(int i = 2; i <= 8; i++)
+        {
+            float best = __int_as_float(0x7f800000);
+            int bk = 1;
+            for(int k = 1; k < i; k++)
+            {
+                const float v = cl[k - 1] + cr[i - k - 1];
+                if(v < best) { best = v; bk = k; }
+            }
+            d[i - 1] = best;
+            kd[i - 1] = (uint8_t)bk;
+        }
+        const BoxF b = nodeBoxes[p];
+        const float dx = b.mx[0] - b.mn[0], dy = b.mx[1] - b.mn[1], dz = b.mx[2] - b.mn[2];
+        const float area = dx * dy + dy * dz + dz * dx;
+        const uint32_t cnt = nodes[p].leafCount;
+        w.c[0] = (cnt <= ml) ? cPrim * (float)cnt * area : cNode * area + d[7];
+        w.split[0] = 0;
+        for(int i = 2; i <= 8; i++)
+        {
+            if(d[i - 1] < w.c[i - 2]) { w.c[i - 1] = d[i - 1]; w.split[i - 1] = kd[i - 1]; }
+            else { w.c[i - 1] = w.c[i - 2]; w.split[i - 1] = 0; }
+        }
+        w.fullSplit = kd[7];
+        costs[p] = w;
+        __threadfence();
+        p = nodes[p].parent;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // PLOC (Meister & Bittner 2018, "Parallel Locally-Ordered Clustering for
 // Bounding Volume Hierarchy Construction"): clusters in Morton order merge
 // with their mutual nearest neighbour (smallest union surface area) inside a
@@ -463,6 +561,8 @@ struct CollapseArgs
     uint32_t*       counters;   // [0] nodes, [1] leaf payloads, [2] next-queue size, [3] error
     uint32_t        leafCount;  // leaves (payload capacity)
     uint32_t        wideCap;    // wide node / queue capacity
+    const WideCost* costs;      // SAH-optimal collapse choices (k_wide_cost), or null: greedy
+    uint32_t        sahMaxLeaf; // the choices apply to wide nodes whose leaf size is at most this
 };
 
 // Child references are validated before every dereference: a malformed tree
@@ -555,6 +655,38 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
     else
     {
         const BinNode& bn = a.nodes[root];
+        if(a.costs && maxLeaf <= a.sahMaxLeaf)
+        {
+            // expand by the recorded choices; the slots of the stack's
+            // entries sum to at most 8, so it never holds more than 8
+            uint32_t stR[8];
+            int stI[8];
+            int sp = 0;
+            const int k0 = (int)a.costs[root].fullSplit;
+            stR[sp] = bn.right; stI[sp++] = (k0 >= 1 && k0 <= 7) ? 8 - k0 : 4;
+            stR[sp] = bn.left;  stI[sp++] = (k0 >= 1 && k0 <= 7) ? k0 : 4;
+            while(sp > 0 && nc < 8)
+            {
+                const uint32_t r = stR[--sp];
+                int i = stI[sp];
+                if(!ref_ok(a, r)) break;
+                if(!(r & kLeafBit))
+                    while(i > 1 && a.costs[r].split[i - 1] == 0) i--;
+                if((r & kLeafBit) || i == 1)
+                {
+                    cand[nc] = r; ref_box(a, r, cbox[nc], ccnt[nc]); nc++;
+                    continue;
+                }
+                const int k = (int)a.costs[r].split[i - 1];
+                if(k < 1 || k >= i || sp + 2 > 8) { atomicOr(&a.counters[3], 1u); break; }
+                const BinNode& on = a.nodes[r];
+                stR[sp] = on.right; stI[sp++] = i - k;
+                stR[sp] = on.left;  stI[sp++] = k;
+            }
+            if(sp > 0) atomicOr(&a.counters[3], 1u);     // more than 8 children: a malformed table
+        }
+        else
+        {
         cand[0] = bn.left;  ref_box(a, bn.left, cbox[0], ccnt[0]);
         cand[1] = bn.right; ref_box(a, bn.right, cbox[1], ccnt[1]);
         nc = 2;
@@ -572,6 +704,7 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
             cand[best] = on.left;  ref_box(a, on.left, cbox[best], ccnt[best]);
             cand[nc] = on.right;   ref_box(a, on.right, cbox[nc], ccnt[nc]);
             nc++;
+        }
         }
     }
 
@@ -782,6 +915,45 @@ inline unsigned gridFor(uint32_t n, int tpb = kTPB) { return (unsigned)((n + tpb
 
 } // namespace
 
+namespace {
+// Collapse of the binary tree to 8-wide nodes, MRG_BVH_COLLAPSE: "sah" the
+// SAH-optimal one (k_wide_cost) everywhere, "sah-blas" for BLASes only,
+// "sah-large" only for BLASes with one triangle per leaf child, "greedy" the
+// largest-child-first expansion everywhere; the default is "sah-blas".
+// MRG_BVH_SAH_CPRIM / MRG_BVH_SAH_CINST are the costs of a triangle test and
+// of an instance entry relative to a wide node test in the SAH.
+enum { kCollapseGreedy = 0, kCollapseSah = 1, kCollapseSahBlas = 2, kCollapseSahLarge = 3 };
+int collapse_mode()
+{
+    const char* v = std::getenv("MRG_BVH_COLLAPSE");
+    if(!v) return kCollapseSahBlas;
+    if(std::strcmp(v, "greedy") == 0) return kCollapseGreedy;
+    if(std::strcmp(v, "sah-blas") == 0) return kCollapseSahBlas;
+    if(std::strcmp(v, "sah-large") == 0) return kCollapseSahLarge;
+    return kCollapseSah;
+}
+// the SAH collapse applies to wide nodes whose leaf size is at most this
+uint32_t sah_max_leaf(bool tlas)
+{
+    switch(collapse_mode())
+    {
+        case kCollapseSah: return 3u;
+        case kCollapseSahBlas: return tlas ? 0u : 3u;
+        case kCollapseSahLarge: return tlas ? 0u : 1u;
+        default: return 0u;
+    }
+}
+float env_cost(const char* name, float dflt)
+{
+    const char* v = std::getenv(name);
+    const float c = v ? (float)std::atof(v) : dflt;
+    return (c > 0.0f && c < 1000.0f) ? c : dflt;
+}
+float sah_cprim() { return env_cost("MRG_BVH_SAH_CPRIM", 1.0f); }
+// an instance entry (transform and a BLAS root) against a node test, for the TLAS
+float sah_cinst() { return env_cost("MRG_BVH_SAH_CINST", 8.0f); }
+} // namespace
+
 bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std::string& err)
 {
     const uint32_t n = in.count;
@@ -791,7 +963,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     BoxF* dLeafBoxes = nullptr; float* dCent = nullptr; uint32_t* dCB = nullptr;
     uint64_t* dCodes[2] = { nullptr, nullptr }; uint32_t* dIds[2] = { nullptr, nullptr };
     void* dTemp = nullptr; size_t tempBytes = 0;
-    BinNode* dNodes = nullptr; BoxF* dNodeBoxes = nullptr; uint32_t* dLeafParent = nullptr;
+    BinNode* dNodes = nullptr; BoxF* dNodeBoxes = nullptr; uint32_t* dLeafParent = nullptr; WideCost* dCosts = nullptr;
     uint32_t* dCnt = nullptr; uint4* dQ[2] = { nullptr, nullptr };
     uint32_t* dCounters = nullptr;
     WideNode* dW = nullptr;
@@ -904,6 +1076,15 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
         k_bottom_up<<<gridFor(n), kTPB, 0, st>>>(dLeafParent, vb.Current(), dLeafBoxes, dNodes,
                                                  dNodeBoxes, dCnt, (int)n, dCounters + 3);
         MRG_CK(cudaGetLastError());
+        if(in.maxLeaf <= sah_max_leaf(in.kind == 1))
+        {
+            MRG_CK(cudaMallocAsync(&dCosts, sizeof(WideCost) * nInt, st));
+            MRG_CK(cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * nInt, st));
+            k_wide_cost<<<gridFor(n), kTPB, 0, st>>>(dLeafParent, vb.Current(), dLeafBoxes, dNodes, dNodeBoxes,
+                                                     dCosts, dCnt, (int)n, nullptr, nullptr, 0u, in.maxLeaf, 1.0f,
+                                                     in.kind == 1 ? sah_cinst() : sah_cprim(), dCounters + 3);
+            MRG_CK(cudaGetLastError());
+        }
         MRG_CK(cudaMemcpyAsync(&rootBox, dNodeBoxes, sizeof(BoxF), cudaMemcpyDeviceToHost, st));
         rootItem = make_uint4(0u, 0u, 0u, 0u);
     }
@@ -934,6 +1115,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     ca.inflate = ext * 1.0e-5f + 1.0e-30f;
     ca.wnodes = dW; ca.tris = out.tris; ca.leafIds = out.leafIds; ca.counters = dCounters;
     ca.leafCount = n; ca.wideCap = wideCap;
+    ca.costs = dCosts; ca.sahMaxLeaf = dCosts ? 3u : 0u;
 
     hostCounters[0] = 1; hostCounters[1] = 0; hostCounters[2] = 0; hostCounters[3] = 0;
     MRG_CK(cudaMemcpyAsync(dCounters, hostCounters, sizeof(hostCounters), cudaMemcpyHostToDevice, st));
@@ -962,7 +1144,7 @@ bool build_wide_bvh(const BuildInput& in, BuildResult& out, cudaStream_t st, std
     cudaFreeAsync(dIds[0], st); cudaFreeAsync(dIds[1], st); cudaFreeAsync(dTemp, st);
     cudaFreeAsync(dNodes, st); cudaFreeAsync(dNodeBoxes, st); cudaFreeAsync(dLeafParent, st);
     cudaFreeAsync(dCnt, st); cudaFreeAsync(dQ[0], st); cudaFreeAsync(dQ[1], st);
-    cudaFreeAsync(dCounters, st); cudaFreeAsync(dW, st);
+    cudaFreeAsync(dCounters, st); cudaFreeAsync(dW, st); cudaFreeAsync(dCosts, st);
     if(cudaStreamSynchronize(st) != cudaSuccess) { err = "stream sync failed"; return false; }
     return true;
 
@@ -971,7 +1153,7 @@ fail:
     cudaFree(dLeafBoxes); cudaFree(dCent); cudaFree(dCB); cudaFree(dCodes[0]); cudaFree(dCodes[1]);
     cudaFree(dIds[0]); cudaFree(dIds[1]); cudaFree(dTemp); cudaFree(dNodes); cudaFree(dNodeBoxes);
     cudaFree(dLeafParent); cudaFree(dCnt); cudaFree(dQ[0]); cudaFree(dQ[1]); cudaFree(dCounters);
-    cudaFree(dW); cudaFree(out.nodes); cudaFree(out.tris); cudaFree(out.leafIds);
+    cudaFree(dW); cudaFree(dCosts); cudaFree(out.nodes); cudaFree(out.tris); cudaFree(out.leafIds);
     out = BuildResult{};
     return false;
 }
@@ -1009,7 +1191,7 @@ bool build_wide_bvh_batch(const std::vector<BatchMeshInput>& meshes, BatchResult
     BoxF* dLeafBoxes = nullptr; float* dCent = nullptr;
     uint64_t* dCodes[2] = { nullptr, nullptr }; uint32_t* dIds[2] = { nullptr, nullptr };
     void* dTemp = nullptr; size_t tempBytes = 0;
-    BinNode* dNodes = nullptr; BoxF* dNodeBoxes = nullptr; uint32_t* dLeafParent = nullptr;
+    BinNode* dNodes = nullptr; BoxF* dNodeBoxes = nullptr; uint32_t* dLeafParent = nullptr; WideCost* dCosts = nullptr;
     uint32_t* dCnt = nullptr; uint4* dQ[2] = { nullptr, nullptr };
     uint32_t* dCounters = nullptr; uint32_t* dMeshRoot = nullptr; BoxF* dMeshBoxes = nullptr;
     WideNode* dW = nullptr;
@@ -1074,6 +1256,15 @@ bool build_wide_bvh_batch(const std::vector<BatchMeshInput>& meshes, BatchResult
         k_bottom_up<<<gridFor(n), kTPB, 0, st>>>(dLeafParent, vb.Current(), dLeafBoxes, dNodes,
                                                  dNodeBoxes, dCnt, (int)n, dCounters + 3);
         MRG_CK(cudaGetLastError());
+        if(sah_max_leaf(false) > 0u)
+        {
+            MRG_CK(cudaMallocAsync(&dCosts, sizeof(WideCost) * nInt, st));
+            MRG_CK(cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * nInt, st));
+            k_wide_cost<<<gridFor(n), kTPB, 0, st>>>(dLeafParent, vb.Current(), dLeafBoxes, dNodes, dNodeBoxes,
+                                                     dCosts, dCnt, (int)n, dFirsts, dSegs, M, 3u, 1.0f,
+                                                     sah_cprim(), dCounters + 3);
+            MRG_CK(cudaGetLastError());
+        }
     }
     k_mesh_boxes<<<gridFor(M), kTPB, 0, st>>>(dMeshRoot, M, dNodeBoxes, dLeafBoxes, vb.Current(), n, dMeshBoxes,
                                               dCounters + 3);
@@ -1111,6 +1302,7 @@ bool build_wide_bvh_batch(const std::vector<BatchMeshInput>& meshes, BatchResult
     ca.primKeyBase = 0; ca.kind = 0; ca.maxLeaf = 3; ca.inflate = 0.0f; ca.rawVerts = 0u;
     ca.wnodes = dW; ca.tris = out.tris; ca.leafIds = nullptr; ca.counters = dCounters;
     ca.leafCount = n; ca.wideCap = wideCap;
+    ca.costs = dCosts; ca.sahMaxLeaf = sah_max_leaf(false);
     hostCounters[0] = M; hostCounters[1] = 0; hostCounters[2] = 0; hostCounters[3] = 0;
     MRG_CK(cudaMemcpyAsync(dCounters, hostCounters, sizeof(hostCounters), cudaMemcpyHostToDevice, st));
     for(int level = 0; qn > 0; level++)
@@ -1139,6 +1331,7 @@ bool build_wide_bvh_batch(const std::vector<BatchMeshInput>& meshes, BatchResult
     cudaFreeAsync(dNodes, st); cudaFreeAsync(dNodeBoxes, st); cudaFreeAsync(dLeafParent, st);
     cudaFreeAsync(dCnt, st); cudaFreeAsync(dQ[0], st); cudaFreeAsync(dQ[1], st);
     cudaFreeAsync(dCounters, st); cudaFreeAsync(dMeshRoot, st); cudaFreeAsync(dMeshBoxes, st); cudaFreeAsync(dW, st);
+    cudaFreeAsync(dCosts, st);
     if(cudaStreamSynchronize(st) != cudaSuccess) { err = "stream sync failed"; return false; }
     return true;
 
@@ -1148,7 +1341,7 @@ fail:
     cudaFree(dLeafBoxes); cudaFree(dCent); cudaFree(dCodes[0]); cudaFree(dCodes[1]);
     cudaFree(dIds[0]); cudaFree(dIds[1]); cudaFree(dTemp); cudaFree(dNodes); cudaFree(dNodeBoxes);
     cudaFree(dLeafParent); cudaFree(dCnt); cudaFree(dQ[0]); cudaFree(dQ[1]); cudaFree(dCounters);
-    cudaFree(dMeshRoot); cudaFree(dMeshBoxes); cudaFree(dW); cudaFree(out.nodes); cudaFree(out.tris);
+    cudaFree(dMeshRoot); cudaFree(dMeshBoxes); cudaFree(dW); cudaFree(dCosts); cudaFree(out.nodes); cudaFree(out.tris);
     out = BatchResult{};
     return false;
 }
