@@ -364,9 +364,9 @@ __global__ void k_bottom_up(const uint32_t* __restrict__ leafParent, const uint3
 // "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs",
 // section 3.1).  Bottom up over the binary tree, C(n, i) is the least SAH
 // cost of the subtree at n written as a forest of at most i roots (i = 1..8):
-//   C(n, 1) = leaf cost cPrim * P(n) * A(n) when the subtree fits a leaf
-//             child (P(n) <= maxLeaf, the collapse's leaf rule), else
-//             cNode * A(n) + D(n, 8), n as a wide node of its own;
+//   C(n, 1) = min(leaf cost cPrim * P(n) * A(n) where the subtree fits a
+//             leaf child (P(n) <= maxLeaf), cNode * A(n) + D(n, 8): n as a
+//             wide node of its own);
 //   C(n, i) = min(C(n, i - 1), D(n, i)),
 //   D(n, i) = min over k of C(left, k) + C(right, i - k);
 // a binary leaf costs cPrim * A for every i.  The collapse then expands each
@@ -378,6 +378,7 @@ struct WideCost
     float   c[8];          // C(n, i), i = 1..8
     uint8_t split[8];      // for i >= 2: 0 = C(n, i - 1), else k of D(n, i)
     uint32_t fullSplit;    // k of D(n, 8): the split of n opened as a wide node
+    uint32_t asLeaf;       // 1: n is a leaf child (it fits one and that is cheaper)
 };
 
 __device__ __forceinline__ float ref_cost(const WideCost* costs, const BoxF* __restrict__ leafBoxes,
@@ -442,7 +443,10 @@ __global__ void k_wide_cost(const uint32_t* __restrict__ leafParent, const uint3
         const float dx = b.mx[0] - b.mn[0], dy = b.mx[1] - b.mn[1], dz = b.mx[2] - b.mn[2];
         const float area = dx * dy + dy * dz + dz * dx;
         const uint32_t cnt = nodes[p].leafCount;
-        w.c[0] = (cnt <= ml) ? cPrim * (float)cnt * area : cNode * area + d[7];
+        const float cInt = cNode * area + d[7];
+        const float cLeaf = cPrim * (float)cnt * area;
+        w.asLeaf = (cnt <= ml && cLeaf <= cInt) ? 1u : 0u;
+        w.c[0] = w.asLeaf ? cLeaf : cInt;
         w.split[0] = 0;
         for(int i = 2; i <= 8; i++)
         {
@@ -648,14 +652,23 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
     int nc = 0;
     BoxF nbox; uint32_t ncnt;
     ref_box(a, root, nbox, ncnt);
-    if((root & kLeafBit) || ncnt <= maxLeaf)
+    const bool sah = a.costs && maxLeaf <= a.sahMaxLeaf;
+    // a child that fits a leaf is one, unless the SAH chose to open it
+    auto as_leaf = [&](uint32_t ref, uint32_t cnt) -> bool
+    {
+        if(ref & kLeafBit) return true;
+        if(cnt > maxLeaf) return false;
+        if(!sah || !ref_ok(a, ref)) return true;
+        return a.costs[ref].asLeaf != 0u;
+    };
+    if(as_leaf(root, ncnt))
     {
         cand[0] = root; cbox[0] = nbox; ccnt[0] = ncnt; nc = 1;
     }
     else
     {
         const BinNode& bn = a.nodes[root];
-        if(a.costs && maxLeaf <= a.sahMaxLeaf)
+        if(sah)
         {
             // expand by the recorded choices; the slots of the stack's
             // entries sum to at most 8, so it never holds more than 8
@@ -778,7 +791,7 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
     uint32_t numInternal = 0, numPayload = 0;
     for(int c = 0; c < nc; c++)
     {
-        bool leaf = (cand[c] & kLeafBit) || ccnt[c] <= maxLeaf;
+        bool leaf = as_leaf(cand[c], ccnt[c]);
         if(leaf) numPayload += ccnt[c]; else numInternal++;
     }
     uint32_t childBase = numInternal ? atomicAdd(&a.counters[0], numInternal) : 0u;
@@ -830,7 +843,7 @@ __global__ void k_collapse(CollapseArgs a, const uint4* __restrict__ queue, uint
             qhi[k][s] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
 #endif
         }
-        bool leaf = (cand[c] & kLeafBit) || ccnt[c] <= maxLeaf;
+        bool leaf = as_leaf(cand[c], ccnt[c]);
         if(!leaf)
         {
             imask |= 1u << s;
