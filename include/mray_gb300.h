@@ -329,6 +329,15 @@ mrg_status mrg_pt_add_texture(mrg_ctx* ctx, uint32_t width, uint32_t height, uin
 /* The instance's albedo comes from the texture at the hit's interpolated uv
  * (its mesh needs uvs); texture_id = 0xFFFFFFFF returns to the constant. */
 mrg_status mrg_pt_set_albedo_texture(mrg_ctx* ctx, uint32_t instance_id, uint32_t texture_id);
+/* Unreal's texturable parameters (UnrealMatData's roughness, metallic and
+ * specular ParamVaryingData, Source/Tracer/MaterialsDefault.h:151-160; read in
+ * UnrealMaterial's constructor, MaterialsDefault.hpp:521-533): each texture's
+ * first channel at the hit's uv (RGBA8: v / 255), read like the albedo
+ * (level 0, or the ray cone's level when the texture has a mip chain),
+ * replaces the instance's constant.  0xFFFFFFFF keeps the constant; the mesh
+ * needs uvs; instances of other materials ignore them. */
+mrg_status mrg_pt_set_unreal_textures(mrg_ctx* ctx, uint32_t instance_id, uint32_t roughness_texture,
+                                      uint32_t metallic_texture, uint32_t specular_texture);
 /* A mip chain for a texture (TextureMemory::GenerateMipmaps with the tracer's
  * mipGenFilter, Source/Tracer/TextureMemory.cpp:491-525,
  * TextureFilter.cu:124-192, 1006-1100): every level down to 1 x 1, each texel

@@ -36,7 +36,7 @@ EXPORTED = [
     "mrg_cache_create", "mrg_cache_query", "mrg_cache_train", "mrg_cache_get_params", "mrg_cache_set_params",
     "mrg_cache_gradients", "mrg_pt_render_cached",
     "mrg_guide_defaults", "mrg_guide_create", "mrg_guide_clear", "mrg_guide_destroy", "mrg_guide_stats",
-    "mrg_guide_read", "mrg_pt_render_guided", "mrg_pt_generate_mips", "mrg_pt_set_texture_mip",
+    "mrg_guide_read", "mrg_pt_render_guided", "mrg_pt_generate_mips", "mrg_pt_set_texture_mip", "mrg_pt_set_unreal_textures",
 ]
 
 MRG_MAT_LAMBERT, MRG_MAT_REFLECT, MRG_MAT_REFRACT, MRG_MAT_UNREAL = 0, 1, 2, 3
@@ -196,6 +196,7 @@ def _declare(lib):
         "mrg_pt_set_albedo_texture": (C.c_int, [vp, u32, u32]),
         "mrg_pt_generate_mips": (C.c_int, [vp, u32, C.c_float]),
         "mrg_pt_set_texture_mip": (C.c_int, [vp, u32, u32, vp]),
+        "mrg_pt_set_unreal_textures": (C.c_int, [vp, u32, u32, u32, u32]),
         "mrg_pt_adjoint": (C.c_int, [vp, C.POINTER(MrgPtParams), u32, vp, vp, vp, vp, vp]),
         "mrg_zsobol_seeds": (C.c_int, [u32, u32, C.c_uint64, vp]),
         "mrg_zsobol_generate": (C.c_int, [u32, u32, vp, u32, u32, u32, C.c_uint64, u32, vp, vp]),

@@ -305,7 +305,7 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
             }
             else if(surfIdx < T.nSurfaces)
             {
-                const PtSurface sf = T.surfaces[surfIdx];
+                PtSurface sf = T.surfaces[surfIdx];
                 const uint32_t gprim = hk.x;
                 const float2 mh = P.meta[i];
                 float3 pos, gn;
@@ -321,6 +321,7 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                 const float2 cn = P.cone[i];
                 const Cone cone = cone_advance(Cone{ cn.x, cn.y }, r1.w);
                 const float3 a3 = surface_albedo_cone(T, sf, gprim, mh, pos, nrm, dir, cone);
+                unreal_params_cone(T, sf, gprim, mh, pos, nrm, dir, cone);
                 const Chan alb = albedo_of<SPEC>(L.spec, a3.x, a3.y, a3.z, waves);
                 const float specv = specularity<NC>(sf, alb);
                 const bool isSpec = specv >= kSpecularThreshold;

@@ -82,6 +82,7 @@ struct mrg_ctx
         float    radiance[3] = { 0, 0, 0 };
         uint32_t twoSided = 0;
         uint32_t texture = 0;         // albedo texture id + 1 (0: constant albedo)
+        uint32_t paramTex[3] = { 0, 0, 0 };  // Unreal roughness / metallic / specular texture id + 1
     };
     struct PtTextureDesc
     {

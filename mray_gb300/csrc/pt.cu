@@ -112,7 +112,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
             {
                 const float4 r0 = P.rays[2 * (size_t)i], r1 = P.rays[2 * (size_t)i + 1];
                 const float3 org = f3(r0), dir = f3(r1);
-                const PtSurface sf = surfaces[surfIdx];
+                PtSurface sf = surfaces[surfIdx];
                 const uint32_t gprim = hk.x;
                 const uint32_t localPrim = gprim - sf.info.z;
                 const float2 mh = P.meta[i];
@@ -186,6 +186,7 @@ k_shade(PtLaunch L, PtPaths P, PtSceneTables T,
                     const float2 cn = P.cone[i];
                     const Cone cone = cone_advance(Cone{ cn.x, cn.y }, r1.w);
                     const float3 a3 = surface_albedo_cone(T, sf, gprim, mh, pos, nrm, dir, cone);
+                    unreal_params_cone(T, sf, gprim, mh, pos, nrm, dir, cone);
                     const Chan alb = albedo_of<SPEC>(L.spec, a3.x, a3.y, a3.z, waves);
                     if(ADJ && L.adj.texIndex != 0u && sf.tex.x == L.adj.texIndex && sf.info.w == kMatLambert &&
                        T.uvs != nullptr && gprim < nTris)

@@ -303,10 +303,11 @@ mrg_status pt_prepare(mrg_ctx* c)
         s.albedo = make_float4(d.albedo[0], d.albedo[1], d.albedo[2], d.roughness);
         s.mat = make_float4(d.metallic, d.specular, d.iorFront, d.iorBack);
         s.info = make_uint4(d.kind == 2 ? 1u : 0u, (uint32_t)lights.size(), mesh.primKeyBase, d.material);
-        s.tex = make_uint4(d.kind == 1 ? d.texture : 0u, 0u, 0u, 0u);
-        if(s.tex.x && mesh.uv.empty())
+        s.tex = d.kind == 1 ? make_uint4(d.texture, d.paramTex[0], d.paramTex[1], d.paramTex[2])
+                            : make_uint4(0u, 0u, 0u, 0u);
+        if((s.tex.x | s.tex.y | s.tex.z | s.tex.w) && mesh.uv.empty())
             return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt: instance " + std::to_string(i) +
-                                  " has an albedo texture but its mesh has no uvs");
+                                  " has a texture but its mesh has no uvs");
         if(d.kind == 2)
         {
             const uint32_t nt = (uint32_t)(mesh.idx.size() / 3);
@@ -660,6 +661,21 @@ mrg_status mrg_pt_set_texture_mip(mrg_ctx* c, uint32_t texId, uint32_t level, co
     if(t.given.size() < full) t.given.resize(full);
     const uint8_t* b = static_cast<const uint8_t*>(texels);
     t.given[level].assign(b, b + bytes);
+    c->ptDirty = true;
+    return MRG_OK;
+}
+
+mrg_status mrg_pt_set_unreal_textures(mrg_ctx* c, uint32_t inst, uint32_t roughnessTex, uint32_t metallicTex,
+                                      uint32_t specularTex)
+{
+    if(!c) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_unreal_textures: null context");
+    if(inst >= c->insts.size()) return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_unreal_textures: bad instance");
+    const uint32_t ids[3] = { roughnessTex, metallicTex, specularTex };
+    for(uint32_t id : ids)
+        if(id != 0xFFFFFFFFu && id >= c->ptTextures.size())
+            return mrg::set_error(MRG_ERR_INVALID_ARG, "mrg_pt_set_unreal_textures: bad texture id");
+    if(c->ptDesc.size() < c->insts.size()) c->ptDesc.resize(c->insts.size());
+    for(int k = 0; k < 3; k++) c->ptDesc[inst].paramTex[k] = (ids[k] == 0xFFFFFFFFu) ? 0u : ids[k] + 1u;
     c->ptDirty = true;
     return MRG_OK;
 }

@@ -1008,10 +1008,10 @@ __device__ __forceinline__ float3 surface_albedo(const PtSceneTables& T, const P
 // normal facing the ray, d: the ray's direction) and the uv gradients along
 // its axes.  The triangle's corner and edges go to world space with the
 // instance transform (edges by its linear part).
-__device__ __forceinline__ float3 albedo_lod(const PtSceneTables& T, const PtSurface& sf, uint32_t gprim, float2 uv,
-                                          float3 pos, float3 f, float3 d, Cone cone)
+__device__ __forceinline__ float3 tex_lod(const PtSceneTables& T, const PtSurface& sf, uint32_t texIdx, uint32_t gprim,
+                                       float2 uv, float3 pos, float3 f, float3 d, Cone cone)
 {
-    const PtTexture tx = T.textures[sf.tex.x - 1u];
+    const PtTexture tx = T.textures[texIdx - 1u];
     const float4 v0 = T.tris[3 * (size_t)gprim], e0 = T.tris[3 * (size_t)gprim + 1], e1 = T.tris[3 * (size_t)gprim + 2];
     float3 P0, E0, E1;
     P0.x = add(add(add(mul(sf.m[0].x, v0.x), mul(sf.m[0].y, v0.y)), mul(sf.m[0].z, v0.z)), sf.m[0].w);
@@ -1032,14 +1032,38 @@ __device__ __forceinline__ float3 albedo_lod(const PtSceneTables& T, const PtSur
     return tex_read_grad(tx, uv.x, uv.y, dpdx, dpdy);
 }
 
+// A texture (index + 1) at the hit's uv: level 0, or the cone's level of a
+// mip-mapped one; dflt without a texture or uvs.
+__device__ __forceinline__ float3 surface_tex_cone(const PtSceneTables& T, const PtSurface& sf, uint32_t texIdx,
+                                                   uint32_t gprim, float2 mh, float3 pos, float3 f, float3 d, Cone cone,
+                                                   float3 dflt)
+{
+    if(texIdx == 0u || T.uvs == nullptr || gprim >= T.nTris) return dflt;
+    const float2 uv = surface_uv(T, gprim, mh);
+    const PtTexture& tx = T.textures[texIdx - 1u];
+    if(tx.mipCount <= 1u) return tex_read(tx, uv.x, uv.y);
+    return tex_lod(T, sf, texIdx, gprim, uv, pos, f, d, cone);
+}
+
 __device__ __forceinline__ float3 surface_albedo_cone(const PtSceneTables& T, const PtSurface& sf, uint32_t gprim,
                                                       float2 mh, float3 pos, float3 f, float3 d, Cone cone)
 {
-    if(sf.tex.x == 0u || T.uvs == nullptr || gprim >= T.nTris) return make_float3(sf.albedo.x, sf.albedo.y, sf.albedo.z);
-    const float2 uv = surface_uv(T, gprim, mh);
-    const PtTexture& tx = T.textures[sf.tex.x - 1u];
-    if(tx.mipCount <= 1u) return tex_read(tx, uv.x, uv.y);
-    return albedo_lod(T, sf, gprim, uv, pos, f, d, cone);
+    return surface_tex_cone(T, sf, sf.tex.x, gprim, mh, pos, f, d, cone,
+                            make_float3(sf.albedo.x, sf.albedo.y, sf.albedo.z));
+}
+
+// Unreal's texturable roughness, metallic and specular (UnrealMaterial's
+// constructor reads each ParamVaryingData<2, Float> at the surface's uv and
+// cone gradients, MaterialsDefault.hpp:521-533): the first channel of the
+// texture, read like the albedo, replaces the constant in the hit's copy of
+// the surface.
+__device__ __forceinline__ void unreal_params_cone(const PtSceneTables& T, PtSurface& sf, uint32_t gprim, float2 mh,
+                                                   float3 pos, float3 f, float3 d, Cone cone)
+{
+    if(sf.info.w != kMatUnreal || (sf.tex.y | sf.tex.z | sf.tex.w) == 0u) return;
+    if(sf.tex.y) sf.albedo.w = surface_tex_cone(T, sf, sf.tex.y, gprim, mh, pos, f, d, cone, make_float3(0, 0, 0)).x;
+    if(sf.tex.z) sf.mat.x = surface_tex_cone(T, sf, sf.tex.z, gprim, mh, pos, f, d, cone, make_float3(0, 0, 0)).x;
+    if(sf.tex.w) sf.mat.y = surface_tex_cone(T, sf, sf.tex.w, gprim, mh, pos, f, d, cone, make_float3(0, 0, 0)).x;
 }
 
 // The cone a scattered ray leaves with (RefractRayCone, then

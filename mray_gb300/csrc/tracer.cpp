@@ -543,7 +543,7 @@ mrg_status pt_texture(mrg_tracer* t, uint32_t tid, uint32_t& ptId)
 }
 
 // A surface material as the path tracer's description.
-mrg_status material_of(mrg_tracer* t, uint32_t mid, mrg_pt_material& m, uint32_t& albedoTex)
+mrg_status material_of(mrg_tracer* t, uint32_t mid, mrg_pt_material& m, uint32_t& albedoTex, uint32_t paramTex[3])
 {
     Group* g;
     uint32_t k;
@@ -559,6 +559,7 @@ mrg_status material_of(mrg_tracer* t, uint32_t mid, mrg_pt_material& m, uint32_t
     m.specular = 0.5f;
     m.iorFront = 1.0f; m.iorBack = 1.5f;
     albedoTex = 0;
+    paramTex[0] = paramTex[1] = paramTex[2] = 0;
     auto vec3 = [&](uint32_t a, float* o) { std::memcpy(o, g->data[a].data() + (size_t)k * 12, 12); };
     if(td.code == MRG_MAT_LAMBERT || td.code == MRG_MAT_UNREAL)
     {
@@ -568,11 +569,13 @@ mrg_status material_of(mrg_tracer* t, uint32_t mid, mrg_pt_material& m, uint32_t
     }
     if(td.code == MRG_MAT_UNREAL)
     {
-        for(uint32_t a = 2; a < 5; a++)
-            if(g->tex[a][k]) return err(std::string(td.name) + ": textured \"" + td.attrs[a].name + "\" is not supported");
-        m.roughness = value<float>(*g, 2, k);
-        m.specular = value<float>(*g, 3, k);
-        m.metallic = value<float>(*g, 4, k);
+        // roughness, specular, metallic: a texture (its first channel) or the constant
+        m.roughness = g->tex[2][k] ? 0.0f : value<float>(*g, 2, k);
+        m.specular = g->tex[3][k] ? 0.0f : value<float>(*g, 3, k);
+        m.metallic = g->tex[4][k] ? 0.0f : value<float>(*g, 4, k);
+        paramTex[0] = g->tex[2][k];
+        paramTex[1] = g->tex[4][k];
+        paramTex[2] = g->tex[3][k];
     }
     if(td.code == MRG_MAT_REFRACT)
     {
@@ -677,10 +680,10 @@ mrg_status commit_surfaces(mrg_tracer* t, mrg_tracer_commit_result* out)
         if((s = transform_of(t, sf.transformId, m)) != MRG_OK) return s;
         for(uint32_t j = 0; j < sf.count; j++)
         {
-            uint32_t mesh, tex;
+            uint32_t mesh, tex, ptex[3];
             mrg_pt_material mat;
             if((s = batch_mesh(t, sf.primBatches[j], mesh)) != MRG_OK) return s;
-            if((s = material_of(t, sf.materials[j], mat, tex)) != MRG_OK) return s;
+            if((s = material_of(t, sf.materials[j], mat, tex, ptex)) != MRG_OK) return s;
             uint32_t id;
             if((s = mrg_add_instance(t->ctx, mesh, m, sf.cullFace[j] ? MRG_INSTANCE_CULL_BACKFACE : 0u,
                                      sf.materials[j], inst, inst, &id)) != MRG_OK)
@@ -691,6 +694,13 @@ mrg_status commit_surfaces(mrg_tracer* t, mrg_tracer_commit_result* out)
                 uint32_t pid;
                 if((s = pt_texture(t, tex, pid)) != MRG_OK) return s;
                 if((s = mrg_pt_set_albedo_texture(t->ctx, id, pid)) != MRG_OK) return s;
+            }
+            if(ptex[0] | ptex[1] | ptex[2])
+            {
+                uint32_t pid[3] = { 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu };
+                for(int q = 0; q < 3; q++)
+                    if(ptex[q] && (s = pt_texture(t, ptex[q], pid[q])) != MRG_OK) return s;
+                if((s = mrg_pt_set_unreal_textures(t->ctx, id, pid[0], pid[1], pid[2])) != MRG_OK) return s;
             }
             inst++;
         }

@@ -116,6 +116,12 @@ class PathTracer:
                              % (level, w, h, max(h >> level, 1), max(w >> level, 1), np.dtype(dt).name))
         N.check(N.lib().mrg_pt_set_texture_mip(self.acc._h, tex_id, level, a.ctypes.data_as(C.c_void_p)))
 
+    def set_unreal_textures(self, inst, roughness=None, metallic=None, specular=None):
+        """Textured roughness / metallic / specular of an Unreal instance
+        (texture ids; None keeps the constant)."""
+        ids = [0xFFFFFFFF if t is None else t for t in (roughness, metallic, specular)]
+        N.check(N.lib().mrg_pt_set_unreal_textures(self.acc._h, inst, *ids))
+
     def set_albedo_texture(self, inst, tex_id):
         N.check(N.lib().mrg_pt_set_albedo_texture(self.acc._h, inst, 0xFFFFFFFF if tex_id is None else tex_id))
 
@@ -278,5 +284,18 @@ def load_box_scene(pt, seed=0):
                     for lv, texels in sorted(s.get("mips_given", {}).items()):
                         pt.set_texture_mip(textures[key], lv, texels)
                 pt.set_albedo_texture(inst, textures[key])
+            params = [s.get(k + "_texture") for k in ("roughness", "metallic", "specular")]
+            if any(t is not None for t in params):
+                ids = []
+                for t in params:
+                    if t is None:
+                        ids.append(None)
+                        continue
+                    if id(t) not in textures:
+                        textures[id(t)] = pt.add_texture(t)
+                        if s.get("mip_radius"):
+                            pt.generate_mips(textures[id(t)], s["mip_radius"])
+                    ids.append(textures[id(t)])
+                pt.set_unreal_textures(inst, *ids)
     pt.build()
     return surf

@@ -264,6 +264,20 @@ def box_scene_textured(seed=0, size=256):
     return s
 
 
+def box_scene_unreal_textured(seed=0, size=64):
+    """The textured box with its back wall and floor made Unreal (GGX) with
+    textured roughness, metallic and specular (RGBA8 noise, first channel
+    used) beside their textured albedos."""
+    s = box_scene_textured(seed, size)
+    rough = value_noise_texture(size, seed + 7, base=0.05, span=0.6)
+    metal = value_noise_texture(size, seed + 8, base=0.0, span=1.0)
+    spec = value_noise_texture(size, seed + 9, base=0.2, span=0.6)
+    for k in (0, 2):
+        s[k].update(material="unreal", roughness=0.3, metallic=0.2, specular=0.5, roughness_texture=rough,
+                    metallic_texture=metal, specular_texture=spec)
+    return s
+
+
 def mipmapped(surf, radius=2.0):
     """Marks every textured surface's texture for a mip chain of the given
     filter radius (MRay's texture-load option, read at the ray cone's level

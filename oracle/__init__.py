@@ -310,13 +310,17 @@ class PtParams(C.Structure):
                 ("coneAperture", C.c_float)]
 
 
+class PtTex(C.Structure):
+    _fields_ = [("texels", vp), ("w", u32), ("h", u32), ("format", u32), ("mips", vp), ("mipCount", u32)]
+
+
 class PtSurface(C.Structure):
     _fields_ = [("isLight", C.c_int), ("albedo", C.c_float * 3), ("matType", C.c_int),
                 ("roughness", C.c_float), ("metallic", C.c_float), ("specular", C.c_float),
                 ("iorFront", C.c_float), ("iorBack", C.c_float), ("lightBase", u32),
                 ("primKeyBase", u32), ("triangles", vp), ("m", C.c_float * 12),
                 ("inv", C.c_float * 12), ("texels", vp), ("texW", u32), ("texH", u32),
-                ("texFormat", u32), ("uvs", vp), ("mips", vp), ("mipCount", u32)]
+                ("texFormat", u32), ("uvs", vp), ("mips", vp), ("mipCount", u32), ("param", PtTex * 3)]
 
 
 class PtLightTri(C.Structure):
@@ -586,6 +590,29 @@ class PtScene:
                     chain, count = mips[key]
                     sf.mips = chain.ctypes.data
                     sf.mipCount = count
+            params = [s.get(k + "_texture") for k in ("roughness", "metallic", "specular")]
+            if any(t is not None for t in params):
+                uv = np.ascontiguousarray(s["uv"], np.float32).reshape(-1, 2)
+                uvp = np.ascontiguousarray(uv[idx].reshape(-1, 6), np.float32)
+                self._keep.append(uvp)
+                sf.uvs = uvp.ctypes.data
+                for j, t in enumerate(params):
+                    if t is None:
+                        continue
+                    t = np.ascontiguousarray(t)
+                    if t.dtype not in (np.uint8, np.float32) or t.ndim != 3 or t.shape[2] != 4:
+                        raise ValueError("texture must be (h, w, 4) uint8 or float32")
+                    self._keep.append(t)
+                    pt_ = sf.param[j]
+                    pt_.texels = t.ctypes.data
+                    pt_.h, pt_.w = t.shape[0], t.shape[1]
+                    pt_.format = 0 if t.dtype == np.uint8 else 1
+                    pt_.mipCount = 1
+                    if s.get("mip_radius"):
+                        chain, count = gen_mips(t, float(s["mip_radius"]))
+                        self._keep.append(chain)
+                        pt_.mips = chain.ctypes.data
+                        pt_.mipCount = count
             if s["kind"] == "light":
                 rad = (C.c_float * 3)(*[float(x) for x in s["radiance"]])
                 m = np.ascontiguousarray(s["m34"], np.float32).reshape(12)

@@ -1203,6 +1203,39 @@ static void albedo_lod(const orc_pt_surface* sf, const float* tri9, const float 
     tex_read_grad(sf, uv, grad[0], grad[1], rgb);
 }
 
+/* Unreal's textured roughness / metallic / specular at a hit (UnrealMaterial's
+ * constructor reads each at the surface's uv and gradients,
+ * MaterialsDefault.hpp:521-533): the first channel, read like the albedo,
+ * replaces the constant in a copy of the surface; other surfaces come back
+ * as they are. */
+static const orc_pt_surface* unreal_params(const orc_pt_surface* sf, uint32_t localPrim, const orc_meta_hit* mh,
+                                           const float* tri9, const float pos[3], const float nrm[3],
+                                           const float dir[3], cone_t cone, orc_pt_surface* tmp)
+{
+    if(sf->matType != ORC_MAT_UNREAL || !sf->uvs ||
+       !(sf->param[0].texels || sf->param[1].texels || sf->param[2].texels))
+        return sf;
+    *tmp = *sf;
+    const float* q = &sf->uvs[6 * localPrim];
+    const float a = mh->bary[0], b = mh->bary[1], c = 1.0f - a - b;
+    float uv[2];
+    for(int k = 0; k < 2; k++) uv[k] = q[k] * a + q[2 + k] * b + q[4 + k] * c;
+    float* dst[3] = { &tmp->roughness, &tmp->metallic, &tmp->specular };
+    for(int k = 0; k < 3; k++)
+    {
+        const orc_pt_tex* t = &sf->param[k];
+        if(!t->texels) continue;
+        orc_pt_surface ts = *sf;
+        ts.texels = t->texels; ts.texW = t->w; ts.texH = t->h; ts.texFormat = t->format;
+        ts.mips = t->mips; ts.mipCount = t->mipCount ? t->mipCount : 1u;
+        float v[4] = { 0, 0, 0, 0 };
+        if(ts.mipCount > 1u) albedo_lod(&ts, tri9, uv, q, pos, nrm, dir, cone, v);
+        else orc_tex_read(ts.texels, ts.texW, ts.texH, ts.texFormat, uv, v);
+        *dst[k] = v[0];
+    }
+    return tmp;
+}
+
 static inline float dot2f(const float a[2], const float b[2]) { return fmaf(a[1], b[1], fmaf(a[0], b[0], 0.0f)); }
 
 static void refract2d(const float v[2], const float n[2], float fromEta, float toEta, float out[2])
@@ -1446,6 +1479,8 @@ static void trace_sample_adj(pt_job* J, uint32_t x, uint32_t y, uint32_t sample,
             if(sf->mipCount > 1u) albedo_lod(sf, tri9, uv, q, pos, nrm, dir, cone_advance(cone, t), alb);
             else orc_tex_read(sf->texels, sf->texW, sf->texH, sf->texFormat, uv, alb);
         }
+        orc_pt_surface sfTex;
+        sf = unreal_params(sf, localPrim, &mh, tri9, pos, nrm, dir, cone_advance(cone, t), &sfTex);
         if(S) { float c3[3] = { alb[0], alb[1], alb[2] }; orc_spec_convert_albedo(S, c3, waves, alb); }
         if(adj && J->adjTexels && sf->texels == J->adjTexels && sf->matType == ORC_MAT_LAMBERT)
         {
@@ -2203,6 +2238,8 @@ static void g_surface_work(const orc_scene* scene, const orc_pt_params* P, const
     float alb[4];
     const cone_t cone = cone_advance(q->cone, q->tmax);
     g_albedo(sf, localPrim, &q->mh, S, q->waves, tri9, pos, nrm, q->dir, cone, alb);
+    orc_pt_surface sfTex;
+    sf = unreal_params(sf, localPrim, &q->mh, tri9, pos, nrm, q->dir, cone, &sfTex);
     const float specv = specularity(sf, alb, nc);
     const int isSpec = specv >= SPECULAR_THRESHOLD;
     float woW[3] = { wo[0], wo[1], wo[2] };

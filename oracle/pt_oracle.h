@@ -43,6 +43,15 @@ typedef struct
 #define ORC_MAT_REFRACT 2
 #define ORC_MAT_UNREAL  3
 
+/* a texture: RGBA, format 0 = UNORM8, 1 = f32, with its mip levels 1.. */
+typedef struct
+{
+    const void*  texels;
+    uint32_t     w, h, format;
+    const void*  mips;
+    uint32_t     mipCount;
+} orc_pt_tex;
+
 typedef struct
 {
     int          isLight;
@@ -64,6 +73,9 @@ typedef struct
     /* the texture's mip levels 1.. (orc_gen_mips), or NULL / 1 for level 0 only */
     const void*  mips;
     uint32_t     mipCount;
+    /* Unreal's roughness, metallic and specular textures (first channel; texels
+     * NULL keeps the constant), read like the albedo texture */
+    orc_pt_tex   param[3];
 } orc_pt_surface;
 
 /* KCGenerateMipmaps (Source/Tracer/TextureFilter.cu:62-192, 1006-1100) with a

@@ -128,6 +128,16 @@ def test_guided_mipmapped_textures_match_oracle():
     pt.close()
 
 
+def test_guided_unreal_parameter_textures_match_oracle():
+    pt = PathTracer(0)
+    surf = load_box_scene(pt, scenes.mipmapped(scenes.box_scene_unreal_textured(0, size=64)))
+    S = oracle.PtScene(surf)
+    g, o, gs, os_ = _render_both(pt, S, 2, seed=7)
+    _check_images(g, o)
+    _check_grids(gs, os_)
+    pt.close()
+
+
 def _spectral_pair(surf, env=None):
     import os
     from mray_gb300 import spectral

@@ -297,6 +297,21 @@ def test_given_mip_levels_per_pixel(radius):
     pt.close()
 
 
+@pytest.mark.parametrize("mips,mode", [(False, 2), (True, 2), (False, 0)])
+def test_unreal_parameter_textures_per_pixel(mips, mode):
+    """Unreal surfaces with textured roughness, metallic and specular (and
+    albedo), read at level 0 or at the ray cone's level of their chains."""
+    surf = scenes.box_scene_unreal_textured(0, size=64)
+    if mips:
+        scenes.mipmapped(surf)
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    g, o, frac = _compare(pt, oracle.PtScene(surf), mode, spp=8)
+    print("unreal textures mips=%d mode %d: close %.4f relMSE %.3g" % (mips, mode, frac, relmse(g, o)))
+    assert frac >= 0.97 and relmse(g, o) <= 1e-3
+    pt.close()
+
+
 def test_generate_mips_errors_and_drop():
     from mray_gb300 import _native as N
     surf = scenes.mipmapped(scenes.box_scene_textured(0, size=64))

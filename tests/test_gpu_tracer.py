@@ -72,7 +72,16 @@ def push_surfaces(t, surfaces, camera):
                     t.push_mat_attribute(g, r, 0, s["albedo"], [None])
             if kind == "unreal":
                 for k, name in enumerate(("roughness", "specular", "metallic")):
-                    t.push_mat_attribute(g, r, 2 + k, [s.get(name, 0.5 if name == "specular" else 0.0)], [None])
+                    pt_tex = s.get(name + "_texture")
+                    if pt_tex is not None:
+                        key = id(pt_tex)
+                        if key not in tex:
+                            tex[key] = (t.create_texture_2d(pt_tex.shape[1], pt_tex.shape[0], 1,
+                                                            "rgba8_unorm" if pt_tex.dtype == np.uint8
+                                                            else "rgba_float"), pt_tex, {})
+                        t.push_mat_attribute(g, r, 2 + k, None, [tex[key][0]])
+                    else:
+                        t.push_mat_attribute(g, r, 2 + k, [s.get(name, 0.5 if name == "specular" else 0.0)], [None])
             if kind == "refract":
                 front, back = s.get("ior", (1.0, 1.5))
                 t.push_mat_attribute(g, r, 0, [back, 0, 0])
@@ -177,6 +186,22 @@ def test_tracer_texture_mips_match_direct_path(gen_mips):
     pt = PathTracer(0)
     load_box_scene(pt, surf)
     want = direct_render(pt, cam, 64, 48, 8, 4, seed=23)
+    pt.close()
+    assert np.array_equal(film, want)
+
+
+def test_tracer_unreal_parameter_textures_match_direct_path():
+    """Textured roughness / specular / metallic pushed through TracerI (with
+    genMips) render as the direct path tracer's Unreal parameter textures."""
+    surf = scenes.mipmapped(_lights_unculled(scenes.box_scene_unreal_textured(0, size=64)), 2.0)
+    cam = scenes.box_camera()
+    with Tracer(seed=29, gen_mips=True) as t:
+        cs = push_surfaces(t, surf, cam)
+        t.commit_surfaces()
+        film, _ = tracer_render(t, cs, 64, 48, 8, 4)
+    pt = PathTracer(0)
+    load_box_scene(pt, surf)
+    want = direct_render(pt, cam, 64, 48, 8, 4, seed=29)
     pt.close()
     assert np.array_equal(film, want)
 

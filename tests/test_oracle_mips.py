@@ -156,3 +156,38 @@ def test_given_levels_are_kept_and_filtered_from():
         oracle.gen_mips(tex, 0.0, {2: lv2})                    # level 1 missing, no filter
     with pytest.raises(ValueError):
         oracle.gen_mips(tex, 2.0, {5: lv2})                    # past the 1 x 1 level
+
+
+def test_unreal_parameter_textures_change_the_image():
+    """Unreal's textured roughness / metallic / specular replace the
+    constants at each hit: the image differs from the constant-parameter
+    one, and textures holding constant values reproduce those constants'
+    image."""
+    cam = scenes.box_camera()
+    surf = scenes.box_scene_unreal_textured(0, size=32)
+    flat = [dict(s) for s in surf]
+    for s in flat:
+        for k in ("roughness_texture", "metallic_texture", "specular_texture"):
+            s.pop(k, None)
+    const = [dict(s) for s in flat]
+    for s in const:
+        if s.get("material") == "unreal":
+            for k, v in (("roughness", 0.2), ("metallic", 0.6), ("specular", 0.4)):
+                s[k + "_texture"] = np.full((8, 8, 4), v, np.float32)
+                s[k] = v
+    imgs = []
+    for sc in (surf, flat, const):
+        S = oracle.PtScene(sc)
+        imgs.append(S.render(S.params(24, 24, 4, cam, seed=5)))
+    a, b, c = (im[..., :3] / im[..., 3:] for im in imgs)
+    assert np.isfinite(a).all() and not np.allclose(a, b)
+    ref = [dict(s) for s in const]
+    for s in ref:
+        for k in ("roughness_texture", "metallic_texture", "specular_texture"):
+            s.pop(k, None)
+    S2 = oracle.PtScene(ref)
+    d = S2.render(S2.params(24, 24, 4, cam, seed=5))
+    # a bilinear read of a constant texture is the constant to an ulp, which
+    # can flip a rare sampling decision: nearly every pixel agrees
+    close = (np.abs(imgs[2] - d) <= 1e-4 * (1.0 + np.abs(d))).all(axis=-1).mean()
+    assert close >= 0.97, close
