@@ -179,6 +179,8 @@ mrg_status mrg_tracer_push_cam_attribute(mrg_tracer* t, uint32_t group_id, uint3
 #define MRG_PIX_RGBA8_UNORM 0u
 #define MRG_PIX_RGB_FLOAT   1u
 #define MRG_PIX_RGBA_FLOAT  2u
+#define MRG_PIX_R8_UNORM    3u   /* single channel: read as (r, r, r, 1) */
+#define MRG_PIX_R_FLOAT     4u
 /* CreateTexture2D: colour space, gamma and read mode are not applied
  * (texels are taken as linear values of the renderer's colour space);
  * filtering is bilinear with wrap addressing on mip 0, the data of further

@@ -111,7 +111,7 @@ TRACER_EXPORTED = [
 MRG_KIND_PRIM, MRG_KIND_MATERIAL, MRG_KIND_TRANSFORM, MRG_KIND_CAMERA = 0, 1, 2, 3
 MRG_KIND_MEDIUM, MRG_KIND_LIGHT, MRG_KIND_RENDERER = 4, 5, 6
 MRG_TRACER_SAMPLER_INDEPENDENT, MRG_TRACER_SAMPLER_ZSOBOL = 0, 1
-MRG_PIX_RGBA8_UNORM, MRG_PIX_RGB_FLOAT, MRG_PIX_RGBA_FLOAT = 0, 1, 2
+MRG_PIX_RGBA8_UNORM, MRG_PIX_RGB_FLOAT, MRG_PIX_RGBA_FLOAT, MRG_PIX_R8_UNORM, MRG_PIX_R_FLOAT = 0, 1, 2, 3, 4
 MRG_ATTR_CONSTANT_ONLY, MRG_ATTR_TEXTURE_OR_CONSTANT, MRG_ATTR_TEXTURE_ONLY = 0, 1, 2
 MRG_DT_NAMES = ["FLOAT", "VECTOR_2", "VECTOR_3", "VECTOR_4", "QUATERNION", "MATRIX_4x4", "UINT32", "VECTOR_2UI",
                 "VECTOR_3UI", "BOOL", "STRING"]

@@ -469,21 +469,40 @@ mrg_status transform_of(mrg_tracer* t, uint32_t id, float m34[12])
     return MRG_OK;
 }
 
-// n texels of a pushed level in the path tracer's RGBA f32 form
+// n texels of a pushed level in RGBA f32 (single-channel types as r, r, r, 1)
 void level_rgba_f32(uint32_t pixel, const uint8_t* data, size_t n, std::vector<float>& out)
 {
     out.resize(4 * n);
-    if(pixel == MRG_PIX_RGBA_FLOAT) std::memcpy(out.data(), data, 16 * n);
-    else if(pixel == MRG_PIX_RGB_FLOAT)
+    const float* f = reinterpret_cast<const float*>(data);
+    for(size_t i = 0; i < n; i++)
     {
-        const float* f = reinterpret_cast<const float*>(data);
-        for(size_t i = 0; i < n; i++)
+        float* o = &out[4 * i];
+        switch(pixel)
         {
-            out[4 * i] = f[3 * i]; out[4 * i + 1] = f[3 * i + 1]; out[4 * i + 2] = f[3 * i + 2]; out[4 * i + 3] = 1.0f;
+            case MRG_PIX_RGBA_FLOAT: o[0] = f[4 * i]; o[1] = f[4 * i + 1]; o[2] = f[4 * i + 2]; o[3] = f[4 * i + 3]; break;
+            case MRG_PIX_RGB_FLOAT:  o[0] = f[3 * i]; o[1] = f[3 * i + 1]; o[2] = f[3 * i + 2]; o[3] = 1.0f; break;
+            case MRG_PIX_R_FLOAT:    o[0] = o[1] = o[2] = f[i]; o[3] = 1.0f; break;
+            case MRG_PIX_R8_UNORM:   o[0] = o[1] = o[2] = (float)data[i] / 255.0f; o[3] = 1.0f; break;
+            default: for(int k = 0; k < 4; k++) o[k] = (float)data[4 * i + k] / 255.0f; break;
         }
     }
-    else
-        for(size_t i = 0; i < 4 * n; i++) out[i] = (float)data[i] / 255.0f;
+}
+
+// A pushed level in the path tracer's own texture form: RGBA8 stays as it
+// is, R8 becomes RGBA8 (r, r, r, 255) so that it keeps the UNORM read, the
+// float types become RGBA f32.
+const void* level_for_pt(uint32_t pixel, const std::vector<uint8_t>& in, size_t n, std::vector<uint8_t>& b8,
+                         std::vector<float>& f32)
+{
+    if(pixel == MRG_PIX_RGBA8_UNORM || pixel == MRG_PIX_RGBA_FLOAT) return in.data();
+    if(pixel == MRG_PIX_R8_UNORM)
+    {
+        b8.resize(4 * n);
+        for(size_t i = 0; i < n; i++) { b8[4 * i] = b8[4 * i + 1] = b8[4 * i + 2] = in[i]; b8[4 * i + 3] = 255; }
+        return b8.data();
+    }
+    level_rgba_f32(pixel, in.data(), n, f32);
+    return f32.data();
 }
 
 mrg_status texture_rgba_f32(mrg_tracer* t, uint32_t tid, std::vector<float>& out, uint32_t& w, uint32_t& h)
@@ -505,16 +524,11 @@ mrg_status pt_texture(mrg_tracer* t, uint32_t tid, uint32_t& ptId)
     if(!x.mip0Set) return err("texture " + std::to_string(tid) + " has no data");
     mrg_status s;
     uint32_t id = 0;
-    if(x.pixel == MRG_PIX_RGB_FLOAT)
-    {
-        std::vector<float> f;
-        uint32_t w, h;
-        if((s = texture_rgba_f32(t, tid, f, w, h)) != MRG_OK) return s;
-        s = mrg_pt_add_texture(t->ctx, w, h, MRG_TEX_RGBA32F, f.data(), 0, &id);
-    }
-    else
-        s = mrg_pt_add_texture(t->ctx, x.w, x.h, x.pixel == MRG_PIX_RGBA8_UNORM ? MRG_TEX_RGBA8 : MRG_TEX_RGBA32F,
-                               x.mip0.data(), 0, &id);
+    const bool unorm = x.pixel == MRG_PIX_RGBA8_UNORM || x.pixel == MRG_PIX_R8_UNORM;
+    std::vector<uint8_t> b8;
+    std::vector<float> f32;
+    s = mrg_pt_add_texture(t->ctx, x.w, x.h, unorm ? MRG_TEX_RGBA8 : MRG_TEX_RGBA32F,
+                           level_for_pt(x.pixel, x.mip0, (size_t)x.w * x.h, b8, f32), 0, &id);
     if(s != MRG_OK) return s;
     // mips: TracerParameters::genMips fills every level the texture does not
     // have with mipGenFilter (TextureMemory.cpp:588-591, 826-830); pushed
@@ -528,14 +542,7 @@ mrg_status pt_texture(mrg_tracer* t, uint32_t tid, uint32_t& ptId)
     {
         if(x.upper[m].empty()) continue;
         const size_t n = (size_t)std::max(x.w >> m, 1u) * std::max(x.h >> m, 1u);
-        if(x.pixel == MRG_PIX_RGB_FLOAT)
-        {
-            std::vector<float> f;
-            level_rgba_f32(x.pixel, x.upper[m].data(), n, f);
-            s = mrg_pt_set_texture_mip(t->ctx, id, m, f.data());
-        }
-        else
-            s = mrg_pt_set_texture_mip(t->ctx, id, m, x.upper[m].data());
+        s = mrg_pt_set_texture_mip(t->ctx, id, m, level_for_pt(x.pixel, x.upper[m], n, b8, f32));
         if(s != MRG_OK) return s;
     }
     x.ptId = ptId = id;
@@ -1299,7 +1306,7 @@ mrg_status mrg_tracer_create_texture2d(mrg_tracer* t, uint32_t width, uint32_t h
     if(!texture_id) return err("null output id");
     if(t->texturesCommitted) return err("textures are committed; no more textures");
     if(width == 0 || height == 0 || mip_count == 0) return err("empty texture");
-    if(pixel_type > MRG_PIX_RGBA_FLOAT) return err("unsupported pixel type " + std::to_string(pixel_type));
+    if(pixel_type > MRG_PIX_R_FLOAT) return err("unsupported pixel type " + std::to_string(pixel_type));
     Texture x;
     x.w = width; x.h = height; x.mips = mip_count; x.pixel = pixel_type;
     t->textures.push_back(std::move(x));
@@ -1324,7 +1331,7 @@ mrg_status mrg_tracer_push_texture_data(mrg_tracer* t, uint32_t texture_id, uint
     Texture& x = t->textures[texture_id - 1];
     if(!x.committed) return err("PushTextureData before CommitTextures");
     if(mip_level >= x.mips) return err("mip level out of range");
-    static const uint32_t pb[3] = { 4, 12, 16 };
+    static const uint32_t pb[5] = { 4, 12, 16, 1, 4 };
     const size_t w = std::max(1u, x.w >> mip_level), h = std::max(1u, x.h >> mip_level);
     if(!data || bytes != w * h * pb[x.pixel])
         return err("texture " + std::to_string(texture_id) + " mip " + std::to_string(mip_level) + " wants " +

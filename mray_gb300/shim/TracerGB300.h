@@ -325,8 +325,10 @@ class TracerGB300 final : public TracerI
             case MRayPixelEnum::MR_RGBA8_UNORM: pix = MRG_PIX_RGBA8_UNORM; break;
             case MRayPixelEnum::MR_RGB_FLOAT:   pix = MRG_PIX_RGB_FLOAT; break;
             case MRayPixelEnum::MR_RGBA_FLOAT:  pix = MRG_PIX_RGBA_FLOAT; break;
+            case MRayPixelEnum::MR_R8_UNORM:    pix = MRG_PIX_R8_UNORM; break;
+            case MRayPixelEnum::MR_R_FLOAT:     pix = MRG_PIX_R_FLOAT; break;
             default: throw MRayError("mray_gb300: texture pixel type is not supported "
-                                     "(RGBA8 UNORM, RGB / RGBA float)");
+                                     "(RGBA8 / R8 UNORM, R / RGB / RGBA float)");
         }
         uint32_t id;
         Check(mrg_tracer_create_texture2d(t, size[0], size[1], mips, pix, &id));

@@ -15,7 +15,8 @@ from . import _native as N
 KIND = {"prim": N.MRG_KIND_PRIM, "material": N.MRG_KIND_MATERIAL, "transform": N.MRG_KIND_TRANSFORM,
         "camera": N.MRG_KIND_CAMERA, "medium": N.MRG_KIND_MEDIUM, "light": N.MRG_KIND_LIGHT,
         "renderer": N.MRG_KIND_RENDERER}
-PIXEL = {"rgba8_unorm": N.MRG_PIX_RGBA8_UNORM, "rgb_float": N.MRG_PIX_RGB_FLOAT, "rgba_float": N.MRG_PIX_RGBA_FLOAT}
+PIXEL = {"rgba8_unorm": N.MRG_PIX_RGBA8_UNORM, "rgb_float": N.MRG_PIX_RGB_FLOAT, "rgba_float": N.MRG_PIX_RGBA_FLOAT,
+         "r8_unorm": N.MRG_PIX_R8_UNORM, "r_float": N.MRG_PIX_R_FLOAT}
 SAMPLER = {"independent": N.MRG_TRACER_SAMPLER_INDEPENDENT, "zsobol": N.MRG_TRACER_SAMPLER_ZSOBOL}
 
 # (P)Triangle attribute indices (PrimitiveDefaultTriangle.cu:169-184)

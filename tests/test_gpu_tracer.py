@@ -76,9 +76,10 @@ def push_surfaces(t, surfaces, camera):
                     if pt_tex is not None:
                         key = id(pt_tex)
                         if key not in tex:
+                            kind4 = "rgba8_unorm" if pt_tex.dtype == np.uint8 else "rgba_float"
+                            kind1 = "r8_unorm" if pt_tex.dtype == np.uint8 else "r_float"
                             tex[key] = (t.create_texture_2d(pt_tex.shape[1], pt_tex.shape[0], 1,
-                                                            "rgba8_unorm" if pt_tex.dtype == np.uint8
-                                                            else "rgba_float"), pt_tex, {})
+                                                            kind1 if pt_tex.ndim == 2 else kind4), pt_tex, {})
                         t.push_mat_attribute(g, r, 2 + k, None, [tex[key][0]])
                     else:
                         t.push_mat_attribute(g, r, 2 + k, [s.get(name, 0.5 if name == "specular" else 0.0)], [None])
@@ -204,6 +205,33 @@ def test_tracer_unreal_parameter_textures_match_direct_path():
     want = direct_render(pt, cam, 64, 48, 8, 4, seed=29)
     pt.close()
     assert np.array_equal(film, want)
+
+
+def test_tracer_single_channel_textures():
+    """R8 UNORM and R float textures (MRay's usual roughness / metallic maps)
+    read as (r, r, r, 1): the film equals the direct path's with the RGBA
+    expansions."""
+    surf = _lights_unculled(scenes.box_scene_unreal_textured(0, size=32))
+    r8 = np.ascontiguousarray(surf[0]["roughness_texture"][..., 0])
+    rf = np.ascontiguousarray(surf[0]["metallic_texture"][..., 0].astype(np.float32) / 255.0)
+    r8x = np.repeat(r8[..., None], 4, axis=2)
+    r8x[..., 3] = 255
+    rfx = np.concatenate([np.repeat(rf[..., None], 3, axis=2), np.ones(rf.shape + (1,), np.float32)], axis=2)
+    single, want = [dict(s) for s in surf], [dict(s) for s in surf]
+    for s1, s2 in zip(single, want):
+        if s1.get("material") == "unreal":
+            s1["roughness_texture"], s1["metallic_texture"] = r8, rf      # 2D: single channel
+            s2["roughness_texture"], s2["metallic_texture"] = r8x, rfx
+    cam = scenes.box_camera()
+    with Tracer(seed=31) as t:
+        cs = push_surfaces(t, single, cam)
+        t.commit_surfaces()
+        film, _ = tracer_render(t, cs, 48, 32, 4, 4)
+    pt = PathTracer(0)
+    load_box_scene(pt, want)
+    ref = direct_render(pt, cam, 48, 32, 4, 4, seed=31)
+    pt.close()
+    assert np.array_equal(film, ref)
 
 
 def test_scene_json_through_tracer_matches_reader():

@@ -147,12 +147,22 @@ def test_order_rules(tr):
         tr.push_mat_attribute(rg, (ids[0], ids[0]), 0, np.ones(3))
 
     t = tr.create_texture_2d(2, 2, 1, "rgba8_unorm")
+    t8 = tr.create_texture_2d(4, 2, 2, "r8_unorm")
+    tf = tr.create_texture_2d(4, 2, 1, "r_float")
     with pytest.raises(N.MRGError, match="before CommitTextures"):
         tr.push_texture_data(t, 0, np.zeros((2, 2, 4), np.uint8))
     tr.commit_textures()
     with pytest.raises(N.MRGError, match="wants 16 bytes"):
         tr.push_texture_data(t, 0, np.zeros((2, 2, 2), np.uint8))
     tr.push_texture_data(t, 0, np.zeros((2, 2, 4), np.uint8))
+    # single-channel types: one byte / one float per texel, per level
+    with pytest.raises(N.MRGError, match="wants 8 bytes"):
+        tr.push_texture_data(t8, 0, np.zeros((2, 4, 4), np.uint8))
+    tr.push_texture_data(t8, 0, np.zeros((2, 4), np.uint8))
+    tr.push_texture_data(t8, 1, np.zeros((1, 2), np.uint8))
+    with pytest.raises(N.MRGError, match="wants 32 bytes"):
+        tr.push_texture_data(tf, 0, np.zeros((2, 4), np.uint8))
+    tr.push_texture_data(tf, 0, np.zeros((2, 4), np.float32))
     with pytest.raises(N.MRGError, match="no more textures"):
         tr.create_texture_2d(2, 2)
 
