@@ -705,18 +705,21 @@ def c4_equal_time(args, dev, spp_per_frame=8):
                           "cold start counts the training frames, steady state does not")
     cache.close()
     out.update(guided_equal_time(pt, P, relmse, timed, t_plain, plain_rel))
+    # the same with zero-weight lobes falling back to the material sample
+    fixed = guided_equal_time(pt, P, relmse, timed, t_plain, plain_rel, fix_zero_weight=True)
+    out.update({k.replace("guided_", "guided_fixed_"): v for k, v in fixed.items() if "relmse" in k or "_ms" in k})
     pt.close()
     return out
 
 
-def guided_equal_time(pt, P, relmse, timed, t_plain, plain_rel, spp=2):
+def guided_equal_time(pt, P, relmse, timed, t_plain, plain_rel, spp=2, fix_zero_weight=False):
     """Guided path tracing (GuidedPTRenderer, default options) on the same
     scene and reference: from an empty grid, frames of `spp` samples per
     pixel accumulated for the plain 16-spp render's time (learning included),
     then, the grid trained, one more 16-spp guided frame against the plain
     16-spp render."""
     import torch
-    pt.guide_create()
+    pt.guide_create(fix_zero_weight=fix_zero_weight)
     pt.render_guided(P(spp, 900, spp_pass=spp))         # allocations, first launches
     pt.guide_clear()
     img, spent, frames = None, 0.0, 0

@@ -509,7 +509,12 @@ typedef struct mrg_guide_params
     uint32_t maxLevelOffset;    /* cacheMaxLvlOffset (3) */
     float    coneAperture;      /* cacheConeAperture, degrees (0.6) */
     float    lobeProbability;   /* lobeProbablity (0.75) */
-    uint32_t reserved[2];
+    uint32_t fixZeroWeight;     /* 0 (MRay): a vertex whose chosen lobe has weight 0 (or
+                                   that has no lobe) takes GaussLobeMixtureT::Sample's +Y
+                                   direction with pdf 0 when it picks the mixture; 1: such
+                                   a vertex samples the material only (mixture
+                                   probability 0), which removes that bias */
+    uint32_t reserved;
 } mrg_guide_params;
 mrg_status mrg_guide_defaults(mrg_guide_params* out);
 /* Allocates the context's grid over the scene box of the last mrg_build

@@ -145,7 +145,7 @@ class MrgTracerRenderInfo(C.Structure):
 class MrgGuideParams(C.Structure):
     _fields_ = [("entryLimit", C.c_uint32), ("posBits", C.c_uint32), ("normalBits", C.c_uint32),
                 ("maxLevelOffset", C.c_uint32), ("coneAperture", C.c_float), ("lobeProbability", C.c_float),
-                ("reserved", C.c_uint32 * 2)]
+                ("fixZeroWeight", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class MrgTracerRenderOutput(C.Structure):

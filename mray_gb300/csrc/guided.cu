@@ -387,6 +387,7 @@ k_shade_guided(PtLaunch L, PtPaths P, GuideGrid G, GuidePaths Q, PtSceneTables T
                 {
                     const float t = fminf(fmaxf(sub(1.0f, specv), 0.0f), 1.0f);
                     mw0 = add(mul(0.0f, sub(1.0f, t)), mul(G.lobeProb, t));     // Math::Lerp(0, p, t)
+                    if(G.fixZeroWeight && (sIdx == guide::kInvalid || mx.f(kMxW, sIdx) == 0.0f)) mw0 = 0.0f;
                 }
                 const float mw1 = sub(1.0f, mw0);
                 Chan refl;

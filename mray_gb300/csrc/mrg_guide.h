@@ -50,6 +50,7 @@ struct GuideGrid
     uint32_t  maxEntryLimit;        // table size * 0.6
     float     tanConeHalfTimes2;
     float     lobeProb;             // lobeProbablity
+    uint32_t  fixZeroWeight;        // 1: no mixture sample where the chosen lobe has weight 0
     float4*   mcA;                  // MCState target xyz, cosine
     float*    mcW;                  // MCState weight
     uint32_t* mcN;                  // MCCount

@@ -1148,6 +1148,7 @@ void guide_view(mrg_ctx* c)
     G.maxEntryLimit = (uint32_t)((float)(G.tableMask + 1u) * 0.6f);
     G.rmin = make_float3(c->sceneBoxExact[0], c->sceneBoxExact[1], c->sceneBoxExact[2]);
     G.lobeProb = p.lobeProbability;
+    G.fixZeroWeight = p.fixZeroWeight ? 1u : 0u;
 }
 
 mrg_status guide_clear(mrg_ctx* c)

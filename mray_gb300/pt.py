@@ -217,7 +217,7 @@ class PathTracer:
 
     # ---- guided path tracing (GuidedPTRenderer) ----
     def guide_create(self, entry_limit=2000000, pos_bits=14, normal_bits=2, max_level_offset=3,
-                     cone_aperture=0.6, lobe_probability=0.75):
+                     cone_aperture=0.6, lobe_probability=0.75, fix_zero_weight=False):
         """Allocates the guiding hash grid over the built scene's box with
         GuidedPTRenderer's options (cacheEntryLimit, cachePosBits,
         cacheNormalBits, cacheMaxLvlOffset, cacheConeAperture in degrees,
@@ -226,6 +226,7 @@ class PathTracer:
         N.check(N.lib().mrg_guide_defaults(C.byref(g)))
         g.entryLimit, g.posBits, g.normalBits = entry_limit, pos_bits, normal_bits
         g.maxLevelOffset, g.coneAperture, g.lobeProbability = max_level_offset, cone_aperture, lobe_probability
+        g.fixZeroWeight = 1 if fix_zero_weight else 0
         N.check(N.lib().mrg_guide_create(self.acc._h, C.byref(g)))
 
     def guide_clear(self):

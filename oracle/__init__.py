@@ -94,7 +94,7 @@ def lib():
         L.orc_conc_octa_batch.argtypes = [vp, vp, vp, vp, u32]
         L.orc_guide_codes_batch.argtypes = [vp, vp, vp, vp, u32]
         L.orc_guide_table_batch.argtypes = [vp, u32, vp, u32, u32, vp, vp]
-        L.orc_guide_new.argtypes = [vp, u32, u32, u32, u32, C.c_float, C.c_float]
+        L.orc_guide_new.argtypes = [vp, u32, u32, u32, u32, C.c_float, C.c_float, C.c_int]
         L.orc_guide_new.restype = vp
         L.orc_guide_delete.argtypes = [vp]
         L.orc_guide_clear.argtypes = [vp]
@@ -693,11 +693,11 @@ class PtScene:
         return p
 
     def guide(self, entry_limit=2000000, pos_bits=14, normal_bits=2, max_level_offset=3, cone_aperture=0.6,
-              lobe_probability=0.75):
+              lobe_probability=0.75, fix_zero_weight=False):
         """A guided path tracer's state (hash grid, chains, irradiance) over
         this scene (GuidedPTRenderer options, as mray_gb300.pt.PathTracer.guide_create)."""
         return GuideState(self, entry_limit, pos_bits, normal_bits, max_level_offset, cone_aperture,
-                          lobe_probability)
+                          lobe_probability, fix_zero_weight)
 
     def render_guided(self, p, guide, samples_per_pass, image=None):
         """Guided samples (single-threaded wavefront) added to image."""
@@ -766,10 +766,11 @@ class GuideState:
     """orc_guide_state: the oracle's guiding grid, chains, irradiance
     averages and backup streams."""
 
-    def __init__(self, scene, entry_limit, pos_bits, normal_bits, max_level_offset, cone_aperture, lobe_probability):
+    def __init__(self, scene, entry_limit, pos_bits, normal_bits, max_level_offset, cone_aperture, lobe_probability,
+                 fix_zero_weight=False):
         self.L = lib()
         self._h = self.L.orc_guide_new(scene.S._h, entry_limit, pos_bits, normal_bits, max_level_offset,
-                                       cone_aperture, lobe_probability)
+                                       cone_aperture, lobe_probability, 1 if fix_zero_weight else 0)
         if not self._h:
             raise MemoryError("orc_guide_new")
 

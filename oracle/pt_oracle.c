@@ -2012,6 +2012,7 @@ struct orc_guide_state
     uint32_t* irrN;
     uint32_t* lock;
     float     lobeProb;
+    int       fixZeroWeight;   /* 1: no mixture sample where the chosen lobe has weight 0 */
     int       camSet;
     uint32_t* bk;           /* backup PCG32 state per path slot */
     uint32_t  bkSlots, bkSeed, bkW, bkH;
@@ -2026,7 +2027,7 @@ static uint32_t next_pow2_u32(uint32_t v)
 }
 
 orc_guide_state* orc_guide_new(const orc_scene* s, uint32_t entryLimit, uint32_t posBits, uint32_t normalBits,
-                               uint32_t maxLevelOffset, float coneDeg, float lobeProb)
+                               uint32_t maxLevelOffset, float coneDeg, float lobeProb, int fixZeroWeight)
 {
     orc_guide_state* G = (orc_guide_state*)calloc(1, sizeof(orc_guide_state));
     if(!G) return NULL;
@@ -2043,6 +2044,7 @@ orc_guide_state* orc_guide_new(const orc_scene* s, uint32_t entryLimit, uint32_t
     G->irrN = (uint32_t*)malloc(sizeof(uint32_t) * T);
     G->lock = (uint32_t*)malloc(sizeof(uint32_t) * T);
     G->lobeProb = lobeProb;
+    G->fixZeroWeight = fixZeroWeight;
     if(!G->g.codes || !G->mcA || !G->mcW || !G->mcN || !G->irr || !G->irrN || !G->lock)
     {
         orc_guide_delete(G);
@@ -2286,6 +2288,7 @@ static void g_surface_work(const orc_scene* scene, const orc_pt_params* P, const
         float t = 1.0f - specv;
         t = fminf(fmaxf(t, 0.0f), 1.0f);
         mw0 = 0.0f * (1.0f - t) + G->lobeProb * t;           /* Math::Lerp(0, p, t) */
+        if(G->fixZeroWeight && (!selected || selW == 0.0f)) mw0 = 0.0f;
     }
     const float mw1 = 1.0f - mw0;
     float refl[4] = { 0, 0, 0, 0 }, pdf0, pdf1, wdir[3], orgOut[3] = { pos[0], pos[1], pos[2] };

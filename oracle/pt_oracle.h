@@ -171,7 +171,7 @@ int orc_pt_adjoint(const orc_scene* s, const orc_pt_params* p, const orc_pt_surf
  * until orc_guide_clear. */
 typedef struct orc_guide_state orc_guide_state;
 orc_guide_state* orc_guide_new(const orc_scene* s, uint32_t entryLimit, uint32_t posBits, uint32_t normalBits,
-                               uint32_t maxLevelOffset, float coneDeg, float lobeProb);
+                               uint32_t maxLevelOffset, float coneDeg, float lobeProb, int fixZeroWeight);
 void     orc_guide_delete(orc_guide_state* G);
 void     orc_guide_clear(orc_guide_state* G);
 uint32_t orc_guide_table_size(const orc_guide_state* G);

@@ -138,6 +138,20 @@ def test_guided_unreal_parameter_textures_match_oracle():
     pt.close()
 
 
+def test_guided_fix_zero_weight_matches_oracle():
+    """The opt-in correction of MRay's zero-weight mixture sample: GPU and
+    oracle agree, and the images differ from the reproduced defect's."""
+    pt = PathTracer(0)
+    surf = load_box_scene(pt, 0)
+    S = oracle.PtScene(surf)
+    g, o, gs, os_ = _render_both(pt, S, 2, seed=5, fix_zero_weight=True)
+    _check_images(g, o)
+    _check_grids(gs, os_)
+    g0, _, _, _ = _render_both(pt, S, 2, seed=5)
+    assert not np.allclose(_img(g), _img(g0))
+    pt.close()
+
+
 def _spectral_pair(surf, env=None):
     import os
     from mray_gb300 import spectral

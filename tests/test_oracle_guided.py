@@ -79,3 +79,24 @@ def test_guided_oracle_learning_reduces_the_zero_weight_bias():
     e, l = np.abs(mean(early) - rm) / rm, np.abs(mean(late) - rm) / rm
     assert e.max() > l.max(), (e, l)
     assert np.all(l < 0.05), l
+
+
+def test_guided_oracle_fix_zero_weight_removes_the_young_grid_bias():
+    """With the opt-in correction a vertex whose chosen lobe has no weight
+    samples the material only, so even the first frames of an empty grid
+    are unbiased: their mean is closer to the plain tracer's than MRay's."""
+    S = oracle.PtScene(scenes.box_scene(0))
+    cam = scenes.box_camera()
+    ref = S.render(S.params(16, 16, 512, cam, max_depth=8, rr_start=2, seed=11))
+    mean = lambda im: (im[..., :3] / im[..., 3:]).mean(axis=(0, 1))
+    rm = mean(ref)
+    errs = []
+    for fix in (False, True):
+        G = S.guide(fix_zero_weight=fix)
+        img = None
+        for c in range(4):
+            p = S.params(16, 16, 16, cam, max_depth=8, rr_start=2, seed=3, sample_start=16 * c)
+            img = S.render_guided(p, G, 16, image=img)
+        errs.append(np.abs(mean(img) - rm) / rm)
+    assert errs[1].max() < errs[0].max(), errs
+    assert np.all(errs[1] < 0.05), errs[1]
